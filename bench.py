@@ -1,0 +1,371 @@
+"""Benchmark: 256^3 pressure-Poisson solves per second on one GB300.
+
+Workload (seeded synthetic inputs; the reference ships no decks): a 256^3 box
+[0,1]^3 tanh-stretched toward the centre (beta 1.5) with a stationary
+ghost-cell sphere (r = 0.15, 4x-subdivided icosphere, 5120 triangles); RHS =
+divergence of a Gaussian random velocity field with |k| <= 8, mean removed and
+made discretely compatible; one step = one solve_poisson from pPrime = 0 to
+relative residual 1e-8 (max-norm <= 1e-8 max|nlu0|).  The headline arm is
+the mixed-precision form (FP32 cycle inside FP64 refinement); the plain FP64
+form is timed on the same inputs and reported beside it.
+
+  value  : solves/s with pPrime/nlu0 resident in HBM (fsi_mg_solve_device),
+           device time from CUDA events on the solver's stream.
+  e2e    : solves/s through fsi_mg_solve with pinned HOST buffers, the H2D of
+           pPrime and nlu0 and the D2H of pPrime inside the timed region.
+  --impl reference : the reference MG algorithm (the C restatement in oracle/,
+           serial like the reference) on all host cores as independent
+           replicas, bounded sample per step.
+
+Multi-GPU: the path does not shard (replicas only); each rank runs its own
+replica and value is the sum over ranks.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+METRIC = "256³ Poisson solves/s @1e-8 resid, mixed vs FP64 GPU; HBM GB/s; adjoint/fwd"
+PEAKS = ROOT / "MEASURED_PEAKS.json"
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--n", type=int, default=256)
+    ap.add_argument("--tol", type=float, default=1e-8)
+    ap.add_argument("--seed", type=int, default=3)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true")
+    return ap.parse_args()
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+class ClockSampler:
+    """nvidia-smi clocks / throttle reasons sampled during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index=0):
+        self.index = index
+        self.lines = []
+        self.proc = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            threading.Thread(target=self._read, daemon=True).start()
+        except OSError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx = float(f[2])
+            except ValueError:
+                continue
+            for nm, v in zip(names, f[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": mx,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def build_problem(n, seed, tol, solver_cls):
+    from flow_structure_interaction_fem_ibm_gb300 import problem as P
+    pr = P.sphere(n, seed=seed, stretch=1.5)
+    # discrete compatibility shift from two stalled FP64 GPU solves
+    def stagnated(f):
+        saved = (pr.params.iterMax_Poisson, pr.params.restol_Poisson, pr.params.precision_mode)
+        pr.params.iterMax_Poisson, pr.params.restol_Poisson, pr.params.precision_mode = 30, 0.0, 0
+        s = solver_cls(pr.params, pr.x, pr.y, pr.z).set_boundary(pr.geom)
+        p = np.zeros(pr.shape, order="F")
+        s.solve_poisson(p, f)
+        s.close()
+        pr.params.iterMax_Poisson, pr.params.restol_Poisson, pr.params.precision_mode = saved
+        return p
+    shift = P.make_compatible(pr, stagnated)
+    pr.params.restol_Poisson = tol * float(np.abs(pr.nlu0).max())
+    pr.params.iterMax_Poisson = 500
+    return pr, shift
+
+
+def oracle_iteration_time(n, seed, reps=1):
+    """Seconds per outer iteration of the oracle (serial reference MG) at n^3."""
+    from flow_structure_interaction_fem_ibm_gb300 import problem as P
+    from oracle.oracle import Oracle
+    pr = P.sphere(n, seed=seed, stretch=1.5)
+    o = Oracle(pr)
+    p = np.zeros(pr.shape, order="F")
+    o.subtract_average(p)
+    t0 = time.perf_counter()
+    for _ in range(reps):
+        o.mg_solver(p, pr.nlu0)
+        o.correct_pressure(p)
+        o.calc_residual(p, pr.nlu0)
+    return (time.perf_counter() - t0) / reps
+
+
+def oracle_iterations(n, seed, tol):
+    """Outer iterations the oracle needs on the same recipe at n^3 (MG iteration
+    counts are nearly size-independent)."""
+    from flow_structure_interaction_fem_ibm_gb300 import problem as P
+    from oracle.oracle import Oracle
+    pr = P.sphere(n, seed=seed, stretch=1.5)
+
+    def stagnated(f):
+        q = P.Problem(pr.params, pr.x, pr.y, pr.z, pr.geom, f, pr.name)
+        return Oracle(q, iterMax_Poisson=30, restol_Poisson=0.0).solve()["p"]
+
+    P.make_compatible(pr, stagnated)
+    pr.params.restol_Poisson = tol * float(np.abs(pr.nlu0).max())
+    pr.params.iterMax_Poisson = 500
+    return Oracle(pr).solve()["iters"]
+
+
+def _replica(args):
+    n, seed = args
+    return oracle_iteration_time(n, seed)
+
+
+def cpu_reference(n_full, seed, tol, sample_n=128, cores=1):
+    """Reference-algorithm solves/s at n_full^3 from a bounded sample: one outer
+    iteration at sample_n^3 per core (independent replicas), scaled by the cell
+    count ratio and the oracle's own iteration count."""
+    iters = oracle_iterations(48, seed, tol)
+    scale = (n_full / sample_n) ** 3
+    if cores <= 1:
+        t = oracle_iteration_time(sample_n, seed)
+        per_core = [t]
+    else:
+        import multiprocessing as mp
+        ctx = mp.get_context("spawn")
+        with ctx.Pool(cores) as pool:
+            per_core = pool.map(_replica, [(sample_n, seed)] * cores)
+    t_iter = float(np.mean(per_core)) * scale
+    value = len(per_core) / (t_iter * iters)
+    return value, iters, t_iter, per_core
+
+
+def run_reference(args, rank, world):
+    if rank != 0:
+        print(json.dumps({"impl": "reference", "rank": rank, "skipped": True}), file=sys.stderr)
+        return
+    cores = os.cpu_count() or 1
+    t0 = time.perf_counter()
+    vals = []
+    for s in range(args.warmup + args.steps):
+        v, iters, t_iter, per = cpu_reference(args.n, args.seed, args.tol, sample_n=64, cores=cores)
+        if s >= args.warmup:
+            vals.append(v)
+    value = float(np.median(vals))
+    out = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": "solves/s", "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 / value * cores,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": f"sphere_{args.n}^3_tanh1.5_r0.15_tol{args.tol:g}", "grid": args.n,
+                   "tol": args.tol, "parallelism": f"{cores} independent serial replicas"},
+        "cpu_baseline": {"value": value, "unit": "solves/s", "cores": cores, "kind": "port",
+                         "sample": (f"one outer iteration (MG_Solver + GCM_correct_pressure + calc_residual) at 64^3 "
+                                    f"per core, scaled by cell count to {args.n}^3, times the oracle's own "
+                                    f"iteration count at 48^3 ({iters})")},
+        "e2e": {"value": value, "unit": "solves/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "wall_s": time.perf_counter() - t0,
+    }
+    print(json.dumps(out))
+
+
+def main():
+    args = parse()
+    rank, world, local = dist_env()
+    if args.impl == "reference":
+        return run_reference(args, rank, world)
+    import torch
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    from flow_structure_interaction_fem_ibm_gb300.build import build_all
+    if rank == 0:
+        build_all()
+    if world > 1:
+        torch.distributed.barrier()
+    from flow_structure_interaction_fem_ibm_gb300.poisson import PoissonSolver
+
+    t_setup = time.perf_counter()
+    pr, shift = build_problem(args.n, args.seed, args.tol, PoissonSolver)
+    import copy
+    p_mixed = copy.deepcopy(pr.params); p_mixed.precision_mode = 1
+    p_fp64 = copy.deepcopy(pr.params); p_fp64.precision_mode = 0
+    s_mixed = PoissonSolver(p_mixed, pr.x, pr.y, pr.z).set_boundary(pr.geom)
+    s_fp64 = PoissonSolver(p_fp64, pr.x, pr.y, pr.z).set_boundary(pr.geom)
+    sh = pr.shape
+    b = torch.from_numpy(np.ascontiguousarray(pr.nlu0.transpose(2, 1, 0))).cuda()
+    p = torch.zeros(sh[::-1], dtype=torch.float64, device="cuda")
+    setup_s = time.perf_counter() - t_setup
+
+    def step(solver):
+        p.zero_()
+        torch.cuda.current_stream().synchronize()
+        st, it, mr, loc, dev_s = solver.solve_poisson_device(p.data_ptr(), b.data_ptr())
+        if st != 0:
+            raise RuntimeError(f"solve did not converge: status {st}, {it} iterations, maxres {mr}")
+        return it, dev_s, solver.stats()["launches"]
+
+    def timed(solver, k, w):
+        for _ in range(w):
+            step(solver)
+        if world > 1:
+            torch.distributed.barrier()
+        torch.cuda.synchronize()
+        l0 = solver.stats()["launches"]
+        dev, iters = [], []
+        t0 = time.perf_counter()
+        for _ in range(k):
+            it, d, _ = step(solver)
+            dev.append(d)
+            iters.append(it)
+        torch.cuda.synchronize()
+        wall = time.perf_counter() - t0
+        launches = solver.stats()["launches"] - l0
+        tot = sum(dev)
+        if world > 1:
+            t = torch.tensor([tot], dtype=torch.float64, device="cuda")
+            torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+            tot = float(t.item())
+        return tot, wall, iters, launches
+
+    with ClockSampler(local) as clk:
+        mixed_s, mixed_wall, mixed_iters, mixed_launch = timed(s_mixed, args.steps, args.warmup)
+    clocks = clk.summary()
+    fp64_s, fp64_wall, fp64_iters, _ = timed(s_fp64, max(2, args.steps // 2), 1)
+    value = world * args.steps / mixed_s
+    fp64_value = world * max(2, args.steps // 2) / fp64_s
+
+    # error of the mixed solution vs the FP64 solution on the same inputs
+    step(s_mixed)
+    pm = p.clone()
+    step(s_fp64)
+    pf = p.clone()
+    fl = 1.0 - torch.from_numpy(np.ascontiguousarray(pr.geom.iblank.transpose(2, 1, 0))).cuda().double()
+    n = args.n
+    I = (slice(1, n + 1),) * 3
+    a, c_, f = pm[I] * fl[I], pf[I] * fl[I], fl[I]
+    a = a - a.sum() / f.sum() * f
+    c_ = c_ - c_.sum() / f.sum() * f
+    err = float(torch.linalg.vector_norm(a - c_) / torch.linalg.vector_norm(c_))
+
+    # e2e through the host-buffer C ABI, pinned buffers
+    e2e = None
+    if not args.no_e2e:
+        hp = torch.zeros(sh[::-1], dtype=torch.float64, pin_memory=True)
+        hb = torch.from_numpy(np.ascontiguousarray(pr.nlu0.transpose(2, 1, 0))).pin_memory()
+        hp_np = hp.numpy().transpose(2, 1, 0)
+        hb_np = hb.numpy().transpose(2, 1, 0)
+        for _ in range(1):
+            hp_np[...] = 0.0
+            s_mixed.solve_poisson(hp_np, hb_np)
+        tot = 0.0
+        k = max(2, args.steps // 2)
+        for _ in range(k):
+            hp_np[...] = 0.0
+            st, it, mr, loc, _ = s_mixed.solve_poisson(hp_np, hb_np)
+            tot += s_mixed.stats()["e2e_seconds"]
+        nbytes = int(np.prod(sh)) * 8
+        e2e = {"value": world * k / tot, "unit": "solves/s", "h2d_bytes_per_step": 2 * nbytes,
+               "d2h_bytes_per_step": nbytes}
+
+    # roofline of the dominant kernel family: level-1 FP32 line sweeps (one colour per launch)
+    peaks = json.loads(PEAKS.read_text()) if PEAKS.exists() else {}
+    peak = peaks.get("hbm_gbs", 6800.0)
+    kern = {}
+    for which, name in ((0, "line_x"), (1, "line_y"), (2, "line_z"), (3, "resid_restrict_x"),
+                        (4, "prolong_correct_x"), (5, "calc_residual")):
+        for prec in (1, 0):
+            ms, nb = s_mixed.time_kernel(which, prec, reps=20)
+            kern[f"{name}_{'fp32' if prec else 'fp64'}"] = {"ms": ms, "alg_bytes": nb,
+                                                           "gbs": nb / (ms * 1e-3) / 1e9}
+    line = [kern[f"line_{a}_fp32"] for a in "xyz"]
+    avg_ms = float(np.mean([q["ms"] for q in line]))
+    alg = line[0]["alg_bytes"]
+    achieved = alg / (avg_ms * 1e-3) / 1e9
+    roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                "traffic": None, "kernel": "k_line<float> (x,y,z average, one colour per launch, level 1)",
+                "peak_source": "measured" if PEAKS.exists() else "fallback"}
+
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        v, iters, t_iter, per = cpu_reference(args.n, args.seed, args.tol, sample_n=128, cores=1)
+        cpu = {"value": v, "unit": "solves/s", "cores": 1, "kind": "port",
+               "sample": (f"one outer iteration of the oracle (serial reference MG) at 128^3 "
+                          f"({per[0]:.2f} s), scaled by cell count x{(args.n / 128) ** 3:.0f}, times the oracle's "
+                          f"iteration count at 48^3 ({iters})")}
+
+    out = {
+        "metric": METRIC, "value": value, "unit": "solves/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": 1e3 * mixed_s / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32 cycle + f64 refinement", "data": "synthetic",
+        "config": {"workload": f"sphere_{args.n}^3_tanh1.5_r0.15_tol{args.tol:g}_mixed", "grid": args.n,
+                   "tol": args.tol, "stretch": 1.5, "radius": 0.15, "triangles": 5120, "nGhost": int(pr.geom.nGhost),
+                   "compat_shift": shift, "l2": "inputs larger than L2 (two 139 MB FP64 fields + hierarchy)",
+                   "parallelism": "replicas" if world > 1 else "single GPU"},
+        "fp64_value": fp64_value, "fp64_ms_per_step": 1e3 * fp64_s / max(2, args.steps // 2),
+        "mixed_over_fp64": value / fp64_value, "mixed_vs_fp64_rel_l2": err,
+        "iters_mixed": mixed_iters[0], "iters_fp64": fp64_iters[0],
+        "wall_ms_per_step": 1e3 * mixed_wall / args.steps,
+        "gpu_launches": int(mixed_launch), "clocks": clocks, "e2e": e2e, "roofline": roofline,
+        "kernels": kern, "cpu_baseline": cpu, "setup_s": setup_s,
+    }
+    if rank == 0:
+        print(json.dumps(out))
+    s_mixed.close()
+    s_fp64.close()
+    if world > 1:
+        torch.distributed.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

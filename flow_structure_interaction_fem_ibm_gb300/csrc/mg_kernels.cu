@@ -1,0 +1,823 @@
+// Kernels of the GB300 pressure-Poisson multigrid.  Each kernel cites the
+// reference routine whose arithmetic it performs.
+#include "mg_kernels.cuh"
+
+#include <cfloat>
+
+namespace fsimg {
+
+namespace {
+
+constexpr int TPB = 256;
+
+inline int nblk(long long n, int tpb = TPB)
+{
+    long long b = (n + tpb - 1) / tpb;
+    return (int)(b < 1 ? 1 : b);
+}
+
+template <int DIR> struct Axes;
+template <> struct Axes<0> { static constexpr int a = 0, b = 1, c = 2; static constexpr bool c_first = false; };
+template <> struct Axes<1> { static constexpr int a = 1, b = 0, c = 2; static constexpr bool c_first = false; };
+template <> struct Axes<2> { static constexpr int a = 2, b = 0, c = 1; static constexpr bool c_first = true; };
+
+__device__ __forceinline__ long long stride_of(const Dims &d, int axis)
+{
+    return axis == 0 ? 1LL : (axis == 1 ? d.sx : d.sxy);
+}
+
+// ---------------------------------------------------------------------------
+// Red-black line relaxation, one colour, one direction (IBM/CORE_MG.F90:1883-2270
+// MG_itsolv with the colour set {lines with (p+q) mod 2 == colour}).  One thread
+// per line: right-hand side assembly with the off-line neighbours, forward
+// elimination with the precomputed factor binv (IBM/CORE_TDMA.F90:10-34), back
+// substitution with gam, relaxation var = var (1-omega) + omega sol.
+// ---------------------------------------------------------------------------
+template <typename T, int DIR, bool OMEGA1>
+__global__ void __launch_bounds__(TPB) k_line(LineArgs<T> A)
+{
+    using X = Axes<DIR>;
+    const Dims &d = A.d;
+    const int nb = d.m[X::b] - 1, nc = d.m[X::c] - 1, L = d.m[X::a] - 1;
+    const int hb = (nb + 1) >> 1;
+    long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= (long long)hb * nc) return;
+    const int q = 1 + (int)(t / hb);
+    const int tp = (int)(t % hb);
+    const int p0 = (((1 + q) & 1) == A.colour) ? 1 : 2;
+    const int p = p0 + 2 * tp;
+    if (p > nb) return;
+    const long long sa = stride_of(d, X::a), sb = stride_of(d, X::b), sc = stride_of(d, X::c);
+    const long long base = p * sb + q * sc;
+    const T cmb = A.c.cm[X::b][p], cpb = A.c.cp[X::b][p];
+    const T cmc = A.c.cm[X::c][q], cpc = A.c.cp[X::c][q];
+    const T *__restrict__ cma = A.c.cm[X::a];
+    const T *__restrict__ cpa = A.c.cp[X::a];
+    const uint8_t bmb = fb_minus(X::b), bpb = fb_plus(X::b), bmc = fb_minus(X::c), bpc = fb_plus(X::c);
+    const uint8_t bma = fb_minus(X::a), bpa = fb_plus(X::a);
+    T *__restrict__ v = A.v;
+    const T *__restrict__ r = A.r;
+    const uint8_t *__restrict__ fl = A.fl;
+    const T *__restrict__ binv = A.binv;
+    const T *__restrict__ gam = A.gam;
+    T *__restrict__ U = A.U;
+    T uprev = T(0);
+    for (int i = 1; i <= L; ++i) {
+        const long long o = base + i * sa;
+        const uint8_t f = fl[o];
+        const bool fluid = !(f & FB_IB);
+        const T ama = (f & bma) ? T(0) : cma[i];
+        const T apa = (f & bpa) ? T(0) : cpa[i];
+        const T amb = (f & bmb) ? T(0) : cmb;
+        const T apb = (f & bpb) ? T(0) : cpb;
+        const T amc = (f & bmc) ? T(0) : cmc;
+        const T apc = (f & bpc) ? T(0) : cpc;
+        const bool allzero = (ama == T(0)) & (apa == T(0)) & (amb == T(0)) & (apb == T(0)) & (amc == T(0)) & (apc == T(0));
+        const bool normal = fluid && !allzero;
+        T rhs;
+        if (normal) {
+            T s = r[o];
+            if (X::c_first) {
+                s = s - v[o - sc] * amc;
+                s = s - v[o + sc] * apc;
+                s = s - v[o - sb] * amb;
+                s = s - v[o + sb] * apb;
+            } else {
+                s = s - v[o - sb] * amb;
+                s = s - v[o + sb] * apb;
+                s = s - v[o - sc] * amc;
+                s = s - v[o + sc] * apc;
+            }
+            rhs = s;
+        } else {
+            rhs = ((f & FB_GM) || fluid) ? v[o] : T(0);
+        }
+        const T aa = normal ? ama : T(0);
+        if (i == 1 && A.dir_lo) rhs = rhs - A.ppp_lo * aa;
+        if (i == L && A.dir_hi) rhs = rhs - A.ppp_hi * (normal ? apa : T(0));
+        const T u = (rhs - aa * uprev) * binv[o];
+        U[o] = u;
+        uprev = u;
+    }
+    T un = uprev;
+    {
+        const long long o = base + (long long)L * sa;
+        v[o] = OMEGA1 ? un : v[o] * (T(1) - A.omega) + A.omega * un;
+    }
+    for (int i = L - 1; i >= 1; --i) {
+        const long long o = base + i * sa;
+        const T u = U[o] - gam[o + sa] * un;
+        v[o] = OMEGA1 ? u : v[o] * (T(1) - A.omega) + A.omega * u;
+        un = u;
+    }
+    if (A.dir_lo) v[base] = A.ppp_lo;
+    if (A.dir_hi) v[base + (long long)(L + 1) * sa] = A.ppp_hi;
+}
+
+// ---------------------------------------------------------------------------
+// Line factorisation (setup).  Coefficients exactly as MG_itsolv builds them
+// (IBM/CORE_MG.F90:1950-1983) and the Thomas recurrences of tdma
+// (IBM/CORE_TDMA.F90:24-28) without contraction, so the factors match a
+// host FP64 evaluation bit for bit.  All lines (both colours).
+// ---------------------------------------------------------------------------
+template <int DIR>
+__global__ void __launch_bounds__(TPB) k_factor(FactorArgs<double> A)
+{
+    using X = Axes<DIR>;
+    const Dims &d = A.d;
+    const int nb = d.m[X::b] - 1, nc = d.m[X::c] - 1, L = d.m[X::a] - 1;
+    long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= (long long)nb * nc) return;
+    const int p = 1 + (int)(t % nb), q = 1 + (int)(t / nb);
+    const long long sa = stride_of(d, X::a), sb = stride_of(d, X::b), sc = stride_of(d, X::c);
+    const long long base = p * sb + q * sc;
+    const double tiny = (double)1.0e-12f;
+    double binv_prev = 0.0, c_prev = 0.0;
+    for (int i = 1; i <= L; ++i) {
+        const long long o = base + i * sa;
+        const uint8_t f = A.fl[o];
+        int idx[3];
+        idx[X::a] = i; idx[X::b] = p; idx[X::c] = q;
+        double am[3], ap[3];
+        for (int ax = 0; ax < 3; ++ax) {
+            am[ax] = (f & fb_minus(ax)) ? 0.0 : A.c.cm[ax][idx[ax]];
+            ap[ax] = (f & fb_plus(ax)) ? 0.0 : A.c.cp[ax][idx[ax]];
+        }
+        const double acx = -__dadd_rn(am[0], ap[0]);
+        const double acy = -__dadd_rn(am[1], ap[1]);
+        const double acz = -__dadd_rn(am[2], ap[2]);
+        const double diag_raw = __dadd_rn(__dadd_rn(acx, acy), acz);
+        const bool solid = (f & FB_IB) != 0;
+        double a = solid ? 0.0 : am[X::a];
+        double c = solid ? 0.0 : ap[X::a];
+        double b = solid ? 1.0 : diag_raw;
+        if (fabs(b) < tiny) { a = 0.0; c = 0.0; b = 1.0; }
+        double binv, gam;
+        if (i == 1) { binv = 1.0 / b; gam = 0.0; }
+        else {
+            gam = __dmul_rn(c_prev, binv_prev);
+            binv = 1.0 / __dsub_rn(b, __dmul_rn(a, gam));
+        }
+        A.binv64[o] = binv; A.gam64[o] = gam;
+        A.binv32[o] = (float)binv; A.gam32[o] = (float)gam;
+        binv_prev = binv; c_prev = c;
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Residual (IBM/CORE_MG.F90:2316-2375 MG_Residual) fused with the restriction
+// along D (IBM/CORE_MG.F90:2464-2723 MG_Restrict_X/Y/Z).  One thread per coarse
+// interior cell; the fine residual is never stored.
+// ---------------------------------------------------------------------------
+template <typename T>
+__device__ __forceinline__ T cell_residual(const T *__restrict__ v, const T *__restrict__ r,
+                                           const uint8_t *__restrict__ fl, const Coef<T> &c,
+                                           const Dims &d, int i, int j, int k)
+{
+    const long long o = d.idx(i, j, k);
+    const uint8_t f = fl[o];
+    if (f & FB_IB) return T(0);
+    const T bmx = (f & fb_minus(0)) ? T(0) : c.cm[0][i];
+    const T bpx = (f & fb_plus(0)) ? T(0) : c.cp[0][i];
+    const T bmy = (f & fb_minus(1)) ? T(0) : c.cm[1][j];
+    const T bpy = (f & fb_plus(1)) ? T(0) : c.cp[1][j];
+    const T bmz = (f & fb_minus(2)) ? T(0) : c.cm[2][k];
+    const T bpz = (f & fb_plus(2)) ? T(0) : c.cp[2][k];
+    const T bc = (-(bmx + bpx) + -(bmy + bpy)) + -(bmz + bpz);
+    T res = r[o] - v[o] * bc;
+    res = res - v[o - 1] * bmx;
+    res = res - v[o + 1] * bpx;
+    res = res - v[o - d.sx] * bmy;
+    res = res - v[o + d.sx] * bpy;
+    res = res - v[o - d.sxy] * bmz;
+    res = res - v[o + d.sxy] * bpz;
+    return res;
+}
+
+template <typename T, int D>
+__global__ void __launch_bounds__(TPB) k_resid_restrict(RestrictArgs<T> A)
+{
+    const Dims &dc = A.dc;
+    const int n0 = dc.m[0] - 1, n1 = dc.m[1] - 1, n2 = dc.m[2] - 1;
+    long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= (long long)n0 * n1 * n2) return;
+    int ci[3];
+    ci[0] = 1 + (int)(t % n0);
+    ci[1] = 1 + (int)((t / n0) % n1);
+    ci[2] = 1 + (int)(t / ((long long)n0 * n1));
+    int f1[3] = {ci[0], ci[1], ci[2]}, f2[3] = {ci[0], ci[1], ci[2]};
+    f1[D] = 2 * ci[D] - 1;
+    f2[D] = 2 * ci[D];
+    const T r1 = cell_residual(A.v, A.r, A.fl, A.c, A.df, f1[0], f1[1], f1[2]);
+    const T r2 = cell_residual(A.v, A.r, A.fl, A.c, A.df, f2[0], f2[1], f2[2]);
+    const T db = (A.fl[A.df.idx(f1[0], f1[1], f1[2])] & FB_IB) ? T(0) : T(1);
+    const T da = (A.fl[A.df.idx(f2[0], f2[1], f2[2])] & FB_IB) ? T(0) : T(1);
+    const T w1 = A.w1[ci[D]], w2 = A.w2[ci[D]];
+    const T sum1 = da * w2 * r2 + db * w1 * r1;
+    const T temp = da * w2 + db * w1;
+    A.rc[dc.idx(ci[0], ci[1], ci[2])] = (temp > T(0)) ? sum1 / temp : sum1;
+}
+
+// ---------------------------------------------------------------------------
+// Prolongation along D with inverse-distance^2 weights masked by the coarse
+// iblank (IBM/CORE_MG.F90:2885-3523) fused with the correction
+// var += phi (1 - iblank) (IBM/CORE_MG.F90:1354-1355).
+// ---------------------------------------------------------------------------
+template <typename T, int D>
+__global__ void __launch_bounds__(TPB) k_prolong_correct(ProlongArgs<T> A)
+{
+    const Dims &df = A.df;
+    const int n0 = df.m[0] - 1, n1 = df.m[1] - 1, n2 = df.m[2] - 1;
+    long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= (long long)n0 * n1 * n2) return;
+    int fi[3];
+    fi[0] = 1 + (int)(t % n0);
+    fi[1] = 1 + (int)((t / n0) % n1);
+    fi[2] = 1 + (int)(t / ((long long)n0 * n1));
+    const long long o = df.idx(fi[0], fi[1], fi[2]);
+    if (A.flf[o] & FB_IB) return;
+    const int q = fi[D];
+    const int mode = A.mode[q];
+    if (mode == 0) return;
+    int ca[3] = {fi[0], fi[1], fi[2]};
+    ca[D] = A.cA[q];
+    const long long oa = A.dc.idx(ca[0], ca[1], ca[2]);
+    T phi;
+    if (mode == 1) {
+        phi = A.phi[oa];
+    } else {
+        int cb[3] = {fi[0], fi[1], fi[2]};
+        cb[D] = A.cB[q];
+        const long long ob = A.dc.idx(cb[0], cb[1], cb[2]);
+        const T d1 = A.wA[q] * ((A.flc[oa] & FB_IB) ? T(0) : T(1));
+        const T d2 = A.wB[q] * ((A.flc[ob] & FB_IB) ? T(0) : T(1));
+        const T delta = d1 + d2;
+        phi = d1 * A.phi[oa] + d2 * A.phi[ob];
+        if (delta > T(0)) phi = phi / delta;
+    }
+    A.v[o] = A.v[o] + phi;
+}
+
+// ---------------------------------------------------------------------------
+// Outer ghost layer (IBM/CORE_SET_OUTER_GHOST.F90:66-213).  The reference sets
+// the x faces, then the y faces (reading the new x-face values), then the z
+// faces; composed, every outer-layer value is the product of the side signs
+// (+1 Neumann copy, -1 Dirichlet anti-copy) of the faces it lies on times the
+// nearest interior value, which is what each thread writes.
+// ---------------------------------------------------------------------------
+template <typename T>
+__global__ void k_outer_ghost(T *v, Dims d, int s0, int s1, int s2, int s3, int s4, int s5)
+{
+    const int m0 = d.m[0], m1 = d.m[1], m2 = d.m[2];
+    const long long fx = (long long)(m1 + 1) * (m2 + 1);
+    const long long fy = (long long)(m0 + 1) * (m2 + 1);
+    const long long fz = (long long)(m0 + 1) * (m1 + 1);
+    long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    int i, j, k;
+    if (t < 2 * fx) {
+        const int side = (int)(t / fx);
+        const long long u = t % fx;
+        i = side ? m0 : 0; j = (int)(u % (m1 + 1)); k = (int)(u / (m1 + 1));
+    } else if ((t -= 2 * fx) < 2 * fy) {
+        const int side = (int)(t / fy);
+        const long long u = t % fy;
+        j = side ? m1 : 0; i = (int)(u % (m0 + 1)); k = (int)(u / (m0 + 1));
+    } else if ((t -= 2 * fy) < 2 * fz) {
+        const int side = (int)(t / fz);
+        const long long u = t % fz;
+        k = side ? m2 : 0; i = (int)(u % (m0 + 1)); j = (int)(u / (m0 + 1));
+    } else {
+        return;
+    }
+    int sg = 1;
+    int ii = i, jj = j, kk = k;
+    if (i == 0) { sg *= s0; ii = 1; } else if (i == m0) { sg *= s1; ii = m0 - 1; }
+    if (j == 0) { sg *= s2; jj = 1; } else if (j == m1) { sg *= s3; jj = m1 - 1; }
+    if (k == 0) { sg *= s4; kk = 1; } else if (k == m2) { sg *= s5; kk = m2 - 1; }
+    const T val = v[d.idx(ii, jj, kk)];
+    v[d.idx(i, j, k)] = (sg < 0) ? -val : val;
+}
+
+// ---------------------------------------------------------------------------
+// Ghost-cell pressure rows (IBM/GCM_GHOSTCELL_VEL_UPDATE_UNSTRUC.F90:250-384):
+// p_g = sum_r coeffGCMN(r,g) p(stencil_r), the ghost's own stencil entry taking
+// uNormal = 0 (viscous flow).  Jacobi sweeps over the compact gather list in one
+// thread block until max |dp| <= max(tol, reltol max|p_g|) or iterMax.
+// ---------------------------------------------------------------------------
+template <typename T>
+__global__ void __launch_bounds__(1024) k_ghost_rows(T *v, GhostArgs g, const T *coeff, T *scratch, int iterMax,
+                                                     double tol, double reltol, int *iters,
+                                                     unsigned long long *maxdelta)
+{
+    __shared__ double s_d[32], s_a[32];
+    __shared__ double s_res[2];
+    const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5, nw = (blockDim.x + 31) >> 5;
+    int it = 0;
+    double maxd = 1.0e10, thr = tol;
+    while (it < iterMax && maxd > thr) {
+        double ld = 0.0, la = 0.0;
+        for (int n = tid; n < g.n; n += blockDim.x) {
+            T acc = T(0);
+#pragma unroll
+            for (int r = 0; r < 8; ++r) {
+                const long long s = g.sidx[8LL * n + r];
+                const T val = (s < 0) ? T(0) : v[s];
+                acc = acc + coeff[8LL * n + r] * val;
+            }
+            const T old = v[g.gidx[n]];
+            scratch[n] = acc;
+            ld = fmax(ld, fabs((double)acc - (double)old));
+            la = fmax(la, fabs((double)acc));
+        }
+        for (int o = 16; o > 0; o >>= 1) {
+            ld = fmax(ld, __shfl_xor_sync(0xffffffffu, ld, o));
+            la = fmax(la, __shfl_xor_sync(0xffffffffu, la, o));
+        }
+        if (lane == 0) { s_d[wid] = ld; s_a[wid] = la; }
+        __syncthreads();
+        if (tid == 0) {
+            double a = 0.0, b = 0.0;
+            for (int w = 0; w < nw; ++w) { a = fmax(a, s_d[w]); b = fmax(b, s_a[w]); }
+            s_res[0] = a; s_res[1] = b;
+        }
+        __syncthreads();
+        for (int n = tid; n < g.n; n += blockDim.x) v[g.gidx[n]] = scratch[n];
+        maxd = s_res[0];
+        thr = fmax(tol, reltol * s_res[1]);
+        ++it;
+        __syncthreads();
+    }
+    if (tid == 0) {
+        atomicAdd(iters, it);
+        unsigned long long bits = (unsigned long long)__double_as_longlong(maxd);
+        atomicMax(maxdelta, bits);
+    }
+}
+
+template <typename T>
+__global__ void k_fill(T *p, long long n, T val)
+{
+    long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t < n) p[t] = val;
+}
+
+// ---------------------------------------------------------------------------
+// calc_residual (IBM/CORE_POISSON.F90:1111-1222): r - A p + nlw0 on fluid
+// cells, max |res| and the first (k,j,i)-ordered location attaining it.
+// Optionally stores the residual in FP32 (inner right-hand side of the
+// mixed-precision refinement).
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ void maxloc_merge(double &v, long long &i, double v2, long long i2)
+{
+    if (v2 > v || (v2 == v && i2 < i)) { v = v2; i = i2; }
+}
+
+__global__ void __launch_bounds__(TPB) k_calc_residual(const double *p, const double *b, const double *nlw0,
+                                                       const uint8_t *fl, Coef<double> c, Dims d, float *r32,
+                                                       MaxLoc *partials)
+{
+    const int n0 = d.m[0] - 1, n1 = d.m[1] - 1, n2 = d.m[2] - 1;
+    const long long total = (long long)n0 * n1 * n2;
+    double best = -1.0;
+    long long bi = 0x7fffffffffffffffLL;
+    for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < total;
+         t += (long long)gridDim.x * blockDim.x) {
+        const int i = 1 + (int)(t % n0), j = 1 + (int)((t / n0) % n1), k = 1 + (int)(t / ((long long)n0 * n1));
+        const long long o = d.idx(i, j, k);
+        double res = cell_residual(p, b, fl, c, d, i, j, k);
+        if (nlw0 && !(fl[o] & FB_IB)) res = res + nlw0[o];
+        if (r32) r32[o] = (float)res;
+        double a = fabs(res);
+        if (!(a == a)) a = INFINITY;   // a NaN residual must not be skipped by the max
+        maxloc_merge(best, bi, a, o);
+    }
+    for (int off = 16; off > 0; off >>= 1) {
+        double v2 = __shfl_xor_sync(0xffffffffu, best, off);
+        long long i2 = __shfl_xor_sync(0xffffffffu, bi, off);
+        maxloc_merge(best, bi, v2, i2);
+    }
+    __shared__ double sv[TPB / 32];
+    __shared__ long long si[TPB / 32];
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    if (lane == 0) { sv[wid] = best; si[wid] = bi; }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        for (int w = 1; w < TPB / 32; ++w) maxloc_merge(best, bi, sv[w], si[w]);
+        partials[blockIdx.x].v = best;
+        partials[blockIdx.x].i = bi;
+    }
+}
+
+__global__ void k_maxloc_final(const MaxLoc *partials, int n, MaxLoc *out)
+{
+    double best = -1.0;
+    long long bi = 0x7fffffffffffffffLL;
+    for (int t = threadIdx.x; t < n; t += blockDim.x) maxloc_merge(best, bi, partials[t].v, partials[t].i);
+    for (int off = 16; off > 0; off >>= 1) {
+        double v2 = __shfl_xor_sync(0xffffffffu, best, off);
+        long long i2 = __shfl_xor_sync(0xffffffffu, bi, off);
+        maxloc_merge(best, bi, v2, i2);
+    }
+    __shared__ double sv[32];
+    __shared__ long long si[32];
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    if (lane == 0) { sv[wid] = best; si[wid] = bi; }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        for (int w = 1; w < (int)(blockDim.x >> 5); ++w) maxloc_merge(best, bi, sv[w], si[w]);
+        out->v = best < 0 ? 0.0 : best;
+        out->i = bi;
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Deterministic block-partial sums (fixed order), shared by the fluid-volume
+// mean (IBM/CORE_POISSON.F90:433-443) and the compatibility flux
+// (IBM/GCM_GLOBAL_MASS_CONSERVE.F90:290-331).
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ double block_sum(double x)
+{
+    for (int off = 16; off > 0; off >>= 1) x += __shfl_xor_sync(0xffffffffu, x, off);
+    __shared__ double s[TPB / 32];
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    __syncthreads();
+    if (lane == 0) s[wid] = x;
+    __syncthreads();
+    double tot = 0.0;
+    if (threadIdx.x == 0)
+        for (int w = 0; w < (int)(blockDim.x >> 5); ++w) tot += s[w];
+    return tot;
+}
+
+__global__ void __launch_bounds__(TPB) k_avg_partial(const double *p, const uint8_t *fl, const double *dx,
+                                                     const double *dy, const double *dz, Dims d,
+                                                     double *partials)
+{
+    const int n0 = d.m[0] - 1, n1 = d.m[1] - 1, n2 = d.m[2] - 1;
+    const long long total = (long long)n0 * n1 * n2;
+    double sp = 0.0, sv = 0.0;
+    for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < total;
+         t += (long long)gridDim.x * blockDim.x) {
+        const int i = 1 + (int)(t % n0), j = 1 + (int)((t / n0) % n1), k = 1 + (int)(t / ((long long)n0 * n1));
+        const long long o = d.idx(i, j, k);
+        if (fl[o] & FB_IB) continue;
+        const double vol = dx[i] * dy[j] * dz[k];
+        sp += p[o] * dx[i] * dy[j] * dz[k];
+        sv += vol;
+    }
+    const double a = block_sum(sp);
+    const double b = block_sum(sv);
+    if (threadIdx.x == 0) { partials[2 * blockIdx.x] = a; partials[2 * blockIdx.x + 1] = b; }
+}
+
+__global__ void k_sum_final(double *partials, int n, int stride, double *out)
+{
+    // out[c] = sum_t partials[stride*t + c] for c < stride, fixed order per thread then tree
+    for (int c = 0; c < stride; ++c) {
+        double x = 0.0;
+        for (int t = threadIdx.x; t < n; t += blockDim.x) x += partials[(long long)stride * t + c];
+        const double tot = block_sum(x);
+        if (threadIdx.x == 0) out[c] = tot;
+        __syncthreads();
+    }
+}
+
+__global__ void __launch_bounds__(TPB) k_avg_apply(double *p, const uint8_t *fl, Dims d, const double *sums)
+{
+    const int n0 = d.m[0] - 1, n1 = d.m[1] - 1, n2 = d.m[2] - 1;
+    const long long total = (long long)n0 * n1 * n2;
+    long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= total) return;
+    const int i = 1 + (int)(t % n0), j = 1 + (int)((t / n0) % n1), k = 1 + (int)(t / ((long long)n0 * n1));
+    const long long o = d.idx(i, j, k);
+    const double pAvg = sums[0] / sums[1];
+    p[o] = (fl[o] & FB_IB) ? 0.0 : p[o] - pAvg;
+}
+
+// compatibility flux, non-periodic branch (IBM/GCM_GLOBAL_MASS_CONSERVE.F90:290-331)
+struct CompatArgs {
+    const double *p;
+    const uint8_t *fl;
+    const double *pg;  // packed pgrad planes
+    const double *dx, *dy, *dz, *dxcinv, *dycinv, *dzcinv;
+    int sf[6];         // raw boundary flag value of each side (ium(1)... iup(nxc)...)
+    Dims d;
+    long long off[6];
+    int pgsx[6];
+};
+
+__device__ __forceinline__ int face_flag(uint8_t f, int axis, int plus, int side_raw, bool at_boundary)
+{
+    if (at_boundary) return side_raw;
+    return (f & (plus ? fb_plus(axis) : fb_minus(axis))) ? 1 : 0;
+}
+
+__global__ void __launch_bounds__(TPB) k_compat_partial(CompatArgs A, double *partials)
+{
+    const Dims &d = A.d;
+    const int n0 = d.m[0] - 1, n1 = d.m[1] - 1, n2 = d.m[2] - 1;
+    const long long total = (long long)n0 * n1 * n2;
+    double acc = 0.0;
+    for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < total;
+         t += (long long)gridDim.x * blockDim.x) {
+        const int i = 1 + (int)(t % n0), j = 1 + (int)((t / n0) % n1), k = 1 + (int)(t / ((long long)n0 * n1));
+        const long long o = d.idx(i, j, k);
+        const uint8_t f = A.fl[o];
+        if (f & FB_IB) continue;
+        const int ium = face_flag(f, 0, 0, A.sf[0], i == 1), iup = face_flag(f, 0, 1, A.sf[1], i == n0);
+        const int jum = face_flag(f, 1, 0, A.sf[2], j == 1), jup = face_flag(f, 1, 1, A.sf[3], j == n1);
+        const int kum = face_flag(f, 2, 0, A.sf[4], k == 1), kup = face_flag(f, 2, 1, A.sf[5], k == n2);
+        const double *P = A.p;
+        const double pgx1 = A.pg[A.off[0] + j + (long long)A.pgsx[0] * k];
+        const double pgx2 = A.pg[A.off[1] + j + (long long)A.pgsx[1] * k];
+        const double pgy1 = A.pg[A.off[2] + i + (long long)A.pgsx[2] * k];
+        const double pgy2 = A.pg[A.off[3] + i + (long long)A.pgsx[3] * k];
+        const double pgz1 = A.pg[A.off[4] + i + (long long)A.pgsx[4] * j];
+        const double pgz2 = A.pg[A.off[5] + i + (long long)A.pgsx[5] * j];
+        const double pgxw = pgx1 * ium + ((double)(1 - ium) * (P[o] - P[o - 1])) * A.dxcinv[i];
+        const double pgxe = pgx2 * iup + ((double)(1 - iup) * (P[o + 1] - P[o])) * A.dxcinv[i + 1];
+        const double pgys = pgy1 * jum + ((double)(1 - jum) * (P[o] - P[o - d.sx])) * A.dycinv[j];
+        const double pgyn = pgy2 * jup + ((double)(1 - jup) * (P[o + d.sx] - P[o])) * A.dycinv[j + 1];
+        const double pgzb = pgz1 * kum + ((double)(1 - kum) * (P[o] - P[o - d.sxy])) * A.dzcinv[k];
+        const double pgzf = pgz2 * kup + ((double)(1 - kup) * (P[o + d.sxy] - P[o])) * A.dzcinv[k + 1];
+        acc += -(pgxw * A.dy[j] * A.dz[k]) + pgxe * A.dy[j] * A.dz[k] - pgys * A.dx[i] * A.dz[k] +
+               pgyn * A.dx[i] * A.dz[k] - pgzb * A.dx[i] * A.dy[j] + pgzf * A.dx[i] * A.dy[j];
+    }
+    const double s = block_sum(acc);
+    if (threadIdx.x == 0) partials[blockIdx.x] = s;
+}
+
+__global__ void k_pgrad_shift(double *pg, long long off, long long n, const double *flux, double outflow_area,
+                              double sign)
+{
+    long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= n) return;
+    const double corr = -flux[0] / outflow_area;
+    pg[off + t] = pg[off + t] + sign * corr;
+}
+
+// nlw0 = -dxinv (iup pgx2 - ium pgx1) - dyinv (...) - dzinv (...), pot_flag = 0
+// (IBM/CORE_POISSON.F90:1813-1821), interior cells.
+__global__ void __launch_bounds__(TPB) k_nlw0(double *nlw0, CompatArgs A, const double *dxinv, const double *dyinv,
+                                              const double *dzinv)
+{
+    const Dims &d = A.d;
+    const int n0 = d.m[0] - 1, n1 = d.m[1] - 1, n2 = d.m[2] - 1;
+    const long long total = (long long)n0 * n1 * n2;
+    long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= total) return;
+    const int i = 1 + (int)(t % n0), j = 1 + (int)((t / n0) % n1), k = 1 + (int)(t / ((long long)n0 * n1));
+    const long long o = d.idx(i, j, k);
+    const uint8_t f = A.fl[o];
+    const int ium = face_flag(f, 0, 0, A.sf[0], i == 1), iup = face_flag(f, 0, 1, A.sf[1], i == n0);
+    const int jum = face_flag(f, 1, 0, A.sf[2], j == 1), jup = face_flag(f, 1, 1, A.sf[3], j == n1);
+    const int kum = face_flag(f, 2, 0, A.sf[4], k == 1), kup = face_flag(f, 2, 1, A.sf[5], k == n2);
+    const double pgx1 = A.pg[A.off[0] + j + (long long)A.pgsx[0] * k];
+    const double pgx2 = A.pg[A.off[1] + j + (long long)A.pgsx[1] * k];
+    const double pgy1 = A.pg[A.off[2] + i + (long long)A.pgsx[2] * k];
+    const double pgy2 = A.pg[A.off[3] + i + (long long)A.pgsx[3] * k];
+    const double pgz1 = A.pg[A.off[4] + i + (long long)A.pgsx[4] * j];
+    const double pgz2 = A.pg[A.off[5] + i + (long long)A.pgsx[5] * j];
+    nlw0[o] = -(dxinv[i] * (iup * pgx2 - ium * pgx1)) - dyinv[j] * (jup * pgy2 - jum * pgy1) -
+              dzinv[k] * (kup * pgz2 - kum * pgz1);
+}
+
+__global__ void k_accumulate(double *p, const float *e, long long n)
+{
+    long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t < n) p[t] = p[t] + (double)e[t];
+}
+__global__ void k_f2d(double *dst, const float *src, long long n)
+{
+    long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t < n) dst[t] = (double)src[t];
+}
+__global__ void k_d2f(float *dst, const double *src, long long n)
+{
+    long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t < n) dst[t] = (float)src[t];
+}
+
+// ---------------------------------------------------------------------------
+// Hierarchy setup (IBM/CORE_MG.F90:699-822 MG_Prepare_Iblank and :1716-1879
+// MG_Prepare).  Level-1 flag bytes are packed on the host from the caller's arrays.
+// ---------------------------------------------------------------------------
+__global__ void k_coarse_iblank(uint8_t *flc, const uint8_t *flf, Dims dc, Dims df, int D)
+{
+    // coarse iblank = product of the two children along D, interior cells only
+    const int n0 = dc.m[0] - 1, n1 = dc.m[1] - 1, n2 = dc.m[2] - 1;
+    long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= dc.count()) return;
+    const int i = (int)(t % dc.sx), j = (int)((t / dc.sx) % (dc.m[1] + 1)), k = (int)(t / dc.sxy);
+    uint8_t out = 0;
+    if (i >= 1 && i <= n0 && j >= 1 && j <= n1 && k >= 1 && k <= n2) {
+        int a[3] = {i, j, k}, b[3] = {i, j, k};
+        a[D] = 2 * a[D] - 1;
+        b[D] = 2 * b[D];
+        const int ia = flf[df.idx(a[0], a[1], a[2])] & FB_IB, ibb = flf[df.idx(b[0], b[1], b[2])] & FB_IB;
+        if (ia && ibb) out = FB_IB;
+    }
+    flc[t] = out;
+}
+
+__global__ void k_coarse_flags(uint8_t *fl, Dims d, int sb0, int sb1, int sb2, int sb3, int sb4, int sb5)
+{
+    // face bit set where the cell is fluid and the neighbour is solid (INT((ib_nb - ib)/2 + 1/2) = 1);
+    // outer faces take the side value (bit set for flag value 1).
+    const int n0 = d.m[0] - 1, n1 = d.m[1] - 1, n2 = d.m[2] - 1;
+    long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= (long long)n0 * n1 * n2) return;
+    const int i = 1 + (int)(t % n0), j = 1 + (int)((t / n0) % n1), k = 1 + (int)(t / ((long long)n0 * n1));
+    const long long o = d.idx(i, j, k);
+    uint8_t f = fl[o] & FB_IB;
+    const int me = f ? 1 : 0;
+    auto sol = [&](long long q) { return (fl[q] & FB_IB) ? 1 : 0; };
+    if (i == 1) { if (sb0) f |= fb_minus(0); } else if (me == 0 && sol(o - 1)) f |= fb_minus(0);
+    if (i == n0) { if (sb1) f |= fb_plus(0); } else if (me == 0 && sol(o + 1)) f |= fb_plus(0);
+    if (j == 1) { if (sb2) f |= fb_minus(1); } else if (me == 0 && sol(o - d.sx)) f |= fb_minus(1);
+    if (j == n1) { if (sb3) f |= fb_plus(1); } else if (me == 0 && sol(o + d.sx)) f |= fb_plus(1);
+    if (k == 1) { if (sb4) f |= fb_minus(2); } else if (me == 0 && sol(o - d.sxy)) f |= fb_minus(2);
+    if (k == n2) { if (sb5) f |= fb_plus(2); } else if (me == 0 && sol(o + d.sxy)) f |= fb_plus(2);
+    fl[o] = f;
+}
+
+} // namespace
+
+// ------------------------------------------------------------- launchers --
+template <typename T>
+void launch_line(int dir, const LineArgs<T> &a, bool omega_one, cudaStream_t s)
+{
+    static const int ob[3] = {1, 0, 0}, oc[3] = {2, 2, 1};
+    const int nb = a.d.m[ob[dir]] - 1, nc = a.d.m[oc[dir]] - 1;
+    const long long n = (long long)((nb + 1) / 2) * nc;
+    const int g = nblk(n);
+#define L_(D, O) k_line<T, D, O><<<g, TPB, 0, s>>>(a)
+    if (omega_one) {
+        if (dir == 0) L_(0, true); else if (dir == 1) L_(1, true); else L_(2, true);
+    } else {
+        if (dir == 0) L_(0, false); else if (dir == 1) L_(1, false); else L_(2, false);
+    }
+#undef L_
+}
+
+void launch_factor(int dir, const FactorArgs<double> &a, cudaStream_t s)
+{
+    static const int ob[3] = {1, 0, 0}, oc[3] = {2, 2, 1};
+    const long long n = (long long)(a.d.m[ob[dir]] - 1) * (a.d.m[oc[dir]] - 1);
+    if (dir == 0) k_factor<0><<<nblk(n), TPB, 0, s>>>(a);
+    else if (dir == 1) k_factor<1><<<nblk(n), TPB, 0, s>>>(a);
+    else k_factor<2><<<nblk(n), TPB, 0, s>>>(a);
+}
+
+template <typename T>
+void launch_resid_restrict(int D, const RestrictArgs<T> &a, cudaStream_t s)
+{
+    const long long n = (long long)(a.dc.m[0] - 1) * (a.dc.m[1] - 1) * (a.dc.m[2] - 1);
+    if (D == 0) k_resid_restrict<T, 0><<<nblk(n), TPB, 0, s>>>(a);
+    else if (D == 1) k_resid_restrict<T, 1><<<nblk(n), TPB, 0, s>>>(a);
+    else k_resid_restrict<T, 2><<<nblk(n), TPB, 0, s>>>(a);
+}
+
+template <typename T>
+void launch_prolong_correct(int D, const ProlongArgs<T> &a, cudaStream_t s)
+{
+    const long long n = (long long)(a.df.m[0] - 1) * (a.df.m[1] - 1) * (a.df.m[2] - 1);
+    if (D == 0) k_prolong_correct<T, 0><<<nblk(n), TPB, 0, s>>>(a);
+    else if (D == 1) k_prolong_correct<T, 1><<<nblk(n), TPB, 0, s>>>(a);
+    else k_prolong_correct<T, 2><<<nblk(n), TPB, 0, s>>>(a);
+}
+
+template <typename T>
+void launch_outer_ghost(T *v, const Dims &d, const int sign[6], cudaStream_t s)
+{
+    const long long n = 2LL * ((long long)(d.m[1] + 1) * (d.m[2] + 1) + (long long)(d.m[0] + 1) * (d.m[2] + 1) +
+                               (long long)(d.m[0] + 1) * (d.m[1] + 1));
+    k_outer_ghost<T><<<nblk(n), TPB, 0, s>>>(v, d, sign[0], sign[1], sign[2], sign[3], sign[4], sign[5]);
+}
+
+template <typename T>
+void launch_ghost_rows(T *v, const GhostArgs &g, const T *coeff, T *scratch, int iterMax, double tol,
+                       double reltol, int *d_iters, unsigned long long *d_maxdelta, cudaStream_t s)
+{
+    if (g.n <= 0) return;
+    k_ghost_rows<T><<<1, 1024, 0, s>>>(v, g, coeff, scratch, iterMax, tol, reltol, d_iters, d_maxdelta);
+}
+
+template <typename T>
+void launch_fill(T *p, long long n, T val, cudaStream_t s)
+{
+    k_fill<T><<<nblk(n), TPB, 0, s>>>(p, n, val);
+}
+
+int calc_residual_blocks(const Dims &d)
+{
+    const long long n = (long long)(d.m[0] - 1) * (d.m[1] - 1) * (d.m[2] - 1);
+    long long b = (n + TPB * 8 - 1) / (TPB * 8);
+    if (b > 2048) b = 2048;
+    return (int)(b < 1 ? 1 : b);
+}
+
+void launch_calc_residual(const double *p, const double *b, const double *nlw0, const uint8_t *fl,
+                          const Coef<double> &c, const Dims &d, float *r32_out, MaxLoc *partials, int nblocks,
+                          MaxLoc *result, cudaStream_t s)
+{
+    k_calc_residual<<<nblocks, TPB, 0, s>>>(p, b, nlw0, fl, c, d, r32_out, partials);
+    k_maxloc_final<<<1, 1024, 0, s>>>(partials, nblocks, result);
+}
+
+void launch_subtract_average(double *p, const uint8_t *fl, const double *dx, const double *dy, const double *dz,
+                             const Dims &d, double *partials, int nblocks, cudaStream_t s)
+{
+    k_avg_partial<<<nblocks, TPB, 0, s>>>(p, fl, dx, dy, dz, d, partials);
+    double *sums = partials + 2LL * nblocks;
+    k_sum_final<<<1, 1024, 0, s>>>(partials, nblocks, 2, sums);
+    const long long n = (long long)(d.m[0] - 1) * (d.m[1] - 1) * (d.m[2] - 1);
+    k_avg_apply<<<nblk(n), TPB, 0, s>>>(p, fl, d, sums);
+}
+
+static CompatArgs make_compat(const double *p, const uint8_t *fl, const double *pg, const double *dx,
+                              const double *dy, const double *dz, const double *dxcinv, const double *dycinv,
+                              const double *dzcinv, const int side_flag[6], const Dims &d, int nx, int ny, int nz)
+{
+    CompatArgs A;
+    A.p = p; A.fl = fl; A.pg = pg; A.dx = dx; A.dy = dy; A.dz = dz;
+    A.dxcinv = dxcinv; A.dycinv = dycinv; A.dzcinv = dzcinv; A.d = d;
+    for (int q = 0; q < 6; ++q) A.sf[q] = side_flag[q];
+    const long long px = (long long)(ny + 2) * (nz + 2), py = (long long)(nx + 2) * (nz + 2),
+                    pz = (long long)(nx + 2) * (ny + 2);
+    A.off[0] = 0; A.off[1] = px; A.off[2] = 2 * px; A.off[3] = 2 * px + py; A.off[4] = 2 * px + 2 * py;
+    A.off[5] = 2 * px + 2 * py + pz;
+    A.pgsx[0] = A.pgsx[1] = ny + 2; A.pgsx[2] = A.pgsx[3] = nx + 2; A.pgsx[4] = A.pgsx[5] = nx + 2;
+    return A;
+}
+
+void launch_compat(const double *p, const uint8_t *fl, const double *pg, const double *dx, const double *dy,
+                   const double *dz, const double *dxcinv, const double *dycinv, const double *dzcinv,
+                   const int side_flag[6], const Dims &d, double *partials, int nblocks, double *pgrad,
+                   const int bc_zero_grad[6], double outflow_area, int nx, int ny, int nz, cudaStream_t s)
+{
+    CompatArgs A = make_compat(p, fl, pg, dx, dy, dz, dxcinv, dycinv, dzcinv, side_flag, d, nx, ny, nz);
+    k_compat_partial<<<nblocks, TPB, 0, s>>>(A, partials);
+    double *flux = partials + nblocks;
+    k_sum_final<<<1, 1024, 0, s>>>(partials, nblocks, 1, flux);
+    const long long px = (long long)(ny + 2) * (nz + 2), py = (long long)(nx + 2) * (nz + 2),
+                    pz = (long long)(nx + 2) * (ny + 2);
+    const long long sizes[6] = {px, px, py, py, pz, pz};
+    const double signs[6] = {-1.0, 1.0, -1.0, 1.0, -1.0, 1.0};
+    for (int q = 0; q < 6; ++q)
+        if (bc_zero_grad[q])
+            k_pgrad_shift<<<nblk(sizes[q]), TPB, 0, s>>>(pgrad, A.off[q], sizes[q], flux, outflow_area, signs[q]);
+}
+
+void launch_nlw0(double *nlw0, const uint8_t *fl, const int side_flag[6], const double *pgrad, const double *dxinv,
+                 const double *dyinv, const double *dzinv, const Dims &d, int nx, int ny, int nz, cudaStream_t s)
+{
+    CompatArgs A = make_compat(nullptr, fl, pgrad, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, side_flag,
+                               d, nx, ny, nz);
+    const long long n = (long long)(d.m[0] - 1) * (d.m[1] - 1) * (d.m[2] - 1);
+    k_nlw0<<<nblk(n), TPB, 0, s>>>(nlw0, A, dxinv, dyinv, dzinv);
+}
+
+void launch_accumulate(double *p, const float *e, long long n, cudaStream_t s)
+{
+    k_accumulate<<<nblk(n), TPB, 0, s>>>(p, e, n);
+}
+void launch_convert_f2d(double *dst, const float *src, long long n, cudaStream_t s)
+{
+    k_f2d<<<nblk(n), TPB, 0, s>>>(dst, src, n);
+}
+void launch_convert_d2f(float *dst, const double *src, long long n, cudaStream_t s)
+{
+    k_d2f<<<nblk(n), TPB, 0, s>>>(dst, src, n);
+}
+
+void launch_coarse_iblank(uint8_t *fl_c, const uint8_t *fl_f, const Dims &dc, const Dims &df, int D,
+                          cudaStream_t s)
+{
+    k_coarse_iblank<<<nblk(dc.count()), TPB, 0, s>>>(fl_c, fl_f, dc, df, D);
+}
+
+void launch_coarse_flags(uint8_t *fl, const Dims &d, const int sb[6], cudaStream_t s)
+{
+    const long long n = (long long)(d.m[0] - 1) * (d.m[1] - 1) * (d.m[2] - 1);
+    k_coarse_flags<<<nblk(n), TPB, 0, s>>>(fl, d, sb[0], sb[1], sb[2], sb[3], sb[4], sb[5]);
+}
+
+// explicit instantiations
+template void launch_line<double>(int, const LineArgs<double> &, bool, cudaStream_t);
+template void launch_line<float>(int, const LineArgs<float> &, bool, cudaStream_t);
+template void launch_resid_restrict<double>(int, const RestrictArgs<double> &, cudaStream_t);
+template void launch_resid_restrict<float>(int, const RestrictArgs<float> &, cudaStream_t);
+template void launch_prolong_correct<double>(int, const ProlongArgs<double> &, cudaStream_t);
+template void launch_prolong_correct<float>(int, const ProlongArgs<float> &, cudaStream_t);
+template void launch_outer_ghost<double>(double *, const Dims &, const int *, cudaStream_t);
+template void launch_outer_ghost<float>(float *, const Dims &, const int *, cudaStream_t);
+template void launch_ghost_rows<double>(double *, const GhostArgs &, const double *, double *, int, double, double,
+                                        int *, unsigned long long *, cudaStream_t);
+template void launch_ghost_rows<float>(float *, const GhostArgs &, const float *, float *, int, double, double,
+                                       int *, unsigned long long *, cudaStream_t);
+template void launch_fill<double>(double *, long long, double, cudaStream_t);
+template void launch_fill<float>(float *, long long, float, cudaStream_t);
+template void launch_fill<uint8_t>(uint8_t *, long long, uint8_t, cudaStream_t);
+
+} // namespace fsimg

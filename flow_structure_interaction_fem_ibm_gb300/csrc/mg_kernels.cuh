@@ -1,0 +1,127 @@
+// Device kernels of the pressure-Poisson multigrid (sm_103a) and their host
+// launchers.  A level array covers (0:m0, 0:m1, 0:m2), column-major with strides
+// sx, sxy (level 1 keeps the caller's (0:nx+1)^3 pitch, coarse levels are dense).
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace fsimg {
+
+// per-cell flag byte
+enum : uint8_t {
+    FB_IB = 1,    // iblank (of this level)
+    FB_GM = 2,    // ghost-cell mark (level 1 only)
+    FB_FACE = 4,  // face bits: 4 << (2*axis) minus side, 8 << (2*axis) plus side (flag value 1)
+};
+__host__ __device__ constexpr uint8_t fb_minus(int axis) { return (uint8_t)(4u << (2 * axis)); }
+__host__ __device__ constexpr uint8_t fb_plus(int axis) { return (uint8_t)(8u << (2 * axis)); }
+
+struct Dims {
+    int m[3];          // upper bounds
+    long long sx, sxy; // strides
+    __host__ __device__ long long idx(int i, int j, int k) const { return i + sx * j + sxy * k; }
+    __host__ __device__ long long count() const { return sxy * (long long)(m[2] + 1); }
+};
+
+template <typename T>
+struct Coef {         // 1D face coefficients per axis: cm[i] = dcinv(i) dinv(i), cp[i] = dcinv(i+1) dinv(i)
+    const T *cm[3];
+    const T *cp[3];
+};
+
+template <typename T>
+struct LineArgs {
+    T *v;
+    const T *r;
+    const uint8_t *fl;
+    const T *binv;
+    const T *gam;
+    T *U;
+    Coef<T> c;
+    Dims d;
+    int colour;
+    T omega;
+    int dir_lo, dir_hi;   // finest-level Dirichlet ends along the line direction
+    T ppp_lo, ppp_hi;
+};
+
+template <typename T>
+struct FactorArgs {   // line factorisation of the smoother's tridiagonal systems
+    const uint8_t *fl;
+    Coef<double> c;
+    Dims d;
+    double *binv64, *gam64;
+    float *binv32, *gam32;
+};
+
+template <typename T>
+struct RestrictArgs {
+    const T *v, *r;          // fine level
+    const uint8_t *fl;       // fine flags
+    Coef<T> c;               // fine coefficients
+    Dims df, dc;
+    const T *w1, *w2;        // per coarse index along D
+    T *rc;                   // coarse rhs
+};
+
+template <typename T>
+struct ProlongArgs {
+    const T *phi;            // coarse correction
+    const uint8_t *flc;      // coarse flags (iblank bit)
+    T *v;                    // fine var
+    const uint8_t *flf;      // fine flags
+    Dims df, dc;
+    const int *cA, *cB;      // per fine index along D
+    const T *wA, *wB;
+    const int8_t *mode;      // 0 skip, 1 copy cA, 2 masked interpolation
+};
+
+struct GhostArgs {
+    int n;
+    const long long *gidx;   // ghost cell linear index (level-1 layout)
+    const long long *sidx;   // 8 stencil indices per ghost, -1 = the ghost itself (uNormal term)
+};
+
+// ---- launchers (all asynchronous on the given stream) ----
+template <typename T>
+void launch_line(int dir, const LineArgs<T> &a, bool omega_one, cudaStream_t s);
+void launch_factor(int dir, const FactorArgs<double> &a, cudaStream_t s);
+template <typename T>
+void launch_resid_restrict(int D, const RestrictArgs<T> &a, cudaStream_t s);
+template <typename T>
+void launch_prolong_correct(int D, const ProlongArgs<T> &a, cudaStream_t s);
+template <typename T>
+void launch_outer_ghost(T *v, const Dims &d, const int sign[6], cudaStream_t s);
+template <typename T>
+void launch_ghost_rows(T *v, const GhostArgs &g, const T *coeff, T *scratch, int iterMax, double tol,
+                       double reltol, int *d_iters, unsigned long long *d_maxdelta, cudaStream_t s);
+template <typename T>
+void launch_fill(T *p, long long n, T val, cudaStream_t s);
+
+// fine-level (level 1) reductions and updates, FP64
+struct MaxLoc { double v; long long i; };
+void launch_calc_residual(const double *p, const double *b, const double *nlw0, const uint8_t *fl,
+                          const Coef<double> &c, const Dims &d, float *r32_out, MaxLoc *partials,
+                          int nblocks, MaxLoc *result, cudaStream_t s);
+int calc_residual_blocks(const Dims &d);
+void launch_subtract_average(double *p, const uint8_t *fl, const double *dx, const double *dy,
+                             const double *dz, const Dims &d, double *partials, int nblocks,
+                             cudaStream_t s);
+void launch_compat(const double *p, const uint8_t *fl, const double *pg, const double *dx,
+                   const double *dy, const double *dz, const double *dxcinv, const double *dycinv,
+                   const double *dzcinv, const int side_flag[6], const Dims &d, double *partials,
+                   int nblocks, double *pgrad, const int bc_zero_grad[6], double outflow_area,
+                   int nx, int ny, int nz, cudaStream_t s);
+void launch_nlw0(double *nlw0, const uint8_t *fl, const int side_flag[6], const double *pgrad,
+                 const double *dxinv, const double *dyinv, const double *dzinv, const Dims &d,
+                 int nx, int ny, int nz, cudaStream_t s);
+void launch_accumulate(double *p, const float *e, long long n, cudaStream_t s);
+void launch_convert_f2d(double *dst, const float *src, long long n, cudaStream_t s);
+void launch_convert_d2f(float *dst, const double *src, long long n, cudaStream_t s);
+
+// hierarchy setup
+void launch_coarse_iblank(uint8_t *fl_c, const uint8_t *fl_f, const Dims &dc, const Dims &df, int D,
+                          cudaStream_t s);
+void launch_coarse_flags(uint8_t *fl, const Dims &d, const int side_bits[6], cudaStream_t s);
+
+} // namespace fsimg

@@ -1,0 +1,192 @@
+"""Host-side interface to the GPU pressure-Poisson multigrid.
+
+Mirrors the reference's operator interface for this path, one method per
+reference routine, with the same argument meaning and the same status codes:
+
+    MG_initial(...)            IBM/CORE_MG.F90:31          -> fsi_mg_create
+    set_boundary(geometry)     IBM/BOUNDARY_SET.F90:8      -> fsi_mg_set_geometry
+    solve_poisson(pPrime,nlu0) IBM/CORE_POISSON.F90:493    -> fsi_mg_solve / fsi_mg_solve_device
+    MG_Solver(var, rr)         IBM/CORE_MG.F90:281         -> fsi_mg_mg_solver
+    calc_residual(var, r)      IBM/CORE_POISSON.F90:1111   -> fsi_mg_calc_residual
+    subtracting_average_pressure(p)  IBM/CORE_POISSON.F90:419
+    GCM_correct_pressure(p)    IBM/CORE_POISSON.F90:1794
+
+Arrays are numpy arrays in Fortran order over the reference's full range
+(0:nx+1, 0:ny+1, 0:nz+1).  All compute runs in the CUDA library; there is no
+CPU fallback -- a missing library or device raises.
+"""
+from __future__ import annotations
+
+import ctypes
+from typing import Optional
+
+import numpy as np
+
+from . import _native
+from .params import FSI_MG_CONVERGED, SolverParams
+
+_dp = ctypes.POINTER(ctypes.c_double)
+_i8 = ctypes.POINTER(ctypes.c_int8)
+_i32 = ctypes.POINTER(ctypes.c_int32)
+
+
+class FsiMgError(RuntimeError):
+    pass
+
+
+def _p(a, t=_dp):
+    if a is None:
+        return None
+    if not a.flags["F_CONTIGUOUS"] and a.ndim > 1:
+        raise ValueError("arrays must be Fortran-contiguous")
+    return a.ctypes.data_as(t)
+
+
+def _check(rc: int):
+    if rc < 0:
+        raise FsiMgError(f"fsi_mg error {rc}: {_native.solver().fsi_mg_last_error().decode()}")
+    return rc
+
+
+class PoissonSolver:
+    """One GPU solver context (the reference's MG module state for one grid)."""
+
+    def __init__(self, params: SolverParams, x: np.ndarray, y: np.ndarray, z: np.ndarray):
+        self.params = params
+        self._cp = params.to_c()
+        self.lib = _native.solver()
+        h = ctypes.c_void_p()
+        self._x, self._y, self._z = (np.ascontiguousarray(a, dtype=np.float64) for a in (x, y, z))
+        _check(self.lib.fsi_mg_create(ctypes.byref(self._cp), _p(self._x), _p(self._y), _p(self._z), ctypes.byref(h)))
+        self.h = h
+        self.shape = (params.nx + 2, params.ny + 2, params.nz + 2)
+
+    # -- MG_initial ------------------------------------------------------
+    @classmethod
+    def MG_initial(cls, params, x, y, z):
+        return cls(params, x, y, z)
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.fsi_mg_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    # -- set_boundary ----------------------------------------------------
+    def set_boundary(self, geom):
+        g = geom
+        fl = [np.asfortranarray(a, dtype=np.int8) for a in g.flags]
+        self._keep = (np.asfortranarray(g.iblank, dtype=np.int8), np.asfortranarray(g.ghost, dtype=np.int8), fl)
+        ib, gm, fl = self._keep
+        n = int(g.nGhost)
+        arrs = [None] * 6
+        coeff = probe = None
+        if n > 0:
+            arrs = [np.ascontiguousarray(a, dtype=np.int32) for a in (g.iG, g.jG, g.kG, g.iCI, g.jCI, g.kCI)]
+            coeff = np.asfortranarray(g.coeff, dtype=np.float64)
+            probe = np.ascontiguousarray(g.probe, dtype=np.float64)
+        pg = None if g.pgrad is None else np.ascontiguousarray(g.pgrad, dtype=np.float64)
+        self._keep2 = (arrs, coeff, probe, pg)
+        _check(self.lib.fsi_mg_set_geometry(self.h, _p(ib, _i8), _p(gm, _i8), *[_p(a, _i8) for a in fl], n,
+                                            *[_p(a, _i32) for a in arrs], _p(coeff), _p(probe), _p(pg)))
+        return self
+
+    # -- solve_poisson ---------------------------------------------------
+    def solve_poisson(self, pPrime: np.ndarray, nlu0: np.ndarray, want_nlw0: bool = False):
+        """In-place solve on host arrays.  Returns (status, iters, maxres, loc, compTime[, nlw0])."""
+        assert pPrime.shape == self.shape and nlu0.shape == self.shape
+        nlw0 = np.zeros(self.shape, order="F") if want_nlw0 else None
+        it, mr, ct = ctypes.c_int(), ctypes.c_double(), ctypes.c_double()
+        loc = (ctypes.c_int * 3)()
+        st = _check(self.lib.fsi_mg_solve(self.h, _p(pPrime), _p(np.asfortranarray(nlu0)), _p(nlw0), ctypes.byref(it),
+                                          ctypes.byref(mr), loc, ctypes.byref(ct)))
+        out = (st, it.value, mr.value, tuple(loc), ct.value)
+        return out + ((nlw0,) if want_nlw0 else ())
+
+    def solve_poisson_device(self, d_pPrime: int, d_nlu0: int, d_nlw0: Optional[int] = None):
+        """Solve on device pointers (e.g. torch tensor .data_ptr()) of full-layout arrays."""
+        it, mr, ct = ctypes.c_int(), ctypes.c_double(), ctypes.c_double()
+        loc = (ctypes.c_int * 3)()
+        st = _check(self.lib.fsi_mg_solve_device(self.h, ctypes.c_void_p(d_pPrime), ctypes.c_void_p(d_nlu0),
+                                                 ctypes.c_void_p(d_nlw0) if d_nlw0 else None, ctypes.byref(it),
+                                                 ctypes.byref(mr), loc, ctypes.byref(ct)))
+        return st, it.value, mr.value, tuple(loc), ct.value
+
+    # -- finer hooks -----------------------------------------------------
+    def MG_Solver(self, var: np.ndarray, rr: np.ndarray) -> float:
+        ct = ctypes.c_double()
+        _check(self.lib.fsi_mg_mg_solver(self.h, _p(var), _p(np.asfortranarray(rr)), ctypes.byref(ct)))
+        return ct.value
+
+    def calc_residual(self, var, r):
+        m = ctypes.c_double()
+        loc = (ctypes.c_int * 3)()
+        _check(self.lib.fsi_mg_calc_residual(self.h, _p(np.asfortranarray(var)), _p(np.asfortranarray(r)),
+                                             ctypes.byref(m), loc))
+        return m.value, tuple(loc)
+
+    def subtracting_average_pressure(self, p):
+        _check(self.lib.fsi_mg_subtract_average(self.h, _p(p)))
+        return p
+
+    def GCM_correct_pressure(self, p, want_nlw0=False):
+        nlw0 = np.zeros(self.shape, order="F") if want_nlw0 else None
+        _check(self.lib.fsi_mg_correct_pressure(self.h, _p(p), _p(nlw0)))
+        return (p, nlw0) if want_nlw0 else p
+
+    def pgrad(self):
+        from .problem import pgrad_size
+        out = np.zeros(pgrad_size(self.params))
+        _check(self.lib.fsi_mg_get_pgrad(self.h, _p(out)))
+        return out
+
+    def level_count(self, d):
+        return _check(self.lib.fsi_mg_level_count(self.h, d))
+
+    def level_size(self, d, n):
+        return _check(self.lib.fsi_mg_level_size(self.h, d, n))
+
+    def level_shape(self, d, n):
+        p = self.params
+        sh = [p.nx + 1, p.ny + 1, p.nz + 1]
+        if n > 1:
+            sh[d] = self.level_size(d, n) + 2
+        return tuple(sh)
+
+    def debug_op(self, op, d, n, a=None, b=None, c=None):
+        def vp(x):
+            return None if x is None else ctypes.c_void_p(x.ctypes.data)
+        return _check(self.lib.fsi_mg_debug_level_op(self.h, op, d, n, vp(a), vp(b), vp(c)))
+
+    def stats(self):
+        out = np.zeros(8)
+        _check(self.lib.fsi_mg_stats(self.h, _p(out), 8))
+        return dict(iters=int(out[0]), maxres=out[1], seconds=out[2], ghost_sweeps=int(out[3]),
+                    launches=int(out[4]), device_bytes=int(out[5]), wall_seconds=out[6], e2e_seconds=out[7])
+
+    def time_kernel(self, which: int, precision: int, reps: int = 20):
+        """Average device time (ms) of one kernel and its algorithmic bytes per launch."""
+        ms, nb = ctypes.c_double(), ctypes.c_double()
+        _check(self.lib.fsi_mg_time_kernel(self.h, which, precision, reps, ctypes.byref(ms), ctypes.byref(nb)))
+        return ms.value, nb.value
+
+
+def solve(problem, p0=None, **overrides):
+    """Convenience: build a solver for ``problem``, solve from ``p0`` (zeros)."""
+    params = problem.params
+    for k, v in overrides.items():
+        setattr(params, k, v)
+    s = PoissonSolver(params, problem.x, problem.y, problem.z).set_boundary(problem.geom)
+    p = np.zeros(problem.shape, order="F") if p0 is None else np.array(p0, order="F", copy=True)
+    st, it, mr, loc, ct, nlw0 = s.solve_poisson(p, problem.nlu0, want_nlw0=True)
+    res = dict(p=p, status=st, iters=it, maxres=mr, loc=loc, seconds=ct, nlw0=nlw0, stats=s.stats())
+    s.close()
+    return res
+
+
+__all__ = ["PoissonSolver", "FsiMgError", "solve", "FSI_MG_CONVERGED"]

@@ -1,0 +1,152 @@
+/*
+ * fsi_mg.h -- C ABI of the GB300 (sm_103a) pressure-Poisson multigrid solver.
+ *
+ * Drop-in boundary for the fractional-step pressure solve of the reference
+ * immersed-boundary FSI code.  Each entry point replaces one reference
+ * routine and keeps its argument meaning; a Fortran host binds them through
+ * ISO_C_BINDING interfaces.
+ *
+ * Array conventions are the reference's: Fortran column-major, lower bound 0.
+ * A full field is REAL(8) (0:nx+1,0:ny+1,0:nz+1); flags are INTEGER(1) over
+ * the same range; node arrays are (0:n+1).  Pointers are host pointers unless
+ * the entry point says otherwise.  One host thread per handle; a handle owns
+ * one CUDA stream and all device memory of its hierarchy.
+ *
+ * Status codes (all entry points):
+ *    0  success / converged
+ *    1  iterMax_Poisson reached with maxres > restol_Poisson (the reference
+ *       prints its non-convergence message and continues,
+ *       IBM/CORE_POISSON.F90:665-669)
+ *    2  the ghost-cell rows did not converge within iterMax_ad
+ *       (IBM/GCM_GHOSTCELL_VEL_UPDATE_UNSTRUC.F90:374-378)
+ *   <0  argument, configuration or CUDA error; fsi_mg_last_error() describes it.
+ */
+#ifndef FSI_MG_H
+#define FSI_MG_H
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Hot-path input flags (IBM/MAIN.F90 read_inputs :415-489).  Field order is
+ * part of the ABI. */
+typedef struct {
+    int ndim;                 /* 2 or 3 (DIM_2D / DIM_3D) */
+    int nx, ny, nz;           /* node counts; cells are n-1; nz = 2 in 2D */
+    int pp_solver_type;       /* must be 3 (PP_SOLVER_TYPE_MG) */
+    int iRedBlack;            /* ignored: the GPU smoother is red-black over all lines */
+    int mgcycle[3];           /* mgCycleX/Y/Z: 1 V, 2 W, 3 F */
+    int iterFinest, iterCoarsest;
+    int mgLevels[3];          /* 0 = automatic (IBM/CORE_MG.F90:48-78) */
+    int iterMax_Poisson, iterMax_ad;
+    int bc[6];                /* velocity BC types bcx1,bcx2,bcy1,bcy2,bcz1,bcz2 */
+    int pbc[6];               /* pressure BC types pbcx1..pbcz2 (1 Dirichlet, 2 Neumann) */
+    int internal_boundary_present;
+    int boundary_formulation; /* 0 none, 2 GCM_METHOD */
+    int coarse_flag_mode;     /* ignored by the GPU (coarse face flags always follow the coarse iblank) */
+    int precision_mode;       /* 0 FP64 throughout, 1 FP32 cycle inside FP64 refinement */
+    double omega;             /* line-SOR relaxation */
+    double restol_Poisson;    /* absolute max-norm tolerance */
+    double restol_ad;         /* ghost-row fixed-point tolerance */
+    double ppp[6];            /* Dirichlet pressure values pppx1..pppz2 */
+    double outflow_area;      /* from set_outflow_area (IBM/BOUNDARY_SET.F90:134-221) */
+} fsi_mg_params;
+
+/* MG_initial (IBM/CORE_MG.F90:31): level counts and sizes, coarse metrics,
+ * device buffers.  x, y, z are the node arrays (0:n+1) produced by make_grid
+ * (IBM/CORE_GRID.F90:29). */
+int fsi_mg_create(const fsi_mg_params *params, const double *x, const double *y, const double *z,
+                  void **handle);
+
+/* Hand over the outputs of set_boundary (IBM/BOUNDARY_SET.F90:8) after every
+ * geometry change: iblank, ghostCellMark and ium..kup (INTEGER(1), full
+ * range), the ordered ghost list iGhost/jGhost/kGhost with the image-point
+ * stencil base iCellIndex/jCellIndex/kCellIndex and coeffGCMN(8,nGhost),
+ * probeLength(nGhost) (IBM/GCM_SET_BOUNDARY.F90:2-304), and the six boundary
+ * pressure-gradient planes pgradx1,pgradx2 (0:ny+1,0:nz+1), pgrady1,pgrady2
+ * (0:nx+1,0:nz+1), pgradz1,pgradz2 (0:nx+1,0:ny+1) packed in that order
+ * (may be NULL: all zero).  Builds the coarse iblank hierarchy, face flags,
+ * line factorisations and the ghost gather list on the device. */
+int fsi_mg_set_geometry(void *handle, const int8_t *iblank, const int8_t *ghostCellMark,
+                        const int8_t *ium, const int8_t *iup, const int8_t *jum, const int8_t *jup,
+                        const int8_t *kum, const int8_t *kup,
+                        int nGhost, const int32_t *iGhost, const int32_t *jGhost, const int32_t *kGhost,
+                        const int32_t *iCellIndex, const int32_t *jCellIndex, const int32_t *kCellIndex,
+                        const double *coeffGCMN, const double *probeLength, const double *pgrad);
+
+/* solve_poisson, MG branch (IBM/CORE_POISSON.F90:493-676): mean removal (or
+ * Dirichlet flagging), then MG_Solver -> GCM_correct_pressure -> calc_residual
+ * until maxres <= restol_Poisson or iterMax_Poisson.  pPrime is INOUT, nlu0 IN,
+ * nlw0_out OUT (may be NULL); iters, maxres, loc[3] (first location of the max
+ * residual) and compTime (seconds) are OUT (each may be NULL).
+ * Host buffers: each call copies pPrime and nlu0 in and pPrime out. */
+int fsi_mg_solve(void *handle, double *pPrime, const double *nlu0, double *nlw0_out,
+                 int *iters, double *maxres, int *loc, double *compTime);
+
+/* Same as fsi_mg_solve with DEVICE pointers to full (0:nx+1)^3 arrays already
+ * resident in HBM (no host transfer of the fields). */
+int fsi_mg_solve_device(void *handle, double *d_pPrime, const double *d_nlu0, double *d_nlw0_out,
+                        int *iters, double *maxres, int *loc, double *compTime);
+
+/* MG_Solver (IBM/CORE_MG.F90:281): one x-, y- (and z-) semi-coarsening cycle
+ * on var (INOUT) with right-hand side rr (IN); compTime OUT.  The smoother and
+ * residual procedure arguments of the reference are fixed here. */
+int fsi_mg_mg_solver(void *handle, double *var, const double *rr, double *compTime);
+
+/* calc_residual (IBM/CORE_POISSON.F90:1111): max-norm of r - A var + nlw0
+ * over fluid cells and the first location (i,j,k) attaining it. */
+int fsi_mg_calc_residual(void *handle, const double *var, const double *r, double *resm, int *loc);
+
+/* subtracting_average_pressure (IBM/CORE_POISSON.F90:419), stationary bodies. */
+int fsi_mg_subtract_average(void *handle, double *pPrime);
+
+/* GCM_correct_pressure (IBM/CORE_POISSON.F90:1794): outer ghost layer,
+ * ghost-cell rows, compatibility correction of pgrad*, and nlw0 (OUT, may be NULL). */
+int fsi_mg_correct_pressure(void *handle, double *pPrime, double *nlw0_out);
+
+/* Current boundary pressure-gradient planes (packed as in set_geometry). */
+int fsi_mg_get_pgrad(void *handle, double *pgrad);
+
+/* Hierarchy introspection: level count of direction d (0 x, 1 y, 2 z) and the
+ * cell count of level n (1-based) along d (mgLevels_X, mgrid_I(n), ...). */
+int fsi_mg_level_count(void *handle, int d);
+int fsi_mg_level_size(void *handle, int d, int n);
+
+/* Single-operator access for parity checks, host buffers in the reference's
+ * level layout (0:m+1 along d at coarse levels, 0:n elsewhere):
+ *   op 0 MG_itsolv at level n of cycle d (a = var INOUT, b = rhs IN)
+ *   op 1 MG_Residual followed by MG_Restrict (a = var, b = rhs, c = coarse OUT)
+ *   op 2 MG_Prolong followed by the correction var += phi (1-iblank)
+ *        (a = coarse phi IN, b = fine var INOUT)
+ *   op 3 coarse iblank of level n (a = int8 OUT)
+ *   op 4 face flags of level n (a = int8 OUT, 6 full arrays ium..kup)
+ *   op 5 ghost-cell rows on a level-1 array (a = var INOUT, b = int OUT iterations)
+ *   op 6 outer ghost layer on a level-1 array (a = var INOUT) */
+int fsi_mg_debug_level_op(void *handle, int op, int d, int n, void *a, void *b, void *c);
+
+/* Counters of the last solve: out[0] iterations, out[1] final maxres,
+ * out[2] solve seconds (CUDA events on the handle's stream), out[3] total
+ * ghost-row sweeps, out[4] kernel launches since create, out[5] device bytes
+ * allocated, out[6] solve wall seconds, out[7] device seconds of the last
+ * host-buffer solve including its host<->device copies. */
+int fsi_mg_stats(void *handle, double *out, int n);
+
+/* Time one kernel of the level-1 hierarchy on the handle's stream with CUDA
+ * events, averaged over reps launches (after one warm-up launch), on the
+ * current staging fields.  which: 0/1/2 one colour of the x/y/z line sweep,
+ * 3 residual + x restriction, 4 x prolongation + correction, 5 calc_residual.
+ * precision 0 FP64, 1 FP32.  alg_bytes (may be NULL) receives the algorithmic
+ * bytes one launch moves.  No counterpart in the reference: a measurement hook. */
+int fsi_mg_time_kernel(void *handle, int which, int precision, int reps, double *avg_ms, double *alg_bytes);
+
+/* Text of the last error on this thread. */
+const char *fsi_mg_last_error(void);
+
+/* deallocate_memory (IBM/CORE_MEMORY_ALLOCATE.F90:189) for this handle. */
+void fsi_mg_destroy(void *handle);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* FSI_MG_H */

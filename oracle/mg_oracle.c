@@ -1,0 +1,1155 @@
+/*
+ * Oracle (TEST INFRASTRUCTURE ONLY) -- CPU FP64 restatement of the reference
+ * pressure-Poisson multigrid path.  See mg_oracle.h for the scope, the array
+ * conventions and the parity pin.  Every routine cites the reference routine
+ * (file:line) whose steps it restates; loop orders and floating-point
+ * evaluation orders follow the reference so that a sweep here and a sweep
+ * there produce the same bits.  Compile with -ffp-contract=off so that the
+ * results are the same on x86-64 and aarch64 hosts.
+ *
+ * Documented choices where the reference is undefined or out of scope:
+ *  - Periodic velocity BCs are rejected: the reference's MG reads
+ *    var(nxc,...) on coarse arrays (IBM/CORE_MG.F90:1958-1961), out of bounds.
+ *  - Coarse z-level ghost metrics (zc_MG(0,n), zc_MG(m+1,n), dz_MG(0,n),
+ *    dz_MG(m+1,n)) are left uninitialised by the reference
+ *    (IBM/CORE_MG.F90:254-266); they are computed here the same way as the
+ *    x and y levels (:186-205).  They only enter through a Dirichlet
+ *    pressure BC on a z face.
+ *  - fresh_cell is 0 (stationary bodies); pot_flag is 0 (viscous flow).
+ *  - nlw (the MG extra term, IBM/CORE_MG.F90:1968) is 0, as in a standalone
+ *    solve (IBM/MAIN.F90:2266).
+ */
+#include "mg_oracle.h"
+#include <math.h>
+#include <stdio.h>
+#include <stdlib.h>
+#include <string.h>
+
+enum { BC_DIRICHLET = 1, BC_ZERO_GRADIENT = 2, BC_PERIODIC = 5 };
+enum { PBC_DIRICHLET = 1, PBC_NEUMANN = 2 };
+enum { GCM_METHOD = 2, DIM_2D = 2, DIM_3D = 3 };
+
+typedef struct { int8_t *a; int sx, sy; } i8v;
+
+struct or_ctx {
+    fsi_mg_params p;
+    int nx, ny, nz, nxc, nyc, nzc;
+    int n[3], nc[3];
+    /* fine grid, (0:n+1) */
+    double *x[3], *xc[3], *dx[3], *dxinv[3], *dxc[3], *dxcinv[3];
+    /* MG grid per level: a[i + (n+2)*(lev-1)] */
+    int nlev[3];
+    int *mgrid[3];
+    double *x_MG[3], *xc_MG[3], *dx_MG[3], *dxinv_MG[3], *dxc_MG[3], *dxcinv_MG[3];
+    /* fine flags (0:nx+1)^3 */
+    int8_t *iblank, *ghost, *fl[6];
+    int8_t *flMG[6];
+    int *ghostMG;
+    int8_t **cib[3];    /* coarse iblank per direction, index n-1 (n>=2) */
+    double *nlw, *nlw0;
+    double *pgrad[6];
+    int pg_sx[6];
+    int nGhost;
+    int32_t *gi[6];
+    double *coeff, *probe;
+    double *pPrime_mod;
+    i8v ibMG;
+    int gs_last_iters;
+    int ghost_nonconv;
+    int geometry_set;
+};
+
+static const int incI[8] = {0, 0, 1, 1, 0, 0, 1, 1};   /* IBM/GCM_MEMORY_ALLOCATE.F90:494-518 */
+static const int incJ[8] = {0, 1, 1, 0, 0, 1, 1, 0};
+static const int incK[8] = {0, 0, 0, 0, 1, 1, 1, 1};
+
+#define FI(c, i, j, k) ((size_t)(i) + (size_t)((c)->nx + 2) * ((size_t)(j) + (size_t)((c)->ny + 2) * (size_t)(k)))
+#define VI(sx, sy, i, j, k) ((size_t)(i) + (size_t)(sx) * ((size_t)(j) + (size_t)(sy) * (size_t)(k)))
+#define IBV(v, i, j, k) ((v).a[VI((v).sx, (v).sy, i, j, k)])
+#define MG1(c, d, arr, i, lev) ((c)->arr[d][(size_t)(i) + (size_t)((c)->n[d] + 2) * (size_t)((lev) - 1)])
+
+static void *zalloc(size_t n) { return calloc(n ? n : 1, 1); }
+static inline double sq_inv(double t) { return 1.0 / (t * t); }
+
+/* ---------------------------------------------------------------- tdma ---- */
+/* IBM/CORE_TDMA.F90:10-34: Thomas algorithm, no pivoting; a(n1), c(n2) unused.
+ * gam is caller-provided work space of length n2+1 (the reference's automatic array). */
+static void tdma_w(const double *a, const double *b, const double *c_, const double *r,
+                   double *u, double *gam, int n1, int n2)
+{
+    double binv = 1.0 / b[n1];
+    u[n1] = r[n1] * binv;
+    for (int j = n1 + 1; j <= n2; ++j) {
+        gam[j] = c_[j - 1] * binv;
+        binv = 1.0 / (b[j] - a[j] * gam[j]);
+        u[j] = (r[j] - a[j] * u[j - 1]) * binv;
+    }
+    for (int j = n2 - 1; j >= n1; --j) u[j] = u[j] - gam[j + 1] * u[j + 1];
+}
+
+void or_tdma(const double *a, const double *b, const double *c_, const double *r,
+             double *u, int n1, int n2)
+{
+    double *gam = (double *)zalloc(sizeof(double) * (size_t)(n2 + 1));
+    tdma_w(a, b, c_, r, u, gam, n1, n2);
+    free(gam);
+}
+
+/* ------------------------------------------------------------ MG_initial -- */
+/* IBM/CORE_MG.F90:31-278 */
+static int auto_levels(int cells)
+{
+    const int nCoarseGrids = 4, MG_LEVEL_MAX = 10;
+    int ii = cells, nLevel;
+    for (nLevel = 1; nLevel <= MG_LEVEL_MAX; ++nLevel) {
+        ii = ii / 2;
+        if (ii >= nCoarseGrids) continue;
+        break;
+    }
+    if (nLevel > MG_LEVEL_MAX) nLevel = MG_LEVEL_MAX; /* Fortran DO exit value is MAX+1; never reached for <=1M cells */
+    return nLevel;
+}
+
+static void mg_initial(or_ctx *c)
+{
+    for (int d = 0; d < 3; ++d) {
+        int N = c->n[d];
+        int cells = (d == 2) ? (c->nz - 1) : c->nc[d];
+        int nl = c->p.mgLevels[d];
+        if (nl == 0) nl = auto_levels(cells);
+        if (d == 2 && c->p.ndim == DIM_2D) nl = (c->p.mgLevels[2] == 0) ? auto_levels(c->nz - 1) : c->p.mgLevels[2];
+        c->nlev[d] = nl;
+        c->mgrid[d] = (int *)zalloc(sizeof(int) * (size_t)(nl + 2));
+        c->mgrid[d][1] = c->nc[d];
+        for (int l = 2; l <= nl; ++l) {
+            int m = c->mgrid[d][l - 1];
+            c->mgrid[d][l] = (m % 2 == 0) ? m / 2 : (m - 1) / 2;
+        }
+        size_t sz = sizeof(double) * (size_t)(N + 2) * (size_t)nl;
+        c->x_MG[d] = zalloc(sz); c->xc_MG[d] = zalloc(sz); c->dx_MG[d] = zalloc(sz);
+        c->dxinv_MG[d] = zalloc(sz); c->dxc_MG[d] = zalloc(sz); c->dxcinv_MG[d] = zalloc(sz);
+        for (int i = 0; i <= N; ++i) {           /* :148-176 */
+            MG1(c, d, dxc_MG, i, 1) = c->dxc[d][i];
+            MG1(c, d, dx_MG, i, 1) = c->dx[d][i];
+            MG1(c, d, dxcinv_MG, i, 1) = c->dxcinv[d][i];
+            MG1(c, d, dxinv_MG, i, 1) = c->dxinv[d][i];
+            MG1(c, d, xc_MG, i, 1) = c->xc[d][i];
+        }
+        for (int i = 0; i <= N + 1; ++i) MG1(c, d, x_MG, i, 1) = c->x[d][i]; /* :178-188 */
+        if (d == 2 && c->p.ndim != DIM_3D) continue;
+        for (int l = 2; l <= nl; ++l) {          /* :190-205 (x), :212-231 (y), :234-266 (z) */
+            int m = c->mgrid[d][l];
+            for (int i = 1; i <= m + 1; ++i) MG1(c, d, x_MG, i, l) = MG1(c, d, x_MG, 2 * i - 1, l - 1);
+            MG1(c, d, x_MG, 0, l) = -MG1(c, d, x_MG, 2, l);
+            MG1(c, d, x_MG, m + 2, l) = 2.0 * MG1(c, d, x_MG, m + 1, l) - MG1(c, d, x_MG, m, l);
+            for (int i = 0; i <= m + 1; ++i) {
+                MG1(c, d, dx_MG, i, l) = MG1(c, d, x_MG, i + 1, l) - MG1(c, d, x_MG, i, l);
+                MG1(c, d, dxinv_MG, i, l) = 1.0 / MG1(c, d, dx_MG, i, l);
+            }
+            for (int i = 0; i <= m + 1; ++i)
+                MG1(c, d, xc_MG, i, l) = 0.5 * (MG1(c, d, x_MG, i, l) + MG1(c, d, x_MG, i + 1, l));
+            for (int i = 1; i <= m + 1; ++i) {
+                MG1(c, d, dxc_MG, i, l) = MG1(c, d, xc_MG, i, l) - MG1(c, d, xc_MG, i - 1, l);
+                MG1(c, d, dxcinv_MG, i, l) = 1.0 / MG1(c, d, dxc_MG, i, l);
+            }
+        }
+    }
+}
+
+/* ------------------------------------------------------------ create ------ */
+or_ctx *or_create(const fsi_mg_params *p, const double *x, const double *y, const double *z)
+{
+    if (!p || !x || !y || !z) return NULL;
+    if (p->ndim != DIM_2D && p->ndim != DIM_3D) return NULL;
+    if (p->nx < 3 || p->ny < 3 || p->nz < 2) return NULL;
+    if (p->ndim == DIM_2D && p->nz != 2) return NULL;
+    for (int s = 0; s < 6; ++s) if (p->bc[s] == BC_PERIODIC) return NULL;
+    or_ctx *c = (or_ctx *)zalloc(sizeof(or_ctx));
+    c->p = *p;
+    c->nx = p->nx; c->ny = p->ny; c->nz = p->nz;
+    c->nxc = p->nx - 1; c->nyc = p->ny - 1; c->nzc = p->nz - 1;
+    c->n[0] = c->nx; c->n[1] = c->ny; c->n[2] = c->nz;
+    c->nc[0] = c->nxc; c->nc[1] = c->nyc; c->nc[2] = c->nzc;
+    const double *xs[3] = {x, y, z};
+    /* IBM/CORE_GRID.F90:96-139 (metrics of the given nodes x(0:n+1)) */
+    for (int d = 0; d < 3; ++d) {
+        int N = c->n[d];
+        size_t sz = sizeof(double) * (size_t)(N + 2);
+        c->x[d] = zalloc(sz); c->xc[d] = zalloc(sz); c->dx[d] = zalloc(sz);
+        c->dxinv[d] = zalloc(sz); c->dxc[d] = zalloc(sz); c->dxcinv[d] = zalloc(sz);
+        memcpy(c->x[d], xs[d], sz);
+        for (int i = 0; i <= N; ++i) {
+            c->xc[d][i] = 0.5 * (c->x[d][i + 1] + c->x[d][i]);
+            c->dx[d][i] = c->x[d][i + 1] - c->x[d][i];
+            c->dxinv[d][i] = 1.0 / c->dx[d][i];
+        }
+        c->xc[d][N + 1] = c->x[d][N + 1];
+        for (int i = 1; i <= N; ++i) {
+            c->dxc[d][i] = c->xc[d][i] - c->xc[d][i - 1];
+            c->dxcinv[d][i] = 1.0 / c->dxc[d][i];
+        }
+    }
+    mg_initial(c);
+    size_t nf = (size_t)(c->nx + 2) * (size_t)(c->ny + 2) * (size_t)(c->nz + 2);
+    c->iblank = zalloc(nf); c->ghost = zalloc(nf);
+    for (int s = 0; s < 6; ++s) { c->fl[s] = zalloc(nf); c->flMG[s] = zalloc(nf); }
+    c->ghostMG = zalloc(nf * sizeof(int));
+    c->nlw = zalloc(nf * sizeof(double));
+    c->nlw0 = zalloc(nf * sizeof(double));
+    int pgs[6][2] = {{c->ny + 2, c->nz + 2}, {c->ny + 2, c->nz + 2}, {c->nx + 2, c->nz + 2},
+                     {c->nx + 2, c->nz + 2}, {c->nx + 2, c->ny + 2}, {c->nx + 2, c->ny + 2}};
+    for (int s = 0; s < 6; ++s) {
+        c->pg_sx[s] = pgs[s][0];
+        c->pgrad[s] = zalloc(sizeof(double) * (size_t)pgs[s][0] * (size_t)pgs[s][1]);
+    }
+    for (int d = 0; d < 3; ++d) {
+        c->cib[d] = (int8_t **)zalloc(sizeof(int8_t *) * (size_t)(c->nlev[d] + 1));
+        for (int l = 2; l <= c->nlev[d]; ++l) {
+            size_t e[3] = {(size_t)c->nx + 1, (size_t)c->ny + 1, (size_t)c->nz + 1};
+            e[d] = (size_t)c->mgrid[d][l] + 2;
+            c->cib[d][l] = zalloc(e[0] * e[1] * e[2]);
+        }
+    }
+    /* default flags: set_outer_iup (IBM/BOUNDARY_SET.F90:54-80) */
+    for (int j = 1; j <= c->ny; ++j) for (int k = 1; k <= c->nz; ++k) {
+        c->fl[0][FI(c, 1, j, k)] = 1; c->fl[1][FI(c, c->nxc, j, k)] = 1; }
+    for (int i = 1; i <= c->nx; ++i) for (int k = 1; k <= c->nz; ++k) {
+        c->fl[2][FI(c, i, 1, k)] = 1; c->fl[3][FI(c, i, c->nyc, k)] = 1; }
+    if (c->p.ndim == DIM_3D)
+        for (int i = 1; i <= c->nx; ++i) for (int j = 1; j <= c->ny; ++j) {
+            c->fl[4][FI(c, i, j, 1)] = 1; c->fl[5][FI(c, i, j, c->nzc)] = 1; }
+    return c;
+}
+
+void or_destroy(or_ctx *c)
+{
+    if (!c) return;
+    for (int d = 0; d < 3; ++d) {
+        free(c->x[d]); free(c->xc[d]); free(c->dx[d]); free(c->dxinv[d]); free(c->dxc[d]); free(c->dxcinv[d]);
+        free(c->x_MG[d]); free(c->xc_MG[d]); free(c->dx_MG[d]); free(c->dxinv_MG[d]);
+        free(c->dxc_MG[d]); free(c->dxcinv_MG[d]); free(c->mgrid[d]);
+        if (c->cib[d]) for (int l = 2; l <= c->nlev[d]; ++l) free(c->cib[d][l]);
+        free(c->cib[d]);
+    }
+    free(c->iblank); free(c->ghost); free(c->ghostMG); free(c->nlw); free(c->nlw0);
+    for (int s = 0; s < 6; ++s) { free(c->fl[s]); free(c->flMG[s]); free(c->pgrad[s]); free(c->gi[s]); }
+    free(c->coeff); free(c->probe);
+    free(c);
+}
+
+int or_set_geometry(or_ctx *c, const int8_t *iblank, const int8_t *ghost,
+                    const int8_t *ium, const int8_t *iup, const int8_t *jum,
+                    const int8_t *jup, const int8_t *kum, const int8_t *kup,
+                    int nGhost, const int32_t *iG, const int32_t *jG, const int32_t *kG,
+                    const int32_t *iCI, const int32_t *jCI, const int32_t *kCI,
+                    const double *coeffGCMN, const double *probeLength, const double *pgrad)
+{
+    size_t nf = (size_t)(c->nx + 2) * (size_t)(c->ny + 2) * (size_t)(c->nz + 2);
+    if (iblank) memcpy(c->iblank, iblank, nf);
+    if (ghost) memcpy(c->ghost, ghost, nf);
+    const int8_t *f[6] = {ium, iup, jum, jup, kum, kup};
+    for (int s = 0; s < 6; ++s) if (f[s]) memcpy(c->fl[s], f[s], nf);
+    for (int s = 0; s < 6; ++s) { free(c->gi[s]); c->gi[s] = NULL; }
+    free(c->coeff); free(c->probe); c->coeff = c->probe = NULL;
+    c->nGhost = nGhost;
+    if (nGhost > 0) {
+        const int32_t *g[6] = {iG, jG, kG, iCI, jCI, kCI};
+        for (int s = 0; s < 6; ++s) {
+            c->gi[s] = zalloc(sizeof(int32_t) * (size_t)nGhost);
+            memcpy(c->gi[s], g[s], sizeof(int32_t) * (size_t)nGhost);
+        }
+        c->coeff = zalloc(sizeof(double) * 8 * (size_t)nGhost);
+        memcpy(c->coeff, coeffGCMN, sizeof(double) * 8 * (size_t)nGhost);
+        c->probe = zalloc(sizeof(double) * (size_t)nGhost);
+        memcpy(c->probe, probeLength, sizeof(double) * (size_t)nGhost);
+        for (int n = 0; n < nGhost; ++n)
+            for (int r = 0; r < 8; ++r) {
+                int ii = iCI[n] + incI[r], jj = jCI[n] + incJ[r], kk = kCI[n] + incK[r];
+                if (ii < 0 || ii > c->nx || jj < 0 || jj > c->ny || kk < 0 || kk > c->nz) return -3;
+            }
+    }
+    if (pgrad) {
+        size_t off = 0;
+        for (int s = 0; s < 6; ++s) {
+            int sy = (s < 2) ? c->nz + 2 : (s < 4 ? c->nz + 2 : c->ny + 2);
+            size_t cnt = (size_t)c->pg_sx[s] * (size_t)sy;
+            memcpy(c->pgrad[s], pgrad + off, sizeof(double) * cnt);
+            off += cnt;
+        }
+    }
+    c->geometry_set = 1;
+    return 0;
+}
+
+void or_get_pgrad(or_ctx *c, double *pgrad)
+{
+    size_t off = 0;
+    for (int s = 0; s < 6; ++s) {
+        int sy = (s < 4) ? c->nz + 2 : c->ny + 2;
+        size_t cnt = (size_t)c->pg_sx[s] * (size_t)sy;
+        memcpy(pgrad + off, c->pgrad[s], sizeof(double) * cnt);
+        off += cnt;
+    }
+}
+
+/* ------------------------------------------------ outer ghost / ghost rows */
+/* IBM/CORE_SET_OUTER_GHOST.F90:66-213; pres is (0:mx,0:my,0:mz), loops use nx,ny,nz. */
+static void set_outer_ghost_pres(or_ctx *c, double *pres, int mx, int my)
+{
+    int nx = c->nx, ny = c->ny, nz = c->nz;
+    int sx = mx + 1, sy = my + 1;
+#define P(i, j, k) pres[VI(sx, sy, i, j, k)]
+    const int *pbc = c->p.pbc;
+    for (int k = 0; k <= nz; ++k) for (int j = 0; j <= ny; ++j)
+        P(0, j, k) = (pbc[0] == PBC_NEUMANN) ? P(1, j, k) : -P(1, j, k);
+    for (int k = 0; k <= nz; ++k) for (int j = 0; j <= ny; ++j)
+        P(nx, j, k) = (pbc[1] == PBC_NEUMANN) ? P(nx - 1, j, k) : -P(nx - 1, j, k);
+    for (int k = 0; k <= nz; ++k) for (int i = 0; i <= nx; ++i)
+        P(i, 0, k) = (pbc[2] == PBC_NEUMANN) ? P(i, 1, k) : -P(i, 1, k);
+    for (int k = 0; k <= nz; ++k) for (int i = 0; i <= nx; ++i)
+        P(i, ny, k) = (pbc[3] == PBC_NEUMANN) ? P(i, ny - 1, k) : -P(i, ny - 1, k);
+    if (c->p.ndim == DIM_3D)
+        for (int j = 0; j <= ny; ++j) for (int i = 0; i <= nx; ++i) {
+            P(i, j, 0) = P(i, j, 1);
+            P(i, j, nz) = P(i, j, nz - 1);
+        }
+    for (int j = 0; j <= ny; ++j) for (int i = 0; i <= nx; ++i)
+        P(i, j, 0) = (pbc[4] == PBC_NEUMANN) ? P(i, j, 1) : -P(i, j, 1);
+    for (int j = 0; j <= ny; ++j) for (int i = 0; i <= nx; ++i)
+        P(i, j, nz) = (pbc[5] == PBC_NEUMANN) ? P(i, j, nz - 1) : -P(i, j, nz - 1);
+#undef P
+}
+
+/* IBM/GCM_GHOSTCELL_VEL_UPDATE_UNSTRUC.F90:250-384 (viscous: uNormal = 0).
+ * Gauss-Seidel over the ordered ghost list until max|dp| <= restol_ad. */
+static void gcm_p_set_bc_internal(or_ctx *c, double *pres, int mx, int my)
+{
+    int sx = mx + 1, sy = my + 1;
+    int iterGC = 0;
+    double resPresMax = 1.0e10;
+    const double uNormal = 0.0;
+    while (iterGC < c->p.iterMax_ad && resPresMax > c->p.restol_ad) {
+        resPresMax = 0.0;
+        for (int n = 0; n < c->nGhost; ++n) {
+            int iG = c->gi[0][n], jG = c->gi[1][n], kG = c->gi[2][n];
+            double pIP = 0.0;
+            for (int r = 0; r < 8; ++r) {
+                int ii = c->gi[3][n] + incI[r], jj = c->gi[4][n] + incJ[r], kk = c->gi[5][n] + incK[r];
+                if (ii == iG && jj == jG && kk == kG) pIP = pIP + c->coeff[8 * (size_t)n + r] * uNormal;
+                else pIP = pIP + c->coeff[8 * (size_t)n + r] * pres[VI(sx, sy, ii, jj, kk)];
+            }
+            size_t g = VI(sx, sy, iG, jG, kG);
+            double pPrev = pres[g];
+            pres[g] = pIP + c->probe[n] * uNormal;
+            double resPres = fabs(pres[g] - pPrev);
+            if (resPres > resPresMax) resPresMax = resPres;
+        }
+        iterGC = iterGC + 1;
+    }
+    c->gs_last_iters = iterGC;
+    if (iterGC == c->p.iterMax_ad && resPresMax > c->p.restol_ad) c->ghost_nonconv = 1;
+}
+
+void or_ghost_update(or_ctx *c, double *var, int mx, int my, int mz, int *iters, double *resmax)
+{
+    (void)mz;
+    c->ghost_nonconv = 0;
+    gcm_p_set_bc_internal(c, var, mx, my);
+    if (iters) *iters = c->gs_last_iters;
+    if (resmax) *resmax = (double)c->ghost_nonconv;
+}
+
+int or_nghost_gs_last(or_ctx *c) { return c->gs_last_iters; }
+
+/* set_outer_ghost_pres on an MG-layout (0:nx,0:ny,0:nz) array. */
+void or_outer_ghost(or_ctx *c, double *var) { set_outer_ghost_pres(c, var, c->nx, c->ny); }
+
+/* IBM/GCM_GLOBAL_MASS_CONSERVE.F90:260-394 (non-periodic branch). */
+static void gcm_enforce_p_compatibility(or_ctx *c, const double *pres, int mx, int my)
+{
+    const int *bc = c->p.bc;
+    int active = 0;
+    for (int s = 0; s < 6; ++s) if (bc[s] == BC_ZERO_GRADIENT) active = 1;
+    if (!active) return;
+    int sx = mx + 1, sy = my + 1;
+#define P(i, j, k) pres[VI(sx, sy, i, j, k)]
+#define PG(s, a, b) c->pgrad[s][(size_t)(a) + (size_t)c->pg_sx[s] * (size_t)(b)]
+    double pgradflux = 0.0;
+    double *dxcinv = c->dxcinv[0], *dycinv = c->dxcinv[1], *dzcinv = c->dxcinv[2];
+    double *dx = c->dx[0], *dy = c->dx[1], *dz = c->dx[2];
+    for (int k = 1; k <= c->nz - 1; ++k)
+        for (int j = 1; j <= c->ny - 1; ++j)
+            for (int i = 1; i <= c->nx - 1; ++i) {
+                size_t f = FI(c, i, j, k);
+                int ium = c->fl[0][f], iup = c->fl[1][f], jum = c->fl[2][f];
+                int jup = c->fl[3][f], kum = c->fl[4][f], kup = c->fl[5][f];
+                double pgxw = PG(0, j, k) * ium + ((double)(1 - ium) * (P(i, j, k) - P(i - 1, j, k))) * dxcinv[i];
+                double pgxe = PG(1, j, k) * iup + ((double)(1 - iup) * (P(i + 1, j, k) - P(i, j, k))) * dxcinv[i + 1];
+                double pgys = PG(2, i, k) * jum + ((double)(1 - jum) * (P(i, j, k) - P(i, j - 1, k))) * dycinv[j];
+                double pgyn = PG(3, i, k) * jup + ((double)(1 - jup) * (P(i, j + 1, k) - P(i, j, k))) * dycinv[j + 1];
+                double pgzb = PG(4, i, j) * kum + ((double)(1 - kum) * (P(i, j, k) - P(i, j, k - 1))) * dzcinv[k];
+                double pgzf = PG(5, i, j) * kup + ((double)(1 - kup) * (P(i, j, k + 1) - P(i, j, k))) * dzcinv[k + 1];
+                pgradflux = pgradflux +
+                    (-(pgxw * dy[j] * dz[k]) + pgxe * dy[j] * dz[k] - pgys * dx[i] * dz[k] +
+                     pgyn * dx[i] * dz[k] - pgzb * dx[i] * dy[j] + pgzf * dx[i] * dy[j]) *
+                    (double)(1 - c->iblank[f]);
+            }
+    double corr = -pgradflux / c->p.outflow_area;
+    for (int k = 0; k <= c->nz; ++k) for (int j = 0; j <= c->ny; ++j) {
+        if (bc[0] == BC_ZERO_GRADIENT) PG(0, j, k) = PG(0, j, k) - corr;
+        if (bc[1] == BC_ZERO_GRADIENT) PG(1, j, k) = PG(1, j, k) + corr;
+    }
+    for (int k = 0; k <= c->nz; ++k) for (int i = 0; i <= c->nx; ++i) {
+        if (bc[2] == BC_ZERO_GRADIENT) PG(2, i, k) = PG(2, i, k) - corr;
+        if (bc[3] == BC_ZERO_GRADIENT) PG(3, i, k) = PG(3, i, k) + corr;
+    }
+    for (int j = 0; j <= c->ny; ++j) for (int i = 0; i <= c->nx; ++i) {
+        if (bc[4] == BC_ZERO_GRADIENT) PG(4, i, j) = PG(4, i, j) - corr;
+        if (bc[5] == BC_ZERO_GRADIENT) PG(5, i, j) = PG(5, i, j) + corr;
+    }
+#undef P
+#undef PG
+}
+
+/* IBM/CORE_POISSON.F90:1794-1823 on a full (0:nx+1)^3 array. */
+void or_gcm_correct_pressure(or_ctx *c, double *p)
+{
+    set_outer_ghost_pres(c, p, c->nx + 1, c->ny + 1);
+    gcm_p_set_bc_internal(c, p, c->nx + 1, c->ny + 1);
+    gcm_enforce_p_compatibility(c, p, c->nx + 1, c->ny + 1);
+#define PG(s, a, b) c->pgrad[s][(size_t)(a) + (size_t)c->pg_sx[s] * (size_t)(b)]
+    for (int k = 1; k <= c->nzc; ++k)
+        for (int j = 1; j <= c->nyc; ++j)
+            for (int i = 1; i <= c->nxc; ++i) {
+                size_t f = FI(c, i, j, k);
+                const double pot = 0.0;
+                c->nlw0[f] = -(c->dxinv[0][i] * (c->fl[1][f] * PG(1, j, k) - c->fl[0][f] * PG(0, j, k)) * (1.0 - pot))
+                             - c->dxinv[1][j] * (c->fl[3][f] * PG(3, i, k) - c->fl[2][f] * PG(2, i, k)) * (1.0 - pot)
+                             - c->dxinv[2][k] * (c->fl[5][f] * PG(5, i, j) - c->fl[4][f] * PG(4, i, j)) * (1.0 - pot);
+            }
+#undef PG
+}
+
+/* ---------------------------------------------------- MG bookkeeping ---- */
+/* IBM/CORE_MG.F90:699-822 MG_Prepare_Iblank (also zeroes coarse ghost marks without a body). */
+static void mg_prepare_iblank(or_ctx *c, int d)
+{
+    for (int l = 2; l <= c->nlev[d]; ++l) {
+        size_t e[3] = {(size_t)c->nx + 1, (size_t)c->ny + 1, (size_t)c->nz + 1};
+        e[d] = (size_t)c->mgrid[d][l] + 2;
+        memset(c->cib[d][l], 0, e[0] * e[1] * e[2]);
+    }
+    int ext[3] = {c->nxc, c->nyc, c->nzc};
+    for (int l = 2; l <= c->nlev[d]; ++l) {
+        int sx = (d == 0) ? c->mgrid[0][l] + 2 : c->nx + 1;
+        int sy = (d == 1) ? c->mgrid[1][l] + 2 : c->ny + 1;
+        int e[3] = {ext[0], ext[1], ext[2]};
+        e[d] = c->mgrid[d][l];
+        if (c->p.internal_boundary_present == 1) {
+            int psx = (l > 2) ? ((d == 0) ? c->mgrid[0][l - 1] + 2 : c->nx + 1) : c->nx + 2;
+            int psy = (l > 2) ? ((d == 1) ? c->mgrid[1][l - 1] + 2 : c->ny + 1) : c->ny + 2;
+            const int8_t *prev = (l > 2) ? c->cib[d][l - 1] : c->iblank;
+            for (int k = 1; k <= e[2]; ++k)
+                for (int j = 1; j <= e[1]; ++j)
+                    for (int i = 1; i <= e[0]; ++i) {
+                        int a[3] = {i, j, k}, b[3] = {i, j, k};
+                        a[d] = 2 * a[d] - 1; b[d] = 2 * b[d];
+                        c->cib[d][l][VI(sx, sy, i, j, k)] =
+                            (int8_t)(prev[VI(psx, psy, a[0], a[1], a[2])] * prev[VI(psx, psy, b[0], b[1], b[2])]);
+                    }
+        } else {
+            for (int k = 1; k <= e[2]; ++k)
+                for (int j = 1; j <= e[1]; ++j)
+                    for (int i = 1; i <= e[0]; ++i) c->ghostMG[FI(c, i, j, k)] = 0;
+        }
+    }
+}
+
+static i8v ib_view(or_ctx *c, int d, int l)
+{
+    i8v v;
+    if (l <= 1) { v.a = c->iblank; v.sx = c->nx + 2; v.sy = c->ny + 2; return v; }
+    v.a = c->cib[d][l];
+    v.sx = (d == 0) ? c->mgrid[0][l] + 2 : c->nx + 1;
+    v.sy = (d == 1) ? c->mgrid[1][l] + 2 : c->ny + 1;
+    return v;
+}
+
+static void gcm_pressure(or_ctx *c, double *var, double *rhs);
+
+/* IBM/CORE_MG.F90:1667-1713 MG_Prepare_BC */
+static void mg_prepare_bc(or_ctx *c, int l)
+{
+    size_t nf = (size_t)(c->nx + 2) * (size_t)(c->ny + 2) * (size_t)(c->nz + 2);
+    if (l == 1) {
+        for (int s = 0; s < 6; ++s) memcpy(c->flMG[s], c->fl[s], nf);
+        if (c->p.internal_boundary_present == 1)
+            for (size_t q = 0; q < nf; ++q) c->ghostMG[q] = c->ghost[q];
+        if (c->p.boundary_formulation == GCM_METHOD) {
+            /* GCM_correct_pressure acts on the module pPrime, not on the MG copy */
+            if (c->pPrime_mod) or_gcm_correct_pressure(c, c->pPrime_mod);
+        } else {
+            memset(c->nlw, 0, nf * sizeof(double));
+        }
+    } else if (c->p.internal_boundary_present == 1) {
+        memset(c->ghostMG, 0, nf * sizeof(int));
+        memset(c->nlw, 0, nf * sizeof(double));
+    }
+}
+
+/* IBM/CORE_MG.F90:1716-1879 MG_Prepare(nlev, mx, my, mz) with mx.. = cell counts. */
+static void mg_prepare(or_ctx *c, int mx, int my, int mz)
+{
+    i8v ib = c->ibMG;
+#define FL(s, i, j, k) c->flMG[s][FI(c, i, j, k)]
+#define UPF(a, b) ((int8_t)(int)((double)((int)(a) - (int)(b)) / 2.0 + 0.5))
+    if (c->p.internal_boundary_present == 1 || c->p.coarse_flag_mode == 1) {
+        for (int k = 1; k <= mz; ++k) {
+            for (int j = 1; j <= my; ++j) {
+                for (int i = 1; i <= mx - 1; ++i) FL(1, i, j, k) = UPF(IBV(ib, i + 1, j, k), IBV(ib, i, j, k));
+                for (int i = 2; i <= mx; ++i) FL(0, i, j, k) = UPF(IBV(ib, i - 1, j, k), IBV(ib, i, j, k));
+            }
+            for (int j = 1; j <= my - 1; ++j)
+                for (int i = 1; i <= mx; ++i) FL(3, i, j, k) = UPF(IBV(ib, i, j + 1, k), IBV(ib, i, j, k));
+            for (int j = 2; j <= my; ++j)
+                for (int i = 1; i <= mx; ++i) FL(2, i, j, k) = UPF(IBV(ib, i, j - 1, k), IBV(ib, i, j, k));
+        }
+        for (int j = 1; j <= my; ++j)
+            for (int i = 1; i <= mx; ++i) {
+                for (int k = 1; k <= mz - 1; ++k) FL(5, i, j, k) = UPF(IBV(ib, i, j, k + 1), IBV(ib, i, j, k));
+                for (int k = 2; k <= mz; ++k) FL(4, i, j, k) = UPF(IBV(ib, i, j, k - 1), IBV(ib, i, j, k));
+            }
+    }
+    const int *pbc = c->p.pbc;
+    for (int k = 1; k <= mz; ++k) for (int j = 1; j <= my; ++j) {
+        FL(0, 1, j, k) = (pbc[0] == PBC_DIRICHLET) ? -1 : 1;
+        FL(1, mx, j, k) = (pbc[1] == PBC_DIRICHLET) ? -1 : 1;
+    }
+    for (int k = 1; k <= mz; ++k) for (int i = 1; i <= mx; ++i) {
+        FL(2, i, 1, k) = (pbc[2] == PBC_DIRICHLET) ? -1 : 1;
+        FL(3, i, my, k) = (pbc[3] == PBC_DIRICHLET) ? -1 : 1;
+    }
+    for (int j = 1; j <= my; ++j) for (int i = 1; i <= mx; ++i) {
+        FL(4, i, j, 1) = (pbc[4] == PBC_DIRICHLET) ? -1 : 1;
+        FL(5, i, j, mz) = (pbc[5] == PBC_DIRICHLET) ? -1 : 1;
+    }
+#undef FL
+#undef UPF
+}
+
+/* --------------------------------------------------------- MG_itsolv ---- */
+/* IBM/CORE_MG.F90:1883-2270.  Coefficients for cell (i,j,k) at levels (lx,ly,lz). */
+typedef struct { double amx, apx, acx, amy, apy, acy, amz, apz, acz; } coefs9;
+
+static inline coefs9 cell_coefs(or_ctx *c, int i, int j, int k, int lx, int ly, int lz)
+{
+    coefs9 q;
+    size_t f = FI(c, i, j, k);
+    double d2 = (double)(c->p.ndim - DIM_2D);
+    q.amx = MG1(c, 0, dxcinv_MG, i, lx) * MG1(c, 0, dxinv_MG, i, lx) * (1.0 - (double)c->flMG[0][f]);
+    q.apx = MG1(c, 0, dxcinv_MG, i + 1, lx) * MG1(c, 0, dxinv_MG, i, lx) * (1.0 - (double)c->flMG[1][f]);
+    q.acx = -(q.amx + q.apx);
+    q.amy = MG1(c, 1, dxcinv_MG, j, ly) * MG1(c, 1, dxinv_MG, j, ly) * (1.0 - (double)c->flMG[2][f]);
+    q.apy = MG1(c, 1, dxcinv_MG, j + 1, ly) * MG1(c, 1, dxinv_MG, j, ly) * (1.0 - (double)c->flMG[3][f]);
+    q.acy = -(q.amy + q.apy);
+    q.amz = MG1(c, 2, dxcinv_MG, k, lz) * MG1(c, 2, dxinv_MG, k, lz) * (1.0 - (double)c->flMG[4][f]) * d2;
+    q.apz = MG1(c, 2, dxcinv_MG, k + 1, lz) * MG1(c, 2, dxinv_MG, k, lz) * (1.0 - (double)c->flMG[5][f]) * d2;
+    q.acz = -(q.amz + q.apz);
+    return q;
+}
+
+static int line_active(or_ctx *c, int dir, int colour, int a, int b)
+{
+    /* colour schedule; returns 1 when the line indexed (a,b) is visited in pass `colour` */
+    int rb = c->p.iRedBlack;
+    int nd = c->p.ndim;
+    if (rb == 3) return ((a + b) & 1) == (colour == 0 ? 0 : 1);
+    if (rb == 0) return colour == 0;
+    /* reference colour loops, IBM/MAIN.F90:548-571 and IBM/CORE_MG.F90:1921-1923,2043-2046,2165-2168 */
+    int TNx = 2, TNy = (rb == 1) ? 1 : 2, TNz = (rb == 1) ? 1 : 2;
+    int iStep = (rb == 1) ? 1 : 2, jStep = 2, kStep = (nd - DIM_2D) + 1;
+    int Ncolor = colour + 1;
+    if (dir == 0) {           /* a = j, b = k */
+        if (Ncolor > TNx) return 0;
+        int kinit = (Ncolor - 1) * (nd - DIM_2D) + 1, jinit = Ncolor;
+        return b >= kinit && (b - kinit) % kStep == 0 && a >= jinit && (a - jinit) % jStep == 0;
+    } else if (dir == 1) {    /* a = i, b = k */
+        if (Ncolor > TNy) return 0;
+        int kinit = (Ncolor - 1) * (nd - DIM_2D) + 1, iinit = Ncolor;
+        return b >= kinit && (b - kinit) % kStep == 0 && a >= iinit && (a - iinit) % iStep == 0;
+    } else {                  /* a = i, b = j */
+        if (Ncolor > TNz) return 0;
+        int jinit = Ncolor, iinit = Ncolor;
+        return b >= jinit && (b - jinit) % jStep == 0 && a >= iinit && (a - iinit) % iStep == 0;
+    }
+}
+
+static void mg_itsolv(or_ctx *c, double *var, const double *R, int lx, int ly, int lz, int mx, int my, int mz)
+{
+    int sx = mx + 1, sy = my + 1;
+    int nmax = mx > my ? mx : my; if (mz > nmax) nmax = mz;
+    double *am = zalloc(sizeof(double) * (size_t)(nmax + 2)), *ac = zalloc(sizeof(double) * (size_t)(nmax + 2));
+    double *ap = zalloc(sizeof(double) * (size_t)(nmax + 2)), *rhs = zalloc(sizeof(double) * (size_t)(nmax + 2));
+    double *sol = zalloc(sizeof(double) * (size_t)(nmax + 2));
+    double *gam = zalloc(sizeof(double) * (size_t)(nmax + 2));
+    i8v ib = c->ibMG;
+    const double om = c->p.omega;
+    const int finest = (lx * ly * lz == 1);
+    const int *pbc = c->p.pbc;
+    const double *ppp = c->p.ppp;
+    const double tiny = (double)1.0e-12f;
+#define V(i, j, k) var[VI(sx, sy, i, j, k)]
+    int ncol = (c->p.iRedBlack == 0) ? 1 : 2;
+    /* x-lines */
+    for (int col = 0; col < ncol; ++col)
+        for (int k = 1; k <= mz - 1; ++k)
+            for (int j = 1; j <= my - 1; ++j) {
+                if (!line_active(c, 0, col, j, k)) continue;
+                for (int i = 1; i <= mx - 1; ++i) {
+                    coefs9 q = cell_coefs(c, i, j, k, lx, ly, lz);
+                    size_t f = FI(c, i, j, k);
+                    double r = R[VI(sx, sy, i, j, k)] - V(i, j - 1, k) * q.amy - V(i, j + 1, k) * q.apy -
+                               V(i, j, k - 1) * q.amz - V(i, j, k + 1) * q.apz + c->nlw[f];
+                    double b = (double)IBV(ib, i, j, k);
+                    am[i] = q.amx * (1.0 - b);
+                    ap[i] = q.apx * (1.0 - b);
+                    ac[i] = (q.acx + q.acy + q.acz) * (1.0 - b) + b;
+                    rhs[i] = r * (1.0 - b) + (double)c->ghostMG[f] * V(i, j, k);
+                    if (fabs(ac[i]) < tiny) { am[i] = 0.0; ap[i] = 0.0; ac[i] = 1.0; rhs[i] = V(i, j, k); }
+                }
+                if (pbc[0] == PBC_DIRICHLET && finest) rhs[1] = rhs[1] - ppp[0] * am[1];
+                if (pbc[1] == PBC_DIRICHLET && finest) rhs[mx - 1] = rhs[mx - 1] - ppp[1] * ap[mx - 1];
+                tdma_w(am, ac, ap, rhs, sol, gam, 1, mx - 1);
+                for (int i = 1; i <= mx - 1; ++i) V(i, j, k) = V(i, j, k) * (1.0 - om) + om * sol[i];
+                if (pbc[0] == PBC_DIRICHLET && finest) V(0, j, k) = ppp[0];
+                if (pbc[1] == PBC_DIRICHLET && finest) V(mx, j, k) = ppp[1];
+            }
+    /* y-lines */
+    for (int col = 0; col < ncol; ++col)
+        for (int k = 1; k <= mz - 1; ++k)
+            for (int i = 1; i <= mx - 1; ++i) {
+                if (!line_active(c, 1, col, i, k)) continue;
+                for (int j = 1; j <= my - 1; ++j) {
+                    coefs9 q = cell_coefs(c, i, j, k, lx, ly, lz);
+                    size_t f = FI(c, i, j, k);
+                    double r = R[VI(sx, sy, i, j, k)] - V(i - 1, j, k) * q.amx - V(i + 1, j, k) * q.apx -
+                               V(i, j, k - 1) * q.amz - V(i, j, k + 1) * q.apz + c->nlw[f];
+                    double b = (double)IBV(ib, i, j, k);
+                    am[j] = q.amy * (1.0 - b);
+                    ap[j] = q.apy * (1.0 - b);
+                    ac[j] = (q.acx + q.acy + q.acz) * (1.0 - b) + b;
+                    rhs[j] = r * (1.0 - b) + (double)c->ghostMG[f] * V(i, j, k);
+                    if (fabs(ac[j]) < tiny) { am[j] = 0.0; ap[j] = 0.0; ac[j] = 1.0; rhs[j] = V(i, j, k); }
+                }
+                if (pbc[2] == PBC_DIRICHLET && finest) rhs[1] = rhs[1] - ppp[2] * am[1];
+                if (pbc[3] == PBC_DIRICHLET && finest) rhs[my - 1] = rhs[my - 1] - ppp[3] * ap[my - 1];
+                tdma_w(am, ac, ap, rhs, sol, gam, 1, my - 1);
+                for (int j = 1; j <= my - 1; ++j) V(i, j, k) = V(i, j, k) * (1.0 - om) + om * sol[j];
+                if (pbc[2] == PBC_DIRICHLET && finest) V(i, 0, k) = ppp[2];
+                if (pbc[3] == PBC_DIRICHLET && finest) V(i, my, k) = ppp[3];
+            }
+    /* z-lines */
+    if (c->p.ndim == DIM_3D)
+        for (int col = 0; col < ncol; ++col)
+            for (int j = 1; j <= my - 1; ++j)
+                for (int i = 1; i <= mx - 1; ++i) {
+                    if (!line_active(c, 2, col, i, j)) continue;
+                    for (int k = 1; k <= mz - 1; ++k) {
+                        coefs9 q = cell_coefs(c, i, j, k, lx, ly, lz);
+                        size_t f = FI(c, i, j, k);
+                        double r = R[VI(sx, sy, i, j, k)] - V(i, j - 1, k) * q.amy - V(i, j + 1, k) * q.apy -
+                                   V(i - 1, j, k) * q.amx - V(i + 1, j, k) * q.apx + c->nlw[f];
+                        double b = (double)IBV(ib, i, j, k);
+                        am[k] = q.amz * (1.0 - b);
+                        ap[k] = q.apz * (1.0 - b);
+                        ac[k] = (q.acx + q.acy + q.acz) * (1.0 - b) + b;
+                        rhs[k] = r * (1.0 - b) + (double)c->ghostMG[f] * V(i, j, k);
+                        if (fabs(ac[k]) < tiny) { am[k] = 0.0; ap[k] = 0.0; ac[k] = 1.0; rhs[k] = V(i, j, k); }
+                    }
+                    if (pbc[4] == PBC_DIRICHLET && finest) rhs[1] = rhs[1] - ppp[4] * am[1];
+                    if (pbc[5] == PBC_DIRICHLET && finest) rhs[mz - 1] = rhs[mz - 1] - ppp[5] * ap[mz - 1];
+                    tdma_w(am, ac, ap, rhs, sol, gam, 1, mz - 1);
+                    for (int k = 1; k <= mz - 1; ++k) V(i, j, k) = V(i, j, k) * (1.0 - om) + om * sol[k];
+                    if (pbc[4] == PBC_DIRICHLET && finest) V(i, j, 0) = ppp[4];
+                    if (pbc[5] == PBC_DIRICHLET && finest) V(i, j, mz) = ppp[5];
+                }
+#undef V
+    free(am); free(ac); free(ap); free(rhs); free(sol); free(gam);
+}
+
+/* IBM/CORE_MG.F90:2274-2387 MG_Residual */
+static void mg_residual(or_ctx *c, const double *var, const double *R, double *resL,
+                        int lx, int ly, int lz, int mx, int my, int mz)
+{
+    int sx = mx + 1, sy = my + 1;
+    i8v ib = c->ibMG;
+#define V(i, j, k) var[VI(sx, sy, i, j, k)]
+    for (int k = 1; k <= mz - 1; ++k)
+        for (int j = 1; j <= my - 1; ++j)
+            for (int i = 1; i <= mx - 1; ++i) {
+                coefs9 q = cell_coefs(c, i, j, k, lx, ly, lz);
+                double b = (double)IBV(ib, i, j, k);
+                double bmx = q.amx * (1.0 - b), bpx = q.apx * (1.0 - b);
+                double bmy = q.amy * (1.0 - b), bpy = q.apy * (1.0 - b);
+                double bmz = q.amz * (1.0 - b), bpz = q.apz * (1.0 - b);
+                double bc = (q.acx + q.acy + q.acz) * (1.0 - b) + b;
+                double res = R[VI(sx, sy, i, j, k)] - V(i, j, k) * bc - V(i - 1, j, k) * bmx - V(i + 1, j, k) * bpx -
+                             V(i, j - 1, k) * bmy - V(i, j + 1, k) * bpy - V(i, j, k - 1) * bmz -
+                             V(i, j, k + 1) * bpz + c->nlw[FI(c, i, j, k)];
+                resL[VI(sx, sy, i, j, k)] = res * (1.0 - b);
+            }
+#undef V
+}
+
+/* IBM/CORE_MG.F90:2464-2723 MG_Restrict_X/Y/Z; nlev = fine level, m1 = coarse upper bound. */
+static void mg_restrict(or_ctx *c, int d, const double *var, double *r, int nlev, int mx, int my, int mz, int m1)
+{
+    int sx = mx + 1, sy = my + 1;
+    int csx = (d == 0) ? m1 + 1 : sx, csy = (d == 1) ? m1 + 1 : sy;
+    i8v ib = c->ibMG;
+    int e[3] = {mx - 1, my - 1, mz - 1};
+    e[d] = m1 - 1;
+    for (int k = 1; k <= e[2]; ++k)
+        for (int j = 1; j <= e[1]; ++j)
+            for (int i = 1; i <= e[0]; ++i) {
+                int cc = (d == 0) ? i : (d == 1 ? j : k);
+                int ii = 2 * cc, iim = 2 * cc - 1, iip = 2 * cc + 1;
+                double area1 = MG1(c, d, x_MG, ii, nlev) - MG1(c, d, x_MG, iim, nlev);
+                double area2 = MG1(c, d, x_MG, iip, nlev) - MG1(c, d, x_MG, ii, nlev);
+                double area = area1 + area2;
+                double w1 = area1 / area, w2 = area2 / area;
+                int a[3] = {i, j, k}, b[3] = {i, j, k};
+                a[d] = ii; b[d] = iim;
+                double da = 1.0 - (double)IBV(ib, a[0], a[1], a[2]);
+                double db = 1.0 - (double)IBV(ib, b[0], b[1], b[2]);
+                double va = var[VI(sx, sy, a[0], a[1], a[2])], vb = var[VI(sx, sy, b[0], b[1], b[2])];
+                double sum1 = da * w2 * va + db * w1 * vb;
+                double temp = (d == 0) ? (da * w2 + db * w1) : (db * w1 + da * w2);
+                r[VI(csx, csy, i, j, k)] = (temp > 0.0) ? sum1 / temp : sum1;
+            }
+}
+
+/* IBM/CORE_MG.F90:2885-3523 MG_Prolong_X/Y/Z: coarse correc -> fine phi.
+ * ibMG must be the coarse (nlev+1) view.  m1 = coarse upper bound, mfine = fine upper bound. */
+static void mg_prolong(or_ctx *c, int d, double *phi, const double *correc, int nlev, int mx, int my, int mz,
+                       int m1, int mfine)
+{
+    i8v ib = c->ibMG;
+    int csx = (d == 0) ? m1 + 1 : mx + 1, csy = (d == 1) ? m1 + 1 : my + 1;
+    int fsx = (d == 0) ? mfine + 1 : mx + 1, fsy = (d == 1) ? mfine + 1 : my + 1;
+    int nc = m1 - 1;
+    double *w1 = zalloc(sizeof(double) * (size_t)(nc + 2)), *w2 = zalloc(sizeof(double) * (size_t)(nc + 2));
+    double *w3 = zalloc(sizeof(double) * (size_t)(nc + 2)), *w4 = zalloc(sizeof(double) * (size_t)(nc + 2));
+    for (int i = 1; i <= nc; ++i) {
+        int ii = 2 * i, iim = 2 * i - 1;
+        double d1 = sq_inv(MG1(c, d, xc_MG, iim, nlev) - MG1(c, d, xc_MG, i, nlev + 1));
+        double d2 = sq_inv(MG1(c, d, xc_MG, iim, nlev) - MG1(c, d, xc_MG, i - 1, nlev + 1));
+        double de = d1 + d2;
+        w1[i] = d1 / de; w2[i] = d2 / de;
+        d1 = sq_inv(MG1(c, d, xc_MG, ii, nlev) - MG1(c, d, xc_MG, i, nlev + 1));
+        d2 = sq_inv(MG1(c, d, xc_MG, ii, nlev) - MG1(c, d, xc_MG, i + 1, nlev + 1));
+        de = d1 + d2;
+        w3[i] = d1 / de; w4[i] = d2 / de;
+    }
+    /* the two other directions run over their interiors */
+    int e[3] = {mx - 1, my - 1, mz - 1};
+    int o1 = (d == 0) ? 1 : 0, o2 = (d == 2) ? 1 : 2;
+    for (int b = 1; b <= e[o2]; ++b)
+        for (int a = 1; a <= e[o1]; ++a) {
+#define CIDX(q) ((d == 0) ? VI(csx, csy, q, a, b) : (d == 1) ? VI(csx, csy, a, q, b) : VI(csx, csy, a, b, q))
+#define FIDX(q) ((d == 0) ? VI(fsx, fsy, q, a, b) : (d == 1) ? VI(fsx, fsy, a, q, b) : VI(fsx, fsy, a, b, q))
+#define DIB(q) (1.0 - (double)((d == 0) ? IBV(ib, q, a, b) : (d == 1) ? IBV(ib, a, q, b) : IBV(ib, a, b, q)))
+            phi[FIDX(1)] = correc[CIDX(1)];
+            double delta1 = w3[1] * DIB(1), delta2 = w4[1] * DIB(2), delta = delta1 + delta2;
+            phi[FIDX(2)] = delta1 * correc[CIDX(1)] + delta2 * correc[CIDX(2)];
+            if (delta > 0.0) phi[FIDX(2)] = phi[FIDX(2)] / delta;
+            for (int i = 2; i <= nc - 1; ++i) {
+                int ii = 2 * i, iim = 2 * i - 1;
+                double v1 = correc[CIDX(i)], v2 = correc[CIDX(i - 1)], v3 = correc[CIDX(i + 1)];
+                delta1 = w1[i] * DIB(i); delta2 = w2[i] * DIB(i - 1); delta = delta1 + delta2;
+                phi[FIDX(iim)] = delta1 * v1 + delta2 * v2;
+                if (delta > 0.0) phi[FIDX(iim)] = phi[FIDX(iim)] / delta;
+                delta1 = w3[i] * DIB(i); delta2 = w4[i] * DIB(i + 1); delta = delta1 + delta2;
+                phi[FIDX(ii)] = delta1 * v1 + delta2 * v3;
+                if (delta > 0.0) phi[FIDX(ii)] = phi[FIDX(ii)] / delta;
+            }
+            int i = nc, ii = 2 * nc, iim = 2 * nc - 1;
+            delta1 = w1[i] * DIB(i); delta2 = w2[i] * DIB(i - 1); delta = delta1 + delta2;
+            phi[FIDX(iim)] = delta1 * correc[CIDX(i)] + delta2 * correc[CIDX(i - 1)];
+            if (delta > 0.0) phi[FIDX(iim)] = phi[FIDX(iim)] / delta;
+            phi[FIDX(ii)] = correc[CIDX(i)];
+            if (nlev == 1 && mfine - 1 > 2 * i) phi[FIDX(mfine - 1)] = correc[CIDX(i)];
+#undef CIDX
+#undef FIDX
+#undef DIB
+        }
+    free(w1); free(w2); free(w3); free(w4);
+}
+
+/* IBM/CORE_MG.F90:4707-4743 GCM_Pressure on the MG copy (0:nx,0:ny,0:nz). */
+static void gcm_pressure(or_ctx *c, double *var, double *rhs)
+{
+    (void)rhs;
+    set_outer_ghost_pres(c, var, c->nx, c->ny);
+    gcm_p_set_bc_internal(c, var, c->nx, c->ny);
+    gcm_enforce_p_compatibility(c, var, c->nx, c->ny);
+    mg_prepare_bc(c, 1);
+}
+
+/* IBM/CORE_MG.F90:1239-1663 MG_X / MG_Y / MG_Z (recursive), direction d. */
+static void mg_cycle(or_ctx *c, int d, double *var, double *rhs, int n, int nlev, int mx, int my, int mz,
+                     int WF, int *GMM, int mgCycle)
+{
+    int lev[3] = {1, 1, 1};
+    lev[d] = n;
+    c->ibMG = ib_view(c, d, n);
+    int totIter = (n == 1) ? c->p.iterFinest : ((n == c->nlev[d]) ? c->p.iterCoarsest : 1);
+    mg_prepare_bc(c, n);
+    if (n != 1) mg_prepare(c, mx - 1, my - 1, mz - 1);
+    int gcm = (c->p.boundary_formulation == GCM_METHOD);
+    if (n == 1 && gcm) gcm_pressure(c, var, rhs);
+    if (WF == 1)
+        for (int it = 0; it < totIter; ++it) mg_itsolv(c, var, rhs, lev[0], lev[1], lev[2], mx, my, mz);
+    if (n == nlev) { if (mgCycle == 3) *GMM = 1; return; }
+    size_t nfield = (size_t)(mx + 1) * (size_t)(my + 1) * (size_t)(mz + 1);
+    double *r = zalloc(sizeof(double) * nfield);
+    mg_residual(c, var, rhs, r, lev[0], lev[1], lev[2], mx, my, mz);
+    int m1 = c->mgrid[d][n + 1] + 1;
+    int cm[3] = {mx, my, mz};
+    cm[d] = m1;
+    size_t ncoarse = (size_t)(cm[0] + 1) * (size_t)(cm[1] + 1) * (size_t)(cm[2] + 1);
+    double *r1 = zalloc(sizeof(double) * ncoarse), *phi = zalloc(sizeof(double) * ncoarse);
+    mg_restrict(c, d, r, r1, n, mx, my, mz, m1);
+    int count = (n != nlev - 1) ? *GMM : 1;
+    for (int I = 1; I <= count; ++I)
+        mg_cycle(c, d, phi, r1, n + 1, nlev, cm[0], cm[1], cm[2], I, GMM, mgCycle);
+    c->ibMG = ib_view(c, d, n + 1);
+    int fm[3] = {mx, my, mz};
+    fm[d] = m1;
+    mg_prolong(c, d, r, phi, n, fm[0], fm[1], fm[2], m1, (d == 0) ? mx : (d == 1 ? my : mz));
+    c->ibMG = ib_view(c, d, n);
+    int sx = mx + 1, sy = my + 1;
+    for (int k = 1; k <= mz - 1; ++k)
+        for (int j = 1; j <= my - 1; ++j)
+            for (int i = 1; i <= mx - 1; ++i) {
+                size_t q = VI(sx, sy, i, j, k);
+                var[q] = var[q] + r[q] * (1.0 - (double)IBV(c->ibMG, i, j, k));
+            }
+    mg_prepare_bc(c, n);
+    if (n != 1) mg_prepare(c, mx - 1, my - 1, mz - 1);
+    if (n == 1 && gcm) gcm_pressure(c, var, rhs);
+    int post;
+    if (d == 0) post = (n == 1) ? 0 : 1;
+    else if (d == 1) post = (n == 1) ? ((c->p.ndim == DIM_2D) ? c->p.iterFinest : 0) : 1;
+    else post = (n == 1) ? c->p.iterFinest : 1;
+    for (int it = 0; it < post; ++it) mg_itsolv(c, var, rhs, lev[0], lev[1], lev[2], mx, my, mz);
+    if (d != 0 && n == 1 && gcm) gcm_pressure(c, var, rhs);
+    if (n == 1 && mgCycle == 3) *GMM = 2;
+    free(r); free(r1); free(phi);
+}
+
+/* IBM/CORE_MG.F90:281-334 MG_Solver on full (0:nx+1)^3 arrays; :391-527 MG_Solv_x/y/z. */
+int or_mg_solver(or_ctx *c, double *var, const double *rr)
+{
+    int nx = c->nx, ny = c->ny, nz = c->nz;
+    size_t n1 = (size_t)(nx + 1) * (size_t)(ny + 1) * (size_t)(nz + 1);
+    double *rr1 = zalloc(sizeof(double) * n1), *var1 = zalloc(sizeof(double) * n1);
+    for (int k = 0; k <= nz; ++k) for (int j = 0; j <= ny; ++j) for (int i = 0; i <= nx; ++i) {
+        rr1[VI(nx + 1, ny + 1, i, j, k)] = rr[FI(c, i, j, k)];
+        var1[VI(nx + 1, ny + 1, i, j, k)] = var[FI(c, i, j, k)];
+    }
+    int nd = (c->p.ndim == DIM_3D) ? 3 : 2;
+    double *save = c->pPrime_mod;
+    c->pPrime_mod = var;
+    for (int d = 0; d < nd; ++d) {
+        mg_prepare_iblank(c, d);
+        int cycle_sel = (d == 2) ? c->p.mgcycle[0] : c->p.mgcycle[d];   /* MG_Solv_z tests mgCycleX, :515 */
+        int GMM = (cycle_sel == 1) ? 1 : 2;
+        mg_cycle(c, d, var1, rr1, 1, c->nlev[d], nx, ny, nz, 1, &GMM, c->p.mgcycle[d]);
+        for (int k = 0; k <= nz; ++k) for (int j = 0; j <= ny; ++j) for (int i = 0; i <= nx; ++i)
+            var[FI(c, i, j, k)] = var1[VI(nx + 1, ny + 1, i, j, k)];
+    }
+    c->pPrime_mod = save;
+    free(rr1); free(var1);
+    return 0;
+}
+
+/* -------------------------------------------------- solve_poisson ------ */
+/* IBM/CORE_POISSON.F90:1111-1222 calc_residual: max-norm over fluid cells, first location of the max. */
+double or_calc_residual(or_ctx *c, const double *var, const double *r, int *loc)
+{
+    double resm = 0.0;
+    int l0 = 0, l1 = 0, l2 = 0;
+    double d2 = (double)(c->p.ndim - DIM_2D);
+    for (int k = 1; k <= c->nzc; ++k)
+        for (int j = 1; j <= c->nyc; ++j)
+            for (int i = 1; i <= c->nxc; ++i) {
+                size_t f = FI(c, i, j, k);
+                double bmx = c->dxcinv[0][i] * c->dxinv[0][i] * (double)(1 - c->fl[0][f]);
+                double bpx = c->dxcinv[0][i + 1] * c->dxinv[0][i] * (double)(1 - c->fl[1][f]);
+                double bcx = -(bmx + bpx);
+                double bmy = c->dxcinv[1][j] * c->dxinv[1][j] * (double)(1 - c->fl[2][f]);
+                double bpy = c->dxcinv[1][j + 1] * c->dxinv[1][j] * (double)(1 - c->fl[3][f]);
+                double bcy = -(bmy + bpy);
+                double bmz = c->dxcinv[2][k] * c->dxinv[2][k] * (double)(1 - c->fl[4][f]) * d2;
+                double bpz = c->dxcinv[2][k + 1] * c->dxinv[2][k] * (double)(1 - c->fl[5][f]) * d2;
+                double bcz = -(bmz + bpz);
+                double b = (double)(1 - c->iblank[f]);
+                bmx *= b; bpx *= b; bmy *= b; bpy *= b; bmz *= b; bpz *= b;
+                double bc = (bcx + bcy + bcz) * b + (double)c->iblank[f];
+                double res = r[f] - var[f] * bc - var[FI(c, i - 1, j, k)] * bmx - var[FI(c, i + 1, j, k)] * bpx -
+                             var[FI(c, i, j - 1, k)] * bmy - var[FI(c, i, j + 1, k)] * bpy -
+                             var[FI(c, i, j, k - 1)] * bmz - var[FI(c, i, j, k + 1)] * bpz + c->nlw0[f];
+                res = res * b;
+                if (fabs(res) > resm) { resm = fabs(res); l0 = i; l1 = j; l2 = k; }
+            }
+    if (loc) { loc[0] = l0; loc[1] = l1; loc[2] = l2; }
+    return resm;
+}
+
+/* IBM/CORE_POISSON.F90:419-490 subtracting_average_pressure (fresh_cell = 0). */
+void or_subtract_average(or_ctx *c, double *p)
+{
+    double pTotal = 0.0, volTotal = 0.0;
+    for (int k = 1; k <= c->nzc; ++k)
+        for (int j = 1; j <= c->nyc; ++j)
+            for (int i = 1; i <= c->nxc; ++i) {
+                size_t f = FI(c, i, j, k);
+                double w = (double)(1 - c->iblank[f]);
+                pTotal = pTotal + p[f] * c->dx[0][i] * c->dx[1][j] * c->dx[2][k] * w;
+                volTotal = volTotal + c->dx[0][i] * c->dx[1][j] * c->dx[2][k] * w;
+            }
+    double pAverage = pTotal / volTotal;
+    for (int k = 1; k <= c->nzc; ++k)
+        for (int j = 1; j <= c->nyc; ++j)
+            for (int i = 1; i <= c->nxc; ++i) {
+                size_t f = FI(c, i, j, k);
+                if (c->iblank[f] == 1) p[f] = 0.0;
+                else p[f] = p[f] - pAverage;
+            }
+}
+
+/* IBM/CORE_SET_BC.F90:635-699 set_pressure_dirichlet_bc */
+static void set_pressure_dirichlet_bc(or_ctx *c)
+{
+    const int *pbc = c->p.pbc;
+    for (int k = 0; k <= c->nz; ++k) for (int j = 0; j <= c->ny; ++j) {
+        if (pbc[0] == PBC_DIRICHLET) c->fl[0][FI(c, 1, j, k)] = -1;
+        if (pbc[1] == PBC_DIRICHLET) c->fl[1][FI(c, c->nxc, j, k)] = -1;
+    }
+    for (int k = 0; k <= c->nz; ++k) for (int i = 0; i <= c->nx; ++i) {
+        if (pbc[2] == PBC_DIRICHLET) c->fl[2][FI(c, i, 1, k)] = -1;
+        if (pbc[3] == PBC_DIRICHLET) c->fl[3][FI(c, i, c->nyc, k)] = -1;
+    }
+    for (int j = 0; j <= c->ny; ++j) for (int i = 0; i <= c->nx; ++i) {
+        if (pbc[4] == PBC_DIRICHLET) c->fl[4][FI(c, i, j, 1)] = -1;
+        if (pbc[5] == PBC_DIRICHLET) c->fl[5][FI(c, i, j, c->nzc)] = -1;
+    }
+}
+
+/* IBM/CORE_POISSON.F90:901-1107 itsolv: plain line-SOR on the fine grid (pp_solver_type = 1). */
+static void lsor_itsolv(or_ctx *c, double *var, const double *r)
+{
+    int nmax = c->nx + 2;
+    if (c->ny + 2 > nmax) nmax = c->ny + 2;
+    if (c->nz + 2 > nmax) nmax = c->nz + 2;
+    double *am = zalloc(sizeof(double) * (size_t)nmax), *ac = zalloc(sizeof(double) * (size_t)nmax);
+    double *ap = zalloc(sizeof(double) * (size_t)nmax), *rhs = zalloc(sizeof(double) * (size_t)nmax);
+    double *sol = zalloc(sizeof(double) * (size_t)nmax);
+    double *gam = zalloc(sizeof(double) * (size_t)nmax);
+    double d2 = (double)(c->p.ndim - DIM_2D), om = c->p.omega;
+    const int *pbc = c->p.pbc;
+    const double *ppp = c->p.ppp;
+#define V(i, j, k) var[FI(c, i, j, k)]
+#define COEF(i, j, k)                                                                                   \
+    size_t f = FI(c, i, j, k);                                                                          \
+    double amx = c->dxcinv[0][i] * c->dxinv[0][i] * (double)(1 - c->fl[0][f]);                          \
+    double apx = c->dxcinv[0][i + 1] * c->dxinv[0][i] * (double)(1 - c->fl[1][f]);                      \
+    double acx = -(amx + apx);                                                                          \
+    double amy = c->dxcinv[1][j] * c->dxinv[1][j] * (double)(1 - c->fl[2][f]);                          \
+    double apy = c->dxcinv[1][j + 1] * c->dxinv[1][j] * (double)(1 - c->fl[3][f]);                      \
+    double acy = -(amy + apy);                                                                          \
+    double amz = c->dxcinv[2][k] * c->dxinv[2][k] * (double)(1 - c->fl[4][f]) * d2;                     \
+    double apz = c->dxcinv[2][k + 1] * c->dxinv[2][k] * (double)(1 - c->fl[5][f]) * d2;                 \
+    double acz = -(amz + apz);                                                                          \
+    double bw = (double)(1 - c->iblank[f]), bb = (double)c->iblank[f];
+    for (int k = 1; k <= c->nzc; ++k)
+        for (int j = 1; j <= c->nyc; ++j) {
+            for (int i = 1; i <= c->nxc; ++i) {
+                COEF(i, j, k)
+                double rr = r[f] - V(i, j - 1, k) * amy - V(i, j + 1, k) * apy - V(i, j, k - 1) * amz -
+                            V(i, j, k + 1) * apz + c->nlw0[f];
+                am[i] = amx * bw; ap[i] = apx * bw;
+                ac[i] = (acx + acy + acz) * bw + bb;
+                rhs[i] = rr * bw + (double)c->ghost[f] * V(i, j, k);
+            }
+            if (pbc[0] == PBC_DIRICHLET && pbc[1] == PBC_DIRICHLET) {
+                rhs[1] = rhs[1] - ppp[0] * am[1];
+                rhs[c->nxc] = rhs[c->nxc] - ppp[1] * ap[c->nxc];
+            }
+            tdma_w(am, ac, ap, rhs, sol, gam, 1, c->nxc);
+            for (int i = 1; i <= c->nxc; ++i) V(i, j, k) = V(i, j, k) + om * (sol[i] - V(i, j, k));
+            if (pbc[0] == PBC_DIRICHLET && pbc[1] == PBC_DIRICHLET) { V(0, j, k) = ppp[0]; V(c->nx, j, k) = ppp[1]; }
+        }
+    for (int k = 1; k <= c->nzc; ++k)
+        for (int i = 1; i <= c->nxc; ++i) {
+            for (int j = 1; j <= c->nyc; ++j) {
+                COEF(i, j, k)
+                double rr = r[f] - V(i - 1, j, k) * amx - V(i + 1, j, k) * apx - V(i, j, k - 1) * amz -
+                            V(i, j, k + 1) * apz + c->nlw0[f];
+                am[j] = amy * bw; ap[j] = apy * bw;
+                ac[j] = (acx + acy + acz) * bw + bb;
+                rhs[j] = rr * bw + (double)c->ghost[f] * V(i, j, k);
+            }
+            if (pbc[2] == PBC_DIRICHLET && pbc[3] == PBC_DIRICHLET) {
+                rhs[1] = rhs[1] - ppp[2] * am[1];
+                rhs[c->nyc] = rhs[c->nyc] - ppp[3] * ap[c->nyc];
+            }
+            tdma_w(am, ac, ap, rhs, sol, gam, 1, c->nyc);
+            for (int j = 1; j <= c->nyc; ++j) V(i, j, k) = V(i, j, k) + om * (sol[j] - V(i, j, k));
+        }
+    if (c->p.ndim == DIM_3D)
+        for (int j = 1; j <= c->nyc; ++j)
+            for (int i = 1; i <= c->nxc; ++i) {
+                for (int k = 1; k <= c->nzc; ++k) {
+                    COEF(i, j, k)
+                    double rr = r[f] - V(i, j - 1, k) * amy - V(i, j + 1, k) * apy - V(i - 1, j, k) * amx -
+                                V(i + 1, j, k) * apx + c->nlw0[f];
+                    am[k] = amz * bw; ap[k] = apz * bw;
+                    ac[k] = (acx + acy + acz) * bw + bb;
+                    rhs[k] = rr * bw + (double)c->ghost[f] * V(i, j, k);
+                }
+                if (pbc[4] == PBC_DIRICHLET && pbc[5] == PBC_DIRICHLET) {
+                    rhs[1] = rhs[1] - ppp[4] * am[1];
+                    rhs[c->nzc] = rhs[c->nzc] - ppp[5] * ap[c->nzc];
+                }
+                tdma_w(am, ac, ap, rhs, sol, gam, 1, c->nzc);
+                for (int k = 1; k <= c->nzc; ++k) V(i, j, k) = V(i, j, k) + om * (sol[k] - V(i, j, k));
+            }
+#undef V
+#undef COEF
+    free(am); free(ac); free(ap); free(rhs); free(sol); free(gam);
+}
+
+/* IBM/CORE_POISSON.F90:493-676 solve_poisson (LSOR and MG branches).
+ * Returns 0 converged, 1 iterMax reached, 2 ghost rows did not converge, <0 error. */
+int or_solve(or_ctx *c, double *pPrime, const double *nlu0, double *nlw0_out,
+             int *iters, double *maxres_out, int *loc, double *res_hist)
+{
+    if (!c->geometry_set) return -2;
+    const int *pbc = c->p.pbc;
+    size_t nf = (size_t)(c->nx + 2) * (size_t)(c->ny + 2) * (size_t)(c->nz + 2);
+    memset(c->nlw0, 0, nf * sizeof(double));   /* rhs_poisson zeroes nlw0, IBM/CORE_POISSON.F90:147 */
+    memset(c->nlw, 0, nf * sizeof(double));    /* standalone solve, IBM/MAIN.F90:2266 */
+    c->ghost_nonconv = 0;
+    if (pbc[0] == PBC_DIRICHLET || pbc[2] == PBC_DIRICHLET || pbc[4] == PBC_DIRICHLET)
+        set_pressure_dirichlet_bc(c);
+    else
+        or_subtract_average(c, pPrime);
+    int iter = 0, l[3] = {0, 0, 0};
+    double maxres = 1.0e10;
+    int gcm = (c->p.boundary_formulation == GCM_METHOD);
+    while (iter < c->p.iterMax_Poisson && maxres > c->p.restol_Poisson) {
+        if (c->p.pp_solver_type == 1) {
+            lsor_itsolv(c, pPrime, nlu0);
+        } else {
+            or_mg_solver(c, pPrime, nlu0);
+        }
+        if (gcm) or_gcm_correct_pressure(c, pPrime);
+        maxres = or_calc_residual(c, pPrime, nlu0, l);
+        if (res_hist) res_hist[iter] = maxres;
+        iter = iter + 1;
+        if (!(maxres == maxres)) break;
+    }
+    if (iters) *iters = iter;
+    if (maxres_out) *maxres_out = maxres;
+    if (loc) { loc[0] = l[0]; loc[1] = l[1]; loc[2] = l[2]; }
+    if (nlw0_out) memcpy(nlw0_out, c->nlw0, nf * sizeof(double));
+    if (!(maxres == maxres)) return -5;
+    if (iter == c->p.iterMax_Poisson && maxres > c->p.restol_Poisson) return 1;
+    if (c->ghost_nonconv) return 2;
+    return 0;
+}
+
+/* ------------------------------------------ level-wise kernels (tests) -- */
+int or_level_count(or_ctx *c, int d) { return c->nlev[d]; }
+int or_level_size(or_ctx *c, int d, int n) { return c->mgrid[d][n]; }
+
+void or_level_metrics(or_ctx *c, int d, int n, double *xnode, double *xc, double *dx,
+                      double *dxinv, double *dxc, double *dxcinv)
+{
+    int N = c->n[d];
+    for (int i = 0; i <= N + 1; ++i) {
+        if (xnode) xnode[i] = MG1(c, d, x_MG, i, n);
+        if (xc) xc[i] = MG1(c, d, xc_MG, i, n);
+        if (dx) dx[i] = MG1(c, d, dx_MG, i, n);
+        if (dxinv) dxinv[i] = MG1(c, d, dxinv_MG, i, n);
+        if (dxc) dxc[i] = MG1(c, d, dxc_MG, i, n);
+        if (dxcinv) dxcinv[i] = MG1(c, d, dxcinv_MG, i, n);
+    }
+}
+
+void or_coarse_iblank(or_ctx *c, int d, int n, int8_t *out)
+{
+    mg_prepare_iblank(c, d);
+    size_t e[3] = {(size_t)c->nx + 1, (size_t)c->ny + 1, (size_t)c->nz + 1};
+    e[d] = (size_t)c->mgrid[d][n] + 2;
+    memcpy(out, c->cib[d][n], e[0] * e[1] * e[2]);
+}
+
+/* Level state as seen by the smoother at level n of the d-cycle: iblank view,
+ * MG flags (recomputed from the coarse iblank), ghost marks. */
+static void level_state(or_ctx *c, int d, int n, int *m)
+{
+    mg_prepare_iblank(c, d);
+    m[0] = c->nx; m[1] = c->ny; m[2] = c->nz;
+    if (n > 1) m[d] = c->mgrid[d][n] + 1;
+    double *save = c->pPrime_mod;
+    c->pPrime_mod = NULL;
+    c->ibMG = ib_view(c, d, n);
+    mg_prepare_bc(c, n);
+    if (n != 1) mg_prepare(c, m[0] - 1, m[1] - 1, m[2] - 1);
+    c->pPrime_mod = save;
+}
+
+void or_level_flags(or_ctx *c, int d, int n, int8_t *out6)
+{
+    int m[3];
+    level_state(c, d, n, m);
+    size_t nf = (size_t)(c->nx + 2) * (size_t)(c->ny + 2) * (size_t)(c->nz + 2);
+    for (int s = 0; s < 6; ++s) memcpy(out6 + (size_t)s * nf, c->flMG[s], nf);
+}
+
+void or_itsolv_level(or_ctx *c, int d, int n, double *var, const double *r)
+{
+    int m[3], lev[3] = {1, 1, 1};
+    lev[d] = n;
+    level_state(c, d, n, m);
+    mg_itsolv(c, var, r, lev[0], lev[1], lev[2], m[0], m[1], m[2]);
+}
+
+void or_residual_level(or_ctx *c, int d, int n, const double *var, const double *r, double *res)
+{
+    int m[3], lev[3] = {1, 1, 1};
+    lev[d] = n;
+    level_state(c, d, n, m);
+    mg_residual(c, var, r, res, lev[0], lev[1], lev[2], m[0], m[1], m[2]);
+}
+
+void or_restrict_level(or_ctx *c, int d, int n, const double *res, double *r1)
+{
+    int m[3];
+    level_state(c, d, n, m);
+    mg_restrict(c, d, res, r1, n, m[0], m[1], m[2], c->mgrid[d][n + 1] + 1);
+}
+
+void or_prolong_level(or_ctx *c, int d, int n, const double *phi, double *corr)
+{
+    int m[3];
+    level_state(c, d, n, m);
+    int m1 = c->mgrid[d][n + 1] + 1;
+    int fm[3] = {m[0], m[1], m[2]};
+    fm[d] = m1;
+    c->ibMG = ib_view(c, d, n + 1);
+    mg_prolong(c, d, corr, phi, n, fm[0], fm[1], fm[2], m1, m[d]);
+}
