@@ -117,14 +117,23 @@ class ClockSampler:
 def build_problem(n, seed, tol, solver_cls):
     from flow_structure_interaction_fem_ibm_gb300 import problem as P
     pr = P.sphere(n, seed=seed, stretch=1.5)
-    # discrete compatibility shift from two stalled FP64 GPU solves
+    # discrete compatibility shift from two GPU solves run to their residual plateau
     def stagnated(f):
         saved = (pr.params.iterMax_Poisson, pr.params.restol_Poisson, pr.params.precision_mode)
-        pr.params.iterMax_Poisson, pr.params.restol_Poisson, pr.params.precision_mode = 30, 0.0, 0
-        s = solver_cls(pr.params, pr.x, pr.y, pr.z).set_boundary(pr.geom)
-        p = np.zeros(pr.shape, order="F")
-        s.solve_poisson(p, f)
-        s.close()
+        pr.params.restol_Poisson, pr.params.precision_mode = 0.0, 1
+        solvers = {}
+
+        def chunk_fn(rhs, p0, iters):
+            pr.params.iterMax_Poisson = iters
+            s = solvers.get(iters)
+            if s is None:
+                s = solvers[iters] = solver_cls(pr.params, pr.x, pr.y, pr.z).set_boundary(pr.geom)
+            s.solve_poisson(p0, rhs)
+            return p0, s.residual_history()
+
+        p = P.stall_until_plateau(chunk_fn, f, pr.shape, chunk=25)
+        for s in solvers.values():
+            s.close()
         pr.params.iterMax_Poisson, pr.params.restol_Poisson, pr.params.precision_mode = saved
         return p
     shift = P.make_compatible(pr, stagnated)
@@ -158,7 +167,13 @@ def oracle_iterations(n, seed, tol):
 
     def stagnated(f):
         q = P.Problem(pr.params, pr.x, pr.y, pr.z, pr.geom, f, pr.name)
-        return Oracle(q, iterMax_Poisson=30, restol_Poisson=0.0).solve()["p"]
+
+        def chunk_fn(rhs, p0, iters):
+            q.nlu0 = rhs
+            r = Oracle(q, iterMax_Poisson=iters, restol_Poisson=0.0).solve(p0)
+            return r["p"], r["hist"]
+
+        return P.stall_until_plateau(chunk_fn, f, pr.shape, chunk=30)
 
     P.make_compatible(pr, stagnated)
     pr.params.restol_Poisson = tol * float(np.abs(pr.nlu0).max())

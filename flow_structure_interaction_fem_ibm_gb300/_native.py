@@ -36,9 +36,10 @@ SOLVER_SYMBOLS = {
     "fsi_mg_get_pgrad": [ctypes.c_void_p, c_double_p],
     "fsi_mg_level_count": [ctypes.c_void_p, ctypes.c_int],
     "fsi_mg_level_size": [ctypes.c_void_p, ctypes.c_int, ctypes.c_int],
-    "fsi_mg_debug_level_op": [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int,
+    "fsi_mg_debug_level_op": [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_int,
                               ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p],
     "fsi_mg_stats": [ctypes.c_void_p, c_double_p, ctypes.c_int],
+    "fsi_mg_residual_history": [ctypes.c_void_p, c_double_p, ctypes.c_int],
     "fsi_mg_time_kernel": [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_int, c_double_p, c_double_p],
     "fsi_mg_last_error": [],
     "fsi_mg_destroy": [ctypes.c_void_p],

@@ -120,6 +120,7 @@ struct Ctx {
     const double *graph_b = nullptr;
 
     // stats
+    std::vector<double> hist;   // max-norm residual after each outer iteration of the last solve
     int last_iters = 0;
     double last_maxres = 0, last_time = 0, last_wall = 0;
     long long ghost_sweeps = 0;
@@ -621,12 +622,14 @@ int solve_device(Ctx &c, double *p, const double *b, int *iters, double *maxres_
     int iter = 0;
     double maxres = 1.0e10;
     long long maxidx = 0;
+    c.hist.clear();
     while (iter < c.p.iterMax_Poisson && maxres > c.p.restol_Poisson) {
         TRY(run_outer(c, p, b));
         CK(cudaMemcpyAsync(c.h_result, c.result, sizeof(MaxLoc), cudaMemcpyDeviceToHost, c.s));
         CK(cudaStreamSynchronize(c.s));
         maxres = c.h_result->v;
         maxidx = c.h_result->i;
+        c.hist.push_back(maxres);
         ++iter;
         if (!std::isfinite(maxres)) break;
     }
@@ -1272,6 +1275,16 @@ int fsi_mg_time_kernel(void *handle, int which, int precision, int reps, double 
         *alg_bytes = bpc * cells;
     }
     return 0;
+}
+
+int fsi_mg_residual_history(void *handle, double *out, int cap)
+{
+    if (!handle) return fail(-1, "null handle");
+    Ctx &c = *(Ctx *)handle;
+    const int n = (int)c.hist.size();
+    if (out)
+        for (int q = 0; q < n && q < cap; ++q) out[q] = c.hist[q];
+    return n;
 }
 
 int fsi_mg_stats(void *handle, double *out, int n)

@@ -437,8 +437,9 @@ __global__ void k_maxloc_final(const MaxLoc *partials, int n, MaxLoc *out)
 // ---------------------------------------------------------------------------
 __device__ __forceinline__ double block_sum(double x)
 {
+    // sized for the largest block that calls it (1024 threads = 32 warps)
     for (int off = 16; off > 0; off >>= 1) x += __shfl_xor_sync(0xffffffffu, x, off);
-    __shared__ double s[TPB / 32];
+    __shared__ double s[32];
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
     __syncthreads();
     if (lane == 0) s[wid] = x;
@@ -547,11 +548,15 @@ __global__ void __launch_bounds__(TPB) k_compat_partial(CompatArgs A, double *pa
     if (threadIdx.x == 0) partials[blockIdx.x] = s;
 }
 
-__global__ void k_pgrad_shift(double *pg, long long off, long long n, const double *flux, double outflow_area,
+// the reference shifts the plane over (0:n_a, 0:n_b), not its last row/column
+// (IBM/GCM_GLOBAL_MASS_CONSERVE.F90:340-361)
+__global__ void k_pgrad_shift(double *pg, long long off, int sa, int sb, const double *flux, double outflow_area,
                               double sign)
 {
     long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= n) return;
+    if (t >= (long long)sa * sb) return;
+    const int a = (int)(t % sa), b = (int)(t / sa);
+    if (a > sa - 2 || b > sb - 2) return;
     const double corr = -flux[0] / outflow_area;
     pg[off + t] = pg[off + t] + sign * corr;
 }
@@ -763,10 +768,12 @@ void launch_compat(const double *p, const uint8_t *fl, const double *pg, const d
     const long long px = (long long)(ny + 2) * (nz + 2), py = (long long)(nx + 2) * (nz + 2),
                     pz = (long long)(nx + 2) * (ny + 2);
     const long long sizes[6] = {px, px, py, py, pz, pz};
+    const int sa[6] = {ny + 2, ny + 2, nx + 2, nx + 2, nx + 2, nx + 2};
+    const int sb[6] = {nz + 2, nz + 2, nz + 2, nz + 2, ny + 2, ny + 2};
     const double signs[6] = {-1.0, 1.0, -1.0, 1.0, -1.0, 1.0};
     for (int q = 0; q < 6; ++q)
         if (bc_zero_grad[q])
-            k_pgrad_shift<<<nblk(sizes[q]), TPB, 0, s>>>(pgrad, A.off[q], sizes[q], flux, outflow_area, signs[q]);
+            k_pgrad_shift<<<nblk(sizes[q]), TPB, 0, s>>>(pgrad, A.off[q], sa[q], sb[q], flux, outflow_area, signs[q]);
 }
 
 void launch_nlw0(double *nlw0, const uint8_t *fl, const int side_flag[6], const double *pgrad, const double *dxinv,

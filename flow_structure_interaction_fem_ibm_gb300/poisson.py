@@ -169,6 +169,12 @@ class PoissonSolver:
         return dict(iters=int(out[0]), maxres=out[1], seconds=out[2], ghost_sweeps=int(out[3]),
                     launches=int(out[4]), device_bytes=int(out[5]), wall_seconds=out[6], e2e_seconds=out[7])
 
+    def residual_history(self):
+        n = _check(self.lib.fsi_mg_residual_history(self.h, None, 0))
+        out = np.zeros(max(n, 1))
+        self.lib.fsi_mg_residual_history(self.h, _p(out), n)
+        return out[:n]
+
     def time_kernel(self, which: int, precision: int, reps: int = 20):
         """Average device time (ms) of one kernel and its algorithmic bytes per launch."""
         ms, nb = ctypes.c_double(), ctypes.c_double()
@@ -184,7 +190,8 @@ def solve(problem, p0=None, **overrides):
     s = PoissonSolver(params, problem.x, problem.y, problem.z).set_boundary(problem.geom)
     p = np.zeros(problem.shape, order="F") if p0 is None else np.array(p0, order="F", copy=True)
     st, it, mr, loc, ct, nlw0 = s.solve_poisson(p, problem.nlu0, want_nlw0=True)
-    res = dict(p=p, status=st, iters=it, maxres=mr, loc=loc, seconds=ct, nlw0=nlw0, stats=s.stats())
+    res = dict(p=p, status=st, iters=it, maxres=mr, loc=loc, seconds=ct, nlw0=nlw0, stats=s.stats(),
+               hist=s.residual_history())
     s.close()
     return res
 

@@ -318,6 +318,24 @@ def compatibility_shift(problem: Problem, stagnated_pressure) -> float:
     return 0.0 if den == 0.0 else -float((r0 * r1).sum()) / den
 
 
+def stall_until_plateau(solve_chunk, f, shape, chunk: int = 25, max_chunks: int = 60, rtol: float = 1e-10):
+    """Iterate an inconsistent solve in warm-started chunks until the max-norm
+    residual stops changing.  ``solve_chunk(f, p, iters) -> (p, history)`` runs
+    ``iters`` outer iterations from ``p``.  MG contracts everything but the
+    inconsistent component at its convergence rate, so the residual history
+    approaches a plateau geometrically; stop when one chunk moves it by less
+    than ``rtol`` relative."""
+    p = np.zeros(shape, order="F")
+    prev = None
+    for _ in range(max_chunks):
+        p, hist = solve_chunk(f, p, chunk)
+        last = float(hist[-1])
+        if prev is not None and abs(last - prev) <= rtol * max(last, 1e-300):
+            break
+        prev = last
+    return p
+
+
 def make_compatible(problem: Problem, stagnated_pressure) -> float:
     c = compatibility_shift(problem, stagnated_pressure)
     problem.nlu0 += c * fluid_indicator(problem)

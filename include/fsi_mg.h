@@ -132,6 +132,11 @@ int fsi_mg_debug_level_op(void *handle, int op, int d, int n, void *a, void *b, 
  * host-buffer solve including its host<->device copies. */
 int fsi_mg_stats(void *handle, double *out, int n);
 
+/* Max-norm residual after each outer iteration of the last solve (the values
+ * the reference prints per iteration, IBM/CORE_POISSON.F90:657-659).  Writes
+ * up to cap values into out (may be NULL) and returns the iteration count. */
+int fsi_mg_residual_history(void *handle, double *out, int cap);
+
 /* Time one kernel of the level-1 hierarchy on the handle's stream with CUDA
  * events, averaged over reps launches (after one warm-up launch), on the
  * current staging fields.  which: 0/1/2 one colour of the x/y/z line sweep,

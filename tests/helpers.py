@@ -9,13 +9,21 @@ from flow_structure_interaction_fem_ibm_gb300 import problem as P
 from oracle.oracle import Oracle
 
 
-def oracle_stagnated(problem, iters=30):
+def oracle_stagnated(problem, chunk=30):
+    """Stalled oracle pressure for the compatibility shift (runs to the plateau)."""
     def run(f):
         q = P.Problem(problem.params, problem.x, problem.y, problem.z, problem.geom, f, problem.name)
         saved = (problem.params.iterMax_Poisson, problem.params.restol_Poisson, problem.params.iRedBlack,
                  problem.params.coarse_flag_mode)
-        o = Oracle(q, iterMax_Poisson=iters, restol_Poisson=0.0, iRedBlack=0, coarse_flag_mode=0)
-        p = o.solve()["p"]
+
+        def chunk_fn(rhs, p0, iters):
+            q.nlu0 = rhs
+            o = Oracle(q, iterMax_Poisson=iters, restol_Poisson=0.0, iRedBlack=0, coarse_flag_mode=0)
+            r = o.solve(p0)
+            o.close()
+            return r["p"], r["hist"]
+
+        p = P.stall_until_plateau(chunk_fn, f, problem.shape, chunk=chunk)
         (problem.params.iterMax_Poisson, problem.params.restol_Poisson, problem.params.iRedBlack,
          problem.params.coarse_flag_mode) = saved
         return p
