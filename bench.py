@@ -51,6 +51,8 @@ def parse():
     ap.add_argument("--seed", type=int, default=3)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--profile", action="store_true",
+                    help="profiling driver: raw RHS, two outer iterations of each precision, no other work")
     return ap.parse_args()
 
 
@@ -249,6 +251,20 @@ def main():
     if world > 1:
         torch.distributed.barrier()
     from flow_structure_interaction_fem_ibm_gb300.poisson import PoissonSolver
+
+    if args.profile:
+        import copy
+        from flow_structure_interaction_fem_ibm_gb300 import problem as P
+        pr = P.sphere(args.n, seed=args.seed, stretch=1.5)
+        for mode in (1, 0):
+            pp = copy.deepcopy(pr.params)
+            pp.precision_mode, pp.iterMax_Poisson, pp.restol_Poisson = mode, 2, 0.0
+            s = PoissonSolver(pp, pr.x, pr.y, pr.z).set_boundary(pr.geom)
+            p = np.zeros(pr.shape, order="F")
+            s.solve_poisson(p, pr.nlu0)
+            print(json.dumps({"profile": True, "precision_mode": mode, "stats": s.stats()}))
+            s.close()
+        return
 
     t_setup = time.perf_counter()
     pr, shift = build_problem(args.n, args.seed, args.tol, PoissonSolver)

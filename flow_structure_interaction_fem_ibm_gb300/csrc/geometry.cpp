@@ -337,19 +337,33 @@ int fsi_geom_gcm_coeffs(int nx, int ny, int nz, const double *x, const double *y
         if (ci < 0 || cj < 0 || ck < 0) return -(n + 1);
         iCI[n] = ci; jCI[n] = cj; kCI[n] = ck;
         V3 bn = nrm[celem];
+        // The reference builds the Vandermonde matrix in absolute coordinates
+        // (IBM/GCM_SET_BOUNDARY.F90:392-440), which loses about log10(1/h^3)
+        // digits on fine cells, so the weights of a constant no longer sum to 1
+        // and the all-Neumann operator stops being singular.  The same trilinear
+        // interpolant is evaluated here in coordinates local to the stencil,
+        // scaled by its cell sizes: identical weights, no cancellation.
+        const double ox = xc[ci], oy = yc[cj], oz = zc[ck];
+        const double sx = xc[ci + 1] - xc[ci], sy = yc[cj + 1] - yc[cj], sz = zc[ck + 1] - zc[ck];
+        auto lx = [&](double v) { return (v - ox) / sx; };
+        auto ly = [&](double v) { return (v - oy) / sy; };
+        auto lz = [&](double v) { return (v - oz) / sz; };
         double V[64];
         for (int r = 0; r < 8; ++r) {
             int i = ci + incI[r], j = cj + incJ[r], k = ck + incK[r];
-            double x1 = xc[i], x2 = yc[j], x3 = zc[k];
+            double x1 = lx(xc[i]), x2 = ly(yc[j]), x3 = lz(zc[k]);
             if (i == g_i && j == g_j && k == g_k) {
-                double a1 = bip.x, a2 = bip.y, a3 = bip.z;
-                V[r + 8 * 0] = bn.x * a2 * a3 + bn.y * a1 * a3 + bn.z * a1 * a2;
-                V[r + 8 * 1] = bn.x * a2 + bn.y * a1;
-                V[r + 8 * 2] = bn.x * a3 + bn.z * a1;
-                V[r + 8 * 3] = bn.y * a3 + bn.z * a2;
-                V[r + 8 * 4] = bn.x;
-                V[r + 8 * 5] = bn.y;
-                V[r + 8 * 6] = bn.z;
+                // Neumann row: n . grad in local coordinates (d/dx = (1/sx) d/dx'); its
+                // right-hand side is uNormal = 0, so the row scale does not matter.
+                double a1 = lx(bip.x), a2 = ly(bip.y), a3 = lz(bip.z);
+                const V3 bn_l{bn.x / sx, bn.y / sy, bn.z / sz};
+                V[r + 8 * 0] = bn_l.x * a2 * a3 + bn_l.y * a1 * a3 + bn_l.z * a1 * a2;
+                V[r + 8 * 1] = bn_l.x * a2 + bn_l.y * a1;
+                V[r + 8 * 2] = bn_l.x * a3 + bn_l.z * a1;
+                V[r + 8 * 3] = bn_l.y * a3 + bn_l.z * a2;
+                V[r + 8 * 4] = bn_l.x;
+                V[r + 8 * 5] = bn_l.y;
+                V[r + 8 * 6] = bn_l.z;
                 V[r + 8 * 7] = 0.0;
             } else {
                 V[r + 8 * 0] = x1 * x2 * x3;
@@ -363,7 +377,8 @@ int fsi_geom_gcm_coeffs(int nx, int ny, int nz, const double *x, const double *y
             }
         }
         if (!inv8(V)) return -(n + 1);
-        double phi[8] = {ipt.x * ipt.y * ipt.z, ipt.x * ipt.y, ipt.x * ipt.z, ipt.y * ipt.z, ipt.x, ipt.y, ipt.z, 1.0};
+        const double px = lx(ipt.x), py = ly(ipt.y), pz = lz(ipt.z);
+        double phi[8] = {px * py * pz, px * py, px * pz, py * pz, px, py, pz, 1.0};
         for (int r = 0; r < 8; ++r) {
             double s = 0.0;
             for (int m = 0; m < 8; ++m) s += V[m + 8 * r] * phi[m];

@@ -69,6 +69,6 @@ def test_image_point_coefficients_reproduce_trilinear_fields():
         selfrow = [(c == [g.iG[n], g.jG[n], g.kG[n]]).all() for c in cells]
         w = g.coeff[:, n]
         others = ~np.array(selfrow)
-        assert abs(w[others].sum() - 1.0) < 1e-9
+        assert abs(w[others].sum() - 1.0) < 1e-12   # constants reproduced: the Neumann operator stays singular
         assert g.probe[n] > 0
     assert np.isfinite(g.coeff).all()
