@@ -15,6 +15,7 @@
 #include <chrono>
 #include <cmath>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <memory>
 #include <string>
@@ -713,6 +714,11 @@ int fsi_mg_create(const fsi_mg_params *params, const double *x, const double *y,
     if (p.precision_mode != 0 && p.precision_mode != 1) return fail(-1, "precision_mode must be 0 or 1");
     int ndev = 0;
     if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return fail(-12, "no CUDA device");
+    CK(init_kernels());
+    {   // FSI_MG_LINE_KERNEL=thread selects the one-thread-per-line smoother (A/B measurements)
+        const char *lk = std::getenv("FSI_MG_LINE_KERNEL");
+        set_line_kernel(lk && std::strcmp(lk, "thread") == 0);
+    }
     auto c = std::make_unique<Ctx>();
     c->p = p;
     c->nx = p.nx; c->ny = p.ny; c->nz = p.nz;

@@ -115,6 +115,215 @@ __global__ void __launch_bounds__(TPB) k_line(LineArgs<T> A)
 }
 
 // ---------------------------------------------------------------------------
+// Red-black line relaxation, warp-per-line partition solver (same arithmetic
+// role as k_line: IBM/CORE_MG.F90:1883-2270 with the TDMA of
+// IBM/CORE_TDMA.F90:10-34).  A CTA of 8 warps relaxes 8 lines of one colour.
+//  1. Staging: coalesced loads build each row's tridiagonal coefficients
+//     (a, b, c) and right-hand side d exactly as MG_itsolv does (masking,
+//     ghost/identity rows, finest-level Dirichlet terms) into shared memory,
+//     padded so that later per-lane segment reads are bank-conflict free.
+//     x-lines: one warp stages one line, lanes along the line.  y/z-lines:
+//     one warp stages 4 rows x 8 neighbouring lines.
+//  2. Solve: lane l owns the S = L/32 contiguous rows [lS, lS+S).  Each lane
+//     eliminates its segment in registers, expressing the interior unknowns
+//     through the previous lane's last unknown and its own last unknown; the
+//     32 last unknowns form a tridiagonal system solved by parallel cyclic
+//     reduction over warp shuffles (5 steps); lanes then back-substitute.
+//  3. Store: relaxation var = var (1-omega) + omega x, coalesced per row.
+// ---------------------------------------------------------------------------
+constexpr int WP_LINES = 8;
+
+template <int S> __host__ __device__ constexpr int wp_pitch() { return 32 * (S + 1) + 4; }
+
+template <typename T>
+__device__ __forceinline__ void pcr_step(T &A, T &B, T &C, T &D, int lane, int h)
+{
+    T Am = __shfl_up_sync(0xffffffffu, A, h), Bm = __shfl_up_sync(0xffffffffu, B, h);
+    T Cm = __shfl_up_sync(0xffffffffu, C, h), Dm = __shfl_up_sync(0xffffffffu, D, h);
+    T Ap = __shfl_down_sync(0xffffffffu, A, h), Bp = __shfl_down_sync(0xffffffffu, B, h);
+    T Cp = __shfl_down_sync(0xffffffffu, C, h), Dp = __shfl_down_sync(0xffffffffu, D, h);
+    if (lane < h) { Am = T(0); Bm = T(1); Cm = T(0); Dm = T(0); }
+    if (lane + h > 31) { Ap = T(0); Bp = T(1); Cp = T(0); Dp = T(0); }
+    const T k1 = A / Bm, k2 = C / Bp;
+    const T nA = -k1 * Am, nC = -k2 * Cp;
+    const T nB = B - k1 * Cm - k2 * Ap;
+    const T nD = D - k1 * Dm - k2 * Dp;
+    A = nA; B = nB; C = nC; D = nD;
+}
+
+template <typename T, int DIR, int S, bool OMEGA1>
+__global__ void __launch_bounds__(256) k_line_wp(LineArgs<T> A)
+{
+    using X = Axes<DIR>;
+    extern __shared__ unsigned char smem_raw[];
+    T *sm = reinterpret_cast<T *>(smem_raw);
+    constexpr int RP = wp_pitch<S>();
+    T *sa = sm, *sb = sm + WP_LINES * RP, *sc = sm + 2 * WP_LINES * RP, *sd = sm + 3 * WP_LINES * RP;
+    const Dims &d = A.d;
+    const int nb = d.m[X::b] - 1, nc = d.m[X::c] - 1, L = d.m[X::a] - 1;
+    const int hb = (nb + 1) >> 1;
+    const long long nlines = (long long)hb * nc;
+    const long long sa_ = stride_of(d, X::a), sb_ = stride_of(d, X::b), sc_ = stride_of(d, X::c);
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+
+    // line g of this CTA -> (p, q); invalid lines (beyond the count or p > nb) are skipped
+    auto line_pq = [&](int g, int &p, int &q) -> bool {
+        const long long t = (long long)blockIdx.x * WP_LINES + g;
+        if (t >= nlines) return false;
+        q = 1 + (int)(t / hb);
+        const int p0 = (((1 + q) & 1) == A.colour) ? 1 : 2;
+        p = p0 + 2 * (int)(t % hb);
+        return p <= nb;
+    };
+    auto sidx = [&](int g, int r) { return g * RP + r + r / S; };
+
+    // ---- 1. staging ----
+    auto stage = [&](int g, int r) {   // r: 0-based row along the line (row index r+1)
+        int p, q;
+        if (!line_pq(g, p, q)) return;
+        const int i = r + 1;
+        const long long o = (long long)p * sb_ + (long long)q * sc_ + (long long)i * sa_;
+        const uint8_t f = A.fl[o];
+        const bool fluid = !(f & FB_IB);
+        const T ama = (f & fb_minus(X::a)) ? T(0) : A.c.cm[X::a][i];
+        const T apa = (f & fb_plus(X::a)) ? T(0) : A.c.cp[X::a][i];
+        const T amb = (f & fb_minus(X::b)) ? T(0) : A.c.cm[X::b][p];
+        const T apb = (f & fb_plus(X::b)) ? T(0) : A.c.cp[X::b][p];
+        const T amc = (f & fb_minus(X::c)) ? T(0) : A.c.cm[X::c][q];
+        const T apc = (f & fb_plus(X::c)) ? T(0) : A.c.cp[X::c][q];
+        const bool allzero = (ama == T(0)) & (apa == T(0)) & (amb == T(0)) & (apb == T(0)) & (amc == T(0)) & (apc == T(0));
+        const bool normal = fluid && !allzero;
+        T aa = T(0), bb = T(1), cc = T(0), dd;
+        if (normal) {
+            T sdd = A.r[o];
+            if (X::c_first) {
+                sdd = sdd - A.v[o - sc_] * amc;
+                sdd = sdd - A.v[o + sc_] * apc;
+                sdd = sdd - A.v[o - sb_] * amb;
+                sdd = sdd - A.v[o + sb_] * apb;
+            } else {
+                sdd = sdd - A.v[o - sb_] * amb;
+                sdd = sdd - A.v[o + sb_] * apb;
+                sdd = sdd - A.v[o - sc_] * amc;
+                sdd = sdd - A.v[o + sc_] * apc;
+            }
+            dd = sdd;
+            // diagonal as the reference sums it: (acx + acy) + acz
+            T am3[3], ap3[3];
+            am3[X::a] = ama; ap3[X::a] = apa; am3[X::b] = amb; ap3[X::b] = apb; am3[X::c] = amc; ap3[X::c] = apc;
+            bb = (-(am3[0] + ap3[0]) + -(am3[1] + ap3[1])) + -(am3[2] + ap3[2]);
+            aa = ama;
+            cc = apa;
+        } else {
+            dd = ((f & FB_GM) || fluid) ? A.v[o] : T(0);
+        }
+        if (i == 1 && A.dir_lo) dd = dd - A.ppp_lo * aa;
+        if (i == L && A.dir_hi) dd = dd - A.ppp_hi * cc;
+        if (i == 1) aa = T(0);   // tdma ignores a(n1) and c(n2)
+        if (i == L) cc = T(0);
+        const int si = sidx(g, r);
+        sa[si] = aa; sb[si] = bb; sc[si] = cc; sd[si] = dd;
+    };
+    if (DIR == 0) {
+        for (int r0 = 0; r0 < L; r0 += 32)
+            if (r0 + lane < L) stage(warp, r0 + lane);
+    } else {
+        const int g = tid & (WP_LINES - 1), rr = tid >> 3;   // 32 rows x 8 lines per pass
+        for (int r0 = 0; r0 < L; r0 += 32)
+            if (r0 + rr < L) stage(g, r0 + rr);
+    }
+    __syncthreads();
+
+    // ---- 2. solve (warp = line) ----
+    {
+        const int g = warp;
+        int p, q;
+        const bool valid = line_pq(g, p, q);
+        T a[S], b[S], c[S], dv[S];
+#pragma unroll
+        for (int s2 = 0; s2 < S; ++s2) {
+            const int r = lane * S + s2;
+            if (valid && r < L) {
+                const int si = sidx(g, r);
+                a[s2] = sa[si]; b[s2] = sb[si]; c[s2] = sc[si]; dv[s2] = sd[si];
+            } else {
+                a[s2] = T(0); b[s2] = T(1); c[s2] = T(0); dv[s2] = T(0);
+            }
+        }
+        // segment elimination: rows 0..S-2 in terms of XL (previous lane's last) and XR (own last)
+        T y[S], u[S], w[S], gg[S];
+        {
+            T gp = T(0), yp = T(0), up = T(0), wp = T(0);
+#pragma unroll
+            for (int s2 = 0; s2 < S - 1; ++s2) {
+                const T inv = T(1) / (b[s2] - a[s2] * gp);
+                y[s2] = (dv[s2] - a[s2] * yp) * inv;
+                u[s2] = ((s2 == 0 ? -a[0] : T(0)) - a[s2] * up) * inv;
+                w[s2] = ((s2 == S - 2 ? -c[S - 2] : T(0)) - a[s2] * wp) * inv;
+                gg[s2] = c[s2] * inv;
+                gp = gg[s2]; yp = y[s2]; up = u[s2]; wp = w[s2];
+            }
+#pragma unroll
+            for (int s2 = S - 3; s2 >= 0; --s2) {
+                y[s2] = y[s2] - gg[s2] * y[s2 + 1];
+                u[s2] = u[s2] - gg[s2] * u[s2 + 1];
+                w[s2] = w[s2] - gg[s2] * w[s2 + 1];
+            }
+        }
+        const T y0 = (S >= 2) ? y[0] : T(0), u0 = (S >= 2) ? u[0] : T(0), w0 = (S >= 2) ? w[0] : T(1);
+        const T yl = (S >= 2) ? y[S - 2 < 0 ? 0 : S - 2] : T(0);
+        const T ul = (S >= 2) ? u[S - 2 < 0 ? 0 : S - 2] : T(1);
+        const T wl = (S >= 2) ? w[S - 2 < 0 ? 0 : S - 2] : T(0);
+        const T y0n = __shfl_down_sync(0xffffffffu, y0, 1);
+        const T u0n = __shfl_down_sync(0xffffffffu, u0, 1);
+        const T w0n = __shfl_down_sync(0xffffffffu, w0, 1);
+        const T an = a[S - 1], bn = b[S - 1], cn = c[S - 1];
+        T RA = an * ul;
+        T RB = bn + an * wl + cn * u0n;
+        T RC = cn * w0n;
+        T RD = dv[S - 1] - an * yl - cn * y0n;
+        if (lane == 31) { RB = bn + an * wl; RC = T(0); RD = dv[S - 1] - an * yl; }
+#pragma unroll
+        for (int h = 1; h < 32; h <<= 1) pcr_step(RA, RB, RC, RD, lane, h);
+        const T XR = RD / RB;
+        T XL = __shfl_up_sync(0xffffffffu, XR, 1);
+        if (lane == 0) XL = T(0);
+        // ---- 3. solution into shared memory (reuse sd) ----
+        __syncwarp();
+#pragma unroll
+        for (int s2 = 0; s2 < S; ++s2) {
+            const int r = lane * S + s2;
+            if (valid && r < L) {
+                const T x = (s2 < S - 1) ? (y[s2 < S - 1 ? s2 : 0] + XL * u[s2 < S - 1 ? s2 : 0] + XR * w[s2 < S - 1 ? s2 : 0]) : XR;
+                sd[sidx(g, r)] = x;
+            }
+        }
+    }
+    __syncthreads();
+
+    // ---- 4. store with relaxation ----
+    auto store = [&](int g, int r) {
+        int p, q;
+        if (!line_pq(g, p, q)) return;
+        const int i = r + 1;
+        const long long base = (long long)p * sb_ + (long long)q * sc_;
+        const long long o = base + (long long)i * sa_;
+        const T x = sd[sidx(g, r)];
+        A.v[o] = OMEGA1 ? x : A.v[o] * (T(1) - A.omega) + A.omega * x;
+        if (i == 1 && A.dir_lo) A.v[base] = A.ppp_lo;
+        if (i == L && A.dir_hi) A.v[base + (long long)(L + 1) * sa_] = A.ppp_hi;
+    };
+    if (DIR == 0) {
+        for (int r0 = 0; r0 < L; r0 += 32)
+            if (r0 + lane < L) store(warp, r0 + lane);
+    } else {
+        const int g = tid & (WP_LINES - 1), rr = tid >> 3;
+        for (int r0 = 0; r0 < L; r0 += 32)
+            if (r0 + rr < L) store(g, r0 + rr);
+    }
+}
+
+// ---------------------------------------------------------------------------
 // Line factorisation (setup).  Coefficients exactly as MG_itsolv builds them
 // (IBM/CORE_MG.F90:1950-1983) and the Thomas recurrences of tdma
 // (IBM/CORE_TDMA.F90:24-28) without contraction, so the factors match a
@@ -649,12 +858,69 @@ __global__ void k_coarse_flags(uint8_t *fl, Dims d, int sb0, int sb1, int sb2, i
 } // namespace
 
 // ------------------------------------------------------------- launchers --
+template <typename T, int DIR, int S, bool O1>
+size_t wp_smem() { return 4 * (size_t)WP_LINES * wp_pitch<S>() * sizeof(T); }
+
+template <typename T, int DIR, int S, bool O1>
+void launch_wp_one(const LineArgs<T> &a, long long nlines, cudaStream_t s)
+{
+    const long long blocks = (nlines + WP_LINES - 1) / WP_LINES;
+    k_line_wp<T, DIR, S, O1><<<(unsigned)blocks, 256, wp_smem<T, DIR, S, O1>(), s>>>(a);
+}
+
+template <typename T, int DIR, int S>
+cudaError_t wp_attr()
+{
+    cudaError_t e = cudaFuncSetAttribute(k_line_wp<T, DIR, S, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)wp_smem<T, DIR, S, true>());
+    if (e != cudaSuccess) return e;
+    return cudaFuncSetAttribute(k_line_wp<T, DIR, S, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                (int)wp_smem<T, DIR, S, false>());
+}
+
+template <typename T, int DIR>
+cudaError_t wp_attr_dir()
+{
+    cudaError_t e;
+    if ((e = wp_attr<T, DIR, 1>()) != cudaSuccess) return e;
+    if ((e = wp_attr<T, DIR, 2>()) != cudaSuccess) return e;
+    if ((e = wp_attr<T, DIR, 4>()) != cudaSuccess) return e;
+    if ((e = wp_attr<T, DIR, 8>()) != cudaSuccess) return e;
+    return wp_attr<T, DIR, 16>();
+}
+
+template <typename T, int DIR, bool O1>
+bool launch_wp_dir(const LineArgs<T> &a, int L, long long nlines, cudaStream_t s)
+{
+    if (L <= 32) launch_wp_one<T, DIR, 1, O1>(a, nlines, s);
+    else if (L <= 64) launch_wp_one<T, DIR, 2, O1>(a, nlines, s);
+    else if (L <= 128) launch_wp_one<T, DIR, 4, O1>(a, nlines, s);
+    else if (L <= 256) launch_wp_one<T, DIR, 8, O1>(a, nlines, s);
+    else if (L <= 512) launch_wp_one<T, DIR, 16, O1>(a, nlines, s);
+    else return false;
+    return true;
+}
+
+bool g_line_thread_per_line = false;   // selects the sequential-Thomas kernel (kept for lines > 512 cells)
+
 template <typename T>
 void launch_line(int dir, const LineArgs<T> &a, bool omega_one, cudaStream_t s)
 {
     static const int ob[3] = {1, 0, 0}, oc[3] = {2, 2, 1};
     const int nb = a.d.m[ob[dir]] - 1, nc = a.d.m[oc[dir]] - 1;
     const long long n = (long long)((nb + 1) / 2) * nc;
+    const int L = a.d.m[dir] - 1;
+    if (!g_line_thread_per_line && L <= 512) {
+        bool ok;
+        if (omega_one) {
+            ok = (dir == 0) ? launch_wp_dir<T, 0, true>(a, L, n, s)
+               : (dir == 1) ? launch_wp_dir<T, 1, true>(a, L, n, s) : launch_wp_dir<T, 2, true>(a, L, n, s);
+        } else {
+            ok = (dir == 0) ? launch_wp_dir<T, 0, false>(a, L, n, s)
+               : (dir == 1) ? launch_wp_dir<T, 1, false>(a, L, n, s) : launch_wp_dir<T, 2, false>(a, L, n, s);
+        }
+        if (ok) return;
+    }
     const int g = nblk(n);
 #define L_(D, O) k_line<T, D, O><<<g, TPB, 0, s>>>(a)
     if (omega_one) {
@@ -809,6 +1075,21 @@ void launch_coarse_flags(uint8_t *fl, const Dims &d, const int sb[6], cudaStream
     const long long n = (long long)(d.m[0] - 1) * (d.m[1] - 1) * (d.m[2] - 1);
     k_coarse_flags<<<nblk(n), TPB, 0, s>>>(fl, d, sb[0], sb[1], sb[2], sb[3], sb[4], sb[5]);
 }
+
+cudaError_t init_kernels()
+{
+    // dynamic shared memory above 48 KB needs an opt-in per kernel; done once per
+    // process before any launch (and outside any stream capture)
+    cudaError_t e;
+    if ((e = wp_attr_dir<float, 0>()) != cudaSuccess) return e;
+    if ((e = wp_attr_dir<float, 1>()) != cudaSuccess) return e;
+    if ((e = wp_attr_dir<float, 2>()) != cudaSuccess) return e;
+    if ((e = wp_attr_dir<double, 0>()) != cudaSuccess) return e;
+    if ((e = wp_attr_dir<double, 1>()) != cudaSuccess) return e;
+    return wp_attr_dir<double, 2>();
+}
+
+void set_line_kernel(int thread_per_line) { g_line_thread_per_line = thread_per_line != 0; }
 
 // explicit instantiations
 template void launch_line<double>(int, const LineArgs<double> &, bool, cudaStream_t);

@@ -82,6 +82,11 @@ struct GhostArgs {
     const long long *sidx;   // 8 stencil indices per ghost, -1 = the ghost itself (uNormal term)
 };
 
+// one-time kernel attributes (call before the first launch, outside stream capture)
+cudaError_t init_kernels();
+// 0: warp-per-line partition solver (default, lines up to 512 cells), 1: one thread per line
+void set_line_kernel(int thread_per_line);
+
 // ---- launchers (all asynchronous on the given stream) ----
 template <typename T>
 void launch_line(int dir, const LineArgs<T> &a, bool omega_one, cudaStream_t s);

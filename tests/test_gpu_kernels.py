@@ -24,6 +24,9 @@ def cases():
         ("sphere16_tanh", lambda: sphere_problem(16, stretch=1.5)),
         ("sphere12_unif", lambda: sphere_problem(12, stretch=None)),
         ("box2d_32", lambda: P.box2d(32, seed=9)),
+        # long lines: the warp-partition smoother with 2, 4 and 8 rows per lane
+        ("box2d_256", lambda: P.box2d(256, seed=9)),
+        ("sphere_48x80x160", lambda: P.sphere((48, 80, 160), seed=5, stretch=1.5)),
     ]
 
 
