@@ -52,7 +52,13 @@ struct Level {
     float *cm32[3] = {}, *cp32[3] = {};
     double *v64 = nullptr, *r64 = nullptr;
     float *v32 = nullptr, *r32 = nullptr;
-    // restriction weights to level n+1 (per coarse index along the cycle direction)
+    int dlo[3] = {}, dhi[3] = {};   // finest-level Dirichlet ends per line direction
+};
+
+// Transfer tables between level n and n+1 of one cycle direction.  Level 1 is
+// shared by the three cycles, so its tables live per direction (Ctx::T1).
+struct Transfer {
+    // restriction weights (per coarse index along the cycle direction)
     double *rw1_64 = nullptr, *rw2_64 = nullptr;
     float *rw1_32 = nullptr, *rw2_32 = nullptr;
     // prolongation from level n+1 (per fine index along the cycle direction)
@@ -60,7 +66,6 @@ struct Level {
     int8_t *pmode = nullptr;
     double *pwA64 = nullptr, *pwB64 = nullptr;
     float *pwA32 = nullptr, *pwB32 = nullptr;
-    int dlo[3] = {}, dhi[3] = {};   // finest-level Dirichlet ends per line direction
 };
 
 struct Ctx {
@@ -80,6 +85,7 @@ struct Ctx {
 
     Level L1;
     std::vector<Level> C[3];   // C[d][n] for n = 2..nlev (index n)
+    std::vector<Transfer> T[3];   // T[d][n]: tables between level n and n+1 of cycle d
 
     // level-1 fields (full layout)
     double *p64 = nullptr, *b64 = nullptr, *nlw0 = nullptr;
@@ -295,7 +301,7 @@ int alloc_level(Ctx &c, Level &L, bool fields)
 }
 
 // transfer tables between fine level F (index n) and coarse level n+1 along d
-int build_transfer(Ctx &c, Level &F, int d, int n)
+int build_transfer(Ctx &c, Transfer &F, int d, int n)
 {
     const int nc = c.mgrid[d][n + 1];
     const int mf = (n == 1) ? (d == 0 ? c.nx : d == 1 ? c.ny : c.nz) : c.mgrid[d][n] + 1;
@@ -428,18 +434,18 @@ void gcm_pressure<float>(Ctx &c, float *v)
     }
 }
 
-template <typename T> const T *rw1(Level &L);
-template <> const double *rw1<double>(Level &L) { return L.rw1_64; }
-template <> const float *rw1<float>(Level &L) { return L.rw1_32; }
-template <typename T> const T *rw2(Level &L);
-template <> const double *rw2<double>(Level &L) { return L.rw2_64; }
-template <> const float *rw2<float>(Level &L) { return L.rw2_32; }
-template <typename T> const T *pwA(Level &L);
-template <> const double *pwA<double>(Level &L) { return L.pwA64; }
-template <> const float *pwA<float>(Level &L) { return L.pwA32; }
-template <typename T> const T *pwB(Level &L);
-template <> const double *pwB<double>(Level &L) { return L.pwB64; }
-template <> const float *pwB<float>(Level &L) { return L.pwB32; }
+template <typename T> const T *rw1(Transfer &L);
+template <> const double *rw1<double>(Transfer &L) { return L.rw1_64; }
+template <> const float *rw1<float>(Transfer &L) { return L.rw1_32; }
+template <typename T> const T *rw2(Transfer &L);
+template <> const double *rw2<double>(Transfer &L) { return L.rw2_64; }
+template <> const float *rw2<float>(Transfer &L) { return L.rw2_32; }
+template <typename T> const T *pwA(Transfer &L);
+template <> const double *pwA<double>(Transfer &L) { return L.pwA64; }
+template <> const float *pwA<float>(Transfer &L) { return L.pwA32; }
+template <typename T> const T *pwB(Transfer &L);
+template <> const double *pwB<double>(Transfer &L) { return L.pwB64; }
+template <> const float *pwB<float>(Transfer &L) { return L.pwB32; }
 
 Level &level_of(Ctx &c, int d, int n) { return n == 1 ? c.L1 : c.C[d][n]; }
 
@@ -476,9 +482,10 @@ void mg_cycle(Ctx &c, int d, T *var, const T *rhs, int n, int WF, int &GMM, bool
     T *phi = lv_v<T>(Cn);
     T *r1 = lv_r<T>(Cn);
     {
+        Transfer &Tn = c.T[d][n];
         RestrictArgs<T> a;
         a.v = var; a.r = rhs; a.fl = L.fl; a.c = coef_of<T>(L); a.df = L.d; a.dc = Cn.d;
-        a.w1 = rw1<T>(L); a.w2 = rw2<T>(L); a.rc = r1;
+        a.w1 = rw1<T>(Tn); a.w2 = rw2<T>(Tn); a.rc = r1;
         launch_resid_restrict<T>(d, a, c.s);
         launch_fill<T>(phi, Cn.d.count(), T(0), c.s);
         c.launches += 2;
@@ -486,9 +493,10 @@ void mg_cycle(Ctx &c, int d, T *var, const T *rhs, int n, int WF, int &GMM, bool
     const int count = (n != nlev - 1) ? GMM : 1;
     for (int I = 1; I <= count; ++I) mg_cycle<T>(c, d, phi, r1, n + 1, I, GMM, true);
     {
+        Transfer &Tn = c.T[d][n];
         ProlongArgs<T> a;
         a.phi = phi; a.flc = Cn.fl; a.v = var; a.flf = L.fl; a.df = L.d; a.dc = Cn.d;
-        a.cA = L.pcA; a.cB = L.pcB; a.wA = pwA<T>(L); a.wB = pwB<T>(L); a.mode = L.pmode;
+        a.cA = Tn.pcA; a.cB = Tn.pcB; a.wA = pwA<T>(Tn); a.wB = pwB<T>(Tn); a.mode = Tn.pmode;
         launch_prolong_correct<T>(d, a, c.s);
         c.launches++;
     }
@@ -760,6 +768,7 @@ int fsi_mg_create(const fsi_mg_params *params, const double *x, const double *y,
     TRY(alloc_level(*c, c->L1, false));
     for (int d = 0; d < c->nd; ++d) {
         c->C[d].resize(c->nlev[d] + 1);
+        c->T[d].resize(c->nlev[d] + 1);
         for (int l = 2; l <= c->nlev[d]; ++l) {
             int m[3] = {c->nx, c->ny, c->nz};
             m[d] = c->mgrid[d][l] + 1;
@@ -896,7 +905,7 @@ int fsi_mg_set_geometry(void *handle, const int8_t *iblank, const int8_t *ghostC
                                c.p.pbc[2 * a + 1] == PBC_DIRICHLET));
             }
         }
-        for (int l = 1; l < c.nlev[d]; ++l) TRY(build_transfer(c, level_of(c, d, l), d, l));
+        for (int l = 1; l < c.nlev[d]; ++l) TRY(build_transfer(c, c.T[d][l], d, l));
     }
     // line factorisations of every level and direction
     auto factor = [&](Level &L) {
@@ -1126,7 +1135,7 @@ int fsi_mg_debug_level_op(void *handle, int op, int d, int n, void *a, void *b, 
         TRY(copy_level(c, L, t1, b, true));
         RestrictArgs<double> ra;
         ra.v = t0; ra.r = t1; ra.fl = L.fl; ra.c = coef_of<double>(L); ra.df = L.d; ra.dc = Cn.d;
-        ra.w1 = L.rw1_64; ra.w2 = L.rw2_64; ra.rc = t2;
+        ra.w1 = c.T[d][n].rw1_64; ra.w2 = c.T[d][n].rw2_64; ra.rc = t2;
         launch_resid_restrict<double>(d, ra, c.s);
         TRY(copy_level(c, Cn, t2, cc, false));
         break;
@@ -1139,7 +1148,8 @@ int fsi_mg_debug_level_op(void *handle, int op, int d, int n, void *a, void *b, 
         TRY(copy_level(c, L, t0, b, true));
         ProlongArgs<double> pa;
         pa.phi = t2; pa.flc = Cn.fl; pa.v = t0; pa.flf = L.fl; pa.df = L.d; pa.dc = Cn.d;
-        pa.cA = L.pcA; pa.cB = L.pcB; pa.wA = L.pwA64; pa.wB = L.pwB64; pa.mode = L.pmode;
+        Transfer &Tn = c.T[d][n];
+        pa.cA = Tn.pcA; pa.cB = Tn.pcB; pa.wA = Tn.pwA64; pa.wB = Tn.pwB64; pa.mode = Tn.pmode;
         launch_prolong_correct<double>(d, pa, c.s);
         TRY(copy_level(c, L, t0, b, false));
         break;
@@ -1240,7 +1250,7 @@ int fsi_mg_time_kernel(void *handle, int which, int precision, int reps, double 
                 Level &Cn = c.C[0][2];
                 RestrictArgs<T> a;
                 a.v = (const T *)v; a.r = (const T *)r; a.fl = c.L1.fl; a.c = coef_of<T>(c.L1); a.df = c.L1.d;
-                a.dc = Cn.d; a.w1 = rw1<T>(c.L1); a.w2 = rw2<T>(c.L1); a.rc = lv_r<T>(Cn);
+                a.dc = Cn.d; a.w1 = rw1<T>(c.T[0][1]); a.w2 = rw2<T>(c.T[0][1]); a.rc = lv_r<T>(Cn);
                 launch_resid_restrict<T>(0, a, c.s);
             };
             if (f32) go(c.e32, c.r32, 0.0f); else go(p, b, 0.0);
@@ -1250,7 +1260,8 @@ int fsi_mg_time_kernel(void *handle, int which, int precision, int reps, double 
                 Level &Cn = c.C[0][2];
                 ProlongArgs<T> a;
                 a.phi = lv_v<T>(Cn); a.flc = Cn.fl; a.v = (T *)v; a.flf = c.L1.fl; a.df = c.L1.d; a.dc = Cn.d;
-                a.cA = c.L1.pcA; a.cB = c.L1.pcB; a.wA = pwA<T>(c.L1); a.wB = pwB<T>(c.L1); a.mode = c.L1.pmode;
+                Transfer &T1 = c.T[0][1];
+                a.cA = T1.pcA; a.cB = T1.pcB; a.wA = pwA<T>(T1); a.wB = pwB<T>(T1); a.mode = T1.pmode;
                 launch_prolong_correct<T>(0, a, c.s);
             };
             if (f32) go(c.e32, 0.0f); else go(p, 0.0);
