@@ -126,6 +126,14 @@ struct Ctx {
     double *graph_p = nullptr;
     const double *graph_b = nullptr;
 
+    // FGMRES state (outer_krylov > 0)
+    int km = 0;
+    std::vector<double *> KV, KZ;          // Arnoldi basis (m+1) and preconditioned directions (m), FP64
+    double *kw = nullptr, *kzp = nullptr, *kzr = nullptr;
+    double *kpart = nullptr, *kdots = nullptr, *h_kdots = nullptr;
+    cudaGraphExec_t pgraph = nullptr;      // MG preconditioner on fixed buffers
+    long long pgraph_kernels = 0;
+
     // stats
     std::vector<double> hist;   // max-norm residual after each outer iteration of the last solve
     int last_iters = 0;
@@ -135,6 +143,8 @@ struct Ctx {
     ~Ctx()
     {
         if (graph) cudaGraphExecDestroy(graph);
+        if (pgraph) cudaGraphExecDestroy(pgraph);
+        if (h_kdots) cudaFreeHost(h_kdots);
         for (cudaEvent_t e : {ev0, ev1, ev2, ev3})
             if (e) cudaEventDestroy(e);
         for (void *a : allocs) cudaFree(a);
@@ -610,10 +620,196 @@ int loc_of(const Ctx &c, long long idx, int *loc)
     return 0;
 }
 
+int ensure_krylov(Ctx &c, int m)
+{
+    if (c.km >= m) return 0;
+    const long long n1 = c.L1.d.count();
+    while ((int)c.KV.size() < m + 1) { double *q; TRY(c.alloc(&q, n1)); c.KV.push_back(q); }
+    while ((int)c.KZ.size() < m) { double *q; TRY(c.alloc(&q, n1)); c.KZ.push_back(q); }
+    if (!c.kw) {
+        TRY(c.alloc(&c.kw, n1));
+        TRY(c.alloc(&c.kzp, n1));
+        TRY(c.alloc(&c.kzr, n1));
+        TRY(c.alloc(&c.kpart, 8 * (size_t)c.nred + 8));
+        TRY(c.alloc(&c.kdots, 256));
+        CK(cudaMallocHost(&c.h_kdots, 256 * sizeof(double)));
+    }
+    if (m > 60) return fail(-1, "outer_krylov must be <= 60");
+    c.km = m;
+    return 0;
+}
+
+// z = M^-1 v: one MG_Solver schedule on the correction (zero initial guess,
+// homogeneous boundary values), FP32 in mixed mode, FP64 otherwise; run as a
+// CUDA graph on fixed buffers (mixed: r32 -> e32, plain: kzr -> kzp).
+int precondition(Ctx &c, const double *v, double *z)
+{
+    const long long n1 = c.L1.d.count();
+    const bool mixed = (c.p.precision_mode == 1);
+    if (mixed) launch_convert_d2f(c.r32, v, n1, c.s);
+    else CK(cudaMemcpyAsync(c.kzr, v, n1 * 8, cudaMemcpyDeviceToDevice, c.s));
+    c.launches++;
+    if (!c.pgraph) {
+        cudaGraph_t g;
+        const long long before = c.launches;
+        CK(cudaStreamBeginCapture(c.s, cudaStreamCaptureModeThreadLocal));
+        if (mixed) {
+            launch_fill<float>(c.e32, n1, 0.0f, c.s);
+            mg_solver<float>(c, c.e32, c.r32, true);
+        } else {
+            launch_fill<double>(c.kzp, n1, 0.0, c.s);
+            mg_solver<double>(c, c.kzp, c.kzr, true);
+        }
+        c.launches++;
+        CK(cudaStreamEndCapture(c.s, &g));
+        c.pgraph_kernels = c.launches - before;
+        c.launches = before;
+        cudaError_t e = cudaGraphInstantiate(&c.pgraph, g, 0);
+        cudaGraphDestroy(g);
+        if (e != cudaSuccess) return fail(-10, std::string("cudaGraphInstantiate: ") + cudaGetErrorString(e));
+    }
+    CK(cudaGraphLaunch(c.pgraph, c.s));
+    c.launches += c.pgraph_kernels;
+    if (mixed) launch_convert_f2d(z, c.e32, n1, c.s);
+    else CK(cudaMemcpyAsync(z, c.kzp, n1 * 8, cudaMemcpyDeviceToDevice, c.s));
+    c.launches++;
+    return 0;
+}
+
+// solve_poisson with FGMRES(m) around MG_Solver (outer_krylov = m).  Same
+// discrete system (fluid rows with ghost values from the ghost-row fixed
+// point), same stopping test (max-norm of the calc_residual residual).
+// Iterations count preconditioner applications (one MG_Solver each).
+int solve_krylov(Ctx &c, double *p, const double *b, int *iters, double *maxres_out, int *loc, double *compTime)
+{
+    const int m = c.p.outer_krylov;
+    TRY(ensure_krylov(c, m));
+    const long long n1 = c.L1.d.count();
+    const bool gcm = (c.p.boundary_formulation == GCM_METHOD);
+    auto t0 = std::chrono::steady_clock::now();
+    CK(cudaEventRecord(c.ev0, c.s));
+    const bool dirichlet = c.p.pbc[0] == PBC_DIRICHLET || c.p.pbc[2] == PBC_DIRICHLET || c.p.pbc[4] == PBC_DIRICHLET;
+    if (dirichlet) return fail(-1, "outer_krylov needs all-Neumann pressure boundaries");
+    if (c.compat_active) return fail(-1, "outer_krylov needs an inactive compatibility correction (no zero-gradient BCs)");
+    if (c.nlw0_nonzero) { launch_fill<double>(c.nlw0, n1, 0.0, c.s); c.launches++; }
+    launch_subtract_average(p, c.L1.fl, c.d_dx[0], c.d_dx[1], c.d_dx[2], c.L1.d, (double *)c.partials, c.nred, c.s);
+    c.launches += 3;
+    CK(cudaMemsetAsync(c.d_iters, 0, sizeof(int), c.s));
+    CK(cudaMemsetAsync(c.d_maxd, 0, sizeof(unsigned long long), c.s));
+    c.hist.clear();
+    int it = 0;
+    double maxres = 1.0e10;
+    long long maxidx = 0;
+    std::vector<double> H((size_t)(m + 1) * m, 0.0), cs(m, 0.0), sn(m, 0.0), g(m + 1, 0.0), y(m, 0.0);
+    auto Hij = [&](int i, int j) -> double & { return H[(size_t)i + (size_t)(m + 1) * j]; };
+    const Coef<double> coef = coef_of<double>(c.L1);
+    while (true) {
+        if (gcm) correct_pressure(c, p, c.nlw0);
+        launch_calc_residual(p, b, c.nlw0_nonzero ? c.nlw0 : nullptr, c.L1.fl, coef, c.L1.d, nullptr, c.partials,
+                             c.nred, c.result, c.s, c.KV[0]);
+        c.launches += 2;
+        CK(cudaMemcpyAsync(c.h_result, c.result, sizeof(MaxLoc), cudaMemcpyDeviceToHost, c.s));
+        CK(cudaStreamSynchronize(c.s));
+        maxres = c.h_result->v;
+        maxidx = c.h_result->i;
+        if (!c.hist.empty()) c.hist.back() = maxres;   // true value at the restart point
+        if (!std::isfinite(maxres) || maxres <= c.p.restol_Poisson || it >= c.p.iterMax_Poisson) break;
+        // beta = ||r||_2 over fluid cells
+        const double *v0 = c.KV[0];
+        launch_mdot(&v0, 1, c.KV[0], c.L1.fl, c.L1.d, c.kpart, c.nred, c.kdots, c.s);
+        CK(cudaMemcpyAsync(c.h_kdots, c.kdots, sizeof(double), cudaMemcpyDeviceToHost, c.s));
+        CK(cudaStreamSynchronize(c.s));
+        const double beta = std::sqrt(c.h_kdots[0]);
+        if (!(beta > 0.0)) break;
+        launch_scale_copy(c.KV[0], c.KV[0], c.kdots, n1, c.s);
+        std::fill(g.begin(), g.end(), 0.0);
+        g[0] = beta;
+        const double target = 0.5 * beta * c.p.restol_Poisson / maxres;
+        int k = 0;
+        for (int j = 0; j < m; ++j) {
+            TRY(precondition(c, c.KV[j], c.KZ[j]));
+            if (gcm) {   // ghost values of z from its fluid values (the map whose matrix A acts on)
+                launch_outer_ghost<double>(c.KZ[j], c.L1.d, c.sign, c.s);
+                if (c.nGhost > 0) {
+                    GhostArgs ga{c.nGhost, c.gidx, c.sidx};
+                    launch_ghost_rows<double>(c.KZ[j], ga, c.gco64, c.gscr64, c.p.iterMax_ad, c.p.restol_ad, 0.0,
+                                              c.d_iters, c.d_maxd, c.s);
+                }
+                c.launches += 2;
+            }
+            launch_apply_op(c.KZ[j], c.kw, c.L1.fl, coef, c.L1.d, c.s);
+            c.launches++;
+            const double *const *Vp = c.KV.data();
+            // classical Gram-Schmidt, twice
+            launch_mdot(Vp, j + 1, c.kw, c.L1.fl, c.L1.d, c.kpart, c.nred, c.kdots, c.s);
+            launch_maxpy(c.kw, Vp, j + 1, c.kdots, -1.0, n1, c.s);
+            launch_mdot(Vp, j + 1, c.kw, c.L1.fl, c.L1.d, c.kpart, c.nred, c.kdots + 64, c.s);
+            launch_maxpy(c.kw, Vp, j + 1, c.kdots + 64, -1.0, n1, c.s);
+            const double *wp = c.kw;
+            launch_mdot(&wp, 1, c.kw, c.L1.fl, c.L1.d, c.kpart, c.nred, c.kdots + 128, c.s);
+            launch_scale_copy(c.KV[j + 1], c.kw, c.kdots + 128, n1, c.s);
+            c.launches += 4 * ((j + 8) / 8) * 2 + 3;
+            CK(cudaMemcpyAsync(c.h_kdots, c.kdots, 256 * sizeof(double), cudaMemcpyDeviceToHost, c.s));
+            CK(cudaStreamSynchronize(c.s));
+            for (int i = 0; i <= j; ++i) Hij(i, j) = c.h_kdots[i] + c.h_kdots[64 + i];
+            const double hn = std::sqrt(c.h_kdots[128]);
+            Hij(j + 1, j) = hn;
+            // Givens rotations
+            for (int i = 0; i < j; ++i) {
+                const double a = Hij(i, j), bb = Hij(i + 1, j);
+                Hij(i, j) = cs[i] * a + sn[i] * bb;
+                Hij(i + 1, j) = -sn[i] * a + cs[i] * bb;
+            }
+            const double a = Hij(j, j), bb = Hij(j + 1, j);
+            const double r = std::hypot(a, bb);
+            cs[j] = (r > 0.0) ? a / r : 1.0;
+            sn[j] = (r > 0.0) ? bb / r : 0.0;
+            Hij(j, j) = r;
+            Hij(j + 1, j) = 0.0;
+            g[j + 1] = -sn[j] * g[j];
+            g[j] = cs[j] * g[j];
+            ++it;
+            k = j + 1;
+            c.hist.push_back(maxres * std::fabs(g[j + 1]) / beta);   // estimate until the next true value
+            if (std::fabs(g[j + 1]) <= target || it >= c.p.iterMax_Poisson || !(hn > 0.0)) break;
+        }
+        // y = H^-1 g (upper triangular k x k), p += sum y_i z_i
+        for (int i = k - 1; i >= 0; --i) {
+            double sacc = g[i];
+            for (int l = i + 1; l < k; ++l) sacc -= Hij(i, l) * y[l];
+            y[i] = sacc / Hij(i, i);
+        }
+        CK(cudaMemcpyAsync(c.kdots + 192, y.data(), k * sizeof(double), cudaMemcpyHostToDevice, c.s));
+        launch_maxpy(p, c.KZ.data(), k, c.kdots + 192, 1.0, n1, c.s);
+        c.launches += (k + 7) / 8;
+    }
+    CK(cudaEventRecord(c.ev1, c.s));
+    int h_iters = 0;
+    unsigned long long h_maxd = 0;
+    CK(cudaMemcpyAsync(&h_iters, c.d_iters, sizeof(int), cudaMemcpyDeviceToHost, c.s));
+    CK(cudaMemcpyAsync(&h_maxd, c.d_maxd, sizeof(h_maxd), cudaMemcpyDeviceToHost, c.s));
+    CK(cudaStreamSynchronize(c.s));
+    c.ghost_sweeps = h_iters;
+    float ms = 0.0f;
+    CK(cudaEventElapsedTime(&ms, c.ev0, c.ev1));
+    c.last_iters = it;
+    c.last_maxres = maxres;
+    c.last_time = 1e-3 * (double)ms;
+    c.last_wall = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+    if (iters) *iters = it;
+    if (maxres_out) *maxres_out = maxres;
+    loc_of(c, maxidx, loc);
+    if (compTime) *compTime = c.last_time;
+    if (!std::isfinite(maxres)) return fail(-5, "residual is not finite (NaN or Inf in the inputs?)");
+    if (maxres > c.p.restol_Poisson) return 1;
+    return 0;
+}
+
 // solve_poisson MG branch on device-resident full-layout arrays
 int solve_device(Ctx &c, double *p, const double *b, int *iters, double *maxres_out, int *loc, double *compTime)
 {
     if (!c.geometry) return fail(-2, "fsi_mg_set_geometry has not been called");
+    if (c.p.outer_krylov > 0) return solve_krylov(c, p, b, iters, maxres_out, loc, compTime);
     auto t0 = std::chrono::steady_clock::now();
     CK(cudaEventRecord(c.ev0, c.s));
     const bool dirichlet = c.p.pbc[0] == PBC_DIRICHLET || c.p.pbc[2] == PBC_DIRICHLET || c.p.pbc[4] == PBC_DIRICHLET;
@@ -720,6 +916,7 @@ int fsi_mg_create(const fsi_mg_params *params, const double *x, const double *y,
         if (p.mgcycle[q] < 1 || p.mgcycle[q] > 3) return fail(-1, "mgcycle must be 1, 2 or 3");
     if (p.omega <= 0.0 || p.omega >= 2.0) return fail(-1, "omega must be in (0,2)");
     if (p.precision_mode != 0 && p.precision_mode != 1) return fail(-1, "precision_mode must be 0 or 1");
+    if (p.outer_krylov < 0 || p.outer_krylov > 60) return fail(-1, "outer_krylov must be in 0..60");
     int ndev = 0;
     if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return fail(-12, "no CUDA device");
     CK(init_kernels());
@@ -974,6 +1171,7 @@ int fsi_mg_set_geometry(void *handle, const int8_t *iblank, const int8_t *ghostC
     if (c.compat_active && !(c.p.outflow_area > 0.0)) return fail(-1, "outflow_area must be > 0 with zero-gradient BCs");
     CK(cudaStreamSynchronize(c.s));
     if (c.graph) { cudaGraphExecDestroy(c.graph); c.graph = nullptr; }
+    if (c.pgraph) { cudaGraphExecDestroy(c.pgraph); c.pgraph = nullptr; }
     c.geometry = true;
     return 0;
 }

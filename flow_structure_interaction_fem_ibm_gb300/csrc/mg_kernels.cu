@@ -3,6 +3,7 @@
 #include "mg_kernels.cuh"
 
 #include <cfloat>
+#include <cooperative_groups.h>
 
 namespace fsimg {
 
@@ -177,13 +178,27 @@ __global__ void __launch_bounds__(256) k_line_wp(LineArgs<T> A)
     };
     auto sidx = [&](int g, int r) { return g * RP + r + r / S; };
 
-    // ---- 1. staging ----
-    auto stage = [&](int g, int r) {   // r: 0-based row along the line (row index r+1)
-        int p, q;
-        if (!line_pq(g, p, q)) return;
-        const int i = r + 1;
-        const long long o = (long long)p * sb_ + (long long)q * sc_ + (long long)i * sa_;
-        const uint8_t f = A.fl[o];
+    // ---- 1. staging (loads for up to 4 rows per thread are issued before any use) ----
+    struct RowIn { uint8_t f; T r, nb0, nb1, nb2, nb3, vo; int p, q; bool ok; };
+    auto load_row = [&](int g, int r, RowIn &in) {
+        int p = 0, q = 0;
+        in.ok = (r < L) && line_pq(g, p, q);
+        in.p = p; in.q = q;
+        if (!in.ok) return;
+        const long long o = (long long)p * sb_ + (long long)q * sc_ + (long long)(r + 1) * sa_;
+        in.f = A.fl[o];
+        in.r = A.r[o];
+        in.vo = A.v[o];
+        if (X::c_first) {
+            in.nb0 = A.v[o - sc_]; in.nb1 = A.v[o + sc_]; in.nb2 = A.v[o - sb_]; in.nb3 = A.v[o + sb_];
+        } else {
+            in.nb0 = A.v[o - sb_]; in.nb1 = A.v[o + sb_]; in.nb2 = A.v[o - sc_]; in.nb3 = A.v[o + sc_];
+        }
+    };
+    auto finish_row = [&](int g, int r, const RowIn &in) {
+        if (!in.ok) return;
+        const int i = r + 1, p = in.p, q = in.q;
+        const uint8_t f = in.f;
         const bool fluid = !(f & FB_IB);
         const T ama = (f & fb_minus(X::a)) ? T(0) : A.c.cm[X::a][i];
         const T apa = (f & fb_plus(X::a)) ? T(0) : A.c.cp[X::a][i];
@@ -195,27 +210,26 @@ __global__ void __launch_bounds__(256) k_line_wp(LineArgs<T> A)
         const bool normal = fluid && !allzero;
         T aa = T(0), bb = T(1), cc = T(0), dd;
         if (normal) {
-            T sdd = A.r[o];
+            T sdd = in.r;
             if (X::c_first) {
-                sdd = sdd - A.v[o - sc_] * amc;
-                sdd = sdd - A.v[o + sc_] * apc;
-                sdd = sdd - A.v[o - sb_] * amb;
-                sdd = sdd - A.v[o + sb_] * apb;
+                sdd = sdd - in.nb0 * amc;
+                sdd = sdd - in.nb1 * apc;
+                sdd = sdd - in.nb2 * amb;
+                sdd = sdd - in.nb3 * apb;
             } else {
-                sdd = sdd - A.v[o - sb_] * amb;
-                sdd = sdd - A.v[o + sb_] * apb;
-                sdd = sdd - A.v[o - sc_] * amc;
-                sdd = sdd - A.v[o + sc_] * apc;
+                sdd = sdd - in.nb0 * amb;
+                sdd = sdd - in.nb1 * apb;
+                sdd = sdd - in.nb2 * amc;
+                sdd = sdd - in.nb3 * apc;
             }
             dd = sdd;
-            // diagonal as the reference sums it: (acx + acy) + acz
-            T am3[3], ap3[3];
+            T am3[3], ap3[3];   // diagonal as the reference sums it: (acx + acy) + acz
             am3[X::a] = ama; ap3[X::a] = apa; am3[X::b] = amb; ap3[X::b] = apb; am3[X::c] = amc; ap3[X::c] = apc;
             bb = (-(am3[0] + ap3[0]) + -(am3[1] + ap3[1])) + -(am3[2] + ap3[2]);
             aa = ama;
             cc = apa;
         } else {
-            dd = ((f & FB_GM) || fluid) ? A.v[o] : T(0);
+            dd = ((f & FB_GM) || fluid) ? in.vo : T(0);
         }
         if (i == 1 && A.dir_lo) dd = dd - A.ppp_lo * aa;
         if (i == L && A.dir_hi) dd = dd - A.ppp_hi * cc;
@@ -224,13 +238,18 @@ __global__ void __launch_bounds__(256) k_line_wp(LineArgs<T> A)
         const int si = sidx(g, r);
         sa[si] = aa; sb[si] = bb; sc[si] = cc; sd[si] = dd;
     };
-    if (DIR == 0) {
-        for (int r0 = 0; r0 < L; r0 += 32)
-            if (r0 + lane < L) stage(warp, r0 + lane);
-    } else {
-        const int g = tid & (WP_LINES - 1), rr = tid >> 3;   // 32 rows x 8 lines per pass
-        for (int r0 = 0; r0 < L; r0 += 32)
-            if (r0 + rr < L) stage(g, r0 + rr);
+    {
+        constexpr int GRP = (S < 4) ? S : 4;
+        const int g = (DIR == 0) ? warp : (tid & (WP_LINES - 1));
+        const int rr = (DIR == 0) ? lane : (tid >> 3);
+#pragma unroll
+        for (int q0 = 0; q0 < S; q0 += GRP) {
+            RowIn in[GRP];
+#pragma unroll
+            for (int u = 0; u < GRP; ++u) load_row(g, (q0 + u) * 32 + rr, in[u]);
+#pragma unroll
+            for (int u = 0; u < GRP; ++u) finish_row(g, (q0 + u) * 32 + rr, in[u]);
+        }
     }
     __syncthreads();
 
@@ -563,6 +582,70 @@ __global__ void __launch_bounds__(1024) k_ghost_rows(T *v, GhostArgs g, const T 
     }
 }
 
+// Same fixed-point iteration spread over a cluster of 8 CTAs (8192 threads):
+// the per-sweep max |dp| is exchanged through distributed shared memory and
+// the sweeps are separated by cluster barriers.  Loop bounds are uniform over
+// the cluster and capped by iterMax.
+constexpr int GHOST_CLUSTER = 8;
+
+template <typename T>
+__global__ void __cluster_dims__(GHOST_CLUSTER, 1, 1) __launch_bounds__(1024)
+    k_ghost_rows_cluster(T *v, GhostArgs g, const T *coeff, T *scratch, int iterMax, double tol, double reltol,
+                         int *iters, unsigned long long *maxdelta)
+{
+    namespace cg = cooperative_groups;
+    cg::cluster_group cluster = cg::this_cluster();
+    __shared__ double s_d[32], s_a[32];
+    __shared__ double slot_d[GHOST_CLUSTER], slot_a[GHOST_CLUSTER];   // used in rank 0 only
+    const unsigned rank = cluster.block_rank();
+    const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5, nw = (blockDim.x + 31) >> 5;
+    const long long gtid = (long long)rank * blockDim.x + tid, gstride = (long long)GHOST_CLUSTER * blockDim.x;
+    double *rslot_d = cluster.map_shared_rank(slot_d, 0);
+    double *rslot_a = cluster.map_shared_rank(slot_a, 0);
+    int it = 0;
+    double maxd = 1.0e10, thr = tol;
+    while (it < iterMax && maxd > thr) {
+        double ld = 0.0, la = 0.0;
+        for (long long n = gtid; n < g.n; n += gstride) {
+            T acc = T(0);
+#pragma unroll
+            for (int r = 0; r < 8; ++r) {
+                const long long sidx = g.sidx[8LL * n + r];
+                const T val = (sidx < 0) ? T(0) : v[sidx];
+                acc = acc + coeff[8LL * n + r] * val;
+            }
+            const T old = v[g.gidx[n]];
+            scratch[n] = acc;
+            ld = fmax(ld, fabs((double)acc - (double)old));
+            la = fmax(la, fabs((double)acc));
+        }
+        for (int o = 16; o > 0; o >>= 1) {
+            ld = fmax(ld, __shfl_xor_sync(0xffffffffu, ld, o));
+            la = fmax(la, __shfl_xor_sync(0xffffffffu, la, o));
+        }
+        if (lane == 0) { s_d[wid] = ld; s_a[wid] = la; }
+        __syncthreads();
+        if (tid == 0) {
+            double a = 0.0, b = 0.0;
+            for (int w = 0; w < nw; ++w) { a = fmax(a, s_d[w]); b = fmax(b, s_a[w]); }
+            rslot_d[rank] = a;
+            rslot_a[rank] = b;
+        }
+        cluster.sync();   // scratch and the slots are complete
+        for (long long n = gtid; n < g.n; n += gstride) v[g.gidx[n]] = scratch[n];
+        double a = 0.0, b = 0.0;
+        for (int q = 0; q < GHOST_CLUSTER; ++q) { a = fmax(a, rslot_d[q]); b = fmax(b, rslot_a[q]); }
+        maxd = a;
+        thr = fmax(tol, reltol * b);
+        ++it;
+        cluster.sync();   // v updated everywhere; rank 0 slots free for the next sweep
+    }
+    if (rank == 0 && tid == 0) {
+        atomicAdd(iters, it);
+        atomicMax(maxdelta, (unsigned long long)__double_as_longlong(maxd));
+    }
+}
+
 template <typename T>
 __global__ void k_fill(T *p, long long n, T val)
 {
@@ -583,7 +666,7 @@ __device__ __forceinline__ void maxloc_merge(double &v, long long &i, double v2,
 
 __global__ void __launch_bounds__(TPB) k_calc_residual(const double *p, const double *b, const double *nlw0,
                                                        const uint8_t *fl, Coef<double> c, Dims d, float *r32,
-                                                       MaxLoc *partials)
+                                                       double *r64, MaxLoc *partials)
 {
     const int n0 = d.m[0] - 1, n1 = d.m[1] - 1, n2 = d.m[2] - 1;
     const long long total = (long long)n0 * n1 * n2;
@@ -596,6 +679,7 @@ __global__ void __launch_bounds__(TPB) k_calc_residual(const double *p, const do
         double res = cell_residual(p, b, fl, c, d, i, j, k);
         if (nlw0 && !(fl[o] & FB_IB)) res = res + nlw0[o];
         if (r32) r32[o] = (float)res;
+        if (r64) r64[o] = res;
         double a = fabs(res);
         if (!(a == a)) a = INFINITY;   // a NaN residual must not be skipped by the max
         maxloc_merge(best, bi, a, o);
@@ -796,6 +880,89 @@ __global__ void __launch_bounds__(TPB) k_nlw0(double *nlw0, CompatArgs A, const 
               dzinv[k] * (kup * pgz2 - kum * pgz1);
 }
 
+// ---------------------------------------------------------------------------
+// Krylov support for the outer solve: operator application on fluid cells,
+// blocked dot products and combined axpys over the level-1 interior.
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(TPB) k_apply_op(const double *z, double *w, const uint8_t *fl, Coef<double> c,
+                                                  Dims d)
+{
+    // w = A z on fluid interior cells (the matrix whose residual calc_residual forms), 0 elsewhere
+    const int n0 = d.m[0] - 1, n1 = d.m[1] - 1, n2 = d.m[2] - 1;
+    const long long total = (long long)n0 * n1 * n2;
+    long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= total) return;
+    const int i = 1 + (int)(t % n0), j = 1 + (int)((t / n0) % n1), k = 1 + (int)(t / ((long long)n0 * n1));
+    const long long o = d.idx(i, j, k);
+    const uint8_t f = fl[o];
+    if (f & FB_IB) { w[o] = 0.0; return; }
+    const double bmx = (f & fb_minus(0)) ? 0.0 : c.cm[0][i];
+    const double bpx = (f & fb_plus(0)) ? 0.0 : c.cp[0][i];
+    const double bmy = (f & fb_minus(1)) ? 0.0 : c.cm[1][j];
+    const double bpy = (f & fb_plus(1)) ? 0.0 : c.cp[1][j];
+    const double bmz = (f & fb_minus(2)) ? 0.0 : c.cm[2][k];
+    const double bpz = (f & fb_plus(2)) ? 0.0 : c.cp[2][k];
+    const double bc = (-(bmx + bpx) + -(bmy + bpy)) + -(bmz + bpz);
+    w[o] = z[o] * bc + z[o - 1] * bmx + z[o + 1] * bpx + z[o - d.sx] * bmy + z[o + d.sx] * bpy +
+           z[o - d.sxy] * bmz + z[o + d.sxy] * bpz;
+}
+
+struct VecSet { const double *v[8]; int n; };
+
+// partials[blk * 8 + q] = sum over fluid interior cells of V_q * w
+__global__ void __launch_bounds__(TPB) k_mdot(VecSet V, const double *w, const uint8_t *fl, Dims d, double *partials)
+{
+    const int n0 = d.m[0] - 1, n1 = d.m[1] - 1, n2 = d.m[2] - 1;
+    const long long total = (long long)n0 * n1 * n2;
+    double acc[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+    for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < total;
+         t += (long long)gridDim.x * blockDim.x) {
+        const int i = 1 + (int)(t % n0), j = 1 + (int)((t / n0) % n1), k = 1 + (int)(t / ((long long)n0 * n1));
+        const long long o = d.idx(i, j, k);
+        if (fl[o] & FB_IB) continue;
+        const double wo = w[o];
+#pragma unroll
+        for (int q = 0; q < 8; ++q)
+            if (q < V.n) acc[q] += V.v[q][o] * wo;
+    }
+    for (int q = 0; q < 8; ++q) {
+        const double s = block_sum(acc[q]);
+        if (threadIdx.x == 0) partials[(long long)blockIdx.x * 8 + q] = s;
+    }
+}
+
+// out[q] = sum_b partials[b * 8 + q]  (fixed order)
+__global__ void k_mdot_final(const double *partials, int nb, int n, double *out)
+{
+    for (int q = 0; q < n; ++q) {
+        double x = 0.0;
+        for (int b = threadIdx.x; b < nb; b += blockDim.x) x += partials[(long long)b * 8 + q];
+        const double tot = block_sum(x);
+        if (threadIdx.x == 0) out[q] = tot;
+        __syncthreads();
+    }
+}
+
+// w += sum_q coef[q] * sign * V_q  over all cells (coef on the device)
+__global__ void __launch_bounds__(TPB) k_maxpy(double *w, VecSet V, const double *coef, double sign, long long n)
+{
+    long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= n) return;
+    double acc = w[t];
+#pragma unroll
+    for (int q = 0; q < 8; ++q)
+        if (q < V.n) acc += sign * coef[q] * V.v[q][t];
+    w[t] = acc;
+}
+
+__global__ void k_scale_copy(double *dst, const double *src, const double *nrm2, long long n)
+{
+    // dst = src / sqrt(nrm2[0])
+    long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= n) return;
+    dst[t] = src[t] / sqrt(nrm2[0]);
+}
+
 __global__ void k_accumulate(double *p, const float *e, long long n)
 {
     long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
@@ -910,7 +1077,7 @@ void launch_line(int dir, const LineArgs<T> &a, bool omega_one, cudaStream_t s)
     const int nb = a.d.m[ob[dir]] - 1, nc = a.d.m[oc[dir]] - 1;
     const long long n = (long long)((nb + 1) / 2) * nc;
     const int L = a.d.m[dir] - 1;
-    if (!g_line_thread_per_line && L <= 512) {
+    if (!g_line_thread_per_line && L > 16 && L <= 512) {   // short lines: one thread per line is cheaper
         bool ok;
         if (omega_one) {
             ok = (dir == 0) ? launch_wp_dir<T, 0, true>(a, L, n, s)
@@ -971,7 +1138,11 @@ void launch_ghost_rows(T *v, const GhostArgs &g, const T *coeff, T *scratch, int
                        double reltol, int *d_iters, unsigned long long *d_maxdelta, cudaStream_t s)
 {
     if (g.n <= 0) return;
-    k_ghost_rows<T><<<1, 1024, 0, s>>>(v, g, coeff, scratch, iterMax, tol, reltol, d_iters, d_maxdelta);
+    if (g.n <= 4096)
+        k_ghost_rows<T><<<1, 1024, 0, s>>>(v, g, coeff, scratch, iterMax, tol, reltol, d_iters, d_maxdelta);
+    else
+        k_ghost_rows_cluster<T><<<GHOST_CLUSTER, 1024, 0, s>>>(v, g, coeff, scratch, iterMax, tol, reltol, d_iters,
+                                                                d_maxdelta);
 }
 
 template <typename T>
@@ -990,9 +1161,9 @@ int calc_residual_blocks(const Dims &d)
 
 void launch_calc_residual(const double *p, const double *b, const double *nlw0, const uint8_t *fl,
                           const Coef<double> &c, const Dims &d, float *r32_out, MaxLoc *partials, int nblocks,
-                          MaxLoc *result, cudaStream_t s)
+                          MaxLoc *result, cudaStream_t s, double *r64_out)
 {
-    k_calc_residual<<<nblocks, TPB, 0, s>>>(p, b, nlw0, fl, c, d, r32_out, partials);
+    k_calc_residual<<<nblocks, TPB, 0, s>>>(p, b, nlw0, fl, c, d, r32_out, r64_out, partials);
     k_maxloc_final<<<1, 1024, 0, s>>>(partials, nblocks, result);
 }
 
@@ -1049,6 +1220,41 @@ void launch_nlw0(double *nlw0, const uint8_t *fl, const int side_flag[6], const 
                                d, nx, ny, nz);
     const long long n = (long long)(d.m[0] - 1) * (d.m[1] - 1) * (d.m[2] - 1);
     k_nlw0<<<nblk(n), TPB, 0, s>>>(nlw0, A, dxinv, dyinv, dzinv);
+}
+
+void launch_apply_op(const double *z, double *w, const uint8_t *fl, const Coef<double> &c, const Dims &d,
+                     cudaStream_t s)
+{
+    const long long n = (long long)(d.m[0] - 1) * (d.m[1] - 1) * (d.m[2] - 1);
+    k_apply_op<<<nblk(n), TPB, 0, s>>>(z, w, fl, c, d);
+}
+
+void launch_mdot(const double *const *V, int nv, const double *w, const uint8_t *fl, const Dims &d,
+                 double *partials, int nblocks, double *out, cudaStream_t s)
+{
+    for (int q0 = 0; q0 < nv; q0 += 8) {
+        VecSet vs;
+        vs.n = (nv - q0 < 8) ? nv - q0 : 8;
+        for (int q = 0; q < 8; ++q) vs.v[q] = (q < vs.n) ? V[q0 + q] : nullptr;
+        k_mdot<<<nblocks, TPB, 0, s>>>(vs, w, fl, d, partials);
+        k_mdot_final<<<1, 1024, 0, s>>>(partials, nblocks, vs.n, out + q0);
+    }
+}
+
+void launch_maxpy(double *w, const double *const *V, int nv, const double *coef, double sign, long long n,
+                  cudaStream_t s)
+{
+    for (int q0 = 0; q0 < nv; q0 += 8) {
+        VecSet vs;
+        vs.n = (nv - q0 < 8) ? nv - q0 : 8;
+        for (int q = 0; q < 8; ++q) vs.v[q] = (q < vs.n) ? V[q0 + q] : nullptr;
+        k_maxpy<<<nblk(n), TPB, 0, s>>>(w, vs, coef + q0, sign, n);
+    }
+}
+
+void launch_scale_copy(double *dst, const double *src, const double *nrm2, long long n, cudaStream_t s)
+{
+    k_scale_copy<<<nblk(n), TPB, 0, s>>>(dst, src, nrm2, n);
 }
 
 void launch_accumulate(double *p, const float *e, long long n, cudaStream_t s)

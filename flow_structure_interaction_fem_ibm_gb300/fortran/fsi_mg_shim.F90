@@ -26,7 +26,7 @@ MODULE fsi_mg_gpu
     INTEGER(C_INT) :: mgcycle(3), iterFinest, iterCoarsest, mgLevels(3)
     INTEGER(C_INT) :: iterMax_Poisson, iterMax_ad, bc(6), pbc(6)
     INTEGER(C_INT) :: internal_boundary_present, boundary_formulation
-    INTEGER(C_INT) :: coarse_flag_mode, precision_mode
+    INTEGER(C_INT) :: coarse_flag_mode, precision_mode, outer_krylov
     REAL(C_DOUBLE) :: omega, restol_Poisson, restol_ad, ppp(6), outflow_area
   END TYPE fsi_mg_params
 
@@ -116,6 +116,7 @@ SUBROUTINE MG_initial()
   p%boundary_formulation = boundary_formulation
   p%coarse_flag_mode = 1
   p%precision_mode = fsi_mg_precision
+  p%outer_krylov = 0                         ! the reference's stationary outer iteration
   p%omega = omega; p%restol_Poisson = restol_Poisson; p%restol_ad = restol_ad
   p%ppp = [pppx1, pppx2, pppy1, pppy2, pppz1, pppz2]
   p%outflow_area = outflow_area

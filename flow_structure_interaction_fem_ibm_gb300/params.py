@@ -44,6 +44,7 @@ class FsiMgParams(ctypes.Structure):
         ("boundary_formulation", ctypes.c_int),
         ("coarse_flag_mode", ctypes.c_int),
         ("precision_mode", ctypes.c_int),
+        ("outer_krylov", ctypes.c_int),
         ("omega", ctypes.c_double),
         ("restol_Poisson", ctypes.c_double),
         ("restol_ad", ctypes.c_double),
@@ -77,6 +78,7 @@ class SolverParams:
     boundary_formulation: int = NO_INTERNAL_BOUNDARY
     coarse_flag_mode: int = 0
     precision_mode: int = PRECISION_FP64
+    outer_krylov: int = 0
     omega: float = 1.0
     restol_Poisson: float = 1e-8
     restol_ad: float = 1e-13

@@ -42,6 +42,7 @@ typedef struct {
     int boundary_formulation; /* 0 none, 2 GCM */
     int coarse_flag_mode;     /* 0 reference (stale coarse flags without a body), 1 recompute */
     int precision_mode;       /* unused by the oracle */
+    int outer_krylov;         /* unused by the oracle */
     double omega, restol_Poisson, restol_ad;
     double ppp[6];            /* Dirichlet pressure values x1,x2,y1,y2,z1,z2 */
     double outflow_area;

@@ -145,3 +145,29 @@ def test_outflow_compatibility_and_nlw0(gpu_built):
     assert np.allclose(s.pgrad(), o.pgrad(), rtol=1e-10, atol=1e-12)
     assert np.abs(s.pgrad()).max() > 0 and np.abs(nlw0).max() > 0
     s.close()
+
+
+@pytest.mark.parametrize("name,make", problems(), ids=[c[0] for c in problems()])
+@pytest.mark.parametrize("mode", [0, 1], ids=["fp64", "mixed"])
+def test_fgmres_outer_solve_reaches_reference_pressure(name, make, mode, gpu_built):
+    """FGMRES(m) around MG_Solver solves the same system to the same max-norm
+    tolerance: converged pressure within 1e-10 (FP64) / 1e-8 (mixed at 1e-10
+    tolerance) of the oracle, in fewer MG cycles than the stationary iteration."""
+    pr = make()
+    tol = (1e-12 if mode == 0 else 1e-10) * abs(pr.nlu0).max()
+    ref = Oracle(make(restol_Poisson=1e-12 * abs(pr.nlu0).max())).solve()
+    stat = solve(make(restol_Poisson=tol, precision_mode=mode))
+    kry = solve(make(restol_Poisson=tol, precision_mode=mode, outer_krylov=30))
+    assert kry["status"] == 0 and kry["maxres"] <= tol
+    m, v, I = mask_vol(pr)
+    err = rel_l2_mean_free(kry["p"][I], ref["p"][I], m, v)
+    assert err <= (1e-10 if mode == 0 else 1e-8), err
+    assert kry["iters"] <= stat["iters"]
+
+
+def test_fgmres_rejects_nonlinear_outflow(gpu_built):
+    pr = sphere_problem(12, stretch=None)
+    pr.params.bc = (1, 2, 1, 1, 1, 1)
+    pr.params.outer_krylov = 10
+    with pytest.raises(FsiMgError):
+        solve(pr)
