@@ -23,6 +23,7 @@ replica and value is the sum over ranks.
 from __future__ import annotations
 
 import argparse
+import copy
 import json
 import os
 import subprocess
@@ -51,6 +52,7 @@ def parse():
     ap.add_argument("--seed", type=int, default=3)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--krylov", type=int, default=30, help="FGMRES restart length around MG_Solver (0: stationary)")
     ap.add_argument("--profile", action="store_true",
                     help="profiling driver: raw RHS, two outer iterations of each precision, no other work")
     return ap.parse_args()
@@ -121,37 +123,43 @@ def build_problem(n, seed, tol, solver_cls):
     pr = P.sphere(n, seed=seed, stretch=1.5)
     # discrete compatibility shift from two GPU solves run to their residual plateau
     def stagnated(f):
-        saved = (pr.params.iterMax_Poisson, pr.params.restol_Poisson, pr.params.precision_mode)
-        pr.params.restol_Poisson, pr.params.precision_mode = 0.0, 1
-        solvers = {}
+        pp = copy.deepcopy(pr.params)
+        pp.restol_Poisson, pp.precision_mode, pp.outer_krylov = 0.0, 1, 0
 
-        def chunk_fn(rhs, p0, iters):
-            pr.params.iterMax_Poisson = iters
-            s = solvers.get(iters)
-            if s is None:
-                s = solvers[iters] = solver_cls(pr.params, pr.x, pr.y, pr.z).set_boundary(pr.geom)
+        def solve_from_zero(rhs, iters):
+            pp.iterMax_Poisson = iters
+            s = solver_cls(pp, pr.x, pr.y, pr.z).set_boundary(pr.geom)
+            p0 = np.zeros(pr.shape, order="F")
             s.solve_poisson(p0, rhs)
-            return p0, s.residual_history()
-
-        p = P.stall_until_plateau(chunk_fn, f, pr.shape, chunk=25)
-        for s in solvers.values():
+            h = s.residual_history()
             s.close()
-        pr.params.iterMax_Poisson, pr.params.restol_Poisson, pr.params.precision_mode = saved
-        return p
+            return p0, h
+
+        return P.stall_until_plateau(solve_from_zero, f, iters=150, rtol=1e-5)
     shift = P.make_compatible(pr, stagnated)
     pr.params.restol_Poisson = tol * float(np.abs(pr.nlu0).max())
     pr.params.iterMax_Poisson = 500
     return pr, shift
 
 
+_ORACLE = {}
+
+
 def oracle_iteration_time(n, seed, reps=1):
-    """Seconds per outer iteration of the oracle (serial reference MG) at n^3."""
+    """Seconds per outer iteration of the oracle (serial reference MG with the
+    reference's line ordering, iRedBlack 0) at n^3: MG_Solver,
+    GCM_correct_pressure and calc_residual, as in IBM/CORE_POISSON.F90:640-663.
+    The oracle is built once per process."""
     from flow_structure_interaction_fem_ibm_gb300 import problem as P
     from oracle.oracle import Oracle
-    pr = P.sphere(n, seed=seed, stretch=1.5)
-    o = Oracle(pr)
-    p = np.zeros(pr.shape, order="F")
-    o.subtract_average(p)
+    key = (n, seed)
+    if key not in _ORACLE:
+        pr = P.sphere(n, seed=seed, stretch=1.5)
+        o = Oracle(pr)
+        p = np.zeros(pr.shape, order="F")
+        o.subtract_average(p)
+        _ORACLE[key] = (pr, o, p)
+    pr, o, p = _ORACLE[key]
     t0 = time.perf_counter()
     for _ in range(reps):
         o.mg_solver(p, pr.nlu0)
@@ -160,9 +168,19 @@ def oracle_iteration_time(n, seed, reps=1):
     return (time.perf_counter() - t0) / reps
 
 
-def oracle_iterations(n, seed, tol):
-    """Outer iterations the oracle needs on the same recipe at n^3 (MG iteration
-    counts are nearly size-independent)."""
+# Outer iterations the reference's stationary solve_poisson needs on this
+# workload (same recipe and compatibility shift, reference line ordering),
+# measured with the oracle: the full solve is hours of serial CPU time at
+# 256^3, so the timed CPU sample is one iteration and the count comes from here.
+REFERENCE_ITERATIONS = {}
+
+
+def reference_iterations(n, seed, tol):
+    key = (n, seed, tol)
+    if key in REFERENCE_ITERATIONS:
+        return REFERENCE_ITERATIONS[key], "measured with the oracle (table in bench.py)"
+    if n > 64:
+        raise SystemExit(f"no reference iteration count recorded for n={n}, seed={seed}, tol={tol:g}")
     from flow_structure_interaction_fem_ibm_gb300 import problem as P
     from oracle.oracle import Oracle
     pr = P.sphere(n, seed=seed, stretch=1.5)
@@ -170,17 +188,17 @@ def oracle_iterations(n, seed, tol):
     def stagnated(f):
         q = P.Problem(pr.params, pr.x, pr.y, pr.z, pr.geom, f, pr.name)
 
-        def chunk_fn(rhs, p0, iters):
+        def solve_from_zero(rhs, iters):
             q.nlu0 = rhs
-            r = Oracle(q, iterMax_Poisson=iters, restol_Poisson=0.0).solve(p0)
+            r = Oracle(q, iterMax_Poisson=iters, restol_Poisson=0.0).solve()
             return r["p"], r["hist"]
 
-        return P.stall_until_plateau(chunk_fn, f, pr.shape, chunk=30)
+        return P.stall_until_plateau(solve_from_zero, f)
 
     P.make_compatible(pr, stagnated)
     pr.params.restol_Poisson = tol * float(np.abs(pr.nlu0).max())
-    pr.params.iterMax_Poisson = 500
-    return Oracle(pr).solve()["iters"]
+    pr.params.iterMax_Poisson = 4000
+    return Oracle(pr).solve()["iters"], "oracle solve at this size"
 
 
 def _replica(args):
@@ -188,23 +206,15 @@ def _replica(args):
     return oracle_iteration_time(n, seed)
 
 
-def cpu_reference(n_full, seed, tol, sample_n=128, cores=1):
-    """Reference-algorithm solves/s at n_full^3 from a bounded sample: one outer
-    iteration at sample_n^3 per core (independent replicas), scaled by the cell
-    count ratio and the oracle's own iteration count."""
-    iters = oracle_iterations(48, seed, tol)
-    scale = (n_full / sample_n) ** 3
-    if cores <= 1:
-        t = oracle_iteration_time(sample_n, seed)
-        per_core = [t]
-    else:
-        import multiprocessing as mp
-        ctx = mp.get_context("spawn")
-        with ctx.Pool(cores) as pool:
-            per_core = pool.map(_replica, [(sample_n, seed)] * cores)
-    t_iter = float(np.mean(per_core)) * scale
-    value = len(per_core) / (t_iter * iters)
-    return value, iters, t_iter, per_core
+def profile_traffic(n):
+    """DRAM bytes per launch of the level-1 FP32 line relaxation from the
+    committed ncu summary for this grid (None when there is none)."""
+    import re
+    f = ROOT / "profiles" / f"line_relaxation_fp32_{n}.md"
+    if not f.exists():
+        return None
+    m = re.search(r"traffic_bytes_per_launch:\s*([0-9.eE+]+)", f.read_text())
+    return float(m.group(1)) if m else None
 
 
 def run_reference(args, rank, world):
@@ -212,12 +222,19 @@ def run_reference(args, rank, world):
         print(json.dumps({"impl": "reference", "rank": rank, "skipped": True}), file=sys.stderr)
         return
     cores = os.cpu_count() or 1
+    sample_n = min(args.n, 128)
+    iters, src = reference_iterations(args.n, args.seed, args.tol)
+    scale = (args.n / sample_n) ** 3
     t0 = time.perf_counter()
+    import multiprocessing as mp
+    ctx = mp.get_context("spawn")
     vals = []
-    for s in range(args.warmup + args.steps):
-        v, iters, t_iter, per = cpu_reference(args.n, args.seed, args.tol, sample_n=64, cores=cores)
-        if s >= args.warmup:
-            vals.append(v)
+    with ctx.Pool(cores) as pool:
+        for s in range(args.warmup + args.steps):
+            per_core = pool.map(_replica, [(sample_n, args.seed)] * cores)
+            t_iter = float(np.mean(per_core)) * scale
+            if s >= args.warmup:
+                vals.append(cores / (t_iter * iters))
     value = float(np.median(vals))
     out = {
         "impl": "reference", "metric": METRIC, "value": value, "unit": "solves/s", "n_gpus": args.gpus,
@@ -226,13 +243,18 @@ def run_reference(args, rank, world):
         "config": {"workload": f"sphere_{args.n}^3_tanh1.5_r0.15_tol{args.tol:g}", "grid": args.n,
                    "tol": args.tol, "parallelism": f"{cores} independent serial replicas"},
         "cpu_baseline": {"value": value, "unit": "solves/s", "cores": cores, "kind": "port",
-                         "sample": (f"one outer iteration (MG_Solver + GCM_correct_pressure + calc_residual) at 64^3 "
-                                    f"per core, scaled by cell count to {args.n}^3, times the oracle's own "
-                                    f"iteration count at 48^3 ({iters})")},
+                         "sample": (f"one outer iteration (MG_Solver + GCM_correct_pressure + calc_residual) at "
+                                    f"{sample_n}^3 per core, scaled by cell count to {args.n}^3, times the "
+                                    f"reference's stationary iteration count {iters} ({src})")},
         "e2e": {"value": value, "unit": "solves/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
         "wall_s": time.perf_counter() - t0,
     }
     print(json.dumps(out))
+
+
+def cpu_iteration_time(seed, sample_n=128):
+    oracle_iteration_time(sample_n, seed)   # builds the oracle (not timed)
+    return oracle_iteration_time(sample_n, seed), sample_n
 
 
 def main():
@@ -253,7 +275,6 @@ def main():
     from flow_structure_interaction_fem_ibm_gb300.poisson import PoissonSolver
 
     if args.profile:
-        import copy
         from flow_structure_interaction_fem_ibm_gb300 import problem as P
         pr = P.sphere(args.n, seed=args.seed, stretch=1.5)
         for mode in (1, 0):
@@ -268,23 +289,29 @@ def main():
 
     t_setup = time.perf_counter()
     pr, shift = build_problem(args.n, args.seed, args.tol, PoissonSolver)
-    import copy
-    p_mixed = copy.deepcopy(pr.params); p_mixed.precision_mode = 1
-    p_fp64 = copy.deepcopy(pr.params); p_fp64.precision_mode = 0
-    s_mixed = PoissonSolver(p_mixed, pr.x, pr.y, pr.z).set_boundary(pr.geom)
-    s_fp64 = PoissonSolver(p_fp64, pr.x, pr.y, pr.z).set_boundary(pr.geom)
+    restol = pr.params.restol_Poisson
+
+    def make(mode, krylov, **kw):
+        q = copy.deepcopy(pr.params)
+        q.precision_mode, q.outer_krylov = mode, krylov
+        for k, v in kw.items():
+            setattr(q, k, v)
+        return PoissonSolver(q, pr.x, pr.y, pr.z).set_boundary(pr.geom)
+
+    s_mixed = make(1, args.krylov)
+    s_fp64 = make(0, args.krylov)
     sh = pr.shape
     b = torch.from_numpy(np.ascontiguousarray(pr.nlu0.transpose(2, 1, 0))).cuda()
     p = torch.zeros(sh[::-1], dtype=torch.float64, device="cuda")
     setup_s = time.perf_counter() - t_setup
 
-    def step(solver):
+    def step(solver, must_converge=True):
         p.zero_()
         torch.cuda.current_stream().synchronize()
         st, it, mr, loc, dev_s = solver.solve_poisson_device(p.data_ptr(), b.data_ptr())
-        if st != 0:
+        if st != 0 and must_converge:
             raise RuntimeError(f"solve did not converge: status {st}, {it} iterations, maxres {mr}")
-        return it, dev_s, solver.stats()["launches"]
+        return st, it, dev_s
 
     def timed(solver, k, w):
         for _ in range(w):
@@ -296,7 +323,7 @@ def main():
         dev, iters = [], []
         t0 = time.perf_counter()
         for _ in range(k):
-            it, d, _ = step(solver)
+            _, it, d = step(solver)
             dev.append(d)
             iters.append(it)
         torch.cuda.synchronize()
@@ -309,86 +336,120 @@ def main():
             tot = float(t.item())
         return tot, wall, iters, launches
 
+    # headline: mixed precision, FGMRES(m) around the MG cycle; level-1 line launches event-timed
+    s_mixed.line_timing(1)   # graphs are captured with the event records during the warm-up
+    for _ in range(args.warmup):
+        step(s_mixed)
+    s_mixed.line_timing(1)   # reset the counters
     with ClockSampler(local) as clk:
-        mixed_s, mixed_wall, mixed_iters, mixed_launch = timed(s_mixed, args.steps, args.warmup)
+        mixed_s, mixed_wall, mixed_iters, mixed_launch = timed(s_mixed, args.steps, 0)
     clocks = clk.summary()
-    fp64_s, fp64_wall, fp64_iters, _ = timed(s_fp64, max(2, args.steps // 2), 1)
+    lt = s_mixed.line_timing(0)["fp32"]
     value = world * args.steps / mixed_s
-    fp64_value = world * max(2, args.steps // 2) / fp64_s
 
-    # error of the mixed solution vs the FP64 solution on the same inputs
-    step(s_mixed)
-    pm = p.clone()
-    step(s_fp64)
-    pf = p.clone()
+    k64 = max(2, args.steps // 2)
+    fp64_s, fp64_wall, fp64_iters, _ = timed(s_fp64, k64, 1)
+    fp64_value = world * k64 / fp64_s
+
+    # the reference's own stationary outer iteration (outer_krylov = 0), mixed: one full solve
+    s_stat = make(1, 0, iterMax_Poisson=4000)
+    st_stat, it_stat, dev_stat = step(s_stat, must_converge=False)
+    s_stat.close()
+    # FP64 stationary: time per outer iteration (the solve needs the same iteration count)
+    s_stat64 = make(0, 0, iterMax_Poisson=12, restol_Poisson=0.0)
+    step(s_stat64, must_converge=False)
+    _, it64, dev64 = step(s_stat64, must_converge=False)
+    s_stat64.close()
+    stationary = {
+        "mixed": {"status": st_stat, "iters": it_stat, "seconds": dev_stat,
+                  "solves_per_s": (1.0 / dev_stat) if st_stat == 0 else None},
+        "fp64": {"ms_per_iteration": 1e3 * dev64 / it64,
+                 "projected_seconds": dev64 / it64 * it_stat,
+                 "note": "FP64 stationary solve = mixed stationary iteration count x measured FP64 time per iteration"},
+    }
+
+    # errors: mixed vs FP64 at the same tolerance, and vs an FP64 solve at restol/100
     fl = 1.0 - torch.from_numpy(np.ascontiguousarray(pr.geom.iblank.transpose(2, 1, 0))).cuda().double()
     n = args.n
     I = (slice(1, n + 1),) * 3
-    a, c_, f = pm[I] * fl[I], pf[I] * fl[I], fl[I]
-    a = a - a.sum() / f.sum() * f
-    c_ = c_ - c_.sum() / f.sum() * f
-    err = float(torch.linalg.vector_norm(a - c_) / torch.linalg.vector_norm(c_))
 
-    # e2e through the host-buffer C ABI, pinned buffers
+    def mean_free(t):
+        a = t[I] * fl[I]
+        return a - a.sum() / fl[I].sum() * fl[I]
+
+    step(s_mixed)
+    pm = mean_free(p.clone())
+    step(s_fp64)
+    pf = mean_free(p.clone())
+    err = float(torch.linalg.vector_norm(pm - pf) / torch.linalg.vector_norm(pf))
+    s_tight = make(0, args.krylov, restol_Poisson=restol * 1e-2, iterMax_Poisson=150)
+    st_t, it_t, _ = step(s_tight, must_converge=False)
+    s_tight.close()
+    pt = mean_free(p.clone())
+    err_tight = float(torch.linalg.vector_norm(pm - pt) / torch.linalg.vector_norm(pt))
+    err64_tight = float(torch.linalg.vector_norm(pf - pt) / torch.linalg.vector_norm(pt))
+
+    # e2e through the host-buffer C ABI (fsi_mg_solve), pinned buffers
     e2e = None
     if not args.no_e2e:
         hp = torch.zeros(sh[::-1], dtype=torch.float64, pin_memory=True)
         hb = torch.from_numpy(np.ascontiguousarray(pr.nlu0.transpose(2, 1, 0))).pin_memory()
         hp_np = hp.numpy().transpose(2, 1, 0)
         hb_np = hb.numpy().transpose(2, 1, 0)
-        for _ in range(1):
-            hp_np[...] = 0.0
-            s_mixed.solve_poisson(hp_np, hb_np)
+        hp_np[...] = 0.0
+        s_mixed.solve_poisson(hp_np, hb_np)
         tot = 0.0
         k = max(2, args.steps // 2)
         for _ in range(k):
             hp_np[...] = 0.0
             st, it, mr, loc, _ = s_mixed.solve_poisson(hp_np, hb_np)
+            if st != 0:
+                raise RuntimeError(f"e2e solve did not converge: status {st}")
             tot += s_mixed.stats()["e2e_seconds"]
         nbytes = int(np.prod(sh)) * 8
         e2e = {"value": world * k / tot, "unit": "solves/s", "h2d_bytes_per_step": 2 * nbytes,
                "d2h_bytes_per_step": nbytes}
 
-    # roofline of the dominant kernel family: level-1 FP32 line sweeps (one colour per launch)
+    # roofline of the dominant kernel: level-1 FP32 line relaxation (k_line_wp<float,dir,8>),
+    # durations from CUDA events around each launch inside the timed solves
     peaks = json.loads(PEAKS.read_text()) if PEAKS.exists() else {}
     peak = peaks.get("hbm_gbs", 6800.0)
-    kern = {}
-    for which, name in ((0, "line_x"), (1, "line_y"), (2, "line_z"), (3, "resid_restrict_x"),
-                        (4, "prolong_correct_x"), (5, "calc_residual")):
-        for prec in (1, 0):
-            ms, nb = s_mixed.time_kernel(which, prec, reps=20)
-            kern[f"{name}_{'fp32' if prec else 'fp64'}"] = {"ms": ms, "alg_bytes": nb,
-                                                           "gbs": nb / (ms * 1e-3) / 1e9}
-    line = [kern[f"line_{a}_fp32"] for a in "xyz"]
-    avg_ms = float(np.mean([q["ms"] for q in line]))
-    alg = line[0]["alg_bytes"]
-    achieved = alg / (avg_ms * 1e-3) / 1e9
+    avg_ms = lt["ms"] / max(lt["launches"], 1)
+    achieved = lt["alg_bytes"] / (avg_ms * 1e-3) / 1e9
+    traffic = profile_traffic(args.n)
     roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                "traffic": None, "kernel": "k_line<float> (x,y,z average, one colour per launch, level 1)",
-                "peak_source": "measured" if PEAKS.exists() else "fallback"}
+                "traffic": traffic, "kernel": "level-1 FP32 line relaxation, one colour per launch (x, y, z)",
+                "launches": lt["launches"], "avg_us": 1e3 * avg_ms, "alg_bytes_per_launch": lt["alg_bytes"],
+                "peak_source": "measured hbm_gbs" if PEAKS.exists() else "fallback"}
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
-        v, iters, t_iter, per = cpu_reference(args.n, args.seed, args.tol, sample_n=128, cores=1)
-        cpu = {"value": v, "unit": "solves/s", "cores": 1, "kind": "port",
-               "sample": (f"one outer iteration of the oracle (serial reference MG) at 128^3 "
-                          f"({per[0]:.2f} s), scaled by cell count x{(args.n / 128) ** 3:.0f}, times the oracle's "
-                          f"iteration count at 48^3 ({iters})")}
+        t_iter, sample_n = cpu_iteration_time(args.seed, sample_n=128)
+        t_iter *= (args.n / sample_n) ** 3
+        cpu = {"value": 1.0 / (t_iter * it_stat), "unit": "solves/s", "cores": 1, "kind": "port",
+               "sample": (f"one outer iteration of the oracle (serial reference MG, reference line ordering) "
+                          f"at {sample_n}^3, scaled by cell count x{(args.n / sample_n) ** 3:.0f}, times the "
+                          f"stationary iteration count measured on the GPU in this run ({it_stat})")}
 
     out = {
         "metric": METRIC, "value": value, "unit": "solves/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": 1e3 * mixed_s / args.steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32 cycle + f64 refinement", "data": "synthetic",
-        "config": {"workload": f"sphere_{args.n}^3_tanh1.5_r0.15_tol{args.tol:g}_mixed", "grid": args.n,
-                   "tol": args.tol, "stretch": 1.5, "radius": 0.15, "triangles": 5120, "nGhost": int(pr.geom.nGhost),
-                   "compat_shift": shift, "l2": "inputs larger than L2 (two 139 MB FP64 fields + hierarchy)",
+        "config": {"workload": f"sphere_{args.n}^3_tanh1.5_r0.15_tol{args.tol:g}_mixed_fgmres{args.krylov}",
+                   "grid": args.n, "tol": args.tol, "restol": restol, "stretch": 1.5, "radius": 0.15,
+                   "triangles": 5120, "nGhost": int(pr.geom.nGhost), "compat_shift": shift,
+                   "outer": f"FGMRES({args.krylov}) preconditioned by MG_Solver" if args.krylov else "stationary",
+                   "l2": "inputs larger than L2 (two 139 MB FP64 fields + hierarchy)",
                    "parallelism": "replicas" if world > 1 else "single GPU"},
-        "fp64_value": fp64_value, "fp64_ms_per_step": 1e3 * fp64_s / max(2, args.steps // 2),
-        "mixed_over_fp64": value / fp64_value, "mixed_vs_fp64_rel_l2": err,
-        "iters_mixed": mixed_iters[0], "iters_fp64": fp64_iters[0],
+        "fp64_value": fp64_value, "fp64_ms_per_step": 1e3 * fp64_s / k64,
+        "mixed_over_fp64": value / fp64_value,
+        "error": {"mixed_vs_fp64_rel_l2": err, "mixed_vs_fp64_tight_rel_l2": err_tight,
+                  "fp64_vs_fp64_tight_rel_l2": err64_tight, "tight_restol": restol * 1e-2,
+                  "tight_status": st_t, "tight_iters": it_t},
+        "iters_mixed": mixed_iters[0], "iters_fp64": fp64_iters[0], "stationary": stationary,
         "wall_ms_per_step": 1e3 * mixed_wall / args.steps,
         "gpu_launches": int(mixed_launch), "clocks": clocks, "e2e": e2e, "roofline": roofline,
-        "kernels": kern, "cpu_baseline": cpu, "setup_s": setup_s,
+        "cpu_baseline": cpu, "setup_s": setup_s,
     }
     if rank == 0:
         print(json.dumps(out))

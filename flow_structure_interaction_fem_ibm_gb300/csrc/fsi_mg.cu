@@ -134,6 +134,17 @@ struct Ctx {
     cudaGraphExec_t pgraph = nullptr;      // MG preconditioner on fixed buffers
     long long pgraph_kernels = 0;
 
+    // optional event timing of the level-1 line launches inside the solve graphs:
+    // pairs [lt_base, lt_base + 2*lt_pairs) of lt_ev belong to the graph being captured
+    bool lt_on = false;
+    std::vector<cudaEvent_t> lt_ev;
+    int lt_next = 0;
+    std::vector<int8_t> lt_f32;            // precision of each pair
+    int graph_lt0 = 0, graph_lt1 = 0;      // pair range of the outer-iteration graph
+    int pgraph_lt0 = 0, pgraph_lt1 = 0;    // pair range of the preconditioner graph
+    double lt_ms[2] = {0, 0};              // [FP64, FP32] summed launch durations
+    long long lt_n[2] = {0, 0};
+
     // stats
     std::vector<double> hist;   // max-norm residual after each outer iteration of the last solve
     int last_iters = 0;
@@ -145,6 +156,7 @@ struct Ctx {
         if (graph) cudaGraphExecDestroy(graph);
         if (pgraph) cudaGraphExecDestroy(pgraph);
         if (h_kdots) cudaFreeHost(h_kdots);
+        for (cudaEvent_t e : lt_ev) cudaEventDestroy(e);
         for (cudaEvent_t e : {ev0, ev1, ev2, ev3})
             if (e) cudaEventDestroy(e);
         for (void *a : allocs) cudaFree(a);
@@ -384,6 +396,19 @@ template <typename T> T *scratch_U(Ctx &c);
 template <> double *scratch_U<double>(Ctx &c) { return c.U64; }
 template <> float *scratch_U<float>(Ctx &c) { return c.U32; }
 
+// Adds the durations of the timed line launches [p0, p1) of a graph that has
+// completed on the stream (the caller has synchronised it).
+void lt_harvest(Ctx &c, int p0, int p1)
+{
+    for (int q = p0; q < p1; ++q) {
+        float ms = 0.0f;
+        if (cudaEventElapsedTime(&ms, c.lt_ev[2 * q], c.lt_ev[2 * q + 1]) == cudaSuccess) {
+            c.lt_ms[c.lt_f32[q]] += ms;
+            c.lt_n[c.lt_f32[q]]++;
+        }
+    }
+}
+
 // MG_itsolv: x-, y- (and z-) line sweeps, each red then black.
 template <typename T>
 void itsolv(Ctx &c, Level &L, T *v, const T *r, bool finest, bool homogeneous)
@@ -401,7 +426,14 @@ void itsolv(Ctx &c, Level &L, T *v, const T *r, bool finest, bool homogeneous)
         a.ppp_hi = homogeneous ? T(0) : (T)c.p.ppp[2 * dir + 1];
         for (int col = 0; col < 2; ++col) {
             a.colour = col;
+            const bool timed = c.lt_on && &L == &c.L1 && 2 * c.lt_next + 1 < (int)c.lt_ev.size();
+            if (timed) cudaEventRecord(c.lt_ev[2 * c.lt_next], c.s);
             launch_line<T>(dir, a, om1, c.s);
+            if (timed) {
+                cudaEventRecord(c.lt_ev[2 * c.lt_next + 1], c.s);
+                c.lt_f32[c.lt_next] = std::is_same<T, float>::value ? 1 : 0;
+                ++c.lt_next;
+            }
             c.launches++;
         }
     }
@@ -593,9 +625,11 @@ int run_outer(Ctx &c, double *p, const double *b)
     if (!c.graph) {
         cudaGraph_t g;
         const long long before = c.launches;
+        c.lt_next = c.graph_lt0 = 0;
         CK(cudaStreamBeginCapture(c.s, cudaStreamCaptureModeThreadLocal));
         outer_iteration(c, p, b);
         CK(cudaStreamEndCapture(c.s, &g));
+        c.graph_lt1 = c.lt_next;
         c.graph_kernels = c.launches - before;
         c.launches = before;
         cudaError_t e = cudaGraphInstantiate(&c.graph, g, 0);
@@ -652,6 +686,7 @@ int precondition(Ctx &c, const double *v, double *z)
     if (!c.pgraph) {
         cudaGraph_t g;
         const long long before = c.launches;
+        c.lt_next = c.pgraph_lt0 = (int)c.lt_ev.size() / 4;   // second half of the pairs
         CK(cudaStreamBeginCapture(c.s, cudaStreamCaptureModeThreadLocal));
         if (mixed) {
             launch_fill<float>(c.e32, n1, 0.0f, c.s);
@@ -662,6 +697,7 @@ int precondition(Ctx &c, const double *v, double *z)
         }
         c.launches++;
         CK(cudaStreamEndCapture(c.s, &g));
+        c.pgraph_lt1 = c.lt_next;
         c.pgraph_kernels = c.launches - before;
         c.launches = before;
         cudaError_t e = cudaGraphInstantiate(&c.pgraph, g, 0);
@@ -751,6 +787,7 @@ int solve_krylov(Ctx &c, double *p, const double *b, int *iters, double *maxres_
             c.launches += 4 * ((j + 8) / 8) * 2 + 3;
             CK(cudaMemcpyAsync(c.h_kdots, c.kdots, 256 * sizeof(double), cudaMemcpyDeviceToHost, c.s));
             CK(cudaStreamSynchronize(c.s));
+            if (c.lt_on) lt_harvest(c, c.pgraph_lt0, c.pgraph_lt1);
             for (int i = 0; i <= j; ++i) Hij(i, j) = c.h_kdots[i] + c.h_kdots[64 + i];
             const double hn = std::sqrt(c.h_kdots[128]);
             Hij(j + 1, j) = hn;
@@ -832,6 +869,7 @@ int solve_device(Ctx &c, double *p, const double *b, int *iters, double *maxres_
         TRY(run_outer(c, p, b));
         CK(cudaMemcpyAsync(c.h_result, c.result, sizeof(MaxLoc), cudaMemcpyDeviceToHost, c.s));
         CK(cudaStreamSynchronize(c.s));
+        if (c.lt_on) lt_harvest(c, c.graph_lt0, c.graph_lt1);
         maxres = c.h_result->v;
         maxidx = c.h_result->i;
         c.hist.push_back(maxres);
@@ -1509,6 +1547,41 @@ int fsi_mg_stats(void *handle, double *out, int n)
     const double v[8] = {(double)c.last_iters, c.last_maxres, c.last_time, (double)c.ghost_sweeps, (double)c.launches,
                          (double)c.bytes, c.last_wall, c.last_e2e};
     for (int q = 0; q < n && q < 8; ++q) out[q] = v[q];
+    return 0;
+}
+
+int fsi_mg_line_timing(void *handle, int enable, double *out)
+{
+    if (!handle) return fail(-1, "null handle");
+    Ctx &c = *(Ctx *)handle;
+    if (enable >= 0 && (enable != 0) != c.lt_on) {
+        CK(cudaStreamSynchronize(c.s));
+        if (enable && c.lt_ev.empty()) {
+            c.lt_ev.resize(2048);
+            c.lt_f32.assign(1024, 0);
+            for (auto &e : c.lt_ev) CK(cudaEventCreate(&e));
+        }
+        c.lt_on = enable != 0;
+        // the solve graphs are re-captured with (or without) the event records
+        if (c.graph) { cudaGraphExecDestroy(c.graph); c.graph = nullptr; }
+        if (c.pgraph) { cudaGraphExecDestroy(c.pgraph); c.pgraph = nullptr; }
+        c.graph_lt0 = c.graph_lt1 = c.pgraph_lt0 = c.pgraph_lt1 = 0;
+    }
+    if (enable == 1) {
+        c.lt_ms[0] = c.lt_ms[1] = 0.0;
+        c.lt_n[0] = c.lt_n[1] = 0;
+    }
+    if (out) {
+        // algorithmic bytes of one colour of a level-1 line sweep: the colour's
+        // rhs, flags and new values plus the other colour's values (omega = 1)
+        const double cells = (double)(c.nx - 1) * (c.ny - 1) * (c.p.ndim == 3 ? c.nz - 1 : 1);
+        out[0] = (double)c.lt_n[1];
+        out[1] = c.lt_ms[1];
+        out[2] = 0.5 * (4.0 + 1.0 + 4.0 + 4.0) * cells;
+        out[3] = (double)c.lt_n[0];
+        out[4] = c.lt_ms[0];
+        out[5] = 0.5 * (8.0 + 1.0 + 8.0 + 8.0) * cells;
+    }
     return 0;
 }
 

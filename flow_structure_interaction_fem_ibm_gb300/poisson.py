@@ -181,6 +181,15 @@ class PoissonSolver:
         _check(self.lib.fsi_mg_time_kernel(self.h, which, precision, reps, ctypes.byref(ms), ctypes.byref(nb)))
         return ms.value, nb.value
 
+    def line_timing(self, enable: int = -1):
+        """Event timing of the level-1 line launches inside solves (enable 1:
+        reset and start, 0: stop, -1: read).  Returns per precision the launch
+        count, summed ms and algorithmic bytes per launch."""
+        out = np.zeros(6)
+        _check(self.lib.fsi_mg_line_timing(self.h, enable, _p(out)))
+        return {"fp32": {"launches": int(out[0]), "ms": out[1], "alg_bytes": out[2]},
+                "fp64": {"launches": int(out[3]), "ms": out[4], "alg_bytes": out[5]}}
+
 
 def solve(problem, p0=None, **overrides):
     """Convenience: build a solver for ``problem``, solve from ``p0`` (zeros)."""

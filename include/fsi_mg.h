@@ -147,6 +147,16 @@ int fsi_mg_residual_history(void *handle, double *out, int cap);
  * bytes one launch moves.  No counterpart in the reference: a measurement hook. */
 int fsi_mg_time_kernel(void *handle, int which, int precision, int reps, double *avg_ms, double *alg_bytes);
 
+/* Event timing of the level-1 line-relaxation launches inside solves (the
+ * dominant kernel family).  enable = 1 resets the counters and turns the
+ * timing on, 0 turns it off, -1 only reads; the solve graphs are re-captured
+ * with a CUDA event pair around every level-1 line launch, read back after
+ * each outer (or Arnoldi) step, which synchronises anyway.  out[6] (may be
+ * NULL): FP32 launches, FP32 summed ms, FP32 algorithmic bytes per launch,
+ * FP64 launches, FP64 summed ms, FP64 algorithmic bytes per launch.  No
+ * counterpart in the reference: a measurement hook. */
+int fsi_mg_line_timing(void *handle, int enable, double *out);
+
 /* Text of the last error on this thread. */
 const char *fsi_mg_last_error(void);
 

@@ -9,21 +9,22 @@ from flow_structure_interaction_fem_ibm_gb300 import problem as P
 from oracle.oracle import Oracle
 
 
-def oracle_stagnated(problem, chunk=30):
-    """Stalled oracle pressure for the compatibility shift (runs to the plateau)."""
+def oracle_stagnated(problem):
+    """Stalled oracle pressure for the compatibility shift (one solve from zero,
+    run to the plateau)."""
     def run(f):
         q = P.Problem(problem.params, problem.x, problem.y, problem.z, problem.geom, f, problem.name)
-        saved = (problem.params.iterMax_Poisson, problem.params.restol_Poisson, problem.params.iRedBlack,
-                 problem.params.coarse_flag_mode)
 
-        def chunk_fn(rhs, p0, iters):
+        def solve_from_zero(rhs, iters):
             q.nlu0 = rhs
             o = Oracle(q, iterMax_Poisson=iters, restol_Poisson=0.0, iRedBlack=0, coarse_flag_mode=0)
-            r = o.solve(p0)
+            r = o.solve()
             o.close()
             return r["p"], r["hist"]
 
-        p = P.stall_until_plateau(chunk_fn, f, problem.shape, chunk=chunk)
+        saved = (problem.params.iterMax_Poisson, problem.params.restol_Poisson, problem.params.iRedBlack,
+                 problem.params.coarse_flag_mode)
+        p = P.stall_until_plateau(solve_from_zero, f)
         (problem.params.iterMax_Poisson, problem.params.restol_Poisson, problem.params.iRedBlack,
          problem.params.coarse_flag_mode) = saved
         return p
