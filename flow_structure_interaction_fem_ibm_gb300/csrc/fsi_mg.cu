@@ -405,6 +405,8 @@ void lt_harvest(Ctx &c, int p0, int p1)
         if (cudaEventElapsedTime(&ms, c.lt_ev[2 * q], c.lt_ev[2 * q + 1]) == cudaSuccess) {
             c.lt_ms[c.lt_f32[q]] += ms;
             c.lt_n[c.lt_f32[q]]++;
+        } else {
+            (void)cudaGetLastError();   // not recorded: skip without leaving the error pending
         }
     }
 }
@@ -427,10 +429,11 @@ void itsolv(Ctx &c, Level &L, T *v, const T *r, bool finest, bool homogeneous)
         for (int col = 0; col < 2; ++col) {
             a.colour = col;
             const bool timed = c.lt_on && &L == &c.L1 && 2 * c.lt_next + 1 < (int)c.lt_ev.size();
-            if (timed) cudaEventRecord(c.lt_ev[2 * c.lt_next], c.s);
+            // external records become event-record nodes when the stream is being captured
+            if (timed) cudaEventRecordWithFlags(c.lt_ev[2 * c.lt_next], c.s, cudaEventRecordExternal);
             launch_line<T>(dir, a, om1, c.s);
             if (timed) {
-                cudaEventRecord(c.lt_ev[2 * c.lt_next + 1], c.s);
+                cudaEventRecordWithFlags(c.lt_ev[2 * c.lt_next + 1], c.s, cudaEventRecordExternal);
                 c.lt_f32[c.lt_next] = std::is_same<T, float>::value ? 1 : 0;
                 ++c.lt_next;
             }

@@ -171,3 +171,24 @@ def test_fgmres_rejects_nonlinear_outflow(gpu_built):
     pr.params.outer_krylov = 10
     with pytest.raises(FsiMgError):
         solve(pr)
+
+
+@pytest.mark.parametrize("krylov", [0, 30])
+def test_line_timing_counts_level1_launches(gpu_built, krylov):
+    """The event-timing hook records every level-1 line launch of a solve
+    (48 per MG_Solver in 3D) and leaves no CUDA error pending."""
+    import torch
+    pr = sphere_problem(16, stretch=1.5)
+    pr.params.precision_mode = 1
+    pr.params.outer_krylov = krylov
+    s = PoissonSolver(pr.params, pr.x, pr.y, pr.z).set_boundary(pr.geom)
+    s.line_timing(1)
+    p = np.zeros(pr.shape, order="F")
+    st, it, mr, loc, _ = s.solve_poisson(p, pr.nlu0)
+    t = s.line_timing(0)
+    s.close()
+    assert st == 0
+    assert t["fp32"]["launches"] == 48 * it
+    assert t["fp32"]["ms"] > 0.0
+    assert t["fp64"]["launches"] == 0
+    torch.zeros(4, device="cuda").sum().item()   # raises if an error were left pending
