@@ -958,6 +958,8 @@ int fsi_mg_create(const fsi_mg_params *params, const double *x, const double *y,
     if (p.omega <= 0.0 || p.omega >= 2.0) return fail(-1, "omega must be in (0,2)");
     if (p.precision_mode != 0 && p.precision_mode != 1) return fail(-1, "precision_mode must be 0 or 1");
     if (p.outer_krylov < 0 || p.outer_krylov > 60) return fail(-1, "outer_krylov must be in 0..60");
+    if ((long long)(p.nx + 1) * (p.ny + 1) * (p.nz + 1) >= (1LL << 31))
+        return fail(-1, "grid too large: the (0:nx+1,0:ny+1,0:nz+1) layout must hold fewer than 2^31 cells");
     int ndev = 0;
     if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return fail(-12, "no CUDA device");
     CK(init_kernels());

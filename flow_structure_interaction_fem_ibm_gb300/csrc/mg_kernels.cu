@@ -136,22 +136,41 @@ constexpr int WP_LINES = 8;
 
 template <int S> __host__ __device__ constexpr int wp_pitch() { return 32 * (S + 1) + 4; }
 
+// Reciprocal used by the partition solver: IEEE division in FP64; the fast
+// approximate reciprocal (about 1 ulp) in FP32, where the smoother only
+// produces a correction inside FP64 refinement.
+template <typename T> __device__ __forceinline__ T wp_rcp(T x);
+template <> __device__ __forceinline__ float wp_rcp<float>(float x) { return __fdividef(1.0f, x); }
+template <> __device__ __forceinline__ double wp_rcp<double>(double x) { return 1.0 / x; }
+
+// One parallel-cyclic-reduction step over the warp at distance h.  Each lane
+// keeps its row (A, B, C, D) and 1/B; rows outside the system are identity
+// rows (A = C = D = 0, B = 1).
 template <typename T>
-__device__ __forceinline__ void pcr_step(T &A, T &B, T &C, T &D, int lane, int h)
+__device__ __forceinline__ void pcr_step(T &A, T &B, T &C, T &D, T &iB, int lane, int h)
 {
-    T Am = __shfl_up_sync(0xffffffffu, A, h), Bm = __shfl_up_sync(0xffffffffu, B, h);
+    T Am = __shfl_up_sync(0xffffffffu, A, h), iBm = __shfl_up_sync(0xffffffffu, iB, h);
     T Cm = __shfl_up_sync(0xffffffffu, C, h), Dm = __shfl_up_sync(0xffffffffu, D, h);
-    T Ap = __shfl_down_sync(0xffffffffu, A, h), Bp = __shfl_down_sync(0xffffffffu, B, h);
+    T Ap = __shfl_down_sync(0xffffffffu, A, h), iBp = __shfl_down_sync(0xffffffffu, iB, h);
     T Cp = __shfl_down_sync(0xffffffffu, C, h), Dp = __shfl_down_sync(0xffffffffu, D, h);
-    if (lane < h) { Am = T(0); Bm = T(1); Cm = T(0); Dm = T(0); }
-    if (lane + h > 31) { Ap = T(0); Bp = T(1); Cp = T(0); Dp = T(0); }
-    const T k1 = A / Bm, k2 = C / Bp;
+    if (lane < h) { Am = T(0); iBm = T(1); Cm = T(0); Dm = T(0); }
+    if (lane + h > 31) { Ap = T(0); iBp = T(1); Cp = T(0); Dp = T(0); }
+    const T k1 = A * iBm, k2 = C * iBp;
     const T nA = -k1 * Am, nC = -k2 * Cp;
     const T nB = B - k1 * Cm - k2 * Ap;
     const T nD = D - k1 * Dm - k2 * Dp;
     A = nA; B = nB; C = nC; D = nD;
+    iB = wp_rcp(nB);
 }
 
+// Warp-per-line partition solver for one colour of a line sweep (lines of
+// L <= 32*S cells).  A CTA owns WP_LINES lines of one colour.  Staging:
+// x-lines are read by one warp per line along the line (coalesced); y- and
+// z-lines by 8 lines side by side (consecutive same-colour lines).  Each lane
+// then eliminates its S consecutive rows in registers (partition method),
+// the 32 interface unknowns of the line are solved by PCR over shuffles, and
+// the rows are back-substituted and written through shared memory.  Index
+// arithmetic is 32-bit (level-1 arrays hold fewer than 2^31 cells).
 template <typename T, int DIR, int S, bool OMEGA1>
 __global__ void __launch_bounds__(256) k_line_wp(LineArgs<T> A)
 {
@@ -163,92 +182,103 @@ __global__ void __launch_bounds__(256) k_line_wp(LineArgs<T> A)
     const Dims &d = A.d;
     const int nb = d.m[X::b] - 1, nc = d.m[X::c] - 1, L = d.m[X::a] - 1;
     const int hb = (nb + 1) >> 1;
-    const long long nlines = (long long)hb * nc;
-    const long long sa_ = stride_of(d, X::a), sb_ = stride_of(d, X::b), sc_ = stride_of(d, X::c);
+    const int nlines = hb * nc;
+    const int sa_ = (int)stride_of(d, X::a), sb_ = (int)stride_of(d, X::b), sc_ = (int)stride_of(d, X::c);
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
 
     // line g of this CTA -> (p, q); invalid lines (beyond the count or p > nb) are skipped
     auto line_pq = [&](int g, int &p, int &q) -> bool {
-        const long long t = (long long)blockIdx.x * WP_LINES + g;
+        const int t = (int)blockIdx.x * WP_LINES + g;
         if (t >= nlines) return false;
-        q = 1 + (int)(t / hb);
+        const int tq = t / hb;
+        q = 1 + tq;
         const int p0 = (((1 + q) & 1) == A.colour) ? 1 : 2;
-        p = p0 + 2 * (int)(t % hb);
+        p = p0 + 2 * (t - tq * hb);
         return p <= nb;
     };
     auto sidx = [&](int g, int r) { return g * RP + r + r / S; };
 
-    // ---- 1. staging (loads for up to 4 rows per thread are issued before any use) ----
-    struct RowIn { uint8_t f; T r, nb0, nb1, nb2, nb3, vo; int p, q; bool ok; };
-    auto load_row = [&](int g, int r, RowIn &in) {
-        int p = 0, q = 0;
-        in.ok = (r < L) && line_pq(g, p, q);
-        in.p = p; in.q = q;
-        if (!in.ok) return;
-        const long long o = (long long)p * sb_ + (long long)q * sc_ + (long long)(r + 1) * sa_;
-        in.f = A.fl[o];
-        in.r = A.r[o];
-        in.vo = A.v[o];
-        if (X::c_first) {
-            in.nb0 = A.v[o - sc_]; in.nb1 = A.v[o + sc_]; in.nb2 = A.v[o - sb_]; in.nb3 = A.v[o + sb_];
-        } else {
-            in.nb0 = A.v[o - sb_]; in.nb1 = A.v[o + sb_]; in.nb2 = A.v[o - sc_]; in.nb3 = A.v[o + sc_];
-        }
-    };
-    auto finish_row = [&](int g, int r, const RowIn &in) {
-        if (!in.ok) return;
-        const int i = r + 1, p = in.p, q = in.q;
-        const uint8_t f = in.f;
-        const bool fluid = !(f & FB_IB);
-        const T ama = (f & fb_minus(X::a)) ? T(0) : A.c.cm[X::a][i];
-        const T apa = (f & fb_plus(X::a)) ? T(0) : A.c.cp[X::a][i];
-        const T amb = (f & fb_minus(X::b)) ? T(0) : A.c.cm[X::b][p];
-        const T apb = (f & fb_plus(X::b)) ? T(0) : A.c.cp[X::b][p];
-        const T amc = (f & fb_minus(X::c)) ? T(0) : A.c.cm[X::c][q];
-        const T apc = (f & fb_plus(X::c)) ? T(0) : A.c.cp[X::c][q];
-        const bool allzero = (ama == T(0)) & (apa == T(0)) & (amb == T(0)) & (apb == T(0)) & (amc == T(0)) & (apc == T(0));
-        const bool normal = fluid && !allzero;
-        T aa = T(0), bb = T(1), cc = T(0), dd;
-        if (normal) {
-            T sdd = in.r;
-            if (X::c_first) {
-                sdd = sdd - in.nb0 * amc;
-                sdd = sdd - in.nb1 * apc;
-                sdd = sdd - in.nb2 * amb;
-                sdd = sdd - in.nb3 * apb;
-            } else {
-                sdd = sdd - in.nb0 * amb;
-                sdd = sdd - in.nb1 * apb;
-                sdd = sdd - in.nb2 * amc;
-                sdd = sdd - in.nb3 * apc;
-            }
-            dd = sdd;
-            T am3[3], ap3[3];   // diagonal as the reference sums it: (acx + acy) + acz
-            am3[X::a] = ama; ap3[X::a] = apa; am3[X::b] = amb; ap3[X::b] = apb; am3[X::c] = amc; ap3[X::c] = apc;
-            bb = (-(am3[0] + ap3[0]) + -(am3[1] + ap3[1])) + -(am3[2] + ap3[2]);
-            aa = ama;
-            cc = apa;
-        } else {
-            dd = ((f & FB_GM) || fluid) ? in.vo : T(0);
-        }
-        if (i == 1 && A.dir_lo) dd = dd - A.ppp_lo * aa;
-        if (i == L && A.dir_hi) dd = dd - A.ppp_hi * cc;
-        if (i == 1) aa = T(0);   // tdma ignores a(n1) and c(n2)
-        if (i == L) cc = T(0);
-        const int si = sidx(g, r);
-        sa[si] = aa; sb[si] = bb; sc[si] = cc; sd[si] = dd;
-    };
-    {
+    // the line this thread stages and stores, and its row offset within the line
+    const int gs = (DIR == 0) ? warp : (tid & (WP_LINES - 1));
+    const int rr = (DIR == 0) ? lane : (tid >> 3);
+    int ps = 1, qs = 1;
+    const bool oks = line_pq(gs, ps, qs);
+    const int base = ps * sb_ + qs * sc_;
+
+    // ---- 1. staging: loads for up to 4 rows are issued before any use ----
+    if (oks) {
+        // transverse coefficients are constant along the line
+        const T cmb = A.c.cm[X::b][ps], cpb = A.c.cp[X::b][ps];
+        const T cmc = A.c.cm[X::c][qs], cpc = A.c.cp[X::c][qs];
+        struct RowIn { uint8_t f; T r, nb0, nb1, nb2, nb3, vo; };
         constexpr int GRP = (S < 4) ? S : 4;
-        const int g = (DIR == 0) ? warp : (tid & (WP_LINES - 1));
-        const int rr = (DIR == 0) ? lane : (tid >> 3);
 #pragma unroll
         for (int q0 = 0; q0 < S; q0 += GRP) {
             RowIn in[GRP];
 #pragma unroll
-            for (int u = 0; u < GRP; ++u) load_row(g, (q0 + u) * 32 + rr, in[u]);
+            for (int u = 0; u < GRP; ++u) {
+                const int r = (q0 + u) * 32 + rr;
+                if (r < L) {
+                    const int o = base + (r + 1) * sa_;
+                    in[u].f = A.fl[o];
+                    in[u].r = A.r[o];
+                    in[u].vo = A.v[o];
+                    if (X::c_first) {
+                        in[u].nb0 = A.v[o - sc_]; in[u].nb1 = A.v[o + sc_];
+                        in[u].nb2 = A.v[o - sb_]; in[u].nb3 = A.v[o + sb_];
+                    } else {
+                        in[u].nb0 = A.v[o - sb_]; in[u].nb1 = A.v[o + sb_];
+                        in[u].nb2 = A.v[o - sc_]; in[u].nb3 = A.v[o + sc_];
+                    }
+                }
+            }
 #pragma unroll
-            for (int u = 0; u < GRP; ++u) finish_row(g, (q0 + u) * 32 + rr, in[u]);
+            for (int u = 0; u < GRP; ++u) {
+                const int r = (q0 + u) * 32 + rr;
+                if (r >= L) continue;
+                const int i = r + 1;
+                const uint8_t f = in[u].f;
+                const bool fluid = !(f & FB_IB);
+                const T ama = (f & fb_minus(X::a)) ? T(0) : A.c.cm[X::a][i];
+                const T apa = (f & fb_plus(X::a)) ? T(0) : A.c.cp[X::a][i];
+                const T amb = (f & fb_minus(X::b)) ? T(0) : cmb;
+                const T apb = (f & fb_plus(X::b)) ? T(0) : cpb;
+                const T amc = (f & fb_minus(X::c)) ? T(0) : cmc;
+                const T apc = (f & fb_plus(X::c)) ? T(0) : cpc;
+                const bool allzero = (ama == T(0)) & (apa == T(0)) & (amb == T(0)) & (apb == T(0)) &
+                                     (amc == T(0)) & (apc == T(0));
+                const bool normal = fluid && !allzero;
+                T aa = T(0), bb = T(1), cc = T(0), dd;
+                if (normal) {
+                    T sdd = in[u].r;
+                    if (X::c_first) {
+                        sdd = sdd - in[u].nb0 * amc;
+                        sdd = sdd - in[u].nb1 * apc;
+                        sdd = sdd - in[u].nb2 * amb;
+                        sdd = sdd - in[u].nb3 * apb;
+                    } else {
+                        sdd = sdd - in[u].nb0 * amb;
+                        sdd = sdd - in[u].nb1 * apb;
+                        sdd = sdd - in[u].nb2 * amc;
+                        sdd = sdd - in[u].nb3 * apc;
+                    }
+                    dd = sdd;
+                    T am3[3], ap3[3];   // diagonal as the reference sums it: (acx + acy) + acz
+                    am3[X::a] = ama; ap3[X::a] = apa; am3[X::b] = amb; ap3[X::b] = apb; am3[X::c] = amc;
+                    ap3[X::c] = apc;
+                    bb = (-(am3[0] + ap3[0]) + -(am3[1] + ap3[1])) + -(am3[2] + ap3[2]);
+                    aa = ama;
+                    cc = apa;
+                } else {
+                    dd = ((f & FB_GM) || fluid) ? in[u].vo : T(0);
+                }
+                if (i == 1 && A.dir_lo) dd = dd - A.ppp_lo * aa;
+                if (i == L && A.dir_hi) dd = dd - A.ppp_hi * cc;
+                if (i == 1) aa = T(0);   // tdma ignores a(n1) and c(n2)
+                if (i == L) cc = T(0);
+                const int si = sidx(gs, r);
+                sa[si] = aa; sb[si] = bb; sc[si] = cc; sd[si] = dd;
+            }
         }
     }
     __syncthreads();
@@ -275,7 +305,7 @@ __global__ void __launch_bounds__(256) k_line_wp(LineArgs<T> A)
             T gp = T(0), yp = T(0), up = T(0), wp = T(0);
 #pragma unroll
             for (int s2 = 0; s2 < S - 1; ++s2) {
-                const T inv = T(1) / (b[s2] - a[s2] * gp);
+                const T inv = wp_rcp(b[s2] - a[s2] * gp);
                 y[s2] = (dv[s2] - a[s2] * yp) * inv;
                 u[s2] = ((s2 == 0 ? -a[0] : T(0)) - a[s2] * up) * inv;
                 w[s2] = ((s2 == S - 2 ? -c[S - 2] : T(0)) - a[s2] * wp) * inv;
@@ -302,9 +332,10 @@ __global__ void __launch_bounds__(256) k_line_wp(LineArgs<T> A)
         T RC = cn * w0n;
         T RD = dv[S - 1] - an * yl - cn * y0n;
         if (lane == 31) { RB = bn + an * wl; RC = T(0); RD = dv[S - 1] - an * yl; }
+        T iRB = wp_rcp(RB);
 #pragma unroll
-        for (int h = 1; h < 32; h <<= 1) pcr_step(RA, RB, RC, RD, lane, h);
-        const T XR = RD / RB;
+        for (int h = 1; h < 32; h <<= 1) pcr_step(RA, RB, RC, RD, iRB, lane, h);
+        const T XR = RD * iRB;
         T XL = __shfl_up_sync(0xffffffffu, XR, 1);
         if (lane == 0) XL = T(0);
         // ---- 3. solution into shared memory (reuse sd) ----
@@ -321,24 +352,18 @@ __global__ void __launch_bounds__(256) k_line_wp(LineArgs<T> A)
     __syncthreads();
 
     // ---- 4. store with relaxation ----
-    auto store = [&](int g, int r) {
-        int p, q;
-        if (!line_pq(g, p, q)) return;
-        const int i = r + 1;
-        const long long base = (long long)p * sb_ + (long long)q * sc_;
-        const long long o = base + (long long)i * sa_;
-        const T x = sd[sidx(g, r)];
-        A.v[o] = OMEGA1 ? x : A.v[o] * (T(1) - A.omega) + A.omega * x;
-        if (i == 1 && A.dir_lo) A.v[base] = A.ppp_lo;
-        if (i == L && A.dir_hi) A.v[base + (long long)(L + 1) * sa_] = A.ppp_hi;
-    };
-    if (DIR == 0) {
-        for (int r0 = 0; r0 < L; r0 += 32)
-            if (r0 + lane < L) store(warp, r0 + lane);
-    } else {
-        const int g = tid & (WP_LINES - 1), rr = tid >> 3;
-        for (int r0 = 0; r0 < L; r0 += 32)
-            if (r0 + rr < L) store(g, r0 + rr);
+    if (oks) {
+#pragma unroll 4
+        for (int r0 = 0; r0 < L; r0 += 32) {
+            const int r = r0 + rr;
+            if (r >= L) break;
+            const int i = r + 1;
+            const int o = base + i * sa_;
+            const T x = sd[sidx(gs, r)];
+            A.v[o] = OMEGA1 ? x : A.v[o] * (T(1) - A.omega) + A.omega * x;
+            if (i == 1 && A.dir_lo) A.v[base] = A.ppp_lo;
+            if (i == L && A.dir_hi) A.v[base + (L + 1) * sa_] = A.ppp_hi;
+        }
     }
 }
 
@@ -747,17 +772,20 @@ __global__ void __launch_bounds__(TPB) k_avg_partial(const double *p, const uint
                                                      const double *dy, const double *dz, Dims d,
                                                      double *partials)
 {
+    // rows (j, k) over blocks, i over threads
     const int n0 = d.m[0] - 1, n1 = d.m[1] - 1, n2 = d.m[2] - 1;
-    const long long total = (long long)n0 * n1 * n2;
+    const int rows = n1 * n2;
     double sp = 0.0, sv = 0.0;
-    for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < total;
-         t += (long long)gridDim.x * blockDim.x) {
-        const int i = 1 + (int)(t % n0), j = 1 + (int)((t / n0) % n1), k = 1 + (int)(t / ((long long)n0 * n1));
-        const long long o = d.idx(i, j, k);
-        if (fl[o] & FB_IB) continue;
-        const double vol = dx[i] * dy[j] * dz[k];
-        sp += p[o] * dx[i] * dy[j] * dz[k];
-        sv += vol;
+    for (int row = blockIdx.x; row < rows; row += gridDim.x) {
+        const int j = 1 + row % n1, k = 1 + row / n1;
+        const double dyz = dy[j] * dz[k];
+        const long long rb = d.idx(0, j, k);
+        for (int i = 1 + threadIdx.x; i <= n0; i += blockDim.x) {
+            if (fl[rb + i] & FB_IB) continue;
+            const double vol = dx[i] * dyz;
+            sp += p[rb + i] * vol;
+            sv += vol;
+        }
     }
     const double a = block_sum(sp);
     const double b = block_sum(sv);
@@ -778,14 +806,16 @@ __global__ void k_sum_final(double *partials, int n, int stride, double *out)
 
 __global__ void __launch_bounds__(TPB) k_avg_apply(double *p, const uint8_t *fl, Dims d, const double *sums)
 {
-    const int n0 = d.m[0] - 1, n1 = d.m[1] - 1, n2 = d.m[2] - 1;
-    const long long total = (long long)n0 * n1 * n2;
-    long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= total) return;
-    const int i = 1 + (int)(t % n0), j = 1 + (int)((t / n0) % n1), k = 1 + (int)(t / ((long long)n0 * n1));
-    const long long o = d.idx(i, j, k);
-    const double pAvg = sums[0] / sums[1];
-    p[o] = (fl[o] & FB_IB) ? 0.0 : p[o] - pAvg;
+    // one block per row (j, k); dead cells (iblank = 1) are zeroed (IBM/CORE_POISSON.F90:447-457)
+    __shared__ double s_avg;
+    if (threadIdx.x == 0) s_avg = sums[0] / sums[1];
+    __syncthreads();
+    const int n0 = d.m[0] - 1, n1 = d.m[1] - 1;
+    const int j = 1 + (int)blockIdx.x % n1, k = 1 + (int)blockIdx.x / n1;
+    const long long rb = d.idx(0, j, k);
+    const double pAvg = s_avg;
+    for (int i = 1 + threadIdx.x; i <= n0; i += blockDim.x)
+        p[rb + i] = (fl[rb + i] & FB_IB) ? 0.0 : p[rb + i] - pAvg;
 }
 
 // compatibility flux, non-periodic branch (IBM/GCM_GLOBAL_MASS_CONSERVE.F90:290-331)
@@ -1173,8 +1203,8 @@ void launch_subtract_average(double *p, const uint8_t *fl, const double *dx, con
     k_avg_partial<<<nblocks, TPB, 0, s>>>(p, fl, dx, dy, dz, d, partials);
     double *sums = partials + 2LL * nblocks;
     k_sum_final<<<1, 1024, 0, s>>>(partials, nblocks, 2, sums);
-    const long long n = (long long)(d.m[0] - 1) * (d.m[1] - 1) * (d.m[2] - 1);
-    k_avg_apply<<<nblk(n), TPB, 0, s>>>(p, fl, d, sums);
+    const int rows = (d.m[1] - 1) * (d.m[2] - 1);
+    k_avg_apply<<<rows, TPB, 0, s>>>(p, fl, d, sums);
 }
 
 static CompatArgs make_compat(const double *p, const uint8_t *fl, const double *pg, const double *dx,
