@@ -53,6 +53,7 @@ struct Level {
     double *v64 = nullptr, *r64 = nullptr;
     float *v32 = nullptr, *r32 = nullptr;
     int dlo[3] = {}, dhi[3] = {};   // finest-level Dirichlet ends per line direction
+    double *wpf[3] = {};            // factored partition tables of the FP64 smoother (or null)
 };
 
 // Transfer tables between level n and n+1 of one cycle direction.  Level 1 is
@@ -420,6 +421,7 @@ void itsolv(Ctx &c, Level &L, T *v, const T *r, bool finest, bool homogeneous)
     a.omega = (T)c.p.omega;
     const bool om1 = (c.p.omega == 1.0);
     for (int dir = 0; dir < c.nd; ++dir) {
+        a.wpf = std::is_same<T, double>::value ? L.wpf[dir] : nullptr;
         a.binv = lv_binv<T>(L, dir);
         a.gam = lv_gam<T>(L, dir);
         a.dir_lo = finest ? L.dlo[dir] : 0;
@@ -1148,17 +1150,26 @@ int fsi_mg_set_geometry(void *handle, const int8_t *iblank, const int8_t *ghostC
         for (int l = 1; l < c.nlev[d]; ++l) TRY(build_transfer(c, c.T[d][l], d, l));
     }
     // line factorisations of every level and direction
-    auto factor = [&](Level &L) {
+    // and the factored partition tables of the FP64 smoother: every level when
+    // the cycle runs in FP64, the coarsest levels (smoothed in FP64) otherwise
+    auto factor = [&](Level &L, bool fp64_level) -> int {
         for (int a = 0; a < c.nd; ++a) {
             FactorArgs<double> fa;
             fa.fl = L.fl; fa.c = coef_of<double>(L); fa.d = L.d;
             fa.binv64 = L.binv64[a]; fa.gam64 = L.gam64[a]; fa.binv32 = L.binv32[a]; fa.gam32 = L.gam32[a];
             launch_factor(a, fa, c.s);
+            const long long nt = fp64_level ? wpf_table_doubles(a, L.d) : 0;
+            if (nt > 0) {
+                if (!L.wpf[a]) TRY(c.alloc(&L.wpf[a], (size_t)nt));
+                launch_wpf_setup(a, fa, L.wpf[a], c.s);
+            }
         }
+        return 0;
     };
-    factor(c.L1);
+    const bool all64 = (c.p.precision_mode == 0);
+    TRY(factor(c.L1, all64));
     for (int d = 0; d < c.nd; ++d)
-        for (int l = 2; l <= c.nlev[d]; ++l) factor(c.C[d][l]);
+        for (int l = 2; l <= c.nlev[d]; ++l) TRY(factor(c.C[d][l], all64 || l == c.nlev[d]));
     // ghost gather list: linear indices in the level-1 layout; the ghost's own
     // stencil entry carries uNormal (0) and is marked -1.
     static const int incI[8] = {0, 0, 1, 1, 0, 0, 1, 1}, incJ[8] = {0, 1, 1, 0, 0, 1, 1, 0},
@@ -1481,6 +1492,7 @@ int fsi_mg_time_kernel(void *handle, int which, int precision, int reps, double 
                 LineArgs<T> a;
                 a.v = (T *)v; a.r = (const T *)r; a.fl = c.L1.fl; a.U = scratch_U<T>(c); a.c = coef_of<T>(c.L1);
                 a.d = c.L1.d; a.omega = (T)c.p.omega; a.binv = lv_binv<T>(c.L1, dir); a.gam = lv_gam<T>(c.L1, dir);
+                a.wpf = std::is_same<T, double>::value ? c.L1.wpf[dir] : nullptr;
                 a.dir_lo = a.dir_hi = 0; a.ppp_lo = a.ppp_hi = T(0); a.colour = 0;
                 launch_line<T>(dir, a, c.p.omega == 1.0, c.s);
             };

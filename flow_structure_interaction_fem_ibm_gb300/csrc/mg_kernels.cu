@@ -22,6 +22,17 @@ template <> struct Axes<0> { static constexpr int a = 0, b = 1, c = 2; static co
 template <> struct Axes<1> { static constexpr int a = 1, b = 0, c = 2; static constexpr bool c_first = false; };
 template <> struct Axes<2> { static constexpr int a = 2, b = 0, c = 1; static constexpr bool c_first = true; };
 
+// (i, j, k), 1-based, of interior cell t of an n0 x n1 x n2 box in column-major
+// order; 32-bit arithmetic (every level holds fewer than 2^31 cells)
+__device__ __forceinline__ void cell_of(unsigned t, unsigned n0, unsigned n1, int &i, int &j, int &k)
+{
+    const unsigned q = t / n0;
+    i = 1 + (int)(t - q * n0);
+    const unsigned kk = q / n1;
+    j = 1 + (int)(q - kk * n1);
+    k = 1 + (int)kk;
+}
+
 __device__ __forceinline__ long long stride_of(const Dims &d, int axis)
 {
     return axis == 0 ? 1LL : (axis == 1 ? d.sx : d.sxy);
@@ -368,6 +379,299 @@ __global__ void __launch_bounds__(256) k_line_wp(LineArgs<T> A)
 }
 
 // ---------------------------------------------------------------------------
+// Factored partition solver (FP64).  The tridiagonal matrix of every line is
+// fixed between geometry updates, so everything in the partition solve that
+// does not depend on the right-hand side is computed once per line by
+// k_wpf_setup: per row the segment pivots 1/(b - a g), the multipliers g and
+// the interface vectors u, w; per lane the PCR multipliers of each step, the
+// final 1/B and the coupling c of the lane's last row.  A sweep then only runs
+// the right-hand-side recurrences (about a dozen FP64 multiply-adds per row,
+// no divisions), which matters on a part whose FP64 rate is 1/64 of FP32.
+// Table of one line: INV, G, U, W as [s][lane] (32*S each), then the
+// WPF_LANE per-lane values as [j][lane]; lines in (p, q) order, both colours.
+// ---------------------------------------------------------------------------
+constexpr int WPF_LANE = 12;   // K1[5], K2[5], 1/B, c_last
+template <int S> __host__ __device__ constexpr int wpf_rec() { return 4 * 32 * S + WPF_LANE * 32; }
+
+template <int DIR, int S>
+__global__ void __launch_bounds__(256) k_wpf_setup(FactorArgs<double> A, double *tab)
+{
+    using X = Axes<DIR>;
+    const Dims &d = A.d;
+    const int nb = d.m[X::b] - 1, nc = d.m[X::c] - 1, L = d.m[X::a] - 1;
+    const int lane = threadIdx.x & 31;
+    const int lid = (int)blockIdx.x * 8 + (int)(threadIdx.x >> 5);
+    if (lid >= nb * nc) return;   // whole warps leave together
+    const int p = 1 + lid % nb, q = 1 + lid / nb;
+    const long long sa_ = stride_of(d, X::a), sb_ = stride_of(d, X::b), sc_ = stride_of(d, X::c);
+    const long long base = p * sb_ + q * sc_;
+    const double cmb = A.c.cm[X::b][p], cpb = A.c.cp[X::b][p];
+    const double cmc = A.c.cm[X::c][q], cpc = A.c.cp[X::c][q];
+    double a[S], b[S], c[S];
+#pragma unroll
+    for (int s2 = 0; s2 < S; ++s2) {
+        const int r = lane * S + s2, i = r + 1;
+        double aa = 0.0, bb = 1.0, cc = 0.0;
+        if (r < L) {
+            const uint8_t f = A.fl[base + i * sa_];
+            const bool fluid = !(f & FB_IB);
+            const double ama = (f & fb_minus(X::a)) ? 0.0 : A.c.cm[X::a][i];
+            const double apa = (f & fb_plus(X::a)) ? 0.0 : A.c.cp[X::a][i];
+            const double amb = (f & fb_minus(X::b)) ? 0.0 : cmb;
+            const double apb = (f & fb_plus(X::b)) ? 0.0 : cpb;
+            const double amc = (f & fb_minus(X::c)) ? 0.0 : cmc;
+            const double apc = (f & fb_plus(X::c)) ? 0.0 : cpc;
+            const bool allzero = (ama == 0.0) & (apa == 0.0) & (amb == 0.0) & (apb == 0.0) & (amc == 0.0) &
+                                 (apc == 0.0);
+            if (fluid && !allzero) {
+                double am3[3], ap3[3];
+                am3[X::a] = ama; ap3[X::a] = apa; am3[X::b] = amb; ap3[X::b] = apb; am3[X::c] = amc;
+                ap3[X::c] = apc;
+                bb = (-(am3[0] + ap3[0]) + -(am3[1] + ap3[1])) + -(am3[2] + ap3[2]);
+                aa = ama;
+                cc = apa;
+            }
+            if (i == 1) aa = 0.0;
+            if (i == L) cc = 0.0;
+        }
+        a[s2] = aa; b[s2] = bb; c[s2] = cc;
+    }
+    double inv[S], gg[S], u[S], w[S];
+#pragma unroll
+    for (int s2 = 0; s2 < S; ++s2) { inv[s2] = 0.0; gg[s2] = 0.0; u[s2] = 0.0; w[s2] = 0.0; }
+    {
+        double gp = 0.0, up = 0.0, wp = 0.0;
+#pragma unroll
+        for (int s2 = 0; s2 < S - 1; ++s2) {
+            inv[s2] = 1.0 / (b[s2] - a[s2] * gp);
+            u[s2] = ((s2 == 0 ? -a[0] : 0.0) - a[s2] * up) * inv[s2];
+            w[s2] = ((s2 == S - 2 ? -c[S - 2] : 0.0) - a[s2] * wp) * inv[s2];
+            gg[s2] = c[s2] * inv[s2];
+            gp = gg[s2]; up = u[s2]; wp = w[s2];
+        }
+#pragma unroll
+        for (int s2 = S - 3; s2 >= 0; --s2) {
+            u[s2] = u[s2] - gg[s2] * u[s2 + 1];
+            w[s2] = w[s2] - gg[s2] * w[s2 + 1];
+        }
+    }
+    const double u0 = (S >= 2) ? u[0] : 0.0, w0 = (S >= 2) ? w[0] : 1.0;
+    const double ul = (S >= 2) ? u[S - 2 < 0 ? 0 : S - 2] : 1.0;
+    const double wl = (S >= 2) ? w[S - 2 < 0 ? 0 : S - 2] : 0.0;
+    const double u0n = __shfl_down_sync(0xffffffffu, u0, 1);
+    const double w0n = __shfl_down_sync(0xffffffffu, w0, 1);
+    const double an = a[S - 1], bn = b[S - 1], cn = c[S - 1];
+    double RA = an * ul, RB = bn + an * wl + cn * u0n, RC = cn * w0n;
+    if (lane == 31) { RB = bn + an * wl; RC = 0.0; }
+    double iRB = 1.0 / RB;
+    double K1[5], K2[5];
+#pragma unroll
+    for (int k = 0; k < 5; ++k) {
+        const int h = 1 << k;
+        double Am = __shfl_up_sync(0xffffffffu, RA, h), iBm = __shfl_up_sync(0xffffffffu, iRB, h);
+        double Cm = __shfl_up_sync(0xffffffffu, RC, h);
+        double Ap = __shfl_down_sync(0xffffffffu, RA, h), iBp = __shfl_down_sync(0xffffffffu, iRB, h);
+        double Cp = __shfl_down_sync(0xffffffffu, RC, h);
+        if (lane < h) { Am = 0.0; iBm = 1.0; Cm = 0.0; }
+        if (lane + h > 31) { Ap = 0.0; iBp = 1.0; Cp = 0.0; }
+        const double k1 = RA * iBm, k2 = RC * iBp;
+        K1[k] = (lane < h) ? 0.0 : k1;
+        K2[k] = (lane + h > 31) ? 0.0 : k2;
+        const double nA = -k1 * Am, nC = -k2 * Cp, nB = RB - k1 * Cm - k2 * Ap;
+        RA = nA; RB = nB; RC = nC;
+        iRB = 1.0 / nB;
+    }
+    double *T = tab + (long long)lid * wpf_rec<S>();
+#pragma unroll
+    for (int s2 = 0; s2 < S; ++s2) {
+        T[0 * 32 * S + s2 * 32 + lane] = inv[s2];
+        T[1 * 32 * S + s2 * 32 + lane] = gg[s2];
+        T[2 * 32 * S + s2 * 32 + lane] = u[s2];
+        T[3 * 32 * S + s2 * 32 + lane] = w[s2];
+    }
+    double *Tl = T + 4 * 32 * S;
+#pragma unroll
+    for (int k = 0; k < 5; ++k) { Tl[k * 32 + lane] = K1[k]; Tl[(5 + k) * 32 + lane] = K2[k]; }
+    Tl[10 * 32 + lane] = iRB;
+    Tl[11 * 32 + lane] = (lane == 31) ? 0.0 : cn;
+}
+
+template <int DIR, int S, int NL, bool OMEGA1>
+__global__ void __launch_bounds__(32 * NL) k_line_fp(LineArgs<double> A)
+{
+    using X = Axes<DIR>;
+    extern __shared__ unsigned char smem_raw[];
+    double *sm = reinterpret_cast<double *>(smem_raw);
+    constexpr int RP = wp_pitch<S>();
+    double *sa = sm, *sd = sm + NL * RP;
+    const Dims &d = A.d;
+    const int nb = d.m[X::b] - 1, nc = d.m[X::c] - 1, L = d.m[X::a] - 1;
+    const int hb = (nb + 1) >> 1;
+    const int nlines = hb * nc;
+    const int sa_ = (int)stride_of(d, X::a), sb_ = (int)stride_of(d, X::b), sc_ = (int)stride_of(d, X::c);
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    auto line_pq = [&](int g, int &p, int &q) -> bool {
+        const int t = (int)blockIdx.x * NL + g;
+        if (t >= nlines) return false;
+        const int tq = t / hb;
+        q = 1 + tq;
+        const int p0 = (((1 + q) & 1) == A.colour) ? 1 : 2;
+        p = p0 + 2 * (t - tq * hb);
+        return p <= nb;
+    };
+    auto sidx = [&](int g, int r) { return g * RP + r + r / S; };
+    const int gs = (DIR == 0) ? warp : (tid % NL);
+    const int rr = (DIR == 0) ? lane : (tid / NL);
+    int ps = 1, qs = 1;
+    const bool oks = line_pq(gs, ps, qs);
+    const int base = ps * sb_ + qs * sc_;
+
+    // ---- 1. staging: sub-diagonal and right-hand side of each row ----
+    if (oks) {
+        const double cmb = A.c.cm[X::b][ps], cpb = A.c.cp[X::b][ps];
+        const double cmc = A.c.cm[X::c][qs], cpc = A.c.cp[X::c][qs];
+        struct RowIn { uint8_t f; double r, nb0, nb1, nb2, nb3, vo; };
+        constexpr int GRP = (S < 4) ? S : 4;
+#pragma unroll
+        for (int q0 = 0; q0 < S; q0 += GRP) {
+            RowIn in[GRP];
+#pragma unroll
+            for (int u = 0; u < GRP; ++u) {
+                const int r = (q0 + u) * 32 + rr;
+                if (r < L) {
+                    const int o = base + (r + 1) * sa_;
+                    in[u].f = A.fl[o];
+                    in[u].r = A.r[o];
+                    in[u].vo = A.v[o];
+                    if (X::c_first) {
+                        in[u].nb0 = A.v[o - sc_]; in[u].nb1 = A.v[o + sc_];
+                        in[u].nb2 = A.v[o - sb_]; in[u].nb3 = A.v[o + sb_];
+                    } else {
+                        in[u].nb0 = A.v[o - sb_]; in[u].nb1 = A.v[o + sb_];
+                        in[u].nb2 = A.v[o - sc_]; in[u].nb3 = A.v[o + sc_];
+                    }
+                }
+            }
+#pragma unroll
+            for (int u = 0; u < GRP; ++u) {
+                const int r = (q0 + u) * 32 + rr;
+                if (r >= L) continue;
+                const int i = r + 1;
+                const uint8_t f = in[u].f;
+                const bool fluid = !(f & FB_IB);
+                const double ama = (f & fb_minus(X::a)) ? 0.0 : A.c.cm[X::a][i];
+                const double apa = (f & fb_plus(X::a)) ? 0.0 : A.c.cp[X::a][i];
+                const double amb = (f & fb_minus(X::b)) ? 0.0 : cmb;
+                const double apb = (f & fb_plus(X::b)) ? 0.0 : cpb;
+                const double amc = (f & fb_minus(X::c)) ? 0.0 : cmc;
+                const double apc = (f & fb_plus(X::c)) ? 0.0 : cpc;
+                const bool allzero = (ama == 0.0) & (apa == 0.0) & (amb == 0.0) & (apb == 0.0) & (amc == 0.0) &
+                                     (apc == 0.0);
+                const bool normal = fluid && !allzero;
+                double aa = 0.0, cc = 0.0, dd;
+                if (normal) {
+                    double sdd = in[u].r;
+                    if (X::c_first) {
+                        sdd = sdd - in[u].nb0 * amc;
+                        sdd = sdd - in[u].nb1 * apc;
+                        sdd = sdd - in[u].nb2 * amb;
+                        sdd = sdd - in[u].nb3 * apb;
+                    } else {
+                        sdd = sdd - in[u].nb0 * amb;
+                        sdd = sdd - in[u].nb1 * apb;
+                        sdd = sdd - in[u].nb2 * amc;
+                        sdd = sdd - in[u].nb3 * apc;
+                    }
+                    dd = sdd;
+                    aa = ama;
+                    cc = apa;
+                } else {
+                    dd = ((f & FB_GM) || fluid) ? in[u].vo : 0.0;
+                }
+                if (i == 1 && A.dir_lo) dd = dd - A.ppp_lo * aa;
+                if (i == L && A.dir_hi) dd = dd - A.ppp_hi * cc;
+                if (i == 1) aa = 0.0;
+                const int si = sidx(gs, r);
+                sa[si] = aa; sd[si] = dd;
+            }
+        }
+    }
+    __syncthreads();
+
+    // ---- 2. right-hand-side recurrences with the line's factors ----
+    if (warp < NL) {
+        const int g = warp;
+        int p, q;
+        const bool valid = line_pq(g, p, q);
+        if (valid) {   // whole warp
+            const double *T = A.wpf + (long long)((p - 1) + nb * (q - 1)) * wpf_rec<S>();
+            double a[S], dv[S], y[S];
+#pragma unroll
+            for (int s2 = 0; s2 < S; ++s2) {
+                const int r = lane * S + s2;
+                if (r < L) { const int si = sidx(g, r); a[s2] = sa[si]; dv[s2] = sd[si]; }
+                else { a[s2] = 0.0; dv[s2] = 0.0; }
+                y[s2] = 0.0;
+            }
+            {
+                double yp = 0.0;
+#pragma unroll
+                for (int s2 = 0; s2 < S - 1; ++s2) {
+                    y[s2] = (dv[s2] - a[s2] * yp) * T[s2 * 32 + lane];
+                    yp = y[s2];
+                }
+#pragma unroll
+                for (int s2 = S - 3; s2 >= 0; --s2) y[s2] = y[s2] - T[32 * S + s2 * 32 + lane] * y[s2 + 1];
+            }
+            const double *Tl = T + 4 * 32 * S;
+            const double y0 = (S >= 2) ? y[0] : 0.0;
+            const double yl = (S >= 2) ? y[S - 2 < 0 ? 0 : S - 2] : 0.0;
+            const double y0n = __shfl_down_sync(0xffffffffu, y0, 1);
+            double D = dv[S - 1] - a[S - 1] * yl - Tl[11 * 32 + lane] * y0n;
+#pragma unroll
+            for (int k = 0; k < 5; ++k) {
+                const int h = 1 << k;
+                double Dm = __shfl_up_sync(0xffffffffu, D, h), Dp = __shfl_down_sync(0xffffffffu, D, h);
+                if (lane < h) Dm = 0.0;
+                if (lane + h > 31) Dp = 0.0;
+                D = D - Tl[k * 32 + lane] * Dm - Tl[(5 + k) * 32 + lane] * Dp;
+            }
+            const double XR = D * Tl[10 * 32 + lane];
+            double XL = __shfl_up_sync(0xffffffffu, XR, 1);
+            if (lane == 0) XL = 0.0;
+            __syncwarp();
+#pragma unroll
+            for (int s2 = 0; s2 < S; ++s2) {
+                const int r = lane * S + s2;
+                if (r < L) {
+                    const double x = (s2 < S - 1)
+                                         ? (y[s2] + XL * T[2 * 32 * S + s2 * 32 + lane] +
+                                            XR * T[3 * 32 * S + s2 * 32 + lane])
+                                         : XR;
+                    sd[sidx(g, r)] = x;
+                }
+            }
+        }
+    }
+    __syncthreads();
+
+    // ---- 3. store with relaxation ----
+    if (oks) {
+#pragma unroll 4
+        for (int r0 = 0; r0 < L; r0 += 32) {
+            const int r = r0 + rr;
+            if (r >= L) break;
+            const int i = r + 1;
+            const int o = base + i * sa_;
+            const double x = sd[sidx(gs, r)];
+            A.v[o] = OMEGA1 ? x : A.v[o] * (1.0 - A.omega) + A.omega * x;
+            if (i == 1 && A.dir_lo) A.v[base] = A.ppp_lo;
+            if (i == L && A.dir_hi) A.v[base + (L + 1) * sa_] = A.ppp_hi;
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
 // Line factorisation (setup).  Coefficients exactly as MG_itsolv builds them
 // (IBM/CORE_MG.F90:1950-1983) and the Thomas recurrences of tdma
 // (IBM/CORE_TDMA.F90:24-28) without contraction, so the factors match a
@@ -455,9 +759,7 @@ __global__ void __launch_bounds__(TPB) k_resid_restrict(RestrictArgs<T> A)
     long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= (long long)n0 * n1 * n2) return;
     int ci[3];
-    ci[0] = 1 + (int)(t % n0);
-    ci[1] = 1 + (int)((t / n0) % n1);
-    ci[2] = 1 + (int)(t / ((long long)n0 * n1));
+    cell_of((unsigned)t, (unsigned)n0, (unsigned)n1, ci[0], ci[1], ci[2]);
     int f1[3] = {ci[0], ci[1], ci[2]}, f2[3] = {ci[0], ci[1], ci[2]};
     f1[D] = 2 * ci[D] - 1;
     f2[D] = 2 * ci[D];
@@ -484,9 +786,7 @@ __global__ void __launch_bounds__(TPB) k_prolong_correct(ProlongArgs<T> A)
     long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= (long long)n0 * n1 * n2) return;
     int fi[3];
-    fi[0] = 1 + (int)(t % n0);
-    fi[1] = 1 + (int)((t / n0) % n1);
-    fi[2] = 1 + (int)(t / ((long long)n0 * n1));
+    cell_of((unsigned)t, (unsigned)n0, (unsigned)n1, fi[0], fi[1], fi[2]);
     const long long o = df.idx(fi[0], fi[1], fi[2]);
     if (A.flf[o] & FB_IB) return;
     const int q = fi[D];
@@ -699,7 +999,8 @@ __global__ void __launch_bounds__(TPB) k_calc_residual(const double *p, const do
     long long bi = 0x7fffffffffffffffLL;
     for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < total;
          t += (long long)gridDim.x * blockDim.x) {
-        const int i = 1 + (int)(t % n0), j = 1 + (int)((t / n0) % n1), k = 1 + (int)(t / ((long long)n0 * n1));
+        int i, j, k;
+        cell_of((unsigned)t, (unsigned)n0, (unsigned)n1, i, j, k);
         const long long o = d.idx(i, j, k);
         double res = cell_residual(p, b, fl, c, d, i, j, k);
         if (nlw0 && !(fl[o] & FB_IB)) res = res + nlw0[o];
@@ -844,7 +1145,8 @@ __global__ void __launch_bounds__(TPB) k_compat_partial(CompatArgs A, double *pa
     double acc = 0.0;
     for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < total;
          t += (long long)gridDim.x * blockDim.x) {
-        const int i = 1 + (int)(t % n0), j = 1 + (int)((t / n0) % n1), k = 1 + (int)(t / ((long long)n0 * n1));
+        int i, j, k;
+        cell_of((unsigned)t, (unsigned)n0, (unsigned)n1, i, j, k);
         const long long o = d.idx(i, j, k);
         const uint8_t f = A.fl[o];
         if (f & FB_IB) continue;
@@ -894,7 +1196,8 @@ __global__ void __launch_bounds__(TPB) k_nlw0(double *nlw0, CompatArgs A, const 
     const long long total = (long long)n0 * n1 * n2;
     long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= total) return;
-    const int i = 1 + (int)(t % n0), j = 1 + (int)((t / n0) % n1), k = 1 + (int)(t / ((long long)n0 * n1));
+    int i, j, k;
+        cell_of((unsigned)t, (unsigned)n0, (unsigned)n1, i, j, k);
     const long long o = d.idx(i, j, k);
     const uint8_t f = A.fl[o];
     const int ium = face_flag(f, 0, 0, A.sf[0], i == 1), iup = face_flag(f, 0, 1, A.sf[1], i == n0);
@@ -922,7 +1225,8 @@ __global__ void __launch_bounds__(TPB) k_apply_op(const double *z, double *w, co
     const long long total = (long long)n0 * n1 * n2;
     long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= total) return;
-    const int i = 1 + (int)(t % n0), j = 1 + (int)((t / n0) % n1), k = 1 + (int)(t / ((long long)n0 * n1));
+    int i, j, k;
+        cell_of((unsigned)t, (unsigned)n0, (unsigned)n1, i, j, k);
     const long long o = d.idx(i, j, k);
     const uint8_t f = fl[o];
     if (f & FB_IB) { w[o] = 0.0; return; }
@@ -947,7 +1251,8 @@ __global__ void __launch_bounds__(TPB) k_mdot(VecSet V, const double *w, const u
     double acc[8] = {0, 0, 0, 0, 0, 0, 0, 0};
     for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < total;
          t += (long long)gridDim.x * blockDim.x) {
-        const int i = 1 + (int)(t % n0), j = 1 + (int)((t / n0) % n1), k = 1 + (int)(t / ((long long)n0 * n1));
+        int i, j, k;
+        cell_of((unsigned)t, (unsigned)n0, (unsigned)n1, i, j, k);
         const long long o = d.idx(i, j, k);
         if (fl[o] & FB_IB) continue;
         const double wo = w[o];
@@ -1038,7 +1343,8 @@ __global__ void k_coarse_flags(uint8_t *fl, Dims d, int sb0, int sb1, int sb2, i
     const int n0 = d.m[0] - 1, n1 = d.m[1] - 1, n2 = d.m[2] - 1;
     long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= (long long)n0 * n1 * n2) return;
-    const int i = 1 + (int)(t % n0), j = 1 + (int)((t / n0) % n1), k = 1 + (int)(t / ((long long)n0 * n1));
+    int i, j, k;
+        cell_of((unsigned)t, (unsigned)n0, (unsigned)n1, i, j, k);
     const long long o = d.idx(i, j, k);
     uint8_t f = fl[o] & FB_IB;
     const int me = f ? 1 : 0;
@@ -1098,6 +1404,87 @@ bool launch_wp_dir(const LineArgs<T> &a, int L, long long nlines, cudaStream_t s
     return true;
 }
 
+template <int DIR, int S>
+cudaError_t fp_attr()
+{
+    const int b8 = (int)(2 * 8 * wp_pitch<S>() * sizeof(double)), b2 = (int)(2 * 2 * wp_pitch<S>() * sizeof(double));
+    cudaError_t e;
+    if ((e = cudaFuncSetAttribute(k_line_fp<DIR, S, 8, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, b8)))
+        return e;
+    if ((e = cudaFuncSetAttribute(k_line_fp<DIR, S, 8, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, b8)))
+        return e;
+    if ((e = cudaFuncSetAttribute(k_line_fp<DIR, S, 2, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, b2)))
+        return e;
+    return cudaFuncSetAttribute(k_line_fp<DIR, S, 2, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, b2);
+}
+
+template <int DIR>
+cudaError_t fp_attr_dir()
+{
+    cudaError_t e;
+    if ((e = fp_attr<DIR, 1>()) != cudaSuccess) return e;
+    if ((e = fp_attr<DIR, 2>()) != cudaSuccess) return e;
+    if ((e = fp_attr<DIR, 4>()) != cudaSuccess) return e;
+    if ((e = fp_attr<DIR, 8>()) != cudaSuccess) return e;
+    return fp_attr<DIR, 16>();
+}
+
+// Lines of a launch per CTA: 8 when the launch has at least 2048 lines (256
+// CTAs), else 2 so that a small level spreads over more SMs.
+template <int DIR, int S, bool O1>
+void launch_fp_one(const LineArgs<double> &a, long long nlines, cudaStream_t s)
+{
+    if (nlines >= 2048) {
+        const long long blocks = (nlines + 7) / 8;
+        k_line_fp<DIR, S, 8, O1><<<(unsigned)blocks, 256, 2 * 8 * wp_pitch<S>() * sizeof(double), s>>>(a);
+    } else {
+        const long long blocks = (nlines + 1) / 2;
+        k_line_fp<DIR, S, 2, O1><<<(unsigned)blocks, 64, 2 * 2 * wp_pitch<S>() * sizeof(double), s>>>(a);
+    }
+}
+
+template <int DIR, bool O1>
+bool launch_fp_dir(const LineArgs<double> &a, int L, long long nlines, cudaStream_t s)
+{
+    if (L <= 32) launch_fp_one<DIR, 1, O1>(a, nlines, s);
+    else if (L <= 64) launch_fp_one<DIR, 2, O1>(a, nlines, s);
+    else if (L <= 128) launch_fp_one<DIR, 4, O1>(a, nlines, s);
+    else if (L <= 256) launch_fp_one<DIR, 8, O1>(a, nlines, s);
+    else if (L <= 512) launch_fp_one<DIR, 16, O1>(a, nlines, s);
+    else return false;
+    return true;
+}
+
+template <typename T>
+bool launch_factored(int, const LineArgs<T> &, int, long long, bool, cudaStream_t) { return false; }
+template <>
+bool launch_factored<double>(int dir, const LineArgs<double> &a, int L, long long n, bool om1, cudaStream_t s)
+{
+    if (!a.wpf) return false;
+    if (om1) return (dir == 0) ? launch_fp_dir<0, true>(a, L, n, s)
+                  : (dir == 1) ? launch_fp_dir<1, true>(a, L, n, s) : launch_fp_dir<2, true>(a, L, n, s);
+    return (dir == 0) ? launch_fp_dir<0, false>(a, L, n, s)
+         : (dir == 1) ? launch_fp_dir<1, false>(a, L, n, s) : launch_fp_dir<2, false>(a, L, n, s);
+}
+
+template <int DIR, int S>
+void wpf_setup_one(const FactorArgs<double> &a, double *tab, long long nl, cudaStream_t s)
+{
+    k_wpf_setup<DIR, S><<<(unsigned)((nl + 7) / 8), 256, 0, s>>>(a, tab);
+}
+
+template <int DIR>
+void wpf_setup_dir(const FactorArgs<double> &a, double *tab, int L, long long nl, cudaStream_t s)
+{
+    if (L <= 32) wpf_setup_one<DIR, 1>(a, tab, nl, s);
+    else if (L <= 64) wpf_setup_one<DIR, 2>(a, tab, nl, s);
+    else if (L <= 128) wpf_setup_one<DIR, 4>(a, tab, nl, s);
+    else if (L <= 256) wpf_setup_one<DIR, 8>(a, tab, nl, s);
+    else wpf_setup_one<DIR, 16>(a, tab, nl, s);
+}
+
+int wp_S(int L) { return L <= 32 ? 1 : L <= 64 ? 2 : L <= 128 ? 4 : L <= 256 ? 8 : 16; }
+
 bool g_line_thread_per_line = false;   // selects the sequential-Thomas kernel (kept for lines > 512 cells)
 
 template <typename T>
@@ -1107,6 +1494,7 @@ void launch_line(int dir, const LineArgs<T> &a, bool omega_one, cudaStream_t s)
     const int nb = a.d.m[ob[dir]] - 1, nc = a.d.m[oc[dir]] - 1;
     const long long n = (long long)((nb + 1) / 2) * nc;
     const int L = a.d.m[dir] - 1;
+    if (!g_line_thread_per_line && L > 16 && L <= 512 && launch_factored<T>(dir, a, L, n, omega_one, s)) return;
     if (!g_line_thread_per_line && L > 16 && L <= 512) {   // short lines: one thread per line is cheaper
         bool ok;
         if (omega_one) {
@@ -1126,6 +1514,26 @@ void launch_line(int dir, const LineArgs<T> &a, bool omega_one, cudaStream_t s)
         if (dir == 0) L_(0, false); else if (dir == 1) L_(1, false); else L_(2, false);
     }
 #undef L_
+}
+
+long long wpf_table_doubles(int dir, const Dims &d)
+{
+    static const int ob[3] = {1, 0, 0}, oc[3] = {2, 2, 1};
+    const int L = d.m[dir] - 1;
+    if (L <= 16 || L > 512) return 0;
+    const long long nl = (long long)(d.m[ob[dir]] - 1) * (d.m[oc[dir]] - 1);
+    const int S = wp_S(L);
+    return nl * (4LL * 32 * S + WPF_LANE * 32);
+}
+
+void launch_wpf_setup(int dir, const FactorArgs<double> &a, double *tab, cudaStream_t s)
+{
+    static const int ob[3] = {1, 0, 0}, oc[3] = {2, 2, 1};
+    const int L = a.d.m[dir] - 1;
+    const long long nl = (long long)(a.d.m[ob[dir]] - 1) * (a.d.m[oc[dir]] - 1);
+    if (dir == 0) wpf_setup_dir<0>(a, tab, L, nl, s);
+    else if (dir == 1) wpf_setup_dir<1>(a, tab, L, nl, s);
+    else wpf_setup_dir<2>(a, tab, L, nl, s);
 }
 
 void launch_factor(int dir, const FactorArgs<double> &a, cudaStream_t s)
@@ -1322,7 +1730,10 @@ cudaError_t init_kernels()
     if ((e = wp_attr_dir<float, 2>()) != cudaSuccess) return e;
     if ((e = wp_attr_dir<double, 0>()) != cudaSuccess) return e;
     if ((e = wp_attr_dir<double, 1>()) != cudaSuccess) return e;
-    return wp_attr_dir<double, 2>();
+    if ((e = wp_attr_dir<double, 2>()) != cudaSuccess) return e;
+    if ((e = fp_attr_dir<0>()) != cudaSuccess) return e;
+    if ((e = fp_attr_dir<1>()) != cudaSuccess) return e;
+    return fp_attr_dir<2>();
 }
 
 void set_line_kernel(int thread_per_line) { g_line_thread_per_line = thread_per_line != 0; }

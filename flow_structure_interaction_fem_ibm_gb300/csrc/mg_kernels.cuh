@@ -43,6 +43,7 @@ struct LineArgs {
     T omega;
     int dir_lo, dir_hi;   // finest-level Dirichlet ends along the line direction
     T ppp_lo, ppp_hi;
+    const double *wpf = nullptr;   // factored partition table of this level and direction (FP64), or null
 };
 
 template <typename T>
@@ -91,6 +92,11 @@ void set_line_kernel(int thread_per_line);
 template <typename T>
 void launch_line(int dir, const LineArgs<T> &a, bool omega_one, cudaStream_t s);
 void launch_factor(int dir, const FactorArgs<double> &a, cudaStream_t s);
+// Factored partition tables (FP64 smoother): doubles needed for direction dir of
+// a level (0 when its lines are not in the partition solver's range), and the
+// setup kernel that fills them from the level's flags and coefficients.
+long long wpf_table_doubles(int dir, const Dims &d);
+void launch_wpf_setup(int dir, const FactorArgs<double> &a, double *tab, cudaStream_t s);
 template <typename T>
 void launch_resid_restrict(int D, const RestrictArgs<T> &a, cudaStream_t s);
 template <typename T>
