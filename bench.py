@@ -55,6 +55,8 @@ def parse():
     ap.add_argument("--krylov", type=int, default=30, help="FGMRES restart length around MG_Solver (0: stationary)")
     ap.add_argument("--profile", action="store_true",
                     help="profiling driver: raw RHS, two outer iterations of each precision, no other work")
+    ap.add_argument("--profile-krylov", action="store_true",
+                    help="profiling driver: raw RHS, one mixed FGMRES solve capped at 6 MG applications")
     return ap.parse_args()
 
 
@@ -273,6 +275,18 @@ def main():
     if world > 1:
         torch.distributed.barrier()
     from flow_structure_interaction_fem_ibm_gb300.poisson import PoissonSolver
+
+    if args.profile_krylov:
+        from flow_structure_interaction_fem_ibm_gb300 import problem as P
+        pr = P.sphere(args.n, seed=args.seed, stretch=1.5)
+        pp = copy.deepcopy(pr.params)
+        pp.precision_mode, pp.outer_krylov, pp.iterMax_Poisson, pp.restol_Poisson = 1, args.krylov, 6, 0.0
+        s = PoissonSolver(pp, pr.x, pr.y, pr.z).set_boundary(pr.geom)
+        p = np.zeros(pr.shape, order="F")
+        s.solve_poisson(p, pr.nlu0)
+        print(json.dumps({"profile": "krylov", "stats": s.stats()}))
+        s.close()
+        return
 
     if args.profile:
         from flow_structure_interaction_fem_ibm_gb300 import problem as P

@@ -130,7 +130,9 @@ struct Ctx {
     // FGMRES state (outer_krylov > 0)
     int km = 0;
     std::vector<double *> KV, KZ;          // Arnoldi basis (m+1) and preconditioned directions (m), FP64
+    std::vector<float *> KV32, KZ32;       // the same in FP32 (mixed precision)
     double *kw = nullptr, *kzp = nullptr, *kzr = nullptr;
+    float *kw32 = nullptr;
     double *kpart = nullptr, *kdots = nullptr, *h_kdots = nullptr;
     cudaGraphExec_t pgraph = nullptr;      // MG preconditioner on fixed buffers
     long long pgraph_kernels = 0;
@@ -662,44 +664,46 @@ int loc_of(const Ctx &c, long long idx, int *loc)
 int ensure_krylov(Ctx &c, int m)
 {
     if (c.km >= m) return 0;
+    if (m > 60) return fail(-1, "outer_krylov must be <= 60");
     const long long n1 = c.L1.d.count();
-    while ((int)c.KV.size() < m + 1) { double *q; TRY(c.alloc(&q, n1)); c.KV.push_back(q); }
-    while ((int)c.KZ.size() < m) { double *q; TRY(c.alloc(&q, n1)); c.KZ.push_back(q); }
+    if (c.p.precision_mode == 1) {
+        while ((int)c.KV32.size() < m + 1) { float *q; TRY(c.alloc(&q, n1)); c.KV32.push_back(q); }
+        while ((int)c.KZ32.size() < m) { float *q; TRY(c.alloc(&q, n1)); c.KZ32.push_back(q); }
+        if (!c.kw32) TRY(c.alloc(&c.kw32, n1));
+    } else {
+        while ((int)c.KV.size() < m + 1) { double *q; TRY(c.alloc(&q, n1)); c.KV.push_back(q); }
+        while ((int)c.KZ.size() < m) { double *q; TRY(c.alloc(&q, n1)); c.KZ.push_back(q); }
+        if (!c.kzp) { TRY(c.alloc(&c.kzp, n1)); TRY(c.alloc(&c.kzr, n1)); }
+    }
     if (!c.kw) {
         TRY(c.alloc(&c.kw, n1));
-        TRY(c.alloc(&c.kzp, n1));
-        TRY(c.alloc(&c.kzr, n1));
         TRY(c.alloc(&c.kpart, 8 * (size_t)c.nred + 8));
         TRY(c.alloc(&c.kdots, 256));
         CK(cudaMallocHost(&c.h_kdots, 256 * sizeof(double)));
     }
-    if (m > 60) return fail(-1, "outer_krylov must be <= 60");
     c.km = m;
     return 0;
 }
 
 // z = M^-1 v: one MG_Solver schedule on the correction (zero initial guess,
-// homogeneous boundary values), FP32 in mixed mode, FP64 otherwise; run as a
-// CUDA graph on fixed buffers (mixed: r32 -> e32, plain: kzr -> kzp).
-int precondition(Ctx &c, const double *v, double *z)
+// homogeneous boundary values) run as a CUDA graph on fixed buffers: FP32
+// (r32 -> e32) in mixed mode, FP64 (kzr -> kzp) otherwise.  v and z are
+// Krylov vectors of the same precision.
+template <typename T>
+int precondition(Ctx &c, const T *v, T *z)
 {
     const long long n1 = c.L1.d.count();
-    const bool mixed = (c.p.precision_mode == 1);
-    if (mixed) launch_convert_d2f(c.r32, v, n1, c.s);
-    else CK(cudaMemcpyAsync(c.kzr, v, n1 * 8, cudaMemcpyDeviceToDevice, c.s));
-    c.launches++;
+    constexpr bool f32 = std::is_same<T, float>::value;
+    T *in = f32 ? (T *)c.r32 : (T *)c.kzr;
+    T *out = f32 ? (T *)c.e32 : (T *)c.kzp;
+    CK(cudaMemcpyAsync(in, v, n1 * sizeof(T), cudaMemcpyDeviceToDevice, c.s));
     if (!c.pgraph) {
         cudaGraph_t g;
         const long long before = c.launches;
         c.lt_next = c.pgraph_lt0 = (int)c.lt_ev.size() / 4;   // second half of the pairs
         CK(cudaStreamBeginCapture(c.s, cudaStreamCaptureModeThreadLocal));
-        if (mixed) {
-            launch_fill<float>(c.e32, n1, 0.0f, c.s);
-            mg_solver<float>(c, c.e32, c.r32, true);
-        } else {
-            launch_fill<double>(c.kzp, n1, 0.0, c.s);
-            mg_solver<double>(c, c.kzp, c.kzr, true);
-        }
+        launch_fill<T>(out, n1, T(0), c.s);
+        mg_solver<T>(c, out, in, true);
         c.launches++;
         CK(cudaStreamEndCapture(c.s, &g));
         c.pgraph_lt1 = c.lt_next;
@@ -711,20 +715,35 @@ int precondition(Ctx &c, const double *v, double *z)
     }
     CK(cudaGraphLaunch(c.pgraph, c.s));
     c.launches += c.pgraph_kernels;
-    if (mixed) launch_convert_f2d(z, c.e32, n1, c.s);
-    else CK(cudaMemcpyAsync(z, c.kzp, n1 * 8, cudaMemcpyDeviceToDevice, c.s));
-    c.launches++;
+    CK(cudaMemcpyAsync(z, out, n1 * sizeof(T), cudaMemcpyDeviceToDevice, c.s));
     return 0;
 }
 
+// Relative reduction one FP32 inner cycle aims for at most; the FP64 residual
+// recomputed at the restart carries the refinement further.
+constexpr double KRYLOV_FP32_INNER_RTOL = 1.0e-5;
+
 // solve_poisson with FGMRES(m) around MG_Solver (outer_krylov = m).  Same
 // discrete system (fluid rows with ghost values from the ghost-row fixed
-// point), same stopping test (max-norm of the calc_residual residual).
-// Iterations count preconditioner applications (one MG_Solver each).
-int solve_krylov(Ctx &c, double *p, const double *b, int *iters, double *maxres_out, int *loc, double *compTime)
+// point), same stopping test (max-norm of the calc_residual residual, FP64).
+// Iterations count preconditioner applications (one MG_Solver each).  T is
+// the precision of the Krylov vectors, the preconditioner and the operator
+// inside a cycle: FP64 in the plain form; FP32 in the mixed form, where each
+// restart recomputes the residual in FP64 and adds the cycle's correction to
+// p in FP64 (iterative refinement with an FP32 FGMRES inner solver).
+template <typename T>
+int solve_krylov_t(Ctx &c, double *p, const double *b, int *iters, double *maxres_out, int *loc, double *compTime)
 {
+    constexpr bool f32 = std::is_same<T, float>::value;
     const int m = c.p.outer_krylov;
     TRY(ensure_krylov(c, m));
+    std::vector<T *> &KV = [&]() -> std::vector<T *> & {
+        if constexpr (f32) return c.KV32; else return c.KV;
+    }();
+    std::vector<T *> &KZ = [&]() -> std::vector<T *> & {
+        if constexpr (f32) return c.KZ32; else return c.KZ;
+    }();
+    T *w = f32 ? (T *)c.kw32 : (T *)c.kw;
     const long long n1 = c.L1.d.count();
     const bool gcm = (c.p.boundary_formulation == GCM_METHOD);
     auto t0 = std::chrono::steady_clock::now();
@@ -744,10 +763,14 @@ int solve_krylov(Ctx &c, double *p, const double *b, int *iters, double *maxres_
     std::vector<double> H((size_t)(m + 1) * m, 0.0), cs(m, 0.0), sn(m, 0.0), g(m + 1, 0.0), y(m, 0.0);
     auto Hij = [&](int i, int j) -> double & { return H[(size_t)i + (size_t)(m + 1) * j]; };
     const Coef<double> coef = coef_of<double>(c.L1);
+    const Coef<T> coefT = coef_of<T>(c.L1);
+    const T *gco = f32 ? (const T *)c.gco32 : (const T *)c.gco64;
+    T *gscr = f32 ? (T *)c.gscr32 : (T *)c.gscr64;
     while (true) {
         if (gcm) correct_pressure(c, p, c.nlw0);
+        // FP64 residual r = b - A p (into kw), its max-norm and 2-norm
         launch_calc_residual(p, b, c.nlw0_nonzero ? c.nlw0 : nullptr, c.L1.fl, coef, c.L1.d, nullptr, c.partials,
-                             c.nred, c.result, c.s, c.KV[0]);
+                             c.nred, c.result, c.s, c.kw);
         c.launches += 2;
         CK(cudaMemcpyAsync(c.h_result, c.result, sizeof(MaxLoc), cudaMemcpyDeviceToHost, c.s));
         CK(cudaStreamSynchronize(c.s));
@@ -755,40 +778,41 @@ int solve_krylov(Ctx &c, double *p, const double *b, int *iters, double *maxres_
         maxidx = c.h_result->i;
         if (!c.hist.empty()) c.hist.back() = maxres;   // true value at the restart point
         if (!std::isfinite(maxres) || maxres <= c.p.restol_Poisson || it >= c.p.iterMax_Poisson) break;
-        // beta = ||r||_2 over fluid cells
-        const double *v0 = c.KV[0];
-        launch_mdot(&v0, 1, c.KV[0], c.L1.fl, c.L1.d, c.kpart, c.nred, c.kdots, c.s);
+        const double *r64 = c.kw;
+        launch_mdot<double>(&r64, 1, c.kw, c.L1.fl, c.L1.d, c.kpart, c.nred, c.kdots, c.s);
         CK(cudaMemcpyAsync(c.h_kdots, c.kdots, sizeof(double), cudaMemcpyDeviceToHost, c.s));
         CK(cudaStreamSynchronize(c.s));
         const double beta = std::sqrt(c.h_kdots[0]);
         if (!(beta > 0.0)) break;
-        launch_scale_copy(c.KV[0], c.KV[0], c.kdots, n1, c.s);
+        launch_scale_copy<T, double>(KV[0], c.kw, c.kdots, n1, c.s);
+        c.launches += 3;
         std::fill(g.begin(), g.end(), 0.0);
         g[0] = beta;
-        const double target = 0.5 * beta * c.p.restol_Poisson / maxres;
+        double target = 0.5 * beta * c.p.restol_Poisson / maxres;
+        if (f32) target = std::max(target, KRYLOV_FP32_INNER_RTOL * beta);
         int k = 0;
         for (int j = 0; j < m; ++j) {
-            TRY(precondition(c, c.KV[j], c.KZ[j]));
+            TRY(precondition<T>(c, KV[j], KZ[j]));
             if (gcm) {   // ghost values of z from its fluid values (the map whose matrix A acts on)
-                launch_outer_ghost<double>(c.KZ[j], c.L1.d, c.sign, c.s);
+                launch_outer_ghost<T>(KZ[j], c.L1.d, c.sign, c.s);
                 if (c.nGhost > 0) {
                     GhostArgs ga{c.nGhost, c.gidx, c.sidx};
-                    launch_ghost_rows<double>(c.KZ[j], ga, c.gco64, c.gscr64, c.p.iterMax_ad, c.p.restol_ad, 0.0,
-                                              c.d_iters, c.d_maxd, c.s);
+                    launch_ghost_rows<T>(KZ[j], ga, gco, gscr, c.p.iterMax_ad, c.p.restol_ad, f32 ? 1.0e-6 : 0.0,
+                                         c.d_iters, c.d_maxd, c.s);
                 }
                 c.launches += 2;
             }
-            launch_apply_op(c.KZ[j], c.kw, c.L1.fl, coef, c.L1.d, c.s);
+            launch_apply_op<T>(KZ[j], w, c.L1.fl, coefT, c.L1.d, c.s);
             c.launches++;
-            const double *const *Vp = c.KV.data();
+            const T *const *Vp = KV.data();
             // classical Gram-Schmidt, twice
-            launch_mdot(Vp, j + 1, c.kw, c.L1.fl, c.L1.d, c.kpart, c.nred, c.kdots, c.s);
-            launch_maxpy(c.kw, Vp, j + 1, c.kdots, -1.0, n1, c.s);
-            launch_mdot(Vp, j + 1, c.kw, c.L1.fl, c.L1.d, c.kpart, c.nred, c.kdots + 64, c.s);
-            launch_maxpy(c.kw, Vp, j + 1, c.kdots + 64, -1.0, n1, c.s);
-            const double *wp = c.kw;
-            launch_mdot(&wp, 1, c.kw, c.L1.fl, c.L1.d, c.kpart, c.nred, c.kdots + 128, c.s);
-            launch_scale_copy(c.KV[j + 1], c.kw, c.kdots + 128, n1, c.s);
+            launch_mdot<T>(Vp, j + 1, w, c.L1.fl, c.L1.d, c.kpart, c.nred, c.kdots, c.s);
+            launch_maxpy<T>(w, Vp, j + 1, c.kdots, -1.0, n1, c.s);
+            launch_mdot<T>(Vp, j + 1, w, c.L1.fl, c.L1.d, c.kpart, c.nred, c.kdots + 64, c.s);
+            launch_maxpy<T>(w, Vp, j + 1, c.kdots + 64, -1.0, n1, c.s);
+            const T *wp = w;
+            launch_mdot<T>(&wp, 1, w, c.L1.fl, c.L1.d, c.kpart, c.nred, c.kdots + 128, c.s);
+            launch_scale_copy<T, T>(KV[j + 1], w, c.kdots + 128, n1, c.s);
             c.launches += 4 * ((j + 8) / 8) * 2 + 3;
             CK(cudaMemcpyAsync(c.h_kdots, c.kdots, 256 * sizeof(double), cudaMemcpyDeviceToHost, c.s));
             CK(cudaStreamSynchronize(c.s));
@@ -822,8 +846,16 @@ int solve_krylov(Ctx &c, double *p, const double *b, int *iters, double *maxres_
             y[i] = sacc / Hij(i, i);
         }
         CK(cudaMemcpyAsync(c.kdots + 192, y.data(), k * sizeof(double), cudaMemcpyHostToDevice, c.s));
-        launch_maxpy(p, c.KZ.data(), k, c.kdots + 192, 1.0, n1, c.s);
-        c.launches += (k + 7) / 8;
+        if constexpr (f32) {
+            // correction summed in FP32, accumulated into p in FP64
+            launch_fill<float>(c.e32, n1, 0.0f, c.s);
+            launch_maxpy<float>(c.e32, KZ.data(), k, c.kdots + 192, 1.0, n1, c.s);
+            launch_accumulate(p, c.e32, n1, c.s);
+            c.launches += 2 + (k + 7) / 8;
+        } else {
+            launch_maxpy<double>(p, KZ.data(), k, c.kdots + 192, 1.0, n1, c.s);
+            c.launches += (k + 7) / 8;
+        }
     }
     CK(cudaEventRecord(c.ev1, c.s));
     int h_iters = 0;
@@ -845,6 +877,12 @@ int solve_krylov(Ctx &c, double *p, const double *b, int *iters, double *maxres_
     if (!std::isfinite(maxres)) return fail(-5, "residual is not finite (NaN or Inf in the inputs?)");
     if (maxres > c.p.restol_Poisson) return 1;
     return 0;
+}
+
+int solve_krylov(Ctx &c, double *p, const double *b, int *iters, double *maxres_out, int *loc, double *compTime)
+{
+    if (c.p.precision_mode == 1) return solve_krylov_t<float>(c, p, b, iters, maxres_out, loc, compTime);
+    return solve_krylov_t<double>(c, p, b, iters, maxres_out, loc, compTime);
 }
 
 // solve_poisson MG branch on device-resident full-layout arrays

@@ -33,6 +33,14 @@ __device__ __forceinline__ void cell_of(unsigned t, unsigned n0, unsigned n1, in
     k = 1 + (int)kk;
 }
 
+// x == 0 (either sign) from its bit pattern: integer instructions only, which
+// keeps the all-zero-row test off the FP64 pipe
+__device__ __forceinline__ bool is_zero(float x) { return (__float_as_uint(x) << 1) == 0u; }
+__device__ __forceinline__ bool is_zero(double x)
+{
+    return ((unsigned long long)__double_as_longlong(x) << 1) == 0ull;
+}
+
 __device__ __forceinline__ long long stride_of(const Dims &d, int axis)
 {
     return axis == 0 ? 1LL : (axis == 1 ? d.sx : d.sxy);
@@ -221,6 +229,7 @@ __global__ void __launch_bounds__(256) k_line_wp(LineArgs<T> A)
         // transverse coefficients are constant along the line
         const T cmb = A.c.cm[X::b][ps], cpb = A.c.cp[X::b][ps];
         const T cmc = A.c.cm[X::c][qs], cpc = A.c.cp[X::c][qs];
+        const bool zmb = is_zero(cmb), zpb = is_zero(cpb), zmc = is_zero(cmc), zpc = is_zero(cpc);
         struct RowIn { uint8_t f; T r, nb0, nb1, nb2, nb3, vo; };
         constexpr int GRP = (S < 4) ? S : 4;
 #pragma unroll
@@ -250,14 +259,16 @@ __global__ void __launch_bounds__(256) k_line_wp(LineArgs<T> A)
                 const int i = r + 1;
                 const uint8_t f = in[u].f;
                 const bool fluid = !(f & FB_IB);
-                const T ama = (f & fb_minus(X::a)) ? T(0) : A.c.cm[X::a][i];
-                const T apa = (f & fb_plus(X::a)) ? T(0) : A.c.cp[X::a][i];
+                const T cma_i = A.c.cm[X::a][i], cpa_i = A.c.cp[X::a][i];
+                const T ama = (f & fb_minus(X::a)) ? T(0) : cma_i;
+                const T apa = (f & fb_plus(X::a)) ? T(0) : cpa_i;
                 const T amb = (f & fb_minus(X::b)) ? T(0) : cmb;
                 const T apb = (f & fb_plus(X::b)) ? T(0) : cpb;
                 const T amc = (f & fb_minus(X::c)) ? T(0) : cmc;
                 const T apc = (f & fb_plus(X::c)) ? T(0) : cpc;
-                const bool allzero = (ama == T(0)) & (apa == T(0)) & (amb == T(0)) & (apb == T(0)) &
-                                     (amc == T(0)) & (apc == T(0));
+                const bool allzero = ((f & fb_minus(X::a)) || is_zero(cma_i)) && ((f & fb_plus(X::a)) || is_zero(cpa_i)) &&
+                                     ((f & fb_minus(X::b)) || zmb) && ((f & fb_plus(X::b)) || zpb) &&
+                                     ((f & fb_minus(X::c)) || zmc) && ((f & fb_plus(X::c)) || zpc);
                 const bool normal = fluid && !allzero;
                 T aa = T(0), bb = T(1), cc = T(0), dd;
                 if (normal) {
@@ -530,6 +541,7 @@ __global__ void __launch_bounds__(32 * NL) k_line_fp(LineArgs<double> A)
     if (oks) {
         const double cmb = A.c.cm[X::b][ps], cpb = A.c.cp[X::b][ps];
         const double cmc = A.c.cm[X::c][qs], cpc = A.c.cp[X::c][qs];
+        const bool zmb = is_zero(cmb), zpb = is_zero(cpb), zmc = is_zero(cmc), zpc = is_zero(cpc);
         struct RowIn { uint8_t f; double r, nb0, nb1, nb2, nb3, vo; };
         constexpr int GRP = (S < 4) ? S : 4;
 #pragma unroll
@@ -559,14 +571,16 @@ __global__ void __launch_bounds__(32 * NL) k_line_fp(LineArgs<double> A)
                 const int i = r + 1;
                 const uint8_t f = in[u].f;
                 const bool fluid = !(f & FB_IB);
-                const double ama = (f & fb_minus(X::a)) ? 0.0 : A.c.cm[X::a][i];
-                const double apa = (f & fb_plus(X::a)) ? 0.0 : A.c.cp[X::a][i];
+                const double cma_i = A.c.cm[X::a][i], cpa_i = A.c.cp[X::a][i];
+                const double ama = (f & fb_minus(X::a)) ? 0.0 : cma_i;
+                const double apa = (f & fb_plus(X::a)) ? 0.0 : cpa_i;
                 const double amb = (f & fb_minus(X::b)) ? 0.0 : cmb;
                 const double apb = (f & fb_plus(X::b)) ? 0.0 : cpb;
                 const double amc = (f & fb_minus(X::c)) ? 0.0 : cmc;
                 const double apc = (f & fb_plus(X::c)) ? 0.0 : cpc;
-                const bool allzero = (ama == 0.0) & (apa == 0.0) & (amb == 0.0) & (apb == 0.0) & (amc == 0.0) &
-                                     (apc == 0.0);
+                const bool allzero = ((f & fb_minus(X::a)) || is_zero(cma_i)) && ((f & fb_plus(X::a)) || is_zero(cpa_i)) &&
+                                     ((f & fb_minus(X::b)) || zmb) && ((f & fb_plus(X::b)) || zpb) &&
+                                     ((f & fb_minus(X::c)) || zmc) && ((f & fb_plus(X::c)) || zpc);
                 const bool normal = fluid && !allzero;
                 double aa = 0.0, cc = 0.0, dd;
                 if (normal) {
@@ -1217,8 +1231,8 @@ __global__ void __launch_bounds__(TPB) k_nlw0(double *nlw0, CompatArgs A, const 
 // Krylov support for the outer solve: operator application on fluid cells,
 // blocked dot products and combined axpys over the level-1 interior.
 // ---------------------------------------------------------------------------
-__global__ void __launch_bounds__(TPB) k_apply_op(const double *z, double *w, const uint8_t *fl, Coef<double> c,
-                                                  Dims d)
+template <typename T>
+__global__ void __launch_bounds__(TPB) k_apply_op(const T *z, T *w, const uint8_t *fl, Coef<T> c, Dims d)
 {
     // w = A z on fluid interior cells (the matrix whose residual calc_residual forms), 0 elsewhere
     const int n0 = d.m[0] - 1, n1 = d.m[1] - 1, n2 = d.m[2] - 1;
@@ -1226,42 +1240,45 @@ __global__ void __launch_bounds__(TPB) k_apply_op(const double *z, double *w, co
     long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= total) return;
     int i, j, k;
-        cell_of((unsigned)t, (unsigned)n0, (unsigned)n1, i, j, k);
+    cell_of((unsigned)t, (unsigned)n0, (unsigned)n1, i, j, k);
     const long long o = d.idx(i, j, k);
     const uint8_t f = fl[o];
-    if (f & FB_IB) { w[o] = 0.0; return; }
-    const double bmx = (f & fb_minus(0)) ? 0.0 : c.cm[0][i];
-    const double bpx = (f & fb_plus(0)) ? 0.0 : c.cp[0][i];
-    const double bmy = (f & fb_minus(1)) ? 0.0 : c.cm[1][j];
-    const double bpy = (f & fb_plus(1)) ? 0.0 : c.cp[1][j];
-    const double bmz = (f & fb_minus(2)) ? 0.0 : c.cm[2][k];
-    const double bpz = (f & fb_plus(2)) ? 0.0 : c.cp[2][k];
-    const double bc = (-(bmx + bpx) + -(bmy + bpy)) + -(bmz + bpz);
+    if (f & FB_IB) { w[o] = T(0); return; }
+    const T bmx = (f & fb_minus(0)) ? T(0) : c.cm[0][i];
+    const T bpx = (f & fb_plus(0)) ? T(0) : c.cp[0][i];
+    const T bmy = (f & fb_minus(1)) ? T(0) : c.cm[1][j];
+    const T bpy = (f & fb_plus(1)) ? T(0) : c.cp[1][j];
+    const T bmz = (f & fb_minus(2)) ? T(0) : c.cm[2][k];
+    const T bpz = (f & fb_plus(2)) ? T(0) : c.cp[2][k];
+    const T bc = (-(bmx + bpx) + -(bmy + bpy)) + -(bmz + bpz);
     w[o] = z[o] * bc + z[o - 1] * bmx + z[o + 1] * bpx + z[o - d.sx] * bmy + z[o + d.sx] * bpy +
            z[o - d.sxy] * bmz + z[o + d.sxy] * bpz;
 }
 
-struct VecSet { const double *v[8]; int n; };
+template <typename T>
+struct VecSet { const T *v[8]; int n; };
 
-// partials[blk * 8 + q] = sum over fluid interior cells of V_q * w
-__global__ void __launch_bounds__(TPB) k_mdot(VecSet V, const double *w, const uint8_t *fl, Dims d, double *partials)
+// partials[blk * 8 + q] = sum over fluid interior cells of V_q * w (per-thread sums
+// in T, block sums in FP64)
+template <typename T>
+__global__ void __launch_bounds__(TPB) k_mdot(VecSet<T> V, const T *w, const uint8_t *fl, Dims d, double *partials)
 {
     const int n0 = d.m[0] - 1, n1 = d.m[1] - 1, n2 = d.m[2] - 1;
     const long long total = (long long)n0 * n1 * n2;
-    double acc[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+    T acc[8] = {0, 0, 0, 0, 0, 0, 0, 0};
     for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < total;
          t += (long long)gridDim.x * blockDim.x) {
         int i, j, k;
         cell_of((unsigned)t, (unsigned)n0, (unsigned)n1, i, j, k);
         const long long o = d.idx(i, j, k);
         if (fl[o] & FB_IB) continue;
-        const double wo = w[o];
+        const T wo = w[o];
 #pragma unroll
         for (int q = 0; q < 8; ++q)
             if (q < V.n) acc[q] += V.v[q][o] * wo;
     }
     for (int q = 0; q < 8; ++q) {
-        const double s = block_sum(acc[q]);
+        const double s = block_sum((double)acc[q]);
         if (threadIdx.x == 0) partials[(long long)blockIdx.x * 8 + q] = s;
     }
 }
@@ -1278,24 +1295,32 @@ __global__ void k_mdot_final(const double *partials, int nb, int n, double *out)
     }
 }
 
-// w += sum_q coef[q] * sign * V_q  over all cells (coef on the device)
-__global__ void __launch_bounds__(TPB) k_maxpy(double *w, VecSet V, const double *coef, double sign, long long n)
+// w += sum_q sign * coef[q] * V_q  over all cells (coef on the device)
+template <typename T>
+__global__ void __launch_bounds__(TPB) k_maxpy(T *w, VecSet<T> V, const double *coef, double sign, long long n)
 {
     long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= n) return;
-    double acc = w[t];
+    T cf[8];
+#pragma unroll
+    for (int q = 0; q < 8; ++q) cf[q] = (q < V.n) ? (T)(sign * coef[q]) : T(0);
+    T acc = w[t];
 #pragma unroll
     for (int q = 0; q < 8; ++q)
-        if (q < V.n) acc += sign * coef[q] * V.v[q][t];
+        if (q < V.n) acc += cf[q] * V.v[q][t];
     w[t] = acc;
 }
 
-__global__ void k_scale_copy(double *dst, const double *src, const double *nrm2, long long n)
+template <typename T, typename S>
+__global__ void k_scale_copy(T *dst, const S *src, const double *nrm2, long long n)
 {
     // dst = src / sqrt(nrm2[0])
+    __shared__ double s_inv;
+    if (threadIdx.x == 0) s_inv = 1.0 / sqrt(nrm2[0]);
+    __syncthreads();
     long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= n) return;
-    dst[t] = src[t] / sqrt(nrm2[0]);
+    dst[t] = (T)((double)src[t] * s_inv);
 }
 
 __global__ void k_accumulate(double *p, const float *e, long long n)
@@ -1660,40 +1685,58 @@ void launch_nlw0(double *nlw0, const uint8_t *fl, const int side_flag[6], const 
     k_nlw0<<<nblk(n), TPB, 0, s>>>(nlw0, A, dxinv, dyinv, dzinv);
 }
 
-void launch_apply_op(const double *z, double *w, const uint8_t *fl, const Coef<double> &c, const Dims &d,
-                     cudaStream_t s)
+template <typename T>
+void launch_apply_op(const T *z, T *w, const uint8_t *fl, const Coef<T> &c, const Dims &d, cudaStream_t s)
 {
     const long long n = (long long)(d.m[0] - 1) * (d.m[1] - 1) * (d.m[2] - 1);
-    k_apply_op<<<nblk(n), TPB, 0, s>>>(z, w, fl, c, d);
+    k_apply_op<T><<<nblk(n), TPB, 0, s>>>(z, w, fl, c, d);
 }
 
-void launch_mdot(const double *const *V, int nv, const double *w, const uint8_t *fl, const Dims &d,
-                 double *partials, int nblocks, double *out, cudaStream_t s)
+template <typename T>
+void launch_mdot(const T *const *V, int nv, const T *w, const uint8_t *fl, const Dims &d, double *partials,
+                 int nblocks, double *out, cudaStream_t s)
 {
     for (int q0 = 0; q0 < nv; q0 += 8) {
-        VecSet vs;
+        VecSet<T> vs;
         vs.n = (nv - q0 < 8) ? nv - q0 : 8;
         for (int q = 0; q < 8; ++q) vs.v[q] = (q < vs.n) ? V[q0 + q] : nullptr;
-        k_mdot<<<nblocks, TPB, 0, s>>>(vs, w, fl, d, partials);
+        k_mdot<T><<<nblocks, TPB, 0, s>>>(vs, w, fl, d, partials);
         k_mdot_final<<<1, 1024, 0, s>>>(partials, nblocks, vs.n, out + q0);
     }
 }
 
-void launch_maxpy(double *w, const double *const *V, int nv, const double *coef, double sign, long long n,
-                  cudaStream_t s)
+template <typename T>
+void launch_maxpy(T *w, const T *const *V, int nv, const double *coef, double sign, long long n, cudaStream_t s)
 {
     for (int q0 = 0; q0 < nv; q0 += 8) {
-        VecSet vs;
+        VecSet<T> vs;
         vs.n = (nv - q0 < 8) ? nv - q0 : 8;
         for (int q = 0; q < 8; ++q) vs.v[q] = (q < vs.n) ? V[q0 + q] : nullptr;
-        k_maxpy<<<nblk(n), TPB, 0, s>>>(w, vs, coef + q0, sign, n);
+        k_maxpy<T><<<nblk(n), TPB, 0, s>>>(w, vs, coef + q0, sign, n);
     }
 }
 
-void launch_scale_copy(double *dst, const double *src, const double *nrm2, long long n, cudaStream_t s)
+template <typename T, typename S>
+void launch_scale_copy(T *dst, const S *src, const double *nrm2, long long n, cudaStream_t s)
 {
-    k_scale_copy<<<nblk(n), TPB, 0, s>>>(dst, src, nrm2, n);
+    k_scale_copy<T, S><<<nblk(n), TPB, 0, s>>>(dst, src, nrm2, n);
 }
+
+template void launch_apply_op<double>(const double *, double *, const uint8_t *, const Coef<double> &, const Dims &,
+                                      cudaStream_t);
+template void launch_apply_op<float>(const float *, float *, const uint8_t *, const Coef<float> &, const Dims &,
+                                     cudaStream_t);
+template void launch_mdot<double>(const double *const *, int, const double *, const uint8_t *, const Dims &, double *,
+                                  int, double *, cudaStream_t);
+template void launch_mdot<float>(const float *const *, int, const float *, const uint8_t *, const Dims &, double *,
+                                 int, double *, cudaStream_t);
+template void launch_maxpy<double>(double *, const double *const *, int, const double *, double, long long,
+                                   cudaStream_t);
+template void launch_maxpy<float>(float *, const float *const *, int, const double *, double, long long,
+                                  cudaStream_t);
+template void launch_scale_copy<double, double>(double *, const double *, const double *, long long, cudaStream_t);
+template void launch_scale_copy<float, float>(float *, const float *, const double *, long long, cudaStream_t);
+template void launch_scale_copy<float, double>(float *, const double *, const double *, long long, cudaStream_t);
 
 void launch_accumulate(double *p, const float *e, long long n, cudaStream_t s)
 {

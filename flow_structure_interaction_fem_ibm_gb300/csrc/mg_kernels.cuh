@@ -114,14 +114,17 @@ struct MaxLoc { double v; long long i; };
 void launch_calc_residual(const double *p, const double *b, const double *nlw0, const uint8_t *fl,
                           const Coef<double> &c, const Dims &d, float *r32_out, MaxLoc *partials,
                           int nblocks, MaxLoc *result, cudaStream_t s, double *r64_out = nullptr);
-// Krylov support (level-1 interior, fluid cells)
-void launch_apply_op(const double *z, double *w, const uint8_t *fl, const Coef<double> &c, const Dims &d,
-                     cudaStream_t s);
-void launch_mdot(const double *const *V, int nv, const double *w, const uint8_t *fl, const Dims &d,
-                 double *partials, int nblocks, double *out, cudaStream_t s);
-void launch_maxpy(double *w, const double *const *V, int nv, const double *coef, double sign, long long n,
-                  cudaStream_t s);
-void launch_scale_copy(double *dst, const double *src, const double *nrm2, long long n, cudaStream_t s);
+// Krylov support (level-1 interior, fluid cells); T = double or float, dot
+// products returned in FP64
+template <typename T>
+void launch_apply_op(const T *z, T *w, const uint8_t *fl, const Coef<T> &c, const Dims &d, cudaStream_t s);
+template <typename T>
+void launch_mdot(const T *const *V, int nv, const T *w, const uint8_t *fl, const Dims &d, double *partials,
+                 int nblocks, double *out, cudaStream_t s);
+template <typename T>
+void launch_maxpy(T *w, const T *const *V, int nv, const double *coef, double sign, long long n, cudaStream_t s);
+template <typename T, typename S>
+void launch_scale_copy(T *dst, const S *src, const double *nrm2, long long n, cudaStream_t s);
 int calc_residual_blocks(const Dims &d);
 void launch_subtract_average(double *p, const uint8_t *fl, const double *dx, const double *dy,
                              const double *dz, const Dims &d, double *partials, int nblocks,
