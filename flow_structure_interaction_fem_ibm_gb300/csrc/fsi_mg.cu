@@ -20,6 +20,7 @@
 #include <memory>
 #include <string>
 #include <type_traits>
+#include <unordered_map>
 #include <vector>
 
 using namespace fsimg;
@@ -98,6 +99,7 @@ struct Ctx {
     // ghost rows
     int nGhost = 0, ghost_cap = 0;
     long long *gidx = nullptr, *sidx = nullptr;
+    int *gsg = nullptr;   // stencil in the ghost-buffer encoding (GhostArgs::sg)
     double *gco64 = nullptr, *gscr64 = nullptr;
     float *gco32 = nullptr, *gscr32 = nullptr;
     int *d_iters = nullptr;
@@ -464,7 +466,7 @@ void gcm_pressure<double>(Ctx &c, double *v)
     launch_outer_ghost<double>(v, c.L1.d, c.sign, c.s);
     c.launches++;
     if (c.nGhost > 0) {
-        GhostArgs g{c.nGhost, c.gidx, c.sidx};
+        GhostArgs g{c.nGhost, c.gidx, c.sidx, c.gsg};
         launch_ghost_rows<double>(v, g, c.gco64, c.gscr64, c.p.iterMax_ad, c.p.restol_ad, 0.0, c.d_iters, c.d_maxd,
                                   c.s);
         c.launches++;
@@ -476,7 +478,7 @@ void gcm_pressure<float>(Ctx &c, float *v)
     launch_outer_ghost<float>(v, c.L1.d, c.sign, c.s);
     c.launches++;
     if (c.nGhost > 0) {
-        GhostArgs g{c.nGhost, c.gidx, c.sidx};
+        GhostArgs g{c.nGhost, c.gidx, c.sidx, c.gsg};
         launch_ghost_rows<float>(v, g, c.gco32, c.gscr32, c.p.iterMax_ad, c.p.restol_ad, 1.0e-6, c.d_iters, c.d_maxd,
                                  c.s);
         c.launches++;
@@ -576,7 +578,7 @@ void correct_pressure(Ctx &c, double *p, double *nlw0)
     launch_outer_ghost<double>(p, c.L1.d, c.sign, c.s);
     c.launches++;
     if (c.nGhost > 0) {
-        GhostArgs g{c.nGhost, c.gidx, c.sidx};
+        GhostArgs g{c.nGhost, c.gidx, c.sidx, c.gsg};
         launch_ghost_rows<double>(p, g, c.gco64, c.gscr64, c.p.iterMax_ad, c.p.restol_ad, 0.0, c.d_iters, c.d_maxd,
                                   c.s);
         c.launches++;
@@ -796,7 +798,7 @@ int solve_krylov_t(Ctx &c, double *p, const double *b, int *iters, double *maxre
             if (gcm) {   // ghost values of z from its fluid values (the map whose matrix A acts on)
                 launch_outer_ghost<T>(KZ[j], c.L1.d, c.sign, c.s);
                 if (c.nGhost > 0) {
-                    GhostArgs ga{c.nGhost, c.gidx, c.sidx};
+                    GhostArgs ga{c.nGhost, c.gidx, c.sidx, c.gsg};
                     launch_ghost_rows<T>(KZ[j], ga, gco, gscr, c.p.iterMax_ad, c.p.restol_ad, f32 ? 1.0e-6 : 0.0,
                                          c.d_iters, c.d_maxd, c.s);
                 }
@@ -1215,6 +1217,7 @@ int fsi_mg_set_geometry(void *handle, const int8_t *iblank, const int8_t *ghostC
     c.nGhost = nGhost;
     if (nGhost > 0) {
         std::vector<long long> gi(nGhost), si(8 * (size_t)nGhost);
+        std::vector<int> sg(8 * (size_t)nGhost);
         std::vector<float> cf(8 * (size_t)nGhost);
         for (int n = 0; n < nGhost; ++n) {
             const int ig = iGhost[n], jg = jGhost[n], kg = kGhost[n];
@@ -1230,9 +1233,19 @@ int fsi_mg_set_geometry(void *handle, const int8_t *iblank, const int8_t *ghostC
                 cf[8 * (size_t)n + r] = (float)coeffGCMN[8 * (size_t)n + r];
             }
         }
+        {   // stencil entries that are ghost cells refer to the ghost's number
+            std::unordered_map<long long, int> gnum;
+            gnum.reserve(2 * (size_t)nGhost);
+            for (int n = 0; n < nGhost; ++n) gnum.emplace(gi[n], n);
+            for (size_t e = 0; e < si.size(); ++e) {
+                if (si[e] < 0) { sg[e] = -1; continue; }
+                auto f = gnum.find(si[e]);
+                sg[e] = (f != gnum.end()) ? -(f->second + 2) : (int)si[e];
+            }
+        }
         if (nGhost > c.ghost_cap) {   // grow-only ghost buffers (body motion changes nGhost)
             for (void *q : {(void *)c.gidx, (void *)c.sidx, (void *)c.gco64, (void *)c.gco32, (void *)c.gscr64,
-                            (void *)c.gscr32}) {
+                            (void *)c.gscr32, (void *)c.gsg}) {
                 auto it = std::find(c.allocs.begin(), c.allocs.end(), q);
                 if (q && it != c.allocs.end()) { cudaFree(q); c.allocs.erase(it); }
             }
@@ -1241,12 +1254,14 @@ int fsi_mg_set_geometry(void *handle, const int8_t *iblank, const int8_t *ghostC
             TRY(c.alloc(&c.sidx, 8 * (size_t)cap));
             TRY(c.alloc(&c.gco64, 8 * (size_t)cap));
             TRY(c.alloc(&c.gco32, 8 * (size_t)cap));
-            TRY(c.alloc(&c.gscr64, cap));
-            TRY(c.alloc(&c.gscr32, cap));
+            TRY(c.alloc(&c.gsg, 8 * (size_t)cap));
+            TRY(c.alloc(&c.gscr64, 2 * (size_t)cap));   // two ping-pong buffers
+            TRY(c.alloc(&c.gscr32, 2 * (size_t)cap));
             c.ghost_cap = cap;
         }
         CK(cudaMemcpyAsync(c.gidx, gi.data(), gi.size() * 8, cudaMemcpyHostToDevice, c.s));
         CK(cudaMemcpyAsync(c.sidx, si.data(), si.size() * 8, cudaMemcpyHostToDevice, c.s));
+        CK(cudaMemcpyAsync(c.gsg, sg.data(), sg.size() * 4, cudaMemcpyHostToDevice, c.s));
         CK(cudaMemcpyAsync(c.gco64, coeffGCMN, 8 * (size_t)nGhost * 8, cudaMemcpyHostToDevice, c.s));
         CK(cudaMemcpyAsync(c.gco32, cf.data(), cf.size() * 4, cudaMemcpyHostToDevice, c.s));
         CK(cudaStreamSynchronize(c.s));
@@ -1480,7 +1495,7 @@ int fsi_mg_debug_level_op(void *handle, int op, int d, int n, void *a, void *b, 
         TRY(copy_level(c, L, t0, a, true));
         CK(cudaMemsetAsync(c.d_iters, 0, sizeof(int), c.s));
         if (c.nGhost > 0) {
-            GhostArgs g{c.nGhost, c.gidx, c.sidx};
+            GhostArgs g{c.nGhost, c.gidx, c.sidx, c.gsg};
             launch_ghost_rows<double>(t0, g, c.gco64, c.gscr64, c.p.iterMax_ad, c.p.restol_ad, 0.0, c.d_iters,
                                       c.d_maxd, c.s);
         }

@@ -921,10 +921,13 @@ __global__ void __launch_bounds__(1024) k_ghost_rows(T *v, GhostArgs g, const T 
     }
 }
 
-// Same fixed-point iteration spread over a cluster of 8 CTAs (8192 threads):
-// the per-sweep max |dp| is exchanged through distributed shared memory and
-// the sweeps are separated by cluster barriers.  Loop bounds are uniform over
-// the cluster and capped by iterMax.
+// Same fixed-point iteration spread over a cluster of 8 CTAs (8192 threads).
+// The ghost values are iterated in two ping-pong buffers (scratch[0:n] and
+// scratch[n:2n]); stencil entries that are ghost cells read the buffer, all
+// others read v, so one cluster barrier per sweep orders everything: each CTA
+// also posts its sweep maxima into rank 0's shared slots, double-buffered by
+// sweep parity.  The converged values are written into v once at the end.
+// Loop bounds are uniform over the cluster and capped by iterMax.
 constexpr int GHOST_CLUSTER = 8;
 
 template <typename T>
@@ -935,27 +938,31 @@ __global__ void __cluster_dims__(GHOST_CLUSTER, 1, 1) __launch_bounds__(1024)
     namespace cg = cooperative_groups;
     cg::cluster_group cluster = cg::this_cluster();
     __shared__ double s_d[32], s_a[32];
-    __shared__ double slot_d[GHOST_CLUSTER], slot_a[GHOST_CLUSTER];   // used in rank 0 only
+    __shared__ double slot_d[2][GHOST_CLUSTER], slot_a[2][GHOST_CLUSTER];   // used in rank 0 only
     const unsigned rank = cluster.block_rank();
     const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5, nw = (blockDim.x + 31) >> 5;
-    const long long gtid = (long long)rank * blockDim.x + tid, gstride = (long long)GHOST_CLUSTER * blockDim.x;
-    double *rslot_d = cluster.map_shared_rank(slot_d, 0);
-    double *rslot_a = cluster.map_shared_rank(slot_a, 0);
-    int it = 0;
+    const int gtid = (int)rank * (int)blockDim.x + tid, gstride = GHOST_CLUSTER * (int)blockDim.x;
+    double *rslot_d = cluster.map_shared_rank(&slot_d[0][0], 0);
+    double *rslot_a = cluster.map_shared_rank(&slot_a[0][0], 0);
+    T *bufA = scratch, *bufB = scratch + g.n;
+    for (int n = gtid; n < g.n; n += gstride) bufA[n] = v[g.gidx[n]];
+    cluster.sync();
+    int it = 0, par = 0;
     double maxd = 1.0e10, thr = tol;
     while (it < iterMax && maxd > thr) {
+        const T *src = par ? bufB : bufA;
+        T *dst = par ? bufA : bufB;
         double ld = 0.0, la = 0.0;
-        for (long long n = gtid; n < g.n; n += gstride) {
+        for (int n = gtid; n < g.n; n += gstride) {
             T acc = T(0);
 #pragma unroll
             for (int r = 0; r < 8; ++r) {
-                const long long sidx = g.sidx[8LL * n + r];
-                const T val = (sidx < 0) ? T(0) : v[sidx];
-                acc = acc + coeff[8LL * n + r] * val;
+                const int e = g.sg[8 * n + r];
+                const T val = (e >= 0) ? v[e] : ((e <= -2) ? src[-e - 2] : T(0));
+                acc = acc + coeff[8 * n + r] * val;
             }
-            const T old = v[g.gidx[n]];
-            scratch[n] = acc;
-            ld = fmax(ld, fabs((double)acc - (double)old));
+            dst[n] = acc;
+            ld = fmax(ld, fabs((double)acc - (double)src[n]));
             la = fmax(la, fabs((double)acc));
         }
         for (int o = 16; o > 0; o >>= 1) {
@@ -967,18 +974,24 @@ __global__ void __cluster_dims__(GHOST_CLUSTER, 1, 1) __launch_bounds__(1024)
         if (tid == 0) {
             double a = 0.0, b = 0.0;
             for (int w = 0; w < nw; ++w) { a = fmax(a, s_d[w]); b = fmax(b, s_a[w]); }
-            rslot_d[rank] = a;
-            rslot_a[rank] = b;
+            rslot_d[par * GHOST_CLUSTER + rank] = a;
+            rslot_a[par * GHOST_CLUSTER + rank] = b;
         }
-        cluster.sync();   // scratch and the slots are complete
-        for (long long n = gtid; n < g.n; n += gstride) v[g.gidx[n]] = scratch[n];
+        cluster.sync();   // dst and this sweep's slots are complete
         double a = 0.0, b = 0.0;
-        for (int q = 0; q < GHOST_CLUSTER; ++q) { a = fmax(a, rslot_d[q]); b = fmax(b, rslot_a[q]); }
+        for (int q = 0; q < GHOST_CLUSTER; ++q) {
+            a = fmax(a, rslot_d[par * GHOST_CLUSTER + q]);
+            b = fmax(b, rslot_a[par * GHOST_CLUSTER + q]);
+        }
         maxd = a;
         thr = fmax(tol, reltol * b);
         ++it;
-        cluster.sync();   // v updated everywhere; rank 0 slots free for the next sweep
+        par ^= 1;
+        __syncthreads();   // s_d / s_a are rewritten by the next sweep
     }
+    const T *fin = par ? bufB : bufA;   // the buffer the last sweep wrote
+    for (int n = gtid; n < g.n; n += gstride) v[g.gidx[n]] = fin[n];
+    cluster.sync();   // rank 0's slots stay alive until every CTA has read them
     if (rank == 0 && tid == 0) {
         atomicAdd(iters, it);
         atomicMax(maxdelta, (unsigned long long)__double_as_longlong(maxd));
@@ -1299,11 +1312,16 @@ __global__ void k_mdot_final(const double *partials, int nb, int n, double *out)
 template <typename T>
 __global__ void __launch_bounds__(TPB) k_maxpy(T *w, VecSet<T> V, const double *coef, double sign, long long n)
 {
+    // coefficients converted once per block (a per-element FP64 multiply would
+    // make this streaming kernel FP64-bound)
+    __shared__ T s_cf[8];
+    if (threadIdx.x < 8) s_cf[threadIdx.x] = (threadIdx.x < (unsigned)V.n) ? (T)(sign * coef[threadIdx.x]) : T(0);
+    __syncthreads();
     long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= n) return;
     T cf[8];
 #pragma unroll
-    for (int q = 0; q < 8; ++q) cf[q] = (q < V.n) ? (T)(sign * coef[q]) : T(0);
+    for (int q = 0; q < 8; ++q) cf[q] = s_cf[q];
     T acc = w[t];
 #pragma unroll
     for (int q = 0; q < 8; ++q)
@@ -1314,13 +1332,13 @@ __global__ void __launch_bounds__(TPB) k_maxpy(T *w, VecSet<T> V, const double *
 template <typename T, typename S>
 __global__ void k_scale_copy(T *dst, const S *src, const double *nrm2, long long n)
 {
-    // dst = src / sqrt(nrm2[0])
-    __shared__ double s_inv;
-    if (threadIdx.x == 0) s_inv = 1.0 / sqrt(nrm2[0]);
+    // dst = src / sqrt(nrm2[0]), multiplied in the precision of the source
+    __shared__ S s_inv;
+    if (threadIdx.x == 0) s_inv = (S)(1.0 / sqrt(nrm2[0]));
     __syncthreads();
     long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= n) return;
-    dst[t] = (T)((double)src[t] * s_inv);
+    dst[t] = (T)(src[t] * s_inv);
 }
 
 __global__ void k_accumulate(double *p, const float *e, long long n)

@@ -81,6 +81,8 @@ struct GhostArgs {
     int n;
     const long long *gidx;   // ghost cell linear index (level-1 layout)
     const long long *sidx;   // 8 stencil indices per ghost, -1 = the ghost itself (uNormal term)
+    const int *sg;           // the same stencil as: cell index (>= 0) of a non-ghost cell,
+                             // -(m + 2) for ghost cell number m, -1 for the uNormal term
 };
 
 // one-time kernel attributes (call before the first launch, outside stream capture)
