@@ -1372,6 +1372,32 @@ int fsi_mg_subtract_average(void *handle, double *pPrime)
     return 0;
 }
 
+int fsi_mg_subtract_average_noalloc(double *d_pPrime, const int8_t *d_iblank, const double *d_dx, const double *d_dy,
+                                    const double *d_dz, int ndim, int nx, int ny, int nz, void *stream)
+{
+    if (!d_pPrime || !d_iblank || !d_dx || !d_dy || !d_dz) return fail(-1, "null argument");
+    if (ndim != 2 && ndim != 3) return fail(-1, "ndim must be 2 or 3");
+    if (nx < 3 || ny < 3 || nz < 2) return fail(-1, "grid too small");
+    if (ndim == 2 && nz != 2) return fail(-1, "2D grids have nz = 2");
+    if ((long long)(nx + 1) * (ny + 1) * (nz + 1) >= (1LL << 31))
+        return fail(-1, "grid too large: the (0:nx+1,0:ny+1,0:nz+1) layout must hold fewer than 2^31 cells");
+    const long long rows = (long long)(ny - 1) * (nz - 1);
+    if (rows > NOALLOC_MAX_ROWS)
+        return fail(-1, "fsi_mg_subtract_average_noalloc: the grid has " + std::to_string(rows) +
+                            " (j,k) rows, (ny-1)*(nz-1); its fixed scratch holds at most " +
+                            std::to_string(NOALLOC_MAX_ROWS) + " (use fsi_mg_subtract_average)");
+    Dims d;
+    d.m[0] = nx; d.m[1] = ny; d.m[2] = nz;
+    d.sx = nx + 2;
+    d.sxy = (long long)(nx + 2) * (ny + 2);
+    // iblank is 0 or 1, so the array serves directly as the flag byte (bit 0 = iblank)
+    const cudaError_t e = launch_subtract_average_noalloc(d_pPrime, reinterpret_cast<const uint8_t *>(d_iblank),
+                                                          d_dx, d_dy, d_dz, d, static_cast<cudaStream_t>(stream));
+    if (e != cudaSuccess)
+        return fail(-10, std::string("fsi_mg_subtract_average_noalloc: ") + cudaGetErrorString(e));
+    return 0;
+}
+
 int fsi_mg_correct_pressure(void *handle, double *pPrime, double *nlw0_out)
 {
     if (!handle || !pPrime) return fail(-1, "null argument");

@@ -3,6 +3,7 @@
 #include "mg_kernels.cuh"
 
 #include <cfloat>
+#include <mutex>
 #include <cooperative_groups.h>
 
 namespace fsimg {
@@ -1401,6 +1402,40 @@ __global__ void k_coarse_flags(uint8_t *fl, Dims d, int sb0, int sb1, int sb2, i
     fl[o] = f;
 }
 
+// ---------------------------------------------------------------------------
+// Allocation-free mean removal.  Scratch for the per-row partial sums lives in
+// this file-scope device array, so the caller needs no cudaMalloc: every GPU
+// that loads the library holds 2*NOALLOC_MAX_ROWS + 8 doubles (about 1 MB)
+// until the process exits.  All calls share it and it keeps the last call's
+// contents; every slot a call reads is first written by that same call, so
+// nothing has to be cleared, but two calls that run at the same time on the
+// GPU (different streams, host threads or devices sharing a context) race on it.
+// ---------------------------------------------------------------------------
+static __device__ __align__(256) double g_noalloc_scratch[2 * NOALLOC_MAX_ROWS + 8];
+
+// One block per (j, k) row: the row's volume-weighted pressure sum and fluid
+// volume (the per-cell terms of IBM/CORE_POISSON.F90:430-440).
+__global__ void __launch_bounds__(TPB) k_avg_partial_rows(const double *p, const uint8_t *fl, const double *dx,
+                                                          const double *dy, const double *dz, Dims d,
+                                                          double *partials)
+{
+    const int n0 = d.m[0] - 1, n1 = d.m[1] - 1;
+    const int row = (int)blockIdx.x;
+    const int j = 1 + row % n1, k = 1 + row / n1;
+    const double dyz = dy[j] * dz[k];
+    const long long rb = d.idx(0, j, k);
+    double sp = 0.0, sv = 0.0;
+    for (int i = 1 + threadIdx.x; i <= n0; i += blockDim.x) {
+        if (fl[rb + i] & FB_IB) continue;
+        const double vol = dx[i] * dyz;
+        sp += p[rb + i] * vol;
+        sv += vol;
+    }
+    const double a = block_sum(sp);
+    const double b = block_sum(sv);
+    if (threadIdx.x == 0) { partials[2 * row] = a; partials[2 * row + 1] = b; }
+}
+
 } // namespace
 
 // ------------------------------------------------------------- launchers --
@@ -1815,5 +1850,42 @@ template void launch_ghost_rows<float>(float *, const GhostArgs &, const float *
 template void launch_fill<double>(double *, long long, double, cudaStream_t);
 template void launch_fill<float>(float *, long long, float, cudaStream_t);
 template void launch_fill<uint8_t>(uint8_t *, long long, uint8_t, cudaStream_t);
+
+// Device address of g_noalloc_scratch on the current device, looked up once
+// per device with that device current (host code cannot use the symbol's name
+// as a device pointer).
+cudaError_t noalloc_scratch(double **out)
+{
+    static std::mutex mu;
+    static double *addr[NOALLOC_MAX_DEVICES] = {};
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return e;
+    if (dev < 0 || dev >= NOALLOC_MAX_DEVICES) return cudaErrorInvalidDevice;
+    std::lock_guard<std::mutex> lock(mu);
+    if (!addr[dev]) {
+        void *q = nullptr;
+        e = cudaGetSymbolAddress(&q, g_noalloc_scratch);
+        if (e != cudaSuccess) return e;
+        addr[dev] = static_cast<double *>(q);
+    }
+    *out = addr[dev];
+    return cudaSuccess;
+}
+
+cudaError_t launch_subtract_average_noalloc(double *p, const uint8_t *fl, const double *dx, const double *dy,
+                                            const double *dz, const Dims &d, cudaStream_t s)
+{
+    const int rows = (d.m[1] - 1) * (d.m[2] - 1);
+    if (rows < 1 || rows > NOALLOC_MAX_ROWS) return cudaErrorInvalidValue;
+    double *scr = nullptr;
+    cudaError_t e = noalloc_scratch(&scr);
+    if (e != cudaSuccess) return e;
+    double *sums = scr + 2 * NOALLOC_MAX_ROWS;
+    k_avg_partial_rows<<<rows, TPB, 0, s>>>(p, fl, dx, dy, dz, d, scr);
+    k_sum_final<<<1, 1024, 0, s>>>(scr, rows, 2, sums);
+    k_avg_apply<<<rows, TPB, 0, s>>>(p, fl, d, sums);
+    return cudaGetLastError();
+}
 
 } // namespace fsimg

@@ -128,6 +128,13 @@ void launch_maxpy(T *w, const T *const *V, int nv, const double *coef, double si
 template <typename T, typename S>
 void launch_scale_copy(T *dst, const S *src, const double *nrm2, long long n, cudaStream_t s);
 int calc_residual_blocks(const Dims &d);
+// Mean removal (subtracting_average_pressure) with its partial sums in a
+// file-scope device array instead of caller or handle memory: at most
+// NOALLOC_MAX_ROWS (j, k) rows; devices numbered below NOALLOC_MAX_DEVICES.
+constexpr int NOALLOC_MAX_ROWS = 65536;
+constexpr int NOALLOC_MAX_DEVICES = 64;
+cudaError_t launch_subtract_average_noalloc(double *p, const uint8_t *fl, const double *dx, const double *dy,
+                                            const double *dz, const Dims &d, cudaStream_t s);
 void launch_subtract_average(double *p, const uint8_t *fl, const double *dx, const double *dy,
                              const double *dz, const Dims &d, double *partials, int nblocks,
                              cudaStream_t s);

@@ -103,6 +103,22 @@ int fsi_mg_calc_residual(void *handle, const double *var, const double *r, doubl
 /* subtracting_average_pressure (IBM/CORE_POISSON.F90:419), stationary bodies. */
 int fsi_mg_subtract_average(void *handle, double *pPrime);
 
+/* The same mean removal on device arrays, for callers that cannot allocate
+ * GPU memory (a host code whose device memory is owned by its own pool, or a
+ * time loop that must not pay cudaMalloc's implicit device synchronisation).
+ * No counterpart in the reference.  It needs no handle and allocates nothing:
+ * its partial sums live in a fixed device array of the library, one slot per
+ * (j,k) row, so grids with (ny-1)*(nz-1) > 65536 rows are rejected (status
+ * -1, message in fsi_mg_last_error).  d_pPrime (in/out) and d_iblank (0 or 1)
+ * use the full (0:nx+1,0:ny+1,0:nz+1) layout; d_dx, d_dy, d_dz hold the cell
+ * widths dx(0:nx+1) etc.  Work is queued on `stream` (a cudaStream_t, NULL
+ * for the default stream) and the call returns without waiting.  The first
+ * call on a device looks up the device address of that array; make this
+ * first call before any stream capture.  All calls share the array, so calls
+ * that can overlap on the GPU (other streams, host threads) race. */
+int fsi_mg_subtract_average_noalloc(double *d_pPrime, const int8_t *d_iblank, const double *d_dx, const double *d_dy,
+                                    const double *d_dz, int ndim, int nx, int ny, int nz, void *stream);
+
 /* GCM_correct_pressure (IBM/CORE_POISSON.F90:1794): outer ghost layer,
  * ghost-cell rows, compatibility correction of pgrad*, and nlw0 (OUT, may be NULL). */
 int fsi_mg_correct_pressure(void *handle, double *pPrime, double *nlw0_out);
