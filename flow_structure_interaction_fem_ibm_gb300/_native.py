@@ -42,6 +42,7 @@ SOLVER_SYMBOLS = {
     "fsi_mg_residual_history": [ctypes.c_void_p, c_double_p, ctypes.c_int],
     "fsi_mg_time_kernel": [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_int, c_double_p, c_double_p],
     "fsi_mg_line_timing": [ctypes.c_void_p, ctypes.c_int, c_double_p],
+    "fsi_mg_set_fresh_cells": [ctypes.c_void_p, ctypes.c_void_p],
     "fsi_mg_subtract_average_noalloc": [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
                                         ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int,
                                         ctypes.c_void_p],

@@ -118,6 +118,8 @@ struct Ctx {
     int sign[6] = {1, 1, 1, 1, 1, 1};
     double *d_dx[3] = {}, *d_dxinv[3] = {}, *d_dxcinv[3] = {};
 
+    uint8_t *fresh = nullptr;   // fresh_cell (level-1 layout) of a moving body
+    bool fresh_on = false;
     bool geometry = false;
     bool bound_device = false;   // p64/b64 point at caller memory
 
@@ -572,6 +574,18 @@ void mg_solver(Ctx &c, T *var, const T *rhs, bool homogeneous)
     }
 }
 
+// subtracting_average_pressure (IBM/CORE_POISSON.F90:419-490): volume-weighted
+// fluid mean removed, dead cells zeroed, then the fresh cells of a moving body
+void subtract_average(Ctx &c, double *p)
+{
+    launch_subtract_average(p, c.L1.fl, c.d_dx[0], c.d_dx[1], c.d_dx[2], c.L1.d, (double *)c.partials, c.nred, c.s);
+    c.launches += 3;
+    if (c.fresh_on) {
+        launch_fresh_cells(p, c.L1.fl, c.fresh, c.L1.d, c.p.ndim == 3, c.s);
+        c.launches++;
+    }
+}
+
 // GCM_correct_pressure on the level-1 FP64 field (IBM/CORE_POISSON.F90:1794-1823)
 void correct_pressure(Ctx &c, double *p, double *nlw0)
 {
@@ -754,8 +768,7 @@ int solve_krylov_t(Ctx &c, double *p, const double *b, int *iters, double *maxre
     if (dirichlet) return fail(-1, "outer_krylov needs all-Neumann pressure boundaries");
     if (c.compat_active) return fail(-1, "outer_krylov needs an inactive compatibility correction (no zero-gradient BCs)");
     if (c.nlw0_nonzero) { launch_fill<double>(c.nlw0, n1, 0.0, c.s); c.launches++; }
-    launch_subtract_average(p, c.L1.fl, c.d_dx[0], c.d_dx[1], c.d_dx[2], c.L1.d, (double *)c.partials, c.nred, c.s);
-    c.launches += 3;
+    subtract_average(c, p);
     CK(cudaMemsetAsync(c.d_iters, 0, sizeof(int), c.s));
     CK(cudaMemsetAsync(c.d_maxd, 0, sizeof(unsigned long long), c.s));
     c.hist.clear();
@@ -897,8 +910,7 @@ int solve_device(Ctx &c, double *p, const double *b, int *iters, double *maxres_
     const bool dirichlet = c.p.pbc[0] == PBC_DIRICHLET || c.p.pbc[2] == PBC_DIRICHLET || c.p.pbc[4] == PBC_DIRICHLET;
     if (c.nlw0_nonzero) { launch_fill<double>(c.nlw0, c.L1.d.count(), 0.0, c.s); c.launches++; }
     if (!dirichlet) {   // subtracting_average_pressure (IBM/CORE_POISSON.F90:527-537)
-        launch_subtract_average(p, c.L1.fl, c.d_dx[0], c.d_dx[1], c.d_dx[2], c.L1.d, (double *)c.partials, c.nred, c.s);
-        c.launches += 3;
+        subtract_average(c, p);
     }
     if (c.p.precision_mode == 1) {
         // initial FP64 residual feeds the first FP32 cycle
@@ -1366,7 +1378,7 @@ int fsi_mg_subtract_average(void *handle, double *pPrime)
     const long long n = c.L1.d.count();
     double *dp = c.stage;
     CK(cudaMemcpyAsync(dp, pPrime, n * 8, cudaMemcpyHostToDevice, c.s));
-    launch_subtract_average(dp, c.L1.fl, c.d_dx[0], c.d_dx[1], c.d_dx[2], c.L1.d, (double *)c.partials, c.nred, c.s);
+    subtract_average(c, dp);
     CK(cudaMemcpyAsync(pPrime, dp, n * 8, cudaMemcpyDeviceToHost, c.s));
     CK(cudaStreamSynchronize(c.s));
     return 0;
@@ -1395,6 +1407,24 @@ int fsi_mg_subtract_average_noalloc(double *d_pPrime, const int8_t *d_iblank, co
                                                           d_dx, d_dy, d_dz, d, static_cast<cudaStream_t>(stream));
     if (e != cudaSuccess)
         return fail(-10, std::string("fsi_mg_subtract_average_noalloc: ") + cudaGetErrorString(e));
+    return 0;
+}
+
+int fsi_mg_set_fresh_cells(void *handle, const int8_t *fresh_cell)
+{
+    if (!handle) return fail(-1, "null handle");
+    Ctx &c = *(Ctx *)handle;
+    if (!fresh_cell) { c.fresh_on = false; return 0; }
+    const long long n = c.L1.d.count();
+    long long nfresh = 0;
+    for (long long q = 0; q < n; ++q) {
+        if (fresh_cell[q] != 0 && fresh_cell[q] != 1) return fail(-3, "fresh_cell values must be 0 or 1");
+        nfresh += fresh_cell[q];
+    }
+    if (!c.fresh) TRY(c.alloc(&c.fresh, (size_t)n));
+    CK(cudaMemcpyAsync(c.fresh, fresh_cell, (size_t)n, cudaMemcpyHostToDevice, c.s));
+    CK(cudaStreamSynchronize(c.s));
+    c.fresh_on = nfresh > 0;
     return 0;
 }
 

@@ -1147,6 +1147,32 @@ __global__ void __launch_bounds__(TPB) k_avg_apply(double *p, const uint8_t *fl,
         p[rb + i] = (fl[rb + i] & FB_IB) ? 0.0 : p[rb + i] - pAvg;
 }
 
+// Fresh cells of a moving body (IBM/CORE_POISSON.F90:459-488): the mean of
+// the neighbours in the 3x3(x3) box that are neither blanked nor fresh, summed
+// in the reference's (kk, jj, ii) order.  Fresh cells read only non-fresh
+// cells, so one thread per cell needs no ordering.
+__global__ void __launch_bounds__(TPB) k_fresh_cells(double *p, const uint8_t *fl, const uint8_t *fresh, Dims d,
+                                                     int three_d)
+{
+    const int n0 = d.m[0] - 1, n1 = d.m[1] - 1, n2 = d.m[2] - 1;
+    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= (long long)n0 * n1 * n2) return;
+    int i, j, k;
+    cell_of((unsigned)t, (unsigned)n0, (unsigned)n1, i, j, k);
+    const long long o = d.idx(i, j, k);
+    if (fresh[o] != 1) return;
+    const int k1 = three_d ? k - 1 : k, k2 = three_d ? k + 1 : k;
+    int cnt = 0;
+    double sum = 0.0;
+    for (int kk = k1; kk <= k2; ++kk)
+        for (int jj = j - 1; jj <= j + 1; ++jj)
+            for (int ii = i - 1; ii <= i + 1; ++ii) {
+                const long long g = d.idx(ii, jj, kk);
+                if (!(fl[g] & FB_IB) && fresh[g] != 1) { ++cnt; sum = sum + p[g]; }
+            }
+    p[o] = sum / (double)cnt;
+}
+
 // compatibility flux, non-periodic branch (IBM/GCM_GLOBAL_MASS_CONSERVE.F90:290-331)
 struct CompatArgs {
     const double *p;
@@ -1691,6 +1717,13 @@ void launch_subtract_average(double *p, const uint8_t *fl, const double *dx, con
     k_sum_final<<<1, 1024, 0, s>>>(partials, nblocks, 2, sums);
     const int rows = (d.m[1] - 1) * (d.m[2] - 1);
     k_avg_apply<<<rows, TPB, 0, s>>>(p, fl, d, sums);
+}
+
+void launch_fresh_cells(double *p, const uint8_t *fl, const uint8_t *fresh, const Dims &d, bool three_d,
+                        cudaStream_t s)
+{
+    const long long n = (long long)(d.m[0] - 1) * (d.m[1] - 1) * (d.m[2] - 1);
+    k_fresh_cells<<<nblk(n), TPB, 0, s>>>(p, fl, fresh, d, three_d ? 1 : 0);
 }
 
 static CompatArgs make_compat(const double *p, const uint8_t *fl, const double *pg, const double *dx,

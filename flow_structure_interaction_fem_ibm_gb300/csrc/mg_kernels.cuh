@@ -128,6 +128,9 @@ void launch_maxpy(T *w, const T *const *V, int nv, const double *coef, double si
 template <typename T, typename S>
 void launch_scale_copy(T *dst, const S *src, const double *nrm2, long long n, cudaStream_t s);
 int calc_residual_blocks(const Dims &d);
+// fresh cells of a moving body take the mean of their non-blanked, non-fresh neighbours
+void launch_fresh_cells(double *p, const uint8_t *fl, const uint8_t *fresh, const Dims &d, bool three_d,
+                        cudaStream_t s);
 // Mean removal (subtracting_average_pressure) with its partial sums in a
 // file-scope device array instead of caller or handle memory: at most
 // NOALLOC_MAX_ROWS (j, k) rows; devices numbered below NOALLOC_MAX_DEVICES.

@@ -49,6 +49,11 @@ MODULE fsi_mg_gpu
       INTEGER(C_INT), INTENT(IN) :: iG(*), jG(*), kG(*), iCI(*), jCI(*), kCI(*)
       REAL(C_DOUBLE), INTENT(IN) :: coeff(*), probe(*), pgrad(*)
     END FUNCTION
+    INTEGER(C_INT) FUNCTION fsi_mg_set_fresh_cells(h, fresh) BIND(C, NAME='fsi_mg_set_fresh_cells')
+      IMPORT :: C_INT, C_INT8_T, C_PTR
+      TYPE(C_PTR), VALUE :: h
+      INTEGER(C_INT8_T), INTENT(IN) :: fresh(*)
+    END FUNCTION
     INTEGER(C_INT) FUNCTION fsi_mg_solve(h, pPrime, nlu0, nlw0, iters, maxres, loc, compTime) &
         BIND(C, NAME='fsi_mg_solve')
       IMPORT :: C_INT, C_DOUBLE, C_PTR
@@ -157,6 +162,11 @@ SUBROUTINE fsi_mg_update_geometry()
   ENDIF
   DEALLOCATE(pg)
   IF (rc /= 0) CALL fsi_mg_abort('fsi_mg_update_geometry', rc)
+  ! fresh cells of a moving body (allocated with the GCM arrays, GCM_MEMORY_ALLOCATE.F90:27)
+  IF (ALLOCATED(fresh_cell)) THEN
+    rc = fsi_mg_set_fresh_cells(fsi_mg_handle, fresh_cell)
+    IF (rc /= 0) CALL fsi_mg_abort('fsi_mg_set_fresh_cells', rc)
+  ENDIF
 END SUBROUTINE fsi_mg_update_geometry
 
 !-----------------------------------------------------------------------------

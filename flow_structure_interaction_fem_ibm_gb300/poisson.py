@@ -130,6 +130,18 @@ class PoissonSolver:
                                              ctypes.byref(m), loc))
         return m.value, tuple(loc)
 
+    def set_fresh_cells(self, fresh_cell):
+        """fresh_cell (int8, full layout) of a moving body for the mean removal;
+        None turns it off (IBM/CORE_POISSON.F90:459-488)."""
+        if fresh_cell is None:
+            _check(self.lib.fsi_mg_set_fresh_cells(self.h, None))
+        else:
+            f = np.asfortranarray(fresh_cell, dtype=np.int8)
+            if f.shape != self.shape:
+                raise ValueError(f"fresh_cell has shape {f.shape}, expected {self.shape}")
+            _check(self.lib.fsi_mg_set_fresh_cells(self.h, f.ctypes.data_as(ctypes.c_void_p)))
+        return self
+
     def subtracting_average_pressure(self, p):
         _check(self.lib.fsi_mg_subtract_average(self.h, _p(p)))
         return p

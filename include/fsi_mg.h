@@ -100,7 +100,8 @@ int fsi_mg_mg_solver(void *handle, double *var, const double *rr, double *compTi
  * over fluid cells and the first location (i,j,k) attaining it. */
 int fsi_mg_calc_residual(void *handle, const double *var, const double *r, double *resm, int *loc);
 
-/* subtracting_average_pressure (IBM/CORE_POISSON.F90:419), stationary bodies. */
+/* subtracting_average_pressure (IBM/CORE_POISSON.F90:419), including the
+ * fresh cells registered with fsi_mg_set_fresh_cells. */
 int fsi_mg_subtract_average(void *handle, double *pPrime);
 
 /* The same mean removal on device arrays, for callers that cannot allocate
@@ -118,6 +119,14 @@ int fsi_mg_subtract_average(void *handle, double *pPrime);
  * that can overlap on the GPU (other streams, host threads) race. */
 int fsi_mg_subtract_average_noalloc(double *d_pPrime, const int8_t *d_iblank, const double *d_dx, const double *d_dy,
                                     const double *d_dz, int ndim, int nx, int ny, int nz, void *stream);
+
+/* fresh_cell (IBM/AMODULES.F90:397, allocated (0:nx+1,0:ny+1,0:nz+1) at
+ * IBM/GCM_MEMORY_ALLOCATE.F90:27) of a moving body, INTEGER(1) 0 or 1: from
+ * now on the mean removal of every solve (and fsi_mg_subtract_average) sets
+ * each fresh cell to the mean of its non-blanked, non-fresh 3x3(x3)
+ * neighbours (IBM/CORE_POISSON.F90:459-488).  NULL (or all zero) turns it
+ * off.  Call after each fsi_mg_set_geometry that moved the body. */
+int fsi_mg_set_fresh_cells(void *handle, const int8_t *fresh_cell);
 
 /* GCM_correct_pressure (IBM/CORE_POISSON.F90:1794): outer ghost layer,
  * ghost-cell rows, compatibility correction of pgrad*, and nlw0 (OUT, may be NULL). */

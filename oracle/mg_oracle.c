@@ -43,6 +43,7 @@ struct or_ctx {
     double *x_MG[3], *xc_MG[3], *dx_MG[3], *dxinv_MG[3], *dxc_MG[3], *dxcinv_MG[3];
     /* fine flags (0:nx+1)^3 */
     int8_t *iblank, *ghost, *fl[6];
+    int8_t *fresh;   /* fresh_cell (0:nx+1)^3 or NULL (no fresh cells) */
     int8_t *flMG[6];
     int *ghostMG;
     int8_t **cib[3];    /* coarse iblank per direction, index n-1 (n>=2) */
@@ -224,6 +225,7 @@ or_ctx *or_create(const fsi_mg_params *p, const double *x, const double *y, cons
 void or_destroy(or_ctx *c)
 {
     if (!c) return;
+    free(c->fresh);
     for (int d = 0; d < 3; ++d) {
         free(c->x[d]); free(c->xc[d]); free(c->dx[d]); free(c->dxinv[d]); free(c->dxc[d]); free(c->dxcinv[d]);
         free(c->x_MG[d]); free(c->xc_MG[d]); free(c->dx_MG[d]); free(c->dxinv_MG[d]);
@@ -927,6 +929,35 @@ void or_subtract_average(or_ctx *c, double *p)
                 if (c->iblank[f] == 1) p[f] = 0.0;
                 else p[f] = p[f] - pAverage;
             }
+    /* fresh cells: mean of the non-blanked, non-fresh 3x3(x3) neighbours
+       (IBM/CORE_POISSON.F90:459-488); a fresh cell without such a neighbour
+       divides 0 by 0, as the reference does */
+    if (!c->fresh) return;
+    for (int k = 1; k <= c->nz - 1; ++k)
+        for (int j = 1; j <= c->ny - 1; ++j)
+            for (int i = 1; i <= c->nx - 1; ++i) {
+                if (c->fresh[FI(c, i, j, k)] != 1) continue;
+                int i1 = 0;
+                double p1 = 0.0;
+                const int k1 = (c->p.ndim == DIM_3D) ? k - 1 : k, k2 = (c->p.ndim == DIM_3D) ? k + 1 : k;
+                for (int kk = k1; kk <= k2; ++kk)
+                    for (int jj = j - 1; jj <= j + 1; ++jj)
+                        for (int ii = i - 1; ii <= i + 1; ++ii) {
+                            size_t g = FI(c, ii, jj, kk);
+                            if (c->iblank[g] != 1 && c->fresh[g] != 1) { i1 = i1 + 1; p1 = p1 + p[g]; }
+                        }
+                p[FI(c, i, j, k)] = p1 / (double)i1;
+            }
+}
+
+void or_set_fresh(or_ctx *c, const int8_t *fresh)
+{
+    const size_t n = (size_t)(c->nx + 2) * (c->ny + 2) * (c->nz + 2);
+    free(c->fresh);
+    c->fresh = NULL;
+    if (!fresh) return;
+    c->fresh = (int8_t *)malloc(n);
+    memcpy(c->fresh, fresh, n);
 }
 
 /* IBM/CORE_SET_BC.F90:635-699 set_pressure_dirichlet_bc */

@@ -64,6 +64,8 @@ int     or_solve(or_ctx *c, double *pPrime, const double *nlu0, double *nlw0_out
 int     or_mg_solver(or_ctx *c, double *var, const double *rr);
 double  or_calc_residual(or_ctx *c, const double *var, const double *r, int *loc);
 void    or_subtract_average(or_ctx *c, double *p);
+/* fresh_cell (0:nx+1)^3 of a moving body for or_subtract_average (NULL: none) */
+void    or_set_fresh(or_ctx *c, const int8_t *fresh);
 void    or_gcm_correct_pressure(or_ctx *c, double *p);
 int     or_level_count(or_ctx *c, int d);
 int     or_level_size(or_ctx *c, int d, int n);

@@ -50,6 +50,8 @@ def lib():
         L.or_calc_residual.restype = ctypes.c_double
         L.or_subtract_average.argtypes = [ctypes.c_void_p, _dp]
         L.or_subtract_average.restype = None
+        L.or_set_fresh.argtypes = [ctypes.c_void_p, _i8]
+        L.or_set_fresh.restype = None
         L.or_gcm_correct_pressure.argtypes = [ctypes.c_void_p, _dp]
         L.or_gcm_correct_pressure.restype = None
         L.or_level_count.argtypes = [ctypes.c_void_p, ctypes.c_int]
@@ -144,6 +146,15 @@ class Oracle:
         loc = (ctypes.c_int * 3)()
         m = lib().or_calc_residual(self.h, _p(var), _p(r), loc)
         return m, tuple(loc)
+
+    def set_fresh(self, fresh):
+        """fresh_cell array (full layout, int8) used by subtract_average; None clears it."""
+        if fresh is None:
+            lib().or_set_fresh(self.h, None)
+        else:
+            self._fresh = np.asfortranarray(fresh, dtype=np.int8)
+            lib().or_set_fresh(self.h, _p(self._fresh, _i8))
+        return self
 
     def subtract_average(self, p):
         lib().or_subtract_average(self.h, _p(p))

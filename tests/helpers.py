@@ -69,3 +69,47 @@ def cell_volumes(problem):
     p = problem.params
     mx, my, mz = Metrics(problem.x), Metrics(problem.y), Metrics(problem.z)
     return (mx.dx[1:p.nx, None, None] * my.dx[None, 1:p.ny, None] * mz.dx[None, None, 1:p.nz])
+
+
+def fresh_shell(problem):
+    """Fresh-cell mask of a moving body for tests: the interior fluid cells with
+    a ghost cell among their six face neighbours (a one-cell shell around the
+    body, so fresh cells also neighbour each other)."""
+    ib, gh = problem.geom.iblank, problem.geom.ghost
+    fresh = np.zeros_like(ib, dtype=np.int8)
+    nx, ny, nz = problem.params.nx, problem.params.ny, problem.params.nz
+    three_d = problem.params.ndim == 3
+    ks = range(1, nz) if three_d else [1]
+    for k in ks:
+        for j in range(1, ny):
+            for i in range(1, nx):
+                if ib[i, j, k] != 0:
+                    continue
+                nb = [gh[i - 1, j, k], gh[i + 1, j, k], gh[i, j - 1, k], gh[i, j + 1, k]]
+                if three_d:
+                    nb += [gh[i, j, k - 1], gh[i, j, k + 1]]
+                if any(v == 1 for v in nb):
+                    fresh[i, j, k] = 1
+    return fresh
+
+
+def fresh_reference(problem, p, fresh):
+    """Fresh-cell step of subtracting_average_pressure restated with numpy
+    loops (IBM/CORE_POISSON.F90:459-488), applied to p in place."""
+    ib = problem.geom.iblank
+    nx, ny, nz = problem.params.nx, problem.params.ny, problem.params.nz
+    three_d = problem.params.ndim == 3
+    for k in range(1, nz):
+        for j in range(1, ny):
+            for i in range(1, nx):
+                if fresh[i, j, k] != 1:
+                    continue
+                cnt, s = 0, 0.0
+                for kk in (range(k - 1, k + 2) if three_d else [k]):
+                    for jj in range(j - 1, j + 2):
+                        for ii in range(i - 1, i + 2):
+                            if ib[ii, jj, kk] != 1 and fresh[ii, jj, kk] != 1:
+                                cnt += 1
+                                s = s + p[ii, jj, kk]
+                p[i, j, k] = s / cnt
+    return p

@@ -195,3 +195,23 @@ def test_mg_solver_one_cycle(pair):
     g.MG_Solver(got, pr.nlu0)
     I = tuple(slice(0, m) for m in (pr.params.nx + 1, pr.params.ny + 1, pr.params.nz + 1))
     assert rel(got[I], ref[I]) < 1e-10
+
+
+def test_subtract_average_fresh_cells(pair):
+    """Mean removal with the fresh cells of a moving body, GPU vs oracle."""
+    from tests.helpers import fresh_shell
+    pr, o, g = pair
+    if pr.geom.nGhost == 0:
+        pytest.skip("no body")
+    fresh = fresh_shell(pr)
+    rng = np.random.default_rng(17)
+    p = np.asfortranarray(rng.standard_normal(pr.shape))
+    o.set_fresh(fresh)
+    g.set_fresh_cells(fresh)
+    try:
+        ref = o.subtract_average(p.copy(order="F"))
+        got = g.subtracting_average_pressure(p.copy(order="F"))
+        assert np.abs(got - ref).max() < 1e-13
+    finally:
+        o.set_fresh(None)
+        g.set_fresh_cells(None)

@@ -139,3 +139,22 @@ def test_golden_fixtures_reproduced():
             assert np.array_equal(data[k], fresh[k]), k
         else:
             assert np.allclose(data[k], fresh[k], rtol=1e-11, atol=1e-14 * max(1.0, abs(data[k]).max())), k
+
+
+def test_fresh_cells_in_mean_removal():
+    """subtracting_average_pressure on a moving body: fresh cells take the mean
+    of their non-blanked, non-fresh neighbours (IBM/CORE_POISSON.F90:459-488)."""
+    from tests.helpers import fresh_reference, fresh_shell
+    pr = P.sphere(12, stretch=None, seed=13)
+    fresh = fresh_shell(pr)
+    assert fresh.sum() > 0
+    rng = np.random.default_rng(3)
+    p = np.asfortranarray(rng.standard_normal(pr.shape))
+    o = Oracle(pr)
+    base = o.subtract_average(p.copy(order="F"))
+    o.set_fresh(fresh)
+    got = o.subtract_average(p.copy(order="F"))
+    o.close()
+    ref = fresh_reference(pr, base.copy(order="F"), fresh)
+    assert np.array_equal(got, ref)
+    assert not np.array_equal(got, base)
