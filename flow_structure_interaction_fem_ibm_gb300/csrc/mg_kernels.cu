@@ -191,7 +191,7 @@ __device__ __forceinline__ void pcr_step(T &A, T &B, T &C, T &D, T &iB, int lane
 // the 32 interface unknowns of the line are solved by PCR over shuffles, and
 // the rows are back-substituted and written through shared memory.  Index
 // arithmetic is 32-bit (level-1 arrays hold fewer than 2^31 cells).
-template <typename T, int DIR, int S, bool OMEGA1>
+template <typename T, int DIR, int S, bool OMEGA1, bool FULL>
 __global__ void __launch_bounds__(256) k_line_wp(LineArgs<T> A)
 {
     using X = Axes<DIR>;
@@ -200,7 +200,8 @@ __global__ void __launch_bounds__(256) k_line_wp(LineArgs<T> A)
     constexpr int RP = wp_pitch<S>();
     T *sa = sm, *sb = sm + WP_LINES * RP, *sc = sm + 2 * WP_LINES * RP, *sd = sm + 3 * WP_LINES * RP;
     const Dims &d = A.d;
-    const int nb = d.m[X::b] - 1, nc = d.m[X::c] - 1, L = d.m[X::a] - 1;
+    const int nb = d.m[X::b] - 1, nc = d.m[X::c] - 1;
+    const int L = FULL ? 32 * S : d.m[X::a] - 1;   // FULL: every row of every lane is a line row
     const int hb = (nb + 1) >> 1;
     const int nlines = hb * nc;
     const int sa_ = (int)stride_of(d, X::a), sb_ = (int)stride_of(d, X::b), sc_ = (int)stride_of(d, X::c);
@@ -295,13 +296,21 @@ __global__ void __launch_bounds__(256) k_line_wp(LineArgs<T> A)
                 } else {
                     dd = ((f & FB_GM) || fluid) ? in[u].vo : T(0);
                 }
-                if (i == 1 && A.dir_lo) dd = dd - A.ppp_lo * aa;
-                if (i == L && A.dir_hi) dd = dd - A.ppp_hi * cc;
-                if (i == 1) aa = T(0);   // tdma ignores a(n1) and c(n2)
-                if (i == L) cc = T(0);
                 const int si = sidx(gs, r);
                 sa[si] = aa; sb[si] = bb; sc[si] = cc; sd[si] = dd;
             }
+        }
+        // line ends (written by this same thread above): finest-level Dirichlet
+        // terms, and tdma ignores a(n1) and c(n2)
+        if (rr == 0) {
+            const int si = sidx(gs, 0);
+            if (A.dir_lo) sd[si] = sd[si] - A.ppp_lo * sa[si];
+            sa[si] = T(0);
+        }
+        if (rr == (L - 1) % 32) {
+            const int si = sidx(gs, L - 1);
+            if (A.dir_hi) sd[si] = sd[si] - A.ppp_hi * sc[si];
+            sc[si] = T(0);
         }
     }
     __syncthreads();
@@ -384,9 +393,9 @@ __global__ void __launch_bounds__(256) k_line_wp(LineArgs<T> A)
             const int o = base + i * sa_;
             const T x = sd[sidx(gs, r)];
             A.v[o] = OMEGA1 ? x : A.v[o] * (T(1) - A.omega) + A.omega * x;
-            if (i == 1 && A.dir_lo) A.v[base] = A.ppp_lo;
-            if (i == L && A.dir_hi) A.v[base + (L + 1) * sa_] = A.ppp_hi;
         }
+        if (rr == 0 && A.dir_lo) A.v[base] = A.ppp_lo;
+        if (rr == (L - 1) % 32 && A.dir_hi) A.v[base + (L + 1) * sa_] = A.ppp_hi;
     }
 }
 
@@ -1471,18 +1480,26 @@ size_t wp_smem() { return 4 * (size_t)WP_LINES * wp_pitch<S>() * sizeof(T); }
 template <typename T, int DIR, int S, bool O1>
 void launch_wp_one(const LineArgs<T> &a, long long nlines, cudaStream_t s)
 {
+    static const int ax[3] = {0, 1, 2};
     const long long blocks = (nlines + WP_LINES - 1) / WP_LINES;
-    k_line_wp<T, DIR, S, O1><<<(unsigned)blocks, 256, wp_smem<T, DIR, S, O1>(), s>>>(a);
+    if (a.d.m[ax[DIR]] - 1 == 32 * S)
+        k_line_wp<T, DIR, S, O1, true><<<(unsigned)blocks, 256, wp_smem<T, DIR, S, O1>(), s>>>(a);
+    else
+        k_line_wp<T, DIR, S, O1, false><<<(unsigned)blocks, 256, wp_smem<T, DIR, S, O1>(), s>>>(a);
 }
 
 template <typename T, int DIR, int S>
 cudaError_t wp_attr()
 {
-    cudaError_t e = cudaFuncSetAttribute(k_line_wp<T, DIR, S, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         (int)wp_smem<T, DIR, S, true>());
-    if (e != cudaSuccess) return e;
-    return cudaFuncSetAttribute(k_line_wp<T, DIR, S, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                (int)wp_smem<T, DIR, S, false>());
+    const int b = (int)wp_smem<T, DIR, S, true>();
+    cudaError_t e;
+    if ((e = cudaFuncSetAttribute(k_line_wp<T, DIR, S, true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, b)))
+        return e;
+    if ((e = cudaFuncSetAttribute(k_line_wp<T, DIR, S, true, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, b)))
+        return e;
+    if ((e = cudaFuncSetAttribute(k_line_wp<T, DIR, S, false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, b)))
+        return e;
+    return cudaFuncSetAttribute(k_line_wp<T, DIR, S, false, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, b);
 }
 
 template <typename T, int DIR>
