@@ -358,43 +358,58 @@ class _DeviceMG:
             s.close()
 
 
+def _flat_view(x):
+    """1-D view (or copy) of a full array in Fortran order."""
+    return x.permute(2, 1, 0).reshape(-1)
+
+
 def fgmres(apply_op, precond, rhs, dot, rtol=1e-12, m=40, max_apps=400):
-    """Right-preconditioned FGMRES (classical Gram-Schmidt twice) on full
-    arrays; returns (x, applications, final relative 2-norm residual)."""
-    beta0 = math.sqrt(dot(rhs, rhs))
-    x = torch.zeros_like(rhs)
+    """Right-preconditioned FGMRES on full arrays: the basis is kept as the
+    rows of one matrix, so classical Gram-Schmidt (twice) is two matrix-vector
+    products per pass and one host transfer per iteration.  Returns (x,
+    applications, final relative 2-norm residual)."""
+    shape = rhs.shape
+    dev = rhs.device
+    N = rhs.numel()
+    unflat = lambda v: v.reshape(tuple(reversed(shape))).permute(2, 1, 0)
+    b = _flat_view(rhs).clone()
+    beta0 = float(torch.linalg.vector_norm(b))
+    x = torch.zeros(N, dtype=torch.float64, device=dev)
     if beta0 == 0.0:
-        return x, 0, 0.0
+        return unflat(x), 0, 0.0
+    V = torch.empty((m + 1, N), dtype=torch.float64, device=dev)
+    Z = torch.empty((m, N), dtype=torch.float64, device=dev)
     apps = 0
-    r = rhs.clone()
+    r = b
     rel = 1.0
     while apps < max_apps:
-        beta = math.sqrt(dot(r, r))
+        beta = float(torch.linalg.vector_norm(r))
         rel = beta / beta0
         if rel <= rtol:
             break
-        V = [r / beta]
-        Z = []
+        V[0] = r / beta
         H = np.zeros((m + 1, m))
         g = np.zeros(m + 1)
         g[0] = beta
         cs, sn = np.zeros(m), np.zeros(m)
         k = 0
         for j in range(m):
-            z = precond(V[j])
-            Z.append(z)
-            wv = apply_op(z)
+            Z[j] = _flat_view(precond(unflat(V[j])))
+            wv = _flat_view(apply_op(unflat(Z[j]))).clone()
             apps += 1
-            for _ in range(2):
-                for i in range(j + 1):
-                    h = dot(V[i], wv)
-                    H[i, j] += h
-                    wv = wv - h * V[i]
-            hn = math.sqrt(dot(wv, wv))
+            Vj = V[:j + 1]
+            h1 = Vj @ wv
+            wv -= Vj.T @ h1
+            h2 = Vj @ wv
+            wv -= Vj.T @ h2
+            hn_d = torch.linalg.vector_norm(wv)
+            hv = torch.cat([h1 + h2, hn_d.reshape(1)]).cpu().numpy()
+            H[:j + 1, j] = hv[:j + 1]
+            hn = float(hv[j + 1])
             H[j + 1, j] = hn
             for i in range(j):
-                a, b = H[i, j], H[i + 1, j]
-                H[i, j], H[i + 1, j] = cs[i] * a + sn[i] * b, -sn[i] * a + cs[i] * b
+                a_, b_ = H[i, j], H[i + 1, j]
+                H[i, j], H[i + 1, j] = cs[i] * a_ + sn[i] * b_, -sn[i] * a_ + cs[i] * b_
             rr = math.hypot(H[j, j], H[j + 1, j])
             cs[j], sn[j] = (H[j, j] / rr, H[j + 1, j] / rr) if rr > 0 else (1.0, 0.0)
             H[j, j], H[j + 1, j] = rr, 0.0
@@ -402,12 +417,11 @@ def fgmres(apply_op, precond, rhs, dot, rtol=1e-12, m=40, max_apps=400):
             k = j + 1
             if abs(g[j + 1]) <= 0.5 * rtol * beta0 or hn == 0.0 or apps >= max_apps:
                 break
-            V.append(wv / hn)
+            V[j + 1] = wv / hn
         y = np.linalg.solve(np.triu(H[:k, :k]), g[:k])
-        for i in range(k):
-            x = x + float(y[i]) * Z[i]
-        r = rhs - apply_op(x)
-    return x, apps, rel
+        x += torch.as_tensor(y, device=dev) @ Z[:k]
+        r = b - _flat_view(apply_op(unflat(x)))
+    return unflat(x), apps, rel
 
 
 class Projection:
