@@ -130,12 +130,37 @@ class ProjectionOperators:
         self.C_GF = sp.csr_matrix((vals_f, (rows_f, cols_f)), shape=(nG, ntot))
         self.C_GG = sp.csr_matrix((vals_g, (rows_g, cols_g)), shape=(nG, nG))
         IG = sp.identity(nG, format="csc")
-        self._lu = spla.splu((IG - self.C_GG).tocsc())
-        self._luT = spla.splu((IG - self.C_GG).T.tocsc())
         self.gidx_np = gi
         self.gidx = torch.as_tensor(gi, device=self.dev)
-        # stencil cells reached by C_GF^T
-        self.C_GF_T = self.C_GF.T.tocsr()
+        # ghost elimination X = (I - C_GG)^-1 C_GF: p_G = X p (extend) and the
+        # transpose X^T y_G (extend_T), both as padded-row gathers on the device
+        X = sp.csr_matrix(spla.spsolve((IG - self.C_GG).tocsc(), self.C_GF.tocsc()))
+        X.eliminate_zeros()
+        self.X = X
+        self._gX = self._padded(X)
+        XT = X.T.tocsr()
+        rows = np.nonzero(np.diff(XT.indptr))[0]          # cells that receive ghost cotangents
+        self._xt_rows = torch.as_tensor(rows, device=self.dev)
+        self._gXT = self._padded(XT[rows])
+
+    def _padded(self, S):
+        """Sparse rows as (cols, vals) padded to the longest row, for a
+        deterministic gather-and-sum product on the device."""
+        S = S.tocsr()
+        nr = S.shape[0]
+        width = max(1, int(np.diff(S.indptr).max())) if nr else 1
+        cols = np.zeros((nr, width), dtype=np.int64)
+        vals = np.zeros((nr, width))
+        for r in range(nr):
+            a, b = S.indptr[r], S.indptr[r + 1]
+            cols[r, :b - a] = S.indices[a:b]
+            vals[r, :b - a] = S.data[a:b]
+        return torch.as_tensor(cols, device=self.dev), torch.as_tensor(vals, device=self.dev)
+
+    @staticmethod
+    def _gather_mv(pad, v):
+        cols, vals = pad
+        return (vals * v[cols]).sum(dim=1)
 
     def _flat(self, x):
         """Fortran-order flat view (copy) of a full array as numpy."""
@@ -146,9 +171,8 @@ class ProjectionOperators:
         out = as_fortran(pf * self.fluid)
         if self.nG == 0:
             return out
-        pg = self._lu.solve(self.C_GF @ self._flat(out))
         flat = out.permute(2, 1, 0).reshape(-1)
-        flat[self.gidx] = torch.as_tensor(pg, device=self.dev)
+        flat[self.gidx] = self._gather_mv(self._gX, flat)
         return out
 
     def extend_T(self, y):
@@ -157,12 +181,9 @@ class ProjectionOperators:
         out = as_fortran(y * self.fluid)
         if self.nG == 0:
             return out
-        yg = y.permute(2, 1, 0).reshape(-1)[self.gidx].cpu().numpy()
-        q = self._luT.solve(yg)
-        add = self.C_GF_T @ q                       # onto the (non-ghost) stencil cells
-        nz = np.nonzero(add)[0]
+        yg = y.permute(2, 1, 0).reshape(-1)[self.gidx]
         flat = out.permute(2, 1, 0).reshape(-1)
-        flat[torch.as_tensor(nz, device=self.dev)] += torch.as_tensor(add[nz], device=self.dev)
+        flat[self._xt_rows] += self._gather_mv(self._gXT, yg)
         return out * self.fluid
 
     # ------------------------------------------------- divergence (D F) --
@@ -443,10 +464,10 @@ class Projection:
         """V M V^-1: forward multigrid conjugated by the fluid cell volumes."""
         return self.vol * (self.mg.precondition(self.volinv * v) * self.ops.fluid)
 
-    def solve_T(self, s, rtol=1e-12):
+    def solve_T(self, s, rtol=1e-10):
         """A_eff^T z = s (s orthogonal to 1_F); returns one solution."""
         z, apps, rel = fgmres(self.ops.apply_eff_T, self._precond_T, s * self.ops.fluid, self.ops.dot,
-                              rtol=rtol)
+                              rtol=rtol, m=60)
         self.stats["transposed_applications"] = apps
         self.stats["transposed_rel_residual"] = rel
         return z
@@ -454,7 +475,7 @@ class Projection:
     def _left_null(self):
         """w with w^T A_eff = 0, scaled so that w . 1_F = volume of the fluid."""
         v1 = self.vol.clone()
-        d = self.solve_T(-self.ops.apply_eff_T(v1))
+        d = self.solve_T(-self.ops.apply_eff_T(v1), rtol=1e-13)
         w = (v1 + d) * self.ops.fluid
         return w * (float(self.vol.sum()) / float(w.sum()))
 
@@ -475,8 +496,9 @@ class Projection:
         gx, gy, gz = self.ops.grad(p)
         return u - gx, v - gy, w - gz, p
 
-    def backward(self, lu, lv, lw, rtol=1e-12):
-        """dL/du* for cotangents (lu, lv, lw) of the corrected velocity."""
+    def backward(self, lu, lv, lw, rtol=1e-10):
+        """dL/du* for cotangents (lu, lv, lw) of the corrected velocity; rtol is
+        the relative 2-norm residual of the transposed solve."""
         o = self.ops
         s = o.extend_T(o.grad_T(lu, lv, lw))
         z = self.solve_T(s, rtol)
@@ -494,8 +516,8 @@ class ProjectionStep(torch.autograd.Function):
     the multigrid solve, backward through the hand-written adjoint."""
 
     @staticmethod
-    def forward(ctx, u, v, w, proj: Projection, rtol: float = 1e-12):
-        ctx.proj, ctx.rtol = proj, rtol
+    def forward(ctx, u, v, w, proj: Projection, rtol: float = 1e-12, rtol_T: float = 1e-10):
+        ctx.proj, ctx.rtol = proj, rtol_T
         un, vn, wn, _ = proj.forward(u.detach(), v.detach(), w.detach(), rtol)
         return un, vn, wn
 
@@ -504,7 +526,7 @@ class ProjectionStep(torch.autograd.Function):
         z = ctx.proj.ops.fluid
         gu, gv, gw = (torch.zeros_like(z) if g is None else g for g in (gu, gv, gw))
         du, dv, dw = ctx.proj.backward(gu, gv, gw, ctx.rtol)
-        return du, dv, dw, None, None
+        return du, dv, dw, None, None, None
 
 
 def box_kinetic_energy(problem, u, v, w, box=((0.6, 0.9), (0.35, 0.65), (0.35, 0.65))):
