@@ -53,6 +53,9 @@ def parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--krylov", type=int, default=30, help="FGMRES restart length around MG_Solver (0: stationary)")
+    ap.add_argument("--no-adjoint", action="store_true")
+    ap.add_argument("--adjoint-n", type=int, default=96)
+    ap.add_argument("--adjoint-dirs", type=int, default=200)
     ap.add_argument("--profile", action="store_true",
                     help="profiling driver: raw RHS, two outer iterations of each precision, no other work")
     ap.add_argument("--profile-krylov", action="store_true",
@@ -257,6 +260,55 @@ def run_reference(args, rank, world):
     print(json.dumps(out))
 
 
+def adjoint_check(n, ndir, h=1e-6):
+    """Projection-step adjoint on the n^3 uniform grid with the r = 0.15 sphere:
+    velocity = seeded Gaussian field (|k| <= 8, seed 4), loss = kinetic energy
+    of the projected field in [0.6,0.9]x[0.35,0.65]^2.  Times one forward and
+    one backward (GPU synchronised, wall clock: the adjoint is a torch harness
+    around the multigrid) and checks the gradient against FP64 central
+    differences on `ndir` seeded random directions."""
+    import torch
+    from flow_structure_interaction_fem_ibm_gb300 import problem as P
+    from flow_structure_interaction_fem_ibm_gb300.adjoint import Projection, box_kinetic_energy
+    pr = P.sphere(n, seed=4, stretch=None)
+    t0 = time.perf_counter()
+    proj = Projection(pr, "cuda")
+    setup = time.perf_counter() - t0
+    rng = np.random.Generator(np.random.PCG64(4))
+    u, v, w = [torch.as_tensor(np.asfortranarray(P.gaussian_field(pr.params, pr.x, pr.y, pr.z, rng, 8)),
+                               device="cuda") for _ in range(3)]
+    fwd, bwd = [], []
+    for _ in range(3):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        un, vn, wn, _ = proj.forward(u, v, w)
+        torch.cuda.synchronize()
+        fwd.append(time.perf_counter() - t0)
+        outs = [t.detach().requires_grad_() for t in (un, vn, wn)]
+        lam = torch.autograd.grad(box_kinetic_energy(pr, *outs), outs)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        gu, gv, gw = proj.backward(*lam)
+        torch.cuda.synchronize()
+        bwd.append(time.perf_counter() - t0)
+    stats = dict(proj.stats)
+    g = torch.Generator().manual_seed(11)
+    loss = lambda a, b, c: float(box_kinetic_energy(pr, *proj.forward(a, b, c)[:3]))
+    worst = 0.0
+    for _ in range(ndir):
+        d = [torch.randn(pr.shape[::-1], dtype=torch.float64, generator=g).permute(2, 1, 0).cuda() for _ in range(3)]
+        fd = (loss(u + h * d[0], v + h * d[1], w + h * d[2]) - loss(u - h * d[0], v - h * d[1], w - h * d[2])) / (2 * h)
+        an = float((gu * d[0]).sum() + (gv * d[1]).sum() + (gw * d[2]).sum())
+        worst = max(worst, abs(fd - an) / abs(an))
+    proj.close()
+    f_s, b_s = float(np.median(fwd)), float(np.median(bwd))
+    return {"config": f"sphere_{n}^3_uniform_r0.15_seed4_box_KE", "forward_s": f_s, "backward_s": b_s,
+            "adjoint_over_forward": b_s / f_s, "forward_mg_applications": stats.get("forward_applications"),
+            "transposed_mg_applications": stats.get("transposed_applications"), "fd_directions": ndir,
+            "fd_h": h, "fd_worst_rel": worst, "setup_s": setup,
+            "timing": "wall clock with the GPU synchronised, median of 3"}
+
+
 def cpu_iteration_time(seed, sample_n=128):
     oracle_iteration_time(sample_n, seed)   # builds the oracle (not timed)
     return oracle_iteration_time(sample_n, seed), sample_n
@@ -427,6 +479,13 @@ def main():
         e2e = {"value": world * k / tot, "unit": "solves/s", "h2d_bytes_per_step": 2 * nbytes,
                "d2h_bytes_per_step": nbytes}
 
+    adjoint = None
+    if rank == 0 and not args.no_adjoint:
+        s_mixed.close()
+        s_fp64.close()
+        s_mixed = s_fp64 = None
+        adjoint = adjoint_check(args.adjoint_n, args.adjoint_dirs)
+
     # roofline of the dominant kernel: level-1 FP32 line relaxation (k_line_wp<float,dir,8>),
     # durations from CUDA events around each launch inside the timed solves
     peaks = json.loads(PEAKS.read_text()) if PEAKS.exists() else {}
@@ -466,12 +525,13 @@ def main():
         "iters_mixed": mixed_iters[0], "iters_fp64": fp64_iters[0], "stationary": stationary,
         "wall_ms_per_step": 1e3 * mixed_wall / args.steps,
         "gpu_launches": int(mixed_launch), "clocks": clocks, "e2e": e2e, "roofline": roofline,
-        "cpu_baseline": cpu, "setup_s": setup_s,
+        "cpu_baseline": cpu, "adjoint": adjoint, "setup_s": setup_s,
     }
     if rank == 0:
         print(json.dumps(out))
-    s_mixed.close()
-    s_fp64.close()
+    for sv in (s_mixed, s_fp64):
+        if sv is not None:
+            sv.close()
     if world > 1:
         torch.distributed.destroy_process_group()
 

@@ -132,16 +132,32 @@ class ProjectionOperators:
         IG = sp.identity(nG, format="csc")
         self.gidx_np = gi
         self.gidx = torch.as_tensor(gi, device=self.dev)
-        # ghost elimination X = (I - C_GG)^-1 C_GF: p_G = X p (extend) and the
-        # transpose X^T y_G (extend_T), both as padded-row gathers on the device
-        X = sp.csr_matrix(spla.spsolve((IG - self.C_GG).tocsc(), self.C_GF.tocsc()))
-        X.eliminate_zeros()
-        self.X = X
-        self._gX = self._padded(X)
-        XT = X.T.tocsr()
-        rows = np.nonzero(np.diff(XT.indptr))[0]          # cells that receive ghost cotangents
-        self._xt_rows = torch.as_tensor(rows, device=self.dev)
-        self._gXT = self._padded(XT[rows])
+        # ghost elimination p_G = (I - C_GG)^-1 C_GF p (extend) and its transpose
+        # (extend_T): C_GF and C_GF^T as padded-row gathers on the device and
+        # (I - C_GG)^-1 as a dense matrix there (host sparse LU above DENSE_GHOSTS)
+        self._gCGF = self._padded(self.C_GF)
+        CT = self.C_GF.T.tocsr()
+        rows = np.nonzero(np.diff(CT.indptr))[0]            # stencil cells that receive cotangents
+        self._ct_rows = torch.as_tensor(rows, device=self.dev)
+        self._gCGFT = self._padded(CT[rows])
+        if nG <= self.DENSE_GHOSTS:
+            M = torch.eye(nG, dtype=torch.float64, device=self.dev) - torch.as_tensor(
+                self.C_GG.toarray(), device=self.dev)
+            self._Minv = torch.linalg.inv(M)
+            self._lu = self._luT = None
+        else:
+            self._Minv = None
+            self._lu = spla.splu((IG - self.C_GG).tocsc())
+            self._luT = spla.splu((IG - self.C_GG).T.tocsc())
+
+    DENSE_GHOSTS = 30000
+
+    def _ghost_solve(self, r, transpose):
+        """(I - C_GG)^-1 r, or its transpose."""
+        if self._Minv is not None:
+            return (self._Minv.T if transpose else self._Minv) @ r
+        lu = self._luT if transpose else self._lu
+        return torch.as_tensor(lu.solve(r.cpu().numpy()), device=self.dev)
 
     def _padded(self, S):
         """Sparse rows as (cols, vals) padded to the longest row, for a
@@ -172,7 +188,7 @@ class ProjectionOperators:
         if self.nG == 0:
             return out
         flat = out.permute(2, 1, 0).reshape(-1)
-        flat[self.gidx] = self._gather_mv(self._gX, flat)
+        flat[self.gidx] = self._ghost_solve(self._gather_mv(self._gCGF, flat), False)
         return out
 
     def extend_T(self, y):
@@ -181,9 +197,9 @@ class ProjectionOperators:
         out = as_fortran(y * self.fluid)
         if self.nG == 0:
             return out
-        yg = y.permute(2, 1, 0).reshape(-1)[self.gidx]
+        q = self._ghost_solve(y.permute(2, 1, 0).reshape(-1)[self.gidx], True)
         flat = out.permute(2, 1, 0).reshape(-1)
-        flat[self._xt_rows] += self._gather_mv(self._gXT, yg)
+        flat[self._ct_rows] += self._gather_mv(self._gCGFT, q)
         return out * self.fluid
 
     # ------------------------------------------------- divergence (D F) --
