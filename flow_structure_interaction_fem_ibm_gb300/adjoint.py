@@ -380,14 +380,18 @@ class _DeviceMG:
         return self.p.clone()
 
     def solve(self, f, rtol=1e-12, krylov=30, iters=400):
-        """Full solve A_eff p = f (f consistent); returns p with ghost values."""
-        self.b.copy_(f)
+        """Full solve A_eff p = f (f consistent); returns p with ghost values.
+        The right-hand side is scaled to unit max-norm so that one handle per
+        (rtol, krylov, iters) serves every call (the problem is linear)."""
+        scale = float(f.abs().max())
+        if scale == 0.0:
+            return torch.zeros_like(self.p), 0, 0, 0.0
+        self.b.copy_(f / scale)
         self.p.zero_()
-        restol = rtol * max(float(f.abs().max()), 1e-300)
-        s = self._solver(restol, krylov, iters)
+        s = self._solver(rtol, krylov, iters)
         torch.cuda.synchronize()
         st, it, mr, loc, _ = s.solve_poisson_device(self.p.data_ptr(), self.b.data_ptr())
-        return self.p.clone(), st, it, mr
+        return self.p * scale, st, it, mr * scale
 
     def close(self):
         self.s_one.close()
