@@ -737,7 +737,8 @@ int precondition(Ctx &c, const T *v, T *z)
 
 // Relative reduction one FP32 inner cycle aims for at most; the FP64 residual
 // recomputed at the restart carries the refinement further.
-constexpr double KRYLOV_FP32_INNER_RTOL = 1.0e-5;
+// (FSI_MG_KRYLOV_INNER_RTOL overrides it for measurements.)
+double g_krylov_inner_rtol = 1.0e-5;
 
 // solve_poisson with FGMRES(m) around MG_Solver (outer_krylov = m).  Same
 // discrete system (fluid rows with ghost values from the ghost-row fixed
@@ -804,7 +805,7 @@ int solve_krylov_t(Ctx &c, double *p, const double *b, int *iters, double *maxre
         std::fill(g.begin(), g.end(), 0.0);
         g[0] = beta;
         double target = 0.5 * beta * c.p.restol_Poisson / maxres;
-        if (f32) target = std::max(target, KRYLOV_FP32_INNER_RTOL * beta);
+        if (f32) target = std::max(target, g_krylov_inner_rtol * beta);
         int k = 0;
         for (int j = 0; j < m; ++j) {
             TRY(precondition<T>(c, KV[j], KZ[j]));
@@ -1020,6 +1021,9 @@ int fsi_mg_create(const fsi_mg_params *params, const double *x, const double *y,
     {   // FSI_MG_LINE_KERNEL=thread selects the one-thread-per-line smoother (A/B measurements)
         const char *lk = std::getenv("FSI_MG_LINE_KERNEL");
         set_line_kernel(lk && std::strcmp(lk, "thread") == 0);
+        const char *kr = std::getenv("FSI_MG_KRYLOV_INNER_RTOL");
+        const double v = kr ? std::atof(kr) : 0.0;
+        g_krylov_inner_rtol = (v > 0.0 && v < 1.0) ? v : 1.0e-5;
     }
     auto c = std::make_unique<Ctx>();
     c->p = p;
