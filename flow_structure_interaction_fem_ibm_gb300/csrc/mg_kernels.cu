@@ -4,6 +4,8 @@
 
 #include <algorithm>
 #include <cfloat>
+#include <cstdlib>
+#include <cstring>
 #include <mutex>
 #include <cooperative_groups.h>
 
@@ -1732,6 +1734,8 @@ __global__ void k_probe_coop(int *out)
 // any capture.  A failure only disables the persistent smoother.
 cudaError_t coarsest_probe()
 {
+    const char *off = std::getenv("FSI_MG_COARSEST_KERNEL");   // "off": per-sweep launches (A/B measurements)
+    if (off && std::strcmp(off, "off") == 0) return cudaSuccess;
     int dev = 0, sms = 0, coop = 0;
     if (cudaGetDevice(&dev) != cudaSuccess) return cudaSuccess;
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
