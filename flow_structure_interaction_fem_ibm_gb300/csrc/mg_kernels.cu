@@ -4,8 +4,6 @@
 
 #include <algorithm>
 #include <cfloat>
-#include <cstdlib>
-#include <cstring>
 #include <mutex>
 #include <cooperative_groups.h>
 
@@ -1734,8 +1732,6 @@ __global__ void k_probe_coop(int *out)
 // any capture.  A failure only disables the persistent smoother.
 cudaError_t coarsest_probe()
 {
-    const char *off = std::getenv("FSI_MG_COARSEST_KERNEL");   // "off": per-sweep launches (A/B measurements)
-    if (off && std::strcmp(off, "off") == 0) return cudaSuccess;
     int dev = 0, sms = 0, coop = 0;
     if (cudaGetDevice(&dev) != cudaSuccess) return cudaSuccess;
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
