@@ -104,8 +104,6 @@ struct Ctx {
     float *gco32 = nullptr, *gscr32 = nullptr;
     int *d_iters = nullptr;
     unsigned long long *d_maxd = nullptr;
-    unsigned *d_bar = nullptr;   // barrier words of the persistent coarsest-level smoother
-    int *d_cerr = nullptr;       // set when one of its barrier waits timed out
 
     // reductions
     int nred = 0;
@@ -452,31 +450,6 @@ void itsolv(Ctx &c, Level &L, T *v, const T *r, bool finest, bool homogeneous)
     }
 }
 
-// iters MG_itsolv calls on a coarsest level (FP64, homogeneous boundary values)
-// in one persistent kernel; false when the level does not fit it (the caller
-// then launches the sweeps one by one).
-bool coarsest_smooth(Ctx &c, Level &L, double *v, const double *r, int iters)
-{
-    if (!coarsest_available() || !c.d_bar) return false;
-    CoarsestArgs a;
-    a.nd = c.nd;
-    a.iters = iters;
-    a.bar = c.d_bar;
-    a.err = c.d_cerr;
-    a.short_dir = -1;
-    for (int dir = 0; dir < c.nd; ++dir) {
-        LineArgs<double> &la = a.la[dir];
-        la.v = v; la.r = r; la.fl = L.fl; la.U = c.U64; la.c = coef_of<double>(L); la.d = L.d;
-        la.omega = c.p.omega; la.binv = L.binv64[dir]; la.gam = L.gam64[dir];
-        la.dir_lo = la.dir_hi = 0; la.ppp_lo = la.ppp_hi = 0.0; la.colour = 0; la.wpf = L.wpf[dir];
-        if (L.d.m[dir] - 1 <= 16) a.short_dir = (a.short_dir < 0) ? dir : 99;
-    }
-    if (a.short_dir < 0 || a.short_dir == 99) return false;
-    if (!launch_coarsest(a, c.p.omega == 1.0, c.s)) return false;
-    c.launches += 2;
-    return true;
-}
-
 template <typename T> T *lv_v(Level &L);
 template <> double *lv_v<double>(Level &L) { return L.v64; }
 template <> float *lv_v<float>(Level &L) { return L.v32; }
@@ -547,12 +520,10 @@ void mg_cycle(Ctx &c, int d, T *var, const T *rhs, int n, int WF, int &GMM, bool
             launch_convert_f2d(L.r64, (const float *)rhs, L.d.count(), c.s);
             launch_convert_f2d(L.v64, (const float *)var, L.d.count(), c.s);
             c.launches += 2;
-            if (!coarsest_smooth(c, L, L.v64, L.r64, totIter))
-                for (int it = 0; it < totIter; ++it) itsolv<double>(c, L, L.v64, L.r64, false, true);
+            for (int it = 0; it < totIter; ++it) itsolv<double>(c, L, L.v64, L.r64, false, true);
             launch_convert_d2f((float *)var, L.v64, L.d.count(), c.s);
             c.launches++;
-        } else if (!(std::is_same<T, double>::value && n == nlev && n > 1 && homogeneous &&
-                     coarsest_smooth(c, L, (double *)var, (const double *)rhs, totIter))) {
+        } else {
             for (int it = 0; it < totIter; ++it) itsolv<T>(c, L, var, rhs, n == 1, homogeneous);
         }
     }
@@ -801,7 +772,6 @@ int solve_krylov_t(Ctx &c, double *p, const double *b, int *iters, double *maxre
     subtract_average(c, p);
     CK(cudaMemsetAsync(c.d_iters, 0, sizeof(int), c.s));
     CK(cudaMemsetAsync(c.d_maxd, 0, sizeof(unsigned long long), c.s));
-    CK(cudaMemsetAsync(c.d_cerr, 0, sizeof(int), c.s));
     c.hist.clear();
     int it = 0;
     double maxres = 1.0e10;
@@ -908,10 +878,7 @@ int solve_krylov_t(Ctx &c, double *p, const double *b, int *iters, double *maxre
     unsigned long long h_maxd = 0;
     CK(cudaMemcpyAsync(&h_iters, c.d_iters, sizeof(int), cudaMemcpyDeviceToHost, c.s));
     CK(cudaMemcpyAsync(&h_maxd, c.d_maxd, sizeof(h_maxd), cudaMemcpyDeviceToHost, c.s));
-    int h_cerr = 0;
-    CK(cudaMemcpyAsync(&h_cerr, c.d_cerr, sizeof(int), cudaMemcpyDeviceToHost, c.s));
     CK(cudaStreamSynchronize(c.s));
-    if (h_cerr) return fail(-13, "coarsest-level smoother: a device-wide barrier wait timed out");
     c.ghost_sweeps = h_iters;
     float ms = 0.0f;
     CK(cudaEventElapsedTime(&ms, c.ev0, c.ev1));
@@ -952,7 +919,6 @@ int solve_device(Ctx &c, double *p, const double *b, int *iters, double *maxres_
     }
     CK(cudaMemsetAsync(c.d_iters, 0, sizeof(int), c.s));
     CK(cudaMemsetAsync(c.d_maxd, 0, sizeof(unsigned long long), c.s));
-    CK(cudaMemsetAsync(c.d_cerr, 0, sizeof(int), c.s));
     int iter = 0;
     double maxres = 1.0e10;
     long long maxidx = 0;
@@ -973,10 +939,7 @@ int solve_device(Ctx &c, double *p, const double *b, int *iters, double *maxres_
     unsigned long long h_maxd = 0;
     CK(cudaMemcpyAsync(&h_iters, c.d_iters, sizeof(int), cudaMemcpyDeviceToHost, c.s));
     CK(cudaMemcpyAsync(&h_maxd, c.d_maxd, sizeof(h_maxd), cudaMemcpyDeviceToHost, c.s));
-    int h_cerr = 0;
-    CK(cudaMemcpyAsync(&h_cerr, c.d_cerr, sizeof(int), cudaMemcpyDeviceToHost, c.s));
     CK(cudaStreamSynchronize(c.s));
-    if (h_cerr) return fail(-13, "coarsest-level smoother: a device-wide barrier wait timed out");
     c.ghost_sweeps = h_iters;
     double maxd;
     std::memcpy(&maxd, &h_maxd, sizeof(maxd));
@@ -1125,8 +1088,6 @@ int fsi_mg_create(const fsi_mg_params *params, const double *x, const double *y,
     TRY(c->alloc(&c->result, 1));
     TRY(c->alloc(&c->d_iters, 1));
     TRY(c->alloc(&c->d_maxd, 1));
-    TRY(c->alloc(&c->d_bar, 2));
-    TRY(c->alloc(&c->d_cerr, 1));
     CK(cudaMallocHost(&c->h_result, sizeof(MaxLoc)));
     for (int d = 0; d < 3; ++d) {
         TRY(c->alloc(&c->d_dx[d], N[d] + 2));

@@ -2,7 +2,6 @@
 // reference routine whose arithmetic it performs.
 #include "mg_kernels.cuh"
 
-#include <algorithm>
 #include <cfloat>
 #include <mutex>
 #include <cooperative_groups.h>
@@ -56,12 +55,13 @@ __device__ __forceinline__ long long stride_of(const Dims &d, int axis)
 // substitution with gam, relaxation var = var (1-omega) + omega sol.
 // ---------------------------------------------------------------------------
 template <typename T, int DIR, bool OMEGA1>
-__device__ __forceinline__ void line_thread(const LineArgs<T> &A, long long t)
+__global__ void __launch_bounds__(TPB) k_line(LineArgs<T> A)
 {
     using X = Axes<DIR>;
     const Dims &d = A.d;
     const int nb = d.m[X::b] - 1, nc = d.m[X::c] - 1, L = d.m[X::a] - 1;
     const int hb = (nb + 1) >> 1;
+    long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= (long long)hb * nc) return;
     const int q = 1 + (int)(t / hb);
     const int tp = (int)(t % hb);
@@ -133,12 +133,6 @@ __device__ __forceinline__ void line_thread(const LineArgs<T> &A, long long t)
     }
     if (A.dir_lo) v[base] = A.ppp_lo;
     if (A.dir_hi) v[base + (long long)(L + 1) * sa] = A.ppp_hi;
-}
-
-template <typename T, int DIR, bool OMEGA1>
-__global__ void __launch_bounds__(TPB) k_line(LineArgs<T> A)
-{
-    line_thread<T, DIR, OMEGA1>(A, (long long)blockIdx.x * blockDim.x + threadIdx.x);
 }
 
 // ---------------------------------------------------------------------------
@@ -523,13 +517,12 @@ __global__ void __launch_bounds__(256) k_wpf_setup(FactorArgs<double> A, double 
     Tl[11 * 32 + lane] = (lane == 31) ? 0.0 : cn;
 }
 
-// One chunk (NL lines) of a factored FP64 sweep, by a CTA of 32 x NL threads
-// (uniform over the CTA: it synchronises), with 2 x NL x wp_pitch<S>() doubles
-// of shared memory at sm.
 template <int DIR, int S, int NL, bool OMEGA1>
-__device__ __forceinline__ void fp_chunk(const LineArgs<double> &A, int chunk, double *sm)
+__global__ void __launch_bounds__(32 * NL) k_line_fp(LineArgs<double> A)
 {
     using X = Axes<DIR>;
+    extern __shared__ unsigned char smem_raw[];
+    double *sm = reinterpret_cast<double *>(smem_raw);
     constexpr int RP = wp_pitch<S>();
     double *sa = sm, *sd = sm + NL * RP;
     const Dims &d = A.d;
@@ -539,7 +532,7 @@ __device__ __forceinline__ void fp_chunk(const LineArgs<double> &A, int chunk, d
     const int sa_ = (int)stride_of(d, X::a), sb_ = (int)stride_of(d, X::b), sc_ = (int)stride_of(d, X::c);
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     auto line_pq = [&](int g, int &p, int &q) -> bool {
-        const int t = chunk * NL + g;
+        const int t = (int)blockIdx.x * NL + g;
         if (t >= nlines) return false;
         const int tq = t / hb;
         q = 1 + tq;
@@ -700,87 +693,6 @@ __device__ __forceinline__ void fp_chunk(const LineArgs<double> &A, int chunk, d
             if (i == L && A.dir_hi) A.v[base + (L + 1) * sa_] = A.ppp_hi;
         }
     }
-}
-
-template <int DIR, int S, int NL, bool OMEGA1>
-__global__ void __launch_bounds__(32 * NL) k_line_fp(LineArgs<double> A)
-{
-    extern __shared__ unsigned char smem_raw[];
-    fp_chunk<DIR, S, NL, OMEGA1>(A, (int)blockIdx.x, reinterpret_cast<double *>(smem_raw));
-}
-
-// ---------------------------------------------------------------------------
-// Persistent coarsest-level smoother.  The coarsest level of a semi-coarsening
-// cycle (e.g. 4 x 256 x 256 at 256^3) is smoothed iterCoarsest times in FP64
-// inside the FP32 cycle; as separate launches its 6 sweeps per MG_itsolv are
-// latency-bound (a few hundred lines each).  Here one cooperative grid runs
-// them all, with a bounded device-wide barrier between sweeps.
-// ---------------------------------------------------------------------------
-constexpr int COARSEST_NL = 2;                  // lines per chunk of a long sweep
-constexpr int COARSEST_THREADS = 32 * COARSEST_NL;
-constexpr unsigned COARSEST_SPIN_LIMIT = 1u << 22;
-
-// All CTAs arrive and leave together; returns false once any CTA gave up
-// waiting (then every CTA stops at its next barrier or wait).
-__device__ __forceinline__ bool grid_barrier(unsigned *bar, int *err)
-{
-    __shared__ int s_ok;
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        volatile unsigned *gen = bar + 1;
-        const unsigned g = *gen;
-        __threadfence();
-        int ok = 1;
-        if (atomicAdd(bar, 1u) == gridDim.x - 1) {
-            atomicExch(bar, 0u);
-            __threadfence();
-            atomicAdd(bar + 1, 1u);
-        } else {
-            unsigned spins = 0;
-            while (*gen == g) {
-                if (++spins > COARSEST_SPIN_LIMIT || *(volatile int *)err) { atomicExch(err, 1); ok = 0; break; }
-                __nanosleep(64);
-            }
-        }
-        __threadfence();
-        if (*(volatile int *)err) ok = 0;
-        s_ok = ok;
-    }
-    __syncthreads();
-    return s_ok != 0;
-}
-
-template <int D, int SHORT, int S, bool O1>
-__device__ __forceinline__ void coarsest_sweep(const LineArgs<double> &a, double *sm)
-{
-    using X = Axes<D>;
-    const int nb = a.d.m[X::b] - 1, nc = a.d.m[X::c] - 1;
-    const long long nlines = (long long)((nb + 1) >> 1) * nc;
-    if constexpr (D == SHORT) {
-        const long long stride = (long long)gridDim.x * blockDim.x;
-        for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < nlines; t += stride)
-            line_thread<double, D, O1>(a, t);
-    } else {
-        const int nchunks = (int)((nlines + COARSEST_NL - 1) / COARSEST_NL);
-        for (int ch = blockIdx.x; ch < nchunks; ch += gridDim.x) fp_chunk<D, S, COARSEST_NL, O1>(a, ch, sm);
-    }
-}
-
-template <int SHORT, int S, bool O1>
-__global__ void __launch_bounds__(COARSEST_THREADS) k_coarsest(CoarsestArgs C)
-{
-    extern __shared__ unsigned char smem_raw[];
-    double *sm = reinterpret_cast<double *>(smem_raw);
-    for (int it = 0; it < C.iters; ++it)
-        for (int dir = 0; dir < C.nd; ++dir)
-            for (int col = 0; col < 2; ++col) {
-                LineArgs<double> a = C.la[dir];
-                a.colour = col;
-                if (dir == 0) coarsest_sweep<0, SHORT, S, O1>(a, sm);
-                else if (dir == 1) coarsest_sweep<1, SHORT, S, O1>(a, sm);
-                else coarsest_sweep<2, SHORT, S, O1>(a, sm);
-                if (!grid_barrier(C.bar, C.err)) return;
-            }
 }
 
 // ---------------------------------------------------------------------------
@@ -1694,94 +1606,6 @@ void wpf_setup_dir(const FactorArgs<double> &a, double *tab, int L, long long nl
 
 int wp_S(int L) { return L <= 32 ? 1 : L <= 64 ? 2 : L <= 128 ? 4 : L <= 256 ? 8 : 16; }
 
-// ---- persistent coarsest-level smoother: launch shapes and capture probe ----
-int g_coarsest_blocks = 0;        // co-resident CTAs used by k_coarsest (0: unavailable)
-
-template <int SHORT, int S, bool O1>
-void *coarsest_fn() { return reinterpret_cast<void *>(&k_coarsest<SHORT, S, O1>); }
-
-template <int SHORT, bool O1>
-void *coarsest_fn_s(int S)
-{
-    switch (S) {
-    case 1: return coarsest_fn<SHORT, 1, O1>();
-    case 2: return coarsest_fn<SHORT, 2, O1>();
-    case 4: return coarsest_fn<SHORT, 4, O1>();
-    case 8: return coarsest_fn<SHORT, 8, O1>();
-    case 16: return coarsest_fn<SHORT, 16, O1>();
-    }
-    return nullptr;
-}
-
-void *coarsest_kernel(int short_dir, int S, bool o1)
-{
-    if (short_dir == 0) return o1 ? coarsest_fn_s<0, true>(S) : coarsest_fn_s<0, false>(S);
-    if (short_dir == 1) return o1 ? coarsest_fn_s<1, true>(S) : coarsest_fn_s<1, false>(S);
-    return o1 ? coarsest_fn_s<2, true>(S) : coarsest_fn_s<2, false>(S);
-}
-
-size_t coarsest_smem(int S) { return 2 * (size_t)COARSEST_NL * (32 * (S + 1) + 4) * sizeof(double); }
-
-__global__ void k_probe_coop(int *out)
-{
-    if (blockIdx.x == 0 && threadIdx.x == 0) *out = 1;
-}
-
-// Whether a cooperative launch can be captured into a CUDA graph and run here,
-// and how many CTAs of k_coarsest are co-resident; once per process, outside
-// any capture.  A failure only disables the persistent smoother.
-cudaError_t coarsest_probe()
-{
-    int dev = 0, sms = 0, coop = 0;
-    if (cudaGetDevice(&dev) != cudaSuccess) return cudaSuccess;
-    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev);
-    if (!coop || sms <= 0) return cudaSuccess;
-    int per_sm = 1 << 30;
-    for (int sd = 0; sd < 3; ++sd)
-        for (int S : {1, 2, 4, 8, 16})
-            for (int o1 = 0; o1 < 2; ++o1) {
-                void *fn = coarsest_kernel(sd, S, o1 != 0);
-                const int bytes = (int)coarsest_smem(S);
-                if (bytes > 48 * 1024)
-                    cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
-                int nb = 0;
-                if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, fn, COARSEST_THREADS, bytes) != cudaSuccess)
-                    nb = 0;
-                per_sm = std::min(per_sm, nb);
-            }
-    (void)cudaGetLastError();
-    if (per_sm < 1) return cudaSuccess;
-    cudaStream_t st = nullptr;
-    int *d_out = nullptr;
-    cudaGraph_t g = nullptr;
-    cudaGraphExec_t ge = nullptr;
-    bool ok = cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking) == cudaSuccess &&
-              cudaMalloc(&d_out, sizeof(int)) == cudaSuccess &&
-              cudaMemsetAsync(d_out, 0, sizeof(int), st) == cudaSuccess &&
-              cudaStreamSynchronize(st) == cudaSuccess;
-    if (ok) {
-        void *args[] = {&d_out};
-        ok = cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal) == cudaSuccess;
-        if (ok) {
-            const cudaError_t le = cudaLaunchCooperativeKernel((void *)k_probe_coop, dim3(2), dim3(32), args, 0, st);
-            const cudaError_t ee = cudaStreamEndCapture(st, &g);
-            ok = le == cudaSuccess && ee == cudaSuccess && g != nullptr;
-        }
-        ok = ok && cudaGraphInstantiate(&ge, g, 0) == cudaSuccess && cudaGraphLaunch(ge, st) == cudaSuccess &&
-             cudaStreamSynchronize(st) == cudaSuccess;
-        int h = 0;
-        ok = ok && cudaMemcpy(&h, d_out, sizeof(int), cudaMemcpyDeviceToHost) == cudaSuccess && h == 1;
-    }
-    if (ge) cudaGraphExecDestroy(ge);
-    if (g) cudaGraphDestroy(g);
-    if (d_out) cudaFree(d_out);
-    if (st) cudaStreamDestroy(st);
-    (void)cudaGetLastError();
-    g_coarsest_blocks = ok ? sms * std::min(per_sm, 2) : 0;
-    return cudaSuccess;
-}
-
 bool g_line_thread_per_line = false;   // selects the sequential-Thomas kernel (kept for lines > 512 cells)
 
 template <typename T>
@@ -2055,44 +1879,10 @@ cudaError_t init_kernels()
     if ((e = wp_attr_dir<double, 2>()) != cudaSuccess) return e;
     if ((e = fp_attr_dir<0>()) != cudaSuccess) return e;
     if ((e = fp_attr_dir<1>()) != cudaSuccess) return e;
-    if ((e = fp_attr_dir<2>()) != cudaSuccess) return e;
-    static bool probed = false;
-    if (!probed) {
-        probed = true;
-        if ((e = coarsest_probe()) != cudaSuccess) return e;
-    }
-    return cudaSuccess;
+    return fp_attr_dir<2>();
 }
 
 void set_line_kernel(int thread_per_line) { g_line_thread_per_line = thread_per_line != 0; }
-
-bool coarsest_available() { return g_coarsest_blocks > 0; }
-
-bool launch_coarsest(const CoarsestArgs &a, bool omega_one, cudaStream_t s)
-{
-    if (g_coarsest_blocks <= 0 || a.short_dir < 0 || a.short_dir >= a.nd) return false;
-    static const int ax[3] = {0, 1, 2};
-    int S = 0;
-    for (int d = 0; d < a.nd; ++d) {
-        const int L = a.la[d].d.m[ax[d]] - 1;
-        if (d == a.short_dir) {
-            if (L > 16) return false;
-            continue;
-        }
-        if (L <= 16 || L > 512 || !a.la[d].wpf) return false;
-        const int Sd = wp_S(L);
-        if (S && Sd != S) return false;      // both long directions share one S
-        S = Sd;
-    }
-    if (!S) return false;
-    void *fn = coarsest_kernel(a.short_dir, S, omega_one);
-    if (!fn) return false;
-    CoarsestArgs c = a;
-    void *args[] = {&c};
-    if (cudaMemsetAsync(a.bar, 0, 2 * sizeof(unsigned), s) != cudaSuccess) return false;
-    return cudaLaunchCooperativeKernel(fn, dim3(g_coarsest_blocks), dim3(COARSEST_THREADS), args,
-                                       coarsest_smem(S), s) == cudaSuccess;
-}
 
 // explicit instantiations
 template void launch_line<double>(int, const LineArgs<double> &, bool, cudaStream_t);

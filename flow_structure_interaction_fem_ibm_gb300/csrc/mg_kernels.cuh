@@ -85,23 +85,6 @@ struct GhostArgs {
                              // -(m + 2) for ghost cell number m, -1 for the uNormal term
 };
 
-// Coarsest-level smoothing (iterCoarsest MG_itsolv calls) in one persistent
-// cooperative FP64 kernel: la[d] are the line arguments of direction d (colour
-// set per sweep), the short direction (lines of at most 16 cells) is relaxed
-// one thread per line, the two long ones by the factored partition solver;
-// sweeps are separated by device-wide barriers whose waits are bounded (on a
-// timeout *err is set and the kernel stops).  bar (2 unsigned) must be zero at
-// launch.  Returns false (nothing launched) when the level does not fit the
-// kernel's shapes or cooperative launches cannot be captured here.
-struct CoarsestArgs {
-    LineArgs<double> la[3];
-    int nd, iters, short_dir;
-    unsigned *bar;
-    int *err;
-};
-bool launch_coarsest(const CoarsestArgs &a, bool omega_one, cudaStream_t s);
-bool coarsest_available();
-
 // one-time kernel attributes (call before the first launch, outside stream capture)
 cudaError_t init_kernels();
 // 0: warp-per-line partition solver (default, lines up to 512 cells), 1: one thread per line
