@@ -27,6 +27,8 @@ def cases():
         # long lines: the warp-partition smoother with 2, 4 and 8 rows per lane
         ("box2d_256", lambda: P.box2d(256, seed=9)),
         ("sphere_48x80x160", lambda: P.sphere((48, 80, 160), seed=5, stretch=1.5)),
+        # cubic: coarsest levels with two long directions of equal length (S = 2)
+        ("sphere48_tanh", lambda: P.sphere(48, seed=6, stretch=1.5)),
     ]
 
 
