@@ -135,6 +135,98 @@ __global__ void __launch_bounds__(TPB) k_line(LineArgs<T> A)
     if (A.dir_hi) v[base + (long long)(L + 1) * sa] = A.ppp_hi;
 }
 
+// Short lines (L <= LM <= 16 cells), one thread per line with the line in
+// registers: every row's loads are issued before the forward elimination
+// (no store comes between them), the eliminated values stay in registers
+// for the back substitution (no scratch array), and the loops are unrolled
+// over the compile-time bound LM with the runtime length as a predicate.
+// Same arithmetic as k_line.
+template <typename T, int DIR, int LM, bool OMEGA1>
+__global__ void __launch_bounds__(TPB) k_line_short(LineArgs<T> A)
+{
+    using X = Axes<DIR>;
+    const Dims &d = A.d;
+    const int nb = d.m[X::b] - 1, nc = d.m[X::c] - 1, L = d.m[X::a] - 1;
+    const int hb = (nb + 1) >> 1;
+    const int t = (int)(blockIdx.x * blockDim.x + threadIdx.x);
+    if (t >= hb * nc) return;
+    const int q = 1 + t / hb;
+    const int p0 = (((1 + q) & 1) == A.colour) ? 1 : 2;
+    const int p = p0 + 2 * (t - (q - 1) * hb);
+    if (p > nb) return;
+    const int sa = (int)stride_of(d, X::a), sb = (int)stride_of(d, X::b), sc = (int)stride_of(d, X::c);
+    const int base = p * sb + q * sc;
+    const T cmb = A.c.cm[X::b][p], cpb = A.c.cp[X::b][p];
+    const T cmc = A.c.cm[X::c][q], cpc = A.c.cp[X::c][q];
+    const bool zmb = is_zero(cmb), zpb = is_zero(cpb), zmc = is_zero(cmc), zpc = is_zero(cpc);
+    const T *__restrict__ cma = A.c.cm[X::a];
+    const T *__restrict__ cpa = A.c.cp[X::a];
+    T *__restrict__ v = A.v;
+    const T *__restrict__ r = A.r;
+    const uint8_t *__restrict__ fl = A.fl;
+    T u[LM], gn[LM];
+    T uprev = T(0);
+#pragma unroll
+    for (int k = 0; k < LM; ++k) {
+        const int i = k + 1;
+        u[k] = T(0);
+        gn[k] = T(0);
+        if (i <= L) {
+            const int o = base + i * sa;
+            const uint8_t f = fl[o];
+            const bool fluid = !(f & FB_IB);
+            const T cma_i = cma[i], cpa_i = cpa[i];
+            const T ama = (f & fb_minus(X::a)) ? T(0) : cma_i;
+            const T apa = (f & fb_plus(X::a)) ? T(0) : cpa_i;
+            const T amb = (f & fb_minus(X::b)) ? T(0) : cmb;
+            const T apb = (f & fb_plus(X::b)) ? T(0) : cpb;
+            const T amc = (f & fb_minus(X::c)) ? T(0) : cmc;
+            const T apc = (f & fb_plus(X::c)) ? T(0) : cpc;
+            const bool allzero = ((f & fb_minus(X::a)) || is_zero(cma_i)) && ((f & fb_plus(X::a)) || is_zero(cpa_i)) &&
+                                 ((f & fb_minus(X::b)) || zmb) && ((f & fb_plus(X::b)) || zpb) &&
+                                 ((f & fb_minus(X::c)) || zmc) && ((f & fb_plus(X::c)) || zpc);
+            const bool normal = fluid && !allzero;
+            T rhs;
+            if (normal) {
+                T s = r[o];
+                if (X::c_first) {
+                    s = s - v[o - sc] * amc;
+                    s = s - v[o + sc] * apc;
+                    s = s - v[o - sb] * amb;
+                    s = s - v[o + sb] * apb;
+                } else {
+                    s = s - v[o - sb] * amb;
+                    s = s - v[o + sb] * apb;
+                    s = s - v[o - sc] * amc;
+                    s = s - v[o + sc] * apc;
+                }
+                rhs = s;
+            } else {
+                rhs = ((f & FB_GM) || fluid) ? v[o] : T(0);
+            }
+            const T aa = normal ? ama : T(0);
+            if (i == 1 && A.dir_lo) rhs = rhs - A.ppp_lo * aa;
+            if (i == L && A.dir_hi) rhs = rhs - A.ppp_hi * (normal ? apa : T(0));
+            gn[k] = A.gam[o];
+            u[k] = (rhs - aa * uprev) * A.binv[o];
+            uprev = u[k];
+        }
+    }
+    T un = T(0);
+#pragma unroll
+    for (int k = LM - 1; k >= 0; --k) {
+        const int i = k + 1;
+        if (i <= L) {
+            const int o = base + i * sa;
+            const T x = (i == L) ? u[k] : u[k] - gn[(k + 1 < LM) ? k + 1 : k] * un;
+            v[o] = OMEGA1 ? x : v[o] * (T(1) - A.omega) + A.omega * x;
+            un = x;
+        }
+    }
+    if (A.dir_lo) v[base] = A.ppp_lo;
+    if (A.dir_hi) v[base + (L + 1) * sa] = A.ppp_hi;
+}
+
 // ---------------------------------------------------------------------------
 // Red-black line relaxation, warp-per-line partition solver (same arithmetic
 // role as k_line: IBM/CORE_MG.F90:1883-2270 with the TDMA of
@@ -1628,6 +1720,18 @@ void launch_line(int dir, const LineArgs<T> &a, bool omega_one, cudaStream_t s)
         if (ok) return;
     }
     const int g = nblk(n);
+    if (!g_line_thread_per_line && L <= 16) {
+#define S_(D, LM, O) k_line_short<T, D, LM, O><<<g, TPB, 0, s>>>(a)
+#define SD_(LM, O) do { if (dir == 0) S_(0, LM, O); else if (dir == 1) S_(1, LM, O); else S_(2, LM, O); } while (0)
+        if (omega_one) {
+            if (L <= 4) SD_(4, true); else if (L <= 8) SD_(8, true); else SD_(16, true);
+        } else {
+            if (L <= 4) SD_(4, false); else if (L <= 8) SD_(8, false); else SD_(16, false);
+        }
+#undef SD_
+#undef S_
+        return;
+    }
 #define L_(D, O) k_line<T, D, O><<<g, TPB, 0, s>>>(a)
     if (omega_one) {
         if (dir == 0) L_(0, true); else if (dir == 1) L_(1, true); else L_(2, true);
