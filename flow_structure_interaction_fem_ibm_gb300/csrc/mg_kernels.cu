@@ -325,7 +325,7 @@ __global__ void __launch_bounds__(256) k_line_wp(LineArgs<T> A)
         const T cmc = A.c.cm[X::c][qs], cpc = A.c.cp[X::c][qs];
         const bool zmb = is_zero(cmb), zpb = is_zero(cpb), zmc = is_zero(cmc), zpc = is_zero(cpc);
         struct RowIn { uint8_t f; T r, nb0, nb1, nb2, nb3, vo; };
-        constexpr int GRP = (DIR == 0) ? ((S < 4) ? S : 4) : ((S < 8) ? S : 8);   // y/z: more rows in flight
+        constexpr int GRP = (S < 4) ? S : 4;
 #pragma unroll
         for (int q0 = 0; q0 < S; q0 += GRP) {
             RowIn in[GRP];
