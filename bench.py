@@ -54,6 +54,9 @@ def parse():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--krylov", type=int, default=30, help="FGMRES restart length around MG_Solver (0: stationary)")
     ap.add_argument("--no-adjoint", action="store_true")
+    ap.add_argument("--no-steps", action="store_true", help="skip the face_vel/correct_vel/update_pressure timing")
+    ap.add_argument("--steps-only", action="store_true",
+                    help="only the face_vel/correct_vel/update_pressure timing on the sphere grid (profiling)")
     ap.add_argument("--adjoint-n", type=int, default=96)
     ap.add_argument("--adjoint-dirs", type=int, default=200)
     ap.add_argument("--profile", action="store_true",
@@ -312,6 +315,51 @@ def adjoint_check(n, ndir, h=1e-6):
             "timing": "wall clock with the GPU synchronised, median of 3"}
 
 
+def projection_steps(solver, pr, peak, reps=20):
+    """The fractional-step routines either side of the solve on device arrays of
+    the bench grid (face_vel + rhs_poisson, correct_vel, update_pressure; both
+    frac_step_type branches): per kernel the device time of a replayed launch
+    (CUDA events on the library's stream, fsi_mg_time_kernel 6/7/8), its
+    algorithmic bytes and the fraction of the measured HBM bandwidth, and the
+    wall time of one synchronous C-ABI call."""
+    import torch
+    rng = torch.Generator(device="cuda").manual_seed(17)
+    sh = pr.shape[::-1]
+    r = lambda: torch.randn(sh, dtype=torch.float64, device="cuda", generator=rng)
+    u, v, w, p, pp = r(), r(), r(), r(), r()
+    faces = [torch.zeros(sh, dtype=torch.float64, device="cuda") for _ in range(3)]
+    nlu0 = torch.zeros(sh, dtype=torch.float64, device="cuda")
+    fp = [t.data_ptr() for t in faces]
+    out = {}
+    for frac, tag in ((0, "no_van_kan"), (1, "van_kan")):
+        calls = {
+            "face_vel_rhs": lambda: solver.face_vel_rhs(1e-3, u.data_ptr(), v.data_ptr(), w.data_ptr(), *fp,
+                                                        nlu0.data_ptr(), frac_step_type=frac, d_p=p.data_ptr()),
+            "correct_vel": lambda: solver.correct_vel(1e-3, pp.data_ptr(), u.data_ptr(), v.data_ptr(),
+                                                      w.data_ptr(), *fp),
+            "update_pressure": lambda: solver.update_pressure(pp.data_ptr(), p.data_ptr(), frac),
+        }
+        res = {}
+        for which, (name, call) in zip((6, 7, 8), calls.items()):
+            if frac == 1 and name == "correct_vel":
+                continue   # correct_vel has no frac_step_type branch
+            call()
+            t0 = time.perf_counter()
+            for _ in range(5):
+                call()
+            wall_us = (time.perf_counter() - t0) / 5 * 1e6
+            ms, nb = solver.time_kernel(which, 0, reps)
+            gbs = nb / (ms * 1e-3) / 1e9
+            res[name] = {"device_us": 1e3 * ms, "alg_bytes": nb, "achieved_gbs": gbs, "frac": gbs / peak,
+                         "call_wall_us": wall_us}
+        out[tag] = res
+    out["note"] = ("device_us: the routine's kernels (face_vel_rhs: shell zeroing, [uTilde], faces+divergence, "
+                   "sum) replayed 20x; alg_bytes: FP64 fields read/written once per interior cell, no bc arrays; "
+                   "update_pressure without its ghost-cell rows")
+    del u, v, w, p, pp, faces, nlu0
+    return out
+
+
 def cpu_iteration_time(seed, sample_n=128):
     oracle_iteration_time(sample_n, seed)   # builds the oracle (not timed)
     return oracle_iteration_time(sample_n, seed), sample_n
@@ -343,6 +391,16 @@ def main():
         p = np.zeros(pr.shape, order="F")
         s.solve_poisson(p, pr.nlu0)
         print(json.dumps({"profile": "krylov", "stats": s.stats()}))
+        s.close()
+        return
+
+    if args.steps_only:
+        from flow_structure_interaction_fem_ibm_gb300 import problem as P
+        pr = P.sphere(args.n, seed=args.seed, stretch=1.5)
+        s = PoissonSolver(pr.params, pr.x, pr.y, pr.z).set_boundary(pr.geom)
+        peaks = json.loads(PEAKS.read_text()) if PEAKS.exists() else {}
+        print(json.dumps({"profile": "projection_steps", "grid": args.n,
+                          "projection_steps": projection_steps(s, pr, peaks.get("hbm_gbs", 6800.0))}))
         s.close()
         return
 
@@ -484,6 +542,10 @@ def main():
         e2e = {"value": world * k / tot, "unit": "solves/s", "h2d_bytes_per_step": 2 * nbytes,
                "d2h_bytes_per_step": nbytes}
 
+    peaks = json.loads(PEAKS.read_text()) if PEAKS.exists() else {}
+    peak = peaks.get("hbm_gbs", 6800.0)
+    steps_ops = projection_steps(s_mixed, pr, peak) if not args.no_steps else None
+
     adjoint = None
     if rank == 0 and not args.no_adjoint:
         s_mixed.close()
@@ -493,8 +555,6 @@ def main():
 
     # roofline of the dominant kernel: level-1 FP32 line relaxation (k_line_wp<float,dir,8>),
     # durations from CUDA events around each launch inside the timed solves
-    peaks = json.loads(PEAKS.read_text()) if PEAKS.exists() else {}
-    peak = peaks.get("hbm_gbs", 6800.0)
     avg_ms = lt["ms"] / max(lt["launches"], 1)
     achieved = lt["alg_bytes"] / (avg_ms * 1e-3) / 1e9
     traffic = profile_traffic(args.n)
@@ -532,7 +592,7 @@ def main():
         "iters_mixed": mixed_iters[0], "iters_fp64": fp64_iters[0], "stationary": stationary,
         "wall_ms_per_step": 1e3 * mixed_wall / args.steps,
         "gpu_launches": int(mixed_launch), "clocks": clocks, "e2e": e2e, "roofline": roofline,
-        "cpu_baseline": cpu, "adjoint": adjoint, "setup_s": setup_s,
+        "cpu_baseline": cpu, "adjoint": adjoint, "projection_steps": steps_ops, "setup_s": setup_s,
     }
     if rank == 0:
         print(json.dumps(out))

@@ -46,6 +46,9 @@ SOLVER_SYMBOLS = {
     "fsi_mg_subtract_average_noalloc": [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
                                         ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int,
                                         ctypes.c_void_p],
+    "fsi_mg_face_vel_rhs": [ctypes.c_void_p, ctypes.c_int, ctypes.c_double] + [ctypes.c_void_p] * 11 + [c_double_p],
+    "fsi_mg_correct_vel": [ctypes.c_void_p, ctypes.c_double] + [ctypes.c_void_p] * 10,
+    "fsi_mg_update_pressure": [ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p],
     "fsi_mg_last_error": [],
     "fsi_mg_destroy": [ctypes.c_void_p],
 }

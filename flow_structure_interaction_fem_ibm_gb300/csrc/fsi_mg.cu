@@ -117,6 +117,13 @@ struct Ctx {
     int side_raw[6] = {1, 1, 1, 1, 1, 1};
     int sign[6] = {1, 1, 1, 1, 1, 1};
     double *d_dx[3] = {}, *d_dxinv[3] = {}, *d_dxcinv[3] = {};
+    double *d_fx[3] = {};   // face interpolation weights fx(1:n) (IBM/CORE_GRID.F90:163-175)
+    double *vtilde = nullptr;   // uTilde, vTilde, wTilde of the VAN_KAN face_vel (allocated on first use)
+    // arguments of the last step calls, replayed by fsi_mg_time_kernel (which 6, 7, 8)
+    StepArgs last_fv{}, last_cv{};
+    bool have_fv = false, have_cv = false, have_up = false, last_fv_vk = false, last_up_vk = false;
+    double *last_up_p = nullptr;
+    const double *last_up_pp = nullptr;
 
     uint8_t *fresh = nullptr;   // fresh_cell (level-1 layout) of a moving body
     bool fresh_on = false;
@@ -1096,6 +1103,12 @@ int fsi_mg_create(const fsi_mg_params *params, const double *x, const double *y,
         CK(cudaMemcpyAsync(c->d_dx[d], c->dx[d].data(), (N[d] + 2) * 8, cudaMemcpyHostToDevice, c->s));
         CK(cudaMemcpyAsync(c->d_dxinv[d], c->dxinv[d].data(), (N[d] + 2) * 8, cudaMemcpyHostToDevice, c->s));
         CK(cudaMemcpyAsync(c->d_dxcinv[d], c->dxcinv[d].data(), (N[d] + 2) * 8, cudaMemcpyHostToDevice, c->s));
+        std::vector<double> fx(N[d] + 2, 0.0);
+        for (int i = 1; i <= N[d]; ++i)
+            fx[i] = (c->x[d][i] - c->xc[d][i - 1]) / (c->xc[d][i] - c->xc[d][i - 1]);
+        TRY(c->alloc(&c->d_fx[d], N[d] + 2));
+        CK(cudaMemcpyAsync(c->d_fx[d], fx.data(), (N[d] + 2) * 8, cudaMemcpyHostToDevice, c->s));
+        CK(cudaStreamSynchronize(c->s));
     }
     c->npgrad = 2 * (size_t)(p.ny + 2) * (p.nz + 2) + 2 * (size_t)(p.nx + 2) * (p.nz + 2) +
                 2 * (size_t)(p.nx + 2) * (p.ny + 2);
@@ -1450,6 +1463,108 @@ int fsi_mg_correct_pressure(void *handle, double *pPrime, double *nlw0_out)
     return 0;
 }
 
+// ---------------------------------------------------------------------------
+// Fractional-step operations either side of the solve, on device arrays.
+// ---------------------------------------------------------------------------
+static int step_ready(Ctx &c)
+{
+    if (!c.geometry) return fail(-2, "fsi_mg_set_geometry has not been called");
+    for (int q = 0; q < 6; ++q)
+        if (c.side_raw[q] == -1)
+            return fail(-1, "face_vel/correct_vel/update_pressure need Neumann pressure sides (the reference "
+                            "flags Dirichlet sides with -1 in iup/ium, which these kernels do not carry)");
+    return 0;
+}
+
+static StepArgs step_args(Ctx &c, double dt)
+{
+    StepArgs a{};
+    a.fl = c.L1.fl;
+    a.d = c.L1.d;
+    a.dt = dt;
+    for (int d = 0; d < 3; ++d) {
+        a.fx[d] = c.d_fx[d]; a.dxinv[d] = c.d_dxinv[d]; a.dxcinv[d] = c.d_dxcinv[d]; a.dx[d] = c.d_dx[d];
+    }
+    return a;
+}
+
+int fsi_mg_face_vel_rhs(void *handle, int frac_step_type, double dt, const double *d_u, const double *d_v,
+                        const double *d_w, const double *d_p, const double *d_bcxu, const double *d_bcyv,
+                        const double *d_bczw, double *d_face_u, double *d_face_v, double *d_face_w, double *d_nlu0,
+                        double *sum)
+{
+    if (!handle || !d_u || !d_v || !d_w || !d_face_u || !d_face_v || !d_face_w || !d_nlu0)
+        return fail(-1, "null argument");
+    if (frac_step_type != 0 && frac_step_type != 1) return fail(-1, "frac_step_type must be 0 (NO_VAN_KAN) or 1 (VAN_KAN)");
+    if (frac_step_type == 1 && !d_p) return fail(-1, "VAN_KAN needs the current pressure p");
+    if (!(dt > 0.0)) return fail(-1, "dt must be positive");
+    Ctx &c = *(Ctx *)handle;
+    TRY(step_ready(c));
+    const long long n = c.L1.d.sxy * (c.nz + 2);   // full (0:nx+1,0:ny+1,0:nz+1) arrays
+    StepArgs a = step_args(c, dt);
+    const double *vel[3] = {d_u, d_v, d_w};
+    const double *bc[3] = {d_bcxu, d_bcyv, d_bczw};
+    double *face[3] = {d_face_u, d_face_v, d_face_w};
+    // (zeroed by alloc; outside the interior uTilde stays zero, where the
+    // reference keeps whatever its module array held: those values reach only
+    // flagged faces, with weight zero, and the open z faces of a 2D grid)
+    if (frac_step_type == 1 && !c.vtilde) TRY(c.alloc(&c.vtilde, (size_t)(3 * n)));
+    for (int d = 0; d < 3; ++d) {
+        a.vel[d] = vel[d]; a.bc[d] = bc[d]; a.face[d] = face[d];
+        a.velo[d] = (frac_step_type == 1) ? c.vtilde + d * n : nullptr;
+    }
+    a.nlu0 = d_nlu0;
+    a.p = d_p;
+    launch_face_vel_rhs(a, frac_step_type == 1, (double *)c.partials, c.nred, (double *)c.result, c.s);
+    c.last_fv = a; c.last_fv_vk = (frac_step_type == 1); c.have_fv = true;
+    c.launches += (frac_step_type == 1) ? 4 : 3;
+    CK(cudaMemcpyAsync(c.h_result, c.result, sizeof(double), cudaMemcpyDeviceToHost, c.s));
+    CK(cudaStreamSynchronize(c.s));
+    if (sum) *sum = *(const double *)c.h_result;
+    return 0;
+}
+
+int fsi_mg_correct_vel(void *handle, double dt, const double *d_pPrime, double *d_u, double *d_v, double *d_w,
+                       const double *d_bcxu, const double *d_bcyv, const double *d_bczw, double *d_face_u,
+                       double *d_face_v, double *d_face_w)
+{
+    if (!handle || !d_pPrime || !d_u || !d_v || !d_w || !d_face_u || !d_face_v || !d_face_w)
+        return fail(-1, "null argument");
+    if (!(dt > 0.0)) return fail(-1, "dt must be positive");
+    Ctx &c = *(Ctx *)handle;
+    TRY(step_ready(c));
+    StepArgs a = step_args(c, dt);
+    double *vel[3] = {d_u, d_v, d_w};
+    const double *bc[3] = {d_bcxu, d_bcyv, d_bczw};
+    double *face[3] = {d_face_u, d_face_v, d_face_w};
+    for (int d = 0; d < 3; ++d) { a.vel[d] = vel[d]; a.velo[d] = vel[d]; a.bc[d] = bc[d]; a.face[d] = face[d]; }
+    a.p = d_pPrime;
+    launch_correct_vel(a, c.s);
+    c.last_cv = a; c.have_cv = true;
+    c.launches++;
+    CK(cudaStreamSynchronize(c.s));
+    return 0;
+}
+
+int fsi_mg_update_pressure(void *handle, int frac_step_type, const double *d_pPrime, double *d_p)
+{
+    if (!handle || !d_pPrime || !d_p) return fail(-1, "null argument");
+    if (frac_step_type != 0 && frac_step_type != 1) return fail(-1, "frac_step_type must be 0 (NO_VAN_KAN) or 1 (VAN_KAN)");
+    Ctx &c = *(Ctx *)handle;
+    TRY(step_ready(c));
+    launch_update_pressure(d_p, d_pPrime, c.L1.d.sxy * (c.nz + 2), frac_step_type == 1, c.s);
+    c.last_up_p = d_p; c.last_up_pp = d_pPrime; c.last_up_vk = (frac_step_type == 1); c.have_up = true;
+    c.launches++;
+    if (c.p.boundary_formulation == GCM_METHOD && c.nGhost > 0) {
+        GhostArgs g{c.nGhost, c.gidx, c.sidx, c.gsg};
+        launch_ghost_rows<double>(d_p, g, c.gco64, c.gscr64, c.p.iterMax_ad, c.p.restol_ad, 0.0, c.d_iters, c.d_maxd,
+                                  c.s);
+        c.launches++;
+    }
+    CK(cudaStreamSynchronize(c.s));
+    return 0;
+}
+
 int fsi_mg_get_pgrad(void *handle, double *pgrad)
 {
     if (!handle || !pgrad) return fail(-1, "null argument");
@@ -1633,8 +1748,16 @@ int fsi_mg_time_kernel(void *handle, int which, int precision, int reps, double 
             if (f32) go(c.e32, 0.0f); else go(p, 0.0);
         } else if (which == 5) {
             calc_residual(c, p, b, f32 ? c.r32 : nullptr);
+        } else if (which == 6 && c.have_fv) {
+            launch_face_vel_rhs(c.last_fv, c.last_fv_vk, (double *)c.partials, c.nred, (double *)c.result, c.s);
+        } else if (which == 7 && c.have_cv) {
+            launch_correct_vel(c.last_cv, c.s);
+        } else if (which == 8 && c.have_up) {
+            launch_update_pressure(c.last_up_p, c.last_up_pp, c.L1.d.sxy * (c.nz + 2), c.last_up_vk, c.s);
         }
     };
+    if ((which == 6 && !c.have_fv) || (which == 7 && !c.have_cv) || (which == 8 && !c.have_up))
+        return fail(-1, "time_kernel 6/7/8 replay the last face_vel_rhs/correct_vel/update_pressure call; make one first");
     once();   // warm-up
     CK(cudaEventRecord(c.ev0, c.s));
     for (int r = 0; r < reps; ++r) once();
@@ -1655,6 +1778,19 @@ int fsi_mg_time_kernel(void *handle, int which, int precision, int reps, double 
         else if (which == 3) bpc = eb + eb + 1.0 + 0.5 * eb;
         else if (which == 4) bpc = 0.5 * eb + 1.0 + eb + eb;
         else if (which == 5) bpc = 8.0 + 8.0 + 1.0 + (f32 ? 4.0 : 0.0);
+        // step routines (FP64): face_vel_rhs reads u, v, w (+ p with VAN_KAN) and the flags
+        // and writes three faces and nlu0; correct_vel reads pPrime and the flags, updates
+        // u, v, w and three faces; update_pressure reads pPrime (+ p) and writes p; each
+        // non-null bc array adds a read
+        else if (which == 6) {
+            bpc = 24.0 + 1.0 + 24.0 + 8.0 + (c.last_fv_vk ? 8.0 : 0.0);
+            for (int d = 0; d < 3; ++d) bpc += c.last_fv.bc[d] ? 8.0 : 0.0;
+        } else if (which == 7) {
+            bpc = 8.0 + 1.0 + 48.0 + 48.0;
+            for (int d = 0; d < 3; ++d) bpc += c.last_cv.bc[d] ? 8.0 : 0.0;
+        } else if (which == 8) {
+            bpc = 16.0 + (c.last_up_vk ? 8.0 : 0.0);
+        }
         *alg_bytes = bpc * cells;
     }
     return 0;

@@ -1274,6 +1274,186 @@ __global__ void __launch_bounds__(TPB) k_fresh_cells(double *p, const uint8_t *f
     p[o] = sum / (double)cnt;
 }
 
+// ---------------------------------------------------------------------------
+// Fractional-step operations either side of the pressure solve.  Face index f
+// of axis a is stored at the cell it is the minus face of; face n+1 sits in
+// the plus-side boundary layer.  Every face is read and written by one thread.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ double bc_at(const double *bc, long long o) { return bc ? bc[o] : 0.0; }
+__device__ __forceinline__ double fbit(uint8_t f, uint8_t bit) { return (f & bit) ? 1.0 : 0.0; }
+
+// face interpolation of face_vel (IBM/CORE_FRAC_STEP_ROUTINES.F90:80-109): the
+// reference writes face f from cell f-1 (plus side) and then from cell f
+// (minus side), so face f keeps cell f's minus expression and face n+1 cell
+// n's plus expression.
+__device__ __forceinline__ double face_interp_minus(const StepArgs &A, const double *U, int a, int i, long long o,
+                                                    long long s, uint8_t f)
+{
+    const double fx = A.fx[a][i], m = fbit(f, fb_minus(a));
+    return (fx * U[o] + (1.0 - fx) * U[o - s]) * (1.0 - m) + bc_at(A.bc[a], o) * m;
+}
+__device__ __forceinline__ double face_interp_last(const StepArgs &A, const double *U, int a, int n, long long o,
+                                                   long long s, uint8_t f)
+{
+    const double fx = A.fx[a][n + 1], m = fbit(f, fb_plus(a));
+    return (fx * U[o + s] + (1.0 - fx) * U[o]) * (1.0 - m) + bc_at(A.bc[a], o) * m;
+}
+// face pressure correction (IBM/CORE_FRAC_STEP_ROUTINES.F90:381-399 and the
+// VAN_KAN branch of face_vel, :111-129): face1/face2 from the old faces, then
+// the plus mask of cell f-1 and the minus mask of cell f, in that order.
+__device__ __forceinline__ double face_corr_minus(const StepArgs &A, double v, int a, int i, long long o, long long s,
+                                                  uint8_t f)
+{
+    const double *P = A.p;
+    const double m = fbit(f, fb_minus(a));
+    v = v - A.dt * ((P[o] - P[o - s]) * A.dxcinv[a][i]) * (1.0 - m);
+    if (i >= 2) {
+        const double pl = fbit(A.fl[o - s], fb_plus(a));
+        v = v * (1.0 - pl) + bc_at(A.bc[a], o - s) * pl;
+    }
+    return v * (1.0 - m) + bc_at(A.bc[a], o) * m;
+}
+__device__ __forceinline__ double face_corr_last(const StepArgs &A, double v, int a, int n, long long o, long long s,
+                                                 uint8_t f)
+{
+    const double *P = A.p;
+    const double m = fbit(f, fb_plus(a));
+    v = v - A.dt * ((P[o + s] - P[o]) * A.dxcinv[a][n + 1]) * (1.0 - m);
+    return v * (1.0 - m) + bc_at(A.bc[a], o) * m;
+}
+// cell-centre pressure gradient of correct_vel / face_vel (IBM/CORE_FRAC_STEP_ROUTINES.F90:272-349)
+__device__ __forceinline__ double cell_pgrad(const StepArgs &A, int a, int i, long long o, long long s, uint8_t f)
+{
+    const double *P = A.p;
+    const double fxm = A.fx[a][i], fxp = A.fx[a][i + 1];
+    const double mm = fbit(f, fb_minus(a)), pp = fbit(f, fb_plus(a));
+    const double pe = (fxp * P[o + s] + (1.0 - fxp) * P[o]) * (1.0 - pp) + P[o] * pp;
+    const double pw = (fxm * P[o] + (1.0 - fxm) * P[o - s]) * (1.0 - mm) + P[o] * mm;
+    return (pe - pw) * A.dxinv[a][i];
+}
+
+// uTilde = u + dt grad p (1 - iblank), the VAN_KAN predictor of face_vel (IBM/CORE_FRAC_STEP_ROUTINES.F90:36-72)
+__global__ void __launch_bounds__(TPB) k_vankan_tilde(StepArgs A)
+{
+    const Dims &d = A.d;
+    const int n0 = d.m[0] - 1, n1 = d.m[1] - 1, n2 = d.m[2] - 1;
+    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= (long long)n0 * n1 * n2) return;
+    int idx[3];
+    cell_of((unsigned)t, (unsigned)n0, (unsigned)n1, idx[0], idx[1], idx[2]);
+    const long long o = d.idx(idx[0], idx[1], idx[2]);
+    const uint8_t f = A.fl[o];
+    const double blank = (f & FB_IB) ? 0.0 : 1.0;
+    for (int a = 0; a < 3; ++a) {
+        const long long s = stride_of(d, a);
+        A.velo[a][o] = A.vel[a][o] + A.dt * cell_pgrad(A, a, idx[a], o, s, f) * blank;
+    }
+}
+
+// face_vel + rhs_poisson (IBM/CORE_POISSON.F90:155-163, 273-281), one thread
+// per interior cell; each cell recomputes its plus face (the next cell's
+// minus face).  U = vel (NO_VAN_KAN) or the uTilde of k_vankan_tilde; with
+// van_kan the faces also take the pressure correction with p.
+template <bool VANKAN>
+__global__ void __launch_bounds__(TPB) k_face_vel_rhs(StepArgs A, double *partials)
+{
+    const Dims &d = A.d;
+    const int n0 = d.m[0] - 1, n1 = d.m[1] - 1, n2 = d.m[2] - 1;
+    const long long total = (long long)n0 * n1 * n2;
+    double acc = 0.0;
+    for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < total;
+         t += (long long)gridDim.x * blockDim.x) {
+        int idx[3];
+        cell_of((unsigned)t, (unsigned)n0, (unsigned)n1, idx[0], idx[1], idx[2]);
+        const long long o = d.idx(idx[0], idx[1], idx[2]);
+        const uint8_t f = A.fl[o];
+        double term[3];
+        for (int a = 0; a < 3; ++a) {
+            const long long s = stride_of(d, a);
+            const int i = idx[a], n = d.m[a] - 1;
+            const double *U = VANKAN ? A.velo[a] : A.vel[a];
+            double fm = face_interp_minus(A, U, a, i, o, s, f);
+            if (VANKAN) fm = face_corr_minus(A, fm, a, i, o, s, f);
+            double fp;
+            if (i < n) {
+                const uint8_t fn = A.fl[o + s];
+                fp = face_interp_minus(A, U, a, i + 1, o + s, s, fn);
+                if (VANKAN) fp = face_corr_minus(A, fp, a, i + 1, o + s, s, fn);
+            } else {
+                fp = face_interp_last(A, U, a, n, o, s, f);
+                if (VANKAN) fp = face_corr_last(A, fp, a, n, o, s, f);
+                A.face[a][o + s] = fp;
+            }
+            A.face[a][o] = fm;
+            term[a] = (fp - fm) * A.dxinv[a][i];
+        }
+        double r = (1.0 / A.dt) * ((term[0] + term[1]) + term[2]);
+        r = r * ((f & FB_IB) ? 0.0 : 1.0);
+        A.nlu0[o] = r;
+        acc += r * A.dx[0][idx[0]] * A.dx[1][idx[1]] * A.dx[2][idx[2]];
+    }
+    const double tot = block_sum(acc);
+    if (threadIdx.x == 0) partials[blockIdx.x] = tot;
+}
+
+// correct_vel without the ghost-cell velocity interpolation
+// (IBM/CORE_FRAC_STEP_ROUTINES.F90:272-366 cell centres, :381-441 faces)
+__global__ void __launch_bounds__(TPB) k_correct_vel(StepArgs A)
+{
+    const Dims &d = A.d;
+    const int n0 = d.m[0] - 1, n1 = d.m[1] - 1, n2 = d.m[2] - 1;
+    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= (long long)n0 * n1 * n2) return;
+    int idx[3];
+    cell_of((unsigned)t, (unsigned)n0, (unsigned)n1, idx[0], idx[1], idx[2]);
+    const long long o = d.idx(idx[0], idx[1], idx[2]);
+    const uint8_t f = A.fl[o];
+    const double blank = (f & FB_IB) ? 0.0 : 1.0;
+    for (int a = 0; a < 3; ++a) {
+        const long long s = stride_of(d, a);
+        const int i = idx[a], n = d.m[a] - 1;
+        A.velo[a][o] = A.vel[a][o] - A.dt * cell_pgrad(A, a, i, o, s, f) * blank;
+        double *F = A.face[a];
+        const double v1 = face_corr_minus(A, F[o], a, i, o, s, f);
+        if (i == n) F[o + s] = face_corr_last(A, F[o + s], a, n, o, s, f);
+        F[o] = v1;
+    }
+}
+
+// zero the non-interior part of a full (0:nx+1,0:ny+1,0:nz+1) array: planes
+// k = 0, nz, nz+1; then rows j = 0, ny, ny+1 of k = 1..nzc; then cells
+// i = 0, nx, nx+1 of the interior rows (the interior is written elsewhere)
+__global__ void k_zero_shell(double *a, Dims d)
+{
+    const int nx = d.m[0], ny = d.m[1], nz = d.m[2];
+    const long long sx = d.sx, sxy = d.sxy;
+    const long long segA = 3 * sxy, segB = 3 * sx * (nz - 1), segC = 3LL * (ny - 1) * (nz - 1);
+    for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < segA + segB + segC;
+         t += (long long)gridDim.x * blockDim.x) {
+        long long o;
+        if (t < segA) {
+            const long long q = t / sxy, r = t - q * sxy;
+            o = (q == 0 ? 0 : (q == 1 ? nz : nz + 1)) * sxy + r;
+        } else if (t < segA + segB) {
+            const long long u = t - segA, q = u / (sx * (nz - 1)), r = u - q * (sx * (nz - 1));
+            const long long k = 1 + r / sx, i = r - (k - 1) * sx;
+            o = i + sx * (q == 0 ? 0 : (q == 1 ? ny : ny + 1)) + sxy * k;
+        } else {
+            const long long u = t - segA - segB, q = u / ((long long)(ny - 1) * (nz - 1));
+            const long long r = u - q * ((long long)(ny - 1) * (nz - 1));
+            const long long k = 1 + r / (ny - 1), j = 1 + r % (ny - 1);
+            o = (q == 0 ? 0 : (q == 1 ? nx : nx + 1)) + sx * j + sxy * k;
+        }
+        a[o] = 0.0;
+    }
+}
+
+__global__ void k_update_pressure(double *p, const double *pPrime, long long n, int van_kan)
+{
+    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t < n) p[t] = van_kan ? p[t] + pPrime[t] : pPrime[t];
+}
+
 // compatibility flux, non-periodic branch (IBM/GCM_GLOBAL_MASS_CONSERVE.F90:290-331)
 struct CompatArgs {
     const double *p;
@@ -1845,6 +2025,33 @@ void launch_fresh_cells(double *p, const uint8_t *fl, const uint8_t *fresh, cons
 {
     const long long n = (long long)(d.m[0] - 1) * (d.m[1] - 1) * (d.m[2] - 1);
     k_fresh_cells<<<nblk(n), TPB, 0, s>>>(p, fl, fresh, d, three_d ? 1 : 0);
+}
+
+void launch_face_vel_rhs(const StepArgs &a, bool van_kan, double *partials, int nblocks, double *sums,
+                         cudaStream_t s)
+{
+    const long long n = (long long)(a.d.m[0] - 1) * (a.d.m[1] - 1) * (a.d.m[2] - 1);
+    // nlu0 = 0 outside the interior (the reference zeroes the whole array first)
+    const long long nshell = 3 * a.d.sxy + 3 * a.d.sx * (a.d.m[2] - 1) + 3LL * (a.d.m[1] - 1) * (a.d.m[2] - 1);
+    k_zero_shell<<<nblk(nshell), TPB, 0, s>>>(a.nlu0, a.d);
+    if (van_kan) {
+        k_vankan_tilde<<<nblk(n), TPB, 0, s>>>(a);
+        k_face_vel_rhs<true><<<nblocks, TPB, 0, s>>>(a, partials);
+    } else {
+        k_face_vel_rhs<false><<<nblocks, TPB, 0, s>>>(a, partials);
+    }
+    k_sum_final<<<1, 1024, 0, s>>>(partials, nblocks, 1, sums);
+}
+
+void launch_correct_vel(const StepArgs &a, cudaStream_t s)
+{
+    const long long n = (long long)(a.d.m[0] - 1) * (a.d.m[1] - 1) * (a.d.m[2] - 1);
+    k_correct_vel<<<nblk(n), TPB, 0, s>>>(a);
+}
+
+void launch_update_pressure(double *p, const double *pPrime, long long n, bool van_kan, cudaStream_t s)
+{
+    k_update_pressure<<<nblk(n), TPB, 0, s>>>(p, pPrime, n, van_kan ? 1 : 0);
 }
 
 static CompatArgs make_compat(const double *p, const uint8_t *fl, const double *pg, const double *dx,

@@ -85,6 +85,32 @@ struct GhostArgs {
                              // -(m + 2) for ghost cell number m, -1 for the uNormal term
 };
 
+// The fractional-step operations either side of the pressure solve, on
+// level-1 full-layout FP64 arrays (face arrays share the cell layout: face
+// index i of axis a sits at the cell (i, j, k) it is the minus face of).
+struct StepArgs {
+    const double *vel[3];     // cell velocities u, v, w
+    double *velo[3];          // corrected velocities (correct_vel; may alias vel), uTilde (face_vel, VAN_KAN)
+    const double *bc[3];      // bcxu, bcyv, bczw (null: zero)
+    double *face[3];          // face_u, face_v, face_w
+    double *nlu0;
+    const double *p;          // pPrime
+    const uint8_t *fl;        // level-1 flag bytes (iblank, face bits)
+    const double *fx[3], *dxinv[3], *dxcinv[3], *dx[3];
+    Dims d;
+    double dt;
+};
+// face_vel + rhs_poisson (IBM/CORE_FRAC_STEP_ROUTINES.F90:36-177, IBM/CORE_POISSON.F90:155-163,
+// 273-281; with van_kan, p is the current pressure and velo the uTilde scratch); sums[0]
+// receives sum nlu0 dx dy dz.  nlu0 is zeroed over the whole array first.
+void launch_face_vel_rhs(const StepArgs &a, bool van_kan, double *partials, int nblocks, double *sums,
+                         cudaStream_t s);
+// correct_vel cell-centre update and face corrections (IBM/CORE_FRAC_STEP_ROUTINES.F90:244-448,
+// without the ghost-cell velocity interpolation)
+void launch_correct_vel(const StepArgs &a, cudaStream_t s);
+// update_pressure without its ghost rows (IBM/CORE_FRAC_STEP_ROUTINES.F90:949-967)
+void launch_update_pressure(double *p, const double *pPrime, long long n, bool van_kan, cudaStream_t s);
+
 // one-time kernel attributes (call before the first launch, outside stream capture)
 cudaError_t init_kernels();
 // 0: warp-per-line partition solver (default, lines up to 512 cells), 1: one thread per line

@@ -71,6 +71,31 @@ MODULE fsi_mg_gpu
       REAL(C_DOUBLE), INTENT(IN) :: rr(*)
       REAL(C_DOUBLE), INTENT(OUT) :: compTime
     END FUNCTION
+    ! Steps either side of the solve on DEVICE arrays (a CUDA Fortran or
+    ! OpenACC caller passes device addresses, e.g. via host_data use_device;
+    ! C_NULL_PTR for an absent bc array).  face_vel + rhs_poisson
+    ! (IBM/CORE_FRAC_STEP_ROUTINES.F90:6, IBM/CORE_POISSON.F90:123),
+    ! correct_vel (:244) without its ghost-cell velocity steps, update_pressure (:949).
+    INTEGER(C_INT) FUNCTION fsi_mg_face_vel_rhs(h, frac_step_type, dt, u, v, w, p, bcxu, bcyv, bczw, &
+        face_u, face_v, face_w, nlu0, total) BIND(C, NAME='fsi_mg_face_vel_rhs')
+      IMPORT :: C_INT, C_DOUBLE, C_PTR
+      TYPE(C_PTR), VALUE :: h, u, v, w, p, bcxu, bcyv, bczw, face_u, face_v, face_w, nlu0
+      INTEGER(C_INT), VALUE :: frac_step_type
+      REAL(C_DOUBLE), VALUE :: dt
+      REAL(C_DOUBLE), INTENT(OUT) :: total
+    END FUNCTION
+    INTEGER(C_INT) FUNCTION fsi_mg_correct_vel(h, dt, pPrime, u, v, w, bcxu, bcyv, bczw, &
+        face_u, face_v, face_w) BIND(C, NAME='fsi_mg_correct_vel')
+      IMPORT :: C_INT, C_DOUBLE, C_PTR
+      TYPE(C_PTR), VALUE :: h, pPrime, u, v, w, bcxu, bcyv, bczw, face_u, face_v, face_w
+      REAL(C_DOUBLE), VALUE :: dt
+    END FUNCTION
+    INTEGER(C_INT) FUNCTION fsi_mg_update_pressure(h, frac_step_type, pPrime, p) &
+        BIND(C, NAME='fsi_mg_update_pressure')
+      IMPORT :: C_INT, C_PTR
+      TYPE(C_PTR), VALUE :: h, pPrime, p
+      INTEGER(C_INT), VALUE :: frac_step_type
+    END FUNCTION
     TYPE(C_PTR) FUNCTION fsi_mg_last_error() BIND(C, NAME='fsi_mg_last_error')
       IMPORT :: C_PTR
     END FUNCTION

@@ -117,6 +117,31 @@ class PoissonSolver:
                                                  ctypes.byref(mr), loc, ctypes.byref(ct)))
         return st, it.value, mr.value, tuple(loc), ct.value
 
+    # -- steps either side of the solve (device pointers, full layout) ----
+    def face_vel_rhs(self, dt: float, d_u: int, d_v: int, d_w: int, d_face_u: int, d_face_v: int, d_face_w: int,
+                     d_nlu0: int, d_bc=(None, None, None), frac_step_type: int = 0, d_p: Optional[int] = None):
+        """face_vel + rhs_poisson (IBM/CORE_FRAC_STEP_ROUTINES.F90:6-240,
+        IBM/CORE_POISSON.F90:123-417) on device arrays.  Returns sum nlu0 dV."""
+        vp = lambda a: ctypes.c_void_p(a) if a else None
+        total = ctypes.c_double()
+        _check(self.lib.fsi_mg_face_vel_rhs(self.h, frac_step_type, float(dt), vp(d_u), vp(d_v), vp(d_w), vp(d_p),
+                                            vp(d_bc[0]), vp(d_bc[1]), vp(d_bc[2]), vp(d_face_u), vp(d_face_v),
+                                            vp(d_face_w), vp(d_nlu0), ctypes.byref(total)))
+        return total.value
+
+    def correct_vel(self, dt: float, d_pPrime: int, d_u: int, d_v: int, d_w: int, d_face_u: int, d_face_v: int,
+                    d_face_w: int, d_bc=(None, None, None)):
+        """correct_vel (IBM/CORE_FRAC_STEP_ROUTINES.F90:244-448) without the
+        ghost-cell velocity steps, on device arrays (updated in place)."""
+        vp = lambda a: ctypes.c_void_p(a) if a else None
+        _check(self.lib.fsi_mg_correct_vel(self.h, float(dt), vp(d_pPrime), vp(d_u), vp(d_v), vp(d_w), vp(d_bc[0]),
+                                           vp(d_bc[1]), vp(d_bc[2]), vp(d_face_u), vp(d_face_v), vp(d_face_w)))
+
+    def update_pressure(self, d_pPrime: int, d_p: int, frac_step_type: int = 0):
+        """update_pressure (IBM/CORE_FRAC_STEP_ROUTINES.F90:949-967) on device arrays."""
+        _check(self.lib.fsi_mg_update_pressure(self.h, frac_step_type, ctypes.c_void_p(d_pPrime),
+                                               ctypes.c_void_p(d_p)))
+
     # -- finer hooks -----------------------------------------------------
     def MG_Solver(self, var: np.ndarray, rr: np.ndarray) -> float:
         ct = ctypes.c_double()

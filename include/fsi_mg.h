@@ -132,6 +132,39 @@ int fsi_mg_set_fresh_cells(void *handle, const int8_t *fresh_cell);
  * ghost-cell rows, compatibility correction of pgrad*, and nlw0 (OUT, may be NULL). */
 int fsi_mg_correct_pressure(void *handle, double *pPrime, double *nlw0_out);
 
+/* The fractional-step operations either side of the solve, on DEVICE arrays
+ * in the full (0:nx+1,0:ny+1,0:nz+1) layout, for a time loop that keeps its
+ * fields in HBM.  Face arrays face_u/face_v/face_w share that layout (face i
+ * of x at (i,j,k), i = 1..nx).  bcxu/bcyv/bczw may be NULL (all zero).  They
+ * use the flags of the last fsi_mg_set_geometry and need Neumann pressure
+ * sides (status -1 otherwise).  Each call waits for its work to finish.
+ *
+ * face_vel (IBM/CORE_FRAC_STEP_ROUTINES.F90:6-240) followed by the
+ * non-hybrid rhs_poisson (IBM/CORE_POISSON.F90:123-417): face velocities from
+ * u, v, w (frac_step_type 0, NO_VAN_KAN) or from uTilde = u + dt grad p with
+ * the face pressure correction (1, VAN_KAN; d_p is then the current
+ * pressure), then nlu0 = div(face)/dt (1 - iblank), zero outside the
+ * interior; sum OUT (may be NULL) = sum nlu0 dx dy dz in a fixed order.  The
+ * ghost-cell face values of GCM_set_face_vel_body stay with the caller. */
+int fsi_mg_face_vel_rhs(void *handle, int frac_step_type, double dt, const double *d_u, const double *d_v,
+                        const double *d_w, const double *d_p, const double *d_bcxu, const double *d_bcyv,
+                        const double *d_bczw, double *d_face_u, double *d_face_v, double *d_face_w, double *d_nlu0,
+                        double *sum);
+
+/* correct_vel (IBM/CORE_FRAC_STEP_ROUTINES.F90:244-448) without periodic
+ * sides and without the ghost-cell velocity interpolation
+ * (GCM_vel_set_bc_internal) and GCM_set_face_vel_body, which stay with the
+ * caller: u, v, w -= dt grad pPrime (1 - iblank) and the face corrections in
+ * the reference's overwrite order (INOUT d_u..d_w, d_face_u..d_face_w). */
+int fsi_mg_correct_vel(void *handle, double dt, const double *d_pPrime, double *d_u, double *d_v, double *d_w,
+                       const double *d_bcxu, const double *d_bcyv, const double *d_bczw, double *d_face_u,
+                       double *d_face_v, double *d_face_w);
+
+/* update_pressure (IBM/CORE_FRAC_STEP_ROUTINES.F90:949-967): p = pPrime
+ * (frac_step_type 0) or p += pPrime (1), then the ghost-cell pressure rows
+ * of GCM_p_set_bc_internal when boundary_formulation is GCM. */
+int fsi_mg_update_pressure(void *handle, int frac_step_type, const double *d_pPrime, double *d_p);
+
 /* Current boundary pressure-gradient planes (packed as in set_geometry). */
 int fsi_mg_get_pgrad(void *handle, double *pgrad);
 
@@ -167,8 +200,12 @@ int fsi_mg_residual_history(void *handle, double *out, int cap);
 /* Time one kernel of the level-1 hierarchy on the handle's stream with CUDA
  * events, averaged over reps launches (after one warm-up launch), on the
  * current staging fields.  which: 0/1/2 one colour of the x/y/z line sweep,
- * 3 residual + x restriction, 4 x prolongation + correction, 5 calc_residual.
- * precision 0 FP64, 1 FP32.  alg_bytes (may be NULL) receives the algorithmic
+ * 3 residual + x restriction, 4 x prolongation + correction, 5 calc_residual,
+ * 6/7/8 the kernels of the last fsi_mg_face_vel_rhs / fsi_mg_correct_vel /
+ * fsi_mg_update_pressure call replayed on its arrays (correct_vel and the
+ * VAN_KAN update_pressure then apply their update reps+1 more times; the
+ * ghost-cell rows of update_pressure are not replayed).
+ * precision 0 FP64, 1 FP32 (0-5 only).  alg_bytes (may be NULL) receives the algorithmic
  * bytes one launch moves.  No counterpart in the reference: a measurement hook. */
 int fsi_mg_time_kernel(void *handle, int which, int precision, int reps, double *avg_ms, double *alg_bytes);
 

@@ -1184,3 +1184,161 @@ void or_prolong_level(or_ctx *c, int d, int n, const double *phi, double *corr)
     c->ibMG = ib_view(c, d, n + 1);
     mg_prolong(c, d, corr, phi, n, fm[0], fm[1], fm[2], m1, m[d]);
 }
+
+/* ------------------------------------- fractional-step routines either side of the solve ---- */
+/* Interpolation weight fx(i) = (x(i) - xc(i-1)) / (xc(i) - xc(i-1)), IBM/CORE_GRID.F90:163-175. */
+static double fxw(or_ctx *c, int d, int i)
+{
+    return (c->x[d][i] - c->xc[d][i - 1]) / (c->xc[d][i] - c->xc[d][i - 1]);
+}
+
+/* Face pressure correction of one direction: face1/face2 from the old faces,
+ * copy-back, then the um/up masks, each in the reference's loop order
+ * (IBM/CORE_FRAC_STEP_ROUTINES.F90:381-441; the same loops close the VAN_KAN
+ * branch of face_vel, :111-177).  d = 0 x, 1 y, 2 z. */
+static void face_correct(or_ctx *c, int d, double dt, const double *p, double *face, const double *bc)
+{
+    const int nc[3] = {c->nxc, c->nyc, c->nzc};
+    const int n = nc[d];
+    const int8_t *um = c->fl[2 * d], *up = c->fl[2 * d + 1];
+    double *face1 = zalloc(sizeof(double) * (size_t)(n + 2)), *face2 = zalloc(sizeof(double) * (size_t)(n + 2));
+    /* outer loops: x (k, j), y (k, i), z (j, i); the inner index runs along d */
+    const int o1 = (d == 2) ? c->nyc : c->nzc, o2 = (d == 0) ? c->nyc : c->nxc;
+    for (int a = 1; a <= o1; ++a)
+        for (int b = 1; b <= o2; ++b) {
+#define AT(t) (d == 0 ? FI(c, (t), b, a) : d == 1 ? FI(c, b, (t), a) : FI(c, b, a, (t)))
+            for (int t = 1; t <= n; ++t) {
+                const double pgm = (p[AT(t)] - p[AT(t - 1)]) * c->dxcinv[d][t];
+                const double pgp = (p[AT(t + 1)] - p[AT(t)]) * c->dxcinv[d][t + 1];
+                face1[t] = face[AT(t)] - dt * pgm * (1 - um[AT(t)]);
+                face2[t] = face[AT(t + 1)] - dt * pgp * (1 - up[AT(t)]);
+            }
+            for (int t = 1; t <= n; ++t) {
+                face[AT(t)] = face1[t];
+                face[AT(t + 1)] = face2[t];
+            }
+            for (int t = 1; t <= n; ++t) {
+                const double bv = bc ? bc[AT(t)] : 0.0;
+                face[AT(t)] = face[AT(t)] * (1 - um[AT(t)]) + bv * um[AT(t)];
+                face[AT(t + 1)] = face[AT(t + 1)] * (1 - up[AT(t)]) + bv * up[AT(t)];
+            }
+#undef AT
+        }
+    free(face1);
+    free(face2);
+}
+
+/* face_vel (IBM/CORE_FRAC_STEP_ROUTINES.F90:6-240 without GCM_set_face_vel_body):
+ * frac_step_type 0 NO_VAN_KAN (uTilde = u), 1 VAN_KAN (uTilde = u + dt grad p on
+ * the interior, zero elsewhere, then the face pressure correction with p).
+ * bc arrays may be NULL (zero). */
+void or_face_vel(or_ctx *c, int frac_step_type, double dt, const double *u, const double *v, const double *w,
+                 const double *p, const double *bcxu, const double *bcyv, const double *bczw,
+                 double *face_u, double *face_v, double *face_w)
+{
+    const size_t nf = (size_t)(c->nx + 2) * (size_t)(c->ny + 2) * (size_t)(c->nz + 2);
+    double *uT = zalloc(sizeof(double) * nf), *vT = zalloc(sizeof(double) * nf), *wT = zalloc(sizeof(double) * nf);
+    const int8_t *ium = c->fl[0], *iup = c->fl[1], *jum = c->fl[2], *jup = c->fl[3], *kum = c->fl[4], *kup = c->fl[5];
+#define BCV(a, f) ((a) ? (a)[f] : 0.0)
+    if (frac_step_type == 1) {
+        for (int k = 1; k <= c->nzc; ++k)
+            for (int j = 1; j <= c->nyc; ++j)
+                for (int i = 1; i <= c->nxc; ++i) {
+                    const size_t f = FI(c, i, j, k);
+                    const double pe = (fxw(c, 0, i + 1) * p[FI(c, i + 1, j, k)] + (1.0 - fxw(c, 0, i + 1)) * p[f]) * (1 - iup[f]) + p[f] * iup[f];
+                    const double pw = (fxw(c, 0, i) * p[f] + (1.0 - fxw(c, 0, i)) * p[FI(c, i - 1, j, k)]) * (1 - ium[f]) + p[f] * ium[f];
+                    const double pn = (fxw(c, 1, j + 1) * p[FI(c, i, j + 1, k)] + (1.0 - fxw(c, 1, j + 1)) * p[f]) * (1 - jup[f]) + p[f] * jup[f];
+                    const double ps = (fxw(c, 1, j) * p[f] + (1.0 - fxw(c, 1, j)) * p[FI(c, i, j - 1, k)]) * (1 - jum[f]) + p[f] * jum[f];
+                    const double pf = (fxw(c, 2, k + 1) * p[FI(c, i, j, k + 1)] + (1.0 - fxw(c, 2, k + 1)) * p[f]) * (1 - kup[f]) + p[f] * kup[f];
+                    const double pb = (fxw(c, 2, k) * p[f] + (1.0 - fxw(c, 2, k)) * p[FI(c, i, j, k - 1)]) * (1 - kum[f]) + p[f] * kum[f];
+                    const double pgx = (pe - pw) * c->dxinv[0][i];
+                    const double pgy = (pn - ps) * c->dxinv[1][j];
+                    const double pgz = (pf - pb) * c->dxinv[2][k];
+                    uT[f] = u[f] + dt * pgx * (double)(1 - c->iblank[f]);
+                    vT[f] = v[f] + dt * pgy * (double)(1 - c->iblank[f]);
+                    wT[f] = w[f] + dt * pgz * (double)(1 - c->iblank[f]);
+                }
+    } else {
+        memcpy(uT, u, sizeof(double) * nf);
+        memcpy(vT, v, sizeof(double) * nf);
+        memcpy(wT, w, sizeof(double) * nf);
+    }
+    for (int k = 1; k <= c->nzc; ++k)
+        for (int j = 1; j <= c->nyc; ++j)
+            for (int i = 1; i <= c->nxc; ++i) {
+                const size_t f = FI(c, i, j, k);
+                face_u[FI(c, i + 1, j, k)] = (fxw(c, 0, i + 1) * uT[FI(c, i + 1, j, k)] + (1.0 - fxw(c, 0, i + 1)) * uT[f]) * (1 - iup[f]) + BCV(bcxu, f) * iup[f];
+                face_u[f] = (fxw(c, 0, i) * uT[f] + (1.0 - fxw(c, 0, i)) * uT[FI(c, i - 1, j, k)]) * (1 - ium[f]) + BCV(bcxu, f) * ium[f];
+                face_v[FI(c, i, j + 1, k)] = (fxw(c, 1, j + 1) * vT[FI(c, i, j + 1, k)] + (1.0 - fxw(c, 1, j + 1)) * vT[f]) * (1 - jup[f]) + BCV(bcyv, f) * jup[f];
+                face_v[f] = (fxw(c, 1, j) * vT[f] + (1.0 - fxw(c, 1, j)) * vT[FI(c, i, j - 1, k)]) * (1 - jum[f]) + BCV(bcyv, f) * jum[f];
+                face_w[FI(c, i, j, k + 1)] = (fxw(c, 2, k + 1) * wT[FI(c, i, j, k + 1)] + (1.0 - fxw(c, 2, k + 1)) * wT[f]) * (1 - kup[f]) + BCV(bczw, f) * kup[f];
+                face_w[f] = (fxw(c, 2, k) * wT[f] + (1.0 - fxw(c, 2, k)) * wT[FI(c, i, j, k - 1)]) * (1 - kum[f]) + BCV(bczw, f) * kum[f];
+            }
+#undef BCV
+    if (frac_step_type == 1) {
+        face_correct(c, 0, dt, p, face_u, bcxu);
+        face_correct(c, 1, dt, p, face_v, bcyv);
+        face_correct(c, 2, dt, p, face_w, bczw);
+    }
+    free(uT); free(vT); free(wT);
+}
+
+/* rhs_poisson without the hybrid cut-cell branch (IBM/CORE_POISSON.F90:123-163,
+ * 273-285): nlu0 zeroed, then dtinv * div(face) * (1 - iblank); returns sum. */
+double or_rhs_poisson(or_ctx *c, double dt, const double *face_u, const double *face_v, const double *face_w,
+                      double *nlu0)
+{
+    const size_t nf = (size_t)(c->nx + 2) * (size_t)(c->ny + 2) * (size_t)(c->nz + 2);
+    const double dtinv = 1.0 / dt;
+    double sum = 0.0;
+    memset(nlu0, 0, sizeof(double) * nf);
+    for (int k = 1; k <= c->nzc; ++k)
+        for (int j = 1; j <= c->nyc; ++j)
+            for (int i = 1; i <= c->nxc; ++i) {
+                const size_t f = FI(c, i, j, k);
+                nlu0[f] = dtinv * ((face_u[FI(c, i + 1, j, k)] - face_u[f]) * c->dxinv[0][i]
+                                   + (face_v[FI(c, i, j + 1, k)] - face_v[f]) * c->dxinv[1][j]
+                                   + (face_w[FI(c, i, j, k + 1)] - face_w[f]) * c->dxinv[2][k]);
+                nlu0[f] = nlu0[f] * (double)(1 - c->iblank[f]);
+                sum = sum + nlu0[f] * c->dx[0][i] * c->dx[1][j] * c->dx[2][k];
+            }
+    return sum;
+}
+
+/* correct_vel (IBM/CORE_FRAC_STEP_ROUTINES.F90:244-448), non-periodic, without
+ * GCM_vel_set_bc_internal and GCM_set_face_vel_body. */
+void or_correct_vel(or_ctx *c, double dt, const double *pPrime, double *u, double *v, double *w,
+                    const double *bcxu, const double *bcyv, const double *bczw,
+                    double *face_u, double *face_v, double *face_w)
+{
+    const double *p = pPrime;
+    const int8_t *ium = c->fl[0], *iup = c->fl[1], *jum = c->fl[2], *jup = c->fl[3], *kum = c->fl[4], *kup = c->fl[5];
+    for (int k = 1; k <= c->nzc; ++k)
+        for (int j = 1; j <= c->nyc; ++j)
+            for (int i = 1; i <= c->nxc; ++i) {
+                const size_t f = FI(c, i, j, k);
+                const double pe = (fxw(c, 0, i + 1) * p[FI(c, i + 1, j, k)] + (1.0 - fxw(c, 0, i + 1)) * p[f]) * (1 - iup[f]) + p[f] * iup[f];
+                const double pw = (fxw(c, 0, i) * p[f] + (1.0 - fxw(c, 0, i)) * p[FI(c, i - 1, j, k)]) * (1 - ium[f]) + p[f] * ium[f];
+                const double pn = (fxw(c, 1, j + 1) * p[FI(c, i, j + 1, k)] + (1.0 - fxw(c, 1, j + 1)) * p[f]) * (1 - jup[f]) + p[f] * jup[f];
+                const double ps = (fxw(c, 1, j) * p[f] + (1.0 - fxw(c, 1, j)) * p[FI(c, i, j - 1, k)]) * (1 - jum[f]) + p[f] * jum[f];
+                const double pf = (fxw(c, 2, k + 1) * p[FI(c, i, j, k + 1)] + (1.0 - fxw(c, 2, k + 1)) * p[f]) * (1 - kup[f]) + p[f] * kup[f];
+                const double pb = (fxw(c, 2, k) * p[f] + (1.0 - fxw(c, 2, k)) * p[FI(c, i, j, k - 1)]) * (1 - kum[f]) + p[f] * kum[f];
+                const double pgx = (pe - pw) * c->dxinv[0][i];
+                const double pgy = (pn - ps) * c->dxinv[1][j];
+                const double pgz = (pf - pb) * c->dxinv[2][k];
+                u[f] = u[f] - dt * pgx * (double)(1 - c->iblank[f]);
+                v[f] = v[f] - dt * pgy * (double)(1 - c->iblank[f]);
+                w[f] = w[f] - dt * pgz * (double)(1 - c->iblank[f]);
+            }
+    face_correct(c, 0, dt, p, face_u, bcxu);
+    face_correct(c, 1, dt, p, face_v, bcyv);
+    face_correct(c, 2, dt, p, face_w, bczw);
+}
+
+/* update_pressure (IBM/CORE_FRAC_STEP_ROUTINES.F90:949-967). */
+void or_update_pressure(or_ctx *c, int frac_step_type, const double *pPrime, double *p)
+{
+    const size_t nf = (size_t)(c->nx + 2) * (size_t)(c->ny + 2) * (size_t)(c->nz + 2);
+    for (size_t t = 0; t < nf; ++t) p[t] = (frac_step_type == 1) ? p[t] + pPrime[t] : pPrime[t];
+    if (c->p.boundary_formulation == GCM_METHOD) gcm_p_set_bc_internal(c, p, c->nx + 1, c->ny + 1);
+}

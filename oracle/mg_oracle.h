@@ -83,4 +83,14 @@ void    or_tdma(const double *a, const double *b, const double *c_, const double
 int     or_nghost_gs_last(or_ctx *c);
 void    or_outer_ghost(or_ctx *c, double *var);
 void    or_get_pgrad(or_ctx *c, double *pgrad);
+/* fractional-step routines either side of the solve (full-layout arrays; bc may be NULL) */
+void    or_face_vel(or_ctx *c, int frac_step_type, double dt, const double *u, const double *v, const double *w,
+                    const double *p, const double *bcxu, const double *bcyv, const double *bczw,
+                    double *face_u, double *face_v, double *face_w);
+double  or_rhs_poisson(or_ctx *c, double dt, const double *face_u, const double *face_v, const double *face_w,
+                       double *nlu0);
+void    or_correct_vel(or_ctx *c, double dt, const double *pPrime, double *u, double *v, double *w,
+                       const double *bcxu, const double *bcyv, const double *bczw,
+                       double *face_u, double *face_v, double *face_w);
+void    or_update_pressure(or_ctx *c, int frac_step_type, const double *pPrime, double *p);
 #endif

@@ -79,6 +79,14 @@ def lib():
         L.or_outer_ghost.restype = None
         L.or_get_pgrad.argtypes = [ctypes.c_void_p, _dp]
         L.or_get_pgrad.restype = None
+        L.or_face_vel.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_double] + [_dp] * 10
+        L.or_face_vel.restype = None
+        L.or_rhs_poisson.argtypes = [ctypes.c_void_p, ctypes.c_double] + [_dp] * 4
+        L.or_rhs_poisson.restype = ctypes.c_double
+        L.or_correct_vel.argtypes = [ctypes.c_void_p, ctypes.c_double] + [_dp] * 10
+        L.or_correct_vel.restype = None
+        L.or_update_pressure.argtypes = [ctypes.c_void_p, ctypes.c_int, _dp, _dp]
+        L.or_update_pressure.restype = None
         _lib = L
     return _lib
 
@@ -169,6 +177,30 @@ class Oracle:
         out = np.zeros(pgrad_size(self.params))
         lib().or_get_pgrad(self.h, _p(out))
         return out
+
+    # ----- fractional-step routines either side of the solve -----
+    def face_vel(self, dt, u, v, w, p=None, bc=(None, None, None), frac_step_type=0, faces=None):
+        """face_vel; returns (face_u, face_v, face_w).  `faces` (three arrays,
+        updated in place) keeps the caller's values outside the written faces."""
+        sh = self.problem.shape
+        fu, fv, fw = faces if faces is not None else (np.zeros(sh, order="F") for _ in range(3))
+        lib().or_face_vel(self.h, frac_step_type, dt, _p(u), _p(v), _p(w), _p(p), _p(bc[0]), _p(bc[1]), _p(bc[2]),
+                          _p(fu), _p(fv), _p(fw))
+        return fu, fv, fw
+
+    def rhs_poisson(self, dt, face_u, face_v, face_w):
+        nlu0 = np.zeros(self.problem.shape, order="F")
+        s = lib().or_rhs_poisson(self.h, dt, _p(face_u), _p(face_v), _p(face_w), _p(nlu0))
+        return nlu0, s
+
+    def correct_vel(self, dt, pPrime, u, v, w, face_u, face_v, face_w, bc=(None, None, None)):
+        """In place on u, v, w and the faces."""
+        lib().or_correct_vel(self.h, dt, _p(pPrime), _p(u), _p(v), _p(w), _p(bc[0]), _p(bc[1]), _p(bc[2]),
+                             _p(face_u), _p(face_v), _p(face_w))
+
+    def update_pressure(self, pPrime, p, frac_step_type=0):
+        lib().or_update_pressure(self.h, frac_step_type, _p(pPrime), _p(p))
+        return p
 
     # ----- per-level operators (kernel parity) -----
     def nlev(self, d):

@@ -113,3 +113,51 @@ def fresh_reference(problem, p, fresh):
                                 s = s + p[ii, jj, kk]
                 p[i, j, k] = s / cnt
     return p
+
+
+# ------------------------------------------------- fractional-step cases ----
+def baffle_problem(cells=(12, 10, 14), stretch=1.5, seed=3):
+    """3D box without a body, stretched grid, with two interior walls: an x-face
+    baffle (iup(i0,...) = ium(i0+1,...) = 1) and a y-face baffle, each set from
+    both sides as set_iup would for a thin body."""
+    import numpy as np
+    from flow_structure_interaction_fem_ibm_gb300 import problem as P
+    p = P.default_params(3, *cells, body=False)
+    kind = "uniform" if stretch is None else "tanh"
+    x, y, z = P.make_grid(p.nx, p.ny, p.nz, kind, beta=stretch or 1.5)
+    geom = P.empty_geometry(p)
+    ium, iup, jum, jup = geom.flags[:4]
+    i0, j0 = cells[0] // 2, cells[1] // 2
+    iup[i0, 3:cells[1] - 2, 4:cells[2] - 3] = 1
+    ium[i0 + 1, 3:cells[1] - 2, 4:cells[2] - 3] = 1
+    jup[2:cells[0] - 3, j0, 2:cells[2] - 5] = 1
+    jum[2:cells[0] - 3, j0 + 1, 2:cells[2] - 5] = 1
+    rng = np.random.Generator(np.random.PCG64(seed))
+    sh = P.full_shape(p)
+    u, v, w = (np.asfortranarray(rng.standard_normal(sh)) for _ in range(3))
+    nlu0 = P.face_divergence(p, x, y, z, u, v, w, geom.iblank, geom.flags)
+    P.remove_fluid_mean(p, x, y, z, nlu0, geom.iblank)
+    return P.Problem(p, x, y, z, geom, nlu0, name=f"baffle_{cells[0]}x{cells[1]}x{cells[2]}")
+
+
+def step_cases():
+    from flow_structure_interaction_fem_ibm_gb300 import problem as P
+    return [
+        ("sphere16_tanh", lambda: sphere_problem(16, stretch=1.5)),
+        ("box2d_24", lambda: P.box2d(24, seed=9)),
+        ("baffle_12x10x14", lambda: baffle_problem()),
+    ]
+
+
+def step_fields(problem, seed, with_bc=True):
+    """Seeded cell velocities, pressures, boundary face velocities and prior
+    face arrays (full layout) for the fractional-step routines."""
+    import numpy as np
+    rng = np.random.Generator(np.random.PCG64(seed))
+    sh = problem.shape
+    r = lambda: np.asfortranarray(rng.standard_normal(sh))
+    f = dict(u=r(), v=r(), w=r(), p=r(), pPrime=r(), faces=[r(), r(), r()])
+    f["bc"] = [r(), r(), r()] if with_bc else [None, None, None]
+    if problem.params.ndim == 2:
+        f["w"][...] = 0.0
+    return f
