@@ -118,6 +118,9 @@ struct Ctx {
     int sign[6] = {1, 1, 1, 1, 1, 1};
     double *d_dx[3] = {}, *d_dxinv[3] = {}, *d_dxcinv[3] = {};
     double *d_fx[3] = {};   // face interpolation weights fx(1:n) (IBM/CORE_GRID.F90:163-175)
+    double *d_gx[3] = {};   // 1 - fx, as the reference forms it
+    double *step_partials = nullptr;   // one partial sum per CTA of face_vel_rhs
+    int step_cap = 0;
     double *vtilde = nullptr;   // uTilde, vTilde, wTilde of the VAN_KAN face_vel (allocated on first use)
     // arguments of the last step calls, replayed by fsi_mg_time_kernel (which 6, 7, 8)
     StepArgs last_fv{}, last_cv{};
@@ -1106,8 +1109,12 @@ int fsi_mg_create(const fsi_mg_params *params, const double *x, const double *y,
         std::vector<double> fx(N[d] + 2, 0.0);
         for (int i = 1; i <= N[d]; ++i)
             fx[i] = (c->x[d][i] - c->xc[d][i - 1]) / (c->xc[d][i] - c->xc[d][i - 1]);
+        std::vector<double> gx(N[d] + 2, 0.0);
+        for (int i = 1; i <= N[d]; ++i) gx[i] = 1.0 - fx[i];
         TRY(c->alloc(&c->d_fx[d], N[d] + 2));
+        TRY(c->alloc(&c->d_gx[d], N[d] + 2));
         CK(cudaMemcpyAsync(c->d_fx[d], fx.data(), (N[d] + 2) * 8, cudaMemcpyHostToDevice, c->s));
+        CK(cudaMemcpyAsync(c->d_gx[d], gx.data(), (N[d] + 2) * 8, cudaMemcpyHostToDevice, c->s));
         CK(cudaStreamSynchronize(c->s));
     }
     c->npgrad = 2 * (size_t)(p.ny + 2) * (p.nz + 2) + 2 * (size_t)(p.nx + 2) * (p.nz + 2) +
@@ -1482,8 +1489,10 @@ static StepArgs step_args(Ctx &c, double dt)
     a.fl = c.L1.fl;
     a.d = c.L1.d;
     a.dt = dt;
+    a.dtinv = 1.0 / dt;   // dtinv = oned/dt (IBM/MAIN.F90:1627)
     for (int d = 0; d < 3; ++d) {
-        a.fx[d] = c.d_fx[d]; a.dxinv[d] = c.d_dxinv[d]; a.dxcinv[d] = c.d_dxcinv[d]; a.dx[d] = c.d_dx[d];
+        a.fx[d] = c.d_fx[d]; a.gx[d] = c.d_gx[d];
+        a.dxinv[d] = c.d_dxinv[d]; a.dxcinv[d] = c.d_dxcinv[d]; a.dx[d] = c.d_dx[d];
     }
     return a;
 }
@@ -1515,7 +1524,11 @@ int fsi_mg_face_vel_rhs(void *handle, int frac_step_type, double dt, const doubl
     }
     a.nlu0 = d_nlu0;
     a.p = d_p;
-    launch_face_vel_rhs(a, frac_step_type == 1, (double *)c.partials, c.nred, (double *)c.result, c.s);
+    if (!c.step_partials) {   // worst case: one CTA per 32 x 8 tile and k
+        c.step_cap = ((c.nx - 1 + 31) / 32) * ((c.ny - 1 + 7) / 8) * (c.nz - 1);
+        TRY(c.alloc(&c.step_partials, (size_t)c.step_cap));
+    }
+    launch_face_vel_rhs(a, frac_step_type == 1, c.step_partials, c.step_cap, (double *)c.result, c.s);
     c.last_fv = a; c.last_fv_vk = (frac_step_type == 1); c.have_fv = true;
     c.launches += (frac_step_type == 1) ? 4 : 3;
     CK(cudaMemcpyAsync(c.h_result, c.result, sizeof(double), cudaMemcpyDeviceToHost, c.s));
@@ -1749,7 +1762,7 @@ int fsi_mg_time_kernel(void *handle, int which, int precision, int reps, double 
         } else if (which == 5) {
             calc_residual(c, p, b, f32 ? c.r32 : nullptr);
         } else if (which == 6 && c.have_fv) {
-            launch_face_vel_rhs(c.last_fv, c.last_fv_vk, (double *)c.partials, c.nred, (double *)c.result, c.s);
+            launch_face_vel_rhs(c.last_fv, c.last_fv_vk, c.step_partials, c.step_cap, (double *)c.result, c.s);
         } else if (which == 7 && c.have_cv) {
             launch_correct_vel(c.last_cv, c.s);
         } else if (which == 8 && c.have_up) {

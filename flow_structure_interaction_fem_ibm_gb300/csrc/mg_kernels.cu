@@ -1277,62 +1277,56 @@ __global__ void __launch_bounds__(TPB) k_fresh_cells(double *p, const uint8_t *f
 // ---------------------------------------------------------------------------
 // Fractional-step operations either side of the pressure solve.  Face index f
 // of axis a is stored at the cell it is the minus face of; face n+1 sits in
-// the plus-side boundary layer.  Every face is read and written by one thread.
+// the plus-side boundary layer.  Every face is written by one thread.
+//
+// FP64 economy (GB300 issues FP64 at 1/64 of the FP32 rate, and these loops
+// are FP64-pipe-bound long before HBM): the reference's mask products
+// x (1 - m) + bc m with m in {0, 1} become selects (equal for finite values),
+// 1 - fx comes from a table (the value the reference forms), dtinv is the
+// host's 1/dt, and each face is interpolated once per cell.
 // ---------------------------------------------------------------------------
 __device__ __forceinline__ double bc_at(const double *bc, long long o) { return bc ? bc[o] : 0.0; }
-__device__ __forceinline__ double fbit(uint8_t f, uint8_t bit) { return (f & bit) ? 1.0 : 0.0; }
 
-// face interpolation of face_vel (IBM/CORE_FRAC_STEP_ROUTINES.F90:80-109): the
-// reference writes face f from cell f-1 (plus side) and then from cell f
-// (minus side), so face f keeps cell f's minus expression and face n+1 cell
-// n's plus expression.
-__device__ __forceinline__ double face_interp_minus(const StepArgs &A, const double *U, int a, int i, long long o,
-                                                    long long s, uint8_t f)
+// Final face value of the minus face of cell t (flat index o) along axis a in
+// face_vel (IBM/CORE_FRAC_STEP_ROUTINES.F90:80-109): the reference writes
+// face f from cell f-1 (plus side) and then from cell f (minus side), so face
+// f keeps cell f's minus expression.  With VANKAN the face correction with p
+// follows (:111-177): face1, then cell f-1's plus mask and cell f's minus mask.
+template <bool VANKAN>
+__device__ __forceinline__ double face_minus(const StepArgs &A, const double *U, int a, int t, long long o,
+                                             long long s, uint8_t f)
 {
-    const double fx = A.fx[a][i], m = fbit(f, fb_minus(a));
-    return (fx * U[o] + (1.0 - fx) * U[o - s]) * (1.0 - m) + bc_at(A.bc[a], o) * m;
-}
-__device__ __forceinline__ double face_interp_last(const StepArgs &A, const double *U, int a, int n, long long o,
-                                                   long long s, uint8_t f)
-{
-    const double fx = A.fx[a][n + 1], m = fbit(f, fb_plus(a));
-    return (fx * U[o + s] + (1.0 - fx) * U[o]) * (1.0 - m) + bc_at(A.bc[a], o) * m;
-}
-// face pressure correction (IBM/CORE_FRAC_STEP_ROUTINES.F90:381-399 and the
-// VAN_KAN branch of face_vel, :111-129): face1/face2 from the old faces, then
-// the plus mask of cell f-1 and the minus mask of cell f, in that order.
-__device__ __forceinline__ double face_corr_minus(const StepArgs &A, double v, int a, int i, long long o, long long s,
-                                                  uint8_t f)
-{
-    const double *P = A.p;
-    const double m = fbit(f, fb_minus(a));
-    v = v - A.dt * ((P[o] - P[o - s]) * A.dxcinv[a][i]) * (1.0 - m);
-    if (i >= 2) {
-        const double pl = fbit(A.fl[o - s], fb_plus(a));
-        v = v * (1.0 - pl) + bc_at(A.bc[a], o - s) * pl;
+    if (f & fb_minus(a)) return bc_at(A.bc[a], o);
+    double v = fma(A.fx[a][t], U[o], A.gx[a][t] * U[o - s]);
+    if (VANKAN) {
+        v = fma(-A.dt, (A.p[o] - A.p[o - s]) * A.dxcinv[a][t], v);
+        if (t >= 2 && (A.fl[o - s] & fb_plus(a))) v = bc_at(A.bc[a], o - s);
     }
-    return v * (1.0 - m) + bc_at(A.bc[a], o) * m;
+    return v;
 }
-__device__ __forceinline__ double face_corr_last(const StepArgs &A, double v, int a, int n, long long o, long long s,
-                                                 uint8_t f)
+// face n+1 from cell n (plus expression, plus mask of cell n)
+template <bool VANKAN>
+__device__ __forceinline__ double face_last(const StepArgs &A, const double *U, int a, int n, long long o,
+                                            long long s, uint8_t f)
+{
+    if (f & fb_plus(a)) return bc_at(A.bc[a], o);
+    double v = fma(A.fx[a][n + 1], U[o + s], A.gx[a][n + 1] * U[o]);
+    if (VANKAN) v = fma(-A.dt, (A.p[o + s] - A.p[o]) * A.dxcinv[a][n + 1], v);
+    return v;
+}
+// cell-centre pressure gradient of correct_vel / face_vel (IBM/CORE_FRAC_STEP_ROUTINES.F90:272-349):
+// pe, pw interpolated to the faces, the cell's own pressure on flagged faces
+__device__ __forceinline__ double cell_pgrad(const StepArgs &A, int a, int t, long long o, long long s, uint8_t f)
 {
     const double *P = A.p;
-    const double m = fbit(f, fb_plus(a));
-    v = v - A.dt * ((P[o + s] - P[o]) * A.dxcinv[a][n + 1]) * (1.0 - m);
-    return v * (1.0 - m) + bc_at(A.bc[a], o) * m;
-}
-// cell-centre pressure gradient of correct_vel / face_vel (IBM/CORE_FRAC_STEP_ROUTINES.F90:272-349)
-__device__ __forceinline__ double cell_pgrad(const StepArgs &A, int a, int i, long long o, long long s, uint8_t f)
-{
-    const double *P = A.p;
-    const double fxm = A.fx[a][i], fxp = A.fx[a][i + 1];
-    const double mm = fbit(f, fb_minus(a)), pp = fbit(f, fb_plus(a));
-    const double pe = (fxp * P[o + s] + (1.0 - fxp) * P[o]) * (1.0 - pp) + P[o] * pp;
-    const double pw = (fxm * P[o] + (1.0 - fxm) * P[o - s]) * (1.0 - mm) + P[o] * mm;
-    return (pe - pw) * A.dxinv[a][i];
+    const double p0 = P[o];
+    const double pe = (f & fb_plus(a)) ? p0 : fma(A.fx[a][t + 1], P[o + s], A.gx[a][t + 1] * p0);
+    const double pw = (f & fb_minus(a)) ? p0 : fma(A.fx[a][t], p0, A.gx[a][t] * P[o - s]);
+    return (pe - pw) * A.dxinv[a][t];
 }
 
-// uTilde = u + dt grad p (1 - iblank), the VAN_KAN predictor of face_vel (IBM/CORE_FRAC_STEP_ROUTINES.F90:36-72)
+// uTilde = u + dt grad p (1 - iblank), the VAN_KAN predictor of face_vel
+// (IBM/CORE_FRAC_STEP_ROUTINES.F90:36-72), one thread per interior cell
 __global__ void __launch_bounds__(TPB) k_vankan_tilde(StepArgs A)
 {
     const Dims &d = A.d;
@@ -1343,61 +1337,93 @@ __global__ void __launch_bounds__(TPB) k_vankan_tilde(StepArgs A)
     cell_of((unsigned)t, (unsigned)n0, (unsigned)n1, idx[0], idx[1], idx[2]);
     const long long o = d.idx(idx[0], idx[1], idx[2]);
     const uint8_t f = A.fl[o];
-    const double blank = (f & FB_IB) ? 0.0 : 1.0;
+    const bool fluid = !(f & FB_IB);
     for (int a = 0; a < 3; ++a) {
         const long long s = stride_of(d, a);
-        A.velo[a][o] = A.vel[a][o] + A.dt * cell_pgrad(A, a, idx[a], o, s, f) * blank;
+        const double u = A.vel[a][o];
+        A.velo[a][o] = fluid ? fma(A.dt, cell_pgrad(A, a, idx[a], o, s, f), u) : u;
     }
 }
 
-// face_vel + rhs_poisson (IBM/CORE_POISSON.F90:155-163, 273-281), one thread
-// per interior cell; each cell recomputes its plus face (the next cell's
-// minus face).  U = vel (NO_VAN_KAN) or the uTilde of k_vankan_tilde; with
-// van_kan the faces also take the pressure correction with p.
+// face_vel + rhs_poisson (IBM/CORE_POISSON.F90:155-163, 273-281).  A CTA of
+// 32 x 8 threads owns a 32 x 8 tile of (i, j) and walks a chunk of k.  Each
+// thread interpolates its cell's minus faces; the x plus face comes from the
+// next lane (shuffle), the y plus face from the next row of the tile (shared
+// memory, double-buffered by k parity), the z plus face is the next
+// iteration's minus face (carried in a register).  The tile's last lane and
+// last row interpolate their plus face themselves.  nlu0 = dtinv div(face)
+// (1 - iblank); the block's share of sum nlu0 dx dy dz goes to partials.
+// Threads past the grid's end run on clamped indices (in bounds) and store nothing.
 template <bool VANKAN>
 __global__ void __launch_bounds__(TPB) k_face_vel_rhs(StepArgs A, double *partials)
 {
     const Dims &d = A.d;
-    const int n0 = d.m[0] - 1, n1 = d.m[1] - 1, n2 = d.m[2] - 1;
-    const long long total = (long long)n0 * n1 * n2;
+    const int nxc = d.m[0] - 1, nyc = d.m[1] - 1, nzc = d.m[2] - 1;
+    const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
+    const int i0 = blockIdx.x * 32 + tx + 1, j0 = blockIdx.y * 8 + ty + 1;
+    const bool act = i0 <= nxc && j0 <= nyc;
+    const int i = min(i0, nxc), j = min(j0, nyc);
+    const int kc = (nzc + (int)gridDim.z - 1) / (int)gridDim.z;
+    const int kb = 1 + (int)blockIdx.z * kc, ke = min(nzc, kb + kc - 1);
+    const long long sx = d.sx, sxy = d.sxy;
+    const double *Ux = VANKAN ? A.velo[0] : A.vel[0];
+    const double *Uy = VANKAN ? A.velo[1] : A.vel[1];
+    const double *Uz = VANKAN ? A.velo[2] : A.vel[2];
+    const double dxi = A.dxinv[0][i], dyi = A.dxinv[1][j], dxdy = A.dx[0][i] * A.dx[1][j];
+    __shared__ double sy[2][8][32];
     double acc = 0.0;
-    for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < total;
-         t += (long long)gridDim.x * blockDim.x) {
-        int idx[3];
-        cell_of((unsigned)t, (unsigned)n0, (unsigned)n1, idx[0], idx[1], idx[2]);
-        const long long o = d.idx(idx[0], idx[1], idx[2]);
+    double fzm = 0.0;
+    if (kb <= ke) {
+        const long long o = d.idx(i, j, kb);
+        fzm = face_minus<VANKAN>(A, Uz, 2, kb, o, sxy, A.fl[o]);
+    }
+    for (int k = kb; k <= ke; ++k) {
+        const long long o = d.idx(i, j, k);
         const uint8_t f = A.fl[o];
-        double term[3];
-        for (int a = 0; a < 3; ++a) {
-            const long long s = stride_of(d, a);
-            const int i = idx[a], n = d.m[a] - 1;
-            const double *U = VANKAN ? A.velo[a] : A.vel[a];
-            double fm = face_interp_minus(A, U, a, i, o, s, f);
-            if (VANKAN) fm = face_corr_minus(A, fm, a, i, o, s, f);
-            double fp;
-            if (i < n) {
-                const uint8_t fn = A.fl[o + s];
-                fp = face_interp_minus(A, U, a, i + 1, o + s, s, fn);
-                if (VANKAN) fp = face_corr_minus(A, fp, a, i + 1, o + s, s, fn);
-            } else {
-                fp = face_interp_last(A, U, a, n, o, s, f);
-                if (VANKAN) fp = face_corr_last(A, fp, a, n, o, s, f);
-                A.face[a][o + s] = fp;
-            }
-            A.face[a][o] = fm;
-            term[a] = (fp - fm) * A.dxinv[a][i];
+        // x
+        const double fxm = face_minus<VANKAN>(A, Ux, 0, i, o, 1, f);
+        const double xn = __shfl_down_sync(0xffffffffu, fxm, 1);
+        double fxp;
+        if (i == nxc) fxp = face_last<VANKAN>(A, Ux, 0, i, o, 1, f);
+        else if (tx < 31) fxp = xn;
+        else fxp = face_minus<VANKAN>(A, Ux, 0, i + 1, o + 1, 1, A.fl[o + 1]);
+        // y
+        const double fym = face_minus<VANKAN>(A, Uy, 1, j, o, sx, f);
+        sy[k & 1][ty][tx] = fym;
+        __syncthreads();
+        double fyp;
+        if (j == nyc) fyp = face_last<VANKAN>(A, Uy, 1, j, o, sx, f);
+        else if (ty < 7) fyp = sy[k & 1][ty + 1][tx];
+        else fyp = face_minus<VANKAN>(A, Uy, 1, j + 1, o + sx, sx, A.fl[o + sx]);
+        // z
+        double fzp;
+        if (k == nzc) fzp = face_last<VANKAN>(A, Uz, 2, k, o, sxy, f);
+        else fzp = face_minus<VANKAN>(A, Uz, 2, k + 1, o + sxy, sxy, A.fl[o + sxy]);
+        double r = (fxp - fxm) * dxi;
+        r = fma(fyp - fym, dyi, r);
+        r = fma(fzp - fzm, A.dxinv[2][k], r);
+        const double nl = (f & FB_IB) ? 0.0 : r * A.dtinv;
+        if (act) {
+            A.face[0][o] = fxm;
+            if (i == nxc) A.face[0][o + 1] = fxp;
+            A.face[1][o] = fym;
+            if (j == nyc) A.face[1][o + sx] = fyp;
+            A.face[2][o] = fzm;
+            if (k == nzc) A.face[2][o + sxy] = fzp;
+            A.nlu0[o] = nl;
+            acc = fma(nl, dxdy * A.dx[2][k], acc);   // nlu0 dx dy dz
         }
-        double r = (1.0 / A.dt) * ((term[0] + term[1]) + term[2]);
-        r = r * ((f & FB_IB) ? 0.0 : 1.0);
-        A.nlu0[o] = r;
-        acc += r * A.dx[0][idx[0]] * A.dx[1][idx[1]] * A.dx[2][idx[2]];
+        fzm = fzp;
     }
     const double tot = block_sum(acc);
-    if (threadIdx.x == 0) partials[blockIdx.x] = tot;
+    if (threadIdx.x == 0) partials[blockIdx.x + gridDim.x * (blockIdx.y + gridDim.y * blockIdx.z)] = tot;
 }
 
 // correct_vel without the ghost-cell velocity interpolation
-// (IBM/CORE_FRAC_STEP_ROUTINES.F90:272-366 cell centres, :381-441 faces)
+// (IBM/CORE_FRAC_STEP_ROUTINES.F90:272-366 cell centres, :381-441 faces):
+// u -= dt grad pPrime (1 - iblank); each face takes face1 of its cell, then the
+// plus mask of the previous cell and its own minus mask (the reference's
+// overwrite order); the last face takes face2 of cell n and its plus mask.
 __global__ void __launch_bounds__(TPB) k_correct_vel(StepArgs A)
 {
     const Dims &d = A.d;
@@ -1408,16 +1434,29 @@ __global__ void __launch_bounds__(TPB) k_correct_vel(StepArgs A)
     cell_of((unsigned)t, (unsigned)n0, (unsigned)n1, idx[0], idx[1], idx[2]);
     const long long o = d.idx(idx[0], idx[1], idx[2]);
     const uint8_t f = A.fl[o];
-    const double blank = (f & FB_IB) ? 0.0 : 1.0;
+    const bool fluid = !(f & FB_IB);
+    const double *P = A.p;
     for (int a = 0; a < 3; ++a) {
         const long long s = stride_of(d, a);
         const int i = idx[a], n = d.m[a] - 1;
-        A.velo[a][o] = A.vel[a][o] - A.dt * cell_pgrad(A, a, i, o, s, f) * blank;
+        const double u = A.vel[a][o];
+        A.velo[a][o] = fluid ? fma(-A.dt, cell_pgrad(A, a, i, o, s, f), u) : u;
         double *F = A.face[a];
-        const double v1 = face_corr_minus(A, F[o], a, i, o, s, f);
-        if (i == n) F[o + s] = face_corr_last(A, F[o + s], a, n, o, s, f);
+        double v1;
+        if (f & fb_minus(a)) v1 = bc_at(A.bc[a], o);
+        else if (i >= 2 && (A.fl[o - s] & fb_plus(a))) v1 = bc_at(A.bc[a], o - s);
+        else v1 = fma(-A.dt, (P[o] - P[o - s]) * A.dxcinv[a][i], F[o]);
+        if (i == n)
+            F[o + s] = (f & fb_plus(a)) ? bc_at(A.bc[a], o)
+                                        : fma(-A.dt, (P[o + s] - P[o]) * A.dxcinv[a][n + 1], F[o + s]);
         F[o] = v1;
     }
+}
+
+__global__ void k_update_pressure(double *p, const double *pPrime, long long n, int van_kan)
+{
+    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t < n) p[t] = van_kan ? p[t] + pPrime[t] : pPrime[t];
 }
 
 // zero the non-interior part of a full (0:nx+1,0:ny+1,0:nz+1) array: planes
@@ -1448,11 +1487,6 @@ __global__ void k_zero_shell(double *a, Dims d)
     }
 }
 
-__global__ void k_update_pressure(double *p, const double *pPrime, long long n, int van_kan)
-{
-    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (t < n) p[t] = van_kan ? p[t] + pPrime[t] : pPrime[t];
-}
 
 // compatibility flux, non-periodic branch (IBM/GCM_GLOBAL_MASS_CONSERVE.F90:290-331)
 struct CompatArgs {
@@ -2027,20 +2061,23 @@ void launch_fresh_cells(double *p, const uint8_t *fl, const uint8_t *fresh, cons
     k_fresh_cells<<<nblk(n), TPB, 0, s>>>(p, fl, fresh, d, three_d ? 1 : 0);
 }
 
-void launch_face_vel_rhs(const StepArgs &a, bool van_kan, double *partials, int nblocks, double *sums,
-                         cudaStream_t s)
+void launch_face_vel_rhs(const StepArgs &a, bool van_kan, double *partials, int cap, double *sums, cudaStream_t s)
 {
-    const long long n = (long long)(a.d.m[0] - 1) * (a.d.m[1] - 1) * (a.d.m[2] - 1);
+    const int nxc = a.d.m[0] - 1, nyc = a.d.m[1] - 1, nzc = a.d.m[2] - 1;
+    const long long n = (long long)nxc * nyc * nzc;
     // nlu0 = 0 outside the interior (the reference zeroes the whole array first)
-    const long long nshell = 3 * a.d.sxy + 3 * a.d.sx * (a.d.m[2] - 1) + 3LL * (a.d.m[1] - 1) * (a.d.m[2] - 1);
+    const long long nshell = 3 * a.d.sxy + 3 * a.d.sx * (nzc) + 3LL * nyc * nzc;
     k_zero_shell<<<nblk(nshell), TPB, 0, s>>>(a.nlu0, a.d);
-    if (van_kan) {
-        k_vankan_tilde<<<nblk(n), TPB, 0, s>>>(a);
-        k_face_vel_rhs<true><<<nblocks, TPB, 0, s>>>(a, partials);
-    } else {
-        k_face_vel_rhs<false><<<nblocks, TPB, 0, s>>>(a, partials);
-    }
-    k_sum_final<<<1, 1024, 0, s>>>(partials, nblocks, 1, sums);
+    if (van_kan) k_vankan_tilde<<<nblk(n), TPB, 0, s>>>(a);
+    // 32 x 8 tiles of (i, j); k split into chunks until the grid covers the
+    // SMs several times over (at most cap blocks: one partial sum each)
+    const int bx = (nxc + 31) / 32, by = (nyc + 7) / 8;
+    int bz = std::max(1, std::min(nzc, (8 * 152 + bx * by - 1) / (bx * by)));
+    bz = std::max(1, std::min(bz, cap / (bx * by)));
+    const dim3 grid(bx, by, bz);
+    if (van_kan) k_face_vel_rhs<true><<<grid, TPB, 0, s>>>(a, partials);
+    else k_face_vel_rhs<false><<<grid, TPB, 0, s>>>(a, partials);
+    k_sum_final<<<1, 1024, 0, s>>>(partials, bx * by * bz, 1, sums);
 }
 
 void launch_correct_vel(const StepArgs &a, cudaStream_t s)

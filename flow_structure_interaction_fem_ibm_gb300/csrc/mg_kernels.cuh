@@ -96,15 +96,14 @@ struct StepArgs {
     double *nlu0;
     const double *p;          // pPrime
     const uint8_t *fl;        // level-1 flag bytes (iblank, face bits)
-    const double *fx[3], *dxinv[3], *dxcinv[3], *dx[3];
+    const double *fx[3], *gx[3], *dxinv[3], *dxcinv[3], *dx[3];   // gx = 1 - fx
     Dims d;
-    double dt;
+    double dt, dtinv;
 };
 // face_vel + rhs_poisson (IBM/CORE_FRAC_STEP_ROUTINES.F90:36-177, IBM/CORE_POISSON.F90:155-163,
 // 273-281; with van_kan, p is the current pressure and velo the uTilde scratch); sums[0]
-// receives sum nlu0 dx dy dz.  nlu0 is zeroed over the whole array first.
-void launch_face_vel_rhs(const StepArgs &a, bool van_kan, double *partials, int nblocks, double *sums,
-                         cudaStream_t s);
+// receives sum nlu0 dx dy dz; partials holds cap doubles.  nlu0 is zero outside the interior.
+void launch_face_vel_rhs(const StepArgs &a, bool van_kan, double *partials, int cap, double *sums, cudaStream_t s);
 // correct_vel cell-centre update and face corrections (IBM/CORE_FRAC_STEP_ROUTINES.F90:244-448,
 // without the ghost-cell velocity interpolation)
 void launch_correct_vel(const StepArgs &a, cudaStream_t s);

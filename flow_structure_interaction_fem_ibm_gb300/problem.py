@@ -233,6 +233,24 @@ def box2d(n: int = 128, seed: int = 1, **kw) -> Problem:
     return Problem(p, x, y, z, geom, nlu0, name=f"box2d_{n}")
 
 
+def box3d(n=128, seed: int = 1, stretch: Optional[float] = 1.5, **kw) -> Problem:
+    """3D box [0,1]^3 without a body, all-Neumann pressure; nlu0 from a seeded
+    N(0,1) cell velocity field (face_vel interpolation), which is compatible
+    (the zero boundary flux telescopes).  ``n`` is an int or (nxc, nyc, nzc)."""
+    nxc, nyc, nzc = (n, n, n) if isinstance(n, int) else n
+    p = default_params(DIM_3D, nxc, nyc, nzc, body=False, **kw)
+    kind = "uniform" if stretch is None else "tanh"
+    x, y, z = make_grid(p.nx, p.ny, p.nz, kind, beta=stretch or 1.5)
+    geom = empty_geometry(p)
+    rng = np.random.Generator(np.random.PCG64(seed))
+    sh = full_shape(p)
+    u, v, w = (np.asfortranarray(rng.standard_normal(sh)) for _ in range(3))
+    nlu0 = face_divergence(p, x, y, z, u, v, w, geom.iblank, geom.flags)
+    remove_fluid_mean(p, x, y, z, nlu0, geom.iblank)
+    tag = "uniform" if stretch is None else f"tanh{stretch}"
+    return Problem(p, x, y, z, geom, nlu0, name=f"box3d_{nxc}x{nyc}x{nzc}_{tag}")
+
+
 def sphere(n=128, seed: int = 2, stretch: Optional[float] = 1.5, radius: float = 0.15, nsub: int = 4,
            kmax: int = 8, **kw) -> Problem:
     """3D box [0,1]^3 with a stationary ghost-cell sphere at the centre.
