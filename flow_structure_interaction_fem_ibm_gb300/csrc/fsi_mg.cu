@@ -122,6 +122,7 @@ struct Ctx {
     double *step_partials = nullptr;   // one partial sum per CTA of face_vel_rhs
     int step_cap = 0;
     double *vtilde = nullptr;   // uTilde, vTilde, wTilde of the VAN_KAN face_vel (allocated on first use)
+    bool coarsest_fp32 = false;   // mixed form: smooth the coarsest level in FP32 too (measurement switch)
     // arguments of the last step calls, replayed by fsi_mg_time_kernel (which 6, 7, 8)
     StepArgs last_fv{}, last_cv{};
     bool have_fv = false, have_cv = false, have_up = false, last_fv_vk = false, last_up_vk = false;
@@ -525,7 +526,7 @@ void mg_cycle(Ctx &c, int d, T *var, const T *rhs, int n, int WF, int &GMM, bool
     const bool gcm = (c.p.boundary_formulation == GCM_METHOD);
     if (n == 1 && gcm) gcm_pressure<T>(c, var);
     if (WF == 1) {
-        if (std::is_same<T, float>::value && n == nlev && n > 1) {
+        if (std::is_same<T, float>::value && n == nlev && n > 1 && !c.coarsest_fp32) {
             // FP64 coarsest-level solve inside the FP32 cycle
             launch_convert_f2d(L.r64, (const float *)rhs, L.d.count(), c.s);
             launch_convert_f2d(L.v64, (const float *)var, L.d.count(), c.s);
@@ -1037,6 +1038,10 @@ int fsi_mg_create(const fsi_mg_params *params, const double *x, const double *y,
     }
     auto c = std::make_unique<Ctx>();
     c->p = p;
+    {   // FSI_MG_COARSEST_FP32=1: FP32 coarsest-level smoothing in the mixed form (A/B measurements)
+        const char *cf = std::getenv("FSI_MG_COARSEST_FP32");
+        c->coarsest_fp32 = cf && std::strcmp(cf, "1") == 0;
+    }
     c->nx = p.nx; c->ny = p.ny; c->nz = p.nz;
     c->nd = (p.ndim == 3) ? 3 : 2;
     CK(cudaStreamCreateWithFlags(&c->s, cudaStreamNonBlocking));
