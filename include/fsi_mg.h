@@ -4,7 +4,7 @@
  * Drop-in boundary for the fractional-step pressure solve of the reference
  * immersed-boundary FSI code.  Each entry point replaces one reference
  * routine and keeps its argument meaning; a Fortran host binds them through
- * ISO_C_BINDING interfaces.
+ * ISO_C_BINDING interfaces (flow_structure_interaction_fem_ibm_gb300/fortran/fsi_mg_shim.F90).
  *
  * Array conventions are the reference's: Fortran column-major, lower bound 0.
  * A full field is REAL(8) (0:nx+1,0:ny+1,0:nz+1); flags are INTEGER(1) over

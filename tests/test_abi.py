@@ -51,3 +51,88 @@ def test_geometry_library_exports():
     g = _native.geometry()
     for n in _native.GEOM_SYMBOLS:
         assert hasattr(g, n)
+
+
+# ---------------------------------------------------------- C host driver --
+import os
+import shutil
+import subprocess
+
+import numpy as np
+import pytest
+
+ROOT = HEADER.parents[1]
+DRIVER_SRC = ROOT / "tests" / "abi_driver" / "fsi_mg_driver.c"
+
+
+def _cc():
+    return shutil.which("gcc") or shutil.which("cc")
+
+
+def test_header_compiles_as_c99_and_cpp():
+    for cmd in ([_cc(), "-std=c99", "-x", "c"], [shutil.which("g++") or "g++", "-std=c++11", "-x", "c++"]):
+        subprocess.run(cmd + ["-Wall", "-Wextra", "-Werror", "-pedantic", "-fsyntax-only", str(HEADER)], check=True)
+
+
+def build_driver(out_dir: Path) -> Path:
+    build_all()
+    lib_dir = _native.solver_lib_path().parent
+    exe = out_dir / "fsi_mg_driver"
+    cuda_lib = Path(os.environ.get("CUDA_HOME", "/usr/local/cuda")) / "lib64"
+    subprocess.run([_cc(), "-std=c99", "-O2", "-Wall", "-Wextra", "-Werror", "-I", str(HEADER.parent),
+                    str(DRIVER_SRC), "-o", str(exe), "-L", str(lib_dir), "-lfsi_mg",
+                    f"-Wl,-rpath,{lib_dir}", f"-Wl,-rpath-link,{cuda_lib}"], check=True)
+    return exe
+
+
+def test_c_driver_builds_against_the_library(tmp_path):
+    assert build_driver(tmp_path).exists()
+
+
+def write_driver_input(path: Path, pr):
+    """The driver's input file: the parameter struct, then every array of the
+    hand-over in the driver's read order (Fortran memory order)."""
+    g = pr.geom
+    f = lambda a, t: np.asarray(a, dtype=t).ravel(order="F").tobytes()
+    with open(path, "wb") as fh:
+        fh.write(bytes(pr.params.to_c()))
+        for c in (pr.x, pr.y, pr.z):
+            fh.write(f(c, np.float64))
+        fh.write(f(g.iblank, np.int8)); fh.write(f(g.ghost, np.int8))
+        for a in g.flags:
+            fh.write(f(a, np.int8))
+        fh.write(np.int32(g.nGhost).tobytes())
+        for a in (g.iG, g.jG, g.kG, g.iCI, g.jCI, g.kCI):
+            fh.write(f(a if g.nGhost else [], np.int32))
+        fh.write(f(g.coeff if g.nGhost else [], np.float64))
+        fh.write(f(g.probe if g.nGhost else [], np.float64))
+        fh.write(f(g.pgrad, np.float64))
+        fh.write(f(pr.nlu0, np.float64))
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("case", ["sphere16_tanh", "box2d_32"])
+def test_c_driver_solves_like_the_python_binding(gpu_built, tmp_path, case):
+    from flow_structure_interaction_fem_ibm_gb300 import problem as P
+    from flow_structure_interaction_fem_ibm_gb300.poisson import solve
+    from tests.helpers import sphere_problem
+    pr = sphere_problem(16, stretch=1.5) if case == "sphere16_tanh" else P.box2d(32, seed=9)
+    pr.params.iterMax_Poisson = 60
+    pr.params.restol_Poisson = 1e-9 * float(np.abs(pr.nlu0).max())
+    exe = build_driver(tmp_path)
+    write_driver_input(tmp_path / "in.bin", pr)
+    subprocess.run([str(exe), str(tmp_path / "in.bin"), str(tmp_path / "out.bin")], check=True)
+    raw = (tmp_path / "out.bin").read_bytes()
+    st, it = np.frombuffer(raw[:8], np.int32)
+    maxres = np.frombuffer(raw[8:16], np.float64)[0]
+    n = int(np.prod(pr.shape))
+    p = np.frombuffer(raw[28:28 + 8 * n], np.float64).reshape(pr.shape, order="F")
+    mean = np.frombuffer(raw[28 + 8 * n:], np.float64)[0]
+    ref = solve(pr)
+    assert (st, it) == (ref["status"], ref["iters"]) and maxres == ref["maxres"]
+    assert np.array_equal(p, ref["p"])
+    from tests.helpers import cell_volumes, interior
+    I = interior(pr)
+    fl = 1.0 - pr.geom.iblank[I]
+    vol = cell_volumes(pr) * fl
+    assert abs(mean - float((ref["p"][I] * vol).sum() / vol.sum())) <= 1e-12 * max(1.0, np.abs(ref["p"]).max())
