@@ -122,7 +122,7 @@ struct Ctx {
     double *step_partials = nullptr;   // one partial sum per CTA of face_vel_rhs
     int step_cap = 0;
     double *vtilde = nullptr;   // uTilde, vTilde, wTilde of the VAN_KAN face_vel (allocated on first use)
-    bool coarsest_fp32 = false;   // mixed form: smooth the coarsest level in FP32 too (measurement switch)
+    bool coarsest_fp32 = true;   // mixed form: the coarsest level is smoothed in FP32 like the others
     // arguments of the last step calls, replayed by fsi_mg_time_kernel (which 6, 7, 8)
     StepArgs last_fv{}, last_cv{};
     bool have_fv = false, have_cv = false, have_up = false, last_fv_vk = false, last_up_vk = false;
@@ -515,7 +515,8 @@ Level &level_of(Ctx &c, int d, int n) { return n == 1 ? c.L1 : c.C[d][n]; }
 
 // MG_X / MG_Y / MG_Z (IBM/CORE_MG.F90:1239-1663) for direction d.  At level 1 the
 // caller passes the level-1 var/rhs; coarse levels use their own arrays.  With
-// mixed precision (T = float) the coarsest level is smoothed in FP64.
+// mixed precision (T = float) the coarsest level can be smoothed in FP64
+// (FSI_MG_COARSEST_FP64=1); by default it runs in FP32 like the other levels.
 template <typename T>
 void mg_cycle(Ctx &c, int d, T *var, const T *rhs, int n, int WF, int &GMM, bool homogeneous)
 {
@@ -1038,9 +1039,9 @@ int fsi_mg_create(const fsi_mg_params *params, const double *x, const double *y,
     }
     auto c = std::make_unique<Ctx>();
     c->p = p;
-    {   // FSI_MG_COARSEST_FP32=1: FP32 coarsest-level smoothing in the mixed form (A/B measurements)
-        const char *cf = std::getenv("FSI_MG_COARSEST_FP32");
-        c->coarsest_fp32 = cf && std::strcmp(cf, "1") == 0;
+    {   // FSI_MG_COARSEST_FP64=1: FP64 coarsest-level smoothing inside the FP32 cycle (A/B measurements)
+        const char *cf = std::getenv("FSI_MG_COARSEST_FP64");
+        c->coarsest_fp32 = !(cf && std::strcmp(cf, "1") == 0);
     }
     c->nx = p.nx; c->ny = p.ny; c->nz = p.nz;
     c->nd = (p.ndim == 3) ? 3 : 2;
@@ -1232,7 +1233,8 @@ int fsi_mg_set_geometry(void *handle, const int8_t *iblank, const int8_t *ghostC
     }
     // line factorisations of every level and direction
     // and the factored partition tables of the FP64 smoother: every level when
-    // the cycle runs in FP64, the coarsest levels (smoothed in FP64) otherwise
+    // the cycle runs in FP64, the coarsest levels when the FP32 cycle smooths
+    // them in FP64 (FSI_MG_COARSEST_FP64=1)
     auto factor = [&](Level &L, bool fp64_level) -> int {
         for (int a = 0; a < c.nd; ++a) {
             FactorArgs<double> fa;
@@ -1250,7 +1252,7 @@ int fsi_mg_set_geometry(void *handle, const int8_t *iblank, const int8_t *ghostC
     const bool all64 = (c.p.precision_mode == 0);
     TRY(factor(c.L1, all64));
     for (int d = 0; d < c.nd; ++d)
-        for (int l = 2; l <= c.nlev[d]; ++l) TRY(factor(c.C[d][l], all64 || l == c.nlev[d]));
+        for (int l = 2; l <= c.nlev[d]; ++l) TRY(factor(c.C[d][l], all64 || (l == c.nlev[d] && !c.coarsest_fp32)));
     // ghost gather list: linear indices in the level-1 layout; the ghost's own
     // stencil entry carries uNormal (0) and is marked -1.
     static const int incI[8] = {0, 0, 1, 1, 0, 0, 1, 1}, incJ[8] = {0, 1, 1, 0, 0, 1, 1, 0},
