@@ -1033,8 +1033,6 @@ int fsi_mg_create(const fsi_mg_params *params, const double *x, const double *y,
     {   // FSI_MG_LINE_KERNEL=thread selects the one-thread-per-line smoother (A/B measurements)
         const char *lk = std::getenv("FSI_MG_LINE_KERNEL");
         set_line_kernel(lk && std::strcmp(lk, "thread") == 0);
-        const char *pd = std::getenv("FSI_MG_PDL");   // FSI_MG_PDL=0: plain stream ordering (A/B)
-        set_pdl(!(pd && std::strcmp(pd, "0") == 0));
         const char *kr = std::getenv("FSI_MG_KRYLOV_INNER_RTOL");
         const double v = kr ? std::atof(kr) : 0.0;
         g_krylov_inner_rtol = (v > 0.0 && v < 1.0) ? v : 1.0e-5;

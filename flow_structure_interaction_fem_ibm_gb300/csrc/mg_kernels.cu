@@ -4,7 +4,6 @@
 
 #include <cfloat>
 #include <mutex>
-#include <utility>
 #include <cooperative_groups.h>
 
 namespace fsimg {
@@ -17,37 +16,6 @@ inline int nblk(long long n, int tpb = TPB)
 {
     long long b = (n + tpb - 1) / tpb;
     return (int)(b < 1 ? 1 : b);
-}
-
-// Programmatic dependent launch: every kernel is launched with programmatic
-// stream serialisation, so the next kernel of the stream (or of the captured
-// graph) is scheduled while the current one drains instead of after it.  Each
-// kernel signals at entry that its dependents may be scheduled, then waits
-// for its predecessor grid to complete (and its memory to be visible) before
-// its first global access.  A kernel launched without the attribute passes the
-// wait at once.
-bool g_pdl = true;
-
-__device__ __forceinline__ void pdl_entry()
-{
-    asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
-    asm volatile("griddepcontrol.wait;" ::: "memory");
-}
-
-template <typename... KArgs, typename... Args>
-inline void launch_k(void (*kernel)(KArgs...), dim3 grid, dim3 block, size_t smem, cudaStream_t s, Args &&...args)
-{
-    cudaLaunchConfig_t cfg = {};
-    cfg.gridDim = grid;
-    cfg.blockDim = block;
-    cfg.dynamicSmemBytes = smem;
-    cfg.stream = s;
-    cudaLaunchAttribute at[1];
-    at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
-    at[0].val.programmaticStreamSerializationAllowed = 1;
-    cfg.attrs = at;
-    cfg.numAttrs = g_pdl ? 1 : 0;
-    cudaLaunchKernelEx(&cfg, kernel, std::forward<Args>(args)...);
 }
 
 template <int DIR> struct Axes;
@@ -89,7 +57,6 @@ __device__ __forceinline__ long long stride_of(const Dims &d, int axis)
 template <typename T, int DIR, bool OMEGA1>
 __global__ void __launch_bounds__(TPB) k_line(LineArgs<T> A)
 {
-    pdl_entry();
     using X = Axes<DIR>;
     const Dims &d = A.d;
     const int nb = d.m[X::b] - 1, nc = d.m[X::c] - 1, L = d.m[X::a] - 1;
@@ -177,7 +144,6 @@ __global__ void __launch_bounds__(TPB) k_line(LineArgs<T> A)
 template <typename T, int DIR, int LM, bool OMEGA1>
 __global__ void __launch_bounds__(TPB) k_line_short(LineArgs<T> A)
 {
-    pdl_entry();
     using X = Axes<DIR>;
     const Dims &d = A.d;
     const int nb = d.m[X::b] - 1, nc = d.m[X::c] - 1, L = d.m[X::a] - 1;
@@ -320,7 +286,6 @@ __device__ __forceinline__ void pcr_step(T &A, T &B, T &C, T &D, T &iB, int lane
 template <typename T, int DIR, int S, bool OMEGA1, bool FULL>
 __global__ void __launch_bounds__(256) k_line_wp(LineArgs<T> A)
 {
-    pdl_entry();
     using X = Axes<DIR>;
     extern __shared__ unsigned char smem_raw[];
     T *sm = reinterpret_cast<T *>(smem_raw);
@@ -544,7 +509,6 @@ template <int S> __host__ __device__ constexpr int wpf_rec() { return 4 * 32 * S
 template <int DIR, int S>
 __global__ void __launch_bounds__(256) k_wpf_setup(FactorArgs<double> A, double *tab)
 {
-    pdl_entry();
     using X = Axes<DIR>;
     const Dims &d = A.d;
     const int nb = d.m[X::b] - 1, nc = d.m[X::c] - 1, L = d.m[X::a] - 1;
@@ -648,7 +612,6 @@ __global__ void __launch_bounds__(256) k_wpf_setup(FactorArgs<double> A, double 
 template <int DIR, int S, int NL, bool OMEGA1>
 __global__ void __launch_bounds__(32 * NL) k_line_fp(LineArgs<double> A)
 {
-    pdl_entry();
     using X = Axes<DIR>;
     extern __shared__ unsigned char smem_raw[];
     double *sm = reinterpret_cast<double *>(smem_raw);
@@ -833,7 +796,6 @@ __global__ void __launch_bounds__(32 * NL) k_line_fp(LineArgs<double> A)
 template <int DIR>
 __global__ void __launch_bounds__(TPB) k_factor(FactorArgs<double> A)
 {
-    pdl_entry();
     using X = Axes<DIR>;
     const Dims &d = A.d;
     const int nb = d.m[X::b] - 1, nc = d.m[X::c] - 1, L = d.m[X::a] - 1;
@@ -908,7 +870,6 @@ __device__ __forceinline__ T cell_residual(const T *__restrict__ v, const T *__r
 template <typename T, int D>
 __global__ void __launch_bounds__(TPB) k_resid_restrict(RestrictArgs<T> A)
 {
-    pdl_entry();
     const Dims &dc = A.dc;
     const int n0 = dc.m[0] - 1, n1 = dc.m[1] - 1, n2 = dc.m[2] - 1;
     long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
@@ -936,7 +897,6 @@ __global__ void __launch_bounds__(TPB) k_resid_restrict(RestrictArgs<T> A)
 template <typename T, int D>
 __global__ void __launch_bounds__(TPB) k_prolong_correct(ProlongArgs<T> A)
 {
-    pdl_entry();
     const Dims &df = A.df;
     const int n0 = df.m[0] - 1, n1 = df.m[1] - 1, n2 = df.m[2] - 1;
     long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
@@ -977,7 +937,6 @@ __global__ void __launch_bounds__(TPB) k_prolong_correct(ProlongArgs<T> A)
 template <typename T>
 __global__ void k_outer_ghost(T *v, Dims d, int s0, int s1, int s2, int s3, int s4, int s5)
 {
-    pdl_entry();
     const int m0 = d.m[0], m1 = d.m[1], m2 = d.m[2];
     const long long fx = (long long)(m1 + 1) * (m2 + 1);
     const long long fy = (long long)(m0 + 1) * (m2 + 1);
@@ -1019,7 +978,6 @@ __global__ void __launch_bounds__(1024) k_ghost_rows(T *v, GhostArgs g, const T 
                                                      double tol, double reltol, int *iters,
                                                      unsigned long long *maxdelta)
 {
-    pdl_entry();
     __shared__ double s_d[32], s_a[32];
     __shared__ double s_res[2];
     const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5, nw = (blockDim.x + 31) >> 5;
@@ -1079,7 +1037,6 @@ __global__ void __cluster_dims__(GHOST_CLUSTER, 1, 1) __launch_bounds__(1024)
     k_ghost_rows_cluster(T *v, GhostArgs g, const T *coeff, T *scratch, int iterMax, double tol, double reltol,
                          int *iters, unsigned long long *maxdelta)
 {
-    pdl_entry();
     namespace cg = cooperative_groups;
     cg::cluster_group cluster = cg::this_cluster();
     __shared__ double s_d[32], s_a[32];
@@ -1146,7 +1103,6 @@ __global__ void __cluster_dims__(GHOST_CLUSTER, 1, 1) __launch_bounds__(1024)
 template <typename T>
 __global__ void k_fill(T *p, long long n, T val)
 {
-    pdl_entry();
     long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (t < n) p[t] = val;
 }
@@ -1166,7 +1122,6 @@ __global__ void __launch_bounds__(TPB) k_calc_residual(const double *p, const do
                                                        const uint8_t *fl, Coef<double> c, Dims d, float *r32,
                                                        double *r64, MaxLoc *partials)
 {
-    pdl_entry();
     const int n0 = d.m[0] - 1, n1 = d.m[1] - 1, n2 = d.m[2] - 1;
     const long long total = (long long)n0 * n1 * n2;
     double best = -1.0;
@@ -1203,7 +1158,6 @@ __global__ void __launch_bounds__(TPB) k_calc_residual(const double *p, const do
 
 __global__ void k_maxloc_final(const MaxLoc *partials, int n, MaxLoc *out)
 {
-    pdl_entry();
     double best = -1.0;
     long long bi = 0x7fffffffffffffffLL;
     for (int t = threadIdx.x; t < n; t += blockDim.x) maxloc_merge(best, bi, partials[t].v, partials[t].i);
@@ -1248,7 +1202,6 @@ __global__ void __launch_bounds__(TPB) k_avg_partial(const double *p, const uint
                                                      const double *dy, const double *dz, Dims d,
                                                      double *partials)
 {
-    pdl_entry();
     // rows (j, k) over blocks, i over threads
     const int n0 = d.m[0] - 1, n1 = d.m[1] - 1, n2 = d.m[2] - 1;
     const int rows = n1 * n2;
@@ -1271,7 +1224,6 @@ __global__ void __launch_bounds__(TPB) k_avg_partial(const double *p, const uint
 
 __global__ void k_sum_final(double *partials, int n, int stride, double *out)
 {
-    pdl_entry();
     // out[c] = sum_t partials[stride*t + c] for c < stride, fixed order per thread then tree
     for (int c = 0; c < stride; ++c) {
         double x = 0.0;
@@ -1284,7 +1236,6 @@ __global__ void k_sum_final(double *partials, int n, int stride, double *out)
 
 __global__ void __launch_bounds__(TPB) k_avg_apply(double *p, const uint8_t *fl, Dims d, const double *sums)
 {
-    pdl_entry();
     // one block per row (j, k); dead cells (iblank = 1) are zeroed (IBM/CORE_POISSON.F90:447-457)
     __shared__ double s_avg;
     if (threadIdx.x == 0) s_avg = sums[0] / sums[1];
@@ -1304,7 +1255,6 @@ __global__ void __launch_bounds__(TPB) k_avg_apply(double *p, const uint8_t *fl,
 __global__ void __launch_bounds__(TPB) k_fresh_cells(double *p, const uint8_t *fl, const uint8_t *fresh, Dims d,
                                                      int three_d)
 {
-    pdl_entry();
     const int n0 = d.m[0] - 1, n1 = d.m[1] - 1, n2 = d.m[2] - 1;
     const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= (long long)n0 * n1 * n2) return;
@@ -1379,7 +1329,6 @@ __device__ __forceinline__ double cell_pgrad(const StepArgs &A, int a, int t, lo
 // (IBM/CORE_FRAC_STEP_ROUTINES.F90:36-72), one thread per interior cell
 __global__ void __launch_bounds__(TPB) k_vankan_tilde(StepArgs A)
 {
-    pdl_entry();
     const Dims &d = A.d;
     const int n0 = d.m[0] - 1, n1 = d.m[1] - 1, n2 = d.m[2] - 1;
     const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
@@ -1408,7 +1357,6 @@ __global__ void __launch_bounds__(TPB) k_vankan_tilde(StepArgs A)
 template <bool VANKAN>
 __global__ void __launch_bounds__(TPB) k_face_vel_rhs(StepArgs A, double *partials)
 {
-    pdl_entry();
     const Dims &d = A.d;
     const int nxc = d.m[0] - 1, nyc = d.m[1] - 1, nzc = d.m[2] - 1;
     const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
@@ -1478,7 +1426,6 @@ __global__ void __launch_bounds__(TPB) k_face_vel_rhs(StepArgs A, double *partia
 // overwrite order); the last face takes face2 of cell n and its plus mask.
 __global__ void __launch_bounds__(TPB) k_correct_vel(StepArgs A)
 {
-    pdl_entry();
     const Dims &d = A.d;
     const int n0 = d.m[0] - 1, n1 = d.m[1] - 1, n2 = d.m[2] - 1;
     const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
@@ -1508,7 +1455,6 @@ __global__ void __launch_bounds__(TPB) k_correct_vel(StepArgs A)
 
 __global__ void k_update_pressure(double *p, const double *pPrime, long long n, int van_kan)
 {
-    pdl_entry();
     const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (t < n) p[t] = van_kan ? p[t] + pPrime[t] : pPrime[t];
 }
@@ -1518,7 +1464,6 @@ __global__ void k_update_pressure(double *p, const double *pPrime, long long n, 
 // i = 0, nx, nx+1 of the interior rows (the interior is written elsewhere)
 __global__ void k_zero_shell(double *a, Dims d)
 {
-    pdl_entry();
     const int nx = d.m[0], ny = d.m[1], nz = d.m[2];
     const long long sx = d.sx, sxy = d.sxy;
     const long long segA = 3 * sxy, segB = 3 * sx * (nz - 1), segC = 3LL * (ny - 1) * (nz - 1);
@@ -1563,7 +1508,6 @@ __device__ __forceinline__ int face_flag(uint8_t f, int axis, int plus, int side
 
 __global__ void __launch_bounds__(TPB) k_compat_partial(CompatArgs A, double *partials)
 {
-    pdl_entry();
     const Dims &d = A.d;
     const int n0 = d.m[0] - 1, n1 = d.m[1] - 1, n2 = d.m[2] - 1;
     const long long total = (long long)n0 * n1 * n2;
@@ -1603,7 +1547,6 @@ __global__ void __launch_bounds__(TPB) k_compat_partial(CompatArgs A, double *pa
 __global__ void k_pgrad_shift(double *pg, long long off, int sa, int sb, const double *flux, double outflow_area,
                               double sign)
 {
-    pdl_entry();
     long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= (long long)sa * sb) return;
     const int a = (int)(t % sa), b = (int)(t / sa);
@@ -1617,7 +1560,6 @@ __global__ void k_pgrad_shift(double *pg, long long off, int sa, int sb, const d
 __global__ void __launch_bounds__(TPB) k_nlw0(double *nlw0, CompatArgs A, const double *dxinv, const double *dyinv,
                                               const double *dzinv)
 {
-    pdl_entry();
     const Dims &d = A.d;
     const int n0 = d.m[0] - 1, n1 = d.m[1] - 1, n2 = d.m[2] - 1;
     const long long total = (long long)n0 * n1 * n2;
@@ -1647,7 +1589,6 @@ __global__ void __launch_bounds__(TPB) k_nlw0(double *nlw0, CompatArgs A, const 
 template <typename T>
 __global__ void __launch_bounds__(TPB) k_apply_op(const T *z, T *w, const uint8_t *fl, Coef<T> c, Dims d)
 {
-    pdl_entry();
     // w = A z on fluid interior cells (the matrix whose residual calc_residual forms), 0 elsewhere
     const int n0 = d.m[0] - 1, n1 = d.m[1] - 1, n2 = d.m[2] - 1;
     const long long total = (long long)n0 * n1 * n2;
@@ -1677,7 +1618,6 @@ struct VecSet { const T *v[8]; int n; };
 template <typename T>
 __global__ void __launch_bounds__(TPB) k_mdot(VecSet<T> V, const T *w, const uint8_t *fl, Dims d, double *partials)
 {
-    pdl_entry();
     const int n0 = d.m[0] - 1, n1 = d.m[1] - 1, n2 = d.m[2] - 1;
     const long long total = (long long)n0 * n1 * n2;
     T acc[8] = {0, 0, 0, 0, 0, 0, 0, 0};
@@ -1701,7 +1641,6 @@ __global__ void __launch_bounds__(TPB) k_mdot(VecSet<T> V, const T *w, const uin
 // out[q] = sum_b partials[b * 8 + q]  (fixed order)
 __global__ void k_mdot_final(const double *partials, int nb, int n, double *out)
 {
-    pdl_entry();
     for (int q = 0; q < n; ++q) {
         double x = 0.0;
         for (int b = threadIdx.x; b < nb; b += blockDim.x) x += partials[(long long)b * 8 + q];
@@ -1715,7 +1654,6 @@ __global__ void k_mdot_final(const double *partials, int nb, int n, double *out)
 template <typename T>
 __global__ void __launch_bounds__(TPB) k_maxpy(T *w, VecSet<T> V, const double *coef, double sign, long long n)
 {
-    pdl_entry();
     // coefficients converted once per block (a per-element FP64 multiply would
     // make this streaming kernel FP64-bound)
     __shared__ T s_cf[8];
@@ -1736,7 +1674,6 @@ __global__ void __launch_bounds__(TPB) k_maxpy(T *w, VecSet<T> V, const double *
 template <typename T, typename S>
 __global__ void k_scale_copy(T *dst, const S *src, const double *nrm2, long long n)
 {
-    pdl_entry();
     // dst = src / sqrt(nrm2[0]), multiplied in the precision of the source
     __shared__ S s_inv;
     if (threadIdx.x == 0) s_inv = (S)(1.0 / sqrt(nrm2[0]));
@@ -1748,19 +1685,16 @@ __global__ void k_scale_copy(T *dst, const S *src, const double *nrm2, long long
 
 __global__ void k_accumulate(double *p, const float *e, long long n)
 {
-    pdl_entry();
     long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (t < n) p[t] = p[t] + (double)e[t];
 }
 __global__ void k_f2d(double *dst, const float *src, long long n)
 {
-    pdl_entry();
     long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (t < n) dst[t] = (double)src[t];
 }
 __global__ void k_d2f(float *dst, const double *src, long long n)
 {
-    pdl_entry();
     long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (t < n) dst[t] = (float)src[t];
 }
@@ -1771,7 +1705,6 @@ __global__ void k_d2f(float *dst, const double *src, long long n)
 // ---------------------------------------------------------------------------
 __global__ void k_coarse_iblank(uint8_t *flc, const uint8_t *flf, Dims dc, Dims df, int D)
 {
-    pdl_entry();
     // coarse iblank = product of the two children along D, interior cells only
     const int n0 = dc.m[0] - 1, n1 = dc.m[1] - 1, n2 = dc.m[2] - 1;
     long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
@@ -1790,7 +1723,6 @@ __global__ void k_coarse_iblank(uint8_t *flc, const uint8_t *flf, Dims dc, Dims 
 
 __global__ void k_coarse_flags(uint8_t *fl, Dims d, int sb0, int sb1, int sb2, int sb3, int sb4, int sb5)
 {
-    pdl_entry();
     // face bit set where the cell is fluid and the neighbour is solid (INT((ib_nb - ib)/2 + 1/2) = 1);
     // outer faces take the side value (bit set for flag value 1).
     const int n0 = d.m[0] - 1, n1 = d.m[1] - 1, n2 = d.m[2] - 1;
@@ -1828,7 +1760,6 @@ __global__ void __launch_bounds__(TPB) k_avg_partial_rows(const double *p, const
                                                           const double *dy, const double *dz, Dims d,
                                                           double *partials)
 {
-    pdl_entry();
     const int n0 = d.m[0] - 1, n1 = d.m[1] - 1;
     const int row = (int)blockIdx.x;
     const int j = 1 + row % n1, k = 1 + row / n1;
@@ -1858,9 +1789,9 @@ void launch_wp_one(const LineArgs<T> &a, long long nlines, cudaStream_t s)
     static const int ax[3] = {0, 1, 2};
     const long long blocks = (nlines + WP_LINES - 1) / WP_LINES;
     if (a.d.m[ax[DIR]] - 1 == 32 * S)
-        launch_k(k_line_wp<T, DIR, S, O1, true>, (unsigned)blocks, 256, wp_smem<T, DIR, S, O1>(), s, a);
+        k_line_wp<T, DIR, S, O1, true><<<(unsigned)blocks, 256, wp_smem<T, DIR, S, O1>(), s>>>(a);
     else
-        launch_k(k_line_wp<T, DIR, S, O1, false>, (unsigned)blocks, 256, wp_smem<T, DIR, S, O1>(), s, a);
+        k_line_wp<T, DIR, S, O1, false><<<(unsigned)blocks, 256, wp_smem<T, DIR, S, O1>(), s>>>(a);
 }
 
 template <typename T, int DIR, int S>
@@ -1932,10 +1863,10 @@ void launch_fp_one(const LineArgs<double> &a, long long nlines, cudaStream_t s)
 {
     if (nlines >= 2048) {
         const long long blocks = (nlines + 7) / 8;
-        launch_k(k_line_fp<DIR, S, 8, O1>, (unsigned)blocks, 256, 2 * 8 * wp_pitch<S>() * sizeof(double), s, a);
+        k_line_fp<DIR, S, 8, O1><<<(unsigned)blocks, 256, 2 * 8 * wp_pitch<S>() * sizeof(double), s>>>(a);
     } else {
         const long long blocks = (nlines + 1) / 2;
-        launch_k(k_line_fp<DIR, S, 2, O1>, (unsigned)blocks, 64, 2 * 2 * wp_pitch<S>() * sizeof(double), s, a);
+        k_line_fp<DIR, S, 2, O1><<<(unsigned)blocks, 64, 2 * 2 * wp_pitch<S>() * sizeof(double), s>>>(a);
     }
 }
 
@@ -1966,7 +1897,7 @@ bool launch_factored<double>(int dir, const LineArgs<double> &a, int L, long lon
 template <int DIR, int S>
 void wpf_setup_one(const FactorArgs<double> &a, double *tab, long long nl, cudaStream_t s)
 {
-    launch_k(k_wpf_setup<DIR, S>, (unsigned)((nl + 7) / 8), 256, 0, s, a, tab);
+    k_wpf_setup<DIR, S><<<(unsigned)((nl + 7) / 8), 256, 0, s>>>(a, tab);
 }
 
 template <int DIR>
@@ -2004,7 +1935,7 @@ void launch_line(int dir, const LineArgs<T> &a, bool omega_one, cudaStream_t s)
     }
     const int g = nblk(n);
     if (!g_line_thread_per_line && L <= 16) {
-#define S_(D, LM, O) launch_k(k_line_short<T, D, LM, O>, g, TPB, 0, s, a)
+#define S_(D, LM, O) k_line_short<T, D, LM, O><<<g, TPB, 0, s>>>(a)
 #define SD_(LM, O) do { if (dir == 0) S_(0, LM, O); else if (dir == 1) S_(1, LM, O); else S_(2, LM, O); } while (0)
         if (omega_one) {
             if (L <= 4) SD_(4, true); else if (L <= 8) SD_(8, true); else SD_(16, true);
@@ -2015,7 +1946,7 @@ void launch_line(int dir, const LineArgs<T> &a, bool omega_one, cudaStream_t s)
 #undef S_
         return;
     }
-#define L_(D, O) launch_k(k_line<T, D, O>, g, TPB, 0, s, a)
+#define L_(D, O) k_line<T, D, O><<<g, TPB, 0, s>>>(a)
     if (omega_one) {
         if (dir == 0) L_(0, true); else if (dir == 1) L_(1, true); else L_(2, true);
     } else {
@@ -2048,27 +1979,27 @@ void launch_factor(int dir, const FactorArgs<double> &a, cudaStream_t s)
 {
     static const int ob[3] = {1, 0, 0}, oc[3] = {2, 2, 1};
     const long long n = (long long)(a.d.m[ob[dir]] - 1) * (a.d.m[oc[dir]] - 1);
-    if (dir == 0) launch_k(k_factor<0>, nblk(n), TPB, 0, s, a);
-    else if (dir == 1) launch_k(k_factor<1>, nblk(n), TPB, 0, s, a);
-    else launch_k(k_factor<2>, nblk(n), TPB, 0, s, a);
+    if (dir == 0) k_factor<0><<<nblk(n), TPB, 0, s>>>(a);
+    else if (dir == 1) k_factor<1><<<nblk(n), TPB, 0, s>>>(a);
+    else k_factor<2><<<nblk(n), TPB, 0, s>>>(a);
 }
 
 template <typename T>
 void launch_resid_restrict(int D, const RestrictArgs<T> &a, cudaStream_t s)
 {
     const long long n = (long long)(a.dc.m[0] - 1) * (a.dc.m[1] - 1) * (a.dc.m[2] - 1);
-    if (D == 0) launch_k(k_resid_restrict<T, 0>, nblk(n), TPB, 0, s, a);
-    else if (D == 1) launch_k(k_resid_restrict<T, 1>, nblk(n), TPB, 0, s, a);
-    else launch_k(k_resid_restrict<T, 2>, nblk(n), TPB, 0, s, a);
+    if (D == 0) k_resid_restrict<T, 0><<<nblk(n), TPB, 0, s>>>(a);
+    else if (D == 1) k_resid_restrict<T, 1><<<nblk(n), TPB, 0, s>>>(a);
+    else k_resid_restrict<T, 2><<<nblk(n), TPB, 0, s>>>(a);
 }
 
 template <typename T>
 void launch_prolong_correct(int D, const ProlongArgs<T> &a, cudaStream_t s)
 {
     const long long n = (long long)(a.df.m[0] - 1) * (a.df.m[1] - 1) * (a.df.m[2] - 1);
-    if (D == 0) launch_k(k_prolong_correct<T, 0>, nblk(n), TPB, 0, s, a);
-    else if (D == 1) launch_k(k_prolong_correct<T, 1>, nblk(n), TPB, 0, s, a);
-    else launch_k(k_prolong_correct<T, 2>, nblk(n), TPB, 0, s, a);
+    if (D == 0) k_prolong_correct<T, 0><<<nblk(n), TPB, 0, s>>>(a);
+    else if (D == 1) k_prolong_correct<T, 1><<<nblk(n), TPB, 0, s>>>(a);
+    else k_prolong_correct<T, 2><<<nblk(n), TPB, 0, s>>>(a);
 }
 
 template <typename T>
@@ -2076,7 +2007,7 @@ void launch_outer_ghost(T *v, const Dims &d, const int sign[6], cudaStream_t s)
 {
     const long long n = 2LL * ((long long)(d.m[1] + 1) * (d.m[2] + 1) + (long long)(d.m[0] + 1) * (d.m[2] + 1) +
                                (long long)(d.m[0] + 1) * (d.m[1] + 1));
-    launch_k(k_outer_ghost<T>, nblk(n), TPB, 0, s, v, d, sign[0], sign[1], sign[2], sign[3], sign[4], sign[5]);
+    k_outer_ghost<T><<<nblk(n), TPB, 0, s>>>(v, d, sign[0], sign[1], sign[2], sign[3], sign[4], sign[5]);
 }
 
 template <typename T>
@@ -2085,7 +2016,7 @@ void launch_ghost_rows(T *v, const GhostArgs &g, const T *coeff, T *scratch, int
 {
     if (g.n <= 0) return;
     if (g.n <= 4096)
-        launch_k(k_ghost_rows<T>, 1, 1024, 0, s, v, g, coeff, scratch, iterMax, tol, reltol, d_iters, d_maxdelta);
+        k_ghost_rows<T><<<1, 1024, 0, s>>>(v, g, coeff, scratch, iterMax, tol, reltol, d_iters, d_maxdelta);
     else
         k_ghost_rows_cluster<T><<<GHOST_CLUSTER, 1024, 0, s>>>(v, g, coeff, scratch, iterMax, tol, reltol, d_iters,
                                                                 d_maxdelta);
@@ -2094,7 +2025,7 @@ void launch_ghost_rows(T *v, const GhostArgs &g, const T *coeff, T *scratch, int
 template <typename T>
 void launch_fill(T *p, long long n, T val, cudaStream_t s)
 {
-    launch_k(k_fill<T>, nblk(n), TPB, 0, s, p, n, val);
+    k_fill<T><<<nblk(n), TPB, 0, s>>>(p, n, val);
 }
 
 int calc_residual_blocks(const Dims &d)
@@ -2109,25 +2040,25 @@ void launch_calc_residual(const double *p, const double *b, const double *nlw0, 
                           const Coef<double> &c, const Dims &d, float *r32_out, MaxLoc *partials, int nblocks,
                           MaxLoc *result, cudaStream_t s, double *r64_out)
 {
-    launch_k(k_calc_residual, nblocks, TPB, 0, s, p, b, nlw0, fl, c, d, r32_out, r64_out, partials);
-    launch_k(k_maxloc_final, 1, 1024, 0, s, partials, nblocks, result);
+    k_calc_residual<<<nblocks, TPB, 0, s>>>(p, b, nlw0, fl, c, d, r32_out, r64_out, partials);
+    k_maxloc_final<<<1, 1024, 0, s>>>(partials, nblocks, result);
 }
 
 void launch_subtract_average(double *p, const uint8_t *fl, const double *dx, const double *dy, const double *dz,
                              const Dims &d, double *partials, int nblocks, cudaStream_t s)
 {
-    launch_k(k_avg_partial, nblocks, TPB, 0, s, p, fl, dx, dy, dz, d, partials);
+    k_avg_partial<<<nblocks, TPB, 0, s>>>(p, fl, dx, dy, dz, d, partials);
     double *sums = partials + 2LL * nblocks;
-    launch_k(k_sum_final, 1, 1024, 0, s, partials, nblocks, 2, sums);
+    k_sum_final<<<1, 1024, 0, s>>>(partials, nblocks, 2, sums);
     const int rows = (d.m[1] - 1) * (d.m[2] - 1);
-    launch_k(k_avg_apply, rows, TPB, 0, s, p, fl, d, sums);
+    k_avg_apply<<<rows, TPB, 0, s>>>(p, fl, d, sums);
 }
 
 void launch_fresh_cells(double *p, const uint8_t *fl, const uint8_t *fresh, const Dims &d, bool three_d,
                         cudaStream_t s)
 {
     const long long n = (long long)(d.m[0] - 1) * (d.m[1] - 1) * (d.m[2] - 1);
-    launch_k(k_fresh_cells, nblk(n), TPB, 0, s, p, fl, fresh, d, three_d ? 1 : 0);
+    k_fresh_cells<<<nblk(n), TPB, 0, s>>>(p, fl, fresh, d, three_d ? 1 : 0);
 }
 
 void launch_face_vel_rhs(const StepArgs &a, bool van_kan, double *partials, int cap, double *sums, cudaStream_t s)
@@ -2136,28 +2067,28 @@ void launch_face_vel_rhs(const StepArgs &a, bool van_kan, double *partials, int 
     const long long n = (long long)nxc * nyc * nzc;
     // nlu0 = 0 outside the interior (the reference zeroes the whole array first)
     const long long nshell = 3 * a.d.sxy + 3 * a.d.sx * (nzc) + 3LL * nyc * nzc;
-    launch_k(k_zero_shell, nblk(nshell), TPB, 0, s, a.nlu0, a.d);
-    if (van_kan) launch_k(k_vankan_tilde, nblk(n), TPB, 0, s, a);
+    k_zero_shell<<<nblk(nshell), TPB, 0, s>>>(a.nlu0, a.d);
+    if (van_kan) k_vankan_tilde<<<nblk(n), TPB, 0, s>>>(a);
     // 32 x 8 tiles of (i, j); k split into chunks until the grid covers the
     // SMs several times over (at most cap blocks: one partial sum each)
     const int bx = (nxc + 31) / 32, by = (nyc + 7) / 8;
     int bz = std::max(1, std::min(nzc, (8 * 152 + bx * by - 1) / (bx * by)));
     bz = std::max(1, std::min(bz, cap / (bx * by)));
     const dim3 grid(bx, by, bz);
-    if (van_kan) launch_k(k_face_vel_rhs<true>, grid, TPB, 0, s, a, partials);
-    else launch_k(k_face_vel_rhs<false>, grid, TPB, 0, s, a, partials);
-    launch_k(k_sum_final, 1, 1024, 0, s, partials, bx * by * bz, 1, sums);
+    if (van_kan) k_face_vel_rhs<true><<<grid, TPB, 0, s>>>(a, partials);
+    else k_face_vel_rhs<false><<<grid, TPB, 0, s>>>(a, partials);
+    k_sum_final<<<1, 1024, 0, s>>>(partials, bx * by * bz, 1, sums);
 }
 
 void launch_correct_vel(const StepArgs &a, cudaStream_t s)
 {
     const long long n = (long long)(a.d.m[0] - 1) * (a.d.m[1] - 1) * (a.d.m[2] - 1);
-    launch_k(k_correct_vel, nblk(n), TPB, 0, s, a);
+    k_correct_vel<<<nblk(n), TPB, 0, s>>>(a);
 }
 
 void launch_update_pressure(double *p, const double *pPrime, long long n, bool van_kan, cudaStream_t s)
 {
-    launch_k(k_update_pressure, nblk(n), TPB, 0, s, p, pPrime, n, van_kan ? 1 : 0);
+    k_update_pressure<<<nblk(n), TPB, 0, s>>>(p, pPrime, n, van_kan ? 1 : 0);
 }
 
 static CompatArgs make_compat(const double *p, const uint8_t *fl, const double *pg, const double *dx,
@@ -2182,9 +2113,9 @@ void launch_compat(const double *p, const uint8_t *fl, const double *pg, const d
                    const int bc_zero_grad[6], double outflow_area, int nx, int ny, int nz, cudaStream_t s)
 {
     CompatArgs A = make_compat(p, fl, pg, dx, dy, dz, dxcinv, dycinv, dzcinv, side_flag, d, nx, ny, nz);
-    launch_k(k_compat_partial, nblocks, TPB, 0, s, A, partials);
+    k_compat_partial<<<nblocks, TPB, 0, s>>>(A, partials);
     double *flux = partials + nblocks;
-    launch_k(k_sum_final, 1, 1024, 0, s, partials, nblocks, 1, flux);
+    k_sum_final<<<1, 1024, 0, s>>>(partials, nblocks, 1, flux);
     const long long px = (long long)(ny + 2) * (nz + 2), py = (long long)(nx + 2) * (nz + 2),
                     pz = (long long)(nx + 2) * (ny + 2);
     const long long sizes[6] = {px, px, py, py, pz, pz};
@@ -2193,7 +2124,7 @@ void launch_compat(const double *p, const uint8_t *fl, const double *pg, const d
     const double signs[6] = {-1.0, 1.0, -1.0, 1.0, -1.0, 1.0};
     for (int q = 0; q < 6; ++q)
         if (bc_zero_grad[q])
-            launch_k(k_pgrad_shift, nblk(sizes[q]), TPB, 0, s, pgrad, A.off[q], sa[q], sb[q], flux, outflow_area, signs[q]);
+            k_pgrad_shift<<<nblk(sizes[q]), TPB, 0, s>>>(pgrad, A.off[q], sa[q], sb[q], flux, outflow_area, signs[q]);
 }
 
 void launch_nlw0(double *nlw0, const uint8_t *fl, const int side_flag[6], const double *pgrad, const double *dxinv,
@@ -2202,14 +2133,14 @@ void launch_nlw0(double *nlw0, const uint8_t *fl, const int side_flag[6], const 
     CompatArgs A = make_compat(nullptr, fl, pgrad, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, side_flag,
                                d, nx, ny, nz);
     const long long n = (long long)(d.m[0] - 1) * (d.m[1] - 1) * (d.m[2] - 1);
-    launch_k(k_nlw0, nblk(n), TPB, 0, s, nlw0, A, dxinv, dyinv, dzinv);
+    k_nlw0<<<nblk(n), TPB, 0, s>>>(nlw0, A, dxinv, dyinv, dzinv);
 }
 
 template <typename T>
 void launch_apply_op(const T *z, T *w, const uint8_t *fl, const Coef<T> &c, const Dims &d, cudaStream_t s)
 {
     const long long n = (long long)(d.m[0] - 1) * (d.m[1] - 1) * (d.m[2] - 1);
-    launch_k(k_apply_op<T>, nblk(n), TPB, 0, s, z, w, fl, c, d);
+    k_apply_op<T><<<nblk(n), TPB, 0, s>>>(z, w, fl, c, d);
 }
 
 template <typename T>
@@ -2220,8 +2151,8 @@ void launch_mdot(const T *const *V, int nv, const T *w, const uint8_t *fl, const
         VecSet<T> vs;
         vs.n = (nv - q0 < 8) ? nv - q0 : 8;
         for (int q = 0; q < 8; ++q) vs.v[q] = (q < vs.n) ? V[q0 + q] : nullptr;
-        launch_k(k_mdot<T>, nblocks, TPB, 0, s, vs, w, fl, d, partials);
-        launch_k(k_mdot_final, 1, 1024, 0, s, partials, nblocks, vs.n, out + q0);
+        k_mdot<T><<<nblocks, TPB, 0, s>>>(vs, w, fl, d, partials);
+        k_mdot_final<<<1, 1024, 0, s>>>(partials, nblocks, vs.n, out + q0);
     }
 }
 
@@ -2232,14 +2163,14 @@ void launch_maxpy(T *w, const T *const *V, int nv, const double *coef, double si
         VecSet<T> vs;
         vs.n = (nv - q0 < 8) ? nv - q0 : 8;
         for (int q = 0; q < 8; ++q) vs.v[q] = (q < vs.n) ? V[q0 + q] : nullptr;
-        launch_k(k_maxpy<T>, nblk(n), TPB, 0, s, w, vs, coef + q0, sign, n);
+        k_maxpy<T><<<nblk(n), TPB, 0, s>>>(w, vs, coef + q0, sign, n);
     }
 }
 
 template <typename T, typename S>
 void launch_scale_copy(T *dst, const S *src, const double *nrm2, long long n, cudaStream_t s)
 {
-    launch_k(k_scale_copy<T, S>, nblk(n), TPB, 0, s, dst, src, nrm2, n);
+    k_scale_copy<T, S><<<nblk(n), TPB, 0, s>>>(dst, src, nrm2, n);
 }
 
 template void launch_apply_op<double>(const double *, double *, const uint8_t *, const Coef<double> &, const Dims &,
@@ -2260,27 +2191,27 @@ template void launch_scale_copy<float, double>(float *, const double *, const do
 
 void launch_accumulate(double *p, const float *e, long long n, cudaStream_t s)
 {
-    launch_k(k_accumulate, nblk(n), TPB, 0, s, p, e, n);
+    k_accumulate<<<nblk(n), TPB, 0, s>>>(p, e, n);
 }
 void launch_convert_f2d(double *dst, const float *src, long long n, cudaStream_t s)
 {
-    launch_k(k_f2d, nblk(n), TPB, 0, s, dst, src, n);
+    k_f2d<<<nblk(n), TPB, 0, s>>>(dst, src, n);
 }
 void launch_convert_d2f(float *dst, const double *src, long long n, cudaStream_t s)
 {
-    launch_k(k_d2f, nblk(n), TPB, 0, s, dst, src, n);
+    k_d2f<<<nblk(n), TPB, 0, s>>>(dst, src, n);
 }
 
 void launch_coarse_iblank(uint8_t *fl_c, const uint8_t *fl_f, const Dims &dc, const Dims &df, int D,
                           cudaStream_t s)
 {
-    launch_k(k_coarse_iblank, nblk(dc.count()), TPB, 0, s, fl_c, fl_f, dc, df, D);
+    k_coarse_iblank<<<nblk(dc.count()), TPB, 0, s>>>(fl_c, fl_f, dc, df, D);
 }
 
 void launch_coarse_flags(uint8_t *fl, const Dims &d, const int sb[6], cudaStream_t s)
 {
     const long long n = (long long)(d.m[0] - 1) * (d.m[1] - 1) * (d.m[2] - 1);
-    launch_k(k_coarse_flags, nblk(n), TPB, 0, s, fl, d, sb[0], sb[1], sb[2], sb[3], sb[4], sb[5]);
+    k_coarse_flags<<<nblk(n), TPB, 0, s>>>(fl, d, sb[0], sb[1], sb[2], sb[3], sb[4], sb[5]);
 }
 
 cudaError_t init_kernels()
@@ -2300,7 +2231,6 @@ cudaError_t init_kernels()
 }
 
 void set_line_kernel(int thread_per_line) { g_line_thread_per_line = thread_per_line != 0; }
-void set_pdl(int on) { g_pdl = on != 0; }
 
 // explicit instantiations
 template void launch_line<double>(int, const LineArgs<double> &, bool, cudaStream_t);
@@ -2350,9 +2280,9 @@ cudaError_t launch_subtract_average_noalloc(double *p, const uint8_t *fl, const 
     cudaError_t e = noalloc_scratch(&scr);
     if (e != cudaSuccess) return e;
     double *sums = scr + 2 * NOALLOC_MAX_ROWS;
-    launch_k(k_avg_partial_rows, rows, TPB, 0, s, p, fl, dx, dy, dz, d, scr);
-    launch_k(k_sum_final, 1, 1024, 0, s, scr, rows, 2, sums);
-    launch_k(k_avg_apply, rows, TPB, 0, s, p, fl, d, sums);
+    k_avg_partial_rows<<<rows, TPB, 0, s>>>(p, fl, dx, dy, dz, d, scr);
+    k_sum_final<<<1, 1024, 0, s>>>(scr, rows, 2, sums);
+    k_avg_apply<<<rows, TPB, 0, s>>>(p, fl, d, sums);
     return cudaGetLastError();
 }
 

@@ -114,8 +114,6 @@ void launch_update_pressure(double *p, const double *pPrime, long long n, bool v
 cudaError_t init_kernels();
 // 0: warp-per-line partition solver (default, lines up to 512 cells), 1: one thread per line
 void set_line_kernel(int thread_per_line);
-// programmatic dependent launch of every kernel (default on)
-void set_pdl(int on);
 
 // ---- launchers (all asynchronous on the given stream) ----
 template <typename T>
