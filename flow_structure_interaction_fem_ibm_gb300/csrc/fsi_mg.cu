@@ -1497,6 +1497,7 @@ static StepArgs step_args(Ctx &c, double dt)
     a.d = c.L1.d;
     a.dt = dt;
     a.dtinv = 1.0 / dt;   // dtinv = oned/dt (IBM/MAIN.F90:1627)
+    a.gcm = (c.p.boundary_formulation == GCM_METHOD) ? 1 : 0;
     for (int d = 0; d < 3; ++d) {
         a.fx[d] = c.d_fx[d]; a.gx[d] = c.d_gx[d];
         a.dxinv[d] = c.d_dxinv[d]; a.dxcinv[d] = c.d_dxcinv[d]; a.dx[d] = c.d_dx[d];

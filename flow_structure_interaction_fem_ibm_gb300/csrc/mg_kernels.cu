@@ -1287,31 +1287,52 @@ __global__ void __launch_bounds__(TPB) k_fresh_cells(double *p, const uint8_t *f
 // ---------------------------------------------------------------------------
 __device__ __forceinline__ double bc_at(const double *bc, long long o) { return bc ? bc[o] : 0.0; }
 
-// Final face value of the minus face of cell t (flat index o) along axis a in
-// face_vel (IBM/CORE_FRAC_STEP_ROUTINES.F90:80-109): the reference writes
-// face f from cell f-1 (plus side) and then from cell f (minus side), so face
-// f keeps cell f's minus expression.  With VANKAN the face correction with p
-// follows (:111-177): face1, then cell f-1's plus mask and cell f's minus mask.
+// dead cell: blanked and not a ghost cell (GCM_set_face_vel_body zeroes its faces)
+__device__ __forceinline__ bool dead_cell(uint8_t f) { return (f & FB_IB) && !(f & FB_GM); }
+
+// Final value of face t of axis a (the minus face of cell t at flat index o)
+// in face_vel (IBM/CORE_FRAC_STEP_ROUTINES.F90:80-240).  The reference writes
+// face f from cell f-1 (plus side) and then from cell f (minus side), so the
+// interpolation keeps cell f's minus expression; with VANKAN the pressure
+// correction with p follows (:111-177); both branches then apply cell f-1's
+// plus mask and cell f's minus mask (:178-195), so a face is bc(f) if
+// ium(f), else bc(f-1) if iup(f-1), else the interpolated (and corrected)
+// value.  With GCM, VAN_KAN re-interpolates the faces of ghost cells from u
+// itself (:197-221) and GCM_set_face_vel_body zeroes the faces of dead cells.
+// Cell 0 lies outside the reference's loops, so face 1 has no previous cell.
 template <bool VANKAN>
 __device__ __forceinline__ double face_minus(const StepArgs &A, const double *U, int a, int t, long long o,
                                              long long s, uint8_t f)
 {
-    if (f & fb_minus(a)) return bc_at(A.bc[a], o);
-    double v = fma(A.fx[a][t], U[o], A.gx[a][t] * U[o - s]);
-    if (VANKAN) {
-        v = fma(-A.dt, (A.p[o] - A.p[o - s]) * A.dxcinv[a][t], v);
-        if (t >= 2 && (A.fl[o - s] & fb_plus(a))) v = bc_at(A.bc[a], o - s);
+    const uint8_t fp = (t >= 2) ? A.fl[o - s] : (uint8_t)0;
+    double v;
+    if (f & fb_minus(a)) v = bc_at(A.bc[a], o);
+    else if (fp & fb_plus(a)) v = bc_at(A.bc[a], o - s);
+    else {
+        v = fma(A.fx[a][t], U[o], A.gx[a][t] * U[o - s]);
+        if (VANKAN) v = fma(-A.dt, (A.p[o] - A.p[o - s]) * A.dxcinv[a][t], v);
+    }
+    if (A.gcm) {
+        if (VANKAN && ((f | fp) & FB_GM)) v = fma(A.fx[a][t], A.vel[a][o], A.gx[a][t] * A.vel[a][o - s]);
+        if (dead_cell(f) || dead_cell(fp)) v = 0.0;
     }
     return v;
 }
-// face n+1 from cell n (plus expression, plus mask of cell n)
+// face n+1 from cell n (plus expression, plus mask of cell n; ghost / dead cell n with GCM)
 template <bool VANKAN>
 __device__ __forceinline__ double face_last(const StepArgs &A, const double *U, int a, int n, long long o,
                                             long long s, uint8_t f)
 {
-    if (f & fb_plus(a)) return bc_at(A.bc[a], o);
-    double v = fma(A.fx[a][n + 1], U[o + s], A.gx[a][n + 1] * U[o]);
-    if (VANKAN) v = fma(-A.dt, (A.p[o + s] - A.p[o]) * A.dxcinv[a][n + 1], v);
+    double v;
+    if (f & fb_plus(a)) v = bc_at(A.bc[a], o);
+    else {
+        v = fma(A.fx[a][n + 1], U[o + s], A.gx[a][n + 1] * U[o]);
+        if (VANKAN) v = fma(-A.dt, (A.p[o + s] - A.p[o]) * A.dxcinv[a][n + 1], v);
+    }
+    if (A.gcm) {
+        if (VANKAN && (f & FB_GM)) v = fma(A.fx[a][n + 1], A.vel[a][o + s], A.gx[a][n + 1] * A.vel[a][o]);
+        if (dead_cell(f)) v = 0.0;
+    }
     return v;
 }
 // cell-centre pressure gradient of correct_vel / face_vel (IBM/CORE_FRAC_STEP_ROUTINES.F90:272-349):
@@ -1420,10 +1441,11 @@ __global__ void __launch_bounds__(TPB) k_face_vel_rhs(StepArgs A, double *partia
 }
 
 // correct_vel without the ghost-cell velocity interpolation
-// (IBM/CORE_FRAC_STEP_ROUTINES.F90:272-366 cell centres, :381-441 faces):
-// u -= dt grad pPrime (1 - iblank); each face takes face1 of its cell, then the
-// plus mask of the previous cell and its own minus mask (the reference's
-// overwrite order); the last face takes face2 of cell n and its plus mask.
+// (IBM/CORE_FRAC_STEP_ROUTINES.F90:272-366 cell centres, :381-441 faces,
+// :446 GCM_set_face_vel_body): u -= dt grad pPrime (1 - iblank); each face
+// takes face1 of its cell, then the plus mask of the previous cell and its own
+// minus mask (the reference's overwrite order); the last face takes face2 of
+// cell n and its plus mask; with GCM the faces of dead cells are zero.
 __global__ void __launch_bounds__(TPB) k_correct_vel(StepArgs A)
 {
     const Dims &d = A.d;
@@ -1442,13 +1464,18 @@ __global__ void __launch_bounds__(TPB) k_correct_vel(StepArgs A)
         const double u = A.vel[a][o];
         A.velo[a][o] = fluid ? fma(-A.dt, cell_pgrad(A, a, i, o, s, f), u) : u;
         double *F = A.face[a];
+        const uint8_t fp = (i >= 2) ? A.fl[o - s] : (uint8_t)0;
         double v1;
         if (f & fb_minus(a)) v1 = bc_at(A.bc[a], o);
-        else if (i >= 2 && (A.fl[o - s] & fb_plus(a))) v1 = bc_at(A.bc[a], o - s);
+        else if (fp & fb_plus(a)) v1 = bc_at(A.bc[a], o - s);
         else v1 = fma(-A.dt, (P[o] - P[o - s]) * A.dxcinv[a][i], F[o]);
-        if (i == n)
-            F[o + s] = (f & fb_plus(a)) ? bc_at(A.bc[a], o)
-                                        : fma(-A.dt, (P[o + s] - P[o]) * A.dxcinv[a][n + 1], F[o + s]);
+        if (A.gcm && (dead_cell(f) || dead_cell(fp))) v1 = 0.0;
+        if (i == n) {
+            double v2 = (f & fb_plus(a)) ? bc_at(A.bc[a], o)
+                                         : fma(-A.dt, (P[o + s] - P[o]) * A.dxcinv[a][n + 1], F[o + s]);
+            if (A.gcm && dead_cell(f)) v2 = 0.0;
+            F[o + s] = v2;
+        }
         F[o] = v1;
     }
 }

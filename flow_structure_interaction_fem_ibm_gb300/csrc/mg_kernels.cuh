@@ -99,6 +99,7 @@ struct StepArgs {
     const double *fx[3], *gx[3], *dxinv[3], *dxcinv[3], *dx[3];   // gx = 1 - fx
     Dims d;
     double dt, dtinv;
+    int gcm;                  // boundary_formulation == GCM_METHOD
 };
 // face_vel + rhs_poisson (IBM/CORE_FRAC_STEP_ROUTINES.F90:36-177, IBM/CORE_POISSON.F90:155-163,
 // 273-281; with van_kan, p is the current pressure and velo the uTilde scratch); sums[0]

@@ -146,22 +146,43 @@ def body_geometry(p: SolverParams, x, y, z, verts, tris, probe_length_normalized
 
 def face_divergence(p: SolverParams, x, y, z, u, v, w, iblank, flags, dt: float = 1.0):
     """nlu0 = dtinv * div(face velocity) * (1 - iblank) with face velocities from
-    the face_vel interpolation (IBM/CORE_FRAC_STEP_ROUTINES.F90:80-109, zero
-    boundary velocity on flagged faces) and rhs_poisson (IBM/CORE_POISSON.F90:
-    155-163).  u, v, w are cell-centred (0:nx+1,...) arrays."""
+    the face_vel interpolation and masks (IBM/CORE_FRAC_STEP_ROUTINES.F90:80-109,
+    178-195: zero boundary velocity on a face flagged from either side) and
+    rhs_poisson (IBM/CORE_POISSON.F90:155-163).  u, v, w are cell-centred
+    (0:nx+1,...) arrays."""
     mx, my, mz = Metrics(x), Metrics(y), Metrics(z)
     nxc, nyc, nzc = p.nx - 1, p.ny - 1, p.nz - 1
     I = slice(1, nxc + 1); J = slice(1, nyc + 1); K = slice(1, nzc + 1)
     ium, iup, jum, jup, kum, kup = [f[I, J, K].astype(np.float64) for f in flags]
     fx, fy, fz = mx.fx, my.fx, mz.fx
-    # face values on the + and - faces of each interior cell
-    fu_p = (fx[2:nxc + 2, None, None] * u[2:nxc + 2, J, K] + (1 - fx[2:nxc + 2, None, None]) * u[I, J, K]) * (1 - iup)
-    fu_m = (fx[1:nxc + 1, None, None] * u[I, J, K] + (1 - fx[1:nxc + 1, None, None]) * u[0:nxc, J, K]) * (1 - ium)
-    fv_p = (fy[None, 2:nyc + 2, None] * v[I, 2:nyc + 2, K] + (1 - fy[None, 2:nyc + 2, None]) * v[I, J, K]) * (1 - jup)
-    fv_m = (fy[None, 1:nyc + 1, None] * v[I, J, K] + (1 - fy[None, 1:nyc + 1, None]) * v[I, 0:nyc, K]) * (1 - jum)
+
+    def shifted(m, ax, step):
+        # m of the neighbouring cell along ax (step -1: previous, +1: next); 0 past the interior
+        out = np.zeros_like(m)
+        src = [slice(None)] * 3
+        dst = [slice(None)] * 3
+        if step < 0:
+            src[ax], dst[ax] = slice(0, -1), slice(1, None)
+        else:
+            src[ax], dst[ax] = slice(1, None), slice(0, -1)
+        out[tuple(dst)] = m[tuple(src)]
+        return out
+
+    # face values on the + and - faces of each interior cell: a face is zero
+    # (wall) when flagged from either side, the reference's final masks
+    fu_p = (fx[2:nxc + 2, None, None] * u[2:nxc + 2, J, K] + (1 - fx[2:nxc + 2, None, None]) * u[I, J, K]) \
+        * (1 - iup) * (1 - shifted(ium, 0, +1))
+    fu_m = (fx[1:nxc + 1, None, None] * u[I, J, K] + (1 - fx[1:nxc + 1, None, None]) * u[0:nxc, J, K]) \
+        * (1 - ium) * (1 - shifted(iup, 0, -1))
+    fv_p = (fy[None, 2:nyc + 2, None] * v[I, 2:nyc + 2, K] + (1 - fy[None, 2:nyc + 2, None]) * v[I, J, K]) \
+        * (1 - jup) * (1 - shifted(jum, 1, +1))
+    fv_m = (fy[None, 1:nyc + 1, None] * v[I, J, K] + (1 - fy[None, 1:nyc + 1, None]) * v[I, 0:nyc, K]) \
+        * (1 - jum) * (1 - shifted(jup, 1, -1))
     if p.ndim == DIM_3D:
-        fw_p = (fz[None, None, 2:nzc + 2] * w[I, J, 2:nzc + 2] + (1 - fz[None, None, 2:nzc + 2]) * w[I, J, K]) * (1 - kup)
-        fw_m = (fz[None, None, 1:nzc + 1] * w[I, J, K] + (1 - fz[None, None, 1:nzc + 1]) * w[I, J, 0:nzc]) * (1 - kum)
+        fw_p = (fz[None, None, 2:nzc + 2] * w[I, J, 2:nzc + 2] + (1 - fz[None, None, 2:nzc + 2]) * w[I, J, K]) \
+            * (1 - kup) * (1 - shifted(kum, 2, +1))
+        fw_m = (fz[None, None, 1:nzc + 1] * w[I, J, K] + (1 - fz[None, None, 1:nzc + 1]) * w[I, J, 0:nzc]) \
+            * (1 - kum) * (1 - shifted(kup, 2, -1))
     else:
         fw_p = fw_m = 0.0
     div = ((fu_p - fu_m) * mx.dxinv[1:nxc + 1, None, None] + (fv_p - fv_m) * my.dxinv[None, 1:nyc + 1, None]

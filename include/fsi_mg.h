@@ -143,9 +143,10 @@ int fsi_mg_correct_pressure(void *handle, double *pPrime, double *nlw0_out);
  * non-hybrid rhs_poisson (IBM/CORE_POISSON.F90:123-417): face velocities from
  * u, v, w (frac_step_type 0, NO_VAN_KAN) or from uTilde = u + dt grad p with
  * the face pressure correction (1, VAN_KAN; d_p is then the current
- * pressure), then nlu0 = div(face)/dt (1 - iblank), zero outside the
- * interior; sum OUT (may be NULL) = sum nlu0 dx dy dz in a fixed order.  The
- * ghost-cell face values of GCM_set_face_vel_body stay with the caller. */
+ * pressure), the boundary masks, and with boundary_formulation GCM the
+ * VAN_KAN ghost-cell faces and GCM_set_face_vel_body; then nlu0 =
+ * div(face)/dt (1 - iblank), zero outside the interior; sum OUT (may be NULL)
+ * = sum nlu0 dx dy dz in a fixed order. */
 int fsi_mg_face_vel_rhs(void *handle, int frac_step_type, double dt, const double *d_u, const double *d_v,
                         const double *d_w, const double *d_p, const double *d_bcxu, const double *d_bcyv,
                         const double *d_bczw, double *d_face_u, double *d_face_v, double *d_face_w, double *d_nlu0,
@@ -153,9 +154,10 @@ int fsi_mg_face_vel_rhs(void *handle, int frac_step_type, double dt, const doubl
 
 /* correct_vel (IBM/CORE_FRAC_STEP_ROUTINES.F90:244-448) without periodic
  * sides and without the ghost-cell velocity interpolation
- * (GCM_vel_set_bc_internal) and GCM_set_face_vel_body, which stay with the
- * caller: u, v, w -= dt grad pPrime (1 - iblank) and the face corrections in
- * the reference's overwrite order (INOUT d_u..d_w, d_face_u..d_face_w). */
+ * (GCM_vel_set_bc_internal, which stays with the caller): u, v, w -= dt grad
+ * pPrime (1 - iblank), the face corrections in the reference's overwrite
+ * order and, with GCM, GCM_set_face_vel_body (INOUT d_u..d_w,
+ * d_face_u..d_face_w). */
 int fsi_mg_correct_vel(void *handle, double dt, const double *d_pPrime, double *d_u, double *d_v, double *d_w,
                        const double *d_bcxu, const double *d_bcyv, const double *d_bczw, double *d_face_u,
                        double *d_face_v, double *d_face_w);

@@ -1228,10 +1228,27 @@ static void face_correct(or_ctx *c, int d, double dt, const double *p, double *f
     free(face2);
 }
 
-/* face_vel (IBM/CORE_FRAC_STEP_ROUTINES.F90:6-240 without GCM_set_face_vel_body):
+/* GCM_set_face_vel_body (IBM/GCM_GHOSTCELL_VEL_UPDATE_UNSTRUC.F90:387-423): the
+ * faces of dead cells (blanked, not ghost) are zero. */
+static void gcm_set_face_vel_body(or_ctx *c, double *face_u, double *face_v, double *face_w)
+{
+    for (int k = 1; k <= c->nzc; ++k)
+        for (int j = 1; j <= c->nyc; ++j)
+            for (int i = 1; i <= c->nxc; ++i) {
+                const size_t f = FI(c, i, j, k);
+                if (c->iblank[f] == 1 && c->ghost[f] == 0) {
+                    face_u[FI(c, i + 1, j, k)] = 0.0; face_u[f] = 0.0;
+                    face_v[FI(c, i, j + 1, k)] = 0.0; face_v[f] = 0.0;
+                    face_w[FI(c, i, j, k + 1)] = 0.0; face_w[f] = 0.0;
+                }
+            }
+}
+
+/* face_vel (IBM/CORE_FRAC_STEP_ROUTINES.F90:6-240):
  * frac_step_type 0 NO_VAN_KAN (uTilde = u), 1 VAN_KAN (uTilde = u + dt grad p on
- * the interior, zero elsewhere, then the face pressure correction with p).
- * bc arrays may be NULL (zero). */
+ * the interior, zero elsewhere, then the face pressure correction with p),
+ * the boundary masks of both branches, and with GCM the ghost-cell faces of
+ * VAN_KAN and GCM_set_face_vel_body.  bc arrays may be NULL (zero). */
 void or_face_vel(or_ctx *c, int frac_step_type, double dt, const double *u, const double *v, const double *w,
                  const double *p, const double *bcxu, const double *bcyv, const double *bczw,
                  double *face_u, double *face_v, double *face_w)
@@ -1274,12 +1291,39 @@ void or_face_vel(or_ctx *c, int frac_step_type, double dt, const double *u, cons
                 face_w[FI(c, i, j, k + 1)] = (fxw(c, 2, k + 1) * wT[FI(c, i, j, k + 1)] + (1.0 - fxw(c, 2, k + 1)) * wT[f]) * (1 - kup[f]) + BCV(bczw, f) * kup[f];
                 face_w[f] = (fxw(c, 2, k) * wT[f] + (1.0 - fxw(c, 2, k)) * wT[FI(c, i, j, k - 1)]) * (1 - kum[f]) + BCV(bczw, f) * kum[f];
             }
-#undef BCV
     if (frac_step_type == 1) {
         face_correct(c, 0, dt, p, face_u, bcxu);
         face_correct(c, 1, dt, p, face_v, bcyv);
         face_correct(c, 2, dt, p, face_w, bczw);
     }
+    /* both branches: the boundary masks once more (IBM/CORE_FRAC_STEP_ROUTINES.F90:178-195) */
+    for (int k = 1; k <= c->nzc; ++k)
+        for (int j = 1; j <= c->nyc; ++j)
+            for (int i = 1; i <= c->nxc; ++i) {
+                const size_t f = FI(c, i, j, k);
+                face_u[f] = face_u[f] * (1 - ium[f]) + BCV(bcxu, f) * ium[f];
+                face_u[FI(c, i + 1, j, k)] = face_u[FI(c, i + 1, j, k)] * (1 - iup[f]) + BCV(bcxu, f) * iup[f];
+                face_v[f] = face_v[f] * (1 - jum[f]) + BCV(bcyv, f) * jum[f];
+                face_v[FI(c, i, j + 1, k)] = face_v[FI(c, i, j + 1, k)] * (1 - jup[f]) + BCV(bcyv, f) * jup[f];
+                face_w[f] = face_w[f] * (1 - kum[f]) + BCV(bczw, f) * kum[f];
+                face_w[FI(c, i, j, k + 1)] = face_w[FI(c, i, j, k + 1)] * (1 - kup[f]) + BCV(bczw, f) * kup[f];
+            }
+#undef BCV
+    /* VAN_KAN with ghost cells: the faces of a ghost cell interpolate u itself (:197-221) */
+    if (frac_step_type == 1 && c->p.boundary_formulation == GCM_METHOD)
+        for (int k = 1; k <= c->nzc; ++k)
+            for (int j = 1; j <= c->nyc; ++j)
+                for (int i = 1; i <= c->nxc; ++i) {
+                    const size_t f = FI(c, i, j, k);
+                    const double gY = (double)c->ghost[f], gN = 1.0 - gY;
+                    face_u[FI(c, i + 1, j, k)] = gN * face_u[FI(c, i + 1, j, k)] + gY * (fxw(c, 0, i + 1) * u[FI(c, i + 1, j, k)] + (1.0 - fxw(c, 0, i + 1)) * u[f]);
+                    face_u[f] = gN * face_u[f] + gY * (fxw(c, 0, i) * u[f] + (1.0 - fxw(c, 0, i)) * u[FI(c, i - 1, j, k)]);
+                    face_v[FI(c, i, j + 1, k)] = gN * face_v[FI(c, i, j + 1, k)] + gY * (fxw(c, 1, j + 1) * v[FI(c, i, j + 1, k)] + (1.0 - fxw(c, 1, j + 1)) * v[f]);
+                    face_v[f] = gN * face_v[f] + gY * (fxw(c, 1, j) * v[f] + (1.0 - fxw(c, 1, j)) * v[FI(c, i, j - 1, k)]);
+                    face_w[FI(c, i, j, k + 1)] = gN * face_w[FI(c, i, j, k + 1)] + gY * (fxw(c, 2, k + 1) * w[FI(c, i, j, k + 1)] + (1.0 - fxw(c, 2, k + 1)) * w[f]);
+                    face_w[f] = gN * face_w[f] + gY * (fxw(c, 2, k) * w[f] + (1.0 - fxw(c, 2, k)) * w[FI(c, i, j, k - 1)]);
+                }
+    if (c->p.boundary_formulation == GCM_METHOD) gcm_set_face_vel_body(c, face_u, face_v, face_w);
     free(uT); free(vT); free(wT);
 }
 
@@ -1306,7 +1350,8 @@ double or_rhs_poisson(or_ctx *c, double dt, const double *face_u, const double *
 }
 
 /* correct_vel (IBM/CORE_FRAC_STEP_ROUTINES.F90:244-448), non-periodic, without
- * GCM_vel_set_bc_internal and GCM_set_face_vel_body. */
+ * GCM_vel_set_bc_internal (the ghost-cell velocities); GCM_set_face_vel_body
+ * closes it when boundary_formulation is GCM. */
 void or_correct_vel(or_ctx *c, double dt, const double *pPrime, double *u, double *v, double *w,
                     const double *bcxu, const double *bcyv, const double *bczw,
                     double *face_u, double *face_v, double *face_w)
@@ -1333,6 +1378,7 @@ void or_correct_vel(or_ctx *c, double dt, const double *pPrime, double *u, doubl
     face_correct(c, 0, dt, p, face_u, bcxu);
     face_correct(c, 1, dt, p, face_v, bcyv);
     face_correct(c, 2, dt, p, face_w, bczw);
+    if (c->p.boundary_formulation == GCM_METHOD) gcm_set_face_vel_body(c, face_u, face_v, face_w);
 }
 
 /* update_pressure (IBM/CORE_FRAC_STEP_ROUTINES.F90:949-967). */

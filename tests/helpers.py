@@ -140,12 +140,38 @@ def baffle_problem(cells=(12, 10, 14), stretch=1.5, seed=3):
     return P.Problem(p, x, y, z, geom, nlu0, name=f"baffle_{cells[0]}x{cells[1]}x{cells[2]}")
 
 
+def unpaired_flags_problem(cells=(10, 12, 9), seed=5, density=0.2):
+    """3D stretched box without a body whose interior face flags are set at
+    random and independently on the two sides of a face (iup(i) without
+    ium(i+1) and so on), so that every branch of the reference's face masks is
+    taken.  The outer faces keep set_outer_iup's flags."""
+    import numpy as np
+    from flow_structure_interaction_fem_ibm_gb300 import problem as P
+    p = P.default_params(3, *cells, body=False)
+    x, y, z = P.make_grid(p.nx, p.ny, p.nz, "tanh", beta=1.5)
+    geom = P.empty_geometry(p)
+    rng = np.random.Generator(np.random.PCG64(seed))
+    n = cells
+    for q, fl in enumerate(geom.flags):
+        ax, hi = q // 2, q % 2
+        sl = [slice(1, n[0] + 1), slice(1, n[1] + 1), slice(1, n[2] + 1)]
+        # interior faces only: skip the outer face of this side
+        sl[ax] = slice(1, n[ax]) if hi else slice(2, n[ax] + 1)
+        view = fl[tuple(sl)]
+        view |= (rng.random(view.shape) < density).astype(np.int8)
+    sh = P.full_shape(p)
+    u, v, w = (np.asfortranarray(rng.standard_normal(sh)) for _ in range(3))
+    nlu0 = P.face_divergence(p, x, y, z, u, v, w, geom.iblank, geom.flags)
+    return P.Problem(p, x, y, z, geom, nlu0, name=f"unpaired_{n[0]}x{n[1]}x{n[2]}")
+
+
 def step_cases():
     from flow_structure_interaction_fem_ibm_gb300 import problem as P
     return [
         ("sphere16_tanh", lambda: sphere_problem(16, stretch=1.5)),
         ("box2d_24", lambda: P.box2d(24, seed=9)),
         ("baffle_12x10x14", lambda: baffle_problem()),
+        ("unpaired_10x12x9", lambda: unpaired_flags_problem()),
     ]
 
 

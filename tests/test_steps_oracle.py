@@ -17,7 +17,7 @@ import pytest
 
 from flow_structure_interaction_fem_ibm_gb300 import problem as P
 from oracle.oracle import Oracle
-from tests.helpers import baffle_problem, step_cases, step_fields
+from tests.helpers import baffle_problem, step_cases, step_fields, unpaired_flags_problem
 
 
 @pytest.mark.parametrize("case", step_cases(), ids=lambda c: c[0])
@@ -36,6 +36,37 @@ def test_face_vel_rhs_equals_vectorised_divergence(case):
         n = pr.params
         vol = mx.dx[1:n.nx, None, None] * my.dx[None, 1:n.ny, None] * mz.dx[None, None, 1:n.nz]
         assert abs(total - float((nlu0[1:n.nx, 1:n.ny, 1:n.nz] * vol).sum())) <= 1e-12 * np.abs(nlu0).max()
+    finally:
+        o.close()
+
+
+def test_face_vel_final_masks_follow_the_overwrite_order():
+    """With unpaired interior flags, face f ends as bc(f) if ium(f), else
+    bc(f-1) if iup(f-1), else the interpolation (the reference's write order,
+    restated here in closed form for the x faces)."""
+    pr = unpaired_flags_problem()
+    f = step_fields(pr, 13)
+    o = Oracle(pr)
+    try:
+        fu = o.face_vel(0.2, f["u"], f["v"], f["w"], bc=f["bc"])[0]
+        n = pr.params
+        nxc, nyc, nzc = n.nx - 1, n.ny - 1, n.nz - 1
+        ium, iup = pr.geom.flags[0], pr.geom.flags[1]
+        fx = P.Metrics(pr.x).fx
+        u, bc = f["u"], f["bc"][0]
+        hits = {"ium": 0, "iup_prev": 0, "interp": 0}
+        for k in range(1, nzc + 1):
+            for j in range(1, nyc + 1):
+                for i in range(1, nxc + 1):
+                    if ium[i, j, k]:
+                        ref, key = bc[i, j, k], "ium"
+                    elif i >= 2 and iup[i - 1, j, k]:
+                        ref, key = bc[i - 1, j, k], "iup_prev"
+                    else:
+                        ref, key = fx[i] * u[i, j, k] + (1 - fx[i]) * u[i - 1, j, k], "interp"
+                    hits[key] += 1
+                    assert abs(fu[i, j, k] - ref) <= 1e-14 * max(1.0, abs(ref))
+        assert min(hits.values()) > 0, hits
     finally:
         o.close()
 
