@@ -49,6 +49,8 @@ SOLVER_SYMBOLS = {
     "fsi_mg_face_vel_rhs": [ctypes.c_void_p, ctypes.c_int, ctypes.c_double] + [ctypes.c_void_p] * 11 + [c_double_p],
     "fsi_mg_correct_vel": [ctypes.c_void_p, ctypes.c_double] + [ctypes.c_void_p] * 10,
     "fsi_mg_update_pressure": [ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p],
+    "fsi_mg_set_velocity_ghosts": [ctypes.c_void_p, c_double_p, c_double_p, c_double_p, c_double_p,
+                                   ctypes.c_double, ctypes.c_double],
     "fsi_mg_last_error": [],
     "fsi_mg_destroy": [ctypes.c_void_p],
 }
@@ -64,7 +66,7 @@ GEOM_SYMBOLS = {
     "fsi_geom_gcm_coeffs": [ctypes.c_int, ctypes.c_int, ctypes.c_int, c_double_p, c_double_p, c_double_p,
                             ctypes.c_int, c_double_p, ctypes.c_int, c_i32_p, ctypes.c_double, ctypes.c_int,
                             c_i32_p, c_i32_p, c_i32_p, c_i32_p, c_i32_p, c_i32_p, c_double_p, c_double_p,
-                            c_double_p, c_double_p],
+                            c_double_p, c_double_p, c_double_p],
 }
 GEOM_RESTYPES = {"fsi_geom_iblank": ctypes.c_long}
 

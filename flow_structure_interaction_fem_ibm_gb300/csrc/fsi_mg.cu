@@ -123,6 +123,13 @@ struct Ctx {
     int step_cap = 0;
     double *vtilde = nullptr;   // uTilde, vTilde, wTilde of the VAN_KAN face_vel (allocated on first use)
     bool coarsest_fp32 = true;   // mixed form: the coarsest level is smoothed in FP32 like the others
+    // ghost-cell velocities (GCM_vel_set_bc_internal), registered by fsi_mg_set_velocity_ghosts
+    bool vg_on = false;
+    int vg_cap = 0;
+    double *vg_coeff = nullptr, *vg_bi = nullptr, *vg_scr = nullptr;
+    bool vg_bi_set = false;
+    double vg_bw = 0.0, vg_iw = 0.0;
+    int vg_last_iters = 0;
     // arguments of the last step calls, replayed by fsi_mg_time_kernel (which 6, 7, 8)
     StepArgs last_fv{}, last_cv{};
     bool have_fv = false, have_cv = false, have_up = false, last_fv_vk = false, last_up_vk = false;
@@ -1322,6 +1329,7 @@ int fsi_mg_set_geometry(void *handle, const int8_t *iblank, const int8_t *ghostC
     CK(cudaStreamSynchronize(c.s));
     if (c.graph) { cudaGraphExecDestroy(c.graph); c.graph = nullptr; }
     if (c.pgraph) { cudaGraphExecDestroy(c.pgraph); c.pgraph = nullptr; }
+    c.vg_on = false;   // the ghost list changed: velocity ghosts are registered again
     c.geometry = true;
     return 0;
 }
@@ -1563,7 +1571,62 @@ int fsi_mg_correct_vel(void *handle, double dt, const double *d_pPrime, double *
     launch_correct_vel(a, c.s);
     c.last_cv = a; c.have_cv = true;
     c.launches++;
+    int rc = 0;
+    if (c.vg_on && c.nGhost > 0) {   // GCM_vel_set_bc_internal (IBM/CORE_FRAC_STEP_ROUTINES.F90:373)
+        CK(cudaMemsetAsync(c.d_iters, 0, sizeof(int), c.s));
+        CK(cudaMemsetAsync(c.d_maxd, 0, sizeof(unsigned long long), c.s));
+        GhostArgs g{c.nGhost, c.gidx, c.sidx, c.gsg};
+        launch_vel_ghosts(d_u, d_v, d_w, g, c.vg_coeff, c.vg_bi_set ? c.vg_bi : nullptr, c.vg_bw, c.vg_iw, c.vg_scr,
+                          c.p.iterMax_ad, c.p.restol_ad, c.d_iters, c.d_maxd, c.s);
+        c.launches++;
+        int h_iters = 0;
+        unsigned long long h_maxd = 0;
+        CK(cudaMemcpyAsync(&h_iters, c.d_iters, sizeof(int), cudaMemcpyDeviceToHost, c.s));
+        CK(cudaMemcpyAsync(&h_maxd, c.d_maxd, sizeof(h_maxd), cudaMemcpyDeviceToHost, c.s));
+        CK(cudaStreamSynchronize(c.s));
+        c.vg_last_iters = h_iters;
+        double maxd;
+        std::memcpy(&maxd, &h_maxd, sizeof(maxd));
+        // the reference prints its non-convergence message and continues
+        if (h_iters >= c.p.iterMax_ad && maxd > c.p.restol_ad) rc = 2;
+    }
     CK(cudaStreamSynchronize(c.s));
+    return rc;
+}
+
+int fsi_mg_set_velocity_ghosts(void *handle, const double *coeffGCMD, const double *uBI, const double *vBI,
+                               const double *wBI, double bodyInterceptWeight, double imagePointWeight)
+{
+    if (!handle) return fail(-1, "null handle");
+    Ctx &c = *(Ctx *)handle;
+    if (!c.geometry) return fail(-2, "fsi_mg_set_geometry has not been called");
+    if (!coeffGCMD) { c.vg_on = false; return 0; }
+    if (c.p.boundary_formulation != GCM_METHOD) return fail(-1, "velocity ghosts need boundary_formulation GCM");
+    if ((uBI == nullptr) != (vBI == nullptr) || (uBI == nullptr) != (wBI == nullptr))
+        return fail(-1, "uBI, vBI, wBI must be all given or all NULL");
+    const int n = c.nGhost;
+    if (n == 0) { c.vg_on = true; return 0; }
+    if (c.vg_cap < c.ghost_cap) {   // grow-only, sized like the pressure ghost buffers
+        for (void *q : {(void *)c.vg_coeff, (void *)c.vg_bi, (void *)c.vg_scr}) {
+            auto it = std::find(c.allocs.begin(), c.allocs.end(), q);
+            if (q && it != c.allocs.end()) { cudaFree(q); c.allocs.erase(it); }
+        }
+        TRY(c.alloc(&c.vg_coeff, 8 * (size_t)c.ghost_cap));
+        TRY(c.alloc(&c.vg_bi, 3 * (size_t)c.ghost_cap));
+        TRY(c.alloc(&c.vg_scr, 6 * (size_t)c.ghost_cap));
+        c.vg_cap = c.ghost_cap;
+    }
+    CK(cudaMemcpyAsync(c.vg_coeff, coeffGCMD, 8 * (size_t)n * 8, cudaMemcpyHostToDevice, c.s));
+    c.vg_bi_set = (uBI != nullptr);
+    if (c.vg_bi_set) {
+        CK(cudaMemcpyAsync(c.vg_bi, uBI, (size_t)n * 8, cudaMemcpyHostToDevice, c.s));
+        CK(cudaMemcpyAsync(c.vg_bi + n, vBI, (size_t)n * 8, cudaMemcpyHostToDevice, c.s));
+        CK(cudaMemcpyAsync(c.vg_bi + 2 * (size_t)n, wBI, (size_t)n * 8, cudaMemcpyHostToDevice, c.s));
+    }
+    CK(cudaStreamSynchronize(c.s));
+    c.vg_bw = bodyInterceptWeight;
+    c.vg_iw = imagePointWeight;
+    c.vg_on = true;
     return 0;
 }
 

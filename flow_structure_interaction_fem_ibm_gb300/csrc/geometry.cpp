@@ -269,7 +269,7 @@ int fsi_geom_gcm_coeffs(int nx, int ny, int nz, const double *x, const double *y
                         double probeLengthNormalized, int nGhost,
                         const int32_t *iG, const int32_t *jG, const int32_t *kG,
                         int32_t *iCI, int32_t *jCI, int32_t *kCI, double *coeff,
-                        double *probeLength, double *bi, double *ip)
+                        double *probeLength, double *bi, double *ip, double *coeffD)
 {
     static const int incI[8] = {0, 0, 1, 1, 0, 0, 1, 1};
     static const int incJ[8] = {0, 1, 1, 0, 0, 1, 1, 0};
@@ -348,11 +348,23 @@ int fsi_geom_gcm_coeffs(int nx, int ny, int nz, const double *x, const double *y
         auto lx = [&](double v) { return (v - ox) / sx; };
         auto ly = [&](double v) { return (v - oy) / sy; };
         auto lz = [&](double v) { return (v - oz) / sz; };
-        double V[64];
+        double V[64], VD[64];
         for (int r = 0; r < 8; ++r) {
             int i = ci + incI[r], j = cj + incJ[r], k = ck + incK[r];
             double x1 = lx(xc[i]), x2 = ly(yc[j]), x3 = lz(zc[k]);
-            if (i == g_i && j == g_j && k == g_k) {
+            // Dirichlet matrix (GCM_Calc_VanMatrixDN, vanMatrixD): the ghost's
+            // own row is the trilinear basis at the body intercept
+            const bool self = (i == g_i && j == g_j && k == g_k);
+            const double d1 = self ? lx(bip.x) : x1, d2 = self ? ly(bip.y) : x2, d3 = self ? lz(bip.z) : x3;
+            VD[r + 8 * 0] = d1 * d2 * d3;
+            VD[r + 8 * 1] = d1 * d2;
+            VD[r + 8 * 2] = d1 * d3;
+            VD[r + 8 * 3] = d2 * d3;
+            VD[r + 8 * 4] = d1;
+            VD[r + 8 * 5] = d2;
+            VD[r + 8 * 6] = d3;
+            VD[r + 8 * 7] = 1.0;
+            if (self) {
                 // Neumann row: n . grad in local coordinates (d/dx = (1/sx) d/dx'); its
                 // right-hand side is uNormal = 0, so the row scale does not matter.
                 double a1 = lx(bip.x), a2 = ly(bip.y), a3 = lz(bip.z);
@@ -383,6 +395,14 @@ int fsi_geom_gcm_coeffs(int nx, int ny, int nz, const double *x, const double *y
             double s = 0.0;
             for (int m = 0; m < 8; ++m) s += V[m + 8 * r] * phi[m];
             coeff[8 * (size_t)n + r] = s;
+        }
+        if (coeffD) {
+            if (!inv8(VD)) return -(n + 1);
+            for (int r = 0; r < 8; ++r) {
+                double s = 0.0;
+                for (int m = 0; m < 8; ++m) s += VD[m + 8 * r] * phi[m];
+                coeffD[8 * (size_t)n + r] = s;
+            }
         }
     }
     return 0;

@@ -1100,6 +1100,84 @@ __global__ void __cluster_dims__(GHOST_CLUSTER, 1, 1) __launch_bounds__(1024)
     }
 }
 
+// Ghost-cell velocities (GCM_vel_set_bc_internal, IBM/GCM_GHOSTCELL_VEL_UPDATE_UNSTRUC.F90:126-247):
+// u_g = uBI bodyInterceptWeight - (sum_r coeffGCMD(r,g) u(stencil_r)) imagePointWeight, the
+// ghost's own stencil entry taking the body-intercept velocity, for u, v and w together,
+// iterated to max |du|+|dv|+|dw| <= tol or iterMax.  The reference sweeps Gauss-Seidel
+// over the ordered list; here Jacobi sweeps over a cluster of 8 CTAs, organised as
+// k_ghost_rows_cluster (ping-pong buffers, one cluster barrier per sweep, uniform loop
+// bounds, the converged values written into u, v, w once).  Both reach the same fixed point.
+__global__ void __cluster_dims__(GHOST_CLUSTER, 1, 1) __launch_bounds__(1024)
+    k_vel_ghosts_cluster(double *u, double *v, double *w, GhostArgs g, const double *coeffD, const double *bi,
+                         double bw, double iw, double *scratch, int iterMax, double tol, int *iters,
+                         unsigned long long *maxdelta)
+{
+    namespace cg = cooperative_groups;
+    cg::cluster_group cluster = cg::this_cluster();
+    __shared__ double s_d[32];
+    __shared__ double slot_d[2][GHOST_CLUSTER];   // used in rank 0 only
+    const unsigned rank = cluster.block_rank();
+    const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5, nw = (blockDim.x + 31) >> 5;
+    const int gtid = (int)rank * (int)blockDim.x + tid, gstride = GHOST_CLUSTER * (int)blockDim.x;
+    const int n3 = 3 * g.n;
+    double *rslot_d = cluster.map_shared_rank(&slot_d[0][0], 0);
+    double *bufA = scratch, *bufB = scratch + n3;
+    for (int n = gtid; n < g.n; n += gstride) {
+        const long long o = g.gidx[n];
+        bufA[n] = u[o]; bufA[g.n + n] = v[o]; bufA[2 * g.n + n] = w[o];
+    }
+    cluster.sync();
+    int it = 0, par = 0;
+    double maxd = 1.0e10;
+    while (it < iterMax && maxd > tol) {
+        const double *src = par ? bufB : bufA;
+        double *dst = par ? bufA : bufB;
+        double ld = 0.0;
+        for (int n = gtid; n < g.n; n += gstride) {
+            const double ub = bi ? bi[n] : 0.0, vb = bi ? bi[g.n + n] : 0.0, wb = bi ? bi[2 * g.n + n] : 0.0;
+            double uip = 0.0, vip = 0.0, wip = 0.0;
+#pragma unroll
+            for (int r = 0; r < 8; ++r) {
+                const int e = g.sg[8 * n + r];
+                const double c = coeffD[8 * n + r];
+                double uu, vv, ww;
+                if (e >= 0) { uu = u[e]; vv = v[e]; ww = w[e]; }
+                else if (e <= -2) { uu = src[-e - 2]; vv = src[g.n - e - 2]; ww = src[2 * g.n - e - 2]; }
+                else { uu = ub; vv = vb; ww = wb; }
+                uip = uip + c * uu; vip = vip + c * vv; wip = wip + c * ww;
+            }
+            const double un = ub * bw - uip * iw, vn = vb * bw - vip * iw, wn = wb * bw - wip * iw;
+            ld = fmax(ld, fabs(un - src[n]) + fabs(vn - src[g.n + n]) + fabs(wn - src[2 * g.n + n]));
+            dst[n] = un; dst[g.n + n] = vn; dst[2 * g.n + n] = wn;
+        }
+        for (int o = 16; o > 0; o >>= 1) ld = fmax(ld, __shfl_xor_sync(0xffffffffu, ld, o));
+        if (lane == 0) s_d[wid] = ld;
+        __syncthreads();
+        if (tid == 0) {
+            double a = 0.0;
+            for (int q = 0; q < nw; ++q) a = fmax(a, s_d[q]);
+            rslot_d[par * GHOST_CLUSTER + rank] = a;
+        }
+        cluster.sync();   // dst and this sweep's slots are complete
+        double a = 0.0;
+        for (int q = 0; q < GHOST_CLUSTER; ++q) a = fmax(a, rslot_d[par * GHOST_CLUSTER + q]);
+        maxd = a;
+        ++it;
+        par ^= 1;
+        __syncthreads();   // s_d is rewritten by the next sweep
+    }
+    const double *fin = par ? bufB : bufA;   // the buffer the last sweep wrote
+    for (int n = gtid; n < g.n; n += gstride) {
+        const long long o = g.gidx[n];
+        u[o] = fin[n]; v[o] = fin[g.n + n]; w[o] = fin[2 * g.n + n];
+    }
+    cluster.sync();   // rank 0's slots stay alive until every CTA has read them
+    if (rank == 0 && tid == 0) {
+        atomicAdd(iters, it);
+        atomicMax(maxdelta, (unsigned long long)__double_as_longlong(maxd));
+    }
+}
+
 template <typename T>
 __global__ void k_fill(T *p, long long n, T val)
 {
@@ -2047,6 +2125,15 @@ void launch_ghost_rows(T *v, const GhostArgs &g, const T *coeff, T *scratch, int
     else
         k_ghost_rows_cluster<T><<<GHOST_CLUSTER, 1024, 0, s>>>(v, g, coeff, scratch, iterMax, tol, reltol, d_iters,
                                                                 d_maxdelta);
+}
+
+void launch_vel_ghosts(double *u, double *v, double *w, const GhostArgs &g, const double *coeffD, const double *bi,
+                       double bw, double iw, double *scratch, int iterMax, double tol, int *d_iters,
+                       unsigned long long *d_maxdelta, cudaStream_t s)
+{
+    if (g.n <= 0) return;
+    k_vel_ghosts_cluster<<<GHOST_CLUSTER, 1024, 0, s>>>(u, v, w, g, coeffD, bi, bw, iw, scratch, iterMax, tol, d_iters,
+                                                        d_maxdelta);
 }
 
 template <typename T>

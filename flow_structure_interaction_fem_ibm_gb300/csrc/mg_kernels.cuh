@@ -108,6 +108,11 @@ void launch_face_vel_rhs(const StepArgs &a, bool van_kan, double *partials, int 
 // correct_vel cell-centre update and face corrections (IBM/CORE_FRAC_STEP_ROUTINES.F90:244-448,
 // without the ghost-cell velocity interpolation)
 void launch_correct_vel(const StepArgs &a, cudaStream_t s);
+// ghost-cell velocities u, v, w (GCM_vel_set_bc_internal); coeffD 8 per ghost, bi the
+// body-intercept velocities (3 x n: u, v, w; null = zero), scratch 6 x n doubles
+void launch_vel_ghosts(double *u, double *v, double *w, const GhostArgs &g, const double *coeffD, const double *bi,
+                       double bw, double iw, double *scratch, int iterMax, double tol, int *d_iters,
+                       unsigned long long *d_maxdelta, cudaStream_t s);
 // update_pressure without its ghost rows (IBM/CORE_FRAC_STEP_ROUTINES.F90:949-967)
 void launch_update_pressure(double *p, const double *pPrime, long long n, bool van_kan, cudaStream_t s);
 

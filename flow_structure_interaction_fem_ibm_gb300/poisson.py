@@ -131,11 +131,26 @@ class PoissonSolver:
 
     def correct_vel(self, dt: float, d_pPrime: int, d_u: int, d_v: int, d_w: int, d_face_u: int, d_face_v: int,
                     d_face_w: int, d_bc=(None, None, None)):
-        """correct_vel (IBM/CORE_FRAC_STEP_ROUTINES.F90:244-448) without the
-        ghost-cell velocity steps, on device arrays (updated in place)."""
+        """correct_vel (IBM/CORE_FRAC_STEP_ROUTINES.F90:244-448) on device
+        arrays (updated in place); the ghost-cell velocities once
+        set_velocity_ghosts registered them.  Returns the status (2: the ghost
+        velocities did not converge)."""
         vp = lambda a: ctypes.c_void_p(a) if a else None
-        _check(self.lib.fsi_mg_correct_vel(self.h, float(dt), vp(d_pPrime), vp(d_u), vp(d_v), vp(d_w), vp(d_bc[0]),
-                                           vp(d_bc[1]), vp(d_bc[2]), vp(d_face_u), vp(d_face_v), vp(d_face_w)))
+        return _check(self.lib.fsi_mg_correct_vel(self.h, float(dt), vp(d_pPrime), vp(d_u), vp(d_v), vp(d_w),
+                                                  vp(d_bc[0]), vp(d_bc[1]), vp(d_bc[2]), vp(d_face_u),
+                                                  vp(d_face_v), vp(d_face_w)))
+
+    def set_velocity_ghosts(self, coeffGCMD, bi=None, probe_length_normalized: float = 2.0):
+        """Ghost-cell velocities for correct_vel (GCM_vel_set_bc_internal):
+        coeffGCMD (8, nGhost) Fortran order, bi = (uBI, vBI, wBI) or None (body
+        at rest); the weights follow probeLengthNormalized (IBM/MAIN.F90:913-914)."""
+        bw = probe_length_normalized / (probe_length_normalized - 1.0)
+        iw = 1.0 / (probe_length_normalized - 1.0)
+        cd = None if coeffGCMD is None else np.asfortranarray(coeffGCMD, dtype=np.float64)
+        u, v, w = (None, None, None) if bi is None else (np.ascontiguousarray(a, dtype=np.float64) for a in bi)
+        _check(self.lib.fsi_mg_set_velocity_ghosts(self.h, _p(cd), _p(u), _p(v), _p(w), bw, iw))
+        self._vg_keep = (cd, u, v, w)
+        return self
 
     def update_pressure(self, d_pPrime: int, d_p: int, frac_step_type: int = 0):
         """update_pressure (IBM/CORE_FRAC_STEP_ROUTINES.F90:949-967) on device arrays."""

@@ -43,9 +43,12 @@ class Geometry:
     iCI: Optional[np.ndarray] = None
     jCI: Optional[np.ndarray] = None
     kCI: Optional[np.ndarray] = None
-    coeff: Optional[np.ndarray] = None       # (8, nGhost) Fortran order
+    coeff: Optional[np.ndarray] = None       # coeffGCMN (8, nGhost) Fortran order
     probe: Optional[np.ndarray] = None
     pgrad: Optional[np.ndarray] = None       # 6 boundary planes packed
+    coeffD: Optional[np.ndarray] = None      # coeffGCMD (8, nGhost): Dirichlet weights of the ghost velocity
+    xBI: Optional[np.ndarray] = None         # (3, nGhost) body intercepts
+    xIP: Optional[np.ndarray] = None         # (3, nGhost) image points
 
 
 @dataclass
@@ -127,6 +130,9 @@ def body_geometry(p: SolverParams, x, y, z, verts, tris, probe_length_normalized
     iG, jG, kG = iG[:n].copy(), jG[:n].copy(), kG[:n].copy()
     iCI = np.zeros(n, np.int32); jCI = np.zeros(n, np.int32); kCI = np.zeros(n, np.int32)
     coeff = np.zeros((8, n), order="F")
+    coeffD = np.zeros((8, n), order="F")
+    xBI = np.zeros((3, n), order="F")
+    xIP = np.zeros((3, n), order="F")
     probe = np.zeros(n)
     rc = g.fsi_geom_gcm_coeffs(p.nx, p.ny, p.nz, _native.ptr(x, ctypes.c_double), _native.ptr(y, ctypes.c_double),
                                _native.ptr(z, ctypes.c_double), nv, _native.ptr(verts, ctypes.c_double), nt,
@@ -135,11 +141,13 @@ def body_geometry(p: SolverParams, x, y, z, verts, tris, probe_length_normalized
                                _native.ptr(kG, ctypes.c_int32), _native.ptr(iCI, ctypes.c_int32),
                                _native.ptr(jCI, ctypes.c_int32), _native.ptr(kCI, ctypes.c_int32),
                                coeff.ctypes.data_as(_native.c_double_p), _native.ptr(probe, ctypes.c_double),
-                               None, None)
+                               xBI.ctypes.data_as(_native.c_double_p), xIP.ctypes.data_as(_native.c_double_p),
+                               coeffD.ctypes.data_as(_native.c_double_p))
     if rc != 0:
         raise RuntimeError(f"image-point stencil search failed for ghost {-rc - 1}")
     return Geometry(iblank=iblank, ghost=ghost, flags=outer_flags(p), nGhost=n, iG=iG, jG=jG, kG=kG,
-                    iCI=iCI, jCI=jCI, kCI=kCI, coeff=coeff, probe=probe, pgrad=np.zeros(pgrad_size(p)))
+                    iCI=iCI, jCI=jCI, kCI=kCI, coeff=coeff, probe=probe, pgrad=np.zeros(pgrad_size(p)),
+                    coeffD=coeffD, xBI=xBI, xIP=xIP)
 
 
 # ---------------------------------------------------------------- RHS ----

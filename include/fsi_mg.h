@@ -153,14 +153,31 @@ int fsi_mg_face_vel_rhs(void *handle, int frac_step_type, double dt, const doubl
                         double *sum);
 
 /* correct_vel (IBM/CORE_FRAC_STEP_ROUTINES.F90:244-448) without periodic
- * sides and without the ghost-cell velocity interpolation
- * (GCM_vel_set_bc_internal, which stays with the caller): u, v, w -= dt grad
- * pPrime (1 - iblank), the face corrections in the reference's overwrite
- * order and, with GCM, GCM_set_face_vel_body (INOUT d_u..d_w,
- * d_face_u..d_face_w). */
+ * sides: u, v, w -= dt grad pPrime (1 - iblank), the ghost-cell velocities
+ * (GCM_vel_set_bc_internal) once fsi_mg_set_velocity_ghosts registered
+ * them, the face corrections in the reference's overwrite order and, with
+ * GCM, GCM_set_face_vel_body (INOUT d_u..d_w, d_face_u..d_face_w).
+ * Status 2: the ghost velocities did not converge within iterMax_ad. */
 int fsi_mg_correct_vel(void *handle, double dt, const double *d_pPrime, double *d_u, double *d_v, double *d_w,
                        const double *d_bcxu, const double *d_bcyv, const double *d_bczw, double *d_face_u,
                        double *d_face_v, double *d_face_w);
+
+/* Ghost-cell velocities of the GCM body for fsi_mg_correct_vel
+ * (GCM_vel_set_bc_internal, IBM/GCM_GHOSTCELL_VEL_UPDATE_UNSTRUC.F90:126-247):
+ * coeffGCMD(8,nGhost), the Dirichlet image-point weights of the ghost list
+ * and stencils of the last fsi_mg_set_geometry (IBM/GCM_SET_BOUNDARY.F90:
+ * 282,305-486), the body-intercept velocities uBodyIntercept,
+ * vBodyIntercept, wBodyIntercept (nGhost each; all NULL: a body at rest) and
+ * bodyInterceptWeight, imagePointWeight (IBM/MAIN.F90:913-914); host
+ * arrays.  From then on fsi_mg_correct_vel ends its cell-centre update with
+ * the ghost-velocity iteration u_g = uBI bodyInterceptWeight -
+ * (sum_r coeffGCMD(r) u_r) imagePointWeight, the ghost's own stencil entry
+ * taking uBI, to max |du|+|dv|+|dw| <= restol_ad (status 2 after iterMax_ad
+ * sweeps, as the reference prints and continues).  Call again after each
+ * fsi_mg_set_geometry (which turns it off) and whenever the intercept
+ * velocities change; coeffGCMD NULL turns it off. */
+int fsi_mg_set_velocity_ghosts(void *handle, const double *coeffGCMD, const double *uBI, const double *vBI,
+                               const double *wBI, double bodyInterceptWeight, double imagePointWeight);
 
 /* update_pressure (IBM/CORE_FRAC_STEP_ROUTINES.F90:949-967): p = pPrime
  * (frac_step_type 0) or p += pPrime (1), then the ghost-cell pressure rows

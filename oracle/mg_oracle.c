@@ -58,6 +58,10 @@ struct or_ctx {
     int gs_last_iters;
     int ghost_nonconv;
     int geometry_set;
+    /* ghost-cell velocities (GCM_vel_set_bc_internal) */
+    double *vg_coeff, *vg_bi;   /* coeffGCMD (8,nGhost); uBI, vBI, wBI (3 x nGhost) or NULL */
+    double vg_bw, vg_iw;
+    int vg_on, vg_last_iters;
 };
 
 static const int incI[8] = {0, 0, 1, 1, 0, 0, 1, 1};   /* IBM/GCM_MEMORY_ALLOCATE.F90:494-518 */
@@ -225,6 +229,7 @@ or_ctx *or_create(const fsi_mg_params *p, const double *x, const double *y, cons
 void or_destroy(or_ctx *c)
 {
     if (!c) return;
+    free(c->vg_coeff); free(c->vg_bi);
     free(c->fresh);
     for (int d = 0; d < 3; ++d) {
         free(c->x[d]); free(c->xc[d]); free(c->dx[d]); free(c->dxinv[d]); free(c->dxc[d]); free(c->dxcinv[d]);
@@ -1228,6 +1233,8 @@ static void face_correct(or_ctx *c, int d, double dt, const double *p, double *f
     free(face2);
 }
 
+static void gcm_vel_set_bc_internal(or_ctx *c, double *u, double *v, double *w);
+
 /* GCM_set_face_vel_body (IBM/GCM_GHOSTCELL_VEL_UPDATE_UNSTRUC.F90:387-423): the
  * faces of dead cells (blanked, not ghost) are zero. */
 static void gcm_set_face_vel_body(or_ctx *c, double *face_u, double *face_v, double *face_w)
@@ -1349,9 +1356,9 @@ double or_rhs_poisson(or_ctx *c, double dt, const double *face_u, const double *
     return sum;
 }
 
-/* correct_vel (IBM/CORE_FRAC_STEP_ROUTINES.F90:244-448), non-periodic, without
- * GCM_vel_set_bc_internal (the ghost-cell velocities); GCM_set_face_vel_body
- * closes it when boundary_formulation is GCM. */
+/* correct_vel (IBM/CORE_FRAC_STEP_ROUTINES.F90:244-448), non-periodic; with
+ * GCM the ghost-cell velocities (once or_set_vel_ghosts registered them) and
+ * GCM_set_face_vel_body. */
 void or_correct_vel(or_ctx *c, double dt, const double *pPrime, double *u, double *v, double *w,
                     const double *bcxu, const double *bcyv, const double *bczw,
                     double *face_u, double *face_v, double *face_w)
@@ -1375,10 +1382,72 @@ void or_correct_vel(or_ctx *c, double dt, const double *pPrime, double *u, doubl
                 v[f] = v[f] - dt * pgy * (double)(1 - c->iblank[f]);
                 w[f] = w[f] - dt * pgz * (double)(1 - c->iblank[f]);
             }
+    /* ghost-cell velocities (:373) */
+    if (c->p.boundary_formulation == GCM_METHOD && c->vg_on) gcm_vel_set_bc_internal(c, u, v, w);
     face_correct(c, 0, dt, p, face_u, bcxu);
     face_correct(c, 1, dt, p, face_v, bcyv);
     face_correct(c, 2, dt, p, face_w, bczw);
     if (c->p.boundary_formulation == GCM_METHOD) gcm_set_face_vel_body(c, face_u, face_v, face_w);
+}
+
+/* Ghost-cell velocities for or_correct_vel (NULL coeffD turns them off). */
+void or_set_vel_ghosts(or_ctx *c, const double *coeffD, const double *uBI, const double *vBI, const double *wBI,
+                       double bodyInterceptWeight, double imagePointWeight)
+{
+    free(c->vg_coeff); free(c->vg_bi);
+    c->vg_coeff = c->vg_bi = NULL;
+    c->vg_on = coeffD != NULL;
+    if (!coeffD) return;
+    const size_t n = (size_t)c->nGhost;
+    c->vg_coeff = zalloc(sizeof(double) * 8 * n);
+    memcpy(c->vg_coeff, coeffD, sizeof(double) * 8 * n);
+    if (uBI) {
+        c->vg_bi = zalloc(sizeof(double) * 3 * n);
+        memcpy(c->vg_bi, uBI, sizeof(double) * n);
+        memcpy(c->vg_bi + n, vBI, sizeof(double) * n);
+        memcpy(c->vg_bi + 2 * n, wBI, sizeof(double) * n);
+    }
+    c->vg_bw = bodyInterceptWeight;
+    c->vg_iw = imagePointWeight;
+}
+
+int or_vel_ghost_iters(or_ctx *c) { return c->vg_last_iters; }
+
+/* GCM_vel_set_bc_internal (IBM/GCM_GHOSTCELL_VEL_UPDATE_UNSTRUC.F90:126-247):
+ * Gauss-Seidel over the ordered ghost list until max |du|+|dv|+|dw| <= restol_ad. */
+static void gcm_vel_set_bc_internal(or_ctx *c, double *u, double *v, double *w)
+{
+    const size_t n0 = (size_t)c->nGhost;
+    int iterGC = 0;
+    double resVelMax = 1.0e10;
+    while (iterGC < c->p.iterMax_ad && resVelMax > c->p.restol_ad) {
+        resVelMax = 0.0;
+        for (int n = 0; n < c->nGhost; ++n) {
+            const int iG = c->gi[0][n], jG = c->gi[1][n], kG = c->gi[2][n];
+            const double ub = c->vg_bi ? c->vg_bi[n] : 0.0, vb = c->vg_bi ? c->vg_bi[n0 + n] : 0.0,
+                         wb = c->vg_bi ? c->vg_bi[2 * n0 + n] : 0.0;
+            double uIP = 0.0, vIP = 0.0, wIP = 0.0;
+            for (int r = 0; r < 8; ++r) {
+                const int ii = c->gi[3][n] + incI[r], jj = c->gi[4][n] + incJ[r], kk = c->gi[5][n] + incK[r];
+                const double cd = c->vg_coeff[8 * (size_t)n + r];
+                if (ii != iG || jj != jG || kk != kG) {
+                    const size_t f = FI(c, ii, jj, kk);
+                    uIP = uIP + cd * u[f]; vIP = vIP + cd * v[f]; wIP = wIP + cd * w[f];
+                } else {
+                    uIP = uIP + cd * ub; vIP = vIP + cd * vb; wIP = wIP + cd * wb;
+                }
+            }
+            const size_t g = FI(c, iG, jG, kG);
+            const double uPrev = u[g], vPrev = v[g], wPrev = w[g];
+            u[g] = ub * c->vg_bw - uIP * c->vg_iw;
+            v[g] = vb * c->vg_bw - vIP * c->vg_iw;
+            w[g] = wb * c->vg_bw - wIP * c->vg_iw;
+            const double resVel = fabs(u[g] - uPrev) + fabs(v[g] - vPrev) + fabs(w[g] - wPrev);
+            if (resVel > resVelMax) resVelMax = resVel;
+        }
+        iterGC = iterGC + 1;
+    }
+    c->vg_last_iters = iterGC;
 }
 
 /* update_pressure (IBM/CORE_FRAC_STEP_ROUTINES.F90:949-967). */

@@ -93,4 +93,7 @@ void    or_correct_vel(or_ctx *c, double dt, const double *pPrime, double *u, do
                        const double *bcxu, const double *bcyv, const double *bczw,
                        double *face_u, double *face_v, double *face_w);
 void    or_update_pressure(or_ctx *c, int frac_step_type, const double *pPrime, double *p);
+void    or_set_vel_ghosts(or_ctx *c, const double *coeffD, const double *uBI, const double *vBI,
+                          const double *wBI, double bodyInterceptWeight, double imagePointWeight);
+int     or_vel_ghost_iters(or_ctx *c);
 #endif

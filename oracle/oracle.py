@@ -87,6 +87,9 @@ def lib():
         L.or_correct_vel.restype = None
         L.or_update_pressure.argtypes = [ctypes.c_void_p, ctypes.c_int, _dp, _dp]
         L.or_update_pressure.restype = None
+        L.or_set_vel_ghosts.argtypes = [ctypes.c_void_p] + [_dp] * 4 + [ctypes.c_double] * 2
+        L.or_set_vel_ghosts.restype = None
+        L.or_vel_ghost_iters.argtypes = [ctypes.c_void_p]
         _lib = L
     return _lib
 
@@ -197,6 +200,18 @@ class Oracle:
         """In place on u, v, w and the faces."""
         lib().or_correct_vel(self.h, dt, _p(pPrime), _p(u), _p(v), _p(w), _p(bc[0]), _p(bc[1]), _p(bc[2]),
                              _p(face_u), _p(face_v), _p(face_w))
+
+    def set_vel_ghosts(self, coeffD, bi=None, probe_length_normalized=2.0):
+        """Ghost-cell velocities for correct_vel (weights of IBM/MAIN.F90:913-914)."""
+        bw = probe_length_normalized / (probe_length_normalized - 1.0)
+        iw = 1.0 / (probe_length_normalized - 1.0)
+        self._vg = (None if coeffD is None else np.asfortranarray(coeffD, dtype=np.float64),) + \
+            ((None, None, None) if bi is None else tuple(np.ascontiguousarray(a, dtype=np.float64) for a in bi))
+        lib().or_set_vel_ghosts(self.h, *(_p(a) for a in self._vg), bw, iw)
+        return self
+
+    def vel_ghost_iters(self):
+        return lib().or_vel_ghost_iters(self.h)
 
     def update_pressure(self, pPrime, p, frac_step_type=0):
         lib().or_update_pressure(self.h, frac_step_type, _p(pPrime), _p(p))

@@ -139,3 +139,58 @@ def test_update_pressure(frac):
         assert np.array_equal(p, ref)
     finally:
         o.close()
+
+
+# ------------------------------------------------------ ghost velocities --
+def _trilinear(pts):
+    x, y, z = pts
+    return 0.3 + 1.7 * x - 0.9 * y + 2.3 * z + 0.5 * x * y - 1.1 * y * z + 0.7 * x * z + 1.3 * x * y * z
+
+
+def test_dirichlet_weights_interpolate_trilinear_fields_at_the_image_point():
+    """coeffGCMD reproduces any trilinear field at the image point from its
+    values at the stencil cell centres, the ghost's own entry taken at the body
+    intercept (the Dirichlet Vandermonde system of IBM/GCM_SET_BOUNDARY.F90:305-486)."""
+    pr = P.sphere(16, seed=2, stretch=1.5)
+    g = pr.geom
+    mx, my, mz = (P.Metrics(c) for c in (pr.x, pr.y, pr.z))
+    inc = np.array([[0, 0, 1, 1, 0, 0, 1, 1], [0, 1, 1, 0, 0, 1, 1, 0], [0, 0, 0, 0, 1, 1, 1, 1]])
+    worst = 0.0
+    for n in range(g.nGhost):
+        ii, jj, kk = g.iCI[n] + inc[0], g.jCI[n] + inc[1], g.kCI[n] + inc[2]
+        pts = np.array([mx.xc[ii], my.xc[jj], mz.xc[kk]])
+        own = (ii == g.iG[n]) & (jj == g.jG[n]) & (kk == g.kG[n])
+        pts[:, own] = g.xBI[:, n:n + 1]
+        val = float(g.coeffD[:, n] @ _trilinear(pts))
+        worst = max(worst, abs(val - _trilinear(g.xIP[:, n])))
+        assert abs(g.coeffD[:, n].sum() - 1.0) < 1e-12
+    assert worst < 1e-11
+
+
+def test_ghost_velocities_extrapolate_a_linear_field():
+    """GCM_vel_set_bc_internal with a linear velocity field and the field's
+    own values at the body intercepts is a fixed point at the ghost centres:
+    u_g = uBI bw - uIP iw is the linear extrapolation through BI and IP."""
+    pr = P.sphere(16, seed=2, stretch=1.5)
+    g = pr.geom
+    mx, my, mz = (P.Metrics(c) for c in (pr.x, pr.y, pr.z))
+    X, Y, Z = np.meshgrid(mx.xc, my.xc, mz.xc, indexing="ij")
+    lin = lambda a, b, c: 0.4 + 1.2 * a - 0.7 * b + 0.9 * c
+    u = np.asfortranarray(lin(X, Y, Z))
+    v = np.asfortranarray(2.0 * u)
+    w = np.asfortranarray(-u)
+    ubi = lin(*g.xBI)
+    o = Oracle(pr)
+    try:
+        o.set_vel_ghosts(g.coeffD, (ubi, 2.0 * ubi, -ubi))
+        uu, vv, ww = u.copy(order="F"), v.copy(order="F"), w.copy(order="F")
+        # scramble the ghosts, then correct_vel with pPrime = 0 runs the ghost iteration
+        gi = (g.iG, g.jG, g.kG)
+        uu[gi] = 0.0; vv[gi] = 5.0; ww[gi] = -3.0
+        faces = [np.zeros(pr.shape, order="F") for _ in range(3)]
+        o.correct_vel(0.1, np.zeros(pr.shape, order="F"), uu, vv, ww, *faces)
+        assert o.vel_ghost_iters() > 1
+        for a, b in ((uu, u), (vv, v), (ww, w)):
+            assert np.abs(a[gi] - b[gi]).max() < 1e-9
+    finally:
+        o.close()
