@@ -90,6 +90,13 @@ MODULE fsi_mg_gpu
       TYPE(C_PTR), VALUE :: h, pPrime, u, v, w, bcxu, bcyv, bczw, face_u, face_v, face_w
       REAL(C_DOUBLE), VALUE :: dt
     END FUNCTION
+    ! coeffGCMD(8,nGhost), u/v/wBodyIntercept(nGhost) (host; C_NULL_PTR for a body at rest)
+    INTEGER(C_INT) FUNCTION fsi_mg_set_velocity_ghosts(h, coeffGCMD, uBI, vBI, wBI, bodyInterceptWeight, &
+        imagePointWeight) BIND(C, NAME='fsi_mg_set_velocity_ghosts')
+      IMPORT :: C_INT, C_DOUBLE, C_PTR
+      TYPE(C_PTR), VALUE :: h, coeffGCMD, uBI, vBI, wBI
+      REAL(C_DOUBLE), VALUE :: bodyInterceptWeight, imagePointWeight
+    END FUNCTION
     INTEGER(C_INT) FUNCTION fsi_mg_update_pressure(h, frac_step_type, pPrime, p) &
         BIND(C, NAME='fsi_mg_update_pressure')
       IMPORT :: C_INT, C_PTR
