@@ -353,6 +353,15 @@ def projection_steps(solver, pr, peak, reps=20):
             res[name] = {"device_us": 1e3 * ms, "alg_bytes": nb, "achieved_gbs": gbs, "frac": gbs / peak,
                          "call_wall_us": wall_us}
         out[tag] = res
+    # momentum right-hand side (rhs_advec_diff, Crank-Nicolson, constant viscosity array, no bc arrays)
+    visc = torch.full(sh, 1e-3, dtype=torch.float64, device="cuda")
+    nl = [torch.zeros(sh, dtype=torch.float64, device="cuda") for _ in range(3)]
+    solver.rhs_advec_diff(1e-3, [u.data_ptr(), v.data_ptr(), w.data_ptr()], fp, visc.data_ptr(),
+                          [t.data_ptr() for t in nl], advec_scheme=2)
+    ms, nb = solver.time_kernel(9, 0, reps)
+    gbs = nb / (ms * 1e-3) / 1e9
+    out["rhs_advec_diff_cn"] = {"device_us": 1e3 * ms, "alg_bytes": nb, "achieved_gbs": gbs, "frac": gbs / peak}
+    del visc, nl
     out["note"] = ("device_us: the routine's kernels (face_vel_rhs: shell zeroing, [uTilde], faces+divergence, "
                    "sum) replayed 20x; alg_bytes: FP64 fields read/written once per interior cell, no bc arrays; "
                    "update_pressure without its ghost-cell rows")

@@ -119,6 +119,8 @@ struct Ctx {
     double *d_dx[3] = {}, *d_dxinv[3] = {}, *d_dxcinv[3] = {};
     double *d_fx[3] = {};   // face interpolation weights fx(1:n) (IBM/CORE_GRID.F90:163-175)
     double *d_gx[3] = {};   // 1 - fx, as the reference forms it
+    // diffusion coefficient tables of rhs_diff: dcinv(i) dinv(i), dcinv(i+1) dinv(i), (2 dinv(i)) dinv(i)
+    double *d_adm[3] = {}, *d_adp[3] = {}, *d_adb[3] = {};
     double *step_partials = nullptr;   // one partial sum per CTA of face_vel_rhs
     int step_cap = 0;
     double *vtilde = nullptr;   // uTilde, vTilde, wTilde of the VAN_KAN face_vel (allocated on first use)
@@ -132,6 +134,8 @@ struct Ctx {
     int vg_last_iters = 0;
     // arguments of the last step calls, replayed by fsi_mg_time_kernel (which 6, 7, 8)
     StepArgs last_fv{}, last_cv{};
+    RhsAdArgs last_ad{};
+    bool have_ad = false;
     bool have_fv = false, have_cv = false, have_up = false, last_fv_vk = false, last_up_vk = false;
     double *last_up_p = nullptr;
     const double *last_up_pp = nullptr;
@@ -1124,6 +1128,18 @@ int fsi_mg_create(const fsi_mg_params *params, const double *x, const double *y,
             fx[i] = (c->x[d][i] - c->xc[d][i - 1]) / (c->xc[d][i] - c->xc[d][i - 1]);
         std::vector<double> gx(N[d] + 2, 0.0);
         for (int i = 1; i <= N[d]; ++i) gx[i] = 1.0 - fx[i];
+        std::vector<double> adm(N[d] + 2, 0.0), adp(N[d] + 2, 0.0), adb(N[d] + 2, 0.0);
+        for (int i = 1; i < N[d]; ++i) {
+            adm[i] = c->dxcinv[d][i] * c->dxinv[d][i];
+            adp[i] = c->dxcinv[d][i + 1] * c->dxinv[d][i];
+            adb[i] = (c->dxinv[d][i] * 2.0) * c->dxinv[d][i];
+        }
+        TRY(c->alloc(&c->d_adm[d], N[d] + 2));
+        TRY(c->alloc(&c->d_adp[d], N[d] + 2));
+        TRY(c->alloc(&c->d_adb[d], N[d] + 2));
+        CK(cudaMemcpyAsync(c->d_adm[d], adm.data(), (N[d] + 2) * 8, cudaMemcpyHostToDevice, c->s));
+        CK(cudaMemcpyAsync(c->d_adp[d], adp.data(), (N[d] + 2) * 8, cudaMemcpyHostToDevice, c->s));
+        CK(cudaMemcpyAsync(c->d_adb[d], adb.data(), (N[d] + 2) * 8, cudaMemcpyHostToDevice, c->s));
         TRY(c->alloc(&c->d_fx[d], N[d] + 2));
         TRY(c->alloc(&c->d_gx[d], N[d] + 2));
         CK(cudaMemcpyAsync(c->d_fx[d], fx.data(), (N[d] + 2) * 8, cudaMemcpyHostToDevice, c->s));
@@ -1594,6 +1610,49 @@ int fsi_mg_correct_vel(void *handle, double dt, const double *d_pPrime, double *
     return rc;
 }
 
+int fsi_mg_rhs_advec_diff(void *handle, int advec_scheme, int frac_step_type, double dt,
+                          const fsi_mg_rhs_ad_fields *fl)
+{
+    if (!handle || !fl) return fail(-1, "null argument");
+    if (advec_scheme < 1 || advec_scheme > 3) return fail(-1, "advec_scheme must be 1 (AB2), 2 or 3 (Crank-Nicolson)");
+    if (frac_step_type != 0 && frac_step_type != 1) return fail(-1, "frac_step_type must be 0 (NO_VAN_KAN) or 1 (VAN_KAN)");
+    if (!(dt > 0.0)) return fail(-1, "dt must be positive");
+    Ctx &c = *(Ctx *)handle;
+    TRY(step_ready(c));
+    const bool three_d = (c.p.ndim == 3);
+    if (!fl->u || !fl->v || !fl->face_u || !fl->face_v || !fl->viscTot || !fl->nlu || !fl->nlv ||
+        (three_d && (!fl->w || !fl->face_w || !fl->nlw)))
+        return fail(-1, "null field");
+    if (advec_scheme == 1 && (!fl->nluOld || !fl->nlvOld || (three_d && !fl->nlwOld)))
+        return fail(-1, "ADAMS_BASHFORTH2 needs nluOld, nlvOld (and nlwOld in 3D)");
+    if (frac_step_type == 1 && (!fl->p || !fl->nlw)) return fail(-1, "VAN_KAN needs p and nlw");
+    RhsAdArgs a{};
+    a.vel[0] = fl->u; a.vel[1] = fl->v; a.vel[2] = fl->w;
+    a.face[0] = fl->face_u; a.face[1] = fl->face_v; a.face[2] = fl->face_w;
+    for (int q = 0; q < 9; ++q) a.bc[q] = fl->bc[q];
+    a.visc = fl->viscTot;
+    for (int q = 0; q < 3; ++q) a.bcvisc[q] = fl->bcvisc[q];
+    a.ew = fl->exp_weight;
+    a.nlold[0] = fl->nluOld; a.nlold[1] = fl->nlvOld; a.nlold[2] = fl->nlwOld;
+    a.p = fl->p;
+    a.nl[0] = fl->nlu; a.nl[1] = fl->nlv; a.nl[2] = fl->nlw;
+    a.fl = c.L1.fl;
+    for (int d = 0; d < 3; ++d) {
+        a.fx[d] = c.d_fx[d]; a.gx[d] = c.d_gx[d]; a.dxinv[d] = c.d_dxinv[d];
+        a.cm[d] = c.d_adm[d]; a.cp[d] = c.d_adp[d]; a.cb[d] = c.d_adb[d];
+    }
+    a.d = c.L1.d;
+    a.dt = dt;
+    a.ab2 = (advec_scheme == 1) ? 1 : 0;
+    a.vankan = (frac_step_type == 1) ? 1 : 0;
+    a.three_d = three_d ? 1 : 0;
+    launch_rhs_advec_diff(a, c.s);
+    c.last_ad = a; c.have_ad = true;
+    c.launches++;
+    CK(cudaStreamSynchronize(c.s));
+    return 0;
+}
+
 int fsi_mg_set_velocity_ghosts(void *handle, const double *coeffGCMD, const double *uBI, const double *vBI,
                                const double *wBI, double bodyInterceptWeight, double imagePointWeight)
 {
@@ -1838,9 +1897,12 @@ int fsi_mg_time_kernel(void *handle, int which, int precision, int reps, double 
             launch_correct_vel(c.last_cv, c.s);
         } else if (which == 8 && c.have_up) {
             launch_update_pressure(c.last_up_p, c.last_up_pp, c.L1.d.sxy * (c.nz + 2), c.last_up_vk, c.s);
+        } else if (which == 9 && c.have_ad) {
+            launch_rhs_advec_diff(c.last_ad, c.s);
         }
     };
-    if ((which == 6 && !c.have_fv) || (which == 7 && !c.have_cv) || (which == 8 && !c.have_up))
+    if ((which == 6 && !c.have_fv) || (which == 7 && !c.have_cv) || (which == 8 && !c.have_up) ||
+        (which == 9 && !c.have_ad))
         return fail(-1, "time_kernel 6/7/8 replay the last face_vel_rhs/correct_vel/update_pressure call; make one first");
     once();   // warm-up
     CK(cudaEventRecord(c.ev0, c.s));
@@ -1874,6 +1936,13 @@ int fsi_mg_time_kernel(void *handle, int which, int precision, int reps, double 
             for (int d = 0; d < 3; ++d) bpc += c.last_cv.bc[d] ? 8.0 : 0.0;
         } else if (which == 8) {
             bpc = 16.0 + (c.last_up_vk ? 8.0 : 0.0);
+        } else if (which == 9) {
+            // u, v, w, three faces, viscTot, flags read; nlu, nlv, nlw written; AB2 history read + written,
+            // exp_weight, p (VAN_KAN) and the non-null bc arrays read
+            const RhsAdArgs &A = c.last_ad;
+            bpc = 24.0 + 24.0 + 8.0 + 1.0 + 24.0 + (A.ab2 ? 48.0 + (A.ew ? 8.0 : 0.0) : 0.0) + (A.vankan ? 8.0 : 0.0);
+            for (int q = 0; q < 9; ++q) bpc += A.bc[q] ? 8.0 : 0.0;
+            for (int q = 0; q < 3; ++q) bpc += A.bcvisc[q] ? 8.0 : 0.0;
         }
         *alg_bytes = bpc * cells;
     }

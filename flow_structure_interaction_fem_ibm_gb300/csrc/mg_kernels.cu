@@ -1564,6 +1564,99 @@ __global__ void k_update_pressure(double *p, const double *pPrime, long long n, 
     if (t < n) p[t] = van_kan ? p[t] + pPrime[t] : pPrime[t];
 }
 
+// ---------------------------------------------------------------------------
+// Momentum right-hand side, rhs_advec_diff (IBM/CORE_RHS_AD.F90:13-75) with
+// rhs_advec (:80-382, non-hybrid), rhs_loadAB (:385-430), rhs_diff (:433-530)
+// and rhs_vankan (:550-585), one thread per interior cell and all three
+// components (each step is local to the cell, so the reference's sequence of
+// whole-array loops fuses).  FP64; mask products become selects and the
+// diffusion coefficients come from per-axis tables holding the reference's
+// products; the sums keep the reference's order.  In 2D the w component is
+// left to rhs_vankan alone, as in the reference.
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(TPB) k_rhs_advec_diff(RhsAdArgs A)
+{
+    const Dims &d = A.d;
+    const int n0 = d.m[0] - 1, n1 = d.m[1] - 1, n2 = d.m[2] - 1;
+    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= (long long)n0 * n1 * n2) return;
+    int idx[3];
+    cell_of((unsigned)t, (unsigned)n0, (unsigned)n1, idx[0], idx[1], idx[2]);
+    const long long o = d.idx(idx[0], idx[1], idx[2]);
+    const uint8_t f = A.fl[o];
+    const int naxes = A.three_d ? 3 : 2;
+    const int ncomp = A.three_d ? 3 : 2;
+    // face viscosities and diffusion coefficients (shared by the components)
+    double am[3] = {0.0, 0.0, 0.0}, ap[3] = {0.0, 0.0, 0.0}, ac[3] = {0.0, 0.0, 0.0};
+    for (int a = 0; a < naxes; ++a) {
+        const long long s = stride_of(d, a);
+        const int i = idx[a];
+        const bool mm = f & fb_minus(a), pp = f & fb_plus(a);
+        const double *V = A.visc;
+        // nuE / nuW: viscosity interpolated to the faces, bc*visc of this cell on flagged faces
+        const double nuP = pp ? bc_at(A.bcvisc[a], o) : fma(A.fx[a][i + 1], V[o + s], A.gx[a][i + 1] * V[o]);
+        const double nuM = mm ? bc_at(A.bcvisc[a], o) : fma(A.fx[a][i], V[o], A.gx[a][i] * V[o - s]);
+        const double cmv = mm ? A.cb[a][i] : A.cm[a][i];
+        const double cpv = pp ? A.cb[a][i] : A.cp[a][i];
+        am[a] = cmv * nuM;
+        ap[a] = cpv * nuP;
+        ac[a] = -(am[a] + ap[a]);
+    }
+    for (int q = 0; q < ncomp; ++q) {
+        const double *U = A.vel[q];
+        const double uc = U[o];
+        // rhs_advec
+        double adv = 0.0;
+        for (int a = 0; a < naxes; ++a) {
+            const long long s = stride_of(d, a);
+            const int i = idx[a];
+            const bool mm = f & fb_minus(a), pp = f & fb_plus(a);
+            const double *bc = A.bc[3 * q + a];
+            const double ve = pp ? bc_at(bc, o) : fma(A.fx[a][i + 1], U[o + s], A.gx[a][i + 1] * uc);
+            const double vw = mm ? bc_at(bc, o) : fma(A.fx[a][i], uc, A.gx[a][i] * U[o - s]);
+            const double term = (ve * A.face[a][o + s] - vw * A.face[a][o]) * A.dxinv[a][i];
+            adv = (a == 0) ? term : adv + term;
+        }
+        // rhs_loadAB
+        double nl;
+        if (A.ab2) {
+            const double ew = A.ew ? A.ew[o] : 1.5;
+            const double old = A.nlold[q][o];
+            nl = ew * adv - (ew - 1.0) * old;
+            A.nlold[q][o] = adv;
+        } else {
+            nl = adv * 0.5;
+        }
+        // rhs_diff: amx W + acx V + apx E + amy S + acy V + apy N + amz B + acz V + apz F
+        double diff = 0.0;
+        bool first = true;
+        for (int a = 0; a < 3; ++a) {
+            if (a >= naxes) break;
+            const long long s = stride_of(d, a);
+            const bool mm = f & fb_minus(a), pp = f & fb_plus(a);
+            const double *bc = A.bc[3 * q + a];
+            const double vW = mm ? bc_at(bc, o) : U[o - s];
+            const double vE = pp ? bc_at(bc, o) : U[o + s];
+            diff = first ? am[a] * vW : fma(am[a], vW, diff);
+            first = false;
+            diff = fma(ac[a], uc, diff);
+            diff = fma(ap[a], vE, diff);
+        }
+        A.nl[q][o] = fma(0.5 * A.dt, diff, fma(-A.dt, nl, uc));
+    }
+    if (A.vankan && !(f & FB_IB)) {
+        const double *P = A.p;
+        const double p0 = P[o];
+        for (int a = 0; a < 3; ++a) {
+            const long long s = stride_of(d, a);
+            const int i = idx[a];
+            const double pe = (f & fb_plus(a)) ? p0 : fma(A.fx[a][i + 1], P[o + s], A.gx[a][i + 1] * p0);
+            const double pw = (f & fb_minus(a)) ? p0 : fma(A.fx[a][i], p0, A.gx[a][i] * P[o - s]);
+            A.nl[a][o] = fma(-A.dt, (pe - pw) * A.dxinv[a][i], A.nl[a][o]);
+        }
+    }
+}
+
 // zero the non-interior part of a full (0:nx+1,0:ny+1,0:nz+1) array: planes
 // k = 0, nz, nz+1; then rows j = 0, ny, ny+1 of k = 1..nzc; then cells
 // i = 0, nx, nx+1 of the interior rows (the interior is written elsewhere)
@@ -2192,6 +2285,12 @@ void launch_face_vel_rhs(const StepArgs &a, bool van_kan, double *partials, int 
     if (van_kan) k_face_vel_rhs<true><<<grid, TPB, 0, s>>>(a, partials);
     else k_face_vel_rhs<false><<<grid, TPB, 0, s>>>(a, partials);
     k_sum_final<<<1, 1024, 0, s>>>(partials, bx * by * bz, 1, sums);
+}
+
+void launch_rhs_advec_diff(const RhsAdArgs &a, cudaStream_t s)
+{
+    const long long n = (long long)(a.d.m[0] - 1) * (a.d.m[1] - 1) * (a.d.m[2] - 1);
+    k_rhs_advec_diff<<<nblk(n), TPB, 0, s>>>(a);
 }
 
 void launch_correct_vel(const StepArgs &a, cudaStream_t s)

@@ -108,6 +108,26 @@ void launch_face_vel_rhs(const StepArgs &a, bool van_kan, double *partials, int 
 // correct_vel cell-centre update and face corrections (IBM/CORE_FRAC_STEP_ROUTINES.F90:244-448,
 // without the ghost-cell velocity interpolation)
 void launch_correct_vel(const StepArgs &a, cudaStream_t s);
+// Momentum right-hand side (rhs_advec_diff, IBM/CORE_RHS_AD.F90:13-585), level-1 full-layout FP64.
+struct RhsAdArgs {
+    const double *vel[3];       // u, v, w
+    const double *face[3];      // face_u, face_v, face_w
+    const double *bc[9];        // bcxu, bcyu, bczu, bcxv, ... (component-major; null = zero)
+    const double *visc;         // viscTot
+    const double *bcvisc[3];    // null = zero
+    const double *ew;           // exp_weight (null = 1.5)
+    double *nlold[3];
+    const double *p;            // VAN_KAN pressure
+    double *nl[3];
+    const uint8_t *fl;
+    const double *fx[3], *gx[3], *dxinv[3];
+    const double *cm[3], *cp[3], *cb[3];   // dcinv(i) dinv(i), dcinv(i+1) dinv(i), (2 dinv(i)) dinv(i)
+    Dims d;
+    double dt;
+    int ab2, vankan, three_d;
+};
+void launch_rhs_advec_diff(const RhsAdArgs &a, cudaStream_t s);
+
 // ghost-cell velocities u, v, w (GCM_vel_set_bc_internal); coeffD 8 per ghost, bi the
 // body-intercept velocities (3 x n: u, v, w; null = zero), scratch 6 x n doubles
 void launch_vel_ghosts(double *u, double *v, double *w, const GhostArgs &g, const double *coeffD, const double *bi,

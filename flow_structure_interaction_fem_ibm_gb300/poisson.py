@@ -34,6 +34,17 @@ class FsiMgError(RuntimeError):
     pass
 
 
+class RhsAdFields(ctypes.Structure):
+    """fsi_mg_rhs_ad_fields of include/fsi_mg.h (device pointers)."""
+    _fields_ = [("u", ctypes.c_void_p), ("v", ctypes.c_void_p), ("w", ctypes.c_void_p),
+                ("face_u", ctypes.c_void_p), ("face_v", ctypes.c_void_p), ("face_w", ctypes.c_void_p),
+                ("bc", ctypes.c_void_p * 9), ("viscTot", ctypes.c_void_p), ("bcvisc", ctypes.c_void_p * 3),
+                ("exp_weight", ctypes.c_void_p),
+                ("nluOld", ctypes.c_void_p), ("nlvOld", ctypes.c_void_p), ("nlwOld", ctypes.c_void_p),
+                ("p", ctypes.c_void_p),
+                ("nlu", ctypes.c_void_p), ("nlv", ctypes.c_void_p), ("nlw", ctypes.c_void_p)]
+
+
 def _p(a, t=_dp):
     if a is None:
         return None
@@ -139,6 +150,26 @@ class PoissonSolver:
         return _check(self.lib.fsi_mg_correct_vel(self.h, float(dt), vp(d_pPrime), vp(d_u), vp(d_v), vp(d_w),
                                                   vp(d_bc[0]), vp(d_bc[1]), vp(d_bc[2]), vp(d_face_u),
                                                   vp(d_face_v), vp(d_face_w)))
+
+    def rhs_advec_diff(self, dt: float, vel, faces, visc, nl, nl_old=(None, None, None), bc=(None,) * 9,
+                       bcvisc=(None,) * 3, exp_weight=None, p=None, advec_scheme: int = 2,
+                       frac_step_type: int = 0):
+        """rhs_advec_diff (IBM/CORE_RHS_AD.F90:13-585) on device pointers:
+        vel = (u, v, w), faces, visc (viscTot), nl = (nlu, nlv, nlw) OUT,
+        nl_old INOUT with AB2 (advec_scheme 1)."""
+        f = RhsAdFields()
+        f.u, f.v, f.w = vel
+        f.face_u, f.face_v, f.face_w = faces
+        for q in range(9):
+            f.bc[q] = bc[q]
+        f.viscTot = visc
+        for q in range(3):
+            f.bcvisc[q] = bcvisc[q]
+        f.exp_weight = exp_weight
+        f.nluOld, f.nlvOld, f.nlwOld = nl_old
+        f.p = p
+        f.nlu, f.nlv, f.nlw = nl
+        _check(self.lib.fsi_mg_rhs_advec_diff(self.h, advec_scheme, frac_step_type, float(dt), ctypes.byref(f)))
 
     def set_velocity_ghosts(self, coeffGCMD, bi=None, probe_length_normalized: float = 2.0):
         """Ghost-cell velocities for correct_vel (GCM_vel_set_bc_internal):

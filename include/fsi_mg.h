@@ -162,6 +162,35 @@ int fsi_mg_correct_vel(void *handle, double dt, const double *d_pPrime, double *
                        const double *d_bcxu, const double *d_bcyv, const double *d_bczw, double *d_face_u,
                        double *d_face_v, double *d_face_w);
 
+/* Fields of the momentum right-hand side (device arrays, full layout).  bc
+ * holds bcxu, bcyu, bczu, bcxv, bcyv, bczv, bcxw, bcyw, bczw and bcvisc
+ * bcxvisc, bcyvisc, bczvisc (IBM/AMODULES.F90 boundary_arrays; NULL entries
+ * are zero); exp_weight NULL means 1.5 everywhere (no fresh cells,
+ * IBM/BOUNDARY_FRESH_CELL.F90:25). */
+typedef struct {
+    const double *u, *v, *w;
+    const double *face_u, *face_v, *face_w;
+    const double *bc[9];
+    const double *viscTot;
+    const double *bcvisc[3];
+    const double *exp_weight;
+    double *nluOld, *nlvOld, *nlwOld;   /* INOUT with ADAMS_BASHFORTH2 */
+    const double *p;                    /* frac_step_type 1 (VAN_KAN) only */
+    double *nlu, *nlv, *nlw;            /* OUT (interior cells) */
+} fsi_mg_rhs_ad_fields;
+
+/* rhs_advec_diff (IBM/CORE_RHS_AD.F90:13-75): central advection with the face
+ * velocities (rhs_advec without the hybrid upwinding, :80-382), the
+ * Adams-Bashforth or Crank-Nicolson loading of the advection term
+ * (rhs_loadAB, :385-430; advec_scheme 1 ADAMS_BASHFORTH2, 2 CRANK_NICOLSON1,
+ * 3 CRANK_NICOLSON2), the explicit half of the diffusion with the total
+ * viscosity (rhs_diff, :433-530) and, with frac_step_type 1, the old
+ * pressure gradient (rhs_vankan, :550-585): nl = vel - dt NL + dt/2 D(vel).
+ * Uses the flags of the last fsi_mg_set_geometry (Neumann pressure sides).
+ * In 2D the w component is only touched by rhs_vankan, as in the reference. */
+int fsi_mg_rhs_advec_diff(void *handle, int advec_scheme, int frac_step_type, double dt,
+                          const fsi_mg_rhs_ad_fields *fields);
+
 /* Ghost-cell velocities of the GCM body for fsi_mg_correct_vel
  * (GCM_vel_set_bc_internal, IBM/GCM_GHOSTCELL_VEL_UPDATE_UNSTRUC.F90:126-247):
  * coeffGCMD(8,nGhost), the Dirichlet image-point weights of the ghost list

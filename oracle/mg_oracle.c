@@ -1457,3 +1457,139 @@ void or_update_pressure(or_ctx *c, int frac_step_type, const double *pPrime, dou
     for (size_t t = 0; t < nf; ++t) p[t] = (frac_step_type == 1) ? p[t] + pPrime[t] : pPrime[t];
     if (c->p.boundary_formulation == GCM_METHOD) gcm_p_set_bc_internal(c, p, c->nx + 1, c->ny + 1);
 }
+
+/* ---------------------------------------------- momentum right-hand side ---- */
+/* rhs_advec_diff (IBM/CORE_RHS_AD.F90:13-75) with its contained routines
+ * rhs_advec (:80-382, the non-hybrid branch), rhs_loadAB (:385-430), rhs_diff
+ * (:433-530) and rhs_vankan (:550-585), in the reference's call order.
+ * advec_scheme 1 ADAMS_BASHFORTH2, 2/3 CRANK_NICOLSON1/2.  Array arguments are
+ * full (0:nx+1,0:ny+1,0:nz+1) fields; bc9 holds bcxu,bcyu,bczu,bcxv,bcyv,bczv,
+ * bcxw,bcyw,bczw and bcvisc3 bcxvisc,bcyvisc,bczvisc (NULL entries: zero);
+ * exp_weight NULL: 1.5 (no fresh cells). */
+static double arr_at(const double *a, size_t f) { return a ? a[f] : 0.0; }
+
+static void rhs_advec_one(or_ctx *c, const double *vel, double *nlvel, const double *bcx, const double *bcy,
+                          const double *bcz, const double *face_u, const double *face_v, const double *face_w)
+{
+    const int8_t *ium = c->fl[0], *iup = c->fl[1], *jum = c->fl[2], *jup = c->fl[3], *kum = c->fl[4], *kup = c->fl[5];
+    for (int k = 1; k <= c->nzc; ++k)
+        for (int j = 1; j <= c->nyc; ++j)
+            for (int i = 1; i <= c->nxc; ++i) {
+                const size_t f = FI(c, i, j, k);
+                const double vele = (fxw(c, 0, i + 1) * vel[FI(c, i + 1, j, k)] + (1.0 - fxw(c, 0, i + 1)) * vel[f]) * (1 - iup[f]) + arr_at(bcx, f) * iup[f];
+                const double velw = (fxw(c, 0, i) * vel[f] + (1.0 - fxw(c, 0, i)) * vel[FI(c, i - 1, j, k)]) * (1 - ium[f]) + arr_at(bcx, f) * ium[f];
+                nlvel[f] = (vele * face_u[FI(c, i + 1, j, k)] - velw * face_u[f]) * c->dxinv[0][i];
+            }
+    for (int k = 1; k <= c->nzc; ++k)
+        for (int j = 1; j <= c->nyc; ++j)
+            for (int i = 1; i <= c->nxc; ++i) {
+                const size_t f = FI(c, i, j, k);
+                const double veln = (fxw(c, 1, j + 1) * vel[FI(c, i, j + 1, k)] + (1.0 - fxw(c, 1, j + 1)) * vel[f]) * (1 - jup[f]) + arr_at(bcy, f) * jup[f];
+                const double vels = (fxw(c, 1, j) * vel[f] + (1.0 - fxw(c, 1, j)) * vel[FI(c, i, j - 1, k)]) * (1 - jum[f]) + arr_at(bcy, f) * jum[f];
+                nlvel[f] = nlvel[f] + (veln * face_v[FI(c, i, j + 1, k)] - vels * face_v[f]) * c->dxinv[1][j];
+            }
+    if (c->p.ndim == DIM_3D)
+        for (int k = 1; k <= c->nzc; ++k)
+            for (int j = 1; j <= c->nyc; ++j)
+                for (int i = 1; i <= c->nxc; ++i) {
+                    const size_t f = FI(c, i, j, k);
+                    const double velf = (fxw(c, 2, k + 1) * vel[FI(c, i, j, k + 1)] + (1.0 - fxw(c, 2, k + 1)) * vel[f]) * (1 - kup[f]) + arr_at(bcz, f) * kup[f];
+                    const double velb = (fxw(c, 2, k) * vel[f] + (1.0 - fxw(c, 2, k)) * vel[FI(c, i, j, k - 1)]) * (1 - kum[f]) + arr_at(bcz, f) * kum[f];
+                    nlvel[f] = nlvel[f] + (velf * face_w[FI(c, i, j, k + 1)] - velb * face_w[f]) * c->dxinv[2][k];
+                }
+}
+
+static void rhs_load_ab(or_ctx *c, int advec_scheme, const double *exp_weight, double *nlvel, double *nlvelOld)
+{
+    for (int k = 1; k <= c->nzc; ++k)
+        for (int j = 1; j <= c->nyc; ++j)
+            for (int i = 1; i <= c->nxc; ++i) {
+                const size_t f = FI(c, i, j, k);
+                if (advec_scheme == 1) {
+                    const double ew = exp_weight ? exp_weight[f] : 1.5;
+                    const double tempvel = ew * nlvel[f] - (ew - 1.0) * nlvelOld[f];
+                    nlvelOld[f] = nlvel[f];
+                    nlvel[f] = tempvel;
+                } else {
+                    nlvel[f] = nlvel[f] * 0.5;
+                }
+            }
+}
+
+static void rhs_diff_one(or_ctx *c, double dt, const double *vel, double *nlvel, const double *bcx, const double *bcy,
+                         const double *bcz, const double *visc, const double *const *bcvisc3)
+{
+    const int8_t *ium = c->fl[0], *iup = c->fl[1], *jum = c->fl[2], *jup = c->fl[3], *kum = c->fl[4], *kup = c->fl[5];
+    const double rnDim = (double)(c->p.ndim - DIM_2D);
+    for (int k = 1; k <= c->nzc; ++k)
+        for (int j = 1; j <= c->nyc; ++j)
+            for (int i = 1; i <= c->nxc; ++i) {
+                const size_t f = FI(c, i, j, k);
+                const double nuE = (fxw(c, 0, i + 1) * visc[FI(c, i + 1, j, k)] + (1.0 - fxw(c, 0, i + 1)) * visc[f]) * (1 - iup[f]) + arr_at(bcvisc3[0], f) * iup[f];
+                const double nuW = (fxw(c, 0, i) * visc[f] + (1.0 - fxw(c, 0, i)) * visc[FI(c, i - 1, j, k)]) * (1 - ium[f]) + arr_at(bcvisc3[0], f) * ium[f];
+                const double nuN = (fxw(c, 1, j + 1) * visc[FI(c, i, j + 1, k)] + (1.0 - fxw(c, 1, j + 1)) * visc[f]) * (1 - jup[f]) + arr_at(bcvisc3[1], f) * jup[f];
+                const double nuS = (fxw(c, 1, j) * visc[f] + (1.0 - fxw(c, 1, j)) * visc[FI(c, i, j - 1, k)]) * (1 - jum[f]) + arr_at(bcvisc3[1], f) * jum[f];
+                const double nuF = (fxw(c, 2, k + 1) * visc[FI(c, i, j, k + 1)] + (1.0 - fxw(c, 2, k + 1)) * visc[f]) * (1 - kup[f]) + arr_at(bcvisc3[2], f) * kup[f];
+                const double nuB = (fxw(c, 2, k) * visc[f] + (1.0 - fxw(c, 2, k)) * visc[FI(c, i, j, k - 1)]) * (1 - kum[f]) + arr_at(bcvisc3[2], f) * kum[f];
+                double amx = (c->dxcinv[0][i] * (1 - ium[f]) + c->dxinv[0][i] * ium[f] * 2.0) * c->dxinv[0][i];
+                double apx = (c->dxcinv[0][i + 1] * (1 - iup[f]) + c->dxinv[0][i] * iup[f] * 2.0) * c->dxinv[0][i];
+                amx = amx * nuW;
+                apx = apx * nuE;
+                const double acx = -(amx + apx);
+                double amy = (c->dxcinv[1][j] * (1 - jum[f]) + c->dxinv[1][j] * jum[f] * 2.0) * c->dxinv[1][j];
+                double apy = (c->dxcinv[1][j + 1] * (1 - jup[f]) + c->dxinv[1][j] * jup[f] * 2.0) * c->dxinv[1][j];
+                amy = amy * nuS;
+                apy = apy * nuN;
+                const double acy = -(amy + apy);
+                double amz = (c->dxcinv[2][k] * (1 - kum[f]) + c->dxinv[2][k] * kum[f] * 2.0) * c->dxinv[2][k] * rnDim;
+                double apz = (c->dxcinv[2][k + 1] * (1 - kup[f]) + c->dxinv[2][k] * kup[f] * 2.0) * c->dxinv[2][k] * rnDim;
+                amz = amz * nuB;
+                apz = apz * nuF;
+                const double acz = -(amz + apz);
+                const double diffvel = amx * (vel[FI(c, i - 1, j, k)] * (1 - ium[f]) + arr_at(bcx, f) * ium[f])
+                                     + acx * vel[f]
+                                     + apx * (vel[FI(c, i + 1, j, k)] * (1 - iup[f]) + arr_at(bcx, f) * iup[f])
+                                     + amy * (vel[FI(c, i, j - 1, k)] * (1 - jum[f]) + arr_at(bcy, f) * jum[f])
+                                     + acy * vel[f]
+                                     + apy * (vel[FI(c, i, j + 1, k)] * (1 - jup[f]) + arr_at(bcy, f) * jup[f])
+                                     + amz * (vel[FI(c, i, j, k - 1)] * (1 - kum[f]) + arr_at(bcz, f) * kum[f])
+                                     + acz * vel[f]
+                                     + apz * (vel[FI(c, i, j, k + 1)] * (1 - kup[f]) + arr_at(bcz, f) * kup[f]);
+                nlvel[f] = vel[f] - dt * nlvel[f] + 0.5 * dt * diffvel;
+            }
+}
+
+void or_rhs_advec_diff(or_ctx *c, int advec_scheme, int frac_step_type, double dt, const double *u,
+                       const double *v, const double *w, const double *face_u, const double *face_v,
+                       const double *face_w, const double *const *bc9, const double *visc,
+                       const double *const *bcvisc3, const double *exp_weight, double *nluOld, double *nlvOld,
+                       double *nlwOld, const double *p, double *nlu, double *nlv, double *nlw)
+{
+    const int three_d = (c->p.ndim == DIM_3D);
+    rhs_advec_one(c, u, nlu, bc9[0], bc9[1], bc9[2], face_u, face_v, face_w);
+    rhs_advec_one(c, v, nlv, bc9[3], bc9[4], bc9[5], face_u, face_v, face_w);
+    if (three_d) rhs_advec_one(c, w, nlw, bc9[6], bc9[7], bc9[8], face_u, face_v, face_w);
+    rhs_load_ab(c, advec_scheme, exp_weight, nlu, nluOld);
+    rhs_load_ab(c, advec_scheme, exp_weight, nlv, nlvOld);
+    if (three_d) rhs_load_ab(c, advec_scheme, exp_weight, nlw, nlwOld);
+    rhs_diff_one(c, dt, u, nlu, bc9[0], bc9[1], bc9[2], visc, bcvisc3);
+    rhs_diff_one(c, dt, v, nlv, bc9[3], bc9[4], bc9[5], visc, bcvisc3);
+    if (three_d) rhs_diff_one(c, dt, w, nlw, bc9[6], bc9[7], bc9[8], visc, bcvisc3);
+    if (frac_step_type == 1) {   /* rhs_vankan */
+        const int8_t *ium = c->fl[0], *iup = c->fl[1], *jum = c->fl[2], *jup = c->fl[3], *kum = c->fl[4], *kup = c->fl[5];
+        for (int k = 1; k <= c->nzc; ++k)
+            for (int j = 1; j <= c->nyc; ++j)
+                for (int i = 1; i <= c->nxc; ++i) {
+                    const size_t f = FI(c, i, j, k);
+                    const double pe = (fxw(c, 0, i + 1) * p[FI(c, i + 1, j, k)] + (1.0 - fxw(c, 0, i + 1)) * p[f]) * (1 - iup[f]) + p[f] * iup[f];
+                    const double pw = (fxw(c, 0, i) * p[f] + (1.0 - fxw(c, 0, i)) * p[FI(c, i - 1, j, k)]) * (1 - ium[f]) + p[f] * ium[f];
+                    const double pn = (fxw(c, 1, j + 1) * p[FI(c, i, j + 1, k)] + (1.0 - fxw(c, 1, j + 1)) * p[f]) * (1 - jup[f]) + p[f] * jup[f];
+                    const double ps = (fxw(c, 1, j) * p[f] + (1.0 - fxw(c, 1, j)) * p[FI(c, i, j - 1, k)]) * (1 - jum[f]) + p[f] * jum[f];
+                    const double pf = (fxw(c, 2, k + 1) * p[FI(c, i, j, k + 1)] + (1.0 - fxw(c, 2, k + 1)) * p[f]) * (1 - kup[f]) + p[f] * kup[f];
+                    const double pb = (fxw(c, 2, k) * p[f] + (1.0 - fxw(c, 2, k)) * p[FI(c, i, j, k - 1)]) * (1 - kum[f]) + p[f] * kum[f];
+                    nlu[f] = nlu[f] - dt * ((pe - pw) * c->dxinv[0][i]) * (double)(1 - c->iblank[f]);
+                    nlv[f] = nlv[f] - dt * ((pn - ps) * c->dxinv[1][j]) * (double)(1 - c->iblank[f]);
+                    nlw[f] = nlw[f] - dt * ((pf - pb) * c->dxinv[2][k]) * (double)(1 - c->iblank[f]);
+                }
+    }
+}

@@ -96,4 +96,10 @@ void    or_update_pressure(or_ctx *c, int frac_step_type, const double *pPrime, 
 void    or_set_vel_ghosts(or_ctx *c, const double *coeffD, const double *uBI, const double *vBI,
                           const double *wBI, double bodyInterceptWeight, double imagePointWeight);
 int     or_vel_ghost_iters(or_ctx *c);
+/* rhs_advec_diff; bc9 = bcxu,bcyu,bczu,bcxv,bcyv,bczv,bcxw,bcyw,bczw, bcvisc3 = bcx/y/zvisc (entries may be NULL) */
+void    or_rhs_advec_diff(or_ctx *c, int advec_scheme, int frac_step_type, double dt, const double *u,
+                          const double *v, const double *w, const double *face_u, const double *face_v,
+                          const double *face_w, const double *const *bc9, const double *visc,
+                          const double *const *bcvisc3, const double *exp_weight, double *nluOld, double *nlvOld,
+                          double *nlwOld, const double *p, double *nlu, double *nlv, double *nlw);
 #endif

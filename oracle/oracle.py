@@ -90,6 +90,9 @@ def lib():
         L.or_set_vel_ghosts.argtypes = [ctypes.c_void_p] + [_dp] * 4 + [ctypes.c_double] * 2
         L.or_set_vel_ghosts.restype = None
         L.or_vel_ghost_iters.argtypes = [ctypes.c_void_p]
+        L.or_rhs_advec_diff.argtypes = ([ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_double] + [_dp] * 6
+                                        + [ctypes.POINTER(_dp), _dp, ctypes.POINTER(_dp)] + [_dp] * 8)
+        L.or_rhs_advec_diff.restype = None
         _lib = L
     return _lib
 
@@ -212,6 +215,17 @@ class Oracle:
 
     def vel_ghost_iters(self):
         return lib().or_vel_ghost_iters(self.h)
+
+    def rhs_advec_diff(self, dt, u, v, w, faces, visc, nl_old, nl, bc9=(None,) * 9, bcvisc=(None,) * 3,
+                       exp_weight=None, p=None, advec_scheme=2, frac_step_type=0):
+        """rhs_advec_diff; nl_old (AB2 history) and nl (nlu, nlv, nlw) are
+        updated in place.  advec_scheme 1 ADAMS_BASHFORTH2, 2/3 CRANK_NICOLSON."""
+        b9 = (_dp * 9)(*[_p(a) for a in bc9])
+        b3 = (_dp * 3)(*[_p(a) for a in bcvisc])
+        lib().or_rhs_advec_diff(self.h, advec_scheme, frac_step_type, dt, _p(u), _p(v), _p(w), *(_p(a) for a in faces),
+                                b9, _p(visc), b3, _p(exp_weight), *(_p(a) for a in nl_old), _p(p),
+                                *(_p(a) for a in nl))
+        return nl
 
     def update_pressure(self, pPrime, p, frac_step_type=0):
         lib().or_update_pressure(self.h, frac_step_type, _p(pPrime), _p(p))
