@@ -50,6 +50,9 @@ SOLVER_SYMBOLS = {
     "fsi_mg_correct_vel": [ctypes.c_void_p, ctypes.c_double] + [ctypes.c_void_p] * 10,
     "fsi_mg_update_pressure": [ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p],
     "fsi_mg_rhs_advec_diff": [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_double, ctypes.c_void_p],
+    "fsi_mg_rhs_adjust_bc": [ctypes.c_void_p, ctypes.c_int, ctypes.c_double, ctypes.c_void_p],
+    "fsi_mg_solve_ad": [ctypes.c_void_p, ctypes.c_int, ctypes.c_double, ctypes.c_void_p, ctypes.c_void_p,
+                        ctypes.c_void_p, ctypes.c_void_p, c_int_p, c_double_p],
     "fsi_mg_set_velocity_ghosts": [ctypes.c_void_p, c_double_p, c_double_p, c_double_p, c_double_p,
                                    ctypes.c_double, ctypes.c_double],
     "fsi_mg_last_error": [],

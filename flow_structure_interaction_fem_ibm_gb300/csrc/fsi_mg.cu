@@ -136,6 +136,7 @@ struct Ctx {
     StepArgs last_fv{}, last_cv{};
     RhsAdArgs last_ad{};
     bool have_ad = false;
+    double *ad_co = nullptr;   // 7 coefficient fields of the implicit momentum operator + gam scratch
     bool have_fv = false, have_cv = false, have_up = false, last_fv_vk = false, last_up_vk = false;
     double *last_up_p = nullptr;
     const double *last_up_pp = nullptr;
@@ -1651,6 +1652,109 @@ int fsi_mg_rhs_advec_diff(void *handle, int advec_scheme, int frac_step_type, do
     c.launches++;
     CK(cudaStreamSynchronize(c.s));
     return 0;
+}
+
+static int ad_coef_args(Ctx &c, int advec_scheme, double dt, const fsi_mg_rhs_ad_fields *fl, AdCoefArgs &a)
+{
+    if (advec_scheme < 1 || advec_scheme > 2)
+        return fail(-1, "advec_scheme must be 1 (AB2) or 2 (CRANK_NICOLSON1); CRANK_NICOLSON2 re-evaluates "
+                        "face_vel inside the iteration and is not supported");
+    if (!(dt > 0.0)) return fail(-1, "dt must be positive");
+    TRY(step_ready(c));
+    const bool three_d = (c.p.ndim == 3);
+    if (!fl || !fl->face_u || !fl->face_v || !fl->face_w || !fl->viscTot) return fail(-1, "null field");
+    const long long n = c.L1.d.sxy * (c.nz + 2);
+    if (!c.ad_co) TRY(c.alloc(&c.ad_co, (size_t)(8 * n)));
+    a = AdCoefArgs{};
+    a.face[0] = fl->face_u; a.face[1] = fl->face_v; a.face[2] = fl->face_w;
+    a.visc = fl->viscTot;
+    for (int q = 0; q < 3; ++q) a.bcvisc[q] = fl->bcvisc[q];
+    for (int q = 0; q < 7; ++q) a.co[q] = c.ad_co + q * n;
+    a.fl = c.L1.fl;
+    for (int d = 0; d < 3; ++d) {
+        a.fx[d] = c.d_fx[d]; a.gx[d] = c.d_gx[d]; a.dxinv[d] = c.d_dxinv[d];
+        a.cm[d] = c.d_adm[d]; a.cp[d] = c.d_adp[d]; a.cb[d] = c.d_adb[d];
+    }
+    a.d = c.L1.d;
+    a.dt = dt;
+    a.half_dt = (advec_scheme == 1) ? 0.0 : 0.5 * dt;
+    a.three_d = three_d ? 1 : 0;
+    return 0;
+}
+
+int fsi_mg_rhs_adjust_bc(void *handle, int advec_scheme, double dt, const fsi_mg_rhs_ad_fields *fl)
+{
+    if (!handle || !fl) return fail(-1, "null argument");
+    Ctx &c = *(Ctx *)handle;
+    AdCoefArgs a;
+    TRY(ad_coef_args(c, advec_scheme, dt, fl, a));
+    if (!fl->nlu || !fl->nlv || !fl->nlw) return fail(-1, "null nlu/nlv/nlw");
+    double *nl[3] = {fl->nlu, fl->nlv, fl->nlw};
+    launch_rhs_adjust_bc(a, fl->bc, nl, c.s);
+    c.launches++;
+    CK(cudaStreamSynchronize(c.s));
+    return 0;
+}
+
+int fsi_mg_solve_ad(void *handle, int advec_scheme, double dt, const fsi_mg_rhs_ad_fields *fl, double *d_u,
+                    double *d_v, double *d_w, int *iters, double *maxres)
+{
+    if (!handle || !fl || !d_u || !d_v) return fail(-1, "null argument");
+    Ctx &c = *(Ctx *)handle;
+    AdCoefArgs a;
+    TRY(ad_coef_args(c, advec_scheme, dt, fl, a));
+    const bool three_d = (c.p.ndim == 3);
+    const bool gcm_vel = (c.p.boundary_formulation == GCM_METHOD) && c.vg_on && c.nGhost > 0;
+    if ((three_d || gcm_vel) && !d_w) return fail(-1, "null w (3D, or ghost-cell velocities)");
+    if (!fl->nlu || !fl->nlv || (three_d && !fl->nlw)) return fail(-1, "null nlu/nlv/nlw");
+    for (int q = 0; q < 6; ++q)
+        if (c.p.bc[q] == BC_ZERO_GRADIENT)
+            return fail(-1, "zero-gradient velocity faces need the mass-flux correction of GCM_GhostCell_Vel, "
+                            "which is not supported");
+    const long long n = c.L1.d.sxy * (c.nz + 2);
+    double *gam = c.ad_co + 7 * n;
+    launch_ad_coef(a, c.s);
+    c.launches++;
+    double *vel[3] = {d_u, d_v, d_w};
+    const double *rr[3] = {fl->nlu, fl->nlv, fl->nlw};
+    const int ncomp = three_d ? 3 : 2;
+    auto residual = [&](double &mr) -> int {
+        CK(cudaMemsetAsync(c.d_maxd, 0, sizeof(unsigned long long), c.s));
+        for (int q = 0; q < ncomp; ++q) launch_ad_residual(a, vel[q], rr[q], c.d_maxd, c.s);
+        c.launches += ncomp;
+        unsigned long long bits = 0;
+        CK(cudaMemcpyAsync(&bits, c.d_maxd, sizeof(bits), cudaMemcpyDeviceToHost, c.s));
+        CK(cudaStreamSynchronize(c.s));
+        std::memcpy(&mr, &bits, sizeof(mr));
+        return 0;
+    };
+    double mr = 0.0;
+    TRY(residual(mr));
+    const bool gcm = (c.p.boundary_formulation == GCM_METHOD);
+    if (gcm) mr = 1.0e10;   // the GCM branch starts its loop unconditionally (IBM/CORE_SOLVE_AD.F90:235)
+    int it = 0, rc = 0;
+    while (it < c.p.iterMax_ad && mr > c.p.restol_ad) {
+        for (int q = 0; q < ncomp; ++q)
+            for (int dir = 0; dir < (three_d ? 3 : 2); ++dir)
+                for (int col = 0; col < 2; ++col) {
+                    launch_ad_line(dir, col, a, vel[q], rr[q], gam, c.s);
+                    c.launches++;
+                }
+        if (gcm && c.vg_on && c.nGhost > 0) {   // GCM_GhostCell_Vel
+            CK(cudaMemsetAsync(c.d_iters, 0, sizeof(int), c.s));
+            CK(cudaMemsetAsync(c.d_maxd, 0, sizeof(unsigned long long), c.s));
+            GhostArgs g{c.nGhost, c.gidx, c.sidx, c.gsg};
+            launch_vel_ghosts(d_u, d_v, d_w, g, c.vg_coeff, c.vg_bi_set ? c.vg_bi : nullptr,
+                              c.vg_bw, c.vg_iw, c.vg_scr, c.p.iterMax_ad, c.p.restol_ad, c.d_iters, c.d_maxd, c.s);
+            c.launches++;
+        }
+        TRY(residual(mr));
+        ++it;
+    }
+    if (it >= c.p.iterMax_ad && mr > c.p.restol_ad) rc = 1;   // the reference prints and continues
+    if (iters) *iters = it;
+    if (maxres) *maxres = mr;
+    return rc;
 }
 
 int fsi_mg_set_velocity_ghosts(void *handle, const double *coeffGCMD, const double *uBI, const double *vBI,

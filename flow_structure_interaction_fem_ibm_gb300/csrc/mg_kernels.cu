@@ -1657,6 +1657,176 @@ __global__ void __launch_bounds__(TPB) k_rhs_advec_diff(RhsAdArgs A)
     }
 }
 
+// ---------------------------------------------------------------------------
+// Implicit momentum solve (solve_ad, LSOR branch; IBM/CORE_SOLVE_AD.F90:12-907,
+// IBM/CORE_SET_SOLVERS.F90:20-95).  The row of a cell is fixed during the
+// iteration, so k_ad_coef forms it once per call: the implicit diffusion
+// coefficients of set_solve_ad (-(dt/2 nu_face) times the metric products of
+// the tables cm / cp / cb) and the Crank-Nicolson convective terms, masked as
+// the sweeps and the residual use them.
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(TPB) k_ad_coef(AdCoefArgs A)
+{
+    const Dims &d = A.d;
+    const int n0 = d.m[0] - 1, n1 = d.m[1] - 1, n2 = d.m[2] - 1;
+    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= (long long)n0 * n1 * n2) return;
+    int idx[3];
+    cell_of((unsigned)t, (unsigned)n0, (unsigned)n1, idx[0], idx[1], idx[2]);
+    const long long o = d.idx(idx[0], idx[1], idx[2]);
+    const uint8_t f = A.fl[o];
+    double acs = 0.0;
+    for (int a = 0; a < 3; ++a) {
+        const long long s = stride_of(d, a);
+        const int i = idx[a];
+        const bool mm = f & fb_minus(a), pp = f & fb_plus(a);
+        const double *V = A.visc;
+        const double nuP = pp ? bc_at(A.bcvisc[a], o) : fma(A.fx[a][i + 1], V[o + s], A.gx[a][i + 1] * V[o]);
+        const double nuM = mm ? bc_at(A.bcvisc[a], o) : fma(A.fx[a][i], V[o], A.gx[a][i] * V[o - s]);
+        const double rn = (a == 2 && !A.three_d) ? 0.0 : 1.0;
+        double am = -(0.5 * A.dt * nuM) * (mm ? A.cb[a][i] : A.cm[a][i]) * rn;
+        double ap = -(0.5 * A.dt * nuP) * (pp ? A.cb[a][i] : A.cp[a][i]) * rn;
+        double ac = -(am + ap);
+        const double F0 = A.face[a][o], F1 = A.face[a][o + s], di = A.dxinv[a][i];
+        am = am - A.half_dt * F0 * A.gx[a][i] * di;
+        ap = ap + A.half_dt * F1 * A.fx[a][i + 1] * di;
+        const double t1 = mm ? 0.0 : A.fx[a][i], t2 = pp ? 0.0 : A.gx[a][i + 1];
+        ac = ac + A.half_dt * (F1 * t2 - F0 * t1) * di;
+        A.co[2 * a][o] = mm ? 0.0 : am;
+        A.co[2 * a + 1][o] = pp ? 0.0 : ap;
+        acs = (a == 0) ? ac : acs + ac;
+    }
+    A.co[6][o] = acs;
+}
+
+// rhs_adjust_bc: the coefficients of rhs_adjust_bc differ from the row's in
+// the convective weights of flagged faces (tmp1 = (1 - fx) (1 - m) + m,
+// tmp2 = fx (1 - p) + p), so they are formed here again.
+__global__ void __launch_bounds__(TPB) k_rhs_adjust_bc(AdCoefArgs A, const double *b0, const double *b1,
+                                                       const double *b2, const double *b3, const double *b4,
+                                                       const double *b5, const double *b6, const double *b7,
+                                                       const double *b8, double *nl0, double *nl1, double *nl2)
+{
+    const Dims &d = A.d;
+    const int n0 = d.m[0] - 1, n1 = d.m[1] - 1, n2 = d.m[2] - 1;
+    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= (long long)n0 * n1 * n2) return;
+    int idx[3];
+    cell_of((unsigned)t, (unsigned)n0, (unsigned)n1, idx[0], idx[1], idx[2]);
+    const long long o = d.idx(idx[0], idx[1], idx[2]);
+    const uint8_t f = A.fl[o];
+    double md[3], pd[3];
+    for (int a = 0; a < 3; ++a) {
+        const long long s = stride_of(d, a);
+        const int i = idx[a];
+        const bool mm = f & fb_minus(a), pp = f & fb_plus(a);
+        const double *V = A.visc;
+        const double nuP = pp ? bc_at(A.bcvisc[a], o) : fma(A.fx[a][i + 1], V[o + s], A.gx[a][i + 1] * V[o]);
+        const double nuM = mm ? bc_at(A.bcvisc[a], o) : fma(A.fx[a][i], V[o], A.gx[a][i] * V[o - s]);
+        const double rn = (a == 2 && !A.three_d) ? 0.0 : 1.0;
+        double am = -(0.5 * A.dt * nuM) * (mm ? A.cb[a][i] : A.cm[a][i]) * rn;
+        double ap = -(0.5 * A.dt * nuP) * (pp ? A.cb[a][i] : A.cp[a][i]) * rn;
+        const double t1 = mm ? 1.0 : A.gx[a][i], t2 = pp ? 1.0 : A.fx[a][i + 1];
+        md[a] = am - A.half_dt * A.face[a][o] * t1 * A.dxinv[a][i];
+        pd[a] = ap + A.half_dt * A.face[a][o + s] * t2 * A.dxinv[a][i];
+    }
+    const double *bc[9] = {b0, b1, b2, b3, b4, b5, b6, b7, b8};
+    double *nl[3] = {nl0, nl1, nl2};
+    for (int q = 0; q < 3; ++q) {
+        if (!nl[q]) continue;
+        double v = nl[q][o];
+        for (int a = 0; a < 3; ++a) {
+            const double *b = bc[3 * q + a];
+            if (f & fb_minus(a)) v = fma(-md[a], bc_at(b, o), v);
+            if (f & fb_plus(a)) v = fma(-pd[a], bc_at(b, o), v);
+        }
+        nl[q][o] = v;
+    }
+}
+
+// One colour of the line sweep along DIR (itsolv_ad_x/y/z): one thread per
+// line, lines of colour (q1 + q2) mod 2 over the transverse indices; the
+// row is assembled as the reference does (identity rows for blanked cells,
+// the ghost's own value kept) and solved by the Thomas algorithm of tdma
+// (IBM/CORE_TDMA.F90:10-34) with gam in a scratch array.
+template <int DIR>
+__global__ void __launch_bounds__(TPB) k_ad_line(AdCoefArgs A, double *var, const double *r, double *gam, int colour)
+{
+    const Dims &d = A.d;
+    using X = Axes<DIR>;
+    const int nb = d.m[X::b] - 1, nc = d.m[X::c] - 1, L = d.m[X::a] - 1;
+    const long long sa = stride_of(d, X::a), sb = stride_of(d, X::b), sc = stride_of(d, X::c);
+    const int hb = (nb + 1) >> 1;
+    const long long tl = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (tl >= (long long)hb * nc) return;
+    const int q = 1 + (int)(tl / hb);
+    const int p0 = (((1 + q) & 1) == colour) ? 1 : 2;
+    const int p = p0 + 2 * (int)(tl - (long long)(q - 1) * hb);
+    if (p > nb) return;
+    const long long base = p * sb + q * sc;
+    // the transverse axes in the reference's order of the right-hand side terms
+    const int t1 = X::b < X::c ? X::b : X::c, t2 = X::b < X::c ? X::c : X::b;
+    const long long s1 = stride_of(d, t1), s2 = stride_of(d, t2);
+    double binv = 0.0, uprev = 0.0, cprev = 0.0;
+    for (int i = 1; i <= L; ++i) {
+        const long long o = base + i * sa;
+        const uint8_t f = A.fl[o];
+        const double rib = (f & FB_IB) ? 0.0 : 1.0;
+        double rhs;
+        if (DIR == 2) {   // z-lines subtract term by term, y before x (IBM/CORE_SOLVE_AD.F90:678-681)
+            rhs = r[o] - var[o - s2] * A.co[2 * t2][o] - var[o + s2] * A.co[2 * t2 + 1][o]
+                  - var[o - s1] * A.co[2 * t1][o] - var[o + s1] * A.co[2 * t1 + 1][o];
+        } else {          // x- and y-lines subtract one sum, lower axis first
+            const double sm = var[o - s1] * A.co[2 * t1][o] + var[o + s1] * A.co[2 * t1 + 1][o]
+                              + var[o - s2] * A.co[2 * t2][o] + var[o + s2] * A.co[2 * t2 + 1][o];
+            rhs = r[o] - sm;
+        }
+        const double aa = A.co[2 * DIR][o] * rib, cc = A.co[2 * DIR + 1][o] * rib;
+        const double bb = 1.0 + A.co[6][o] * rib;
+        const double dd = rhs * rib + ((f & FB_GM) ? var[o] : 0.0);
+        if (i == 1) {
+            binv = 1.0 / bb;
+            uprev = dd * binv;
+        } else {
+            const double g = cprev * binv;
+            gam[o] = g;
+            binv = 1.0 / (bb - aa * g);
+            uprev = (dd - aa * uprev) * binv;
+        }
+        var[o] = uprev;   // the forward solution; the row's own value was read above
+        cprev = cc;
+    }
+    for (int i = L - 1; i >= 1; --i) {
+        const long long o = base + i * sa;
+        var[o] = var[o] - gam[o + sa] * var[o + sa];
+    }
+}
+
+__global__ void __launch_bounds__(TPB) k_ad_residual(AdCoefArgs A, const double *var, const double *r,
+                                                     unsigned long long *maxbits)
+{
+    const Dims &d = A.d;
+    const int n0 = d.m[0] - 1, n1 = d.m[1] - 1, n2 = d.m[2] - 1;
+    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    double res = 0.0;
+    if (t < (long long)n0 * n1 * n2) {
+        int idx[3];
+        cell_of((unsigned)t, (unsigned)n0, (unsigned)n1, idx[0], idx[1], idx[2]);
+        const long long o = d.idx(idx[0], idx[1], idx[2]);
+        if (!(A.fl[o] & FB_IB)) {
+            double v = r[o] - var[o] * (1.0 + A.co[6][o]);
+            for (int a = 0; a < 3; ++a) {
+                const long long s = stride_of(d, a);
+                v = v - var[o - s] * A.co[2 * a][o];
+                v = v - var[o + s] * A.co[2 * a + 1][o];
+            }
+            res = fabs(v);
+        }
+    }
+    for (int off = 16; off > 0; off >>= 1) res = fmax(res, __shfl_xor_sync(0xffffffffu, res, off));
+    if ((threadIdx.x & 31) == 0 && res > 0.0) atomicMax(maxbits, (unsigned long long)__double_as_longlong(res));
+}
+
 // zero the non-interior part of a full (0:nx+1,0:ny+1,0:nz+1) array: planes
 // k = 0, nz, nz+1; then rows j = 0, ny, ny+1 of k = 1..nzc; then cells
 // i = 0, nx, nx+1 of the interior rows (the interior is written elsewhere)
@@ -2291,6 +2461,37 @@ void launch_rhs_advec_diff(const RhsAdArgs &a, cudaStream_t s)
 {
     const long long n = (long long)(a.d.m[0] - 1) * (a.d.m[1] - 1) * (a.d.m[2] - 1);
     k_rhs_advec_diff<<<nblk(n), TPB, 0, s>>>(a);
+}
+
+void launch_ad_coef(const AdCoefArgs &a, cudaStream_t s)
+{
+    const long long n = (long long)(a.d.m[0] - 1) * (a.d.m[1] - 1) * (a.d.m[2] - 1);
+    k_ad_coef<<<nblk(n), TPB, 0, s>>>(a);
+}
+
+void launch_rhs_adjust_bc(const AdCoefArgs &c, const double *const bc[9], double *const nl[3], cudaStream_t s)
+{
+    const long long n = (long long)(c.d.m[0] - 1) * (c.d.m[1] - 1) * (c.d.m[2] - 1);
+    k_rhs_adjust_bc<<<nblk(n), TPB, 0, s>>>(c, bc[0], bc[1], bc[2], bc[3], bc[4], bc[5], bc[6], bc[7], bc[8], nl[0],
+                                            nl[1], nl[2]);
+}
+
+void launch_ad_line(int dir, int colour, const AdCoefArgs &c, double *var, const double *r, double *gam,
+                    cudaStream_t s)
+{
+    const int a = dir, b = (dir == 0) ? 1 : 0, cc = (dir == 2) ? 1 : 2;
+    const long long lines = (long long)((c.d.m[b] - 1 + 1) / 2) * (c.d.m[cc] - 1);
+    if (dir == 0) k_ad_line<0><<<nblk(lines), TPB, 0, s>>>(c, var, r, gam, colour);
+    else if (dir == 1) k_ad_line<1><<<nblk(lines), TPB, 0, s>>>(c, var, r, gam, colour);
+    else k_ad_line<2><<<nblk(lines), TPB, 0, s>>>(c, var, r, gam, colour);
+    (void)a;
+}
+
+void launch_ad_residual(const AdCoefArgs &c, const double *var, const double *r, unsigned long long *maxbits,
+                        cudaStream_t s)
+{
+    const long long n = (long long)(c.d.m[0] - 1) * (c.d.m[1] - 1) * (c.d.m[2] - 1);
+    k_ad_residual<<<nblk(n), TPB, 0, s>>>(c, var, r, maxbits);
 }
 
 void launch_correct_vel(const StepArgs &a, cudaStream_t s)

@@ -128,6 +128,31 @@ struct RhsAdArgs {
 };
 void launch_rhs_advec_diff(const RhsAdArgs &a, cudaStream_t s);
 
+// Implicit momentum operator (set_solve_ad + the Crank-Nicolson convective terms of
+// itsolv_ad / calc_residual_ad): per cell the masked off-diagonals co[2a] = am_a (1 - m_a),
+// co[2a+1] = ap_a (1 - p_a) and co[6] = acx + acy + acz (unmasked, without the 1).
+struct AdCoefArgs {
+    const double *face[3];
+    const double *visc;
+    const double *bcvisc[3];
+    double *co[7];
+    const uint8_t *fl;
+    const double *fx[3], *gx[3], *dxinv[3];
+    const double *cm[3], *cp[3], *cb[3];
+    Dims d;
+    double dt, half_dt;
+    int three_d;
+};
+void launch_ad_coef(const AdCoefArgs &a, cudaStream_t s);
+// rhs_adjust_bc (IBM/CORE_RHS_AD.F90:588-780): nl -= (boundary values of flagged faces) x coefficients
+void launch_rhs_adjust_bc(const AdCoefArgs &c, const double *const bc[9], double *const nl[3], cudaStream_t s);
+// one colour of the line sweep of itsolv_ad along axis dir on var with right-hand side r
+void launch_ad_line(int dir, int colour, const AdCoefArgs &c, double *var, const double *r, double *gam,
+                    cudaStream_t s);
+// max |calc_residual_ad| of var into *maxbits (as the bits of a non-negative double, atomicMax)
+void launch_ad_residual(const AdCoefArgs &c, const double *var, const double *r, unsigned long long *maxbits,
+                        cudaStream_t s);
+
 // ghost-cell velocities u, v, w (GCM_vel_set_bc_internal); coeffD 8 per ghost, bi the
 // body-intercept velocities (3 x n: u, v, w; null = zero), scratch 6 x n doubles
 void launch_vel_ghosts(double *u, double *v, double *w, const GhostArgs &g, const double *coeffD, const double *bi,

@@ -171,6 +171,33 @@ class PoissonSolver:
         f.nlu, f.nlv, f.nlw = nl
         _check(self.lib.fsi_mg_rhs_advec_diff(self.h, advec_scheme, frac_step_type, float(dt), ctypes.byref(f)))
 
+    @staticmethod
+    def _ad_fields(faces, visc, nl, bc=(None,) * 9, bcvisc=(None,) * 3):
+        f = RhsAdFields()
+        f.face_u, f.face_v, f.face_w = faces
+        for q in range(9):
+            f.bc[q] = bc[q]
+        f.viscTot = visc
+        for q in range(3):
+            f.bcvisc[q] = bcvisc[q]
+        f.nlu, f.nlv, f.nlw = nl
+        return f
+
+    def rhs_adjust_bc(self, dt: float, faces, visc, nl, bc=(None,) * 9, bcvisc=(None,) * 3, advec_scheme: int = 2):
+        """rhs_adjust_bc (IBM/CORE_RHS_AD.F90:588-780) on device pointers; nl INOUT."""
+        f = self._ad_fields(faces, visc, nl, bc, bcvisc)
+        _check(self.lib.fsi_mg_rhs_adjust_bc(self.h, advec_scheme, float(dt), ctypes.byref(f)))
+
+    def solve_ad(self, dt: float, faces, visc, vel, nl, bcvisc=(None,) * 3, advec_scheme: int = 2):
+        """solve_ad (IBM/CORE_SOLVE_AD.F90:12-267) on device pointers: vel =
+        (u, v, w) INOUT, nl the right-hand sides.  Returns (status, iterations, maxres)."""
+        f = self._ad_fields(faces, visc, nl, bcvisc=bcvisc)
+        it, mr = ctypes.c_int(), ctypes.c_double()
+        st = _check(self.lib.fsi_mg_solve_ad(self.h, advec_scheme, float(dt), ctypes.byref(f),
+                                             *(ctypes.c_void_p(a) if a else None for a in vel), ctypes.byref(it),
+                                             ctypes.byref(mr)))
+        return st, it.value, mr.value
+
     def set_velocity_ghosts(self, coeffGCMD, bi=None, probe_length_normalized: float = 2.0):
         """Ghost-cell velocities for correct_vel (GCM_vel_set_bc_internal):
         coeffGCMD (8, nGhost) Fortran order, bi = (uBI, vBI, wBI) or None (body

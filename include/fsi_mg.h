@@ -191,6 +191,29 @@ typedef struct {
 int fsi_mg_rhs_advec_diff(void *handle, int advec_scheme, int frac_step_type, double dt,
                           const fsi_mg_rhs_ad_fields *fields);
 
+/* rhs_adjust_bc (IBM/CORE_RHS_AD.F90:588-780, stationary boundary, no FSI):
+ * the boundary values bc of flagged faces, times the implicit coefficients
+ * (diffusion with viscTot / bcvisc, Crank-Nicolson convection with the
+ * faces), move from the operator to nlu, nlv, nlw (INOUT).  Uses face_*,
+ * bc, viscTot, bcvisc and nl* of the fields; advec_scheme 1 (AB2) or 2
+ * (CRANK_NICOLSON1). */
+int fsi_mg_rhs_adjust_bc(void *handle, int advec_scheme, double dt, const fsi_mg_rhs_ad_fields *fields);
+
+/* solve_ad (IBM/CORE_SOLVE_AD.F90:12-267), line-SOR branch, stationary
+ * boundary: the implicit operator of set_solve_ad (IBM/CORE_SET_SOLVERS.F90:
+ * 20-95) plus the Crank-Nicolson convective terms, applied to u, v (, w)
+ * (device, INOUT) with right-hand sides nlu, nlv, nlw of the fields, line
+ * sweeps along x, y, z per component, red-black over the lines (the
+ * reference sweeps them lexicographically; both converge to the same
+ * solution), then under GCM the ghost-cell velocities of
+ * fsi_mg_set_velocity_ghosts, until max |calc_residual_ad| <= restol_ad or
+ * iterMax_ad iterations (status 1, the reference prints and continues).
+ * advec_scheme 1 (AB2) or 2 (CRANK_NICOLSON1); zero-gradient velocity faces
+ * (whose mass-flux correction runs inside GCM_GhostCell_Vel) are rejected.
+ * iters and maxres OUT (may be NULL). */
+int fsi_mg_solve_ad(void *handle, int advec_scheme, double dt, const fsi_mg_rhs_ad_fields *fields, double *d_u,
+                    double *d_v, double *d_w, int *iters, double *maxres);
+
 /* Ghost-cell velocities of the GCM body for fsi_mg_correct_vel
  * (GCM_vel_set_bc_internal, IBM/GCM_GHOSTCELL_VEL_UPDATE_UNSTRUC.F90:126-247):
  * coeffGCMD(8,nGhost), the Dirichlet image-point weights of the ghost list

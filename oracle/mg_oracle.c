@@ -1593,3 +1593,227 @@ void or_rhs_advec_diff(or_ctx *c, int advec_scheme, int frac_step_type, double d
                 }
     }
 }
+
+/* ------------------------------------------- implicit momentum solve ---- */
+/* set_solve_ad (IBM/CORE_SET_SOLVERS.F90:20-95, stationary boundary): the
+ * implicit diffusion coefficients amx_ad..apz_ad (0:nx+1)^3, kept in the
+ * context for or_rhs_adjust_bc / or_solve_ad. */
+static double *g_ad[6];   /* amx_ad, apx_ad, amy_ad, apy_ad, amz_ad, apz_ad */
+static size_t g_ad_n;
+
+void or_set_solve_ad(or_ctx *c, double dt, const double *visc, const double *const *bcvisc3)
+{
+    const size_t nf = (size_t)(c->nx + 2) * (size_t)(c->ny + 2) * (size_t)(c->nz + 2);
+    if (g_ad_n != nf) {
+        for (int q = 0; q < 6; ++q) { free(g_ad[q]); g_ad[q] = zalloc(sizeof(double) * nf); }
+        g_ad_n = nf;
+    }
+    for (int q = 0; q < 6; ++q) memset(g_ad[q], 0, sizeof(double) * nf);
+    const int8_t *ium = c->fl[0], *iup = c->fl[1], *jum = c->fl[2], *jup = c->fl[3], *kum = c->fl[4], *kup = c->fl[5];
+    const double rnDim = (double)(c->p.ndim - DIM_2D);
+    for (int k = 1; k <= c->nz - 1; ++k)
+        for (int j = 1; j <= c->ny - 1; ++j)
+            for (int i = 1; i <= c->nx - 1; ++i) {
+                const size_t f = FI(c, i, j, k);
+                const double nuE = (fxw(c, 0, i + 1) * visc[FI(c, i + 1, j, k)] + (1.0 - fxw(c, 0, i + 1)) * visc[f]) * (1 - iup[f]) + arr_at(bcvisc3[0], f) * iup[f];
+                const double nuW = (fxw(c, 0, i) * visc[f] + (1.0 - fxw(c, 0, i)) * visc[FI(c, i - 1, j, k)]) * (1 - ium[f]) + arr_at(bcvisc3[0], f) * ium[f];
+                const double nuN = (fxw(c, 1, j + 1) * visc[FI(c, i, j + 1, k)] + (1.0 - fxw(c, 1, j + 1)) * visc[f]) * (1 - jup[f]) + arr_at(bcvisc3[1], f) * jup[f];
+                const double nuS = (fxw(c, 1, j) * visc[f] + (1.0 - fxw(c, 1, j)) * visc[FI(c, i, j - 1, k)]) * (1 - jum[f]) + arr_at(bcvisc3[1], f) * jum[f];
+                const double nuF = (fxw(c, 2, k + 1) * visc[FI(c, i, j, k + 1)] + (1.0 - fxw(c, 2, k + 1)) * visc[f]) * (1 - kup[f]) + arr_at(bcvisc3[2], f) * kup[f];
+                const double nuB = (fxw(c, 2, k) * visc[f] + (1.0 - fxw(c, 2, k)) * visc[FI(c, i, j, k - 1)]) * (1 - kum[f]) + arr_at(bcvisc3[2], f) * kum[f];
+                double t;
+                t = (c->dxcinv[0][i] * (1 - ium[f]) + c->dxinv[0][i] * ium[f] * 2.0) * c->dxinv[0][i];
+                g_ad[0][f] = -(0.5 * dt * nuW) * t;
+                t = (c->dxcinv[0][i + 1] * (1 - iup[f]) + c->dxinv[0][i] * iup[f] * 2.0) * c->dxinv[0][i];
+                g_ad[1][f] = -(0.5 * dt * nuE) * t;
+                t = (c->dxcinv[1][j] * (1 - jum[f]) + c->dxinv[1][j] * jum[f] * 2.0) * c->dxinv[1][j];
+                g_ad[2][f] = -(0.5 * dt * nuS) * t;
+                t = (c->dxcinv[1][j + 1] * (1 - jup[f]) + c->dxinv[1][j] * jup[f] * 2.0) * c->dxinv[1][j];
+                g_ad[3][f] = -(0.5 * dt * nuN) * t;
+                t = (c->dxcinv[2][k] * (1 - kum[f]) + c->dxinv[2][k] * kum[f] * 2.0) * c->dxinv[2][k];
+                g_ad[4][f] = -(0.5 * dt * nuB) * t * rnDim;
+                t = (c->dxcinv[2][k + 1] * (1 - kup[f]) + c->dxinv[2][k] * kup[f] * 2.0) * c->dxinv[2][k];
+                g_ad[5][f] = -(0.5 * dt * nuF) * t * rnDim;
+            }
+}
+
+/* The row of cell (i,j,k) as itsolv_ad_x/y/z and calc_residual_ad form it
+ * (IBM/CORE_SOLVE_AD.F90:343-390): per axis the coefficients with the
+ * Crank-Nicolson convective terms (half_dt = 0 for ADAMS_BASHFORTH2). */
+static void ad_row(or_ctx *c, double half_dt, const double *const *faces, int i, int j, int k, double am[3],
+                   double ap[3], double ac[3])
+{
+    const size_t f = FI(c, i, j, k);
+    const int idx[3] = {i, j, k};
+    for (int a = 0; a < 3; ++a) {
+        const int t = idx[a];
+        const int8_t mm = c->fl[2 * a][f], pp = c->fl[2 * a + 1][f];
+        const size_t fp = (a == 0) ? FI(c, i + 1, j, k) : (a == 1) ? FI(c, i, j + 1, k) : FI(c, i, j, k + 1);
+        am[a] = g_ad[2 * a][f];
+        ap[a] = g_ad[2 * a + 1][f];
+        ac[a] = -(am[a] + ap[a]);
+        double tmp1 = 1.0 - fxw(c, a, t), tmp2 = fxw(c, a, t + 1);
+        am[a] = am[a] - half_dt * faces[a][f] * tmp1 * c->dxinv[a][t];
+        ap[a] = ap[a] + half_dt * faces[a][fp] * tmp2 * c->dxinv[a][t];
+        tmp1 = fxw(c, a, t) * (1 - mm);
+        tmp2 = (1.0 - fxw(c, a, t + 1)) * (1 - pp);
+        ac[a] = ac[a] + half_dt * (faces[a][fp] * tmp2 - faces[a][f] * tmp1) * c->dxinv[a][t];
+    }
+}
+
+/* rhs_adjust_bc (IBM/CORE_RHS_AD.F90:588-780, stationary boundary, no FSI):
+ * the boundary values of flagged faces move to the right-hand side. */
+void or_rhs_adjust_bc(or_ctx *c, int advec_scheme, double dt, const double *const *faces, const double *const *bc9,
+                      double *nlu, double *nlv, double *nlw)
+{
+    const double half_dt = (advec_scheme == 1) ? 0.0 : 0.5 * dt;
+    for (int k = 1; k <= c->nzc; ++k)
+        for (int j = 1; j <= c->nyc; ++j)
+            for (int i = 1; i <= c->nxc; ++i) {
+                const size_t f = FI(c, i, j, k);
+                const int idx[3] = {i, j, k};
+                double md[3], pd[3];
+                for (int a = 0; a < 3; ++a) {
+                    const int t = idx[a];
+                    const int8_t mm = c->fl[2 * a][f], pp = c->fl[2 * a + 1][f];
+                    const size_t fp = (a == 0) ? FI(c, i + 1, j, k) : (a == 1) ? FI(c, i, j + 1, k) : FI(c, i, j, k + 1);
+                    md[a] = g_ad[2 * a][f];
+                    pd[a] = g_ad[2 * a + 1][f];
+                    const double tmp1 = (1.0 - fxw(c, a, t)) * (1 - mm) + mm;
+                    const double tmp2 = fxw(c, a, t + 1) * (1 - pp) + pp;
+                    md[a] = md[a] - half_dt * faces[a][f] * tmp1 * c->dxinv[a][t];
+                    pd[a] = pd[a] + half_dt * faces[a][fp] * tmp2 * c->dxinv[a][t];
+                }
+                double *nl[3] = {nlu, nlv, nlw};
+                for (int q = 0; q < 3; ++q) {
+                    const double *bx = bc9[3 * q], *by = bc9[3 * q + 1], *bz = bc9[3 * q + 2];
+                    nl[q][f] = nl[q][f] - md[0] * arr_at(bx, f) * c->fl[0][f] - pd[0] * arr_at(bx, f) * c->fl[1][f]
+                               - md[1] * arr_at(by, f) * c->fl[2][f] - pd[1] * arr_at(by, f) * c->fl[3][f]
+                               - md[2] * arr_at(bz, f) * c->fl[4][f] - pd[2] * arr_at(bz, f) * c->fl[5][f];
+                }
+            }
+}
+
+/* itsolv_ad_x / _y / _z (IBM/CORE_SOLVE_AD.F90:314-762 and the _AB variants):
+ * line Gauss-Seidel along axis d.  order 0: the reference's lexicographic
+ * line order; order 1: red-black over the two transverse indices (colour 0
+ * first), the order of the GPU sweep. */
+static void itsolv_ad_dir(or_ctx *c, int d, double half_dt, const double *const *faces, double *var, const double *r,
+                          int order)
+{
+    const int nc[3] = {c->nxc, c->nyc, c->nzc};
+    const int n = nc[d];
+    double *A = zalloc(sizeof(double) * (size_t)(n + 2)), *B = zalloc(sizeof(double) * (size_t)(n + 2));
+    double *C = zalloc(sizeof(double) * (size_t)(n + 2)), *R = zalloc(sizeof(double) * (size_t)(n + 2));
+    double *U = zalloc(sizeof(double) * (size_t)(n + 2)), *G = zalloc(sizeof(double) * (size_t)(n + 2));
+    /* outer loops: x (k, j), y (k, i), z (i, j) */
+    const int o1 = (d == 2) ? c->nxc : c->nzc;
+    const int o2 = (d == 0) ? c->nyc : (d == 1 ? c->nxc : c->nyc);
+    for (int pass = 0; pass < (order ? 2 : 1); ++pass)
+        for (int q1 = 1; q1 <= o1; ++q1)
+            for (int q2 = 1; q2 <= o2; ++q2) {
+                if (order && ((q1 + q2) & 1) != pass) continue;
+                for (int t = 1; t <= n; ++t) {
+                    const int i = (d == 0) ? t : (d == 1 ? q2 : q1);
+                    const int j = (d == 0) ? q2 : (d == 1 ? t : q2);
+                    const int k = (d == 0) ? q1 : (d == 1 ? q1 : t);
+                    const size_t f = FI(c, i, j, k);
+                    double am[3], ap[3], ac[3];
+                    ad_row(c, half_dt, faces, i, j, k, am, ap, ac);
+                    const double rib = 1.0 - (double)c->iblank[f];
+                    const size_t nb[3][2] = {{FI(c, i - 1, j, k), FI(c, i + 1, j, k)},
+                                             {FI(c, i, j - 1, k), FI(c, i, j + 1, k)},
+                                             {FI(c, i, j, k - 1), FI(c, i, j, k + 1)}};
+                    double rhs;
+                    if (d == 2) {   /* z-lines subtract term by term, y before x (:678-681) */
+                        rhs = r[f] - var[nb[1][0]] * am[1] * (1 - c->fl[2][f]) - var[nb[1][1]] * ap[1] * (1 - c->fl[3][f])
+                              - var[nb[0][0]] * am[0] * (1 - c->fl[0][f]) - var[nb[0][1]] * ap[0] * (1 - c->fl[1][f]);
+                    } else {        /* x- and y-lines subtract one parenthesised sum */
+                        const int a1 = (d == 0) ? 1 : 0;
+                        const double s = var[nb[a1][0]] * am[a1] * (1 - c->fl[2 * a1][f])
+                                       + var[nb[a1][1]] * ap[a1] * (1 - c->fl[2 * a1 + 1][f])
+                                       + var[nb[2][0]] * am[2] * (1 - c->fl[4][f])
+                                       + var[nb[2][1]] * ap[2] * (1 - c->fl[5][f]);
+                        rhs = r[f] - s;
+                    }
+                    A[t] = am[d] * rib * (1 - c->fl[2 * d][f]);
+                    C[t] = ap[d] * rib * (1 - c->fl[2 * d + 1][f]);
+                    B[t] = 1.0 + (ac[0] + ac[1] + ac[2]) * rib;
+                    R[t] = rhs * rib + var[f] * (double)c->ghost[f];
+                }
+                tdma_w(A, B, C, R, U, G, 1, n);
+                for (int t = 1; t <= n; ++t) {
+                    const int i = (d == 0) ? t : (d == 1 ? q2 : q1);
+                    const int j = (d == 0) ? q2 : (d == 1 ? t : q2);
+                    const int k = (d == 0) ? q1 : (d == 1 ? q1 : t);
+                    var[FI(c, i, j, k)] = U[t];
+                }
+            }
+    free(A); free(B); free(C); free(R); free(U); free(G);
+}
+
+/* calc_residual_ad (IBM/CORE_SOLVE_AD.F90:766-907, no fresh cells): max |res|
+ * over the interior, res masked by (1 - iblank). */
+static double calc_residual_ad(or_ctx *c, double half_dt, const double *const *faces, const double *var,
+                               const double *r)
+{
+    double resm = 0.0;
+    for (int k = 1; k <= c->nzc; ++k)
+        for (int j = 1; j <= c->nyc; ++j)
+            for (int i = 1; i <= c->nxc; ++i) {
+                const size_t f = FI(c, i, j, k);
+                double am[3], ap[3], ac[3];
+                ad_row(c, half_dt, faces, i, j, k, am, ap, ac);
+                double res = r[f] - var[f] * (1.0 + (ac[0] + ac[1] + ac[2]))
+                             - var[FI(c, i - 1, j, k)] * am[0] * (1 - c->fl[0][f])
+                             - var[FI(c, i + 1, j, k)] * ap[0] * (1 - c->fl[1][f])
+                             - var[FI(c, i, j - 1, k)] * am[1] * (1 - c->fl[2][f])
+                             - var[FI(c, i, j + 1, k)] * ap[1] * (1 - c->fl[3][f])
+                             - var[FI(c, i, j, k - 1)] * am[2] * (1 - c->fl[4][f])
+                             - var[FI(c, i, j, k + 1)] * ap[2] * (1 - c->fl[5][f]);
+                res = res * (double)(1 - c->iblank[f]);
+                if (fabs(res) > resm) resm = fabs(res);
+            }
+    return resm;
+}
+
+/* solve_ad (IBM/CORE_SOLVE_AD.F90:12-267), LSOR branch, stationary boundary:
+ * itsolv_ad on u, v (, w), then with GCM the ghost-cell velocities
+ * (GCM_GhostCell_Vel, IBM/GCM_GHOSTCELL_VEL_UPDATE_UNSTRUC.F90:20-122, whose
+ * mass-flux correction is inactive without zero-gradient faces), until the
+ * largest residual is <= restol_ad or iterMax_ad iterations.  order: 0 the
+ * reference's lexicographic line order, 1 red-black.  Returns the iteration
+ * count; *maxres receives the final residual. */
+int or_solve_ad(or_ctx *c, int advec_scheme, double dt, const double *const *faces, double *u, double *v, double *w,
+                const double *nlu, const double *nlv, const double *nlw, int order, double *maxres)
+{
+    const double half_dt = (advec_scheme == 1) ? 0.0 : 0.5 * dt;
+    const int three_d = (c->p.ndim == DIM_3D);
+    const int gcm = (c->p.boundary_formulation == GCM_METHOD);
+    double *vel[3] = {u, v, w};
+    const double *rr[3] = {nlu, nlv, nlw};
+    const int ncomp = three_d ? 3 : 2;
+    double mr = 0.0;
+    for (int q = 0; q < ncomp; ++q) {
+        const double rq = calc_residual_ad(c, half_dt, faces, vel[q], rr[q]);
+        if (rq > mr) mr = rq;
+    }
+    int iter = 0;
+    if (gcm) mr = 1.0e10;   /* the GCM branch starts its loop unconditionally */
+    while (iter < c->p.iterMax_ad && mr > c->p.restol_ad) {
+        for (int q = 0; q < ncomp; ++q) {
+            itsolv_ad_dir(c, 0, half_dt, faces, vel[q], rr[q], order);
+            itsolv_ad_dir(c, 1, half_dt, faces, vel[q], rr[q], order);
+            if (three_d) itsolv_ad_dir(c, 2, half_dt, faces, vel[q], rr[q], order);
+        }
+        if (gcm && c->vg_on) gcm_vel_set_bc_internal(c, u, v, w);
+        mr = 0.0;
+        for (int q = 0; q < ncomp; ++q) {
+            const double rq = calc_residual_ad(c, half_dt, faces, vel[q], rr[q]);
+            if (rq > mr) mr = rq;
+        }
+        ++iter;
+    }
+    if (maxres) *maxres = mr;
+    return iter;
+}

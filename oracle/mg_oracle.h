@@ -102,4 +102,11 @@ void    or_rhs_advec_diff(or_ctx *c, int advec_scheme, int frac_step_type, doubl
                           const double *face_w, const double *const *bc9, const double *visc,
                           const double *const *bcvisc3, const double *exp_weight, double *nluOld, double *nlvOld,
                           double *nlwOld, const double *p, double *nlu, double *nlv, double *nlw);
+/* implicit momentum solve: set_solve_ad, rhs_adjust_bc, solve_ad (order 0 reference, 1 red-black) */
+void    or_set_solve_ad(or_ctx *c, double dt, const double *visc, const double *const *bcvisc3);
+void    or_rhs_adjust_bc(or_ctx *c, int advec_scheme, double dt, const double *const *faces,
+                         const double *const *bc9, double *nlu, double *nlv, double *nlw);
+int     or_solve_ad(or_ctx *c, int advec_scheme, double dt, const double *const *faces, double *u, double *v,
+                    double *w, const double *nlu, const double *nlv, const double *nlw, int order,
+                    double *maxres);
 #endif

@@ -93,6 +93,14 @@ def lib():
         L.or_rhs_advec_diff.argtypes = ([ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_double] + [_dp] * 6
                                         + [ctypes.POINTER(_dp), _dp, ctypes.POINTER(_dp)] + [_dp] * 8)
         L.or_rhs_advec_diff.restype = None
+        L.or_set_solve_ad.argtypes = [ctypes.c_void_p, ctypes.c_double, _dp, ctypes.POINTER(_dp)]
+        L.or_set_solve_ad.restype = None
+        L.or_rhs_adjust_bc.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_double, ctypes.POINTER(_dp),
+                                       ctypes.POINTER(_dp), _dp, _dp, _dp]
+        L.or_rhs_adjust_bc.restype = None
+        L.or_solve_ad.argtypes = ([ctypes.c_void_p, ctypes.c_int, ctypes.c_double, ctypes.POINTER(_dp)] + [_dp] * 6
+                                  + [ctypes.c_int, _dp])
+        L.or_solve_ad.restype = ctypes.c_int
         _lib = L
     return _lib
 
@@ -226,6 +234,22 @@ class Oracle:
                                 b9, _p(visc), b3, _p(exp_weight), *(_p(a) for a in nl_old), _p(p),
                                 *(_p(a) for a in nl))
         return nl
+
+    # ----- implicit momentum solve -----
+    def set_solve_ad(self, dt, visc, bcvisc=(None,) * 3):
+        lib().or_set_solve_ad(self.h, dt, _p(visc), (_dp * 3)(*[_p(a) for a in bcvisc]))
+
+    def rhs_adjust_bc(self, dt, faces, nl, bc9=(None,) * 9, advec_scheme=2):
+        lib().or_rhs_adjust_bc(self.h, advec_scheme, dt, (_dp * 3)(*[_p(a) for a in faces]),
+                               (_dp * 9)(*[_p(a) for a in bc9]), *(_p(a) for a in nl))
+        return nl
+
+    def solve_ad(self, dt, faces, vel, nl, advec_scheme=2, order=0):
+        """solve_ad on vel = (u, v, w) in place; returns (iterations, maxres)."""
+        mr = ctypes.c_double()
+        it = lib().or_solve_ad(self.h, advec_scheme, dt, (_dp * 3)(*[_p(a) for a in faces]), *(_p(a) for a in vel),
+                               *(_p(a) for a in nl), order, ctypes.byref(mr))
+        return it, mr.value
 
     def update_pressure(self, pPrime, p, frac_step_type=0):
         lib().or_update_pressure(self.h, frac_step_type, _p(pPrime), _p(p))
