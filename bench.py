@@ -369,56 +369,77 @@ def projection_steps(solver, pr, peak, reps=20):
     return out
 
 
-def device_projection_step(n, seed, tol, krylov, steps=3):
-    """One fractional projection step kept in HBM through the C ABI, on the n^3
-    stretched box without a body (its face_vel right-hand side is compatible):
-    fsi_mg_face_vel_rhs -> fsi_mg_solve_device (mixed, FGMRES) ->
-    fsi_mg_correct_vel -> fsi_mg_update_pressure, no host copy of pPrime or
-    nlu0.  Wall time per routine (each call waits for its work), and the
-    size-independent check of the step: the corrected face velocities are
-    divergence-free to the solver's residual, max |div(face)/dt| over the
-    interior <= restol (the face gradient of correct_vel and the Poisson
-    operator are the same stencil)."""
+def device_time_step(n, seed, tol, krylov, steps=3, reinv=1e-3, dt=1e-3):
+    """One fractional time step kept in HBM through the C ABI, on the n^3
+    stretched box without a body (its face_vel right-hand side is compatible),
+    in the reference's order (IBM/CORE_TIME_STEP.F90:201-267):
+    fsi_mg_rhs_advec_diff (Crank-Nicolson) -> fsi_mg_rhs_adjust_bc ->
+    fsi_mg_solve_ad -> fsi_mg_face_vel_rhs -> fsi_mg_solve_device (mixed,
+    FGMRES) -> fsi_mg_correct_vel -> fsi_mg_update_pressure, no host copy of a
+    field.  Every timed step starts from the same state.  Wall time per routine
+    (each call waits for its work), and the size-independent check of the
+    step: the corrected face velocities are divergence-free to the solver's
+    residual, max |div(face)/dt| over the interior <= restol (the face
+    gradient of correct_vel and the Poisson operator are the same stencil)."""
     import torch
     from flow_structure_interaction_fem_ibm_gb300 import problem as P
     from flow_structure_interaction_fem_ibm_gb300.grid import Metrics
     from flow_structure_interaction_fem_ibm_gb300.poisson import PoissonSolver
     pr = P.box3d(n, seed=seed, stretch=1.5)
     q = copy.deepcopy(pr.params)
-    dt = 1e-3
     q.restol_Poisson = tol * float(np.abs(pr.nlu0).max()) / dt
     q.iterMax_Poisson, q.precision_mode, q.outer_krylov = 400, 1, krylov
+    q.restol_ad, q.iterMax_ad = 1e-10, 200
     s = PoissonSolver(q, pr.x, pr.y, pr.z).set_boundary(pr.geom)
     sh = pr.shape[::-1]
     g = torch.Generator(device="cuda").manual_seed(seed)
-    u, v, w = (torch.randn(sh, dtype=torch.float64, device="cuda", generator=g) for _ in range(3))
-    faces = [torch.zeros(sh, dtype=torch.float64, device="cuda") for _ in range(3)]
-    nlu0, pp, p = (torch.zeros(sh, dtype=torch.float64, device="cuda") for _ in range(3))
+    z = lambda: torch.zeros(sh, dtype=torch.float64, device="cuda")
+    u0, v0, w0 = (torch.randn(sh, dtype=torch.float64, device="cuda", generator=g) for _ in range(3))
+    u, v, w = z(), z(), z()
+    faces, faces0 = [z() for _ in range(3)], [z() for _ in range(3)]
+    nl = [z() for _ in range(3)]
+    nlu0, pp, p = z(), z(), z()
+    visc = torch.full(sh, reinv, dtype=torch.float64, device="cuda")
     fp = [t.data_ptr() for t in faces]
+    vp = [u.data_ptr(), v.data_ptr(), w.data_ptr()]
+    nlp = [t.data_ptr() for t in nl]
+    vis = [visc.data_ptr()] * 3
+    # the previous step's face velocities
+    s.face_vel_rhs(dt, u0.data_ptr(), v0.data_ptr(), w0.data_ptr(), *[t.data_ptr() for t in faces0], nlu0.data_ptr())
     dinv = [torch.from_numpy(Metrics(c).dxinv).cuda() for c in (pr.x, pr.y, pr.z)]
-    times = {"face_vel_rhs": [], "solve": [], "correct_vel": [], "update_pressure": []}
-    iters, worst = [], 0.0
-    u0, v0, w0 = u.clone(), v.clone(), w.clone()
+    names = ["rhs_advec_diff", "rhs_adjust_bc", "solve_ad", "face_vel_rhs", "solve", "correct_vel",
+             "update_pressure"]
+    times = {k: [] for k in names}
+    iters, ad_iters, worst = [], [], 0.0
     for it in range(steps + 1):
         u.copy_(u0); v.copy_(v0); w.copy_(w0); pp.zero_()
+        for a, b in zip(faces, faces0):
+            a.copy_(b)
         torch.cuda.synchronize()
-        t0 = time.perf_counter()
-        s.face_vel_rhs(dt, u.data_ptr(), v.data_ptr(), w.data_ptr(), *fp, nlu0.data_ptr())
-        t1 = time.perf_counter()
+        t = [time.perf_counter()]
+        s.rhs_advec_diff(dt, vp, fp, visc.data_ptr(), nlp, bcvisc=vis, advec_scheme=2)
+        t.append(time.perf_counter())
+        s.rhs_adjust_bc(dt, fp, visc.data_ptr(), nlp, bcvisc=vis, advec_scheme=2)
+        t.append(time.perf_counter())
+        st_ad, nad, mr_ad = s.solve_ad(dt, fp, visc.data_ptr(), vp, nlp, bcvisc=vis, advec_scheme=2)
+        t.append(time.perf_counter())
+        s.face_vel_rhs(dt, *vp, *fp, nlu0.data_ptr())
+        t.append(time.perf_counter())
         st, nit, mr, _, _ = s.solve_poisson_device(pp.data_ptr(), nlu0.data_ptr())
-        t2 = time.perf_counter()
-        s.correct_vel(dt, pp.data_ptr(), u.data_ptr(), v.data_ptr(), w.data_ptr(), *fp)
-        t3 = time.perf_counter()
+        t.append(time.perf_counter())
+        s.correct_vel(dt, pp.data_ptr(), *vp, *fp)
+        t.append(time.perf_counter())
         s.update_pressure(pp.data_ptr(), p.data_ptr(), 0)
-        t4 = time.perf_counter()
-        if st != 0:
-            raise RuntimeError(f"device projection step: solve status {st}, {nit} iterations, maxres {mr}")
+        t.append(time.perf_counter())
+        if st != 0 or st_ad != 0:
+            raise RuntimeError(f"device time step: solve status {st} ({nit} iterations, maxres {mr}), "
+                               f"solve_ad status {st_ad} ({nad} iterations, maxres {mr_ad})")
         if it == 0:
             continue   # warm-up (graph capture)
-        for k, a, b in (("face_vel_rhs", t0, t1), ("solve", t1, t2), ("correct_vel", t2, t3),
-                        ("update_pressure", t3, t4)):
-            times[k].append(1e3 * (b - a))
+        for k, a_, b_ in zip(names, t[:-1], t[1:]):
+            times[k].append(1e3 * (b_ - a_))
         iters.append(nit)
+        ad_iters.append(nad)
         # (z, y, x) tensors: divergence of the corrected faces over the interior
         fu, fv, fw = faces
         I = slice(1, n + 1)
@@ -427,9 +448,10 @@ def device_projection_step(n, seed, tol, krylov, steps=3):
                + (fw[2:n + 2, I, I] - fw[I, I, I]) * dinv[2][I].view(-1, 1, 1)) / dt
         worst = max(worst, float(div.abs().max()))
     s.close()
-    ms = {k: float(np.median(v)) for k, v in times.items()}
-    return {"workload": f"box3d_{n}^3_tanh1.5_no_body_mixed_fgmres{krylov}", "steps": steps,
-            "ms": ms, "step_ms": sum(ms.values()), "iters": iters, "restol": q.restol_Poisson,
+    ms = {k: float(np.median(v_)) for k, v_ in times.items()}
+    return {"workload": f"box3d_{n}^3_tanh1.5_no_body_Re{1 / reinv:g}_dt{dt:g}_CN_mixed_fgmres{krylov}",
+            "steps": steps, "ms": ms, "step_ms": sum(ms.values()), "poisson_iters": iters,
+            "solve_ad_iters": ad_iters, "restol": q.restol_Poisson, "restol_ad": q.restol_ad,
             "max_div_after_correction": worst, "divergence_free": worst <= q.restol_Poisson,
             "host_copies_per_step": 0}
 
@@ -473,9 +495,10 @@ def main():
         pr = P.sphere(args.n, seed=args.seed, stretch=1.5)
         s = PoissonSolver(pr.params, pr.x, pr.y, pr.z).set_boundary(pr.geom)
         peaks = json.loads(PEAKS.read_text()) if PEAKS.exists() else {}
-        print(json.dumps({"profile": "projection_steps", "grid": args.n,
-                          "projection_steps": projection_steps(s, pr, peaks.get("hbm_gbs", 6800.0))}))
+        out = projection_steps(s, pr, peaks.get("hbm_gbs", 6800.0))
         s.close()
+        out["device_step"] = device_time_step(args.n, args.seed, args.tol, args.krylov)
+        print(json.dumps({"profile": "projection_steps", "grid": args.n, "projection_steps": out}))
         return
 
     if args.profile:
@@ -621,7 +644,7 @@ def main():
     steps_ops = None
     if not args.no_steps:
         steps_ops = projection_steps(s_mixed, pr, peak)
-        steps_ops["device_step"] = device_projection_step(args.n, args.seed, args.tol, args.krylov)
+        steps_ops["device_step"] = device_time_step(args.n, args.seed, args.tol, args.krylov)
 
     adjoint = None
     if rank == 0 and not args.no_adjoint:
