@@ -30,6 +30,14 @@ MODULE fsi_mg_gpu
     REAL(C_DOUBLE) :: omega, restol_Poisson, restol_ad, ppp(6), outflow_area
   END TYPE fsi_mg_params
 
+  ! device pointers of the momentum right-hand side (fsi_mg_rhs_ad_fields)
+  TYPE, BIND(C) :: fsi_mg_rhs_ad_fields
+    TYPE(C_PTR) :: u, v, w, face_u, face_v, face_w
+    TYPE(C_PTR) :: bc(9)                 ! bcxu, bcyu, bczu, bcxv, bcyv, bczv, bcxw, bcyw, bczw
+    TYPE(C_PTR) :: viscTot, bcvisc(3), exp_weight
+    TYPE(C_PTR) :: nluOld, nlvOld, nlwOld, p, nlu, nlv, nlw
+  END TYPE fsi_mg_rhs_ad_fields
+
   TYPE(C_PTR), SAVE :: fsi_mg_handle = C_NULL_PTR
   INTEGER, SAVE :: fsi_mg_precision = 0      ! 0 FP64, 1 mixed (set before MG_initial)
 
@@ -89,6 +97,33 @@ MODULE fsi_mg_gpu
       IMPORT :: C_INT, C_DOUBLE, C_PTR
       TYPE(C_PTR), VALUE :: h, pPrime, u, v, w, bcxu, bcyv, bczw, face_u, face_v, face_w
       REAL(C_DOUBLE), VALUE :: dt
+    END FUNCTION
+    ! momentum predictor on device arrays: rhs_advec_diff (IBM/CORE_RHS_AD.F90:13),
+    ! rhs_adjust_bc (:588), solve_ad (IBM/CORE_SOLVE_AD.F90:12)
+    INTEGER(C_INT) FUNCTION fsi_mg_rhs_advec_diff(h, advec_scheme, frac_step_type, dt, fields) &
+        BIND(C, NAME='fsi_mg_rhs_advec_diff')
+      IMPORT :: C_INT, C_DOUBLE, C_PTR, fsi_mg_rhs_ad_fields
+      TYPE(C_PTR), VALUE :: h
+      INTEGER(C_INT), VALUE :: advec_scheme, frac_step_type
+      REAL(C_DOUBLE), VALUE :: dt
+      TYPE(fsi_mg_rhs_ad_fields), INTENT(IN) :: fields
+    END FUNCTION
+    INTEGER(C_INT) FUNCTION fsi_mg_rhs_adjust_bc(h, advec_scheme, dt, fields) BIND(C, NAME='fsi_mg_rhs_adjust_bc')
+      IMPORT :: C_INT, C_DOUBLE, C_PTR, fsi_mg_rhs_ad_fields
+      TYPE(C_PTR), VALUE :: h
+      INTEGER(C_INT), VALUE :: advec_scheme
+      REAL(C_DOUBLE), VALUE :: dt
+      TYPE(fsi_mg_rhs_ad_fields), INTENT(IN) :: fields
+    END FUNCTION
+    INTEGER(C_INT) FUNCTION fsi_mg_solve_ad(h, advec_scheme, dt, fields, u, v, w, iters, maxres) &
+        BIND(C, NAME='fsi_mg_solve_ad')
+      IMPORT :: C_INT, C_DOUBLE, C_PTR, fsi_mg_rhs_ad_fields
+      TYPE(C_PTR), VALUE :: h, u, v, w
+      INTEGER(C_INT), VALUE :: advec_scheme
+      REAL(C_DOUBLE), VALUE :: dt
+      TYPE(fsi_mg_rhs_ad_fields), INTENT(IN) :: fields
+      INTEGER(C_INT), INTENT(OUT) :: iters
+      REAL(C_DOUBLE), INTENT(OUT) :: maxres
     END FUNCTION
     ! coeffGCMD(8,nGhost), u/v/wBodyIntercept(nGhost) (host; C_NULL_PTR for a body at rest)
     INTEGER(C_INT) FUNCTION fsi_mg_set_velocity_ghosts(h, coeffGCMD, uBI, vBI, wBI, bodyInterceptWeight, &
