@@ -100,6 +100,10 @@ struct Ctx {
     int nGhost = 0, ghost_cap = 0;
     long long *gidx = nullptr, *sidx = nullptr;
     int *gsg = nullptr;   // stencil in the ghost-buffer encoding (GhostArgs::sg)
+    int *gg_ptr = nullptr, *gg_idx = nullptr;   // ghost-ghost couplings (CSR)
+    int gg_cap = 0;
+    double *ggc64 = nullptr;
+    float *ggc32 = nullptr;
     double *gco64 = nullptr, *gscr64 = nullptr;
     float *gco32 = nullptr, *gscr32 = nullptr;
     int *d_iters = nullptr;
@@ -491,8 +495,8 @@ void gcm_pressure<double>(Ctx &c, double *v)
     launch_outer_ghost<double>(v, c.L1.d, c.sign, c.s);
     c.launches++;
     if (c.nGhost > 0) {
-        GhostArgs g{c.nGhost, c.gidx, c.sidx, c.gsg};
-        launch_ghost_rows<double>(v, g, c.gco64, c.gscr64, c.p.iterMax_ad, c.p.restol_ad, 0.0, c.d_iters, c.d_maxd,
+        GhostArgs g{c.nGhost, c.gidx, c.sidx, c.gsg, c.gg_ptr, c.gg_idx};
+        launch_ghost_rows<double>(v, g, c.gco64, c.ggc64, c.gscr64, c.p.iterMax_ad, c.p.restol_ad, 0.0, c.d_iters, c.d_maxd,
                                   c.s);
         c.launches++;
     }
@@ -503,8 +507,8 @@ void gcm_pressure<float>(Ctx &c, float *v)
     launch_outer_ghost<float>(v, c.L1.d, c.sign, c.s);
     c.launches++;
     if (c.nGhost > 0) {
-        GhostArgs g{c.nGhost, c.gidx, c.sidx, c.gsg};
-        launch_ghost_rows<float>(v, g, c.gco32, c.gscr32, c.p.iterMax_ad, c.p.restol_ad, 1.0e-6, c.d_iters, c.d_maxd,
+        GhostArgs g{c.nGhost, c.gidx, c.sidx, c.gsg, c.gg_ptr, c.gg_idx};
+        launch_ghost_rows<float>(v, g, c.gco32, c.ggc32, c.gscr32, c.p.iterMax_ad, c.p.restol_ad, 1.0e-6, c.d_iters, c.d_maxd,
                                  c.s);
         c.launches++;
     }
@@ -616,8 +620,8 @@ void correct_pressure(Ctx &c, double *p, double *nlw0)
     launch_outer_ghost<double>(p, c.L1.d, c.sign, c.s);
     c.launches++;
     if (c.nGhost > 0) {
-        GhostArgs g{c.nGhost, c.gidx, c.sidx, c.gsg};
-        launch_ghost_rows<double>(p, g, c.gco64, c.gscr64, c.p.iterMax_ad, c.p.restol_ad, 0.0, c.d_iters, c.d_maxd,
+        GhostArgs g{c.nGhost, c.gidx, c.sidx, c.gsg, c.gg_ptr, c.gg_idx};
+        launch_ghost_rows<double>(p, g, c.gco64, c.ggc64, c.gscr64, c.p.iterMax_ad, c.p.restol_ad, 0.0, c.d_iters, c.d_maxd,
                                   c.s);
         c.launches++;
     }
@@ -836,8 +840,9 @@ int solve_krylov_t(Ctx &c, double *p, const double *b, int *iters, double *maxre
             if (gcm) {   // ghost values of z from its fluid values (the map whose matrix A acts on)
                 launch_outer_ghost<T>(KZ[j], c.L1.d, c.sign, c.s);
                 if (c.nGhost > 0) {
-                    GhostArgs ga{c.nGhost, c.gidx, c.sidx, c.gsg};
-                    launch_ghost_rows<T>(KZ[j], ga, gco, gscr, c.p.iterMax_ad, c.p.restol_ad, f32 ? 1.0e-6 : 0.0,
+                    GhostArgs ga{c.nGhost, c.gidx, c.sidx, c.gsg, c.gg_ptr, c.gg_idx};
+                    launch_ghost_rows<T>(KZ[j], ga, gco, f32 ? (const T *)c.ggc32 : (const T *)c.ggc64, gscr,
+                                         c.p.iterMax_ad, c.p.restol_ad, f32 ? 1.0e-6 : 0.0,
                                          c.d_iters, c.d_maxd, c.s);
                 }
                 c.launches += 2;
@@ -1310,6 +1315,36 @@ int fsi_mg_set_geometry(void *handle, const int8_t *iblank, const int8_t *ghostC
                 sg[e] = (f != gnum.end()) ? -(f->second + 2) : (int)si[e];
             }
         }
+        // ghost-ghost couplings in CSR form (the sweeps of the cluster kernel read only these)
+        std::vector<int> ggp(nGhost + 1, 0), ggi;
+        std::vector<double> ggc;
+        for (int n = 0; n < nGhost; ++n) {
+            for (int r = 0; r < 8; ++r) {
+                const int e = sg[8 * (size_t)n + r];
+                if (e <= -2) { ggi.push_back(-e - 2); ggc.push_back(coeffGCMN[8 * (size_t)n + r]); }
+            }
+            ggp[n + 1] = (int)ggi.size();
+        }
+        std::vector<float> ggcf(ggc.begin(), ggc.end());
+        if (nGhost > c.ghost_cap || (int)ggi.size() > c.gg_cap) {
+            for (void *q : {(void *)c.gg_ptr, (void *)c.gg_idx, (void *)c.ggc64, (void *)c.ggc32}) {
+                auto it = std::find(c.allocs.begin(), c.allocs.end(), q);
+                if (q && it != c.allocs.end()) { cudaFree(q); c.allocs.erase(it); }
+            }
+            const int cap = nGhost + nGhost / 4 + 64, ecap = std::max(8 * cap, (int)ggi.size() + 64);
+            TRY(c.alloc(&c.gg_ptr, (size_t)cap + 1));
+            TRY(c.alloc(&c.gg_idx, (size_t)ecap));
+            TRY(c.alloc(&c.ggc64, (size_t)ecap));
+            TRY(c.alloc(&c.ggc32, (size_t)ecap));
+            c.gg_cap = ecap;
+        }
+        CK(cudaMemcpyAsync(c.gg_ptr, ggp.data(), ggp.size() * 4, cudaMemcpyHostToDevice, c.s));
+        if (!ggi.empty()) {
+            CK(cudaMemcpyAsync(c.gg_idx, ggi.data(), ggi.size() * 4, cudaMemcpyHostToDevice, c.s));
+            CK(cudaMemcpyAsync(c.ggc64, ggc.data(), ggc.size() * 8, cudaMemcpyHostToDevice, c.s));
+            CK(cudaMemcpyAsync(c.ggc32, ggcf.data(), ggcf.size() * 4, cudaMemcpyHostToDevice, c.s));
+        }
+        CK(cudaStreamSynchronize(c.s));
         if (nGhost > c.ghost_cap) {   // grow-only ghost buffers (body motion changes nGhost)
             for (void *q : {(void *)c.gidx, (void *)c.sidx, (void *)c.gco64, (void *)c.gco32, (void *)c.gscr64,
                             (void *)c.gscr32, (void *)c.gsg}) {
@@ -1322,8 +1357,8 @@ int fsi_mg_set_geometry(void *handle, const int8_t *iblank, const int8_t *ghostC
             TRY(c.alloc(&c.gco64, 8 * (size_t)cap));
             TRY(c.alloc(&c.gco32, 8 * (size_t)cap));
             TRY(c.alloc(&c.gsg, 8 * (size_t)cap));
-            TRY(c.alloc(&c.gscr64, 2 * (size_t)cap));   // two ping-pong buffers
-            TRY(c.alloc(&c.gscr32, 2 * (size_t)cap));
+            TRY(c.alloc(&c.gscr64, 3 * (size_t)cap));   // two ping-pong buffers and the rows' fixed parts
+            TRY(c.alloc(&c.gscr32, 3 * (size_t)cap));
             c.ghost_cap = cap;
         }
         CK(cudaMemcpyAsync(c.gidx, gi.data(), gi.size() * 8, cudaMemcpyHostToDevice, c.s));
@@ -1592,7 +1627,7 @@ int fsi_mg_correct_vel(void *handle, double dt, const double *d_pPrime, double *
     if (c.vg_on && c.nGhost > 0) {   // GCM_vel_set_bc_internal (IBM/CORE_FRAC_STEP_ROUTINES.F90:373)
         CK(cudaMemsetAsync(c.d_iters, 0, sizeof(int), c.s));
         CK(cudaMemsetAsync(c.d_maxd, 0, sizeof(unsigned long long), c.s));
-        GhostArgs g{c.nGhost, c.gidx, c.sidx, c.gsg};
+        GhostArgs g{c.nGhost, c.gidx, c.sidx, c.gsg, c.gg_ptr, c.gg_idx};
         launch_vel_ghosts(d_u, d_v, d_w, g, c.vg_coeff, c.vg_bi_set ? c.vg_bi : nullptr, c.vg_bw, c.vg_iw, c.vg_scr,
                           c.p.iterMax_ad, c.p.restol_ad, c.d_iters, c.d_maxd, c.s);
         c.launches++;
@@ -1743,7 +1778,7 @@ int fsi_mg_solve_ad(void *handle, int advec_scheme, double dt, const fsi_mg_rhs_
         if (gcm && c.vg_on && c.nGhost > 0) {   // GCM_GhostCell_Vel
             CK(cudaMemsetAsync(c.d_iters, 0, sizeof(int), c.s));
             CK(cudaMemsetAsync(c.d_maxd, 0, sizeof(unsigned long long), c.s));
-            GhostArgs g{c.nGhost, c.gidx, c.sidx, c.gsg};
+            GhostArgs g{c.nGhost, c.gidx, c.sidx, c.gsg, c.gg_ptr, c.gg_idx};
             launch_vel_ghosts(d_u, d_v, d_w, g, c.vg_coeff, c.vg_bi_set ? c.vg_bi : nullptr,
                               c.vg_bw, c.vg_iw, c.vg_scr, c.p.iterMax_ad, c.p.restol_ad, c.d_iters, c.d_maxd, c.s);
             c.launches++;
@@ -1803,8 +1838,8 @@ int fsi_mg_update_pressure(void *handle, int frac_step_type, const double *d_pPr
     c.last_up_p = d_p; c.last_up_pp = d_pPrime; c.last_up_vk = (frac_step_type == 1); c.have_up = true;
     c.launches++;
     if (c.p.boundary_formulation == GCM_METHOD && c.nGhost > 0) {
-        GhostArgs g{c.nGhost, c.gidx, c.sidx, c.gsg};
-        launch_ghost_rows<double>(d_p, g, c.gco64, c.gscr64, c.p.iterMax_ad, c.p.restol_ad, 0.0, c.d_iters, c.d_maxd,
+        GhostArgs g{c.nGhost, c.gidx, c.sidx, c.gsg, c.gg_ptr, c.gg_idx};
+        launch_ghost_rows<double>(d_p, g, c.gco64, c.ggc64, c.gscr64, c.p.iterMax_ad, c.p.restol_ad, 0.0, c.d_iters, c.d_maxd,
                                   c.s);
         c.launches++;
     }
@@ -1917,8 +1952,8 @@ int fsi_mg_debug_level_op(void *handle, int op, int d, int n, void *a, void *b, 
         TRY(copy_level(c, L, t0, a, true));
         CK(cudaMemsetAsync(c.d_iters, 0, sizeof(int), c.s));
         if (c.nGhost > 0) {
-            GhostArgs g{c.nGhost, c.gidx, c.sidx, c.gsg};
-            launch_ghost_rows<double>(t0, g, c.gco64, c.gscr64, c.p.iterMax_ad, c.p.restol_ad, 0.0, c.d_iters,
+            GhostArgs g{c.nGhost, c.gidx, c.sidx, c.gsg, c.gg_ptr, c.gg_idx};
+            launch_ghost_rows<double>(t0, g, c.gco64, c.ggc64, c.gscr64, c.p.iterMax_ad, c.p.restol_ad, 0.0, c.d_iters,
                                       c.d_maxd, c.s);
         }
         TRY(copy_level(c, L, t0, a, false));

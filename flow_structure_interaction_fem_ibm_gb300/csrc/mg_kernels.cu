@@ -1024,18 +1024,21 @@ __global__ void __launch_bounds__(1024) k_ghost_rows(T *v, GhostArgs g, const T 
 }
 
 // Same fixed-point iteration spread over a cluster of 8 CTAs (8192 threads).
-// The ghost values are iterated in two ping-pong buffers (scratch[0:n] and
-// scratch[n:2n]); stencil entries that are ghost cells read the buffer, all
-// others read v, so one cluster barrier per sweep orders everything: each CTA
-// also posts its sweep maxima into rank 0's shared slots, double-buffered by
-// sweep parity.  The converged values are written into v once at the end.
+// The stencil entries that are not ghost cells do not change during the
+// iteration, so each row's sum over them is formed once (scratch[2n:3n]);
+// a sweep then adds only the row's ghost-ghost couplings (a CSR list, under
+// one entry per ghost on average) read from the current buffer.  The ghost
+// values are iterated in two ping-pong buffers (scratch[0:n] and
+// scratch[n:2n]), so one cluster barrier per sweep orders everything: each
+// CTA also posts its sweep maxima into rank 0's shared slots, double-buffered
+// by sweep parity.  The converged values are written into v once at the end.
 // Loop bounds are uniform over the cluster and capped by iterMax.
 constexpr int GHOST_CLUSTER = 8;
 
 template <typename T>
 __global__ void __cluster_dims__(GHOST_CLUSTER, 1, 1) __launch_bounds__(1024)
-    k_ghost_rows_cluster(T *v, GhostArgs g, const T *coeff, T *scratch, int iterMax, double tol, double reltol,
-                         int *iters, unsigned long long *maxdelta)
+    k_ghost_rows_cluster(T *v, GhostArgs g, const T *coeff, const T *ggc, T *scratch, int iterMax, double tol,
+                         double reltol, int *iters, unsigned long long *maxdelta)
 {
     namespace cg = cooperative_groups;
     cg::cluster_group cluster = cg::this_cluster();
@@ -1046,8 +1049,17 @@ __global__ void __cluster_dims__(GHOST_CLUSTER, 1, 1) __launch_bounds__(1024)
     const int gtid = (int)rank * (int)blockDim.x + tid, gstride = GHOST_CLUSTER * (int)blockDim.x;
     double *rslot_d = cluster.map_shared_rank(&slot_d[0][0], 0);
     double *rslot_a = cluster.map_shared_rank(&slot_a[0][0], 0);
-    T *bufA = scratch, *bufB = scratch + g.n;
-    for (int n = gtid; n < g.n; n += gstride) bufA[n] = v[g.gidx[n]];
+    T *bufA = scratch, *bufB = scratch + g.n, *fixed = scratch + 2 * g.n;
+    for (int n = gtid; n < g.n; n += gstride) {
+        bufA[n] = v[g.gidx[n]];
+        T acc = T(0);
+#pragma unroll
+        for (int r = 0; r < 8; ++r) {
+            const int e = g.sg[8 * n + r];
+            if (e >= 0) acc = acc + coeff[8 * n + r] * v[e];
+        }
+        fixed[n] = acc;
+    }
     cluster.sync();
     int it = 0, par = 0;
     double maxd = 1.0e10, thr = tol;
@@ -1056,13 +1068,8 @@ __global__ void __cluster_dims__(GHOST_CLUSTER, 1, 1) __launch_bounds__(1024)
         T *dst = par ? bufA : bufB;
         double ld = 0.0, la = 0.0;
         for (int n = gtid; n < g.n; n += gstride) {
-            T acc = T(0);
-#pragma unroll
-            for (int r = 0; r < 8; ++r) {
-                const int e = g.sg[8 * n + r];
-                const T val = (e >= 0) ? v[e] : ((e <= -2) ? src[-e - 2] : T(0));
-                acc = acc + coeff[8 * n + r] * val;
-            }
+            T acc = fixed[n];
+            for (int q = g.gg_ptr[n]; q < g.gg_ptr[n + 1]; ++q) acc = acc + ggc[q] * src[g.gg_idx[q]];
             dst[n] = acc;
             ld = fmax(ld, fabs((double)acc - (double)src[n]));
             la = fmax(la, fabs((double)acc));
@@ -2379,15 +2386,15 @@ void launch_outer_ghost(T *v, const Dims &d, const int sign[6], cudaStream_t s)
 }
 
 template <typename T>
-void launch_ghost_rows(T *v, const GhostArgs &g, const T *coeff, T *scratch, int iterMax, double tol,
-                       double reltol, int *d_iters, unsigned long long *d_maxdelta, cudaStream_t s)
+void launch_ghost_rows(T *v, const GhostArgs &g, const T *coeff, const T *gg_coef, T *scratch, int iterMax,
+                       double tol, double reltol, int *d_iters, unsigned long long *d_maxdelta, cudaStream_t s)
 {
     if (g.n <= 0) return;
     if (g.n <= 4096)
         k_ghost_rows<T><<<1, 1024, 0, s>>>(v, g, coeff, scratch, iterMax, tol, reltol, d_iters, d_maxdelta);
     else
-        k_ghost_rows_cluster<T><<<GHOST_CLUSTER, 1024, 0, s>>>(v, g, coeff, scratch, iterMax, tol, reltol, d_iters,
-                                                                d_maxdelta);
+        k_ghost_rows_cluster<T><<<GHOST_CLUSTER, 1024, 0, s>>>(v, g, coeff, gg_coef, scratch, iterMax, tol, reltol,
+                                                                d_iters, d_maxdelta);
 }
 
 void launch_vel_ghosts(double *u, double *v, double *w, const GhostArgs &g, const double *coeffD, const double *bi,
@@ -2655,10 +2662,10 @@ template void launch_prolong_correct<double>(int, const ProlongArgs<double> &, c
 template void launch_prolong_correct<float>(int, const ProlongArgs<float> &, cudaStream_t);
 template void launch_outer_ghost<double>(double *, const Dims &, const int *, cudaStream_t);
 template void launch_outer_ghost<float>(float *, const Dims &, const int *, cudaStream_t);
-template void launch_ghost_rows<double>(double *, const GhostArgs &, const double *, double *, int, double, double,
-                                        int *, unsigned long long *, cudaStream_t);
-template void launch_ghost_rows<float>(float *, const GhostArgs &, const float *, float *, int, double, double,
-                                       int *, unsigned long long *, cudaStream_t);
+template void launch_ghost_rows<double>(double *, const GhostArgs &, const double *, const double *, double *, int,
+                                        double, double, int *, unsigned long long *, cudaStream_t);
+template void launch_ghost_rows<float>(float *, const GhostArgs &, const float *, const float *, float *, int,
+                                       double, double, int *, unsigned long long *, cudaStream_t);
 template void launch_fill<double>(double *, long long, double, cudaStream_t);
 template void launch_fill<float>(float *, long long, float, cudaStream_t);
 template void launch_fill<uint8_t>(uint8_t *, long long, uint8_t, cudaStream_t);

@@ -83,6 +83,8 @@ struct GhostArgs {
     const long long *sidx;   // 8 stencil indices per ghost, -1 = the ghost itself (uNormal term)
     const int *sg;           // the same stencil as: cell index (>= 0) of a non-ghost cell,
                              // -(m + 2) for ghost cell number m, -1 for the uNormal term
+    const int *gg_ptr;       // ghost-ghost couplings in CSR form: entries gg_ptr[n] .. gg_ptr[n+1]-1
+    const int *gg_idx;       // of ghost n refer to ghost gg_idx[q] with weight (per precision) gg_coef[q]
 };
 
 // The fractional-step operations either side of the pressure solve, on
@@ -181,9 +183,11 @@ template <typename T>
 void launch_prolong_correct(int D, const ProlongArgs<T> &a, cudaStream_t s);
 template <typename T>
 void launch_outer_ghost(T *v, const Dims &d, const int sign[6], cudaStream_t s);
+// scratch holds 3 n values of T (two ping-pong buffers and the fixed fluid part of each row);
+// gg_coef: the ghost-ghost weights in the CSR order of g.gg_ptr / g.gg_idx
 template <typename T>
-void launch_ghost_rows(T *v, const GhostArgs &g, const T *coeff, T *scratch, int iterMax, double tol,
-                       double reltol, int *d_iters, unsigned long long *d_maxdelta, cudaStream_t s);
+void launch_ghost_rows(T *v, const GhostArgs &g, const T *coeff, const T *gg_coef, T *scratch, int iterMax,
+                       double tol, double reltol, int *d_iters, unsigned long long *d_maxdelta, cudaStream_t s);
 template <typename T>
 void launch_fill(T *p, long long n, T val, cudaStream_t s);
 
