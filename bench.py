@@ -635,7 +635,9 @@ def main():
             if st != 0:
                 raise RuntimeError(f"e2e solve did not converge: status {st}")
             tot += s_mixed.stats()["e2e_seconds"]
-        nbytes = int(np.prod(sh)) * 8
+        # the library copies the (0:nx+1,0:ny+1,0:nz) part of each full array: the
+        # (nz+1) plane is padding that no routine of the solve reads or writes
+        nbytes = int(sh[0] * sh[1] * (sh[2] - 1)) * 8
         e2e = {"value": world * k / tot, "unit": "solves/s", "h2d_bytes_per_step": 2 * nbytes,
                "d2h_bytes_per_step": nbytes}
 
