@@ -2486,12 +2486,12 @@ void launch_rhs_adjust_bc(const AdCoefArgs &c, const double *const bc[9], double
 void launch_ad_line(int dir, int colour, const AdCoefArgs &c, double *var, const double *r, double *gam,
                     cudaStream_t s)
 {
-    const int a = dir, b = (dir == 0) ? 1 : 0, cc = (dir == 2) ? 1 : 2;
+    // the transverse axes of Axes<dir>: lines of one colour = ceil(nb / 2) x nc
+    const int b = (dir == 0) ? 1 : 0, cc = (dir == 2) ? 1 : 2;
     const long long lines = (long long)((c.d.m[b] - 1 + 1) / 2) * (c.d.m[cc] - 1);
     if (dir == 0) k_ad_line<0><<<nblk(lines), TPB, 0, s>>>(c, var, r, gam, colour);
     else if (dir == 1) k_ad_line<1><<<nblk(lines), TPB, 0, s>>>(c, var, r, gam, colour);
     else k_ad_line<2><<<nblk(lines), TPB, 0, s>>>(c, var, r, gam, colour);
-    (void)a;
 }
 
 void launch_ad_residual(const AdCoefArgs &c, const double *var, const double *r, unsigned long long *maxbits,

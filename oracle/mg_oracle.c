@@ -62,6 +62,8 @@ struct or_ctx {
     double *vg_coeff, *vg_bi;   /* coeffGCMD (8,nGhost); uBI, vBI, wBI (3 x nGhost) or NULL */
     double vg_bw, vg_iw;
     int vg_on, vg_last_iters;
+    /* implicit momentum coefficients amx_ad, apx_ad, amy_ad, apy_ad, amz_ad, apz_ad (or_set_solve_ad) */
+    double *ad[6];
 };
 
 static const int incI[8] = {0, 0, 1, 1, 0, 0, 1, 1};   /* IBM/GCM_MEMORY_ALLOCATE.F90:494-518 */
@@ -230,6 +232,7 @@ void or_destroy(or_ctx *c)
 {
     if (!c) return;
     free(c->vg_coeff); free(c->vg_bi);
+    for (int q = 0; q < 6; ++q) free(c->ad[q]);
     free(c->fresh);
     for (int d = 0; d < 3; ++d) {
         free(c->x[d]); free(c->xc[d]); free(c->dx[d]); free(c->dxinv[d]); free(c->dxc[d]); free(c->dxcinv[d]);
@@ -1598,17 +1601,13 @@ void or_rhs_advec_diff(or_ctx *c, int advec_scheme, int frac_step_type, double d
 /* set_solve_ad (IBM/CORE_SET_SOLVERS.F90:20-95, stationary boundary): the
  * implicit diffusion coefficients amx_ad..apz_ad (0:nx+1)^3, kept in the
  * context for or_rhs_adjust_bc / or_solve_ad. */
-static double *g_ad[6];   /* amx_ad, apx_ad, amy_ad, apy_ad, amz_ad, apz_ad */
-static size_t g_ad_n;
-
 void or_set_solve_ad(or_ctx *c, double dt, const double *visc, const double *const *bcvisc3)
 {
     const size_t nf = (size_t)(c->nx + 2) * (size_t)(c->ny + 2) * (size_t)(c->nz + 2);
-    if (g_ad_n != nf) {
-        for (int q = 0; q < 6; ++q) { free(g_ad[q]); g_ad[q] = zalloc(sizeof(double) * nf); }
-        g_ad_n = nf;
+    for (int q = 0; q < 6; ++q) {
+        if (!c->ad[q]) c->ad[q] = zalloc(sizeof(double) * nf);
+        memset(c->ad[q], 0, sizeof(double) * nf);
     }
-    for (int q = 0; q < 6; ++q) memset(g_ad[q], 0, sizeof(double) * nf);
     const int8_t *ium = c->fl[0], *iup = c->fl[1], *jum = c->fl[2], *jup = c->fl[3], *kum = c->fl[4], *kup = c->fl[5];
     const double rnDim = (double)(c->p.ndim - DIM_2D);
     for (int k = 1; k <= c->nz - 1; ++k)
@@ -1623,17 +1622,17 @@ void or_set_solve_ad(or_ctx *c, double dt, const double *visc, const double *con
                 const double nuB = (fxw(c, 2, k) * visc[f] + (1.0 - fxw(c, 2, k)) * visc[FI(c, i, j, k - 1)]) * (1 - kum[f]) + arr_at(bcvisc3[2], f) * kum[f];
                 double t;
                 t = (c->dxcinv[0][i] * (1 - ium[f]) + c->dxinv[0][i] * ium[f] * 2.0) * c->dxinv[0][i];
-                g_ad[0][f] = -(0.5 * dt * nuW) * t;
+                c->ad[0][f] = -(0.5 * dt * nuW) * t;
                 t = (c->dxcinv[0][i + 1] * (1 - iup[f]) + c->dxinv[0][i] * iup[f] * 2.0) * c->dxinv[0][i];
-                g_ad[1][f] = -(0.5 * dt * nuE) * t;
+                c->ad[1][f] = -(0.5 * dt * nuE) * t;
                 t = (c->dxcinv[1][j] * (1 - jum[f]) + c->dxinv[1][j] * jum[f] * 2.0) * c->dxinv[1][j];
-                g_ad[2][f] = -(0.5 * dt * nuS) * t;
+                c->ad[2][f] = -(0.5 * dt * nuS) * t;
                 t = (c->dxcinv[1][j + 1] * (1 - jup[f]) + c->dxinv[1][j] * jup[f] * 2.0) * c->dxinv[1][j];
-                g_ad[3][f] = -(0.5 * dt * nuN) * t;
+                c->ad[3][f] = -(0.5 * dt * nuN) * t;
                 t = (c->dxcinv[2][k] * (1 - kum[f]) + c->dxinv[2][k] * kum[f] * 2.0) * c->dxinv[2][k];
-                g_ad[4][f] = -(0.5 * dt * nuB) * t * rnDim;
+                c->ad[4][f] = -(0.5 * dt * nuB) * t * rnDim;
                 t = (c->dxcinv[2][k + 1] * (1 - kup[f]) + c->dxinv[2][k] * kup[f] * 2.0) * c->dxinv[2][k];
-                g_ad[5][f] = -(0.5 * dt * nuF) * t * rnDim;
+                c->ad[5][f] = -(0.5 * dt * nuF) * t * rnDim;
             }
 }
 
@@ -1649,8 +1648,8 @@ static void ad_row(or_ctx *c, double half_dt, const double *const *faces, int i,
         const int t = idx[a];
         const int8_t mm = c->fl[2 * a][f], pp = c->fl[2 * a + 1][f];
         const size_t fp = (a == 0) ? FI(c, i + 1, j, k) : (a == 1) ? FI(c, i, j + 1, k) : FI(c, i, j, k + 1);
-        am[a] = g_ad[2 * a][f];
-        ap[a] = g_ad[2 * a + 1][f];
+        am[a] = c->ad[2 * a][f];
+        ap[a] = c->ad[2 * a + 1][f];
         ac[a] = -(am[a] + ap[a]);
         double tmp1 = 1.0 - fxw(c, a, t), tmp2 = fxw(c, a, t + 1);
         am[a] = am[a] - half_dt * faces[a][f] * tmp1 * c->dxinv[a][t];
@@ -1667,6 +1666,7 @@ void or_rhs_adjust_bc(or_ctx *c, int advec_scheme, double dt, const double *cons
                       double *nlu, double *nlv, double *nlw)
 {
     const double half_dt = (advec_scheme == 1) ? 0.0 : 0.5 * dt;
+    if (!c->ad[0]) return;   /* or_set_solve_ad first */
     for (int k = 1; k <= c->nzc; ++k)
         for (int j = 1; j <= c->nyc; ++j)
             for (int i = 1; i <= c->nxc; ++i) {
@@ -1677,8 +1677,8 @@ void or_rhs_adjust_bc(or_ctx *c, int advec_scheme, double dt, const double *cons
                     const int t = idx[a];
                     const int8_t mm = c->fl[2 * a][f], pp = c->fl[2 * a + 1][f];
                     const size_t fp = (a == 0) ? FI(c, i + 1, j, k) : (a == 1) ? FI(c, i, j + 1, k) : FI(c, i, j, k + 1);
-                    md[a] = g_ad[2 * a][f];
-                    pd[a] = g_ad[2 * a + 1][f];
+                    md[a] = c->ad[2 * a][f];
+                    pd[a] = c->ad[2 * a + 1][f];
                     const double tmp1 = (1.0 - fxw(c, a, t)) * (1 - mm) + mm;
                     const double tmp2 = fxw(c, a, t + 1) * (1 - pp) + pp;
                     md[a] = md[a] - half_dt * faces[a][f] * tmp1 * c->dxinv[a][t];
@@ -1788,6 +1788,7 @@ int or_solve_ad(or_ctx *c, int advec_scheme, double dt, const double *const *fac
                 const double *nlu, const double *nlv, const double *nlw, int order, double *maxres)
 {
     const double half_dt = (advec_scheme == 1) ? 0.0 : 0.5 * dt;
+    if (!c->ad[0]) return -1;   /* or_set_solve_ad first */
     const int three_d = (c->p.ndim == DIM_3D);
     const int gcm = (c->p.boundary_formulation == GCM_METHOD);
     double *vel[3] = {u, v, w};
