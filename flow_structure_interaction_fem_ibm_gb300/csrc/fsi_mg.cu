@@ -140,7 +140,7 @@ struct Ctx {
     StepArgs last_fv{}, last_cv{};
     RhsAdArgs last_ad{};
     bool have_ad = false;
-    double *ad_co = nullptr;   // 7 coefficient fields of the implicit momentum operator + line factors
+    double *ad_co = nullptr;   // 7 coefficient fields of the implicit momentum operator + gam scratch
     bool have_fv = false, have_cv = false, have_up = false, last_fv_vk = false, last_up_vk = false;
     double *last_up_p = nullptr;
     const double *last_up_pp = nullptr;
@@ -1699,8 +1699,7 @@ static int ad_coef_args(Ctx &c, int advec_scheme, double dt, const fsi_mg_rhs_ad
     const bool three_d = (c.p.ndim == 3);
     if (!fl || !fl->face_u || !fl->face_v || !fl->face_w || !fl->viscTot) return fail(-1, "null field");
     const long long n = c.L1.d.sxy * (c.nz + 2);
-    // 7 coefficient fields, then binv and gam of the x-, y- and z-lines
-    if (!c.ad_co) TRY(c.alloc(&c.ad_co, (size_t)(13 * n)));
+    if (!c.ad_co) TRY(c.alloc(&c.ad_co, (size_t)(8 * n)));
     a = AdCoefArgs{};
     a.face[0] = fl->face_u; a.face[1] = fl->face_v; a.face[2] = fl->face_w;
     a.visc = fl->viscTot;
@@ -1748,11 +1747,9 @@ int fsi_mg_solve_ad(void *handle, int advec_scheme, double dt, const fsi_mg_rhs_
             return fail(-1, "zero-gradient velocity faces need the mass-flux correction of GCM_GhostCell_Vel, "
                             "which is not supported");
     const long long n = c.L1.d.sxy * (c.nz + 2);
-    double *binv[3], *gam[3];
-    for (int dir = 0; dir < 3; ++dir) { binv[dir] = c.ad_co + (7 + 2 * dir) * n; gam[dir] = c.ad_co + (8 + 2 * dir) * n; }
+    double *gam = c.ad_co + 7 * n;
     launch_ad_coef(a, c.s);
-    for (int dir = 0; dir < (three_d ? 3 : 2); ++dir) launch_ad_factor(dir, a, binv[dir], gam[dir], c.s);
-    c.launches += 1 + (three_d ? 3 : 2);
+    c.launches++;
     double *vel[3] = {d_u, d_v, d_w};
     const double *rr[3] = {fl->nlu, fl->nlv, fl->nlw};
     const int ncomp = three_d ? 3 : 2;
@@ -1775,7 +1772,7 @@ int fsi_mg_solve_ad(void *handle, int advec_scheme, double dt, const fsi_mg_rhs_
         for (int q = 0; q < ncomp; ++q)
             for (int dir = 0; dir < (three_d ? 3 : 2); ++dir)
                 for (int col = 0; col < 2; ++col) {
-                    launch_ad_line(dir, col, a, vel[q], rr[q], binv[dir], gam[dir], c.s);
+                    launch_ad_line(dir, col, a, vel[q], rr[q], gam, c.s);
                     c.launches++;
                 }
         if (gcm && c.vg_on && c.nGhost > 0) {   // GCM_GhostCell_Vel

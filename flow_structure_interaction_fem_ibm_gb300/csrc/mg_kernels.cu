@@ -1751,51 +1751,13 @@ __global__ void __launch_bounds__(TPB) k_rhs_adjust_bc(AdCoefArgs A, const doubl
     }
 }
 
-// Thomas factors of the lines along DIR (tdma, IBM/CORE_TDMA.F90:10-34):
-// binv(i) = 1 / (b(i) - a(i) gam(i)), gam(i) = c(i-1) binv(i-1), one thread
-// per line, every line of both colours.  The rows of the implicit momentum
-// operator are fixed during solve_ad and shared by u, v and w, so the
-// divisions leave the sweeps (GB300 issues FP64 at 1/64 of its FP32 rate, and
-// a division is a dozen FP64 instructions).
-template <int DIR>
-__global__ void __launch_bounds__(TPB) k_ad_factor(AdCoefArgs A, double *binv_out, double *gam)
-{
-    const Dims &d = A.d;
-    using X = Axes<DIR>;
-    const int nb = d.m[X::b] - 1, nc = d.m[X::c] - 1, L = d.m[X::a] - 1;
-    const long long sa = stride_of(d, X::a), sb = stride_of(d, X::b), sc = stride_of(d, X::c);
-    const long long tl = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (tl >= (long long)nb * nc) return;
-    const int q = 1 + (int)(tl / nb), p = 1 + (int)(tl - (long long)(q - 1) * nb);
-    const long long base = p * sb + q * sc;
-    double binv = 0.0, cprev = 0.0;
-    for (int i = 1; i <= L; ++i) {
-        const long long o = base + i * sa;
-        const uint8_t f = A.fl[o];
-        const bool fluid = !(f & FB_IB);
-        const double aa = fluid ? A.co[2 * DIR][o] : 0.0, cc = fluid ? A.co[2 * DIR + 1][o] : 0.0;
-        const double bb = fluid ? 1.0 + A.co[6][o] : 1.0;
-        if (i == 1) {
-            binv = 1.0 / bb;
-            gam[o] = 0.0;
-        } else {
-            const double g = cprev * binv;
-            gam[o] = g;
-            binv = 1.0 / (bb - aa * g);
-        }
-        binv_out[o] = binv;
-        cprev = cc;
-    }
-}
-
 // One colour of the line sweep along DIR (itsolv_ad_x/y/z): one thread per
 // line, lines of colour (q1 + q2) mod 2 over the transverse indices; the
-// right-hand side is assembled as the reference does (identity rows for
-// blanked cells, the ghost's own value kept) and the factored Thomas
-// recurrences of tdma run forward and back.
+// row is assembled as the reference does (identity rows for blanked cells,
+// the ghost's own value kept) and solved by the Thomas algorithm of tdma
+// (IBM/CORE_TDMA.F90:10-34) with gam in a scratch array.
 template <int DIR>
-__global__ void __launch_bounds__(TPB) k_ad_line(AdCoefArgs A, double *var, const double *r, const double *binvs,
-                                                 const double *gam, int colour)
+__global__ void __launch_bounds__(TPB) k_ad_line(AdCoefArgs A, double *var, const double *r, double *gam, int colour)
 {
     const Dims &d = A.d;
     using X = Axes<DIR>;
@@ -1812,11 +1774,11 @@ __global__ void __launch_bounds__(TPB) k_ad_line(AdCoefArgs A, double *var, cons
     // the transverse axes in the reference's order of the right-hand side terms
     const int t1 = X::b < X::c ? X::b : X::c, t2 = X::b < X::c ? X::c : X::b;
     const long long s1 = stride_of(d, t1), s2 = stride_of(d, t2);
-    double uprev = 0.0;
+    double binv = 0.0, uprev = 0.0, cprev = 0.0;
     for (int i = 1; i <= L; ++i) {
         const long long o = base + i * sa;
         const uint8_t f = A.fl[o];
-        const bool fluid = !(f & FB_IB);
+        const double rib = (f & FB_IB) ? 0.0 : 1.0;
         double rhs;
         if (DIR == 2) {   // z-lines subtract term by term, y before x (IBM/CORE_SOLVE_AD.F90:678-681)
             rhs = r[o] - var[o - s2] * A.co[2 * t2][o] - var[o + s2] * A.co[2 * t2 + 1][o]
@@ -1826,15 +1788,20 @@ __global__ void __launch_bounds__(TPB) k_ad_line(AdCoefArgs A, double *var, cons
                               + var[o - s2] * A.co[2 * t2][o] + var[o + s2] * A.co[2 * t2 + 1][o];
             rhs = r[o] - sm;
         }
-        // dd = rhs (1 - iblank) + var ghostCellMark
-        const double dd = fluid ? rhs : ((f & FB_GM) ? var[o] : 0.0);
+        const double aa = A.co[2 * DIR][o] * rib, cc = A.co[2 * DIR + 1][o] * rib;
+        const double bb = 1.0 + A.co[6][o] * rib;
+        const double dd = rhs * rib + ((f & FB_GM) ? var[o] : 0.0);
         if (i == 1) {
-            uprev = dd * binvs[o];
+            binv = 1.0 / bb;
+            uprev = dd * binv;
         } else {
-            const double aa = fluid ? A.co[2 * DIR][o] : 0.0;
-            uprev = (dd - aa * uprev) * binvs[o];
+            const double g = cprev * binv;
+            gam[o] = g;
+            binv = 1.0 / (bb - aa * g);
+            uprev = (dd - aa * uprev) * binv;
         }
         var[o] = uprev;   // the forward solution; the row's own value was read above
+        cprev = cc;
     }
     for (int i = L - 1; i >= 1; --i) {
         const long long o = base + i * sa;
@@ -2516,24 +2483,15 @@ void launch_rhs_adjust_bc(const AdCoefArgs &c, const double *const bc[9], double
                                             nl[1], nl[2]);
 }
 
-void launch_ad_factor(int dir, const AdCoefArgs &c, double *binv, double *gam, cudaStream_t s)
-{
-    const int b = (dir == 0) ? 1 : 0, cc = (dir == 2) ? 1 : 2;
-    const long long lines = (long long)(c.d.m[b] - 1) * (c.d.m[cc] - 1);
-    if (dir == 0) k_ad_factor<0><<<nblk(lines), TPB, 0, s>>>(c, binv, gam);
-    else if (dir == 1) k_ad_factor<1><<<nblk(lines), TPB, 0, s>>>(c, binv, gam);
-    else k_ad_factor<2><<<nblk(lines), TPB, 0, s>>>(c, binv, gam);
-}
-
-void launch_ad_line(int dir, int colour, const AdCoefArgs &c, double *var, const double *r, const double *binv,
-                    const double *gam, cudaStream_t s)
+void launch_ad_line(int dir, int colour, const AdCoefArgs &c, double *var, const double *r, double *gam,
+                    cudaStream_t s)
 {
     // the transverse axes of Axes<dir>: lines of one colour = ceil(nb / 2) x nc
     const int b = (dir == 0) ? 1 : 0, cc = (dir == 2) ? 1 : 2;
     const long long lines = (long long)((c.d.m[b] - 1 + 1) / 2) * (c.d.m[cc] - 1);
-    if (dir == 0) k_ad_line<0><<<nblk(lines), TPB, 0, s>>>(c, var, r, binv, gam, colour);
-    else if (dir == 1) k_ad_line<1><<<nblk(lines), TPB, 0, s>>>(c, var, r, binv, gam, colour);
-    else k_ad_line<2><<<nblk(lines), TPB, 0, s>>>(c, var, r, binv, gam, colour);
+    if (dir == 0) k_ad_line<0><<<nblk(lines), TPB, 0, s>>>(c, var, r, gam, colour);
+    else if (dir == 1) k_ad_line<1><<<nblk(lines), TPB, 0, s>>>(c, var, r, gam, colour);
+    else k_ad_line<2><<<nblk(lines), TPB, 0, s>>>(c, var, r, gam, colour);
 }
 
 void launch_ad_residual(const AdCoefArgs &c, const double *var, const double *r, unsigned long long *maxbits,

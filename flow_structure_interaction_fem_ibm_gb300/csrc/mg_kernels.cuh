@@ -148,12 +148,9 @@ struct AdCoefArgs {
 void launch_ad_coef(const AdCoefArgs &a, cudaStream_t s);
 // rhs_adjust_bc (IBM/CORE_RHS_AD.F90:588-780): nl -= (boundary values of flagged faces) x coefficients
 void launch_rhs_adjust_bc(const AdCoefArgs &c, const double *const bc[9], double *const nl[3], cudaStream_t s);
-// the Thomas factors of every line along axis dir (binv = 1 / pivot and gam per row), fixed
-// during solve_ad: the rows do not change with the iteration or the velocity component
-void launch_ad_factor(int dir, const AdCoefArgs &c, double *binv, double *gam, cudaStream_t s);
 // one colour of the line sweep of itsolv_ad along axis dir on var with right-hand side r
-void launch_ad_line(int dir, int colour, const AdCoefArgs &c, double *var, const double *r, const double *binv,
-                    const double *gam, cudaStream_t s);
+void launch_ad_line(int dir, int colour, const AdCoefArgs &c, double *var, const double *r, double *gam,
+                    cudaStream_t s);
 // max |calc_residual_ad| of var into *maxbits (as the bits of a non-negative double, atomicMax)
 void launch_ad_residual(const AdCoefArgs &c, const double *var, const double *r, unsigned long long *maxbits,
                         cudaStream_t s);
