@@ -129,6 +129,7 @@ struct Ctx {
     int step_cap = 0;
     double *vtilde = nullptr;   // uTilde, vTilde, wTilde of the VAN_KAN face_vel (allocated on first use)
     bool coarsest_fp32 = true;   // mixed form: the coarsest level is smoothed in FP32 like the others
+    double ghost32_reltol = 1.0e-6;   // FP32 ghost rows stop at max|dp| <= this x max|p_g| (FSI_MG_GHOST32_RELTOL)
     // ghost-cell velocities (GCM_vel_set_bc_internal), registered by fsi_mg_set_velocity_ghosts
     bool vg_on = false;
     int vg_cap = 0;
@@ -508,7 +509,8 @@ void gcm_pressure<float>(Ctx &c, float *v)
     c.launches++;
     if (c.nGhost > 0) {
         GhostArgs g{c.nGhost, c.gidx, c.sidx, c.gsg, c.gg_ptr, c.gg_idx};
-        launch_ghost_rows<float>(v, g, c.gco32, c.ggc32, c.gscr32, c.p.iterMax_ad, c.p.restol_ad, 1.0e-6, c.d_iters, c.d_maxd,
+        launch_ghost_rows<float>(v, g, c.gco32, c.ggc32, c.gscr32, c.p.iterMax_ad, c.p.restol_ad, c.ghost32_reltol,
+                                 c.d_iters, c.d_maxd,
                                  c.s);
         c.launches++;
     }
@@ -842,7 +844,7 @@ int solve_krylov_t(Ctx &c, double *p, const double *b, int *iters, double *maxre
                 if (c.nGhost > 0) {
                     GhostArgs ga{c.nGhost, c.gidx, c.sidx, c.gsg, c.gg_ptr, c.gg_idx};
                     launch_ghost_rows<T>(KZ[j], ga, gco, f32 ? (const T *)c.ggc32 : (const T *)c.ggc64, gscr,
-                                         c.p.iterMax_ad, c.p.restol_ad, f32 ? 1.0e-6 : 0.0,
+                                         c.p.iterMax_ad, c.p.restol_ad, f32 ? c.ghost32_reltol : 0.0,
                                          c.d_iters, c.d_maxd, c.s);
                 }
                 c.launches += 2;
@@ -1056,6 +1058,11 @@ int fsi_mg_create(const fsi_mg_params *params, const double *x, const double *y,
     }
     auto c = std::make_unique<Ctx>();
     c->p = p;
+    {   // FSI_MG_GHOST32_RELTOL: relative stopping threshold of the FP32 ghost rows (A/B measurements)
+        const char *gr = std::getenv("FSI_MG_GHOST32_RELTOL");
+        const double v = gr ? std::atof(gr) : 0.0;
+        if (v > 0.0 && v < 1.0) c->ghost32_reltol = v;
+    }
     {   // FSI_MG_COARSEST_FP64=1: FP64 coarsest-level smoothing inside the FP32 cycle (A/B measurements)
         const char *cf = std::getenv("FSI_MG_COARSEST_FP64");
         c->coarsest_fp32 = !(cf && std::strcmp(cf, "1") == 0);
