@@ -1023,11 +1023,29 @@ __global__ void __launch_bounds__(1024) k_ghost_rows(T *v, GhostArgs g, const T 
     }
 }
 
-// Same fixed-point iteration spread over a cluster of 8 CTAs (8192 threads).
-// The stencil entries that are not ghost cells do not change during the
-// iteration, so each row's sum over them is formed once (scratch[2n:3n]);
-// a sweep then adds only the row's ghost-ghost couplings (a CSR list, under
-// one entry per ghost on average) read from the current buffer.  The ghost
+// The stencil entries of a ghost row that are not ghost cells do not change
+// during the iteration: their sum is formed once per call, with the starting
+// ghost values, by a grid over all SMs (the gather is latency-bound and
+// needs the memory parallelism of the whole GPU, not of one cluster).
+template <typename T>
+__global__ void __launch_bounds__(TPB) k_ghost_fixed(const T *v, GhostArgs g, const T *coeff, T *scratch)
+{
+    const int n = blockIdx.x * blockDim.x + threadIdx.x;
+    if (n >= g.n) return;
+    T acc = T(0);
+#pragma unroll
+    for (int r = 0; r < 8; ++r) {
+        const int e = g.sg[8 * n + r];
+        if (e >= 0) acc = acc + coeff[8 * n + r] * v[e];
+    }
+    scratch[n] = v[g.gidx[n]];      // bufA: the starting ghost values
+    scratch[2 * g.n + n] = acc;     // the row's fixed part
+}
+
+// Same fixed-point iteration spread over a cluster of 8 CTAs (8192 threads),
+// after k_ghost_fixed: a sweep adds to each row's fixed part only its
+// ghost-ghost couplings (a CSR list, under one entry per ghost on average)
+// read from the current buffer.  The ghost
 // values are iterated in two ping-pong buffers (scratch[0:n] and
 // scratch[n:2n]), so one cluster barrier per sweep orders everything: each
 // CTA also posts its sweep maxima into rank 0's shared slots, double-buffered
@@ -1049,18 +1067,10 @@ __global__ void __cluster_dims__(GHOST_CLUSTER, 1, 1) __launch_bounds__(1024)
     const int gtid = (int)rank * (int)blockDim.x + tid, gstride = GHOST_CLUSTER * (int)blockDim.x;
     double *rslot_d = cluster.map_shared_rank(&slot_d[0][0], 0);
     double *rslot_a = cluster.map_shared_rank(&slot_a[0][0], 0);
-    T *bufA = scratch, *bufB = scratch + g.n, *fixed = scratch + 2 * g.n;
-    for (int n = gtid; n < g.n; n += gstride) {
-        bufA[n] = v[g.gidx[n]];
-        T acc = T(0);
-#pragma unroll
-        for (int r = 0; r < 8; ++r) {
-            const int e = g.sg[8 * n + r];
-            if (e >= 0) acc = acc + coeff[8 * n + r] * v[e];
-        }
-        fixed[n] = acc;
-    }
-    cluster.sync();
+    T *bufA = scratch, *bufB = scratch + g.n;
+    const T *fixed = scratch + 2 * g.n;
+    (void)coeff;   // the fluid part of each row was summed by k_ghost_fixed
+    cluster.sync();   // every CTA of the cluster runs before rank 0's slots are written
     int it = 0, par = 0;
     double maxd = 1.0e10, thr = tol;
     while (it < iterMax && maxd > thr) {
@@ -2392,9 +2402,11 @@ void launch_ghost_rows(T *v, const GhostArgs &g, const T *coeff, const T *gg_coe
     if (g.n <= 0) return;
     if (g.n <= 4096)
         k_ghost_rows<T><<<1, 1024, 0, s>>>(v, g, coeff, scratch, iterMax, tol, reltol, d_iters, d_maxdelta);
-    else
+    else {
+        k_ghost_fixed<T><<<nblk(g.n), TPB, 0, s>>>(v, g, coeff, scratch);
         k_ghost_rows_cluster<T><<<GHOST_CLUSTER, 1024, 0, s>>>(v, g, coeff, gg_coef, scratch, iterMax, tol, reltol,
                                                                 d_iters, d_maxdelta);
+    }
 }
 
 void launch_vel_ghosts(double *u, double *v, double *w, const GhostArgs &g, const double *coeffD, const double *bi,
