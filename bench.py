@@ -199,9 +199,9 @@ def oracle_iteration_time(n, seed, reps=1):
 # (n, seed, tol): (iterations, how they were obtained)
 REFERENCE_ITERATIONS = {
     (128, 3, 1e-8): (121, "oracle solve to convergence at 128^3 (reference line order, iRedBlack 0)"),
-    (256, 3, 1e-8): (416, "estimate: the stationary count of the GPU line order at 256^3 (523) times the "
-                          "reference-order / GPU-order ratio measured at 128^3 (121 / 152); the oracle's first "
-                          "40 iterations at 256^3 contract at 0.93-0.95 and have not reached their asymptote"),
+    (256, 3, 1e-8): (413, "160 oracle iterations run at 256^3 (reference line order; maxres 0.0199 against "
+                          "restol 3.50e-6, 1.9 h on one core) and the remaining 253 extrapolated at the "
+                          "asymptotic contraction 0.9664 per iteration, constant over the last 25 iterations"),
 }
 
 
