@@ -1333,6 +1333,7 @@ int fsi_mg_set_geometry(void *handle, const int8_t *iblank, const int8_t *ghostC
             ggp[n + 1] = (int)ggi.size();
         }
         std::vector<float> ggcf(ggc.begin(), ggc.end());
+        if ((long long)ggi.size() >= (1LL << 27)) return fail(-3, "too many ghost-ghost couplings");
         if (nGhost > c.ghost_cap || (int)ggi.size() > c.gg_cap) {
             for (void *q : {(void *)c.gg_ptr, (void *)c.gg_idx, (void *)c.ggc64, (void *)c.ggc32}) {
                 auto it = std::find(c.allocs.begin(), c.allocs.end(), q);

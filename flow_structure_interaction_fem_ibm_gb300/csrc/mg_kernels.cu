@@ -1070,6 +1070,21 @@ __global__ void __cluster_dims__(GHOST_CLUSTER, 1, 1) __launch_bounds__(1024)
     T *bufA = scratch, *bufB = scratch + g.n;
     const T *fixed = scratch + 2 * g.n;
     (void)coeff;   // the fluid part of each row was summed by k_ghost_fixed
+    // the first GHOST_REG ghosts of this thread keep their CSR range and fixed
+    // part in registers across the sweeps, so a sweep only issues the
+    // couplings' loads (independent over the ghosts); the rest use the list
+    // (CSR start << 4 | count: a row has at most 8 ghost couplings)
+    constexpr int GHOST_REG = 5;
+    int qp[GHOST_REG];
+    T fx[GHOST_REG];
+#pragma unroll
+    for (int k = 0; k < GHOST_REG; ++k) {
+        const int n = gtid + k * gstride;
+        const bool in = n < g.n;
+        const int a = in ? g.gg_ptr[n] : 0, b = in ? g.gg_ptr[n + 1] : 0;
+        qp[k] = (a << 4) | (b - a);
+        fx[k] = in ? fixed[n] : T(0);
+    }
     cluster.sync();   // every CTA of the cluster runs before rank 0's slots are written
     int it = 0, par = 0;
     double maxd = 1.0e10, thr = tol;
@@ -1077,7 +1092,19 @@ __global__ void __cluster_dims__(GHOST_CLUSTER, 1, 1) __launch_bounds__(1024)
         const T *src = par ? bufB : bufA;
         T *dst = par ? bufA : bufB;
         double ld = 0.0, la = 0.0;
-        for (int n = gtid; n < g.n; n += gstride) {
+#pragma unroll
+        for (int k = 0; k < GHOST_REG; ++k) {
+            const int n = gtid + k * gstride;
+            if (n < g.n) {
+                T acc = fx[k];
+                const int qa = qp[k] >> 4, qb = qa + (qp[k] & 15);
+                for (int q = qa; q < qb; ++q) acc = acc + ggc[q] * src[g.gg_idx[q]];
+                dst[n] = acc;
+                ld = fmax(ld, fabs((double)acc - (double)src[n]));
+                la = fmax(la, fabs((double)acc));
+            }
+        }
+        for (int n = gtid + GHOST_REG * gstride; n < g.n; n += gstride) {
             T acc = fixed[n];
             for (int q = g.gg_ptr[n]; q < g.gg_ptr[n + 1]; ++q) acc = acc + ggc[q] * src[g.gg_idx[q]];
             dst[n] = acc;
