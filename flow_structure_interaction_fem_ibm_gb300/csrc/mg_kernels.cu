@@ -1060,7 +1060,7 @@ __global__ void __cluster_dims__(GHOST_CLUSTER, 1, 1) __launch_bounds__(1024)
 {
     namespace cg = cooperative_groups;
     cg::cluster_group cluster = cg::this_cluster();
-    __shared__ double s_d[32], s_a[32];
+    __shared__ double s_d[32], s_a[32], s_res[2];
     __shared__ double slot_d[2][GHOST_CLUSTER], slot_a[2][GHOST_CLUSTER];   // used in rank 0 only
     const unsigned rank = cluster.block_rank();
     const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5, nw = (blockDim.x + 31) >> 5;
@@ -1124,16 +1124,21 @@ __global__ void __cluster_dims__(GHOST_CLUSTER, 1, 1) __launch_bounds__(1024)
             rslot_a[par * GHOST_CLUSTER + rank] = b;
         }
         cluster.sync();   // dst and this sweep's slots are complete
-        double a = 0.0, b = 0.0;
-        for (int q = 0; q < GHOST_CLUSTER; ++q) {
-            a = fmax(a, rslot_d[par * GHOST_CLUSTER + q]);
-            b = fmax(b, rslot_a[par * GHOST_CLUSTER + q]);
+        if (tid == 0) {   // one thread per CTA reads rank 0's slots (not every thread)
+            double a = 0.0, b = 0.0;
+            for (int q = 0; q < GHOST_CLUSTER; ++q) {
+                a = fmax(a, rslot_d[par * GHOST_CLUSTER + q]);
+                b = fmax(b, rslot_a[par * GHOST_CLUSTER + q]);
+            }
+            s_res[0] = a;
+            s_res[1] = b;
         }
-        maxd = a;
-        thr = fmax(tol, reltol * b);
+        __syncthreads();
+        maxd = s_res[0];
+        thr = fmax(tol, reltol * s_res[1]);
         ++it;
         par ^= 1;
-        __syncthreads();   // s_d / s_a are rewritten by the next sweep
+        __syncthreads();   // s_d / s_a / s_res are rewritten by the next sweep
     }
     const T *fin = par ? bufB : bufA;   // the buffer the last sweep wrote
     for (int n = gtid; n < g.n; n += gstride) v[g.gidx[n]] = fin[n];
@@ -1158,7 +1163,7 @@ __global__ void __cluster_dims__(GHOST_CLUSTER, 1, 1) __launch_bounds__(1024)
 {
     namespace cg = cooperative_groups;
     cg::cluster_group cluster = cg::this_cluster();
-    __shared__ double s_d[32];
+    __shared__ double s_d[32], s_res;
     __shared__ double slot_d[2][GHOST_CLUSTER];   // used in rank 0 only
     const unsigned rank = cluster.block_rank();
     const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5, nw = (blockDim.x + 31) >> 5;
@@ -1203,12 +1208,16 @@ __global__ void __cluster_dims__(GHOST_CLUSTER, 1, 1) __launch_bounds__(1024)
             rslot_d[par * GHOST_CLUSTER + rank] = a;
         }
         cluster.sync();   // dst and this sweep's slots are complete
-        double a = 0.0;
-        for (int q = 0; q < GHOST_CLUSTER; ++q) a = fmax(a, rslot_d[par * GHOST_CLUSTER + q]);
-        maxd = a;
+        if (tid == 0) {   // one thread per CTA reads rank 0's slots (not every thread)
+            double a = 0.0;
+            for (int q = 0; q < GHOST_CLUSTER; ++q) a = fmax(a, rslot_d[par * GHOST_CLUSTER + q]);
+            s_res = a;
+        }
+        __syncthreads();
+        maxd = s_res;
         ++it;
         par ^= 1;
-        __syncthreads();   // s_d is rewritten by the next sweep
+        __syncthreads();   // s_d / s_res are rewritten by the next sweep
     }
     const double *fin = par ? bufB : bufA;   // the buffer the last sweep wrote
     for (int n = gtid; n < g.n; n += gstride) {
