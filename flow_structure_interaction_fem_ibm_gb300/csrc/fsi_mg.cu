@@ -166,7 +166,6 @@ struct Ctx {
     double *kw = nullptr, *kzp = nullptr, *kzr = nullptr;
     float *kw32 = nullptr;
     double *kpart = nullptr, *kdots = nullptr, *h_kdots = nullptr;
-    int *kskip = nullptr;   // 1: the second Gram-Schmidt pass of this iteration is skipped
     cudaGraphExec_t pgraph = nullptr;      // MG preconditioner on fixed buffers
     long long pgraph_kernels = 0;
 
@@ -726,7 +725,6 @@ int ensure_krylov(Ctx &c, int m)
         TRY(c.alloc(&c.kw, n1));
         TRY(c.alloc(&c.kpart, 8 * (size_t)c.nred + 8));
         TRY(c.alloc(&c.kdots, 256));
-        TRY(c.alloc(&c.kskip, 1));
         CK(cudaMallocHost(&c.h_kdots, 256 * sizeof(double)));
     }
     c.km = m;
@@ -854,19 +852,15 @@ int solve_krylov_t(Ctx &c, double *p, const double *b, int *iters, double *maxre
             launch_apply_op<T>(KZ[j], w, c.L1.fl, coefT, c.L1.d, c.s);
             c.launches++;
             const T *const *Vp = KV.data();
-            // classical Gram-Schmidt; the second pass only where the first lost
-            // more than |w| / sqrt 2 (the Daniel-Gragg-Kaufman-Stewart test)
-            std::vector<const T *> Vw(Vp, Vp + j + 1);
-            Vw.push_back(w);   // |w|^2 with the first pass's dots
-            launch_mdot<T>(Vw.data(), j + 2, w, c.L1.fl, c.L1.d, c.kpart, c.nred, c.kdots, c.s);
+            // classical Gram-Schmidt, twice
+            launch_mdot<T>(Vp, j + 1, w, c.L1.fl, c.L1.d, c.kpart, c.nred, c.kdots, c.s);
             launch_maxpy<T>(w, Vp, j + 1, c.kdots, -1.0, n1, c.s);
-            launch_reorth_test(c.kdots, j + 1, c.kdots + 64, c.kskip, c.s);
-            launch_mdot<T>(Vp, j + 1, w, c.L1.fl, c.L1.d, c.kpart, c.nred, c.kdots + 64, c.s, c.kskip);
-            launch_maxpy<T>(w, Vp, j + 1, c.kdots + 64, -1.0, n1, c.s, c.kskip);
+            launch_mdot<T>(Vp, j + 1, w, c.L1.fl, c.L1.d, c.kpart, c.nred, c.kdots + 64, c.s);
+            launch_maxpy<T>(w, Vp, j + 1, c.kdots + 64, -1.0, n1, c.s);
             const T *wp = w;
             launch_mdot<T>(&wp, 1, w, c.L1.fl, c.L1.d, c.kpart, c.nred, c.kdots + 128, c.s);
             launch_scale_copy<T, T>(KV[j + 1], w, c.kdots + 128, n1, c.s);
-            c.launches += 4 * ((j + 8) / 8) * 2 + 4;
+            c.launches += 4 * ((j + 8) / 8) * 2 + 3;
             CK(cudaMemcpyAsync(c.h_kdots, c.kdots, 256 * sizeof(double), cudaMemcpyDeviceToHost, c.s));
             CK(cudaStreamSynchronize(c.s));
             if (c.lt_on) lt_harvest(c, c.pgraph_lt0, c.pgraph_lt1);

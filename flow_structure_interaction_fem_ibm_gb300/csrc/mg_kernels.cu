@@ -2036,13 +2036,9 @@ struct VecSet { const T *v[8]; int n; };
 
 // partials[blk * 8 + q] = sum over fluid interior cells of V_q * w (per-thread sums
 // in T, block sums in FP64)
-// (skip: a device flag, non-zero = do nothing; the selective second pass of
-// the Gram-Schmidt orthogonalisation)
 template <typename T>
-__global__ void __launch_bounds__(TPB) k_mdot(VecSet<T> V, const T *w, const uint8_t *fl, Dims d, double *partials,
-                                              const int *skip)
+__global__ void __launch_bounds__(TPB) k_mdot(VecSet<T> V, const T *w, const uint8_t *fl, Dims d, double *partials)
 {
-    if (skip && *skip) return;
     const int n0 = d.m[0] - 1, n1 = d.m[1] - 1, n2 = d.m[2] - 1;
     const long long total = (long long)n0 * n1 * n2;
     T acc[8] = {0, 0, 0, 0, 0, 0, 0, 0};
@@ -2064,9 +2060,8 @@ __global__ void __launch_bounds__(TPB) k_mdot(VecSet<T> V, const T *w, const uin
 }
 
 // out[q] = sum_b partials[b * 8 + q]  (fixed order)
-__global__ void k_mdot_final(const double *partials, int nb, int n, double *out, const int *skip)
+__global__ void k_mdot_final(const double *partials, int nb, int n, double *out)
 {
-    if (skip && *skip) return;
     for (int q = 0; q < n; ++q) {
         double x = 0.0;
         for (int b = threadIdx.x; b < nb; b += blockDim.x) x += partials[(long long)b * 8 + q];
@@ -2078,10 +2073,8 @@ __global__ void k_mdot_final(const double *partials, int nb, int n, double *out,
 
 // w += sum_q sign * coef[q] * V_q  over all cells (coef on the device)
 template <typename T>
-__global__ void __launch_bounds__(TPB) k_maxpy(T *w, VecSet<T> V, const double *coef, double sign, long long n,
-                                               const int *skip)
+__global__ void __launch_bounds__(TPB) k_maxpy(T *w, VecSet<T> V, const double *coef, double sign, long long n)
 {
-    if (skip && *skip) return;
     // coefficients converted once per block (a per-element FP64 multiply would
     // make this streaming kernel FP64-bound)
     __shared__ T s_cf[8];
@@ -2621,48 +2614,26 @@ void launch_apply_op(const T *z, T *w, const uint8_t *fl, const Coef<T> &c, cons
 
 template <typename T>
 void launch_mdot(const T *const *V, int nv, const T *w, const uint8_t *fl, const Dims &d, double *partials,
-                 int nblocks, double *out, cudaStream_t s, const int *skip)
+                 int nblocks, double *out, cudaStream_t s)
 {
     for (int q0 = 0; q0 < nv; q0 += 8) {
         VecSet<T> vs;
         vs.n = (nv - q0 < 8) ? nv - q0 : 8;
         for (int q = 0; q < 8; ++q) vs.v[q] = (q < vs.n) ? V[q0 + q] : nullptr;
-        k_mdot<T><<<nblocks, TPB, 0, s>>>(vs, w, fl, d, partials, skip);
-        k_mdot_final<<<1, 1024, 0, s>>>(partials, nblocks, vs.n, out + q0, skip);
+        k_mdot<T><<<nblocks, TPB, 0, s>>>(vs, w, fl, d, partials);
+        k_mdot_final<<<1, 1024, 0, s>>>(partials, nblocks, vs.n, out + q0);
     }
-}
-
-// Daniel-Gragg-Kaufman-Stewart test after the first Gram-Schmidt pass: with
-// h = V^T w and ww = |w|^2 from that pass, |w - V h|^2 = ww - |h|^2; a second
-// pass is needed only if that is below half of ww (|w'| < |w| / sqrt 2).
-// Otherwise the second pass's coefficients are zero and its kernels skip.
-__global__ void k_reorth_test(double *dots, int nv, double *dots2, int *skip)
-{
-    if (threadIdx.x != 0) return;
-    double h2 = 0.0;
-    for (int q = 0; q < nv; ++q) h2 += dots[q] * dots[q];
-    const double ww = dots[nv];
-    const int sk = (ww - h2 > 0.5 * ww) ? 1 : 0;
-    *skip = sk;
-    if (sk)
-        for (int q = 0; q < nv; ++q) dots2[q] = 0.0;
 }
 
 template <typename T>
-void launch_maxpy(T *w, const T *const *V, int nv, const double *coef, double sign, long long n, cudaStream_t s,
-                  const int *skip)
+void launch_maxpy(T *w, const T *const *V, int nv, const double *coef, double sign, long long n, cudaStream_t s)
 {
     for (int q0 = 0; q0 < nv; q0 += 8) {
         VecSet<T> vs;
         vs.n = (nv - q0 < 8) ? nv - q0 : 8;
         for (int q = 0; q < 8; ++q) vs.v[q] = (q < vs.n) ? V[q0 + q] : nullptr;
-        k_maxpy<T><<<nblk(n), TPB, 0, s>>>(w, vs, coef + q0, sign, n, skip);
+        k_maxpy<T><<<nblk(n), TPB, 0, s>>>(w, vs, coef + q0, sign, n);
     }
-}
-
-void launch_reorth_test(double *dots, int nv, double *dots2, int *skip, cudaStream_t s)
-{
-    k_reorth_test<<<1, 32, 0, s>>>(dots, nv, dots2, skip);
 }
 
 template <typename T, typename S>
@@ -2676,13 +2647,13 @@ template void launch_apply_op<double>(const double *, double *, const uint8_t *,
 template void launch_apply_op<float>(const float *, float *, const uint8_t *, const Coef<float> &, const Dims &,
                                      cudaStream_t);
 template void launch_mdot<double>(const double *const *, int, const double *, const uint8_t *, const Dims &, double *,
-                                  int, double *, cudaStream_t, const int *);
+                                  int, double *, cudaStream_t);
 template void launch_mdot<float>(const float *const *, int, const float *, const uint8_t *, const Dims &, double *,
-                                 int, double *, cudaStream_t, const int *);
+                                 int, double *, cudaStream_t);
 template void launch_maxpy<double>(double *, const double *const *, int, const double *, double, long long,
-                                   cudaStream_t, const int *);
+                                   cudaStream_t);
 template void launch_maxpy<float>(float *, const float *const *, int, const double *, double, long long,
-                                  cudaStream_t, const int *);
+                                  cudaStream_t);
 template void launch_scale_copy<double, double>(double *, const double *, const double *, long long, cudaStream_t);
 template void launch_scale_copy<float, float>(float *, const float *, const double *, long long, cudaStream_t);
 template void launch_scale_copy<float, double>(float *, const double *, const double *, long long, cudaStream_t);

@@ -202,14 +202,9 @@ template <typename T>
 void launch_apply_op(const T *z, T *w, const uint8_t *fl, const Coef<T> &c, const Dims &d, cudaStream_t s);
 template <typename T>
 void launch_mdot(const T *const *V, int nv, const T *w, const uint8_t *fl, const Dims &d, double *partials,
-                 int nblocks, double *out, cudaStream_t s,
-                 const int *skip = nullptr);
+                 int nblocks, double *out, cudaStream_t s);
 template <typename T>
-void launch_maxpy(T *w, const T *const *V, int nv, const double *coef, double sign, long long n, cudaStream_t s,
-                  const int *skip = nullptr);
-// selective re-orthogonalisation: dots = V^T w with |w|^2 at dots[nv]; sets *skip and zeroes dots2 when
-// the first Gram-Schmidt pass kept more than |w| / sqrt 2
-void launch_reorth_test(double *dots, int nv, double *dots2, int *skip, cudaStream_t s);
+void launch_maxpy(T *w, const T *const *V, int nv, const double *coef, double sign, long long n, cudaStream_t s);
 template <typename T, typename S>
 void launch_scale_copy(T *dst, const S *src, const double *nrm2, long long n, cudaStream_t s);
 int calc_residual_blocks(const Dims &d);
