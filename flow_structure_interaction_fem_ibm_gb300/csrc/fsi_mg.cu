@@ -129,11 +129,6 @@ struct Ctx {
     int step_cap = 0;
     double *vtilde = nullptr;   // uTilde, vTilde, wTilde of the VAN_KAN face_vel (allocated on first use)
     bool coarsest_fp32 = true;   // mixed form: the coarsest level is smoothed in FP32 like the others
-    // x-parity-split copies of the level-1 FP32 rhs and flags for the y/z line sweeps
-    float *r32s = nullptr;
-    uint8_t *fl1s = nullptr;
-    const float *r32s_src = nullptr;   // the rhs the split copy was made of (per MG_Solver application)
-    bool split_on = true;              // FSI_MG_SPLIT=0 turns it off (A/B)
     double ghost32_reltol = 1.0e-6;   // FP32 ghost rows stop at max|dp| <= this x max|p_g| (FSI_MG_GHOST32_RELTOL)
     // ghost-cell velocities (GCM_vel_set_bc_internal), registered by fsi_mg_set_velocity_ghosts
     bool vg_on = false;
@@ -459,11 +454,7 @@ void itsolv(Ctx &c, Level &L, T *v, const T *r, bool finest, bool homogeneous)
     a.v = v; a.r = r; a.fl = L.fl; a.U = scratch_U<T>(c); a.c = coef_of<T>(L); a.d = L.d;
     a.omega = (T)c.p.omega;
     const bool om1 = (c.p.omega == 1.0);
-    const bool split = std::is_same<T, float>::value && &L == &c.L1 && c.r32s_src != nullptr &&
-                       (const void *)r == (const void *)c.r32s_src;
     for (int dir = 0; dir < c.nd; ++dir) {
-        a.rs = (split && dir != 0) ? (const T *)(const void *)c.r32s : nullptr;
-        a.fls = (split && dir != 0) ? c.fl1s : nullptr;
         a.wpf = std::is_same<T, double>::value ? L.wpf[dir] : nullptr;
         a.binv = lv_binv<T>(L, dir);
         a.gam = lv_gam<T>(L, dir);
@@ -606,18 +597,11 @@ void mg_cycle(Ctx &c, int d, T *var, const T *rhs, int n, int WF, int &GMM, bool
 template <typename T>
 void mg_solver(Ctx &c, T *var, const T *rhs, bool homogeneous)
 {
-    if (std::is_same<T, float>::value && c.split_on && c.r32s) {
-        // the level-1 rhs is fixed through the three cycles: its split copy feeds the y/z sweeps
-        launch_split_x<float>(c.r32s, (const float *)rhs, c.L1.d, c.s);
-        c.launches++;
-        c.r32s_src = (const float *)rhs;
-    }
     for (int d = 0; d < c.nd; ++d) {
         const int sel = (d == 2) ? c.p.mgcycle[0] : c.p.mgcycle[d];   // MG_Solv_z tests mgCycleX (:515)
         int GMM = (sel == 1) ? 1 : 2;
         mg_cycle<T>(c, d, var, rhs, 1, 1, GMM, homogeneous);
     }
-    c.r32s_src = nullptr;
 }
 
 // subtracting_average_pressure (IBM/CORE_POISSON.F90:419-490): volume-weighted
@@ -1074,10 +1058,6 @@ int fsi_mg_create(const fsi_mg_params *params, const double *x, const double *y,
     }
     auto c = std::make_unique<Ctx>();
     c->p = p;
-    {   // FSI_MG_SPLIT=0: y/z line sweeps read the natural layout (A/B measurements)
-        const char *sp = std::getenv("FSI_MG_SPLIT");
-        c->split_on = !(sp && std::strcmp(sp, "0") == 0);
-    }
     {   // FSI_MG_GHOST32_RELTOL: relative stopping threshold of the FP32 ghost rows (A/B measurements)
         const char *gr = std::getenv("FSI_MG_GHOST32_RELTOL");
         const double v = gr ? std::atof(gr) : 0.0;
@@ -1263,10 +1243,6 @@ int fsi_mg_set_geometry(void *handle, const int8_t *iblank, const int8_t *ghostC
     if (nsolid > 0 && c.p.internal_boundary_present != 1)
         return fail(-1, "iblank has solid cells but internal_boundary_present is 0");
     CK(cudaMemcpyAsync(c.L1.fl, fl.data(), nf, cudaMemcpyHostToDevice, c.s));
-    if (c.p.precision_mode == 1 && c.split_on) {
-        if (!c.r32s) { TRY(c.alloc(&c.r32s, (size_t)nf)); TRY(c.alloc(&c.fl1s, (size_t)nf)); }
-        launch_split_x<uint8_t>(c.fl1s, c.L1.fl, d1, c.s);
-    }
     // level-1 coefficients; Dirichlet at the finest level
     const int N[3] = {nx, ny, nz};
     for (int a = 0; a < 3; ++a) {

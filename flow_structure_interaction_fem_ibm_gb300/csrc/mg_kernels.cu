@@ -317,11 +317,6 @@ __global__ void __launch_bounds__(256) k_line_wp(LineArgs<T> A)
     int ps = 1, qs = 1;
     const bool oks = line_pq(gs, ps, qs);
     const int base = ps * sb_ + qs * sc_;
-    // y- and z-lines with split copies: offset from the natural to the split index
-    // (the line's x position ps moves to its parity half)
-    const bool split = (DIR != 0) && A.rs != nullptr;
-    const int sxd = (int)d.sx;
-    const int dsplit = split ? (((ps & 1) ? ((sxd + 1) >> 1) + (ps >> 1) : (ps >> 1)) - ps) : 0;
 
     // ---- 1. staging: loads for up to 4 rows are issued before any use ----
     if (oks) {
@@ -339,8 +334,8 @@ __global__ void __launch_bounds__(256) k_line_wp(LineArgs<T> A)
                 const int r = (q0 + u) * 32 + rr;
                 if (r < L) {
                     const int o = base + (r + 1) * sa_;
-                    in[u].f = split ? A.fls[o + dsplit] : A.fl[o];
-                    in[u].r = split ? A.rs[o + dsplit] : A.r[o];
+                    in[u].f = A.fl[o];
+                    in[u].r = A.r[o];
                     in[u].vo = A.v[o];
                     if (X::c_first) {
                         in[u].nb0 = A.v[o - sc_]; in[u].nb1 = A.v[o + sc_];
@@ -1234,17 +1229,6 @@ __global__ void __cluster_dims__(GHOST_CLUSTER, 1, 1) __launch_bounds__(1024)
         atomicAdd(iters, it);
         atomicMax(maxdelta, (unsigned long long)__double_as_longlong(maxd));
     }
-}
-
-// x-parity split of a level-1 array: dst[split(o)] = src[o]
-template <typename T>
-__global__ void __launch_bounds__(TPB) k_split_x(T *dst, const T *src, Dims d)
-{
-    const long long o = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (o >= d.count()) return;
-    const long long i = o % d.sx;
-    const long long xs = (i & 1) ? ((d.sx + 1) >> 1) + (i >> 1) : (i >> 1);
-    dst[o - i + xs] = src[o];
 }
 
 template <typename T>
@@ -2533,14 +2517,6 @@ void launch_rhs_advec_diff(const RhsAdArgs &a, cudaStream_t s)
     const long long n = (long long)(a.d.m[0] - 1) * (a.d.m[1] - 1) * (a.d.m[2] - 1);
     k_rhs_advec_diff<<<nblk(n), TPB, 0, s>>>(a);
 }
-
-template <typename T>
-void launch_split_x(T *dst, const T *src, const Dims &d, cudaStream_t s)
-{
-    k_split_x<T><<<nblk(d.count()), TPB, 0, s>>>(dst, src, d);
-}
-template void launch_split_x<float>(float *, const float *, const Dims &, cudaStream_t);
-template void launch_split_x<uint8_t>(uint8_t *, const uint8_t *, const Dims &, cudaStream_t);
 
 void launch_ad_coef(const AdCoefArgs &a, cudaStream_t s)
 {

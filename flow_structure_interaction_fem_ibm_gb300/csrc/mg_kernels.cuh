@@ -44,14 +44,7 @@ struct LineArgs {
     int dir_lo, dir_hi;   // finest-level Dirichlet ends along the line direction
     T ppp_lo, ppp_hi;
     const double *wpf = nullptr;   // factored partition table of this level and direction (FP64), or null
-    // x-parity-split copies of r and fl (level 1, y- and z-lines): cell i of a row sits at
-    // i / 2 (even i) or (sx + 1) / 2 + i / 2 (odd i), so the cells of one colour are contiguous
-    const T *rs = nullptr;
-    const uint8_t *fls = nullptr;
 };
-// x-parity split of a level-1 array (the layout of LineArgs::rs / fls)
-template <typename T>
-void launch_split_x(T *dst, const T *src, const Dims &d, cudaStream_t s);
 
 template <typename T>
 struct FactorArgs {   // line factorisation of the smoother's tridiagonal systems
