@@ -49,6 +49,8 @@ SOLVER_SYMBOLS = {
     "fsi_mg_face_vel_rhs": [ctypes.c_void_p, ctypes.c_int, ctypes.c_double] + [ctypes.c_void_p] * 11 + [c_double_p],
     "fsi_mg_correct_vel": [ctypes.c_void_p, ctypes.c_double] + [ctypes.c_void_p] * 10,
     "fsi_mg_update_pressure": [ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p],
+    "fsi_mg_set_bc": [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
+                      ctypes.c_void_p, c_double_p],
     "fsi_mg_rhs_advec_diff": [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_double, ctypes.c_void_p],
     "fsi_mg_rhs_adjust_bc": [ctypes.c_void_p, ctypes.c_int, ctypes.c_double, ctypes.c_void_p],
     "fsi_mg_solve_ad": [ctypes.c_void_p, ctypes.c_int, ctypes.c_double, ctypes.c_void_p, ctypes.c_void_p,

@@ -121,6 +121,7 @@ struct Ctx {
     int side_raw[6] = {1, 1, 1, 1, 1, 1};
     int sign[6] = {1, 1, 1, 1, 1, 1};
     double *d_dx[3] = {}, *d_dxinv[3] = {}, *d_dxcinv[3] = {};
+    double *d_xn[3] = {};   // node coordinates x(0:n+1) (shear boundary profiles)
     double *d_fx[3] = {};   // face interpolation weights fx(1:n) (IBM/CORE_GRID.F90:163-175)
     double *d_gx[3] = {};   // 1 - fx, as the reference forms it
     // diffusion coefficient tables of rhs_diff: dcinv(i) dinv(i), dcinv(i+1) dinv(i), (2 dinv(i)) dinv(i)
@@ -1133,6 +1134,8 @@ int fsi_mg_create(const fsi_mg_params *params, const double *x, const double *y,
         TRY(c->alloc(&c->d_dx[d], N[d] + 2));
         TRY(c->alloc(&c->d_dxinv[d], N[d] + 2));
         TRY(c->alloc(&c->d_dxcinv[d], N[d] + 2));
+        TRY(c->alloc(&c->d_xn[d], N[d] + 2));
+        CK(cudaMemcpyAsync(c->d_xn[d], c->x[d].data(), (N[d] + 2) * 8, cudaMemcpyHostToDevice, c->s));
         CK(cudaMemcpyAsync(c->d_dx[d], c->dx[d].data(), (N[d] + 2) * 8, cudaMemcpyHostToDevice, c->s));
         CK(cudaMemcpyAsync(c->d_dxinv[d], c->dxinv[d].data(), (N[d] + 2) * 8, cudaMemcpyHostToDevice, c->s));
         CK(cudaMemcpyAsync(c->d_dxcinv[d], c->dxcinv[d].data(), (N[d] + 2) * 8, cudaMemcpyHostToDevice, c->s));
@@ -1558,6 +1561,15 @@ static int step_ready(Ctx &c)
     return 0;
 }
 
+// one partial sum per CTA of the step reductions; worst case one CTA per
+// 32 x 8 tile and k of face_vel_rhs
+static int ensure_step_partials(Ctx &c)
+{
+    if (c.step_partials) return 0;
+    c.step_cap = ((c.nx - 1 + 31) / 32) * ((c.ny - 1 + 7) / 8) * (c.nz - 1);
+    return c.alloc(&c.step_partials, (size_t)c.step_cap);
+}
+
 static StepArgs step_args(Ctx &c, double dt)
 {
     StepArgs a{};
@@ -1600,10 +1612,7 @@ int fsi_mg_face_vel_rhs(void *handle, int frac_step_type, double dt, const doubl
     }
     a.nlu0 = d_nlu0;
     a.p = d_p;
-    if (!c.step_partials) {   // worst case: one CTA per 32 x 8 tile and k
-        c.step_cap = ((c.nx - 1 + 31) / 32) * ((c.ny - 1 + 7) / 8) * (c.nz - 1);
-        TRY(c.alloc(&c.step_partials, (size_t)c.step_cap));
-    }
+    TRY(ensure_step_partials(c));
     launch_face_vel_rhs(a, frac_step_type == 1, c.step_partials, c.step_cap, (double *)c.result, c.s);
     c.last_fv = a; c.last_fv_vk = (frac_step_type == 1); c.have_fv = true;
     c.launches += (frac_step_type == 1) ? 4 : 3;
@@ -1652,6 +1661,60 @@ int fsi_mg_correct_vel(void *handle, double dt, const double *d_pPrime, double *
     }
     CK(cudaStreamSynchronize(c.s));
     return rc;
+}
+
+int fsi_mg_set_bc(void *handle, const fsi_mg_bc_values *values, double *d_u, double *d_v, double *d_w,
+                  double *const d_bc[9], double *correction_vel)
+{
+    if (!handle || !values || !d_u || !d_v || !d_w || !d_bc) return fail(-1, "null argument");
+    for (int q = 0; q < 9; ++q)
+        if (!d_bc[q]) return fail(-1, "set_bc needs all nine boundary-value arrays");
+    Ctx &c = *(Ctx *)handle;
+    TRY(step_ready(c));
+    SetBcArgs a{};
+    bool zero_gradient = false;
+    const double pi = 4.0 * std::atan(1.0);   // IBM/MAIN.F90:264
+    for (int s = 0; s < 6; ++s) {
+        const int t = c.p.bc[s];
+        if (t == 6) return fail(-1, "user-specified (Blasius) velocity boundaries are not supported");
+        if (t != 1 && t != 2 && t != 3 && t != 4 && t != 7)
+            return fail(-1, "velocity boundary type must be 1, 2, 3, 4 or 7");
+        a.type[s] = t;
+        zero_gradient |= (t == BC_ZERO_GRADIENT);
+        for (int q = 0; q < 3; ++q) {
+            const double amp = values->vel[s][q];
+            double v = amp;
+            if (t == 3) {   // pulsatile inflow: amp sin(2 pi freq time); x2 u gust switch (IBM/CORE_SET_BC.F90:96-106)
+                const double arg = 2.0 * pi * values->freq[s][q] * values->time;
+                v = amp * std::sin(arg);
+                if (s == 1 && q == 0) v = (values->time > values->tstart_gust) ? amp * std::fabs(std::sin(arg)) : 0.0;
+            }
+            a.val[s][q] = v;
+        }
+    }
+    if (zero_gradient && !(c.p.outflow_area > 0.0)) return fail(-1, "outflow_area must be > 0 with zero-gradient BCs");
+    double *vel[3] = {d_u, d_v, d_w};
+    for (int d = 0; d < 3; ++d) { a.vel[d] = vel[d]; a.xn[d] = c.d_xn[d]; a.dx[d] = c.d_dx[d]; }
+    for (int q = 0; q < 9; ++q) a.bc[q] = d_bc[q];
+    a.fl = c.L1.fl;
+    a.d = c.L1.d;
+    a.xout = values->xout;
+    a.yout = values->yout;
+    a.outflow_area = c.p.outflow_area;
+    a.sums = (const double *)c.result;
+    launch_set_bc_planes(a, c.s);
+    c.launches++;
+    if (zero_gradient) {
+        TRY(ensure_step_partials(c));
+        launch_bc_massflux(a, c.step_partials, c.step_cap, (double *)c.result, c.s);
+        c.launches += 2;
+    }
+    for (int axis = 0; axis < 3; ++axis) launch_outer_ghost_vel(a, axis, zero_gradient, c.s);
+    c.launches += 3;
+    if (zero_gradient) CK(cudaMemcpyAsync(c.h_result, c.result, sizeof(double), cudaMemcpyDeviceToHost, c.s));
+    CK(cudaStreamSynchronize(c.s));
+    if (correction_vel) *correction_vel = zero_gradient ? -*(const double *)c.h_result / c.p.outflow_area : 0.0;
+    return 0;
 }
 
 int fsi_mg_rhs_advec_diff(void *handle, int advec_scheme, int frac_step_type, double dt,
@@ -1750,10 +1813,12 @@ int fsi_mg_solve_ad(void *handle, int advec_scheme, double dt, const fsi_mg_rhs_
     const bool gcm_vel = (c.p.boundary_formulation == GCM_METHOD) && c.vg_on && c.nGhost > 0;
     if ((three_d || gcm_vel) && !d_w) return fail(-1, "null w (3D, or ghost-cell velocities)");
     if (!fl->nlu || !fl->nlv || (three_d && !fl->nlw)) return fail(-1, "null nlu/nlv/nlw");
+    // the GCM branch's GCM_GhostCell_Vel re-balances zero-gradient outflow every
+    // iteration (GCM_enforce_global_mass_consv); the branch without a body has no such step
     for (int q = 0; q < 6; ++q)
-        if (c.p.bc[q] == BC_ZERO_GRADIENT)
-            return fail(-1, "zero-gradient velocity faces need the mass-flux correction of GCM_GhostCell_Vel, "
-                            "which is not supported");
+        if (c.p.bc[q] == BC_ZERO_GRADIENT && c.p.boundary_formulation == GCM_METHOD)
+            return fail(-1, "zero-gradient velocity faces with a GCM body need the mass-flux correction of "
+                            "GCM_GhostCell_Vel, which is not supported");
     const long long n = c.L1.d.sxy * (c.nz + 2);
     double *gam = c.ad_co + 7 * n;
     launch_ad_coef(a, c.s);

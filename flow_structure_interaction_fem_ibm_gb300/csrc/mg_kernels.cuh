@@ -110,6 +110,27 @@ void launch_face_vel_rhs(const StepArgs &a, bool van_kan, double *partials, int 
 // correct_vel cell-centre update and face corrections (IBM/CORE_FRAC_STEP_ROUTINES.F90:244-448,
 // without the ghost-cell velocity interpolation)
 void launch_correct_vel(const StepArgs &a, cudaStream_t s);
+// Outer boundary values (set_bc, IBM/CORE_SET_BC.F90:22-298), level-1 full-layout FP64.
+struct SetBcArgs {
+    double *vel[3];             // u, v, w (outer ghost layers written by the ghost phase)
+    double *bc[9];              // bcxu, bcyu, bczu, bcxv, ... (component-major: bc[3 comp + axis])
+    const double *xn[3];        // node coordinates x(0:n+1)
+    const uint8_t *fl;
+    const double *dx[3];
+    const double *sums;         // sums[0] = boundary mass flux (ghost phase, zero-gradient sides)
+    int type[6];                // bcx1 .. bcz2
+    double val[6][3];           // per side and component: the Dirichlet / pulsatile value or shear amplitude
+    double xout, yout, outflow_area;
+    Dims d;
+};
+// the boundary-value planes of all three axes
+void launch_set_bc_planes(const SetBcArgs &a, cudaStream_t s);
+// enforce_global_mass_consv's flux (IBM/CORE_SET_BC.F90:319-337) into sums[0]; partials holds cap doubles
+void launch_bc_massflux(const SetBcArgs &a, double *partials, int cap, double *sums, cudaStream_t s);
+// the zero-gradient corrections of axis `axis` (when mass_consv) followed by set_outer_ghost_vel's
+// update of that axis' ghost layers (IBM/CORE_SET_OUTER_GHOST.F90); axes run in the order x, y, z
+void launch_outer_ghost_vel(const SetBcArgs &a, int axis, bool mass_consv, cudaStream_t s);
+
 // Momentum right-hand side (rhs_advec_diff, IBM/CORE_RHS_AD.F90:13-585), level-1 full-layout FP64.
 struct RhsAdArgs {
     const double *vel[3];       // u, v, w

@@ -38,6 +38,13 @@ MODULE fsi_mg_gpu
     TYPE(C_PTR) :: nluOld, nlvOld, nlwOld, p, nlu, nlv, nlw
   END TYPE fsi_mg_rhs_ad_fields
 
+  ! fsi_mg_bc_values: vel(component u/v/w, side x1..z2) = ux1, vx1, wx1, ux2, ...;
+  ! freq likewise (pulsatile inflow)
+  TYPE, BIND(C) :: fsi_mg_bc_values
+    REAL(C_DOUBLE) :: vel(3,6), freq(3,6)
+    REAL(C_DOUBLE) :: time, tstart_gust, xout, yout
+  END TYPE fsi_mg_bc_values
+
   TYPE(C_PTR), SAVE :: fsi_mg_handle = C_NULL_PTR
   INTEGER, SAVE :: fsi_mg_precision = 0      ! 0 FP64, 1 mixed (set before MG_initial)
 
@@ -131,6 +138,14 @@ MODULE fsi_mg_gpu
       IMPORT :: C_INT, C_DOUBLE, C_PTR
       TYPE(C_PTR), VALUE :: h, coeffGCMD, uBI, vBI, wBI
       REAL(C_DOUBLE), VALUE :: bodyInterceptWeight, imagePointWeight
+    END FUNCTION
+    INTEGER(C_INT) FUNCTION fsi_mg_set_bc(h, values, u, v, w, bc, correction_vel) &
+        BIND(C, NAME='fsi_mg_set_bc')
+      IMPORT :: C_INT, C_DOUBLE, C_PTR, fsi_mg_bc_values
+      TYPE(C_PTR), VALUE :: h, u, v, w
+      TYPE(fsi_mg_bc_values), INTENT(IN) :: values
+      TYPE(C_PTR), INTENT(IN) :: bc(9)     ! bcxu, bcyu, bczu, bcxv, bcyv, bczv, bcxw, bcyw, bczw
+      REAL(C_DOUBLE), INTENT(OUT) :: correction_vel
     END FUNCTION
     INTEGER(C_INT) FUNCTION fsi_mg_update_pressure(h, frac_step_type, pPrime, p) &
         BIND(C, NAME='fsi_mg_update_pressure')

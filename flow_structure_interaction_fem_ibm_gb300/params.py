@@ -13,7 +13,8 @@ from dataclasses import dataclass, field
 
 # IBM/AMODULES.F90:14-118
 VISCOUS_FLOW, POTENTIAL_FLOW = 1, 2
-BC_TYPE_DIRICHLET, BC_TYPE_ZERO_GRADIENT, BC_TYPE_PERIODIC = 1, 2, 5
+BC_TYPE_DIRICHLET, BC_TYPE_ZERO_GRADIENT, BC_TYPE_PULSATILE_INFLOW, BC_TYPE_SYMMETRY = 1, 2, 3, 4
+BC_TYPE_PERIODIC, BC_TYPE_USER_SPECIFIED, BC_TYPE_SHEAR = 5, 6, 7
 PBC_DIRICHLET, PBC_NEUMANN = 1, 2
 PP_SOLVER_TYPE_LSOR, PP_SOLVER_TYPE_MG = 1, 3
 NO_INTERNAL_BOUNDARY, GCM_METHOD = 0, 2

@@ -45,6 +45,13 @@ class RhsAdFields(ctypes.Structure):
                 ("nlu", ctypes.c_void_p), ("nlv", ctypes.c_void_p), ("nlw", ctypes.c_void_p)]
 
 
+class BcValues(ctypes.Structure):
+    """fsi_mg_bc_values of include/fsi_mg.h."""
+    _fields_ = [("vel", (ctypes.c_double * 3) * 6), ("freq", (ctypes.c_double * 3) * 6),
+                ("time", ctypes.c_double), ("tstart_gust", ctypes.c_double),
+                ("xout", ctypes.c_double), ("yout", ctypes.c_double)]
+
+
 def _p(a, t=_dp):
     if a is None:
         return None
@@ -209,6 +216,27 @@ class PoissonSolver:
         _check(self.lib.fsi_mg_set_velocity_ghosts(self.h, _p(cd), _p(u), _p(v), _p(w), bw, iw))
         self._vg_keep = (cd, u, v, w)
         return self
+
+    def set_bc(self, d_vel, d_bc9, values, freq=None, time: float = 0.0, tstart_gust: float = 0.0,
+               xout: float = 1.0, yout: float = 1.0) -> float:
+        """set_bc (IBM/CORE_SET_BC.F90:22-298, outer sides) with
+        enforce_global_mass_consv and set_outer_ghost_vel on device arrays:
+        d_vel = (u, v, w) INOUT, d_bc9 the nine boundary-value arrays in the
+        order bcxu, bcyu, bczu, bcxv, ... (OUT on the planes); values / freq
+        6 x 3 (side x1..z2, component u, v, w).  Returns correction_vel."""
+        bv = BcValues()
+        val = np.asarray(values, dtype=np.float64).reshape(6, 3)
+        fr = np.zeros((6, 3)) if freq is None else np.asarray(freq, dtype=np.float64).reshape(6, 3)
+        for s in range(6):
+            for q in range(3):
+                bv.vel[s][q] = float(val[s, q])
+                bv.freq[s][q] = float(fr[s, q])
+        bv.time, bv.tstart_gust, bv.xout, bv.yout = float(time), float(tstart_gust), float(xout), float(yout)
+        bcs = (ctypes.c_void_p * 9)(*[ctypes.c_void_p(a) for a in d_bc9])
+        corr = ctypes.c_double()
+        _check(self.lib.fsi_mg_set_bc(self.h, ctypes.byref(bv), *(ctypes.c_void_p(a) for a in d_vel), bcs,
+                                      ctypes.byref(corr)))
+        return corr.value
 
     def update_pressure(self, d_pPrime: int, d_p: int, frac_step_type: int = 0):
         """update_pressure (IBM/CORE_FRAC_STEP_ROUTINES.F90:949-967) on device arrays."""

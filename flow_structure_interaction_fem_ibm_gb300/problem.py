@@ -24,7 +24,8 @@ import numpy as np
 
 from . import _native
 from .grid import Metrics, make_grid
-from .params import (BC_TYPE_DIRICHLET, DIM_2D, DIM_3D, GCM_METHOD, NO_INTERNAL_BOUNDARY, SolverParams)
+from .params import (BC_TYPE_DIRICHLET, BC_TYPE_ZERO_GRADIENT, DIM_2D, DIM_3D, GCM_METHOD, NO_INTERNAL_BOUNDARY,
+                     SolverParams)
 
 
 def full_shape(p: SolverParams):
@@ -231,6 +232,20 @@ def gaussian_field(p: SolverParams, x, y, z, rng, kmax: int = 8, lengths=(1.0, 1
     out = np.empty((ex.shape[0], ey.shape[0], ez.shape[0]), order="F")
     out[...] = np.einsum("ijc,kc->ijk", t2, ez).real
     return out / np.sqrt(max(mask.sum(), 1))
+
+
+def outflow_area(p: SolverParams, x, y, z, iblank) -> float:
+    """set_outflow_area (IBM/BOUNDARY_SET.F90:134-221): the fluid area of the
+    zero-gradient sides (the first / last cell layer of each side, cells with
+    iblank = 0), the value fsi_mg_params.outflow_area carries."""
+    mx, my, mz = Metrics(x), Metrics(y), Metrics(z)
+    nxc, nyc, nzc = p.nx - 1, p.ny - 1, p.nz - 1
+    dx, dy, dz = mx.dx[1:nxc + 1], my.dx[1:nyc + 1], mz.dx[1:nzc + 1]
+    fl = 1.0 - iblank[1:nxc + 1, 1:nyc + 1, 1:nzc + 1]
+    areas = [(dy[:, None] * dz[None, :] * fl[0]).sum(), (dy[:, None] * dz[None, :] * fl[-1]).sum(),
+             (dx[:, None] * dz[None, :] * fl[:, 0, :]).sum(), (dx[:, None] * dz[None, :] * fl[:, -1, :]).sum(),
+             (dx[:, None] * dy[None, :] * fl[:, :, 0]).sum(), (dx[:, None] * dy[None, :] * fl[:, :, -1]).sum()]
+    return float(sum(a for a, t in zip(areas, p.bc) if t == BC_TYPE_ZERO_GRADIENT))
 
 
 def default_params(ndim: int, nxc: int, nyc: int, nzc: int, body: bool, **kw) -> SolverParams:

@@ -179,6 +179,35 @@ typedef struct {
     double *nlu, *nlv, *nlw;            /* OUT (interior cells) */
 } fsi_mg_rhs_ad_fields;
 
+/* Outer boundary values of set_bc, per side x1, x2, y1, y2, z1, z2 and
+ * component u, v, w: vel = ux1, vx1, wx1, ux2, ... (IBM/AMODULES.F90
+ * flow_parameters), freq = freq_ux1, ... (pulsatile inflow), the simulation
+ * time, tstart_gust (gust switch of the x2 pulsatile u) and the domain
+ * lengths xout, yout (shear profiles).  Field order is part of the ABI. */
+typedef struct {
+    double vel[6][3];
+    double freq[6][3];
+    double time, tstart_gust;
+    double xout, yout;
+} fsi_mg_bc_values;
+
+/* set_bc, outer part (IBM/CORE_SET_BC.F90:22-298): the boundary values of
+ * the first and last cells of each axis (full planes j = 0..ny, k = 0..nz
+ * etc.) by the side types of fsi_mg_params.bc (1 Dirichlet, 2 zero gradient,
+ * 3 pulsatile, 4 symmetry, 7 shear; 6 user-specified needs the Blasius
+ * profile and is rejected), then with any zero-gradient side
+ * enforce_global_mass_consv (:304-377: the boundary mass flux over the
+ * face flags of the last fsi_mg_set_geometry, corrected by -massflux /
+ * outflow_area on the zero-gradient sides; iMarkm..kMarkp are zero outside
+ * SSM) and set_outer_ghost_vel (IBM/CORE_SET_OUTER_GHOST.F90:1-63: u, v, w of
+ * the outer ghost layers, INOUT).  bc = the nine arrays in the order of
+ * fsi_mg_rhs_ad_fields.bc (device, full layout, all required, OUT on the
+ * planes).  The body-intercept values of a GCM body
+ * (GCM_SetBodyInterceptValues) are fsi_mg_set_velocity_ghosts' inputs.
+ * correction_vel OUT (0 without zero-gradient sides; may be NULL). */
+int fsi_mg_set_bc(void *handle, const fsi_mg_bc_values *values, double *d_u, double *d_v, double *d_w,
+                  double *const d_bc[9], double *correction_vel);
+
 /* rhs_advec_diff (IBM/CORE_RHS_AD.F90:13-75): central advection with the face
  * velocities (rhs_advec without the hybrid upwinding, :80-382), the
  * Adams-Bashforth or Crank-Nicolson loading of the advection term
@@ -209,7 +238,8 @@ int fsi_mg_rhs_adjust_bc(void *handle, int advec_scheme, double dt, const fsi_mg
  * fsi_mg_set_velocity_ghosts, until max |calc_residual_ad| <= restol_ad or
  * iterMax_ad iterations (status 1, the reference prints and continues).
  * advec_scheme 1 (AB2) or 2 (CRANK_NICOLSON1); zero-gradient velocity faces
- * (whose mass-flux correction runs inside GCM_GhostCell_Vel) are rejected.
+ * with a GCM body (whose mass-flux correction runs inside GCM_GhostCell_Vel)
+ * are rejected.
  * iters and maxres OUT (may be NULL). */
 int fsi_mg_solve_ad(void *handle, int advec_scheme, double dt, const fsi_mg_rhs_ad_fields *fields, double *d_u,
                     double *d_v, double *d_w, int *iters, double *maxres);

@@ -1461,6 +1461,151 @@ void or_update_pressure(or_ctx *c, int frac_step_type, const double *pPrime, dou
     if (c->p.boundary_formulation == GCM_METHOD) gcm_p_set_bc_internal(c, p, c->nx + 1, c->ny + 1);
 }
 
+/* ------------------------------------------------------------------ set_bc -- */
+/* One side of set_bc's SELECT CASE (IBM/CORE_SET_BC.F90:56-280): side s
+ * (0 x1 .. 5 z2), uvw the cell's u, v, w, (i, j) its first two indices. */
+static void set_bc_side(or_ctx *c, int s, const double *vel3, const double *freq3, double time,
+                        double tstart_gust, double xout, double yout, const double *const *uvw, int i, int j,
+                        double *out)
+{
+    const double pi = 4.0 * atan(1.0);   /* IBM/MAIN.F90:264 */
+    const int a = s / 2;
+    switch (c->p.bc[s]) {
+    case BC_DIRICHLET:
+        for (int q = 0; q < 3; ++q) out[q] = vel3[q];
+        break;
+    case BC_ZERO_GRADIENT:
+        for (int q = 0; q < 3; ++q) out[q] = *uvw[q];
+        break;
+    case 3:   /* BC_TYPE_PULSATILE_INFLOW */
+        for (int q = 0; q < 3; ++q) out[q] = vel3[q] * sin(2.0 * pi * freq3[q] * time);
+        if (s == 1) {   /* :96-104, the x2 gust switch */
+            if (time > tstart_gust) out[0] = vel3[0] * fabs(sin(2.0 * pi * freq3[0] * time));
+            else out[0] = 0;
+        }
+        break;
+    case 4:   /* BC_TYPE_SYMMETRY: normal component zero */
+        for (int q = 0; q < 3; ++q) out[q] = (q == a) ? 0.0 : *uvw[q];
+        break;
+    case 7:   /* BC_TYPE_SHEAR */
+        for (int q = 0; q < 3; ++q) out[q] = vel3[q];
+        if (a == 1) out[1] = vel3[1] * c->x[0][i] / xout;
+        else out[a] = vel3[a] * c->x[1][j] / yout;
+        break;
+    }
+}
+
+/* set_bc without its internal-boundary calls (IBM/CORE_SET_BC.F90:22-298),
+ * enforce_global_mass_consv (:304-377; iMarkm..kMarkp are zero outside SSM,
+ * IBM/GCM_MEMORY_ALLOCATE.F90:68-69) and set_outer_ghost_vel
+ * (IBM/CORE_SET_OUTER_GHOST.F90:1-63).  val and freq hold 6 x 3 values (side
+ * x1..z2, component u, v, w); bc9 = bcxu,bcyu,bczu,bcxv,bcyv,bczv,bcxw,bcyw,bczw.
+ * Returns -1 for a side type it does not restate (user-specified), else 0;
+ * *correction = correction_vel (0 without zero-gradient sides). */
+int or_set_bc(or_ctx *c, const double *val, const double *freq, double time, double tstart_gust, double xout,
+              double yout, double *u, double *v, double *w, double *const *bc9, double *correction)
+{
+    for (int s = 0; s < 6; ++s) {
+        const int t = c->p.bc[s];
+        if (t != BC_DIRICHLET && t != BC_ZERO_GRADIENT && t != 3 && t != 4 && t != 7) return -1;
+    }
+    double *vel[3] = {u, v, w};
+    double out[3];
+    const int nx = c->nx, ny = c->ny, nz = c->nz;
+    /* x sides, :50-135 */
+    for (int k = 0; k <= nz; ++k)
+        for (int j = 0; j <= ny; ++j)
+            for (int side = 0; side < 2; ++side) {
+                const int i = side == 0 ? 1 : c->nxc;
+                const size_t f = FI(c, i, j, k);
+                const double *uvw[3] = {u + f, v + f, w + f};
+                set_bc_side(c, side, val + 3 * side, freq + 3 * side, time, tstart_gust, xout, yout, uvw, i, j, out);
+                for (int q = 0; q < 3; ++q) bc9[3 * q + 0][f] = out[q];
+            }
+    /* y sides, :137-221 */
+    for (int k = 0; k <= nz; ++k)
+        for (int i = 0; i <= nx; ++i)
+            for (int side = 0; side < 2; ++side) {
+                const int j = side == 0 ? 1 : c->nyc, s = 2 + side;
+                const size_t f = FI(c, i, j, k);
+                const double *uvw[3] = {u + f, v + f, w + f};
+                set_bc_side(c, s, val + 3 * s, freq + 3 * s, time, tstart_gust, xout, yout, uvw, i, j, out);
+                for (int q = 0; q < 3; ++q) bc9[3 * q + 1][f] = out[q];
+            }
+    /* z sides, :223-283 */
+    for (int j = 0; j <= ny; ++j)
+        for (int i = 0; i <= nx; ++i)
+            for (int side = 0; side < 2; ++side) {
+                const int k = side == 0 ? 1 : c->nzc, s = 4 + side;
+                const size_t f = FI(c, i, j, k);
+                const double *uvw[3] = {u + f, v + f, w + f};
+                set_bc_side(c, s, val + 3 * s, freq + 3 * s, time, tstart_gust, xout, yout, uvw, i, j, out);
+                for (int q = 0; q < 3; ++q) bc9[3 * q + 2][f] = out[q];
+            }
+    /* enforce_global_mass_consv */
+    int zg = 0;
+    for (int s = 0; s < 6; ++s) zg |= (c->p.bc[s] == BC_ZERO_GRADIENT);
+    double correction_vel = 0.0;
+    if (zg) {
+        const int8_t *ium = c->fl[0], *iup = c->fl[1], *jum = c->fl[2], *jup = c->fl[3], *kum = c->fl[4], *kup = c->fl[5];
+        double *bcxu = bc9[0], *bcyv = bc9[4], *bczw = bc9[8];
+        double massflux = 0.0;
+        for (int k = 1; k <= c->nzc; ++k)
+            for (int j = 1; j <= c->nyc; ++j)
+                for (int i = 1; i <= c->nxc; ++i) {
+                    const size_t f = FI(c, i, j, k);
+                    const double dx = c->dx[0][i], dy = c->dx[1][j], dz = c->dx[2][k];
+                    massflux = massflux + (-(bcxu[f] * ium[f] * dy * dz) + bcxu[f] * iup[f] * dy * dz
+                                           - bcyv[f] * jum[f] * dx * dz + bcyv[f] * jup[f] * dx * dz
+                                           - bczw[f] * kum[f] * dx * dy + bczw[f] * kup[f] * dx * dy)
+                                              * (double)(1 - c->iblank[f]);
+                }
+        correction_vel = -massflux / c->p.outflow_area;
+        for (int k = 0; k <= nz; ++k)
+            for (int j = 0; j <= ny; ++j) {
+                if (c->p.bc[0] == BC_ZERO_GRADIENT) bcxu[FI(c, 1, j, k)] = bcxu[FI(c, 1, j, k)] - correction_vel;
+                if (c->p.bc[1] == BC_ZERO_GRADIENT) bcxu[FI(c, c->nxc, j, k)] = bcxu[FI(c, c->nxc, j, k)] + correction_vel;
+            }
+        for (int k = 0; k <= nz; ++k)
+            for (int i = 0; i <= nx; ++i) {
+                if (c->p.bc[2] == BC_ZERO_GRADIENT) bcyv[FI(c, i, 1, k)] = bcyv[FI(c, i, 1, k)] - correction_vel;
+                if (c->p.bc[3] == BC_ZERO_GRADIENT) bcyv[FI(c, i, c->nyc, k)] = bcyv[FI(c, i, c->nyc, k)] + correction_vel;
+            }
+        for (int j = 0; j <= ny; ++j)
+            for (int i = 0; i <= nx; ++i) {
+                if (c->p.bc[4] == BC_ZERO_GRADIENT) bczw[FI(c, i, j, 1)] = bczw[FI(c, i, j, 1)] - correction_vel;
+                if (c->p.bc[5] == BC_ZERO_GRADIENT) bczw[FI(c, i, j, c->nzc)] = bczw[FI(c, i, j, c->nzc)] + correction_vel;
+            }
+    }
+    if (correction) *correction = correction_vel;
+    /* set_outer_ghost_vel */
+    for (int k = 0; k <= nz; ++k)
+        for (int j = 0; j <= ny; ++j)
+            for (int q = 0; q < 3; ++q) {
+                double *a = vel[q];
+                const double *b = bc9[3 * q + 0];
+                a[FI(c, 0, j, k)] = 2.0 * b[FI(c, 1, j, k)] - a[FI(c, 1, j, k)];
+                a[FI(c, nx, j, k)] = 2.0 * b[FI(c, nx - 1, j, k)] - a[FI(c, nx - 1, j, k)];
+            }
+    for (int k = 0; k <= nz; ++k)
+        for (int i = 0; i <= nx; ++i)
+            for (int q = 0; q < 3; ++q) {
+                double *a = vel[q];
+                const double *b = bc9[3 * q + 1];
+                a[FI(c, i, 0, k)] = 2.0 * b[FI(c, i, 1, k)] - a[FI(c, i, 1, k)];
+                a[FI(c, i, ny, k)] = 2.0 * b[FI(c, i, ny - 1, k)] - a[FI(c, i, ny - 1, k)];
+            }
+    for (int j = 0; j <= ny; ++j)
+        for (int i = 0; i <= nx; ++i)
+            for (int q = 0; q < 3; ++q) {
+                double *a = vel[q];
+                const double *b = bc9[3 * q + 2];
+                a[FI(c, i, j, 0)] = 2.0 * b[FI(c, i, j, 1)] - a[FI(c, i, j, 1)];
+                a[FI(c, i, j, nz)] = 2.0 * b[FI(c, i, j, nz - 1)] - a[FI(c, i, j, nz - 1)];
+            }
+    return 0;
+}
+
 /* ---------------------------------------------- momentum right-hand side ---- */
 /* rhs_advec_diff (IBM/CORE_RHS_AD.F90:13-75) with its contained routines
  * rhs_advec (:80-382, the non-hybrid branch), rhs_loadAB (:385-430), rhs_diff

@@ -93,6 +93,9 @@ void    or_correct_vel(or_ctx *c, double dt, const double *pPrime, double *u, do
                        const double *bcxu, const double *bcyv, const double *bczw,
                        double *face_u, double *face_v, double *face_w);
 void    or_update_pressure(or_ctx *c, int frac_step_type, const double *pPrime, double *p);
+/* set_bc (outer sides), enforce_global_mass_consv, set_outer_ghost_vel; val/freq 6 x 3 (side, component) */
+int     or_set_bc(or_ctx *c, const double *val, const double *freq, double time, double tstart_gust, double xout,
+                  double yout, double *u, double *v, double *w, double *const *bc9, double *correction);
 void    or_set_vel_ghosts(or_ctx *c, const double *coeffD, const double *uBI, const double *vBI,
                           const double *wBI, double bodyInterceptWeight, double imagePointWeight);
 int     or_vel_ghost_iters(or_ctx *c);

@@ -87,6 +87,9 @@ def lib():
         L.or_correct_vel.restype = None
         L.or_update_pressure.argtypes = [ctypes.c_void_p, ctypes.c_int, _dp, _dp]
         L.or_update_pressure.restype = None
+        L.or_set_bc.argtypes = ([ctypes.c_void_p, _dp, _dp] + [ctypes.c_double] * 4 + [_dp] * 3
+                                + [ctypes.POINTER(_dp), _dp])
+        L.or_set_bc.restype = ctypes.c_int
         L.or_set_vel_ghosts.argtypes = [ctypes.c_void_p] + [_dp] * 4 + [ctypes.c_double] * 2
         L.or_set_vel_ghosts.restype = None
         L.or_vel_ghost_iters.argtypes = [ctypes.c_void_p]
@@ -250,6 +253,19 @@ class Oracle:
         it = lib().or_solve_ad(self.h, advec_scheme, dt, (_dp * 3)(*[_p(a) for a in faces]), *(_p(a) for a in vel),
                                *(_p(a) for a in nl), order, ctypes.byref(mr))
         return it, mr.value
+
+    def set_bc(self, vel, bc9, values, freq=None, time=0.0, tstart_gust=0.0, xout=1.0, yout=1.0):
+        """set_bc (outer sides), enforce_global_mass_consv and set_outer_ghost_vel;
+        vel = (u, v, w) and the nine bc arrays updated in place; values and freq
+        are 6 x 3 (side x1..z2, component u, v, w).  Returns correction_vel."""
+        val = np.ascontiguousarray(values, dtype=np.float64).reshape(18)
+        fr = np.zeros(18) if freq is None else np.ascontiguousarray(freq, dtype=np.float64).reshape(18)
+        corr = ctypes.c_double()
+        rc = lib().or_set_bc(self.h, _p(val), _p(fr), time, tstart_gust, xout, yout, *(_p(a) for a in vel),
+                             (_dp * 9)(*[_p(a) for a in bc9]), ctypes.byref(corr))
+        if rc != 0:
+            raise ValueError("set_bc: unsupported boundary type")
+        return corr.value
 
     def update_pressure(self, pPrime, p, frac_step_type=0):
         lib().or_update_pressure(self.h, frac_step_type, _p(pPrime), _p(p))

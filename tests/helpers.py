@@ -187,3 +187,44 @@ def step_fields(problem, seed, with_bc=True):
     if problem.params.ndim == 2:
         f["w"][...] = 0.0
     return f
+
+
+SET_BC_TYPES = {
+    # velocity BC types x1, x2, y1, y2, z1, z2 (1 Dirichlet, 2 zero gradient,
+    # 3 pulsatile, 4 symmetry, 7 shear)
+    "dirichlet": (1, 1, 1, 1, 1, 1),
+    "channel": (1, 2, 4, 4, 4, 4),
+    "mixed": (3, 2, 7, 4, 2, 7),
+    "shear_x": (7, 2, 4, 4, 4, 4),
+    "gust_on": (1, 3, 1, 1, 1, 1),
+    "gust_off": (1, 3, 1, 1, 1, 1),
+    "unpaired_zg": (2, 2, 1, 1, 1, 1),
+    "sphere_channel": (1, 2, 4, 4, 4, 4),
+    "box2d_channel": (1, 2, 4, 4, 4, 4),
+}
+
+
+def set_bc_case(name, seed=17):
+    """A problem with the velocity BC types of SET_BC_TYPES[name] (outflow_area
+    from set_outflow_area) and seeded inputs of set_bc: cell velocities, prior
+    contents of the nine bc arrays, side values and frequencies, time."""
+    import numpy as np
+    from flow_structure_interaction_fem_ibm_gb300 import problem as P
+    if name == "unpaired_zg":
+        pr = unpaired_flags_problem()
+    elif name == "sphere_channel":
+        pr = sphere_problem(16, stretch=1.5)
+    elif name == "box2d_channel":
+        pr = P.box2d(24, seed=9)
+    else:
+        pr = baffle_problem(cells=(10, 12, 9))
+    p = pr.params
+    p.bc = SET_BC_TYPES[name]
+    p.outflow_area = P.outflow_area(p, pr.x, pr.y, pr.z, pr.geom.iblank) if 2 in p.bc else 1.0
+    rng = np.random.Generator(np.random.PCG64(seed))
+    sh = pr.shape
+    r = lambda: np.asfortranarray(rng.standard_normal(sh))
+    f = dict(vel=[r(), r(), r()], bc9=[r() for _ in range(9)], val=rng.standard_normal((6, 3)),
+             freq=rng.uniform(0.5, 3.0, (6, 3)), time=0.37, tstart_gust=0.5 if name == "gust_off" else 0.2,
+             xout=float(pr.x[p.nx] - pr.x[1]), yout=float(pr.y[p.ny] - pr.y[1]))
+    return pr, f
