@@ -129,6 +129,7 @@ struct Ctx {
     double *step_partials = nullptr;   // one partial sum per CTA of face_vel_rhs
     int step_cap = 0;
     double *vtilde = nullptr;   // uTilde, vTilde, wTilde of the VAN_KAN face_vel (allocated on first use)
+    double *zg_div = nullptr;   // divergence scratch of the face_vel inside solve_ad (zero-gradient sides, GCM)
     bool coarsest_fp32 = true;   // mixed form: the coarsest level is smoothed in FP32 like the others
     double ghost32_reltol = 1.0e-6;   // FP32 ghost rows stop at max|dp| <= this x max|p_g| (FSI_MG_GHOST32_RELTOL)
     // ghost-cell velocities (GCM_vel_set_bc_internal), registered by fsi_mg_set_velocity_ghosts
@@ -1815,11 +1816,39 @@ int fsi_mg_solve_ad(void *handle, int advec_scheme, double dt, const fsi_mg_rhs_
     if (!fl->nlu || !fl->nlv || (three_d && !fl->nlw)) return fail(-1, "null nlu/nlv/nlw");
     // the GCM branch's GCM_GhostCell_Vel re-balances zero-gradient outflow every
     // iteration (GCM_enforce_global_mass_consv); the branch without a body has no such step
-    for (int q = 0; q < 6; ++q)
-        if (c.p.bc[q] == BC_ZERO_GRADIENT && c.p.boundary_formulation == GCM_METHOD)
-            return fail(-1, "zero-gradient velocity faces with a GCM body need the mass-flux correction of "
-                            "GCM_GhostCell_Vel, which is not supported");
+    bool zero_gradient = false;
+    for (int q = 0; q < 6; ++q) zero_gradient |= (c.p.bc[q] == BC_ZERO_GRADIENT);
+    const bool mass_consv = zero_gradient && c.p.boundary_formulation == GCM_METHOD;
     const long long n = c.L1.d.sxy * (c.nz + 2);
+    StepArgs fv{};
+    ZgArgs zg{};
+    if (mass_consv) {
+        for (int q = 0; q < 9; ++q)
+            if (!fl->bc[q]) return fail(-1, "solve_ad with zero-gradient sides and a GCM body needs all nine bc arrays");
+        if (fl->p) return fail(-1, "solve_ad with zero-gradient sides and a GCM body re-evaluates face_vel, "
+                                   "which is restated for NO_VAN_KAN only (fields.p must be NULL)");
+        if (!d_w) return fail(-1, "null w");
+        if (!(c.p.outflow_area > 0.0)) return fail(-1, "outflow_area must be > 0 with zero-gradient BCs");
+        if (!c.zg_div) TRY(c.alloc(&c.zg_div, (size_t)n));
+        TRY(ensure_step_partials(c));
+        // face_vel into the step's faces; with dt = 1 the divergence sum is the net face flux
+        fv = step_args(c, 1.0);
+        const double *vl[3] = {d_u, d_v, d_w};
+        double *fc[3] = {const_cast<double *>(fl->face_u), const_cast<double *>(fl->face_v),
+                         const_cast<double *>(fl->face_w)};
+        for (int d = 0; d < 3; ++d) { fv.vel[d] = vl[d]; fv.bc[d] = fl->bc[4 * d]; fv.face[d] = fc[d]; }
+        fv.nlu0 = c.zg_div;
+        zg.nl[0] = fl->nlu; zg.nl[1] = fl->nlv; zg.nl[2] = fl->nlw;   // nlw may be NULL in 2D
+        for (int q = 0; q < 9; ++q) zg.bc[q] = const_cast<double *>(fl->bc[q]);
+        zg.fl = c.L1.fl;
+        for (int d = 0; d < 3; ++d) { zg.cm[d] = c.d_adm[d]; zg.cp[d] = c.d_adp[d]; zg.cb[d] = c.d_adb[d]; }
+        zg.sums = (const double *)c.result;
+        for (int q = 0; q < 6; ++q) zg.type[q] = c.p.bc[q];
+        zg.hdr = 0.50 * dt * fl->reinv;
+        zg.outflow_area = c.p.outflow_area;
+        zg.three_d = three_d ? 1 : 0;
+        zg.d = c.L1.d;
+    }
     double *gam = c.ad_co + 7 * n;
     launch_ad_coef(a, c.s);
     c.launches++;
@@ -1855,6 +1884,16 @@ int fsi_mg_solve_ad(void *handle, int advec_scheme, double dt, const fsi_mg_rhs_
             launch_vel_ghosts(d_u, d_v, d_w, g, c.vg_coeff, c.vg_bi_set ? c.vg_bi : nullptr,
                               c.vg_bw, c.vg_iw, c.vg_scr, c.p.iterMax_ad, c.p.restol_ad, c.d_iters, c.d_maxd, c.s);
             c.launches++;
+        }
+        if (mass_consv) {   // GCM_enforce_global_mass_consv
+            launch_face_vel_rhs(fv, false, c.step_partials, c.step_cap, (double *)c.result, c.s);
+            launch_zg_rhs_terms(zg, c.s);
+            launch_zg_planes(zg, c.s);
+            c.launches += 5;
+            if (advec_scheme == 2) {   // the Crank-Nicolson terms of the rows follow the new faces
+                launch_ad_coef(a, c.s);
+                c.launches++;
+            }
         }
         TRY(residual(mr));
         ++it;

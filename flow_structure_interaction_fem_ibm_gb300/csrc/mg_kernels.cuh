@@ -131,6 +131,25 @@ void launch_bc_massflux(const SetBcArgs &a, double *partials, int cap, double *s
 // update of that axis' ghost layers (IBM/CORE_SET_OUTER_GHOST.F90); axes run in the order x, y, z
 void launch_outer_ghost_vel(const SetBcArgs &a, int axis, bool mass_consv, cudaStream_t s);
 
+// GCM_enforce_global_mass_consv's right-hand-side and boundary-value update
+// (IBM/GCM_GLOBAL_MASS_CONSERVE.F90:52-84) after the face flux sum is in sums[0].
+struct ZgArgs {
+    double *nl[3];              // nlu, nlv, nlw
+    double *bc[9];              // as SetBcArgs::bc
+    const uint8_t *fl;
+    const double *cm[3], *cp[3], *cb[3];   // dcinv(i) dinv(i), dcinv(i+1) dinv(i), (2 dinv(i)) dinv(i)
+    const double *sums;
+    int type[6];
+    double hdr;                 // 0.5 dt reinv
+    double outflow_area;
+    int three_d;
+    Dims d;
+};
+// remove_rhs_adjust_bc with the current boundary values, then rhs_readjust_bc with the corrected ones
+void launch_zg_rhs_terms(const ZgArgs &a, cudaStream_t s);
+// the zero-gradient corrections of the normal components on the whole planes
+void launch_zg_planes(const ZgArgs &a, cudaStream_t s);
+
 // Momentum right-hand side (rhs_advec_diff, IBM/CORE_RHS_AD.F90:13-585), level-1 full-layout FP64.
 struct RhsAdArgs {
     const double *vel[3];       // u, v, w

@@ -340,6 +340,95 @@ __global__ void __launch_bounds__(TPB) k_outer_ghost_vel(SetBcArgs A, int mass_c
     }
 }
 
+// remove_rhs_adjust_bc then rhs_readjust_bc (IBM/GCM_GLOBAL_MASS_CONSERVE.F90:90-252)
+// for one interior cell: nl += sum a_f bc_f over its flagged faces with the
+// current boundary values, then nl -= the same sum with the corrected values
+// (the zero-gradient normal components of this cell, minus side then plus
+// side, as the plane corrections form them).  a_f is the implicit diffusion
+// coefficient with the constant reinv, -(0.5 dt reinv) x (dcinv dinv, or
+// 2 dinv dinv on a flagged face), the z pair times (ndim - 2).  Cells without
+// flagged faces add exact zeros and are skipped.
+__global__ void __launch_bounds__(TPB) k_zg_rhs_terms(ZgArgs A)
+{
+    const Dims &d = A.d;
+    const unsigned n0 = d.m[0] - 1, n1 = d.m[1] - 1, n2 = d.m[2] - 1;
+    const unsigned t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= n0 * n1 * n2) return;
+    int ix[3];
+    cell_of(t, n0, n1, ix[0], ix[1], ix[2]);
+    const long long o = d.idx(ix[0], ix[1], ix[2]);
+    const uint8_t f = A.fl[o];
+    if (!(f & 0xFC)) return;
+    const double corr = -A.sums[0] / A.outflow_area;
+    double am[3], ap[3];
+    for (int a = 0; a < 3; ++a) {
+        const int i = ix[a];
+        am[a] = (f & fb_minus(a)) ? A.cb[a][i] : A.cm[a][i];
+        ap[a] = (f & fb_plus(a)) ? A.cb[a][i] : A.cp[a][i];
+        am[a] = -A.hdr * am[a];
+        ap[a] = -A.hdr * ap[a];
+    }
+    const double rnDim = A.three_d ? 1.0 : 0.0;
+    am[2] = am[2] * rnDim;
+    ap[2] = ap[2] * rnDim;
+    const int ncells[3] = {(int)n0, (int)n1, (int)n2};
+    for (int q = 0; q < 3; ++q) {
+        if (!A.nl[q]) continue;   // nlw of a 2D run may be absent
+        double b_old[3], b_new[3];
+        for (int a = 0; a < 3; ++a) {
+            b_old[a] = A.bc[3 * q + a][o];
+            double b = b_old[a];
+            if (q == a) {   // bcxu, bcyv, bczw: the zero-gradient corrections of this cell
+                if (ix[a] == 1 && A.type[2 * a] == BCT_ZERO_GRADIENT) b = b - corr;
+                if (ix[a] == ncells[a] && A.type[2 * a + 1] == BCT_ZERO_GRADIENT) b = b + corr;
+            }
+            b_new[a] = b;
+        }
+        double r = A.nl[q][o];
+        for (int a = 0; a < 3; ++a) {
+            if (f & fb_minus(a)) r = r + am[a] * b_old[a];
+            if (f & fb_plus(a)) r = r + ap[a] * b_old[a];
+        }
+        for (int a = 0; a < 3; ++a) {
+            if (f & fb_minus(a)) r = r - am[a] * b_new[a];
+            if (f & fb_plus(a)) r = r - ap[a] * b_new[a];
+        }
+        A.nl[q][o] = r;
+    }
+}
+
+// the plane corrections of GCM_enforce_global_mass_consv (IBM/GCM_GLOBAL_MASS_CONSERVE.F90:60-79):
+// one thread per plane point of all three axes, minus side then plus side
+__global__ void __launch_bounds__(TPB) k_zg_planes(ZgArgs A)
+{
+    const Dims &d = A.d;
+    const long long P[3] = {(long long)(d.m[1] + 1) * (d.m[2] + 1), (long long)(d.m[0] + 1) * (d.m[2] + 1),
+                            (long long)(d.m[0] + 1) * (d.m[1] + 1)};
+    long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    int a = 0;
+    while (a < 3 && t >= P[a]) t -= P[a++];
+    if (a == 3) return;
+    const bool lo = A.type[2 * a] == BCT_ZERO_GRADIENT, hi = A.type[2 * a + 1] == BCT_ZERO_GRADIENT;
+    if (!lo && !hi) return;
+    int b, c;
+    plane_axes(a, b, c);
+    int ix[3];
+    ix[b] = (int)(t % (d.m[b] + 1));
+    ix[c] = (int)(t / (d.m[b] + 1));
+    const double corr = -A.sums[0] / A.outflow_area;
+    double *bn = A.bc[4 * a];
+    if (lo) {
+        ix[a] = 1;
+        const long long o = d.idx(ix[0], ix[1], ix[2]);
+        bn[o] = bn[o] - corr;
+    }
+    if (hi) {
+        ix[a] = d.m[a] - 1;
+        const long long o = d.idx(ix[0], ix[1], ix[2]);
+        bn[o] = bn[o] + corr;
+    }
+}
+
 // ---------------------------------------------------------------------------
 // Momentum right-hand side, rhs_advec_diff (IBM/CORE_RHS_AD.F90:13-75) with
 // rhs_advec (:80-382, non-hybrid), rhs_loadAB (:385-430), rhs_diff (:433-530)
@@ -721,5 +810,17 @@ void launch_outer_ghost_vel(const SetBcArgs &a, int axis, bool mass_consv, cudaS
     if (axis == 0) k_outer_ghost_vel<0><<<nb, TPB, 0, s>>>(a, mass_consv ? 1 : 0);
     else if (axis == 1) k_outer_ghost_vel<1><<<nb, TPB, 0, s>>>(a, mass_consv ? 1 : 0);
     else k_outer_ghost_vel<2><<<nb, TPB, 0, s>>>(a, mass_consv ? 1 : 0);
+}
+
+void launch_zg_rhs_terms(const ZgArgs &a, cudaStream_t s)
+{
+    const long long n = (long long)(a.d.m[0] - 1) * (a.d.m[1] - 1) * (a.d.m[2] - 1);
+    k_zg_rhs_terms<<<nblk(n), TPB, 0, s>>>(a);
+}
+
+void launch_zg_planes(const ZgArgs &a, cudaStream_t s)
+{
+    const long long m0 = a.d.m[0] + 1, m1 = a.d.m[1] + 1, m2 = a.d.m[2] + 1;
+    k_zg_planes<<<nblk(m1 * m2 + m0 * m2 + m0 * m1), TPB, 0, s>>>(a);
 }
 } // namespace fsimg

@@ -36,6 +36,7 @@ MODULE fsi_mg_gpu
     TYPE(C_PTR) :: bc(9)                 ! bcxu, bcyu, bczu, bcxv, bcyv, bczv, bcxw, bcyw, bczw
     TYPE(C_PTR) :: viscTot, bcvisc(3), exp_weight
     TYPE(C_PTR) :: nluOld, nlvOld, nlwOld, p, nlu, nlv, nlw
+    REAL(C_DOUBLE) :: reinv              ! 1/Re (solve_ad with zero-gradient sides and a GCM body)
   END TYPE fsi_mg_rhs_ad_fields
 
   ! fsi_mg_bc_values: vel(component u/v/w, side x1..z2) = ux1, vx1, wx1, ux2, ...;

@@ -42,7 +42,8 @@ class RhsAdFields(ctypes.Structure):
                 ("exp_weight", ctypes.c_void_p),
                 ("nluOld", ctypes.c_void_p), ("nlvOld", ctypes.c_void_p), ("nlwOld", ctypes.c_void_p),
                 ("p", ctypes.c_void_p),
-                ("nlu", ctypes.c_void_p), ("nlv", ctypes.c_void_p), ("nlw", ctypes.c_void_p)]
+                ("nlu", ctypes.c_void_p), ("nlv", ctypes.c_void_p), ("nlw", ctypes.c_void_p),
+                ("reinv", ctypes.c_double)]
 
 
 class BcValues(ctypes.Structure):
@@ -179,8 +180,9 @@ class PoissonSolver:
         _check(self.lib.fsi_mg_rhs_advec_diff(self.h, advec_scheme, frac_step_type, float(dt), ctypes.byref(f)))
 
     @staticmethod
-    def _ad_fields(faces, visc, nl, bc=(None,) * 9, bcvisc=(None,) * 3):
+    def _ad_fields(faces, visc, nl, bc=(None,) * 9, bcvisc=(None,) * 3, reinv=0.0):
         f = RhsAdFields()
+        f.reinv = float(reinv)
         f.face_u, f.face_v, f.face_w = faces
         for q in range(9):
             f.bc[q] = bc[q]
@@ -195,10 +197,14 @@ class PoissonSolver:
         f = self._ad_fields(faces, visc, nl, bc, bcvisc)
         _check(self.lib.fsi_mg_rhs_adjust_bc(self.h, advec_scheme, float(dt), ctypes.byref(f)))
 
-    def solve_ad(self, dt: float, faces, visc, vel, nl, bcvisc=(None,) * 3, advec_scheme: int = 2):
+    def solve_ad(self, dt: float, faces, visc, vel, nl, bcvisc=(None,) * 3, advec_scheme: int = 2,
+                 bc=(None,) * 9, reinv: float = 0.0):
         """solve_ad (IBM/CORE_SOLVE_AD.F90:12-267) on device pointers: vel =
-        (u, v, w) INOUT, nl the right-hand sides.  Returns (status, iterations, maxres)."""
-        f = self._ad_fields(faces, visc, nl, bcvisc=bcvisc)
+        (u, v, w) INOUT, nl the right-hand sides.  With zero-gradient sides and
+        a GCM body the faces, the zero-gradient planes of bc (all nine arrays)
+        and nl are INOUT too (GCM_enforce_global_mass_consv with 1/Re = reinv).
+        Returns (status, iterations, maxres)."""
+        f = self._ad_fields(faces, visc, nl, bc=bc, bcvisc=bcvisc, reinv=reinv)
         it, mr = ctypes.c_int(), ctypes.c_double()
         st = _check(self.lib.fsi_mg_solve_ad(self.h, advec_scheme, float(dt), ctypes.byref(f),
                                              *(ctypes.c_void_p(a) if a else None for a in vel), ctypes.byref(it),

@@ -177,6 +177,8 @@ typedef struct {
     double *nluOld, *nlvOld, *nlwOld;   /* INOUT with ADAMS_BASHFORTH2 */
     const double *p;                    /* frac_step_type 1 (VAN_KAN) only */
     double *nlu, *nlv, *nlw;            /* OUT (interior cells) */
+    double reinv;                       /* 1/Re: the boundary terms of GCM_enforce_global_mass_consv (solve_ad
+                                           with zero-gradient sides and a GCM body) */
 } fsi_mg_rhs_ad_fields;
 
 /* Outer boundary values of set_bc, per side x1, x2, y1, y2, z1, z2 and
@@ -237,9 +239,13 @@ int fsi_mg_rhs_adjust_bc(void *handle, int advec_scheme, double dt, const fsi_mg
  * solution), then under GCM the ghost-cell velocities of
  * fsi_mg_set_velocity_ghosts, until max |calc_residual_ad| <= restol_ad or
  * iterMax_ad iterations (status 1, the reference prints and continues).
- * advec_scheme 1 (AB2) or 2 (CRANK_NICOLSON1); zero-gradient velocity faces
- * with a GCM body (whose mass-flux correction runs inside GCM_GhostCell_Vel)
- * are rejected.
+ * advec_scheme 1 (AB2) or 2 (CRANK_NICOLSON1).  With zero-gradient sides and
+ * a GCM body every iteration ends with GCM_enforce_global_mass_consv
+ * (IBM/GCM_GLOBAL_MASS_CONSERVE.F90:6-252): face_vel of the current velocities
+ * (NO_VAN_KAN; fields.p must be NULL) into fields.face_u..face_w, the net face
+ * flux, the boundary terms with reinv removed from nlu..nlw, the zero-gradient
+ * planes of fields.bc corrected by -massflux / outflow_area and the terms put
+ * back; these fields are then INOUT and all nine bc arrays are required.
  * iters and maxres OUT (may be NULL). */
 int fsi_mg_solve_ad(void *handle, int advec_scheme, double dt, const fsi_mg_rhs_ad_fields *fields, double *d_u,
                     double *d_v, double *d_w, int *iters, double *maxres);

@@ -1495,6 +1495,31 @@ static void set_bc_side(or_ctx *c, int s, const double *vel3, const double *freq
     }
 }
 
+/* The zero-gradient corrections of enforce_global_mass_consv
+ * (IBM/CORE_SET_BC.F90:352-371) and GCM_enforce_global_mass_consv
+ * (IBM/GCM_GLOBAL_MASS_CONSERVE.F90:60-79): the normal component on the
+ * whole plane of each zero-gradient side, minus side - corr, plus side + corr. */
+static void zg_correct_planes(or_ctx *c, double *const *bc9, double correction_vel)
+{
+    const int nx = c->nx, ny = c->ny, nz = c->nz;
+    double *bcxu = bc9[0], *bcyv = bc9[4], *bczw = bc9[8];
+    for (int k = 0; k <= nz; ++k)
+        for (int j = 0; j <= ny; ++j) {
+            if (c->p.bc[0] == BC_ZERO_GRADIENT) bcxu[FI(c, 1, j, k)] = bcxu[FI(c, 1, j, k)] - correction_vel;
+            if (c->p.bc[1] == BC_ZERO_GRADIENT) bcxu[FI(c, c->nxc, j, k)] = bcxu[FI(c, c->nxc, j, k)] + correction_vel;
+        }
+    for (int k = 0; k <= nz; ++k)
+        for (int i = 0; i <= nx; ++i) {
+            if (c->p.bc[2] == BC_ZERO_GRADIENT) bcyv[FI(c, i, 1, k)] = bcyv[FI(c, i, 1, k)] - correction_vel;
+            if (c->p.bc[3] == BC_ZERO_GRADIENT) bcyv[FI(c, i, c->nyc, k)] = bcyv[FI(c, i, c->nyc, k)] + correction_vel;
+        }
+    for (int j = 0; j <= ny; ++j)
+        for (int i = 0; i <= nx; ++i) {
+            if (c->p.bc[4] == BC_ZERO_GRADIENT) bczw[FI(c, i, j, 1)] = bczw[FI(c, i, j, 1)] - correction_vel;
+            if (c->p.bc[5] == BC_ZERO_GRADIENT) bczw[FI(c, i, j, c->nzc)] = bczw[FI(c, i, j, c->nzc)] + correction_vel;
+        }
+}
+
 /* set_bc without its internal-boundary calls (IBM/CORE_SET_BC.F90:22-298),
  * enforce_global_mass_consv (:304-377; iMarkm..kMarkp are zero outside SSM,
  * IBM/GCM_MEMORY_ALLOCATE.F90:68-69) and set_outer_ghost_vel
@@ -1561,21 +1586,7 @@ int or_set_bc(or_ctx *c, const double *val, const double *freq, double time, dou
                                               * (double)(1 - c->iblank[f]);
                 }
         correction_vel = -massflux / c->p.outflow_area;
-        for (int k = 0; k <= nz; ++k)
-            for (int j = 0; j <= ny; ++j) {
-                if (c->p.bc[0] == BC_ZERO_GRADIENT) bcxu[FI(c, 1, j, k)] = bcxu[FI(c, 1, j, k)] - correction_vel;
-                if (c->p.bc[1] == BC_ZERO_GRADIENT) bcxu[FI(c, c->nxc, j, k)] = bcxu[FI(c, c->nxc, j, k)] + correction_vel;
-            }
-        for (int k = 0; k <= nz; ++k)
-            for (int i = 0; i <= nx; ++i) {
-                if (c->p.bc[2] == BC_ZERO_GRADIENT) bcyv[FI(c, i, 1, k)] = bcyv[FI(c, i, 1, k)] - correction_vel;
-                if (c->p.bc[3] == BC_ZERO_GRADIENT) bcyv[FI(c, i, c->nyc, k)] = bcyv[FI(c, i, c->nyc, k)] + correction_vel;
-            }
-        for (int j = 0; j <= ny; ++j)
-            for (int i = 0; i <= nx; ++i) {
-                if (c->p.bc[4] == BC_ZERO_GRADIENT) bczw[FI(c, i, j, 1)] = bczw[FI(c, i, j, 1)] - correction_vel;
-                if (c->p.bc[5] == BC_ZERO_GRADIENT) bczw[FI(c, i, j, c->nzc)] = bczw[FI(c, i, j, c->nzc)] + correction_vel;
-            }
+        zg_correct_planes(c, bc9, correction_vel);
     }
     if (correction) *correction = correction_vel;
     /* set_outer_ghost_vel */
@@ -1929,9 +1940,79 @@ static double calc_residual_ad(or_ctx *c, double half_dt, const double *const *f
  * largest residual is <= restol_ad or iterMax_ad iterations.  order: 0 the
  * reference's lexicographic line order, 1 red-black.  Returns the iteration
  * count; *maxres receives the final residual. */
-int or_solve_ad(or_ctx *c, int advec_scheme, double dt, const double *const *faces, double *u, double *v, double *w,
-                const double *nlu, const double *nlv, const double *nlw, int order, double *maxres)
+/* remove_rhs_adjust_bc (sign +1) and rhs_readjust_bc (sign -1),
+ * IBM/GCM_GLOBAL_MASS_CONSERVE.F90:90-252: the implicit diffusion coefficients
+ * with the constant reinv (not viscTot, no convective part) times the boundary
+ * values of flagged faces, added to or taken from nlu, nlv, nlw. */
+static void rhs_bc_terms(or_ctx *c, double dt, double reinv, double *const *bc9, double *const *nl, int sign)
 {
+    const double rnDim = (double)(c->p.ndim - DIM_2D);
+    const int8_t *ium = c->fl[0], *iup = c->fl[1], *jum = c->fl[2], *jup = c->fl[3], *kum = c->fl[4], *kup = c->fl[5];
+    for (int k = 1; k <= c->nzc; ++k)
+        for (int j = 1; j <= c->nyc; ++j)
+            for (int i = 1; i <= c->nxc; ++i) {
+                const size_t f = FI(c, i, j, k);
+                double amxd = (c->dxcinv[0][i] * (1 - ium[f]) + c->dxinv[0][i] * ium[f] * 2.0) * c->dxinv[0][i];
+                double apxd = (c->dxcinv[0][i + 1] * (1 - iup[f]) + c->dxinv[0][i] * iup[f] * 2.0) * c->dxinv[0][i];
+                double amyd = (c->dxcinv[1][j] * (1 - jum[f]) + c->dxinv[1][j] * jum[f] * 2.0) * c->dxinv[1][j];
+                double apyd = (c->dxcinv[1][j + 1] * (1 - jup[f]) + c->dxinv[1][j] * jup[f] * 2.0) * c->dxinv[1][j];
+                double amzd = (c->dxcinv[2][k] * (1 - kum[f]) + c->dxinv[2][k] * kum[f] * 2.0) * c->dxinv[2][k];
+                double apzd = (c->dxcinv[2][k + 1] * (1 - kup[f]) + c->dxinv[2][k] * kup[f] * 2.0) * c->dxinv[2][k];
+                amxd = -(0.50 * dt * reinv) * amxd;
+                apxd = -(0.50 * dt * reinv) * apxd;
+                amyd = -(0.50 * dt * reinv) * amyd;
+                apyd = -(0.50 * dt * reinv) * apyd;
+                amzd = -(0.50 * dt * reinv) * amzd * rnDim;
+                apzd = -(0.50 * dt * reinv) * apzd * rnDim;
+                for (int q = 0; q < 3; ++q) {
+                    const double *bx = bc9[3 * q], *by = bc9[3 * q + 1], *bz = bc9[3 * q + 2];
+                    double *r = nl[q];
+                    if (sign > 0)
+                        r[f] = r[f] + amxd * bx[f] * ium[f] + apxd * bx[f] * iup[f] + amyd * by[f] * jum[f]
+                               + apyd * by[f] * jup[f] + amzd * bz[f] * kum[f] + apzd * bz[f] * kup[f];
+                    else
+                        r[f] = r[f] - amxd * bx[f] * ium[f] - apxd * bx[f] * iup[f] - amyd * by[f] * jum[f]
+                               - apyd * by[f] * jup[f] - amzd * bz[f] * kum[f] - apzd * bz[f] * kup[f];
+                }
+            }
+}
+
+/* GCM_enforce_global_mass_consv (IBM/GCM_GLOBAL_MASS_CONSERVE.F90:6-86), the
+ * end of GCM_GhostCell_Vel with zero-gradient sides: face_vel of the current
+ * velocities (NO_VAN_KAN) into the step's faces, the net face flux out of the
+ * fluid cells, the boundary terms of the right-hand sides removed, the
+ * zero-gradient planes corrected by -massflux / outflow_area and the terms
+ * put back with the corrected values. */
+static void gcm_enforce_global_mass_consv(or_ctx *c, double dt, double reinv, double *u, double *v, double *w,
+                                          double *const *faces, double *const *bc9, double *const *nl)
+{
+    or_face_vel(c, 0, dt, u, v, w, NULL, bc9[0], bc9[4], bc9[8], faces[0], faces[1], faces[2]);
+    const double *fu = faces[0], *fv = faces[1], *fw = faces[2];
+    double massflux = 0.0;
+    for (int k = 1; k <= c->nzc; ++k)
+        for (int j = 1; j <= c->nyc; ++j)
+            for (int i = 1; i <= c->nxc; ++i) {
+                const size_t f = FI(c, i, j, k);
+                const double dx = c->dx[0][i], dy = c->dx[1][j], dz = c->dx[2][k];
+                massflux = massflux + (-(fu[f] * dy * dz) + fu[FI(c, i + 1, j, k)] * dy * dz
+                                       - fv[f] * dx * dz + fv[FI(c, i, j + 1, k)] * dx * dz
+                                       - fw[f] * dx * dy + fw[FI(c, i, j, k + 1)] * dx * dy)
+                                          * (double)(1 - c->iblank[f]);
+            }
+    rhs_bc_terms(c, dt, reinv, bc9, nl, +1);
+    zg_correct_planes(c, bc9, -massflux / c->p.outflow_area);
+    rhs_bc_terms(c, dt, reinv, bc9, nl, -1);
+}
+
+int or_solve_ad(or_ctx *c, int advec_scheme, double dt, double *const *faces_w, double *u, double *v, double *w,
+                double *nlu, double *nlv, double *nlw, double *const *bc9, double reinv, int order, double *maxres)
+{
+    const double *const *faces = (const double *const *)faces_w;
+    int zg = 0;
+    for (int s = 0; s < 6; ++s) zg |= (c->p.bc[s] == BC_ZERO_GRADIENT);
+    const int mass_consv = zg && c->p.boundary_formulation == GCM_METHOD;
+    if (mass_consv && (!bc9 || !(c->p.outflow_area > 0.0))) return -1;
+    double *nlr[3] = {nlu, nlv, nlw};
     const double half_dt = (advec_scheme == 1) ? 0.0 : 0.5 * dt;
     if (!c->ad[0]) return -1;   /* or_set_solve_ad first */
     const int three_d = (c->p.ndim == DIM_3D);
@@ -1953,6 +2034,7 @@ int or_solve_ad(or_ctx *c, int advec_scheme, double dt, const double *const *fac
             if (three_d) itsolv_ad_dir(c, 2, half_dt, faces, vel[q], rr[q], order);
         }
         if (gcm && c->vg_on) gcm_vel_set_bc_internal(c, u, v, w);
+        if (mass_consv) gcm_enforce_global_mass_consv(c, dt, reinv, u, v, w, faces_w, bc9, nlr);
         mr = 0.0;
         for (int q = 0; q < ncomp; ++q) {
             const double rq = calc_residual_ad(c, half_dt, faces, vel[q], rr[q]);

@@ -109,7 +109,9 @@ void    or_rhs_advec_diff(or_ctx *c, int advec_scheme, int frac_step_type, doubl
 void    or_set_solve_ad(or_ctx *c, double dt, const double *visc, const double *const *bcvisc3);
 void    or_rhs_adjust_bc(or_ctx *c, int advec_scheme, double dt, const double *const *faces,
                          const double *const *bc9, double *nlu, double *nlv, double *nlw);
-int     or_solve_ad(or_ctx *c, int advec_scheme, double dt, const double *const *faces, double *u, double *v,
-                    double *w, const double *nlu, const double *nlv, const double *nlw, int order,
-                    double *maxres);
+/* with zero-gradient sides and a GCM body every iteration ends with GCM_enforce_global_mass_consv,
+ * which rewrites faces, the zero-gradient planes of bc9 and nlu..nlw (reinv: 1/Re) */
+int     or_solve_ad(or_ctx *c, int advec_scheme, double dt, double *const *faces, double *u, double *v,
+                    double *w, double *nlu, double *nlv, double *nlw, double *const *bc9, double reinv,
+                    int order, double *maxres);
 #endif

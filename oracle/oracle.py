@@ -102,7 +102,7 @@ def lib():
                                        ctypes.POINTER(_dp), _dp, _dp, _dp]
         L.or_rhs_adjust_bc.restype = None
         L.or_solve_ad.argtypes = ([ctypes.c_void_p, ctypes.c_int, ctypes.c_double, ctypes.POINTER(_dp)] + [_dp] * 6
-                                  + [ctypes.c_int, _dp])
+                                  + [ctypes.POINTER(_dp), ctypes.c_double, ctypes.c_int, _dp])
         L.or_solve_ad.restype = ctypes.c_int
         _lib = L
     return _lib
@@ -247,11 +247,17 @@ class Oracle:
                                (_dp * 9)(*[_p(a) for a in bc9]), *(_p(a) for a in nl))
         return nl
 
-    def solve_ad(self, dt, faces, vel, nl, advec_scheme=2, order=0):
-        """solve_ad on vel = (u, v, w) in place; returns (iterations, maxres)."""
+    def solve_ad(self, dt, faces, vel, nl, advec_scheme=2, order=0, bc9=None, reinv=0.0):
+        """solve_ad on vel = (u, v, w) in place; returns (iterations, maxres).
+        With zero-gradient sides and a GCM body each iteration also rewrites
+        faces, the zero-gradient planes of bc9 and nl (GCM_enforce_global_mass_consv
+        with 1/Re = reinv)."""
         mr = ctypes.c_double()
+        b9 = None if bc9 is None else (_dp * 9)(*[_p(a) for a in bc9])
         it = lib().or_solve_ad(self.h, advec_scheme, dt, (_dp * 3)(*[_p(a) for a in faces]), *(_p(a) for a in vel),
-                               *(_p(a) for a in nl), order, ctypes.byref(mr))
+                               *(_p(a) for a in nl), b9, reinv, order, ctypes.byref(mr))
+        if it < 0:
+            raise ValueError("solve_ad: zero-gradient sides with a GCM body need bc9 and outflow_area > 0")
         return it, mr.value
 
     def set_bc(self, vel, bc9, values, freq=None, time=0.0, tstart_gust=0.0, xout=1.0, yout=1.0):
