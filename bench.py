@@ -57,6 +57,10 @@ def parse():
     ap.add_argument("--no-steps", action="store_true", help="skip the face_vel/correct_vel/update_pressure timing")
     ap.add_argument("--steps-only", action="store_true",
                     help="only the face_vel/correct_vel/update_pressure timing on the sphere grid (profiling)")
+    ap.add_argument("--rollout", type=int, default=0,
+                    help="run N fractional steps of the 192x128x128 sphere channel (Re 300, dt 0.005) and print "
+                         "their line instead of the solve benchmark")
+    ap.add_argument("--rollout-cells", type=int, nargs=3, default=(192, 128, 128))
     ap.add_argument("--adjoint-n", type=int, default=96)
     ap.add_argument("--adjoint-dirs", type=int, default=200)
     ap.add_argument("--profile", action="store_true",
@@ -472,6 +476,71 @@ def device_time_step(n, seed, tol, krylov, steps=3, reinv=1e-3, dt=1e-3):
             "host_copies_per_step": 0}
 
 
+def channel_rollout(steps, cells=(192, 128, 128), warmup=2, restol=1e-6, dt=0.005, re=300.0):
+    """The sphere-wake rollout: a 192 x 128 x 128 uniform channel on [0,6] x
+    [0,4]^2, sphere of diameter 1 at (1.5, 2, 2) (GCM ghost cells), uniform
+    inflow U = 1, zero-gradient outflow with the outflow mass balance,
+    symmetry sides, Re 300, dt 0.005, Crank-Nicolson, mixed-precision
+    pressure solve every step (the stationary outer iteration: FGMRES refuses
+    the outflow compatibility correction, which moves the right-hand side
+    between iterations), absolute tolerances restol (pressure) and 1e-10
+    (momentum).
+    FractionalStep keeps every field in HBM; a step is one call per routine.
+    Reports steps/s over the untimed steps after `warmup`, the per-stage wall
+    time of one extra instrumented step, the solvers' iteration counts, the
+    divergence of the corrected faces and the peak device memory."""
+    import torch
+    from flow_structure_interaction_fem_ibm_gb300 import problem as P
+    from flow_structure_interaction_fem_ibm_gb300.grid import Metrics
+    from flow_structure_interaction_fem_ibm_gb300.time_step import FractionalStep
+    t0 = time.perf_counter()
+    pr = P.channel(tuple(cells))
+    q = pr.params
+    q.precision_mode, q.outer_krylov = 1, 0
+    q.restol_Poisson, q.iterMax_Poisson = restol, 2000
+    q.restol_ad, q.iterMax_ad = 1e-10, 200
+    inflow = np.array([[1.0, 0.0, 0.0]] + [[0.0, 0.0, 0.0]] * 5)
+    fluid = 1.0 - pr.geom.iblank
+    u0 = np.asfortranarray(fluid.astype(np.float64))
+    zero = np.zeros(pr.shape, order="F")
+    torch.cuda.reset_peak_memory_stats()
+    free0, total = torch.cuda.mem_get_info()
+    fs = FractionalStep(pr, dt, 1.0 / re, inflow, advec_scheme=2).start(u0, zero, zero)
+    setup_s = time.perf_counter() - t0
+    for _ in range(warmup):
+        fs.step()
+    torch.cuda.synchronize()
+    t1 = time.perf_counter()
+    recs = [fs.step() for _ in range(steps)]
+    torch.cuda.synchronize()
+    wall = time.perf_counter() - t1
+    stage = fs.step(timed=True)
+    free1, _ = torch.cuda.mem_get_info()
+    lib_bytes = int(fs.s.stats()["device_bytes"])
+    n = [c for c in cells]
+    fu, fv, fw = fs.faces
+    dinv = [torch.from_numpy(Metrics(c).dxinv).cuda() for c in (pr.x, pr.y, pr.z)]
+    I, J, K = slice(1, n[0] + 1), slice(1, n[1] + 1), slice(1, n[2] + 1)
+    fl = torch.from_numpy(np.ascontiguousarray(fluid.transpose())).cuda()[K, J, I]
+    div = ((fu[K, J, 2:n[0] + 2] - fu[K, J, I]) * dinv[0][I].view(1, 1, -1)
+           + (fv[K, 2:n[1] + 2, I] - fv[K, J, I]) * dinv[1][J].view(1, -1, 1)
+           + (fw[2:n[2] + 2, J, I] - fw[K, J, I]) * dinv[2][K].view(-1, 1, 1)) * fl
+    u = fs.vel[0]
+    out = {"profile": "channel_rollout",
+           "workload": f"channel_{n[0]}x{n[1]}x{n[2]}_[0,6]x[0,4]^2_sphere_d1_at_(1.5,2,2)_Re{re:g}_dt{dt:g}_CN_"
+                       f"mixed_stationary",
+           "steps": steps, "warmup": warmup, "ms_per_step": 1e3 * wall / steps, "steps_per_s": steps / wall,
+           "stage_ms": stage["ms"], "poisson_iters": [r["poisson_iters"] for r in recs],
+           "ad_iters": [r["ad_iters"] for r in recs],
+           "statuses_ok": all(r["poisson_status"] == 0 and r["ad_status"] == 0 for r in recs),
+           "max_abs_div_after_correction": float(div.abs().max()), "restol_Poisson": restol,
+           "u_max": float(u.abs().max()), "time": fs.time, "ghost_cells": int(pr.geom.nGhost),
+           "device_bytes_in_use": int(free0 - free1), "torch_peak_bytes": int(torch.cuda.max_memory_allocated()),
+           "library_bytes": lib_bytes, "setup_s": setup_s}
+    fs.close()
+    return out
+
+
 def cpu_iteration_time(seed, sample_n=128):
     oracle_iteration_time(sample_n, seed)   # builds the oracle (not timed)
     return oracle_iteration_time(sample_n, seed), sample_n
@@ -504,6 +573,10 @@ def main():
         s.solve_poisson(p, pr.nlu0)
         print(json.dumps({"profile": "krylov", "stats": s.stats()}))
         s.close()
+        return
+
+    if args.rollout > 0:
+        print(json.dumps(channel_rollout(args.rollout, args.rollout_cells)))
         return
 
     if args.steps_only:

@@ -315,6 +315,26 @@ def sphere(n=128, seed: int = 2, stretch: Optional[float] = 1.5, radius: float =
     return Problem(p, x, y, z, geom, nlu0, name=f"sphere_{nxc}x{nyc}x{nzc}_{tag}")
 
 
+CHANNEL_BC = (1, 2, 4, 4, 4, 4)   # Dirichlet inflow, zero-gradient outflow, symmetry sides
+
+
+def channel(cells=(192, 128, 128), lengths=(6.0, 4.0, 4.0), centre=(1.5, 2.0, 2.0), diameter: float = 1.0,
+            nsub: int = 4, **kw) -> Problem:
+    """Channel with a stationary ghost-cell sphere: uniform grid on
+    [0,Lx] x [0,Ly] x [0,Lz], velocity BC types CHANNEL_BC (x1 inflow, x2
+    zero-gradient outflow, symmetry sides), Neumann pressure, outflow_area
+    from set_outflow_area.  nlu0 is zero: a time loop forms it every step.
+    The default is the 192 x 128 x 128 channel of the sphere-wake rollout."""
+    p = default_params(DIM_3D, *cells, body=True, **kw)
+    p.bc = CHANNEL_BC
+    x, y, z = make_grid(p.nx, p.ny, p.nz, "uniform", lengths=lengths)
+    verts, tris = icosphere(nsub, 0.5 * diameter, centre)
+    geom = body_geometry(p, x, y, z, verts, tris)
+    p.outflow_area = outflow_area(p, x, y, z, geom.iblank)
+    name = f"channel_{cells[0]}x{cells[1]}x{cells[2]}_sphere_d{diameter:g}"
+    return Problem(p, x, y, z, geom, np.zeros(full_shape(p), order="F"), name=name)
+
+
 def kat2d(n: int = 64, **kw) -> Problem:
     """Poisson_Tester known-answer case (IBM/CORE_POISSON.F90:1386-1444):
     domain [0,pi]^2, all-Neumann, nlu0 = -2 cos(xc) cos(yc); the exact answer is
