@@ -25,8 +25,8 @@ INCLUDE = ROOT / "include"
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
-CUDA_SOURCES = ["fsi_mg.cu", "mg_kernels.cu", "step_kernels.cu"]
-CUDA_HEADERS = ["mg_kernels.cuh", "device_util.cuh"]
+CUDA_SOURCES = ["fsi_mg.cu", "step_api.cu", "mg_kernels.cu", "step_kernels.cu"]
+CUDA_HEADERS = ["mg_kernels.cuh", "device_util.cuh", "mg_context.h"]
 
 
 def nvcc() -> str:
