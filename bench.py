@@ -476,15 +476,15 @@ def device_time_step(n, seed, tol, krylov, steps=3, reinv=1e-3, dt=1e-3):
             "host_copies_per_step": 0}
 
 
-def channel_rollout(steps, cells=(192, 128, 128), warmup=2, restol=1e-6, dt=0.005, re=300.0):
+def channel_rollout(steps, cells=(192, 128, 128), krylov=30, warmup=2, restol=1e-6, dt=0.005, re=300.0):
     """The sphere-wake rollout: a 192 x 128 x 128 uniform channel on [0,6] x
     [0,4]^2, sphere of diameter 1 at (1.5, 2, 2) (GCM ghost cells), uniform
     inflow U = 1, zero-gradient outflow with the outflow mass balance,
     symmetry sides, Re 300, dt 0.005, Crank-Nicolson, mixed-precision
-    pressure solve every step (the stationary outer iteration: FGMRES refuses
-    the outflow compatibility correction, which moves the right-hand side
-    between iterations), absolute tolerances restol (pressure) and 1e-10
-    (momentum).
+    pressure solve every step (FGMRES(krylov) around MG_Solver on the
+    operator of the outflow compatibility fixed point; krylov 0: the
+    stationary outer iteration), absolute tolerances restol (pressure) and
+    1e-10 (momentum).
     FractionalStep keeps every field in HBM; a step is one call per routine.
     Reports steps/s over the untimed steps after `warmup`, the per-stage wall
     time of one extra instrumented step, the solvers' iteration counts, the
@@ -496,7 +496,7 @@ def channel_rollout(steps, cells=(192, 128, 128), warmup=2, restol=1e-6, dt=0.00
     t0 = time.perf_counter()
     pr = P.channel(tuple(cells))
     q = pr.params
-    q.precision_mode, q.outer_krylov = 1, 0
+    q.precision_mode, q.outer_krylov = 1, krylov
     q.restol_Poisson, q.iterMax_Poisson = restol, 2000
     q.restol_ad, q.iterMax_ad = 1e-10, 200
     inflow = np.array([[1.0, 0.0, 0.0]] + [[0.0, 0.0, 0.0]] * 5)
@@ -528,7 +528,7 @@ def channel_rollout(steps, cells=(192, 128, 128), warmup=2, restol=1e-6, dt=0.00
     u = fs.vel[0]
     out = {"profile": "channel_rollout",
            "workload": f"channel_{n[0]}x{n[1]}x{n[2]}_[0,6]x[0,4]^2_sphere_d1_at_(1.5,2,2)_Re{re:g}_dt{dt:g}_CN_"
-                       f"mixed_stationary",
+                       f"mixed_{'fgmres' + str(krylov) if krylov else 'stationary'}",
            "steps": steps, "warmup": warmup, "ms_per_step": 1e3 * wall / steps, "steps_per_s": steps / wall,
            "stage_ms": stage["ms"], "poisson_iters": [r["poisson_iters"] for r in recs],
            "ad_iters": [r["ad_iters"] for r in recs],
@@ -576,7 +576,7 @@ def main():
         return
 
     if args.rollout > 0:
-        print(json.dumps(channel_rollout(args.rollout, args.rollout_cells)))
+        print(json.dumps(channel_rollout(args.rollout, args.rollout_cells, args.krylov)))
         return
 
     if args.steps_only:

@@ -596,6 +596,41 @@ double g_krylov_inner_rtol = 1.0e-5;
 // inside a cycle: FP64 in the plain form; FP32 in the mixed form, where each
 // restart recomputes the residual in FP64 and adds the cycle's correction to
 // p in FP64 (iterative refinement with an FP32 FGMRES inner solver).
+// n1 = nlw0 of a unit shift of the zero-gradient planes (-1 on minus sides, +1 on plus
+// sides, over the (0:n_a-1, 0:n_b-1) part of each plane that GCM_enforce_p_compatibility
+// shifts), in FP64 and FP32; depends on the flags only
+int ensure_compat_rank1(Ctx &c)
+{
+    if (c.n1_ready) return 0;
+    const long long n1 = c.L1.d.count();
+    if (!c.pg_unit) TRY(c.alloc(&c.pg_unit, c.npgrad));
+    if (!c.n1_64) TRY(c.alloc(&c.n1_64, (size_t)n1));
+    if (!c.n1_32) TRY(c.alloc(&c.n1_32, (size_t)n1));
+    if (!c.kflux) TRY(c.alloc(&c.kflux, 2));
+    const long long px = (long long)(c.ny + 2) * (c.nz + 2), py = (long long)(c.nx + 2) * (c.nz + 2),
+                    pz = (long long)(c.nx + 2) * (c.ny + 2);
+    const long long off[6] = {0, px, 2 * px, 2 * px + py, 2 * px + 2 * py, 2 * px + 2 * py + pz};
+    const int sa[6] = {c.ny + 2, c.ny + 2, c.nx + 2, c.nx + 2, c.nx + 2, c.nx + 2};
+    const int sb[6] = {c.nz + 2, c.nz + 2, c.nz + 2, c.nz + 2, c.ny + 2, c.ny + 2};
+    if ((size_t)(off[5] + pz) > c.npgrad) return fail(-1, "pgrad buffer smaller than its six planes");
+    std::vector<double> h(c.npgrad, 0.0);
+    for (int q = 0; q < 6; ++q) {
+        if (c.p.bc[q] != BC_ZERO_GRADIENT) continue;
+        const double sign = (q % 2 == 0) ? -1.0 : 1.0;
+        for (int b = 0; b <= sb[q] - 2; ++b)
+            for (int a = 0; a <= sa[q] - 2; ++a) h[(size_t)(off[q] + a + (long long)sa[q] * b)] = sign;
+    }
+    CK(cudaMemcpyAsync(c.pg_unit, h.data(), c.npgrad * sizeof(double), cudaMemcpyHostToDevice, c.s));
+    CK(cudaMemsetAsync(c.n1_64, 0, (size_t)n1 * sizeof(double), c.s));
+    launch_nlw0(c.n1_64, c.L1.fl, c.side_raw, c.pg_unit, c.d_dxinv[0], c.d_dxinv[1], c.d_dxinv[2], c.L1.d, c.nx, c.ny,
+                c.nz, c.s);
+    launch_convert_d2f(c.n1_32, c.n1_64, n1, c.s);
+    c.launches += 2;
+    CK(cudaStreamSynchronize(c.s));   // h leaves scope
+    c.n1_ready = true;
+    return 0;
+}
+
 template <typename T>
 int solve_krylov_t(Ctx &c, double *p, const double *b, int *iters, double *maxres_out, int *loc, double *compTime)
 {
@@ -615,7 +650,14 @@ int solve_krylov_t(Ctx &c, double *p, const double *b, int *iters, double *maxre
     CK(cudaEventRecord(c.ev0, c.s));
     const bool dirichlet = c.p.pbc[0] == PBC_DIRICHLET || c.p.pbc[2] == PBC_DIRICHLET || c.p.pbc[4] == PBC_DIRICHLET;
     if (dirichlet) return fail(-1, "outer_krylov needs all-Neumann pressure boundaries");
-    if (c.compat_active) return fail(-1, "outer_krylov needs an inactive compatibility correction (no zero-gradient BCs)");
+    // With zero-gradient sides each restart's GCM_correct_pressure shifts the outflow planes by
+    // -(phi . p + chi(pgrad)) / outflow_area, a linear function of p: the iteration's fixed point
+    // solves A p + (phi . p / outflow_area) n1 = b', b' independent of the planes.  The cycles
+    // apply that operator (the rank-one term below), so the shift at the next restart leaves
+    // the residual they reduced unchanged.
+    const bool rank1 = c.compat_active && gcm;
+    if (rank1) TRY(ensure_compat_rank1(c));
+    const T *n1T = f32 ? (const T *)c.n1_32 : (const T *)c.n1_64;
     if (c.nlw0_nonzero) { launch_fill<double>(c.nlw0, n1, 0.0, c.s); c.launches++; }
     subtract_average(c, p);
     CK(cudaMemsetAsync(c.d_iters, 0, sizeof(int), c.s));
@@ -669,6 +711,12 @@ int solve_krylov_t(Ctx &c, double *p, const double *b, int *iters, double *maxre
             }
             launch_apply_op<T>(KZ[j], w, c.L1.fl, coefT, c.L1.d, c.s);
             c.launches++;
+            if (rank1) {
+                launch_compat_rank1<T>(KZ[j], w, n1T, c.L1.fl, c.d_dx[0], c.d_dx[1], c.d_dx[2], c.d_dxcinv[0],
+                                       c.d_dxcinv[1], c.d_dxcinv[2], c.side_raw, c.L1.d, (double *)c.partials,
+                                       c.nred, c.kflux, c.p.outflow_area, c.nx, c.ny, c.nz, c.s);
+                c.launches += 3;
+            }
             const T *const *Vp = KV.data();
             // classical Gram-Schmidt, twice
             launch_mdot<T>(Vp, j + 1, w, c.L1.fl, c.L1.d, c.kpart, c.nred, c.kdots, c.s);
@@ -1211,6 +1259,7 @@ int fsi_mg_set_geometry(void *handle, const int8_t *iblank, const int8_t *ghostC
     if (c.pgraph) { cudaGraphExecDestroy(c.pgraph); c.pgraph = nullptr; }
     c.vg_on = false;   // the ghost list changed: velocity ghosts are registered again
     c.geometry = true;
+    c.n1_ready = false;   // the unit-shift term follows the flags
     return 0;
 }
 

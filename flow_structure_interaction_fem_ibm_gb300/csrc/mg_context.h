@@ -100,6 +100,11 @@ struct Ctx {
     double *pgrad = nullptr;
     size_t npgrad = 0;
     bool compat_active = false, nlw0_nonzero = false;
+    // FGMRES with the compatibility correction: n1 = nlw0 of a unit shift of the zero-gradient
+    // planes (per precision), the unit planes themselves and the flux scalar of phi . z
+    double *pg_unit = nullptr, *n1_64 = nullptr, *kflux = nullptr;
+    float *n1_32 = nullptr;
+    bool n1_ready = false;
     int side_raw[6] = {1, 1, 1, 1, 1, 1};
     int sign[6] = {1, 1, 1, 1, 1, 1};
     double *d_dx[3] = {}, *d_dxinv[3] = {}, *d_dxcinv[3] = {};

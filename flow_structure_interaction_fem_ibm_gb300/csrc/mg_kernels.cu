@@ -1391,6 +1391,47 @@ __global__ void __launch_bounds__(TPB) k_compat_partial(CompatArgs A, double *pa
     if (threadIdx.x == 0) partials[blockIdx.x] = s;
 }
 
+// phi . z: the pressure-gradient flux of z out of the fluid cells through their
+// unflagged faces, GCM_enforce_p_compatibility's sum with zero boundary planes
+// (its pgrad terms are the part that does not depend on the pressure)
+template <typename T>
+__global__ void __launch_bounds__(TPB) k_grad_flux(const T *z, CompatArgs A, double *partials)
+{
+    const Dims &d = A.d;
+    const int n0 = d.m[0] - 1, n1 = d.m[1] - 1, n2 = d.m[2] - 1;
+    const long long total = (long long)n0 * n1 * n2;
+    double acc = 0.0;
+    for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < total;
+         t += (long long)gridDim.x * blockDim.x) {
+        int i, j, k;
+        cell_of((unsigned)t, (unsigned)n0, (unsigned)n1, i, j, k);
+        const long long o = d.idx(i, j, k);
+        const uint8_t f = A.fl[o];
+        if (f & FB_IB) continue;
+        const int ium = face_flag(f, 0, 0, A.sf[0], i == 1), iup = face_flag(f, 0, 1, A.sf[1], i == n0);
+        const int jum = face_flag(f, 1, 0, A.sf[2], j == 1), jup = face_flag(f, 1, 1, A.sf[3], j == n1);
+        const int kum = face_flag(f, 2, 0, A.sf[4], k == 1), kup = face_flag(f, 2, 1, A.sf[5], k == n2);
+        const double zo = (double)z[o];
+        const double gw = ium ? 0.0 : (zo - (double)z[o - 1]) * A.dxcinv[i];
+        const double ge = iup ? 0.0 : ((double)z[o + 1] - zo) * A.dxcinv[i + 1];
+        const double gs = jum ? 0.0 : (zo - (double)z[o - d.sx]) * A.dycinv[j];
+        const double gn = jup ? 0.0 : ((double)z[o + d.sx] - zo) * A.dycinv[j + 1];
+        const double gb = kum ? 0.0 : (zo - (double)z[o - d.sxy]) * A.dzcinv[k];
+        const double gf = kup ? 0.0 : ((double)z[o + d.sxy] - zo) * A.dzcinv[k + 1];
+        acc += (ge - gw) * A.dy[j] * A.dz[k] + (gn - gs) * A.dx[i] * A.dz[k] + (gf - gb) * A.dx[i] * A.dy[j];
+    }
+    const double s = block_sum(acc);
+    if (threadIdx.x == 0) partials[blockIdx.x] = s;
+}
+
+// w += (flux / outflow_area) n1
+template <typename T>
+__global__ void k_add_scaled(T *w, const T *n1, const double *flux, double inv_area, long long n)
+{
+    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t < n) w[t] = w[t] + (T)(flux[0] * inv_area) * n1[t];
+}
+
 // the reference shifts the plane over (0:n_a, 0:n_b), not its last row/column
 // (IBM/GCM_GLOBAL_MASS_CONSERVE.F90:340-361)
 __global__ void k_pgrad_shift(double *pg, long long off, int sa, int sb, const double *flux, double outflow_area,
@@ -1956,6 +1997,26 @@ void launch_compat(const double *p, const uint8_t *fl, const double *pg, const d
         if (bc_zero_grad[q])
             k_pgrad_shift<<<nblk(sizes[q]), TPB, 0, s>>>(pgrad, A.off[q], sa[q], sb[q], flux, outflow_area, signs[q]);
 }
+
+template <typename T>
+void launch_compat_rank1(const T *z, T *w, const T *n1, const uint8_t *fl, const double *dx, const double *dy,
+                         const double *dz, const double *dxcinv, const double *dycinv, const double *dzcinv,
+                         const int side_flag[6], const Dims &d, double *partials, int nblocks, double *flux,
+                         double outflow_area, int nx, int ny, int nz, cudaStream_t s)
+{
+    CompatArgs A = make_compat(nullptr, fl, nullptr, dx, dy, dz, dxcinv, dycinv, dzcinv, side_flag, d, nx, ny, nz);
+    k_grad_flux<T><<<nblocks, TPB, 0, s>>>(z, A, partials);
+    k_sum_final<<<1, 1024, 0, s>>>(partials, nblocks, 1, flux);
+    k_add_scaled<T><<<nblk(d.count()), TPB, 0, s>>>(w, n1, flux, 1.0 / outflow_area, d.count());
+}
+template void launch_compat_rank1<double>(const double *, double *, const double *, const uint8_t *, const double *,
+                                          const double *, const double *, const double *, const double *,
+                                          const double *, const int *, const Dims &, double *, int, double *, double,
+                                          int, int, int, cudaStream_t);
+template void launch_compat_rank1<float>(const float *, float *, const float *, const uint8_t *, const double *,
+                                         const double *, const double *, const double *, const double *,
+                                         const double *, const int *, const Dims &, double *, int, double *, double,
+                                         int, int, int, cudaStream_t);
 
 void launch_nlw0(double *nlw0, const uint8_t *fl, const int side_flag[6], const double *pgrad, const double *dxinv,
                  const double *dyinv, const double *dzinv, const Dims &d, int nx, int ny, int nz, cudaStream_t s)

@@ -266,6 +266,14 @@ void launch_compat(const double *p, const uint8_t *fl, const double *pg, const d
                    const double *dzcinv, const int side_flag[6], const Dims &d, double *partials,
                    int nblocks, double *pgrad, const int bc_zero_grad[6], double outflow_area,
                    int nx, int ny, int nz, cudaStream_t s);
+// w += (phi . z / outflow_area) n1: the rank-one part of the operator that the compatibility
+// correction adds (phi . z the pressure-gradient flux of z through the unflagged faces of the
+// fluid cells, n1 the nlw0 of a unit shift of the zero-gradient planes); flux receives phi . z
+template <typename T>
+void launch_compat_rank1(const T *z, T *w, const T *n1, const uint8_t *fl, const double *dx, const double *dy,
+                         const double *dz, const double *dxcinv, const double *dycinv, const double *dzcinv,
+                         const int side_flag[6], const Dims &d, double *partials, int nblocks, double *flux,
+                         double outflow_area, int nx, int ny, int nz, cudaStream_t s);
 void launch_nlw0(double *nlw0, const uint8_t *fl, const int side_flag[6], const double *pgrad,
                  const double *dxinv, const double *dyinv, const double *dzinv, const Dims &d,
                  int nx, int ny, int nz, cudaStream_t s);

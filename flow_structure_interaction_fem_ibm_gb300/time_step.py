@@ -41,11 +41,11 @@ class FractionalStep:
         self.freq = None if bc_freq is None else np.asarray(bc_freq, dtype=np.float64).reshape(6, 3)
         self.tstart_gust = float(tstart_gust)
         p = problem.params
-        if 2 in tuple(p.bc) and p.precision_mode != 1:
-            # zero-gradient outflow makes nlw0 non-zero; the plain MG form keeps the
-            # reference's smoother, which adds nlw instead, and stalls
-            raise ValueError("zero-gradient outflow needs the mixed pressure solve (precision_mode 1), whose "
-                             "defect correction includes the outflow pressure-gradient term nlw0")
+        if 2 in tuple(p.bc) and p.precision_mode != 1 and p.outer_krylov == 0:
+            # zero-gradient outflow makes nlw0 non-zero; the plain stationary MG form keeps
+            # the reference's smoother, which adds nlw instead, and stalls
+            raise ValueError("zero-gradient outflow needs a pressure solve whose residual includes the outflow "
+                             "term nlw0: the mixed form (precision_mode 1) or FGMRES (outer_krylov > 0)")
         self.xout = float(problem.x[p.nx] - problem.x[1])
         self.yout = float(problem.y[p.ny] - problem.y[1])
         self.s = PoissonSolver(p, problem.x, problem.y, problem.z).set_boundary(problem.geom)

@@ -9,8 +9,10 @@ Zero-gradient outflow makes nlw0 (the outflow pressure-gradient term of
 GCM_correct_pressure) non-zero.  The reference's MG smoother adds nlw
 instead, so its stationary MG iteration converges to a system without
 nlw0 while calc_residual measures the one with it, and stalls.  The
-pressure solve here is the mixed form's stationary outer iteration: defect
-correction on b - A p + nlw0.  Its reference is the reference's LSOR branch of
+pressure solve here is the mixed form's stationary outer iteration, a
+defect correction on b - A p + nlw0, or FGMRES(30).  FGMRES runs in FP64
+or mixed and applies the operator of the compatibility fixed point:
+A p + (phi . p / outflow_area) n1.  Its reference is the reference's LSOR branch of
 solve_poisson, whose smoother adds nlw0 (the oracle with pp_solver_type
 1).  Both solve the consistent system.  Both iterative solves run to tight
 tolerances; after three steps the velocities, faces, boundary values and
@@ -87,10 +89,13 @@ def oracle_rollout(pr, u0, v0, w0, steps, scheme):
 
 
 @pytest.mark.gpu
+@pytest.mark.parametrize("solver", [(1, 0), (1, 30), (0, 30)], ids=["mixed_stationary", "mixed_fgmres30",
+                                                                    "fp64_fgmres30"])
 @pytest.mark.parametrize("scheme", [1, 2], ids=["ab2", "cn"])
-def test_gpu_channel_rollout_matches_oracle(gpu_built, scheme):
+def test_gpu_channel_rollout_matches_oracle(gpu_built, scheme, solver):
     from flow_structure_interaction_fem_ibm_gb300.time_step import FractionalStep
     pr = small_channel()
+    pr.params.precision_mode, pr.params.outer_krylov = solver
     u0, v0, w0 = initial_velocity(pr)
     ref = oracle_rollout(pr, u0, v0, w0, STEPS, scheme)
     for it_ad, mr_ad, st, it, mr in ref["iters"]:
