@@ -61,6 +61,8 @@ def parse():
                     help="run N fractional steps of the 192x128x128 sphere channel (Re 300, dt 0.005) and print "
                          "their line instead of the solve benchmark")
     ap.add_argument("--rollout-cells", type=int, nargs=3, default=(192, 128, 128))
+    ap.add_argument("--no-rollout", action="store_true",
+                    help="skip the 20-step sphere-wake channel rollout reported beside the solve benchmark")
     ap.add_argument("--adjoint-n", type=int, default=96)
     ap.add_argument("--adjoint-dirs", type=int, default=200)
     ap.add_argument("--profile", action="store_true",
@@ -741,6 +743,10 @@ def main():
         s_mixed = s_fp64 = None
         adjoint = adjoint_check(args.adjoint_n, args.adjoint_dirs)
 
+    rollout = None
+    if rank == 0 and not args.no_rollout:
+        rollout = channel_rollout(20, krylov=args.krylov)
+
     # roofline of the dominant kernel: level-1 FP32 line relaxation (k_line_wp<float,dir,8>),
     # durations from CUDA events around each launch inside the timed solves
     avg_ms = lt["ms"] / max(lt["launches"], 1)
@@ -780,7 +786,8 @@ def main():
         "iters_mixed": mixed_iters[0], "iters_fp64": fp64_iters[0], "stationary": stationary,
         "wall_ms_per_step": 1e3 * mixed_wall / args.steps,
         "gpu_launches": int(mixed_launch), "clocks": clocks, "e2e": e2e, "roofline": roofline,
-        "cpu_baseline": cpu, "adjoint": adjoint, "projection_steps": steps_ops, "setup_s": setup_s,
+        "cpu_baseline": cpu, "adjoint": adjoint, "projection_steps": steps_ops, "channel_rollout": rollout,
+        "setup_s": setup_s,
     }
     if rank == 0:
         print(json.dumps(out))
