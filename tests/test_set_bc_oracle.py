@@ -192,3 +192,15 @@ def test_outflow_area_matches_reference_formula():
     area_right = sum(my.dx[j] * mz.dx[k] * (1 - pr.geom.iblank[nxc, j, k])
                      for j in range(1, p.ny) for k in range(1, p.nz))
     assert abs(P.outflow_area(p, pr.x, pr.y, pr.z, pr.geom.iblank) - area_right) <= 1e-14 * area_right
+
+
+def test_fractional_step_refuses_outflow_with_the_plain_stationary_solve():
+    """Zero-gradient outflow with the plain stationary MG form would stall (the
+    reference's MG smoother adds nlw, not the outflow term nlw0); FractionalStep
+    refuses it before it touches the device."""
+    pytest.importorskip("torch")
+    from flow_structure_interaction_fem_ibm_gb300.time_step import FractionalStep
+    pr = P.channel((24, 16, 16))
+    pr.params.precision_mode, pr.params.outer_krylov = 0, 0
+    with pytest.raises(ValueError, match="nlw0"):
+        FractionalStep(pr, 0.005, 1.0 / 300.0, np.zeros((6, 3)))
