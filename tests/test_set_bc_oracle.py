@@ -204,3 +204,21 @@ def test_fractional_step_refuses_outflow_with_the_plain_stationary_solve():
     pr.params.precision_mode, pr.params.outer_krylov = 0, 0
     with pytest.raises(ValueError, match="nlw0"):
         FractionalStep(pr, 0.005, 1.0 / 300.0, np.zeros((6, 3)))
+
+
+def test_channel_builder():
+    """The sphere-wake channel: 192 x 128 x 128 cells on [0,6] x [0,4]^2, inflow,
+    zero-gradient outflow and symmetry sides, outflow_area the 4 x 4 outflow
+    plane (the sphere of diameter 1 at (1.5, 2, 2) does not reach it)."""
+    pr = P.channel()
+    p = pr.params
+    assert (p.nx, p.ny, p.nz) == (193, 129, 129)
+    assert tuple(p.bc) == P.CHANNEL_BC
+    assert abs(p.outflow_area - 16.0) <= 1e-12
+    assert abs(pr.x[p.nx] - 6.0) <= 1e-12 and abs(pr.y[p.ny] - 4.0) <= 1e-12
+    g = pr.geom
+    assert g.nGhost > 0 and int(g.iblank.sum()) > 0
+    # every blanked cell lies inside the sphere's bounding box
+    ii, jj, kk = np.nonzero(g.iblank)
+    xc = 0.5 * (pr.x[ii] + pr.x[ii + 1])
+    assert xc.min() > 0.9 and xc.max() < 2.1
