@@ -5,7 +5,10 @@ of the right-hand sides, corrects the zero-gradient planes by -massflux /
 outflow_area and puts the terms back.
 
 CPU: the oracle's literal restatement converges and leaves the faces of the
-converged velocities without net flux out of the fluid cells.  GPU: the
+converged velocities without net flux out of the fluid cells.  The pressure
+solve's compatibility shift of the outflow planes is linear in p and
+balances the flux in one application; the FGMRES operator with zero-gradient
+outflow is built on those two facts.  GPU: the
 converged velocities, the faces, the nine bc arrays and the right-hand sides
 agree with the oracle's reference-order solve to 1e-9.
 """
@@ -143,3 +146,39 @@ def test_gpu_outflow_balance_in_solve_ad_matches_oracle(gpu_built, scheme):
         assert abs(m) <= 1e-11 * gross
     finally:
         s.close()
+
+
+def _compat_shift(pr, p):
+    """The outflow planes' shift of one GCM_correct_pressure on p (fresh oracle,
+    planes starting at zero), and the p it leaves (ghost layers updated)."""
+    o = Oracle(pr)
+    try:
+        q = o.correct_pressure(np.array(p, order="F", copy=True))
+        return o.pgrad(), q, o
+    except Exception:
+        o.close()
+        raise
+
+
+def test_compatibility_shift_is_linear_in_p_and_balances_the_flux():
+    """The two facts behind the FGMRES operator with zero-gradient outflow
+    (IBM/GCM_GLOBAL_MASS_CONSERVE.F90:260-394): the shift of the outflow
+    planes is a linear function of p (with planes starting at zero,
+    shift(p1 + p2) = shift(p1) + shift(p2)); and after one correction the
+    pressure-gradient flux balances, so a second correction with the same p
+    leaves the planes where they are."""
+    pr = sphere_problem(12, stretch=None, bc=(1, 2, 1, 1, 1, 1), outflow_area=1.0)
+    rng = np.random.default_rng(11)
+    p1 = np.asfortranarray(rng.standard_normal(pr.shape))
+    p2 = np.asfortranarray(rng.standard_normal(pr.shape))
+    g1, _, o1 = _compat_shift(pr, p1)
+    g2, _, o2 = _compat_shift(pr, p2)
+    g12, q12, o12 = _compat_shift(pr, p1 + p2)
+    try:
+        assert np.abs(g12).max() > 1e-3                 # the planes moved
+        np.testing.assert_allclose(g12, g1 + g2, rtol=0, atol=1e-12 * np.abs(g12).max())
+        o12.correct_pressure(q12)                        # same p, planes already balanced
+        np.testing.assert_allclose(o12.pgrad(), g12, rtol=0, atol=1e-12 * np.abs(g12).max())
+    finally:
+        for o in (o1, o2, o12):
+            o.close()
