@@ -47,7 +47,9 @@ typedef struct {
     int coarse_flag_mode;     /* ignored by the GPU (coarse face flags always follow the coarse iblank) */
     int precision_mode;       /* 0 FP64 throughout, 1 FP32 cycle inside FP64 refinement */
     int outer_krylov;         /* 0: the reference's stationary outer iteration; m > 0: FGMRES(m) with
-                                 MG_Solver as the preconditioner (same system, same max-norm test) */
+                                 MG_Solver as the preconditioner (same system, same max-norm test;
+                                 with zero-gradient sides and a GCM body the cycles apply the
+                                 operator of the compatibility correction's fixed point) */
     double omega;             /* line-SOR relaxation */
     double restol_Poisson;    /* absolute max-norm tolerance */
     double restol_ad;         /* ghost-row fixed-point tolerance */
