@@ -351,8 +351,8 @@ Level &level_of(Ctx &c, int d, int n) { return n == 1 ? c.L1 : c.C[d][n]; }
 
 // MG_X / MG_Y / MG_Z (IBM/CORE_MG.F90:1239-1663) for direction d.  At level 1 the
 // caller passes the level-1 var/rhs; coarse levels use their own arrays.  With
-// mixed precision (T = float) the coarsest level can be smoothed in FP64
-// (FSI_MG_COARSEST_FP64=1); by default it runs in FP32 like the other levels.
+// mixed precision (T = float) every level, the coarsest included, is smoothed
+// in FP32.
 template <typename T>
 void mg_cycle(Ctx &c, int d, T *var, const T *rhs, int n, int WF, int &GMM, bool homogeneous)
 {
@@ -363,17 +363,7 @@ void mg_cycle(Ctx &c, int d, T *var, const T *rhs, int n, int WF, int &GMM, bool
     const bool gcm = (c.p.boundary_formulation == GCM_METHOD);
     if (n == 1 && gcm) gcm_pressure<T>(c, var);
     if (WF == 1) {
-        if (std::is_same<T, float>::value && n == nlev && n > 1 && !c.coarsest_fp32) {
-            // FP64 coarsest-level solve inside the FP32 cycle
-            launch_convert_f2d(L.r64, (const float *)rhs, L.d.count(), c.s);
-            launch_convert_f2d(L.v64, (const float *)var, L.d.count(), c.s);
-            c.launches += 2;
-            for (int it = 0; it < totIter; ++it) itsolv<double>(c, L, L.v64, L.r64, false, true);
-            launch_convert_d2f((float *)var, L.v64, L.d.count(), c.s);
-            c.launches++;
-        } else {
-            for (int it = 0; it < totIter; ++it) itsolv<T>(c, L, var, rhs, n == 1, homogeneous);
-        }
+        for (int it = 0; it < totIter; ++it) itsolv<T>(c, L, var, rhs, n == 1, homogeneous);
     }
     if (n == nlev) {
         if (mgCycle == 3) GMM = 1;
@@ -585,8 +575,7 @@ int precondition(Ctx &c, const T *v, T *z)
 
 // Relative reduction one FP32 inner cycle aims for at most; the FP64 residual
 // recomputed at the restart carries the refinement further.
-// (FSI_MG_KRYLOV_INNER_RTOL overrides it for measurements.)
-double g_krylov_inner_rtol = 1.0e-5;
+constexpr double kKrylovInnerRtol = 1.0e-5;
 
 // solve_poisson with FGMRES(m) around MG_Solver (outer_krylov = m).  Same
 // discrete system (fluid rows with ghost values from the ghost-row fixed
@@ -695,7 +684,7 @@ int solve_krylov_t(Ctx &c, double *p, const double *b, int *iters, double *maxre
         std::fill(g.begin(), g.end(), 0.0);
         g[0] = beta;
         double target = 0.5 * beta * c.p.restol_Poisson / maxres;
-        if (f32) target = std::max(target, g_krylov_inner_rtol * beta);
+        if (f32) target = std::max(target, kKrylovInnerRtol * beta);
         int k = 0;
         for (int j = 0; j < m; ++j) {
             TRY(precondition<T>(c, KV[j], KZ[j]));
@@ -915,24 +904,8 @@ int fsi_mg_create(const fsi_mg_params *params, const double *x, const double *y,
     int ndev = 0;
     if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return fail(-12, "no CUDA device");
     CK(init_kernels());
-    {   // FSI_MG_LINE_KERNEL=thread selects the one-thread-per-line smoother (A/B measurements)
-        const char *lk = std::getenv("FSI_MG_LINE_KERNEL");
-        set_line_kernel(lk && std::strcmp(lk, "thread") == 0);
-        const char *kr = std::getenv("FSI_MG_KRYLOV_INNER_RTOL");
-        const double v = kr ? std::atof(kr) : 0.0;
-        g_krylov_inner_rtol = (v > 0.0 && v < 1.0) ? v : 1.0e-5;
-    }
     auto c = std::make_unique<Ctx>();
     c->p = p;
-    {   // FSI_MG_GHOST32_RELTOL: relative stopping threshold of the FP32 ghost rows (A/B measurements)
-        const char *gr = std::getenv("FSI_MG_GHOST32_RELTOL");
-        const double v = gr ? std::atof(gr) : 0.0;
-        if (v > 0.0 && v < 1.0) c->ghost32_reltol = v;
-    }
-    {   // FSI_MG_COARSEST_FP64=1: FP64 coarsest-level smoothing inside the FP32 cycle (A/B measurements)
-        const char *cf = std::getenv("FSI_MG_COARSEST_FP64");
-        c->coarsest_fp32 = !(cf && std::strcmp(cf, "1") == 0);
-    }
     c->nx = p.nx; c->ny = p.ny; c->nz = p.nz;
     c->nd = (p.ndim == 3) ? 3 : 2;
     CK(cudaStreamCreateWithFlags(&c->s, cudaStreamNonBlocking));
@@ -1135,10 +1108,8 @@ int fsi_mg_set_geometry(void *handle, const int8_t *iblank, const int8_t *ghostC
         }
         for (int l = 1; l < c.nlev[d]; ++l) TRY(build_transfer(c, c.T[d][l], d, l));
     }
-    // line factorisations of every level and direction
-    // and the factored partition tables of the FP64 smoother: every level when
-    // the cycle runs in FP64, the coarsest levels when the FP32 cycle smooths
-    // them in FP64 (FSI_MG_COARSEST_FP64=1)
+    // line factorisations of every level and direction and, when the cycle
+    // runs in FP64, the factored partition tables of the FP64 smoother
     auto factor = [&](Level &L, bool fp64_level) -> int {
         for (int a = 0; a < c.nd; ++a) {
             FactorArgs<double> fa;
@@ -1156,7 +1127,7 @@ int fsi_mg_set_geometry(void *handle, const int8_t *iblank, const int8_t *ghostC
     const bool all64 = (c.p.precision_mode == 0);
     TRY(factor(c.L1, all64));
     for (int d = 0; d < c.nd; ++d)
-        for (int l = 2; l <= c.nlev[d]; ++l) TRY(factor(c.C[d][l], all64 || (l == c.nlev[d] && !c.coarsest_fp32)));
+        for (int l = 2; l <= c.nlev[d]; ++l) TRY(factor(c.C[d][l], all64));
     // ghost gather list: linear indices in the level-1 layout; the ghost's own
     // stencil entry carries uNormal (0) and is marked -1.
     static const int incI[8] = {0, 0, 1, 1, 0, 0, 1, 1}, incJ[8] = {0, 1, 1, 0, 0, 1, 1, 0},
@@ -1370,7 +1341,7 @@ int fsi_mg_subtract_average_noalloc(double *d_pPrime, const int8_t *d_iblank, co
     d.m[0] = nx; d.m[1] = ny; d.m[2] = nz;
     d.sx = nx + 2;
     d.sxy = (long long)(nx + 2) * (ny + 2);
-    // iblank is 0 or 1, so the array serves directly as the flag byte (bit 0 = iblank)
+    // the kernels read d_iblank as it is: a cell is blanked where it is non-zero
     const cudaError_t e = launch_subtract_average_noalloc(d_pPrime, reinterpret_cast<const uint8_t *>(d_iblank),
                                                           d_dx, d_dy, d_dz, d, static_cast<cudaStream_t>(stream));
     if (e != cudaSuccess)
@@ -1561,6 +1532,7 @@ int fsi_mg_time_kernel(void *handle, int which, int precision, int reps, double 
         launch_convert_d2f(c.e32, p, n1, c.s);
         launch_convert_d2f(c.r32, b, n1, c.s);
     }
+    double dfma_flops = 0.0;
     auto once = [&]() {
         if (which >= 0 && which <= 2) {
             if (which >= c.nd) return;
@@ -1606,6 +1578,8 @@ int fsi_mg_time_kernel(void *handle, int which, int precision, int reps, double 
             launch_update_pressure(c.last_up_p, c.last_up_pp, c.L1.d.sxy * (c.nz + 2), c.last_up_vk, c.s);
         } else if (which == 9 && c.have_ad) {
             launch_rhs_advec_diff(c.last_ad, c.s);
+        } else if (which == 10) {
+            dfma_flops = launch_dfma_peak(c.stage, c.s);
         }
     };
     if ((which == 6 && !c.have_fv) || (which == 7 && !c.have_cv) || (which == 8 && !c.have_up) ||
@@ -1651,7 +1625,7 @@ int fsi_mg_time_kernel(void *handle, int which, int precision, int reps, double 
             for (int q = 0; q < 9; ++q) bpc += A.bc[q] ? 8.0 : 0.0;
             for (int q = 0; q < 3; ++q) bpc += A.bcvisc[q] ? 8.0 : 0.0;
         }
-        *alg_bytes = bpc * cells;
+        *alg_bytes = (which == 10) ? dfma_flops : bpc * cells;
     }
     return 0;
 }

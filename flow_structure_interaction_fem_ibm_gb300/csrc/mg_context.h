@@ -117,8 +117,7 @@ struct Ctx {
     int step_cap = 0;
     double *vtilde = nullptr;   // uTilde, vTilde, wTilde of the VAN_KAN face_vel (allocated on first use)
     double *zg_div = nullptr;   // divergence scratch of the face_vel inside solve_ad (zero-gradient sides, GCM)
-    bool coarsest_fp32 = true;   // mixed form: the coarsest level is smoothed in FP32 like the others
-    double ghost32_reltol = 1.0e-6;   // FP32 ghost rows stop at max|dp| <= this x max|p_g| (FSI_MG_GHOST32_RELTOL)
+    double ghost32_reltol = 1.0e-6;   // FP32 ghost rows stop at max|dp| <= this x max|p_g|
     // ghost-cell velocities (GCM_vel_set_bc_internal), registered by fsi_mg_set_velocity_ghosts
     bool vg_on = false;
     int vg_cap = 0;

@@ -3,6 +3,7 @@
 #include "device_util.cuh"
 
 #include <cfloat>
+#include <cuda.h>   // driver API types (CUcontext) for the no-alloc scratch lookup
 #include <mutex>
 #include <cooperative_groups.h>
 
@@ -1296,6 +1297,12 @@ __global__ void __launch_bounds__(TPB) k_avg_partial(const double *p, const uint
     if (threadIdx.x == 0) { partials[2 * blockIdx.x] = a; partials[2 * blockIdx.x + 1] = b; }
 }
 
+// IBLANK_BYTE: fl is a plain iblank array (blanked where non-zero) instead of
+// the flag byte (blanked where bit 0 is set).
+template <bool IBLANK_BYTE>
+__device__ __forceinline__ bool avg_blanked(uint8_t f) { return IBLANK_BYTE ? (f != 0) : ((f & FB_IB) != 0); }
+
+template <bool IBLANK_BYTE>
 __global__ void __launch_bounds__(TPB) k_avg_apply(double *p, const uint8_t *fl, Dims d, const double *sums)
 {
     // one block per row (j, k); dead cells (iblank = 1) are zeroed (IBM/CORE_POISSON.F90:447-457)
@@ -1307,7 +1314,7 @@ __global__ void __launch_bounds__(TPB) k_avg_apply(double *p, const uint8_t *fl,
     const long long rb = d.idx(0, j, k);
     const double pAvg = s_avg;
     for (int i = 1 + threadIdx.x; i <= n0; i += blockDim.x)
-        p[rb + i] = (fl[rb + i] & FB_IB) ? 0.0 : p[rb + i] - pAvg;
+        p[rb + i] = avg_blanked<IBLANK_BYTE>(fl[rb + i]) ? 0.0 : p[rb + i] - pAvg;
 }
 
 // Fresh cells of a moving body (IBM/CORE_POISSON.F90:459-488): the mean of
@@ -1645,8 +1652,9 @@ __global__ void k_coarse_flags(uint8_t *fl, Dims d, int sb0, int sb1, int sb2, i
 static __device__ __align__(256) double g_noalloc_scratch[2 * NOALLOC_MAX_ROWS + 8];
 
 // One block per (j, k) row: the row's volume-weighted pressure sum and fluid
-// volume (the per-cell terms of IBM/CORE_POISSON.F90:430-440).
-__global__ void __launch_bounds__(TPB) k_avg_partial_rows(const double *p, const uint8_t *fl, const double *dx,
+// volume (the per-cell terms of IBM/CORE_POISSON.F90:430-440).  ib is the
+// caller's iblank array: a cell counts as fluid where it is zero.
+__global__ void __launch_bounds__(TPB) k_avg_partial_rows(const double *p, const uint8_t *ib, const double *dx,
                                                           const double *dy, const double *dz, Dims d,
                                                           double *partials)
 {
@@ -1657,7 +1665,7 @@ __global__ void __launch_bounds__(TPB) k_avg_partial_rows(const double *p, const
     const long long rb = d.idx(0, j, k);
     double sp = 0.0, sv = 0.0;
     for (int i = 1 + threadIdx.x; i <= n0; i += blockDim.x) {
-        if (fl[rb + i] & FB_IB) continue;
+        if (ib[rb + i] != 0) continue;
         const double vol = dx[i] * dyz;
         sp += p[rb + i] * vol;
         sv += vol;
@@ -1802,8 +1810,6 @@ void wpf_setup_dir(const FactorArgs<double> &a, double *tab, int L, long long nl
 
 int wp_S(int L) { return L <= 32 ? 1 : L <= 64 ? 2 : L <= 128 ? 4 : L <= 256 ? 8 : 16; }
 
-bool g_line_thread_per_line = false;   // selects the sequential-Thomas kernel (kept for lines > 512 cells)
-
 template <typename T>
 void launch_line(int dir, const LineArgs<T> &a, bool omega_one, cudaStream_t s)
 {
@@ -1811,8 +1817,8 @@ void launch_line(int dir, const LineArgs<T> &a, bool omega_one, cudaStream_t s)
     const int nb = a.d.m[ob[dir]] - 1, nc = a.d.m[oc[dir]] - 1;
     const long long n = (long long)((nb + 1) / 2) * nc;
     const int L = a.d.m[dir] - 1;
-    if (!g_line_thread_per_line && L > 16 && L <= 512 && launch_factored<T>(dir, a, L, n, omega_one, s)) return;
-    if (!g_line_thread_per_line && L > 16 && L <= 512) {   // short lines: one thread per line is cheaper
+    if (L > 16 && L <= 512 && launch_factored<T>(dir, a, L, n, omega_one, s)) return;
+    if (L > 16 && L <= 512) {   // short lines: one thread per line is cheaper
         bool ok;
         if (omega_one) {
             ok = (dir == 0) ? launch_wp_dir<T, 0, true>(a, L, n, s)
@@ -1824,7 +1830,7 @@ void launch_line(int dir, const LineArgs<T> &a, bool omega_one, cudaStream_t s)
         if (ok) return;
     }
     const int g = nblk(n);
-    if (!g_line_thread_per_line && L <= 16) {
+    if (L <= 16) {
 #define S_(D, LM, O) k_line_short<T, D, LM, O><<<g, TPB, 0, s>>>(a)
 #define SD_(LM, O) do { if (dir == 0) S_(0, LM, O); else if (dir == 1) S_(1, LM, O); else S_(2, LM, O); } while (0)
         if (omega_one) {
@@ -1952,7 +1958,7 @@ void launch_subtract_average(double *p, const uint8_t *fl, const double *dx, con
     double *sums = partials + 2LL * nblocks;
     k_sum_final<<<1, 1024, 0, s>>>(partials, nblocks, 2, sums);
     const int rows = (d.m[1] - 1) * (d.m[2] - 1);
-    k_avg_apply<<<rows, TPB, 0, s>>>(p, fl, d, sums);
+    k_avg_apply<false><<<rows, TPB, 0, s>>>(p, fl, d, sums);
 }
 
 void launch_fresh_cells(double *p, const uint8_t *fl, const uint8_t *fresh, const Dims &d, bool three_d,
@@ -2121,7 +2127,6 @@ cudaError_t init_kernels()
     return fp_attr_dir<2>();
 }
 
-void set_line_kernel(int thread_per_line) { g_line_thread_per_line = thread_per_line != 0; }
 
 // explicit instantiations
 template void launch_line<double>(int, const LineArgs<double> &, bool, cudaStream_t);
@@ -2140,25 +2145,63 @@ template void launch_fill<double>(double *, long long, double, cudaStream_t);
 template void launch_fill<float>(float *, long long, float, cudaStream_t);
 template void launch_fill<uint8_t>(uint8_t *, long long, uint8_t, cudaStream_t);
 
-// Device address of g_noalloc_scratch on the current device, looked up once
-// per device with that device current (host code cannot use the symbol's name
-// as a device pointer).
+// Unique id of the calling thread's current CUDA context (driver API entry
+// points resolved through the runtime, so the library needs no link against
+// libcuda).  *have is false while no context is current yet.
+cudaError_t current_context_id(unsigned long long *id, bool *have)
+{
+    using GetCurrent = CUresult (*)(CUcontext *);
+    using GetId = CUresult (*)(CUcontext, unsigned long long *);
+    static GetCurrent get_current = nullptr;
+    static GetId get_id = nullptr;
+    static cudaError_t lookup = cudaSuccess;
+    static std::once_flag once;
+    std::call_once(once, [] {
+        cudaDriverEntryPointQueryResult q1 = cudaDriverEntryPointSymbolNotFound, q2 = q1;
+        lookup = cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", (void **)&get_current, 12000, cudaEnableDefault, &q1);
+        if (lookup == cudaSuccess)
+            lookup = cudaGetDriverEntryPointByVersion("cuCtxGetId", (void **)&get_id, 12000, cudaEnableDefault, &q2);
+        if (lookup == cudaSuccess && (q1 != cudaDriverEntryPointSuccess || q2 != cudaDriverEntryPointSuccess))
+            lookup = cudaErrorNotSupported;
+    });
+    if (lookup != cudaSuccess) return lookup;
+    CUcontext ctx = nullptr;
+    if (get_current(&ctx) != CUDA_SUCCESS) return cudaErrorDeviceUninitialized;
+    *have = (ctx != nullptr);
+    if (!ctx) return cudaSuccess;
+    return get_id(ctx, id) == CUDA_SUCCESS ? cudaSuccess : cudaErrorDeviceUninitialized;
+}
+
+// Device address of g_noalloc_scratch in the current context, looked up once
+// per device and context with that device current (host code cannot use the
+// symbol's name as a device pointer).  The cache is keyed on the context's
+// unique id, so a context destroyed and re-created (cudaDeviceReset, or a host
+// that tears its context down) gets a fresh lookup instead of a stale address.
 cudaError_t noalloc_scratch(double **out)
 {
+    struct Entry { unsigned long long ctx = 0; double *addr = nullptr; };
     static std::mutex mu;
-    static double *addr[NOALLOC_MAX_DEVICES] = {};
+    static Entry cache[NOALLOC_MAX_DEVICES];
     int dev = 0;
     cudaError_t e = cudaGetDevice(&dev);
     if (e != cudaSuccess) return e;
     if (dev < 0 || dev >= NOALLOC_MAX_DEVICES) return cudaErrorInvalidDevice;
+    unsigned long long id = 0;
+    bool have = false;
+    if ((e = current_context_id(&id, &have)) != cudaSuccess) return e;
     std::lock_guard<std::mutex> lock(mu);
-    if (!addr[dev]) {
-        void *q = nullptr;
-        e = cudaGetSymbolAddress(&q, g_noalloc_scratch);
-        if (e != cudaSuccess) return e;
-        addr[dev] = static_cast<double *>(q);
+    if (have && cache[dev].addr && cache[dev].ctx == id) {
+        *out = cache[dev].addr;
+        return cudaSuccess;
     }
-    *out = addr[dev];
+    void *q = nullptr;
+    e = cudaGetSymbolAddress(&q, g_noalloc_scratch);   // also makes the primary context current if none was
+    if (e != cudaSuccess) return e;
+    if ((e = current_context_id(&id, &have)) != cudaSuccess) return e;
+    if (!have) return cudaErrorDeviceUninitialized;
+    cache[dev].ctx = id;
+    cache[dev].addr = static_cast<double *>(q);
+    *out = cache[dev].addr;
     return cudaSuccess;
 }
 
@@ -2173,8 +2216,40 @@ cudaError_t launch_subtract_average_noalloc(double *p, const uint8_t *fl, const 
     double *sums = scr + 2 * NOALLOC_MAX_ROWS;
     k_avg_partial_rows<<<rows, TPB, 0, s>>>(p, fl, dx, dy, dz, d, scr);
     k_sum_final<<<1, 1024, 0, s>>>(scr, rows, 2, sums);
-    k_avg_apply<<<rows, TPB, 0, s>>>(p, fl, d, sums);
+    k_avg_apply<true><<<rows, TPB, 0, s>>>(p, fl, d, sums);
     return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------------------
+// FP64 pipe roof: independent DFMA chains per thread, nothing read or written
+// but one guarded store that keeps the chains live.  No reference counterpart;
+// it measures the denominator of the FP64 kernels' pipe fraction.
+// ---------------------------------------------------------------------------
+constexpr int DFMA_CHAINS = 4;
+
+__global__ void __launch_bounds__(256) k_dfma_peak(double *out, int iters, double a, double b)
+{
+    double x[DFMA_CHAINS];
+#pragma unroll
+    for (int q = 0; q < DFMA_CHAINS; ++q) x[q] = 1e-3 * (threadIdx.x + q);
+    for (int it = 0; it < iters; ++it) {
+#pragma unroll
+        for (int q = 0; q < DFMA_CHAINS; ++q) x[q] = fma(x[q], a, b);
+    }
+    double acc = 0.0;
+#pragma unroll
+    for (int q = 0; q < DFMA_CHAINS; ++q) acc += x[q];
+    if (acc == -1.0) out[0] = acc;   // never true for these inputs; the compiler cannot drop the chains
+}
+
+double launch_dfma_peak(double *out, cudaStream_t s)
+{
+    int dev = 0, sms = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    const int blocks = 8 * sms, threads = 256, iters = 4096;
+    k_dfma_peak<<<blocks, threads, 0, s>>>(out, iters, 0.999999, 1e-6);
+    return 2.0 * DFMA_CHAINS * (double)iters * (double)blocks * threads;
 }
 
 } // namespace fsimg

@@ -202,11 +202,11 @@ void launch_vel_ghosts(double *u, double *v, double *w, const GhostArgs &g, cons
                        unsigned long long *d_maxdelta, cudaStream_t s);
 // update_pressure without its ghost rows (IBM/CORE_FRAC_STEP_ROUTINES.F90:949-967)
 void launch_update_pressure(double *p, const double *pPrime, long long n, bool van_kan, cudaStream_t s);
+// FP64 pipe roof: launches the DFMA-throughput kernel, returns its FP64 flops per launch
+double launch_dfma_peak(double *out, cudaStream_t s);
 
 // one-time kernel attributes (call before the first launch, outside stream capture)
 cudaError_t init_kernels();
-// 0: warp-per-line partition solver (default, lines up to 512 cells), 1: one thread per line
-void set_line_kernel(int thread_per_line);
 
 // ---- launchers (all asynchronous on the given stream) ----
 template <typename T>

@@ -106,19 +106,25 @@ int fsi_mg_calc_residual(void *handle, const double *var, const double *r, doubl
  * fresh cells registered with fsi_mg_set_fresh_cells. */
 int fsi_mg_subtract_average(void *handle, double *pPrime);
 
-/* The same mean removal on device arrays, for callers that cannot allocate
- * GPU memory (a host code whose device memory is owned by its own pool, or a
+/* The mean removal on device arrays, for callers that cannot allocate GPU
+ * memory (a host code whose device memory is owned by its own pool, or a
  * time loop that must not pay cudaMalloc's implicit device synchronisation).
  * No counterpart in the reference.  It needs no handle and allocates nothing:
  * its partial sums live in a fixed device array of the library, one slot per
  * (j,k) row, so grids with (ny-1)*(nz-1) > 65536 rows are rejected (status
- * -1, message in fsi_mg_last_error).  d_pPrime (in/out) and d_iblank (0 or 1)
- * use the full (0:nx+1,0:ny+1,0:nz+1) layout; d_dx, d_dy, d_dz hold the cell
- * widths dx(0:nx+1) etc.  Work is queued on `stream` (a cudaStream_t, NULL
- * for the default stream) and the call returns without waiting.  The first
- * call on a device looks up the device address of that array; make this
- * first call before any stream capture.  All calls share the array, so calls
- * that can overlap on the GPU (other streams, host threads) race. */
+ * -1, message in fsi_mg_last_error).  d_pPrime (in/out) and d_iblank use the
+ * full (0:nx+1,0:ny+1,0:nz+1) layout; d_dx, d_dy, d_dz hold the cell widths
+ * dx(0:nx+1) etc.  d_iblank must hold 0 or 1 as the reference's iblank does:
+ * it is not validated (that would need a copy to the host), and a cell counts
+ * as blanked wherever it is non-zero.  Unlike fsi_mg_subtract_average it does
+ * not set fresh cells of a moving body to their neighbours' mean
+ * (IBM/CORE_POISSON.F90:459-488): callers with a moving body use the handle
+ * entry point.  Work is queued on `stream` (a cudaStream_t, NULL for the
+ * default stream) and the call returns without waiting.  The first call in a
+ * CUDA context looks up the device address of that array (again after a
+ * cudaDeviceReset or a re-created context); make that call before any stream
+ * capture.  All calls share the array, so calls that can overlap on the GPU
+ * (other streams, host threads) race. */
 int fsi_mg_subtract_average_noalloc(double *d_pPrime, const int8_t *d_iblank, const double *d_dx, const double *d_dy,
                                     const double *d_dz, int ndim, int nx, int ny, int nz, void *stream);
 
@@ -313,7 +319,9 @@ int fsi_mg_residual_history(void *handle, double *out, int cap);
  * 6/7/8 the kernels of the last fsi_mg_face_vel_rhs / fsi_mg_correct_vel /
  * fsi_mg_update_pressure call replayed on its arrays (correct_vel and the
  * VAN_KAN update_pressure then apply their update reps+1 more times; the
- * ghost-cell rows of update_pressure are not replayed).
+ * ghost-cell rows of update_pressure are not replayed), 9 the kernel of the last
+ * fsi_mg_rhs_advec_diff call, 10 the FP64 pipe roof (independent DFMA chains on
+ * every SM, no memory traffic; alg_bytes then receives its FP64 flops per launch).
  * precision 0 FP64, 1 FP32 (0-5 only).  alg_bytes (may be NULL) receives the algorithmic
  * bytes one launch moves.  No counterpart in the reference: a measurement hook. */
 int fsi_mg_time_kernel(void *handle, int which, int precision, int reps, double *avg_ms, double *alg_bytes);

@@ -34,32 +34,46 @@ def _host(t):
     return t.cpu().numpy().transpose()
 
 
-def _noalloc(lib, pr, p_dev, ib_dev, dx_dev, dy_dev, dz_dev):
+def _noalloc(lib, pr, p_dev, ib_dev, dx_dev, dy_dev, dz_dev, stream=None):
     import torch
     prm = pr.params
+    st = stream if stream is not None else torch.cuda.current_stream()
     rc = lib.fsi_mg_subtract_average_noalloc(
         ctypes.c_void_p(p_dev.data_ptr()), ctypes.c_void_p(ib_dev.data_ptr()),
         ctypes.c_void_p(dx_dev.data_ptr()), ctypes.c_void_p(dy_dev.data_ptr()),
         ctypes.c_void_p(dz_dev.data_ptr()), prm.ndim, prm.nx, prm.ny, prm.nz,
-        ctypes.c_void_p(torch.cuda.current_stream().cuda_stream))
+        ctypes.c_void_p(st.cuda_stream))
     assert rc == 0, lib.fsi_mg_last_error().decode()
     torch.cuda.synchronize()
 
 
-@pytest.mark.parametrize("case", ["sphere16_tanh", "box2d_32"])
-def test_noalloc_mean_removal_matches_handle_entry_point(gpu_built, case):
+def _case(name):
+    if name == "sphere16_tanh":
+        return P.sphere(16, seed=2, stretch=1.5)
+    if name == "box2d_32":
+        return P.box2d(32, seed=9)
+    # the largest grid the fixed scratch accepts: (ny-1)*(nz-1) = 256*256 = 65536 rows
+    return P.box3d((2, 256, 256), seed=4, stretch=1.5)
+
+
+@pytest.mark.parametrize("case,own_stream", [("sphere16_tanh", False), ("box2d_32", False),
+                                             ("sphere16_tanh", True), ("rows65536", True)])
+def test_noalloc_mean_removal_matches_handle_entry_point(gpu_built, case, own_stream):
+    import torch
     lib = gpu_built
-    pr = P.sphere(16, seed=2, stretch=1.5) if case == "sphere16_tanh" else P.box2d(32, seed=9)
+    pr = _case(case)
     s = PoissonSolver(pr.params, pr.x, pr.y, pr.z).set_boundary(pr.geom)
     ib_dev = _dev(pr.geom.iblank, np.int8)
     dx_dev, dy_dev, dz_dev = (_dev(Metrics(c).dx, np.float64) for c in (pr.x, pr.y, pr.z))
+    stream = torch.cuda.Stream() if own_stream else None   # a freshly created non-default stream
     rng = np.random.default_rng(21)
     try:
         for call in range(2):   # two calls in a row share the library's scratch array
             p = np.asfortranarray(rng.standard_normal(pr.shape) + 3.0 * call)
             ref = s.subtracting_average_pressure(p.copy(order="F"))
             p_dev = _dev(p, np.float64)
-            _noalloc(lib, pr, p_dev, ib_dev, dx_dev, dy_dev, dz_dev)
+            torch.cuda.synchronize()
+            _noalloc(lib, pr, p_dev, ib_dev, dx_dev, dy_dev, dz_dev, stream)
             got = _host(p_dev)
             assert np.abs(got - ref).max() < TOL, (call, np.abs(got - ref).max())
     finally:
