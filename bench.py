@@ -14,8 +14,14 @@ form is timed on the same inputs and reported beside it.
   e2e    : solves/s through fsi_mg_solve with pinned HOST buffers, the H2D of
            pPrime and nlu0 and the D2H of pPrime inside the timed region.
   --impl reference : the reference MG algorithm (the C restatement in oracle/,
-           serial like the reference) on all host cores as independent
-           replicas, bounded sample per step.
+           serial like the reference, its own line order) timed on complete
+           solves of the 128^3 config-2 workload, K solves as concurrent
+           single-threaded replicas on the host cores.
+  cpu_baseline : one complete 128^3 config-2 solve of the same oracle on one
+           core, in the same run as the GPU's config-2 solves (config2 block:
+           solves/s of four GPU forms, the timed ratios, and the parity of the
+           converged pressures); a 256^3 figure is only reported as a labelled
+           model (reference_model_256).
 
 Multi-GPU: the path does not shard (replicas only); each rank runs its own
 replica and value is the sum over ranks.
@@ -211,35 +217,72 @@ REFERENCE_ITERATIONS = {
 }
 
 
-def reference_iterations(n, seed, tol):
-    key = (n, seed, tol)
-    if key in REFERENCE_ITERATIONS:
-        return REFERENCE_ITERATIONS[key]
-    if n > 64:
-        raise SystemExit(f"no reference iteration count recorded for n={n}, seed={seed}, tol={tol:g}")
+def _oracle_complete_solve(params_blob, x, y, z, geom, nlu0):
+    """One complete solve_poisson of the oracle (serial C restatement of the
+    reference MG, the reference's own lexicographic line order, iRedBlack 0)
+    from pPrime = 0, timed end to end on this process's core."""
     from flow_structure_interaction_fem_ibm_gb300 import problem as P
     from oracle.oracle import Oracle
-    pr = P.sphere(n, seed=seed, stretch=1.5)
-
-    def stagnated(f):
-        q = P.Problem(pr.params, pr.x, pr.y, pr.z, pr.geom, f, pr.name)
-
-        def solve_from_zero(rhs, iters):
-            q.nlu0 = rhs
-            r = Oracle(q, iterMax_Poisson=iters, restol_Poisson=0.0).solve()
-            return r["p"], r["hist"]
-
-        return P.stall_until_plateau(solve_from_zero, f)
-
-    P.make_compatible(pr, stagnated)
-    pr.params.restol_Poisson = tol * float(np.abs(pr.nlu0).max())
-    pr.params.iterMax_Poisson = 4000
-    return Oracle(pr).solve()["iters"], "oracle solve to convergence at this size"
+    pr = P.Problem(params_blob, x, y, z, geom, nlu0, "oracle_complete")
+    pr.params.iRedBlack, pr.params.coarse_flag_mode = 0, 0
+    t0 = time.perf_counter()
+    o = Oracle(pr)
+    t1 = time.perf_counter()
+    r = o.solve()
+    t2 = time.perf_counter()
+    o.close()
+    return {"p": r["p"], "status": r["status"], "iters": r["iters"], "maxres": r["maxres"],
+            "setup_s": t1 - t0, "solve_s": t2 - t1}
 
 
-def _replica(args):
-    n, seed = args
-    return oracle_iteration_time(n, seed)
+def _oracle_worker(inbox, outbox):
+    """Spawned before the first GPU call: runs the oracle jobs the main process
+    sends (the CPU side of the same run) on its own core."""
+    while True:
+        job = inbox.get()
+        if job is None:
+            return
+        kind, payload = job
+        try:
+            if kind == "complete":
+                outbox.put((kind, _oracle_complete_solve(*payload)))
+            elif kind == "iteration":
+                n, seed = payload
+                oracle_iteration_time(n, seed)   # builds the oracle state (not timed)
+                outbox.put((kind, {"n": n, "seconds": oracle_iteration_time(n, seed)}))
+        except Exception as e:   # reported in the bench line, never hides a GPU result
+            outbox.put((kind, {"error": repr(e)}))
+
+
+class OracleJobs:
+    """Two spawned CPU workers (one core each) for the oracle work that runs
+    beside the GPU benchmark: the complete 128^3 solve and one 256^3 outer
+    iteration."""
+
+    def __init__(self, n_workers=2):
+        import multiprocessing as mp
+        ctx = mp.get_context("spawn")
+        self.workers = []
+        for _ in range(n_workers):
+            inbox, outbox = ctx.Queue(), ctx.Queue()
+            proc = ctx.Process(target=_oracle_worker, args=(inbox, outbox), daemon=True)
+            proc.start()
+            self.workers.append((proc, inbox, outbox))
+
+    def submit(self, w, kind, payload):
+        self.workers[w][1].put((kind, payload))
+
+    def result(self, w, timeout=None):
+        kind, res = self.workers[w][2].get(timeout=timeout)
+        return res
+
+    def close(self):
+        for proc, inbox, _ in self.workers:
+            inbox.put(None)
+        for proc, _, _ in self.workers:
+            proc.join(timeout=10)
+            if proc.is_alive():
+                proc.terminate()
 
 
 def profile_traffic(n):
@@ -253,37 +296,106 @@ def profile_traffic(n):
     return float(m.group(1)) if m else None
 
 
+# Discrete compatibility shifts of the config-2 workload (128^3 stretched
+# sphere, seed 2), as this benchmark's GPU plateau solves compute them (the
+# value its own line prints as config2.compat_shift).  The reference arm runs
+# no GPU code, so it takes the shift from here; the shift is a property of the
+# discrete operator and the right-hand side, not of the solver.
+CONFIG2_SHIFT = {1e-8: -0.00035806123334163623}
+
+
+def config2_problem(tol, shift=None, solver_cls=None):
+    """Config 2: 128^3 [0,1]^3 tanh-stretched (beta 1.5) with the r = 0.15
+    ghost-cell sphere, Gaussian |k| <= 8 right-hand side (seed 2), mean
+    removed and made discretely compatible, restol = tol max|nlu0|."""
+    from flow_structure_interaction_fem_ibm_gb300 import problem as P
+    if shift is None:
+        pr, shift = build_problem(128, 2, tol, solver_cls)
+        return pr, shift
+    pr = P.sphere(128, seed=2, stretch=1.5)
+    pr.nlu0 += shift * P.fluid_indicator(pr)
+    pr.params.restol_Poisson = tol * float(np.abs(pr.nlu0).max())
+    pr.params.iterMax_Poisson = 2000
+    return pr, shift
+
+
+def _reference_replica(job):
+    """One replica of the reference arm: warm-up outer iterations (untimed),
+    then its share of the complete solves, each timed end to end."""
+    tol, shift, warm_iters, nsolve, ready, start_evt = job
+    from oracle.oracle import Oracle
+    pr, _ = config2_problem(tol, shift)
+    pr.params.iRedBlack, pr.params.coarse_flag_mode = 0, 0
+    if warm_iters > 0:
+        q = copy.deepcopy(pr)
+        q.params.iterMax_Poisson, q.params.restol_Poisson = warm_iters, 0.0
+        Oracle(q).solve()
+    o = Oracle(pr)   # MG_initial and the geometry hand-over happen once, outside the timed solves
+    ready.put(1)
+    start_evt.wait()
+    out = []
+    for _ in range(nsolve):
+        t0 = time.perf_counter()
+        r = o.solve()
+        out.append({"seconds": time.perf_counter() - t0, "iters": r["iters"], "status": r["status"],
+                    "end": time.time()})
+    o.close()
+    return out
+
+
 def run_reference(args, rank, world):
+    """The reference arm: the oracle (serial C restatement of the reference's
+    MG, its own lexicographic line order) timed on complete solves of the
+    config-2 workload on the host cores.  The K timed steps are K complete
+    solves run as concurrent single-threaded replicas (at most one process per
+    solve); value = K / wall time of the timed region."""
     if rank != 0:
         print(json.dumps({"impl": "reference", "rank": rank, "skipped": True}), file=sys.stderr)
         return
-    cores = os.cpu_count() or 1
-    sample_n = min(args.n, 128)
-    iters, src = reference_iterations(args.n, args.seed, args.tol)
-    scale = (args.n / sample_n) ** 3
-    t0 = time.perf_counter()
     import multiprocessing as mp
+    cores = os.cpu_count() or 1
+    key = args.tol
+    if key not in CONFIG2_SHIFT:
+        print(json.dumps({"impl": "reference", "unavailable": f"no recorded compatibility shift for tol {key:g}"}))
+        return
+    shift = CONFIG2_SHIFT[key]
+    nproc = max(1, min(args.steps, 2 * cores))
+    share = [args.steps // nproc + (1 if i < args.steps % nproc else 0) for i in range(nproc)]
     ctx = mp.get_context("spawn")
-    vals = []
-    with ctx.Pool(cores) as pool:
-        for s in range(args.warmup + args.steps):
-            per_core = pool.map(_replica, [(sample_n, args.seed)] * cores)
-            t_iter = float(np.mean(per_core)) * scale
-            if s >= args.warmup:
-                vals.append(cores / (t_iter * iters))
-    value = float(np.median(vals))
+    t_all = time.perf_counter()
+    with ctx.Manager() as mgr:
+        start, ready = mgr.Event(), mgr.Queue()
+        with ctx.Pool(nproc) as pool:
+            res = pool.map_async(_reference_replica,
+                                 [(args.tol, shift, args.warmup, k, ready, start) for k in share])
+            # every replica builds its state and runs its warm-up iterations, then waits for the start
+            for _ in range(nproc):
+                ready.get(timeout=1200)
+            t0 = time.time()
+            start.set()
+            runs = [r for part in res.get() for r in part]
+    wall = max(r["end"] for r in runs) - t0
+    ok = all(r["status"] == 0 for r in runs)
+    value = args.steps / wall
+    per = [r["seconds"] for r in runs]
     out = {
         "impl": "reference", "metric": METRIC, "value": value, "unit": "solves/s", "n_gpus": args.gpus,
-        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 / value * cores,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * wall / args.steps,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": {"workload": f"sphere_{args.n}^3_tanh1.5_r0.15_tol{args.tol:g}", "grid": args.n,
-                   "tol": args.tol, "parallelism": f"{cores} independent serial replicas"},
-        "cpu_baseline": {"value": value, "unit": "solves/s", "cores": cores, "kind": "port",
-                         "sample": (f"one outer iteration (MG_Solver + GCM_correct_pressure + calc_residual) at "
-                                    f"{sample_n}^3 per core, scaled by cell count to {args.n}^3, times the "
-                                    f"reference's stationary iteration count {iters} ({src})")},
+        "config": {"workload": f"sphere_128^3_tanh1.5_r0.15_seed2_tol{args.tol:g} (config 2)", "grid": 128,
+                   "tol": args.tol, "compat_shift": shift,
+                   "parallelism": f"{nproc} concurrent single-threaded replicas on {cores} host cores",
+                   "same_config_as_gpu_arm": False,
+                   "why": "a complete 256^3 solve of the reference takes hours on one core; the GPU arm's "
+                          "line carries its own 128^3 config-2 solves timed beside one complete oracle solve"},
+        "cpu_baseline": {"value": value, "unit": "solves/s", "cores": min(nproc, cores), "kind": "port",
+                         "sample": (f"{args.steps} complete solve_poisson runs of the 128^3 config-2 workload "
+                                    f"(oracle, reference line order, tol {args.tol:g}) as concurrent replicas; "
+                                    f"warm-up: {args.warmup} outer iterations per replica, untimed")},
         "e2e": {"value": value, "unit": "solves/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
-        "wall_s": time.perf_counter() - t0,
+        "solve_seconds": {"min": min(per), "median": float(np.median(per)), "max": max(per)},
+        "iters": sorted({r["iters"] for r in runs}), "all_converged": ok,
+        "wall_s": time.perf_counter() - t_all,
     }
     print(json.dumps(out))
 
@@ -384,6 +496,10 @@ def projection_steps(solver, pr, peak, reps=20):
     gbs = nb / (ms * 1e-3) / 1e9
     out["rhs_advec_diff_cn"] = {"device_us": 1e3 * ms, "alg_bytes": nb, "achieved_gbs": gbs, "frac": gbs / peak}
     del visc, nl
+    # FP64 pipe roof on this GPU: independent DFMA chains on every SM (CUDA events, no settings changed)
+    ms, flops = solver.time_kernel(10, 0, 10)
+    out["fp64_roof"] = {"tflops": flops / (ms * 1e-3) / 1e12, "ms": ms, "flops_per_launch": flops,
+                        "method": "k_dfma_peak: 4 independent DFMA chains x 4096 per thread, 8 CTAs of 256 per SM"}
     out["note"] = ("device_us: the routine's kernels (face_vel_rhs: shell zeroing, [uTilde], faces+divergence, "
                    "sum) replayed 20x; alg_bytes: FP64 fields read/written once per interior cell, no bc arrays; "
                    "update_pressure without its ghost-cell rows")
@@ -527,6 +643,13 @@ def channel_rollout(steps, cells=(192, 128, 128), krylov=30, warmup=2, restol=1e
     div = ((fu[K, J, 2:n[0] + 2] - fu[K, J, I]) * dinv[0][I].view(1, 1, -1)
            + (fv[K, 2:n[1] + 2, I] - fv[K, J, I]) * dinv[1][J].view(1, -1, 1)
            + (fw[2:n[2] + 2, J, I] - fw[K, J, I]) * dinv[2][K].view(-1, 1, 1)) * fl
+    # the outflow cell layer (i = nx-1) carries div = -dt nlw0: its faces keep the zero-gradient
+    # set_bc values while nlw0 adds the outflow pressure-gradient planes to the Poisson rows
+    adiv = div.abs()
+    am = int(torch.argmax(adiv))
+    kk, rem = divmod(am, n[1] * n[0])
+    jj, ii = divmod(rem, n[0])
+    closure = (div + dt * fs.nlw0[K, J, I] * fl).abs()
     u = fs.vel[0]
     out = {"profile": "channel_rollout",
            "workload": f"channel_{n[0]}x{n[1]}x{n[2]}_[0,6]x[0,4]^2_sphere_d1_at_(1.5,2,2)_Re{re:g}_dt{dt:g}_CN_"
@@ -535,7 +658,14 @@ def channel_rollout(steps, cells=(192, 128, 128), krylov=30, warmup=2, restol=1e
            "stage_ms": stage["ms"], "poisson_iters": [r["poisson_iters"] for r in recs],
            "ad_iters": [r["ad_iters"] for r in recs],
            "statuses_ok": all(r["poisson_status"] == 0 and r["ad_status"] == 0 for r in recs),
-           "max_abs_div_after_correction": float(div.abs().max()), "restol_Poisson": restol,
+           "max_abs_div_after_correction": float(adiv.max()),
+           "argmax_div_cell": [ii + 1, jj + 1, kk + 1],
+           "max_abs_div_outside_outflow_layer": float(adiv[:, :, :-1].max()),
+           "max_abs_div_plus_dt_nlw0": float(closure.max()),
+           "divergence_note": "the maximum sits in the outflow cell layer, where div(face) = -dt nlw0 (the "
+                              "reference's own chain gives the same, to 1e-12); div + dt nlw0 is the projection's "
+                              "residual everywhere",
+           "restol_Poisson": restol,
            "u_max": float(u.abs().max()), "time": fs.time, "ghost_cells": int(pr.geom.nGhost),
            "device_bytes_in_use": int(free0 - free1), "torch_peak_bytes": int(torch.cuda.max_memory_allocated()),
            "library_bytes": lib_bytes, "setup_s": setup_s}
@@ -543,9 +673,56 @@ def channel_rollout(steps, cells=(192, 128, 128), krylov=30, warmup=2, restol=1e
     return out
 
 
-def cpu_iteration_time(seed, sample_n=128):
-    oracle_iteration_time(sample_n, seed)   # builds the oracle (not timed)
-    return oracle_iteration_time(sample_n, seed), sample_n
+def rel_l2_mean_free(pr, a, b):
+    """Relative L2 distance (cell-volume weights, fluid cells) of two
+    pressures after removing each one's volume-weighted fluid mean."""
+    from flow_structure_interaction_fem_ibm_gb300.grid import Metrics
+    n0, n1, n2 = pr.params.nx - 1, pr.params.ny - 1, pr.params.nz - 1
+    I = (slice(1, n0 + 1), slice(1, n1 + 1), slice(1, n2 + 1))
+    mx, my, mz = Metrics(pr.x), Metrics(pr.y), Metrics(pr.z)
+    vol = mx.dx[1:n0 + 1, None, None] * my.dx[None, 1:n1 + 1, None] * mz.dx[None, None, 1:n2 + 1]
+    w = vol * (1.0 - pr.geom.iblank[I])
+    da = (a[I] - (a[I] * w).sum() / w.sum()) * (w > 0)
+    db = (b[I] - (b[I] * w).sum() / w.sum()) * (w > 0)
+    return float(np.sqrt(((da - db) ** 2 * vol).sum() / max((db ** 2 * vol).sum(), 1e-300)))
+
+
+def config2_gpu(pr, solver_cls, krylov, reps=3):
+    """Config 2 on the GPU: complete solves of the 128^3 stretched sphere at
+    the config's tolerance in four forms (FP64 and mixed; the reference's
+    stationary outer iteration and FGMRES(krylov)), each timed with CUDA
+    events over `reps` solves after one warm-up, and an FP64 solve at 1e-4 of
+    the tolerance as the converged reference."""
+    import torch
+    sh = pr.shape
+    b = torch.from_numpy(np.ascontiguousarray(pr.nlu0.transpose(2, 1, 0))).cuda()
+    p = torch.zeros(sh[::-1], dtype=torch.float64, device="cuda")
+    out, fields = {}, {}
+    forms = (("fp64_stationary", 0, 0), ("fp64_fgmres", 0, krylov), ("mixed_stationary", 1, 0),
+             ("mixed_fgmres", 1, krylov), ("fp64_tight", 0, krylov))
+    for name, mode, kr in forms:
+        q = copy.deepcopy(pr.params)
+        q.precision_mode, q.outer_krylov, q.iterMax_Poisson = mode, kr, 2000
+        if name == "fp64_tight":
+            # 1e-10: the compatibility shift holds the consistent part of the right-hand side
+            # to about 1e-11 of max|nlu0|, so FP64 solves stall between 1e-11 and 1e-12
+            q.restol_Poisson = pr.params.restol_Poisson * 1e-2
+        s = solver_cls(q, pr.x, pr.y, pr.z).set_boundary(pr.geom)
+        dev, iters, st = [], [], 0
+        for r in range(1 + (reps if name != "fp64_tight" else 0)):
+            p.zero_()
+            torch.cuda.synchronize()
+            st, it, mr, loc, d = s.solve_poisson_device(p.data_ptr(), b.data_ptr())
+            if r > 0 or name == "fp64_tight":
+                dev.append(d)
+                iters.append(it)
+        s.close()
+        fields[name] = p.cpu().numpy().transpose(2, 1, 0).copy()
+        out[name] = {"status": st, "iters": iters[-1], "seconds": float(np.median(dev)),
+                     "solves_per_s": 1.0 / float(np.median(dev))}
+    del b, p
+    torch.cuda.empty_cache()
+    return out, fields
 
 
 def main():
@@ -553,6 +730,15 @@ def main():
     rank, world, local = dist_env()
     if args.impl == "reference":
         return run_reference(args, rank, world)
+    special = args.profile or args.profile_krylov or args.rollout > 0 or args.steps_only
+    want_cpu = rank == 0 and world == 1 and not args.no_cpu_baseline and not special
+    jobs = None
+    if want_cpu:
+        # CPU workers spawned before the first GPU call: one 256^3 outer iteration
+        # of the oracle now, the complete 128^3 config-2 solve once its
+        # right-hand side is ready
+        jobs = OracleJobs(2)
+        jobs.submit(1, "iteration", (args.n, args.seed))
     import torch
     torch.cuda.set_device(local)
     if world > 1:
@@ -604,6 +790,11 @@ def main():
             print(json.dumps({"profile": True, "precision_mode": mode, "stats": s.stats()}))
             s.close()
         return
+
+    pr2 = shift2 = None
+    if want_cpu:
+        pr2, shift2 = config2_problem(args.tol, solver_cls=PoissonSolver)
+        jobs.submit(0, "complete", (pr2.params, pr2.x, pr2.y, pr2.z, pr2.geom, pr2.nlu0))
 
     t_setup = time.perf_counter()
     pr, shift = build_problem(args.n, args.seed, args.tol, PoissonSolver)
@@ -705,6 +896,28 @@ def main():
     err_tight = float(torch.linalg.vector_norm(pm - pt) / torch.linalg.vector_norm(pt))
     err64_tight = float(torch.linalg.vector_norm(pf - pt) / torch.linalg.vector_norm(pt))
 
+    # config 3 at tolerance 1e-10: both forms timed, errors against an FP64 solve run to 1e-11
+    # (the floor the compatibility shift leaves lies between 1e-11 and 1e-12)
+    tol10 = {"tol": args.tol * 1e-2, "restol": restol * 1e-2}
+    p10 = {}
+    for name, mode in (("mixed", 1), ("fp64", 0)):
+        sv = make(mode, args.krylov, restol_Poisson=restol * 1e-2, iterMax_Poisson=400)
+        t10, _, it10, _ = timed(sv, 2, 1)
+        p10[name] = mean_free(p.clone())
+        tol10[name] = {"solves_per_s": replica_throughput(world, 2, t10), "ms_per_solve": 1e3 * t10 / 2,
+                       "iters": it10[0]}
+        sv.close()
+    sv = make(0, args.krylov, restol_Poisson=restol * 1e-3, iterMax_Poisson=300)
+    st12, it12, _ = step(sv, must_converge=False)
+    sv.close()
+    p12 = mean_free(p.clone())
+    for name in ("mixed", "fp64"):
+        tol10[name]["rel_l2_vs_fp64_1e11"] = float(torch.linalg.vector_norm(p10[name] - p12)
+                                                   / torch.linalg.vector_norm(p12))
+    tol10["mixed_over_fp64"] = tol10["mixed"]["solves_per_s"] / tol10["fp64"]["solves_per_s"]
+    tol10["reference_solve"] = {"tol": args.tol * 1e-3, "status": st12, "iters": it12}
+    del p10, p12
+
     # e2e through the host-buffer C ABI (fsi_mg_solve), pinned buffers
     e2e = None
     if not args.no_e2e:
@@ -753,20 +966,61 @@ def main():
     achieved = lt["alg_bytes"] / (avg_ms * 1e-3) / 1e9
     traffic = profile_traffic(args.n)
     roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                "traffic": traffic, "kernel": "level-1 FP32 line relaxation, one colour per launch (x, y, z)",
+                "traffic": traffic,
+                "traffic_source": f"profiles/line_relaxation_fp32_{args.n}.md (ncu capture, not this run)",
+                "kernel": "level-1 FP32 line relaxation, one colour per launch (x, y, z)",
                 "launches": lt["launches"], "avg_us": 1e3 * avg_ms, "alg_bytes_per_launch": lt["alg_bytes"],
                 "peak_source": "measured hbm_gbs" if PEAKS.exists() else "fallback"}
 
-    cpu = None
-    if rank == 0 and world == 1 and not args.no_cpu_baseline:
-        t_iter, sample_n = cpu_iteration_time(args.seed, sample_n=128)
-        t_iter *= (args.n / sample_n) ** 3
-        key = (args.n, args.seed, args.tol)
-        ref_it, src = REFERENCE_ITERATIONS.get(key, (it_stat, "the GPU's stationary count in this run"))
-        cpu = {"value": 1.0 / (t_iter * ref_it), "unit": "solves/s", "cores": 1, "kind": "port",
-               "sample": (f"one outer iteration of the oracle (serial reference MG, reference line ordering) "
-                          f"at {sample_n}^3, scaled by cell count x{(args.n / sample_n) ** 3:.0f}, times the "
-                          f"reference's stationary iteration count {ref_it} ({src})")}
+    cpu = config2 = model256 = None
+    if want_cpu:
+        # config 2 on the GPU while the oracle's complete solve runs on its core
+        for sv in (s_mixed, s_fp64):
+            if sv is not None:
+                sv.close()
+        s_mixed = s_fp64 = None
+        g2, f2 = config2_gpu(pr2, PoissonSolver, args.krylov)
+        ref2 = jobs.result(0, timeout=3600)
+        it256 = jobs.result(1, timeout=3600)
+        jobs.close()
+        config2 = {"workload": "sphere_128^3_tanh1.5_r0.15_seed2_tol%g" % args.tol, "compat_shift": shift2,
+                   "restol": pr2.params.restol_Poisson, "gpu": g2}
+        if "error" not in ref2:
+            t_ref = ref2["solve_s"]
+            config2["oracle"] = {"status": ref2["status"], "iters": ref2["iters"], "maxres": ref2["maxres"],
+                                 "seconds": t_ref, "solves_per_s": 1.0 / t_ref, "cores": 1,
+                                 "host_cores": os.cpu_count(),
+                                 "what": "complete solve_poisson of the oracle (serial C restatement of the "
+                                         "reference MG, reference lexicographic line order), timed end to end"}
+            po = ref2["p"]
+            config2["parity"] = {
+                "gpu_fp64_stationary_vs_oracle_rel_l2": rel_l2_mean_free(pr2, f2["fp64_stationary"], po),
+                "gpu_fp64_fgmres_vs_oracle_rel_l2": rel_l2_mean_free(pr2, f2["fp64_fgmres"], po),
+                "gpu_mixed_fgmres_vs_oracle_rel_l2": rel_l2_mean_free(pr2, f2["mixed_fgmres"], po),
+                "oracle_vs_gpu_fp64_tight_rel_l2": rel_l2_mean_free(pr2, po, f2["fp64_tight"]),
+                "gpu_fp64_stationary_vs_gpu_fp64_tight_rel_l2":
+                    rel_l2_mean_free(pr2, f2["fp64_stationary"], f2["fp64_tight"]),
+                "gpu_mixed_fgmres_vs_gpu_fp64_tight_rel_l2":
+                    rel_l2_mean_free(pr2, f2["mixed_fgmres"], f2["fp64_tight"]),
+                "note": "each solve stops inside its own residual ball at tol; the oracle's distance to the "
+                        "tight solution (oracle_vs_gpu_fp64_tight) is the scale the GPU-vs-oracle figures "
+                        "are read against"}
+            config2["vs_reference"] = {k: g2[k]["solves_per_s"] * t_ref for k in
+                                       ("fp64_stationary", "fp64_fgmres", "mixed_stationary", "mixed_fgmres")}
+            cpu = {"value": 1.0 / t_ref, "unit": "solves/s", "cores": 1, "kind": "port",
+                   "sample": ("one complete solve_poisson of the 128^3 config-2 workload (stretched sphere, "
+                              f"tol {args.tol:g}; the 256^3 headline workload takes hours on one core) by the "
+                              "oracle in the reference's line order, timed end to end on one of "
+                              f"{os.cpu_count()} host cores; same run as the GPU's config2 solves")}
+        else:
+            config2["oracle"] = ref2
+        if "error" not in it256:
+            ref_it, src = REFERENCE_ITERATIONS[(args.n, args.seed, args.tol)] \
+                if (args.n, args.seed, args.tol) in REFERENCE_ITERATIONS else (it_stat, "GPU stationary count")
+            model256 = {"seconds_per_iteration": it256["seconds"], "iterations": ref_it, "iterations_source": src,
+                        "solves_per_s": 1.0 / (it256["seconds"] * ref_it),
+                        "what": (f"MODEL, not a timed solve: one oracle outer iteration at {args.n}^3 timed in "
+                                 "this run x the reference's stationary iteration count")}
 
     out = {
         "metric": METRIC, "value": value, "unit": "solves/s", "n_gpus": world, "steps": args.steps,
@@ -786,7 +1040,8 @@ def main():
         "iters_mixed": mixed_iters[0], "iters_fp64": fp64_iters[0], "stationary": stationary,
         "wall_ms_per_step": 1e3 * mixed_wall / args.steps,
         "gpu_launches": int(mixed_launch), "clocks": clocks, "e2e": e2e, "roofline": roofline,
-        "cpu_baseline": cpu, "adjoint": adjoint, "projection_steps": steps_ops, "channel_rollout": rollout,
+        "cpu_baseline": cpu, "config2": config2, "reference_model_256": model256, "tol_1e10": tol10,
+        "adjoint": adjoint, "projection_steps": steps_ops, "channel_rollout": rollout,
         "setup_s": setup_s,
     }
     if rank == 0:

@@ -60,6 +60,11 @@ class FractionalStep:
         self.nl_old = [z() for _ in range(3)]
         self.visc = torch.full(shape, self.reinv, dtype=torch.float64, device="cuda")
         self.pPrime, self.p, self.nlu0 = z(), z(), z()
+        # the outflow boundary term of GCM_correct_pressure (IBM/CORE_POISSON.F90:1813-1821) of the
+        # last solve: with zero-gradient outflow the corrected faces satisfy div(face) = -dt nlw0
+        # in the outflow cell layer (the outflow faces keep their set_bc values), and
+        # div(face) = 0 to the solver's residual everywhere else
+        self.nlw0 = z()
         self.time = 0.0
         self.ntime = 0
         self.history = []
@@ -122,7 +127,8 @@ class FractionalStep:
         mark("solve_ad")
         s.face_vel_rhs(dt, *vp, *fp, self.nlu0.data_ptr(), d_bc=self._normal_bc())
         mark("face_vel_rhs")
-        st, it, mr, _, _ = s.solve_poisson_device(self.pPrime.data_ptr(), self.nlu0.data_ptr())
+        st, it, mr, _, _ = s.solve_poisson_device(self.pPrime.data_ptr(), self.nlu0.data_ptr(),
+                                                  self.nlw0.data_ptr())
         mark("solve_poisson")
         st_cv = s.correct_vel(dt, self.pPrime.data_ptr(), *vp, *fp, d_bc=self._normal_bc())
         mark("correct_vel")
