@@ -26,7 +26,7 @@ INCLUDE = ROOT / "include"
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 CUDA_SOURCES = ["fsi_mg.cu", "step_api.cu", "mg_kernels.cu", "step_kernels.cu"]
-CUDA_HEADERS = ["mg_kernels.cuh", "device_util.cuh", "mg_context.h"]
+CUDA_HEADERS = ["mg_kernels.cuh", "device_util.cuh", "partition_solve.cuh", "mg_context.h"]
 
 
 def nvcc() -> str:

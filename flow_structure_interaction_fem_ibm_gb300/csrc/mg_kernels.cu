@@ -1,8 +1,11 @@
 // Kernels of the GB300 pressure-Poisson multigrid.  Each kernel cites the
 // reference routine whose arithmetic it performs.
 #include "device_util.cuh"
+#include "partition_solve.cuh"
 
+#include <algorithm>
 #include <cfloat>
+#include <type_traits>
 #include <cuda.h>   // driver API types (CUcontext) for the no-alloc scratch lookup
 #include <mutex>
 #include <cooperative_groups.h>
@@ -208,35 +211,97 @@ __global__ void __launch_bounds__(TPB) k_line_short(LineArgs<T> A)
 //     reduction over warp shuffles (5 steps); lanes then back-substitute.
 //  3. Store: relaxation var = var (1-omega) + omega x, coalesced per row.
 // ---------------------------------------------------------------------------
-constexpr int WP_LINES = 8;
-
-template <int S> __host__ __device__ constexpr int wp_pitch() { return 32 * (S + 1) + 4; }
-
-// Reciprocal used by the partition solver: IEEE division in FP64; the fast
-// approximate reciprocal (about 1 ulp) in FP32, where the smoother only
-// produces a correction inside FP64 refinement.
-template <typename T> __device__ __forceinline__ T wp_rcp(T x);
-template <> __device__ __forceinline__ float wp_rcp<float>(float x) { return __fdividef(1.0f, x); }
-template <> __device__ __forceinline__ double wp_rcp<double>(double x) { return 1.0 / x; }
-
-// One parallel-cyclic-reduction step over the warp at distance h.  Each lane
-// keeps its row (A, B, C, D) and 1/B; rows outside the system are identity
-// rows (A = C = D = 0, B = 1).
-template <typename T>
-__device__ __forceinline__ void pcr_step(T &A, T &B, T &C, T &D, T &iB, int lane, int h)
+// Rows of one line of a colour sweep, assembled exactly as MG_itsolv builds
+// them (IBM/CORE_MG.F90:1950-1983: masked coefficients, identity rows for
+// solid and ghost cells and for the all-zero rule, finest-level Dirichlet
+// terms; tdma ignores a(n1) and c(n2)).  The calling thread stages rows
+// rr, rr + 32, ... of the line at `base`; loads for up to 4 rows are issued
+// before any is used.  put(r, a, b, c, d) stores row r.
+template <typename T, int DIR, int S, bool FULL, class Put>
+__device__ __forceinline__ void stage_line_rows(const LineArgs<T> &A, int L, int base, int ps, int qs, int rr,
+                                                int sa_, int sb_, int sc_, Put put)
 {
-    T Am = __shfl_up_sync(0xffffffffu, A, h), iBm = __shfl_up_sync(0xffffffffu, iB, h);
-    T Cm = __shfl_up_sync(0xffffffffu, C, h), Dm = __shfl_up_sync(0xffffffffu, D, h);
-    T Ap = __shfl_down_sync(0xffffffffu, A, h), iBp = __shfl_down_sync(0xffffffffu, iB, h);
-    T Cp = __shfl_down_sync(0xffffffffu, C, h), Dp = __shfl_down_sync(0xffffffffu, D, h);
-    if (lane < h) { Am = T(0); iBm = T(1); Cm = T(0); Dm = T(0); }
-    if (lane + h > 31) { Ap = T(0); iBp = T(1); Cp = T(0); Dp = T(0); }
-    const T k1 = A * iBm, k2 = C * iBp;
-    const T nA = -k1 * Am, nC = -k2 * Cp;
-    const T nB = B - k1 * Cm - k2 * Ap;
-    const T nD = D - k1 * Dm - k2 * Dp;
-    A = nA; B = nB; C = nC; D = nD;
-    iB = wp_rcp(nB);
+    using X = Axes<DIR>;
+    // transverse coefficients are constant along the line
+    const T cmb = A.c.cm[X::b][ps], cpb = A.c.cp[X::b][ps];
+    const T cmc = A.c.cm[X::c][qs], cpc = A.c.cp[X::c][qs];
+    const bool zmb = is_zero(cmb), zpb = is_zero(cpb), zmc = is_zero(cmc), zpc = is_zero(cpc);
+    struct RowIn { uint8_t f; T r, nb0, nb1, nb2, nb3, vo; };
+    constexpr int GRP = (S < 4) ? S : 4;
+#pragma unroll
+    for (int q0 = 0; q0 < S; q0 += GRP) {
+        RowIn in[GRP];
+#pragma unroll
+        for (int u = 0; u < GRP; ++u) {
+            const int r = (q0 + u) * 32 + rr;
+            if (r < L) {
+                const int o = base + (r + 1) * sa_;
+                in[u].f = A.fl[o];
+                in[u].r = A.r[o];
+                in[u].vo = A.v[o];
+                if (X::c_first) {
+                    in[u].nb0 = A.v[o - sc_]; in[u].nb1 = A.v[o + sc_];
+                    in[u].nb2 = A.v[o - sb_]; in[u].nb3 = A.v[o + sb_];
+                } else {
+                    in[u].nb0 = A.v[o - sb_]; in[u].nb1 = A.v[o + sb_];
+                    in[u].nb2 = A.v[o - sc_]; in[u].nb3 = A.v[o + sc_];
+                }
+            }
+        }
+#pragma unroll
+        for (int u = 0; u < GRP; ++u) {
+            const int r = (q0 + u) * 32 + rr;
+            if (r >= L) continue;
+            const int i = r + 1;
+            const uint8_t f = in[u].f;
+            const bool fluid = !(f & FB_IB);
+            const T cma_i = A.c.cm[X::a][i], cpa_i = A.c.cp[X::a][i];
+            const T ama = (f & fb_minus(X::a)) ? T(0) : cma_i;
+            const T apa = (f & fb_plus(X::a)) ? T(0) : cpa_i;
+            const T amb = (f & fb_minus(X::b)) ? T(0) : cmb;
+            const T apb = (f & fb_plus(X::b)) ? T(0) : cpb;
+            const T amc = (f & fb_minus(X::c)) ? T(0) : cmc;
+            const T apc = (f & fb_plus(X::c)) ? T(0) : cpc;
+            const bool allzero = ((f & fb_minus(X::a)) || is_zero(cma_i)) && ((f & fb_plus(X::a)) || is_zero(cpa_i)) &&
+                                 ((f & fb_minus(X::b)) || zmb) && ((f & fb_plus(X::b)) || zpb) &&
+                                 ((f & fb_minus(X::c)) || zmc) && ((f & fb_plus(X::c)) || zpc);
+            const bool normal = fluid && !allzero;
+            T aa = T(0), bb = T(1), cc = T(0), dd;
+            if (normal) {
+                T sdd = in[u].r;
+                if (X::c_first) {
+                    sdd = sdd - in[u].nb0 * amc;
+                    sdd = sdd - in[u].nb1 * apc;
+                    sdd = sdd - in[u].nb2 * amb;
+                    sdd = sdd - in[u].nb3 * apb;
+                } else {
+                    sdd = sdd - in[u].nb0 * amb;
+                    sdd = sdd - in[u].nb1 * apb;
+                    sdd = sdd - in[u].nb2 * amc;
+                    sdd = sdd - in[u].nb3 * apc;
+                }
+                dd = sdd;
+                T am3[3], ap3[3];   // diagonal as the reference sums it: (acx + acy) + acz
+                am3[X::a] = ama; ap3[X::a] = apa; am3[X::b] = amb; ap3[X::b] = apb; am3[X::c] = amc;
+                ap3[X::c] = apc;
+                bb = (-(am3[0] + ap3[0]) + -(am3[1] + ap3[1])) + -(am3[2] + ap3[2]);
+                aa = ama;
+                cc = apa;
+            } else {
+                dd = ((f & FB_GM) || fluid) ? in[u].vo : T(0);
+            }
+            // line ends: finest-level Dirichlet terms, and tdma ignores a(n1) and c(n2)
+            if (r == 0) {
+                if (A.dir_lo) dd = dd - A.ppp_lo * aa;
+                aa = T(0);
+            }
+            if (r == L - 1) {
+                if (A.dir_hi) dd = dd - A.ppp_hi * cc;
+                cc = T(0);
+            }
+            put(r, aa, bb, cc, dd);
+        }
+    }
 }
 
 // Warp-per-line partition solver for one colour of a line sweep (lines of
@@ -283,92 +348,11 @@ __global__ void __launch_bounds__(256) k_line_wp(LineArgs<T> A)
     const int base = ps * sb_ + qs * sc_;
 
     // ---- 1. staging: loads for up to 4 rows are issued before any use ----
-    if (oks) {
-        // transverse coefficients are constant along the line
-        const T cmb = A.c.cm[X::b][ps], cpb = A.c.cp[X::b][ps];
-        const T cmc = A.c.cm[X::c][qs], cpc = A.c.cp[X::c][qs];
-        const bool zmb = is_zero(cmb), zpb = is_zero(cpb), zmc = is_zero(cmc), zpc = is_zero(cpc);
-        struct RowIn { uint8_t f; T r, nb0, nb1, nb2, nb3, vo; };
-        constexpr int GRP = (S < 4) ? S : 4;
-#pragma unroll
-        for (int q0 = 0; q0 < S; q0 += GRP) {
-            RowIn in[GRP];
-#pragma unroll
-            for (int u = 0; u < GRP; ++u) {
-                const int r = (q0 + u) * 32 + rr;
-                if (r < L) {
-                    const int o = base + (r + 1) * sa_;
-                    in[u].f = A.fl[o];
-                    in[u].r = A.r[o];
-                    in[u].vo = A.v[o];
-                    if (X::c_first) {
-                        in[u].nb0 = A.v[o - sc_]; in[u].nb1 = A.v[o + sc_];
-                        in[u].nb2 = A.v[o - sb_]; in[u].nb3 = A.v[o + sb_];
-                    } else {
-                        in[u].nb0 = A.v[o - sb_]; in[u].nb1 = A.v[o + sb_];
-                        in[u].nb2 = A.v[o - sc_]; in[u].nb3 = A.v[o + sc_];
-                    }
-                }
-            }
-#pragma unroll
-            for (int u = 0; u < GRP; ++u) {
-                const int r = (q0 + u) * 32 + rr;
-                if (r >= L) continue;
-                const int i = r + 1;
-                const uint8_t f = in[u].f;
-                const bool fluid = !(f & FB_IB);
-                const T cma_i = A.c.cm[X::a][i], cpa_i = A.c.cp[X::a][i];
-                const T ama = (f & fb_minus(X::a)) ? T(0) : cma_i;
-                const T apa = (f & fb_plus(X::a)) ? T(0) : cpa_i;
-                const T amb = (f & fb_minus(X::b)) ? T(0) : cmb;
-                const T apb = (f & fb_plus(X::b)) ? T(0) : cpb;
-                const T amc = (f & fb_minus(X::c)) ? T(0) : cmc;
-                const T apc = (f & fb_plus(X::c)) ? T(0) : cpc;
-                const bool allzero = ((f & fb_minus(X::a)) || is_zero(cma_i)) && ((f & fb_plus(X::a)) || is_zero(cpa_i)) &&
-                                     ((f & fb_minus(X::b)) || zmb) && ((f & fb_plus(X::b)) || zpb) &&
-                                     ((f & fb_minus(X::c)) || zmc) && ((f & fb_plus(X::c)) || zpc);
-                const bool normal = fluid && !allzero;
-                T aa = T(0), bb = T(1), cc = T(0), dd;
-                if (normal) {
-                    T sdd = in[u].r;
-                    if (X::c_first) {
-                        sdd = sdd - in[u].nb0 * amc;
-                        sdd = sdd - in[u].nb1 * apc;
-                        sdd = sdd - in[u].nb2 * amb;
-                        sdd = sdd - in[u].nb3 * apb;
-                    } else {
-                        sdd = sdd - in[u].nb0 * amb;
-                        sdd = sdd - in[u].nb1 * apb;
-                        sdd = sdd - in[u].nb2 * amc;
-                        sdd = sdd - in[u].nb3 * apc;
-                    }
-                    dd = sdd;
-                    T am3[3], ap3[3];   // diagonal as the reference sums it: (acx + acy) + acz
-                    am3[X::a] = ama; ap3[X::a] = apa; am3[X::b] = amb; ap3[X::b] = apb; am3[X::c] = amc;
-                    ap3[X::c] = apc;
-                    bb = (-(am3[0] + ap3[0]) + -(am3[1] + ap3[1])) + -(am3[2] + ap3[2]);
-                    aa = ama;
-                    cc = apa;
-                } else {
-                    dd = ((f & FB_GM) || fluid) ? in[u].vo : T(0);
-                }
-                const int si = sidx(gs, r);
-                sa[si] = aa; sb[si] = bb; sc[si] = cc; sd[si] = dd;
-            }
-        }
-        // line ends (written by this same thread above): finest-level Dirichlet
-        // terms, and tdma ignores a(n1) and c(n2)
-        if (rr == 0) {
-            const int si = sidx(gs, 0);
-            if (A.dir_lo) sd[si] = sd[si] - A.ppp_lo * sa[si];
-            sa[si] = T(0);
-        }
-        if (rr == (L - 1) % 32) {
-            const int si = sidx(gs, L - 1);
-            if (A.dir_hi) sd[si] = sd[si] - A.ppp_hi * sc[si];
-            sc[si] = T(0);
-        }
-    }
+    if (oks)
+        stage_line_rows<T, DIR, S, FULL>(A, L, base, ps, qs, rr, sa_, sb_, sc_, [&](int r, T aa, T bb, T cc, T dd) {
+            const int si = sidx(gs, r);
+            sa[si] = aa; sb[si] = bb; sc[si] = cc; sd[si] = dd;
+        });
     __syncthreads();
 
     // ---- 2. solve (warp = line) ----
@@ -452,6 +436,150 @@ __global__ void __launch_bounds__(256) k_line_wp(LineArgs<T> A)
         }
         if (rr == 0 && A.dir_lo) A.v[base] = A.ppp_lo;
         if (rr == (L - 1) % 32 && A.dir_hi) A.v[base + (L + 1) * sa_] = A.ppp_hi;
+    }
+}
+
+// ---------------------------------------------------------------------------
+// mbarrier helpers (shared::cta).  Every wait is bounded: after WAIT_LIMIT
+// polls the waiting thread records the failure in *err (when given) and goes
+// on, so a logic error can cost a wrong result, which the host reports, but
+// never a hung kernel.
+// ---------------------------------------------------------------------------
+constexpr int WAIT_LIMIT = 1 << 22;
+
+__device__ __forceinline__ unsigned smem_addr(const void *p) { return (unsigned)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ void mbar_init(unsigned long long *bar, unsigned count)
+{
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(bar)), "r"(count) : "memory");
+}
+
+__device__ __forceinline__ void mbar_arrive(unsigned long long *bar)
+{
+    asm volatile("{\n\t.reg .b64 st;\n\tmbarrier.arrive.shared::cta.b64 st, [%0];\n\t}" ::"r"(smem_addr(bar))
+                 : "memory");
+}
+
+__device__ __forceinline__ bool mbar_test(unsigned long long *bar, unsigned parity)
+{
+    unsigned ok;
+    asm volatile("{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+                 "selp.u32 %0, 1, 0, p;\n\t}"
+                 : "=r"(ok)
+                 : "r"(smem_addr(bar)), "r"(parity)
+                 : "memory");
+    return ok != 0;
+}
+
+__device__ __forceinline__ void mbar_wait(unsigned long long *bar, unsigned parity, int *err)
+{
+    for (int n = 0; n < WAIT_LIMIT; ++n) {
+        if (mbar_test(bar, parity)) return;
+        if (n > 64) __nanosleep(64);
+    }
+    if (err) atomicExch(err, 1);
+}
+
+// ---------------------------------------------------------------------------
+// Pipelined red-black line relaxation for lines of exactly 32*S cells (the
+// level-1 sweeps at 256^3 and every level that keeps 256-cell lines): the
+// same rows (stage_line_rows) and partition solve (wp_solve_line) as
+// k_line_wp, reorganised so that loads never wait for a solve.  A persistent
+// CTA of 16 warps walks groups of WP_LINES lines of the colour: warps 0-7
+// stage group n into one of two row buffers while warps 8-15 solve group
+// n-1 from the other and store it (each consumer warp solves one line; the
+// stores use the staging layout, so y/z stores still coalesce over 8
+// neighbouring lines).  The buffers are handed over with mbarriers: FULL[b]
+// (256 producer arrivals) and EMPTY[b] (256 consumer arrivals, after the
+// stores that read the buffer's solutions).  Group n uses buffer n & 1 for
+// the (n >> 1)-th time, so its FULL phase parity is (n >> 1) & 1 and its
+// producer first waits for EMPTY's phase (n >> 1) - 1.  Producers and
+// consumers walk the same group sequence, so every arrival is matched.
+// ---------------------------------------------------------------------------
+constexpr int PIPE_THREADS = 512;
+
+template <typename T, int DIR, int S, bool OMEGA1>
+__global__ void __launch_bounds__(PIPE_THREADS, 2) k_line_pipe(LineArgs<T> A)
+{
+    using X = Axes<DIR>;
+    constexpr int RP4 = wp_rows_pitch<S>();
+    constexpr int L = 32 * S;
+    extern __shared__ unsigned char smem_raw[];
+    WpRow<T> *buf = reinterpret_cast<WpRow<T> *>(smem_raw);   // two buffers of WP_LINES * RP4 rows
+    __shared__ unsigned long long bars[4];                     // FULL[0], FULL[1], EMPTY[0], EMPTY[1]
+    const Dims &d = A.d;
+    const int nb = d.m[X::b] - 1, nc = d.m[X::c] - 1;
+    const int hb = (nb + 1) >> 1;
+    const int nlines = hb * nc;
+    const int ngroups = (nlines + WP_LINES - 1) / WP_LINES;
+    const int sa_ = (int)stride_of(d, X::a), sb_ = (int)stride_of(d, X::b), sc_ = (int)stride_of(d, X::c);
+    const int tid = threadIdx.x;
+    const bool producer = tid < PIPE_THREADS / 2;
+    const int rt = producer ? tid : tid - PIPE_THREADS / 2;   // thread within its role
+    const int lane = rt & 31, rwarp = rt >> 5;
+
+    if (tid == 0) {
+        mbar_init(&bars[0], PIPE_THREADS / 2);
+        mbar_init(&bars[1], PIPE_THREADS / 2);
+        mbar_init(&bars[2], PIPE_THREADS / 2);
+        mbar_init(&bars[3], PIPE_THREADS / 2);
+    }
+    __syncthreads();
+
+    // line g of group grp -> (p, q); invalid lines (beyond the count or p > nb) are skipped
+    auto line_pq = [&](int grp, int g, int &p, int &q) -> bool {
+        const int t = grp * WP_LINES + g;
+        if (t >= nlines) return false;
+        const int tq = t / hb;
+        q = 1 + tq;
+        const int p0 = (((1 + q) & 1) == A.colour) ? 1 : 2;
+        p = p0 + 2 * (t - tq * hb);
+        return p <= nb;
+    };
+    // the staging / storing layout (the same for both roles)
+    const int gs = (DIR == 0) ? rwarp : (rt & (WP_LINES - 1));
+    const int rr = (DIR == 0) ? lane : (rt >> 3);
+
+    int n = 0;
+    for (int grp = (int)blockIdx.x; grp < ngroups; grp += (int)gridDim.x, ++n) {
+        const int bsel = n & 1;
+        const unsigned use = (unsigned)(n >> 1);
+        WpRow<T> *rows = buf + bsel * (WP_LINES * RP4);
+        if (producer) {
+            if (use > 0) mbar_wait(&bars[2 + bsel], (use - 1) & 1, A.werr);   // consumers are done with it
+            int ps = 1, qs = 1;
+            if (line_pq(grp, gs, ps, qs))
+                stage_line_rows<T, DIR, S, true>(A, L, ps * sb_ + qs * sc_, ps, qs, rr, sa_, sb_, sc_,
+                                                 [&](int r, T aa, T bb, T cc, T dd) {
+                                                     WpRow<T> w;
+                                                     w.a = aa; w.b = bb; w.c = cc; w.d = dd;
+                                                     rows[gs * RP4 + r + r / S] = w;
+                                                 });
+            mbar_arrive(&bars[bsel]);
+        } else {
+            mbar_wait(&bars[bsel], use & 1, A.werr);
+            T *x = reinterpret_cast<T *>(rows);   // line g's solution overwrites its rows: x + 4 g RP4
+            {
+                int p, q;
+                const bool valid = line_pq(grp, rwarp, p, q);
+                wp_solve_line<T, S>(rows + rwarp * RP4, x + 4 * rwarp * RP4, L, valid, lane);
+            }
+            asm volatile("bar.sync 1, %0;" ::"n"(PIPE_THREADS / 2) : "memory");   // consumers only
+            int ps = 1, qs = 1;
+            if (line_pq(grp, gs, ps, qs)) {
+                const int base = ps * sb_ + qs * sc_;
+#pragma unroll 4
+                for (int r0 = 0; r0 < L; r0 += 32) {
+                    const int r = r0 + rr;
+                    const int o = base + (r + 1) * sa_;
+                    const T xv = x[4 * gs * RP4 + r + r / S];
+                    A.v[o] = OMEGA1 ? xv : A.v[o] * (T(1) - A.omega) + A.omega * xv;
+                }
+                if (rr == 0 && A.dir_lo) A.v[base] = A.ppp_lo;
+                if (rr == (L - 1) % 32 && A.dir_hi) A.v[base + (L + 1) * sa_] = A.ppp_hi;
+            }
+            mbar_arrive(&bars[2 + bsel]);
+        }
     }
 }
 
@@ -1213,13 +1341,27 @@ __device__ __forceinline__ void maxloc_merge(double &v, long long &i, double v2,
     if (v2 > v || (v2 == v && i2 < i)) { v = v2; i = i2; }
 }
 
+// |x| as the bits of a non-negative double, NaN mapped to +Inf: for non-negative
+// doubles the integer order of the bits is the numeric order, so the max-norm
+// and its location are found on the integer pipe, not the FP64 one.
+__device__ __forceinline__ unsigned long long abs_key(double x)
+{
+    const unsigned long long k = (unsigned long long)__double_as_longlong(x) & 0x7fffffffffffffffULL;
+    return k > 0x7ff0000000000000ULL ? 0x7ff0000000000000ULL : k;   // a NaN residual must not be skipped
+}
+
+__device__ __forceinline__ void keyloc_merge(unsigned long long &v, long long &i, unsigned long long v2, long long i2)
+{
+    if (v2 > v || (v2 == v && i2 < i)) { v = v2; i = i2; }
+}
+
 __global__ void __launch_bounds__(TPB) k_calc_residual(const double *p, const double *b, const double *nlw0,
                                                        const uint8_t *fl, Coef<double> c, Dims d, float *r32,
                                                        double *r64, MaxLoc *partials)
 {
     const int n0 = d.m[0] - 1, n1 = d.m[1] - 1, n2 = d.m[2] - 1;
     const long long total = (long long)n0 * n1 * n2;
-    double best = -1.0;
+    unsigned long long best = 0;
     long long bi = 0x7fffffffffffffffLL;
     for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < total;
          t += (long long)gridDim.x * blockDim.x) {
@@ -1230,23 +1372,21 @@ __global__ void __launch_bounds__(TPB) k_calc_residual(const double *p, const do
         if (nlw0 && !(fl[o] & FB_IB)) res = res + nlw0[o];
         if (r32) r32[o] = (float)res;
         if (r64) r64[o] = res;
-        double a = fabs(res);
-        if (!(a == a)) a = INFINITY;   // a NaN residual must not be skipped by the max
-        maxloc_merge(best, bi, a, o);
+        keyloc_merge(best, bi, abs_key(res), o);
     }
     for (int off = 16; off > 0; off >>= 1) {
-        double v2 = __shfl_xor_sync(0xffffffffu, best, off);
-        long long i2 = __shfl_xor_sync(0xffffffffu, bi, off);
-        maxloc_merge(best, bi, v2, i2);
+        const unsigned long long v2 = __shfl_xor_sync(0xffffffffu, best, off);
+        const long long i2 = __shfl_xor_sync(0xffffffffu, bi, off);
+        keyloc_merge(best, bi, v2, i2);
     }
-    __shared__ double sv[TPB / 32];
+    __shared__ unsigned long long sv[TPB / 32];
     __shared__ long long si[TPB / 32];
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
     if (lane == 0) { sv[wid] = best; si[wid] = bi; }
     __syncthreads();
     if (threadIdx.x == 0) {
-        for (int w = 1; w < TPB / 32; ++w) maxloc_merge(best, bi, sv[w], si[w]);
-        partials[blockIdx.x].v = best;
+        for (int w = 1; w < TPB / 32; ++w) keyloc_merge(best, bi, sv[w], si[w]);
+        partials[blockIdx.x].v = __longlong_as_double((long long)best);
         partials[blockIdx.x].i = bi;
     }
 }
@@ -1681,11 +1821,24 @@ __global__ void __launch_bounds__(TPB) k_avg_partial_rows(const double *p, const
 template <typename T, int DIR, int S, bool O1>
 size_t wp_smem() { return 4 * (size_t)WP_LINES * wp_pitch<S>() * sizeof(T); }
 
+int g_num_sms = 0;   // multiprocessors of the current device (init_kernels)
+
+template <typename T, int S>
+size_t pipe_smem() { return 2 * sizeof(WpRow<T>) * (size_t)WP_LINES * wp_rows_pitch<S>(); }
+
 template <typename T, int DIR, int S, bool O1>
 void launch_wp_one(const LineArgs<T> &a, long long nlines, cudaStream_t s)
 {
     static const int ax[3] = {0, 1, 2};
     const long long blocks = (nlines + WP_LINES - 1) / WP_LINES;
+    if constexpr (std::is_same<T, float>::value && S == 8) {
+        if (a.d.m[ax[DIR]] - 1 == 32 * S && g_num_sms > 0) {
+            // FP32 256-cell lines: the pipelined persistent kernel, two CTAs per SM
+            const long long grid = std::min<long long>(blocks, 2LL * g_num_sms);
+            k_line_pipe<T, DIR, S, O1><<<(unsigned)grid, PIPE_THREADS, pipe_smem<T, S>(), s>>>(a);
+            return;
+        }
+    }
     if (a.d.m[ax[DIR]] - 1 == 32 * S)
         k_line_wp<T, DIR, S, O1, true><<<(unsigned)blocks, 256, wp_smem<T, DIR, S, O1>(), s>>>(a);
     else
@@ -2111,11 +2264,26 @@ void launch_coarse_flags(uint8_t *fl, const Dims &d, const int sb[6], cudaStream
     k_coarse_flags<<<nblk(n), TPB, 0, s>>>(fl, d, sb[0], sb[1], sb[2], sb[3], sb[4], sb[5]);
 }
 
+template <int DIR>
+cudaError_t pipe_attr_dir()
+{
+    const int b = (int)pipe_smem<float, 8>();
+    cudaError_t e = cudaFuncSetAttribute(k_line_pipe<float, DIR, 8, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, b);
+    if (e != cudaSuccess) return e;
+    return cudaFuncSetAttribute(k_line_pipe<float, DIR, 8, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, b);
+}
+
 cudaError_t init_kernels()
 {
     // dynamic shared memory above 48 KB needs an opt-in per kernel; done once per
     // process before any launch (and outside any stream capture)
     cudaError_t e;
+    int dev = 0;
+    if ((e = cudaGetDevice(&dev)) != cudaSuccess) return e;
+    if ((e = cudaDeviceGetAttribute(&g_num_sms, cudaDevAttrMultiProcessorCount, dev)) != cudaSuccess) return e;
+    if ((e = pipe_attr_dir<0>()) != cudaSuccess) return e;
+    if ((e = pipe_attr_dir<1>()) != cudaSuccess) return e;
+    if ((e = pipe_attr_dir<2>()) != cudaSuccess) return e;
     if ((e = wp_attr_dir<float, 0>()) != cudaSuccess) return e;
     if ((e = wp_attr_dir<float, 1>()) != cudaSuccess) return e;
     if ((e = wp_attr_dir<float, 2>()) != cudaSuccess) return e;
@@ -2124,7 +2292,8 @@ cudaError_t init_kernels()
     if ((e = wp_attr_dir<double, 2>()) != cudaSuccess) return e;
     if ((e = fp_attr_dir<0>()) != cudaSuccess) return e;
     if ((e = fp_attr_dir<1>()) != cudaSuccess) return e;
-    return fp_attr_dir<2>();
+    if ((e = fp_attr_dir<2>()) != cudaSuccess) return e;
+    return init_ad_line_kernels();
 }
 
 

@@ -44,6 +44,7 @@ struct LineArgs {
     int dir_lo, dir_hi;   // finest-level Dirichlet ends along the line direction
     T ppp_lo, ppp_hi;
     const double *wpf = nullptr;   // factored partition table of this level and direction (FP64), or null
+    int *werr = nullptr;           // set to 1 by a pipelined sweep whose bounded buffer hand-over wait ran out
 };
 
 template <typename T>
@@ -188,6 +189,8 @@ struct AdCoefArgs {
 void launch_ad_coef(const AdCoefArgs &a, cudaStream_t s);
 // rhs_adjust_bc (IBM/CORE_RHS_AD.F90:588-780): nl -= (boundary values of flagged faces) x coefficients
 void launch_rhs_adjust_bc(const AdCoefArgs &c, const double *const bc[9], double *const nl[3], cudaStream_t s);
+// one-time attributes of the warp-per-line momentum sweeps (called by init_kernels)
+cudaError_t init_ad_line_kernels();
 // one colour of the line sweep of itsolv_ad along axis dir on var with right-hand side r
 void launch_ad_line(int dir, int colour, const AdCoefArgs &c, double *var, const double *r, double *gam,
                     cudaStream_t s);

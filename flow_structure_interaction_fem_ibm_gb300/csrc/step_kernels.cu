@@ -3,6 +3,7 @@
 // momentum predictor (rhs_advec_diff, rhs_adjust_bc, solve_ad).  Each kernel
 // cites the reference routine whose arithmetic it performs.
 #include "device_util.cuh"
+#include "partition_solve.cuh"
 
 #include <algorithm>
 
@@ -667,6 +668,132 @@ __global__ void __launch_bounds__(TPB) k_ad_line(AdCoefArgs A, double *var, cons
     }
 }
 
+// The same colour sweep with one warp per line (lines of 17..256 cells): the
+// rows are assembled exactly as k_ad_line assembles them, staged in shared
+// memory (x-lines: one warp along the line; y- and z-lines: 8 same-colour
+// lines side by side, so the loads coalesce), and solved by the partition
+// solver of the pressure smoother.  A CTA owns WP_LINES lines; each line's
+// solution overwrites its own staged rows.
+template <int DIR, int S, bool FULL>
+__global__ void __launch_bounds__(256) k_ad_line_wp(AdCoefArgs A, double *var, const double *r, int colour)
+{
+    using X = Axes<DIR>;
+    extern __shared__ unsigned char smem_raw[];
+    constexpr int RP4 = wp_rows_pitch<S>();
+    WpRow<double> *srow = reinterpret_cast<WpRow<double> *>(smem_raw);
+    double *sx = reinterpret_cast<double *>(smem_raw);   // line g's solution: sx + 4 g RP4, row r at r + r/S
+    const Dims &d = A.d;
+    const int nb = d.m[X::b] - 1, nc = d.m[X::c] - 1;
+    const int L = FULL ? 32 * S : d.m[X::a] - 1;
+    const int hb = (nb + 1) >> 1;
+    const int nlines = hb * nc;
+    const int sa_ = (int)stride_of(d, X::a), sb_ = (int)stride_of(d, X::b), sc_ = (int)stride_of(d, X::c);
+    // the transverse axes in the reference's order of the right-hand side terms
+    constexpr int t1 = X::b < X::c ? X::b : X::c, t2 = X::b < X::c ? X::c : X::b;
+    const int s1 = (t1 == X::b) ? sb_ : sc_, s2 = (t2 == X::b) ? sb_ : sc_;
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    auto line_pq = [&](int g, int &p, int &q) -> bool {
+        const int t = (int)blockIdx.x * WP_LINES + g;
+        if (t >= nlines) return false;
+        const int tq = t / hb;
+        q = 1 + tq;
+        const int p0 = (((1 + q) & 1) == colour) ? 1 : 2;
+        p = p0 + 2 * (t - tq * hb);
+        return p <= nb;
+    };
+    const int gs = (DIR == 0) ? warp : (tid & (WP_LINES - 1));
+    const int rr = (DIR == 0) ? lane : (tid >> 3);
+    int ps = 1, qs = 1;
+    const bool oks = line_pq(gs, ps, qs);
+    const int base = ps * sb_ + qs * sc_;
+    if (oks) {
+#pragma unroll 2
+        for (int q0 = 0; q0 < S; ++q0) {
+            const int rw = q0 * 32 + rr;
+            if (rw >= L) break;
+            const int o = base + (rw + 1) * sa_;
+            const uint8_t f = A.fl[o];
+            const double rib = (f & FB_IB) ? 0.0 : 1.0;
+            double rhs;
+            if (DIR == 2) {   // z-lines subtract term by term, y before x (IBM/CORE_SOLVE_AD.F90:678-681)
+                rhs = r[o] - var[o - s2] * A.co[2 * t2][o] - var[o + s2] * A.co[2 * t2 + 1][o]
+                      - var[o - s1] * A.co[2 * t1][o] - var[o + s1] * A.co[2 * t1 + 1][o];
+            } else {          // x- and y-lines subtract one sum, lower axis first
+                const double sm = var[o - s1] * A.co[2 * t1][o] + var[o + s1] * A.co[2 * t1 + 1][o]
+                                  + var[o - s2] * A.co[2 * t2][o] + var[o + s2] * A.co[2 * t2 + 1][o];
+                rhs = r[o] - sm;
+            }
+            WpRow<double> w;
+            w.a = (rw == 0) ? 0.0 : A.co[2 * DIR][o] * rib;            // tdma ignores a(1) ...
+            w.c = (rw == L - 1) ? 0.0 : A.co[2 * DIR + 1][o] * rib;    // ... and c(n)
+            w.b = 1.0 + A.co[6][o] * rib;
+            w.d = rhs * rib + ((f & FB_GM) ? var[o] : 0.0);
+            srow[gs * RP4 + rw + rw / S] = w;
+        }
+    }
+    __syncthreads();
+    {
+        int p, q;
+        const bool valid = line_pq(warp, p, q);
+        wp_solve_line<double, S>(srow + warp * RP4, sx + 4 * warp * RP4, L, valid, lane);
+    }
+    __syncthreads();
+    if (oks) {
+#pragma unroll 4
+        for (int q0 = 0; q0 < S; ++q0) {
+            const int rw = q0 * 32 + rr;
+            if (rw >= L) break;
+            var[base + (rw + 1) * sa_] = sx[4 * gs * RP4 + rw + rw / S];
+        }
+    }
+}
+
+template <int S>
+size_t ad_wp_smem() { return sizeof(WpRow<double>) * (size_t)WP_LINES * wp_rows_pitch<S>(); }
+
+template <int DIR, int S>
+void launch_ad_wp_one(const AdCoefArgs &c, double *var, const double *r, int colour, long long lines, cudaStream_t s)
+{
+    const unsigned blocks = (unsigned)((lines + WP_LINES - 1) / WP_LINES);
+    if (c.d.m[DIR] - 1 == 32 * S)
+        k_ad_line_wp<DIR, S, true><<<blocks, 256, ad_wp_smem<S>(), s>>>(c, var, r, colour);
+    else
+        k_ad_line_wp<DIR, S, false><<<blocks, 256, ad_wp_smem<S>(), s>>>(c, var, r, colour);
+}
+
+// lines of 17..256 cells take the warp-per-line kernel; shorter ones one
+// thread per line, longer ones too (no register room for S = 16 in FP64)
+template <int DIR>
+bool launch_ad_wp_dir(const AdCoefArgs &c, double *var, const double *r, int colour, int L, long long lines,
+                      cudaStream_t s)
+{
+    if (L <= 16 || L > 256) return false;
+    if (L <= 32) launch_ad_wp_one<DIR, 1>(c, var, r, colour, lines, s);
+    else if (L <= 64) launch_ad_wp_one<DIR, 2>(c, var, r, colour, lines, s);
+    else if (L <= 128) launch_ad_wp_one<DIR, 4>(c, var, r, colour, lines, s);
+    else launch_ad_wp_one<DIR, 8>(c, var, r, colour, lines, s);
+    return true;
+}
+
+template <int DIR, int S>
+cudaError_t ad_wp_attr()
+{
+    const int b = (int)ad_wp_smem<S>();
+    cudaError_t e = cudaFuncSetAttribute(k_ad_line_wp<DIR, S, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, b);
+    if (e != cudaSuccess) return e;
+    return cudaFuncSetAttribute(k_ad_line_wp<DIR, S, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, b);
+}
+
+template <int DIR>
+cudaError_t ad_wp_attr_dir()
+{
+    cudaError_t e;
+    if ((e = ad_wp_attr<DIR, 1>()) != cudaSuccess) return e;
+    if ((e = ad_wp_attr<DIR, 2>()) != cudaSuccess) return e;
+    if ((e = ad_wp_attr<DIR, 4>()) != cudaSuccess) return e;
+    return ad_wp_attr<DIR, 8>();
+}
+
 __global__ void __launch_bounds__(TPB) k_ad_residual(AdCoefArgs A, const double *var, const double *r,
                                                      unsigned long long *maxbits)
 {
@@ -760,12 +887,25 @@ void launch_rhs_adjust_bc(const AdCoefArgs &c, const double *const bc[9], double
                                             nl[1], nl[2]);
 }
 
+cudaError_t init_ad_line_kernels()
+{
+    cudaError_t e;
+    if ((e = ad_wp_attr_dir<0>()) != cudaSuccess) return e;
+    if ((e = ad_wp_attr_dir<1>()) != cudaSuccess) return e;
+    return ad_wp_attr_dir<2>();
+}
+
 void launch_ad_line(int dir, int colour, const AdCoefArgs &c, double *var, const double *r, double *gam,
                     cudaStream_t s)
 {
     // the transverse axes of Axes<dir>: lines of one colour = ceil(nb / 2) x nc
     const int b = (dir == 0) ? 1 : 0, cc = (dir == 2) ? 1 : 2;
     const long long lines = (long long)((c.d.m[b] - 1 + 1) / 2) * (c.d.m[cc] - 1);
+    const int L = c.d.m[dir] - 1;
+    if (dir == 0 ? launch_ad_wp_dir<0>(c, var, r, colour, L, lines, s)
+        : dir == 1 ? launch_ad_wp_dir<1>(c, var, r, colour, L, lines, s)
+                   : launch_ad_wp_dir<2>(c, var, r, colour, L, lines, s))
+        return;
     if (dir == 0) k_ad_line<0><<<nblk(lines), TPB, 0, s>>>(c, var, r, gam, colour);
     else if (dir == 1) k_ad_line<1><<<nblk(lines), TPB, 0, s>>>(c, var, r, gam, colour);
     else k_ad_line<2><<<nblk(lines), TPB, 0, s>>>(c, var, r, gam, colour);

@@ -297,7 +297,9 @@ int fsi_mg_level_size(void *handle, int d, int n);
  *   op 3 coarse iblank of level n (a = int8 OUT)
  *   op 4 face flags of level n (a = int8 OUT, 6 full arrays ium..kup)
  *   op 5 ghost-cell rows on a level-1 array (a = var INOUT, b = int OUT iterations)
- *   op 6 outer ghost layer on a level-1 array (a = var INOUT) */
+ *   op 6 outer ghost layer on a level-1 array (a = var INOUT)
+ *   op 7 MG_itsolv in FP32, the mixed form's smoother (a = var INOUT, b = rhs
+ *        IN, both rounded to FP32 on the device; the result is widened) */
 int fsi_mg_debug_level_op(void *handle, int op, int d, int n, void *a, void *b, void *c);
 
 /* Counters of the last solve: out[0] iterations, out[1] final maxres,

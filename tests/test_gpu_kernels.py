@@ -29,6 +29,8 @@ def cases():
         ("sphere_48x80x160", lambda: P.sphere((48, 80, 160), seed=5, stretch=1.5)),
         # cubic: coarsest levels with two long directions of equal length (S = 2)
         ("sphere48_tanh", lambda: P.sphere(48, seed=6, stretch=1.5)),
+        # 256-cell x- and z-lines: the pipelined FP32 sweep in those directions
+        ("sphere_256x20x256", lambda: P.sphere((256, 20, 256), seed=7, stretch=1.5)),
     ]
 
 
@@ -102,6 +104,45 @@ def test_line_smoother_sweep(pair):
         got = v0.copy(order="F")
         g.debug_op(0, d, n, got, r)
         assert rel(got, ref) < RTOL, (d, n, rel(got, ref))
+
+
+def test_line_smoother_sweep_partition_fp64(pair):
+    """The same sweep through the warp-per-line partition solver in FP64 (a
+    mixed-form handle keeps no factored FP64 tables, so its FP64 sweeps take
+    that kernel): 1e-12 against the oracle."""
+    pr, o, g = pair
+    import copy
+    q = copy.deepcopy(pr.params)
+    q.precision_mode = 1
+    gm = PoissonSolver(q, pr.x, pr.y, pr.z).set_boundary(pr.geom)
+    try:
+        rng = np.random.default_rng(11)
+        for d, n in levels(o, pr.params.ndim):
+            sh = o.level_shape(d, n)
+            v0 = np.asfortranarray(rng.standard_normal(sh))
+            r = np.asfortranarray(rng.standard_normal(sh))
+            ref = o.itsolv(d, n, v0.copy(order="F"), r)
+            got = v0.copy(order="F")
+            gm.debug_op(0, d, n, got, r)
+            assert rel(got, ref) < RTOL, (d, n, rel(got, ref))
+    finally:
+        gm.close()
+
+
+def test_line_smoother_sweep_fp32(pair):
+    """One MG_itsolv of the mixed form's FP32 smoother at every level against
+    the FP64 oracle on the same FP32-rounded inputs: the sweep's rounding
+    only (2e-5 relative to the largest value)."""
+    pr, o, g = pair
+    rng = np.random.default_rng(12)
+    for d, n in levels(o, pr.params.ndim):
+        sh = o.level_shape(d, n)
+        v0 = np.asfortranarray(rng.standard_normal(sh).astype(np.float32).astype(np.float64))
+        r = np.asfortranarray(rng.standard_normal(sh).astype(np.float32).astype(np.float64))
+        ref = o.itsolv(d, n, v0.copy(order="F"), r)
+        got = v0.copy(order="F")
+        g.debug_op(7, d, n, got, r)
+        assert rel(got, ref) < 2e-5, (d, n, rel(got, ref))
 
 
 def test_residual_restriction(pair):
