@@ -271,7 +271,6 @@ void itsolv(Ctx &c, Level &L, T *v, const T *r, bool finest, bool homogeneous)
     LineArgs<T> a;
     a.v = v; a.r = r; a.fl = L.fl; a.U = scratch_U<T>(c); a.c = coef_of<T>(L); a.d = L.d;
     a.omega = (T)c.p.omega;
-    a.werr = c.d_werr;
     const bool om1 = (c.p.omega == 1.0);
     for (int dir = 0; dir < c.nd; ++dir) {
         a.wpf = std::is_same<T, double>::value ? L.wpf[dir] : nullptr;
@@ -789,33 +788,7 @@ int solve_krylov(Ctx &c, double *p, const double *b, int *iters, double *maxres_
 }
 
 // solve_poisson MG branch on device-resident full-layout arrays
-int solve_device_body(Ctx &c, double *p, const double *b, int *iters, double *maxres_out, int *loc,
-                      double *compTime);
-
-// A pipelined line sweep that ran out of its bounded wait for a buffer
-// hand-over leaves a flag instead of hanging; the solve then reports an error.
-int check_line_waits(Ctx &c)
-{
-    int h = 0;
-    CK(cudaMemcpyAsync(&h, c.d_werr, sizeof(int), cudaMemcpyDeviceToHost, c.s));
-    CK(cudaStreamSynchronize(c.s));
-    if (h != 0) {
-        CK(cudaMemsetAsync(c.d_werr, 0, sizeof(int), c.s));
-        return fail(-13, "a pipelined line sweep timed out waiting for a buffer hand-over (results invalid)");
-    }
-    return 0;
-}
-
 int solve_device(Ctx &c, double *p, const double *b, int *iters, double *maxres_out, int *loc, double *compTime)
-{
-    const int rc = solve_device_body(c, p, b, iters, maxres_out, loc, compTime);
-    if (rc < 0) return rc;
-    TRY(check_line_waits(c));
-    return rc;
-}
-
-int solve_device_body(Ctx &c, double *p, const double *b, int *iters, double *maxres_out, int *loc,
-                      double *compTime)
 {
     if (!c.geometry) return fail(-2, "fsi_mg_set_geometry has not been called");
     if (c.p.outer_krylov > 0) return solve_krylov(c, p, b, iters, maxres_out, loc, compTime);
@@ -993,7 +966,6 @@ int fsi_mg_create(const fsi_mg_params *params, const double *x, const double *y,
     TRY(c->alloc(&c->partials, (size_t)c->nred * 2 + 8));
     TRY(c->alloc(&c->result, 1));
     TRY(c->alloc(&c->d_iters, 1));
-    TRY(c->alloc(&c->d_werr, 1));
     TRY(c->alloc(&c->d_maxd, 1));
     CK(cudaMallocHost(&c->h_result, sizeof(MaxLoc)));
     for (int d = 0; d < 3; ++d) {
@@ -1555,7 +1527,6 @@ int fsi_mg_debug_level_op(void *handle, int op, int d, int n, void *a, void *b, 
     }
     CK(cudaGetLastError());
     CK(cudaStreamSynchronize(c.s));
-    if (rc == 0) rc = check_line_waits(c);
     // release the temporaries (they were appended last)
     for (double *t : {t2, t1, t0}) {
         if (!t) continue;

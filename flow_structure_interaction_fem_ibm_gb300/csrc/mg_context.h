@@ -89,7 +89,6 @@ struct Ctx {
     double *gco64 = nullptr, *gscr64 = nullptr;
     float *gco32 = nullptr, *gscr32 = nullptr;
     int *d_iters = nullptr;
-    int *d_werr = nullptr;   // set by a pipelined line sweep whose bounded buffer hand-over wait ran out
     unsigned long long *d_maxd = nullptr;
 
     // reductions

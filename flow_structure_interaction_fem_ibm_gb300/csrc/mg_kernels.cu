@@ -440,150 +440,6 @@ __global__ void __launch_bounds__(256) k_line_wp(LineArgs<T> A)
 }
 
 // ---------------------------------------------------------------------------
-// mbarrier helpers (shared::cta).  Every wait is bounded: after WAIT_LIMIT
-// polls the waiting thread records the failure in *err (when given) and goes
-// on, so a logic error can cost a wrong result, which the host reports, but
-// never a hung kernel.
-// ---------------------------------------------------------------------------
-constexpr int WAIT_LIMIT = 1 << 22;
-
-__device__ __forceinline__ unsigned smem_addr(const void *p) { return (unsigned)__cvta_generic_to_shared(p); }
-
-__device__ __forceinline__ void mbar_init(unsigned long long *bar, unsigned count)
-{
-    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(bar)), "r"(count) : "memory");
-}
-
-__device__ __forceinline__ void mbar_arrive(unsigned long long *bar)
-{
-    asm volatile("{\n\t.reg .b64 st;\n\tmbarrier.arrive.shared::cta.b64 st, [%0];\n\t}" ::"r"(smem_addr(bar))
-                 : "memory");
-}
-
-__device__ __forceinline__ bool mbar_test(unsigned long long *bar, unsigned parity)
-{
-    unsigned ok;
-    asm volatile("{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
-                 "selp.u32 %0, 1, 0, p;\n\t}"
-                 : "=r"(ok)
-                 : "r"(smem_addr(bar)), "r"(parity)
-                 : "memory");
-    return ok != 0;
-}
-
-__device__ __forceinline__ void mbar_wait(unsigned long long *bar, unsigned parity, int *err)
-{
-    for (int n = 0; n < WAIT_LIMIT; ++n) {
-        if (mbar_test(bar, parity)) return;
-        if (n > 64) __nanosleep(64);
-    }
-    if (err) atomicExch(err, 1);
-}
-
-// ---------------------------------------------------------------------------
-// Pipelined red-black line relaxation for lines of exactly 32*S cells (the
-// level-1 sweeps at 256^3 and every level that keeps 256-cell lines): the
-// same rows (stage_line_rows) and partition solve (wp_solve_line) as
-// k_line_wp, reorganised so that loads never wait for a solve.  A persistent
-// CTA of 16 warps walks groups of WP_LINES lines of the colour: warps 0-7
-// stage group n into one of two row buffers while warps 8-15 solve group
-// n-1 from the other and store it (each consumer warp solves one line; the
-// stores use the staging layout, so y/z stores still coalesce over 8
-// neighbouring lines).  The buffers are handed over with mbarriers: FULL[b]
-// (256 producer arrivals) and EMPTY[b] (256 consumer arrivals, after the
-// stores that read the buffer's solutions).  Group n uses buffer n & 1 for
-// the (n >> 1)-th time, so its FULL phase parity is (n >> 1) & 1 and its
-// producer first waits for EMPTY's phase (n >> 1) - 1.  Producers and
-// consumers walk the same group sequence, so every arrival is matched.
-// ---------------------------------------------------------------------------
-constexpr int PIPE_THREADS = 512;
-
-template <typename T, int DIR, int S, bool OMEGA1>
-__global__ void __launch_bounds__(PIPE_THREADS, 2) k_line_pipe(LineArgs<T> A)
-{
-    using X = Axes<DIR>;
-    constexpr int RP4 = wp_rows_pitch<S>();
-    constexpr int L = 32 * S;
-    extern __shared__ unsigned char smem_raw[];
-    WpRow<T> *buf = reinterpret_cast<WpRow<T> *>(smem_raw);   // two buffers of WP_LINES * RP4 rows
-    __shared__ unsigned long long bars[4];                     // FULL[0], FULL[1], EMPTY[0], EMPTY[1]
-    const Dims &d = A.d;
-    const int nb = d.m[X::b] - 1, nc = d.m[X::c] - 1;
-    const int hb = (nb + 1) >> 1;
-    const int nlines = hb * nc;
-    const int ngroups = (nlines + WP_LINES - 1) / WP_LINES;
-    const int sa_ = (int)stride_of(d, X::a), sb_ = (int)stride_of(d, X::b), sc_ = (int)stride_of(d, X::c);
-    const int tid = threadIdx.x;
-    const bool producer = tid < PIPE_THREADS / 2;
-    const int rt = producer ? tid : tid - PIPE_THREADS / 2;   // thread within its role
-    const int lane = rt & 31, rwarp = rt >> 5;
-
-    if (tid == 0) {
-        mbar_init(&bars[0], PIPE_THREADS / 2);
-        mbar_init(&bars[1], PIPE_THREADS / 2);
-        mbar_init(&bars[2], PIPE_THREADS / 2);
-        mbar_init(&bars[3], PIPE_THREADS / 2);
-    }
-    __syncthreads();
-
-    // line g of group grp -> (p, q); invalid lines (beyond the count or p > nb) are skipped
-    auto line_pq = [&](int grp, int g, int &p, int &q) -> bool {
-        const int t = grp * WP_LINES + g;
-        if (t >= nlines) return false;
-        const int tq = t / hb;
-        q = 1 + tq;
-        const int p0 = (((1 + q) & 1) == A.colour) ? 1 : 2;
-        p = p0 + 2 * (t - tq * hb);
-        return p <= nb;
-    };
-    // the staging / storing layout (the same for both roles)
-    const int gs = (DIR == 0) ? rwarp : (rt & (WP_LINES - 1));
-    const int rr = (DIR == 0) ? lane : (rt >> 3);
-
-    int n = 0;
-    for (int grp = (int)blockIdx.x; grp < ngroups; grp += (int)gridDim.x, ++n) {
-        const int bsel = n & 1;
-        const unsigned use = (unsigned)(n >> 1);
-        WpRow<T> *rows = buf + bsel * (WP_LINES * RP4);
-        if (producer) {
-            if (use > 0) mbar_wait(&bars[2 + bsel], (use - 1) & 1, A.werr);   // consumers are done with it
-            int ps = 1, qs = 1;
-            if (line_pq(grp, gs, ps, qs))
-                stage_line_rows<T, DIR, S, true>(A, L, ps * sb_ + qs * sc_, ps, qs, rr, sa_, sb_, sc_,
-                                                 [&](int r, T aa, T bb, T cc, T dd) {
-                                                     WpRow<T> w;
-                                                     w.a = aa; w.b = bb; w.c = cc; w.d = dd;
-                                                     rows[gs * RP4 + r + r / S] = w;
-                                                 });
-            mbar_arrive(&bars[bsel]);
-        } else {
-            mbar_wait(&bars[bsel], use & 1, A.werr);
-            T *x = reinterpret_cast<T *>(rows);   // line g's solution overwrites its rows: x + 4 g RP4
-            {
-                int p, q;
-                const bool valid = line_pq(grp, rwarp, p, q);
-                wp_solve_line<T, S>(rows + rwarp * RP4, x + 4 * rwarp * RP4, L, valid, lane);
-            }
-            asm volatile("bar.sync 1, %0;" ::"n"(PIPE_THREADS / 2) : "memory");   // consumers only
-            int ps = 1, qs = 1;
-            if (line_pq(grp, gs, ps, qs)) {
-                const int base = ps * sb_ + qs * sc_;
-#pragma unroll 4
-                for (int r0 = 0; r0 < L; r0 += 32) {
-                    const int r = r0 + rr;
-                    const int o = base + (r + 1) * sa_;
-                    const T xv = x[4 * gs * RP4 + r + r / S];
-                    A.v[o] = OMEGA1 ? xv : A.v[o] * (T(1) - A.omega) + A.omega * xv;
-                }
-                if (rr == 0 && A.dir_lo) A.v[base] = A.ppp_lo;
-                if (rr == (L - 1) % 32 && A.dir_hi) A.v[base + (L + 1) * sa_] = A.ppp_hi;
-            }
-            mbar_arrive(&bars[2 + bsel]);
-        }
-    }
-}
-
-// ---------------------------------------------------------------------------
 // Factored partition solver (FP64).  The tridiagonal matrix of every line is
 // fixed between geometry updates, so everything in the partition solve that
 // does not depend on the right-hand side is computed once per line by
@@ -1821,24 +1677,11 @@ __global__ void __launch_bounds__(TPB) k_avg_partial_rows(const double *p, const
 template <typename T, int DIR, int S, bool O1>
 size_t wp_smem() { return 4 * (size_t)WP_LINES * wp_pitch<S>() * sizeof(T); }
 
-int g_num_sms = 0;   // multiprocessors of the current device (init_kernels)
-
-template <typename T, int S>
-size_t pipe_smem() { return 2 * sizeof(WpRow<T>) * (size_t)WP_LINES * wp_rows_pitch<S>(); }
-
 template <typename T, int DIR, int S, bool O1>
 void launch_wp_one(const LineArgs<T> &a, long long nlines, cudaStream_t s)
 {
     static const int ax[3] = {0, 1, 2};
     const long long blocks = (nlines + WP_LINES - 1) / WP_LINES;
-    if constexpr (std::is_same<T, float>::value && S == 8) {
-        if (a.d.m[ax[DIR]] - 1 == 32 * S && g_num_sms > 0) {
-            // FP32 256-cell lines: the pipelined persistent kernel, two CTAs per SM
-            const long long grid = std::min<long long>(blocks, 2LL * g_num_sms);
-            k_line_pipe<T, DIR, S, O1><<<(unsigned)grid, PIPE_THREADS, pipe_smem<T, S>(), s>>>(a);
-            return;
-        }
-    }
     if (a.d.m[ax[DIR]] - 1 == 32 * S)
         k_line_wp<T, DIR, S, O1, true><<<(unsigned)blocks, 256, wp_smem<T, DIR, S, O1>(), s>>>(a);
     else
@@ -2264,26 +2107,11 @@ void launch_coarse_flags(uint8_t *fl, const Dims &d, const int sb[6], cudaStream
     k_coarse_flags<<<nblk(n), TPB, 0, s>>>(fl, d, sb[0], sb[1], sb[2], sb[3], sb[4], sb[5]);
 }
 
-template <int DIR>
-cudaError_t pipe_attr_dir()
-{
-    const int b = (int)pipe_smem<float, 8>();
-    cudaError_t e = cudaFuncSetAttribute(k_line_pipe<float, DIR, 8, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, b);
-    if (e != cudaSuccess) return e;
-    return cudaFuncSetAttribute(k_line_pipe<float, DIR, 8, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, b);
-}
-
 cudaError_t init_kernels()
 {
     // dynamic shared memory above 48 KB needs an opt-in per kernel; done once per
     // process before any launch (and outside any stream capture)
     cudaError_t e;
-    int dev = 0;
-    if ((e = cudaGetDevice(&dev)) != cudaSuccess) return e;
-    if ((e = cudaDeviceGetAttribute(&g_num_sms, cudaDevAttrMultiProcessorCount, dev)) != cudaSuccess) return e;
-    if ((e = pipe_attr_dir<0>()) != cudaSuccess) return e;
-    if ((e = pipe_attr_dir<1>()) != cudaSuccess) return e;
-    if ((e = pipe_attr_dir<2>()) != cudaSuccess) return e;
     if ((e = wp_attr_dir<float, 0>()) != cudaSuccess) return e;
     if ((e = wp_attr_dir<float, 1>()) != cudaSuccess) return e;
     if ((e = wp_attr_dir<float, 2>()) != cudaSuccess) return e;

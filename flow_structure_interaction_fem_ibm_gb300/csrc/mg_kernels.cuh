@@ -44,7 +44,6 @@ struct LineArgs {
     int dir_lo, dir_hi;   // finest-level Dirichlet ends along the line direction
     T ppp_lo, ppp_hi;
     const double *wpf = nullptr;   // factored partition table of this level and direction (FP64), or null
-    int *werr = nullptr;           // set to 1 by a pipelined sweep whose bounded buffer hand-over wait ran out
 };
 
 template <typename T>
