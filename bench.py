@@ -68,13 +68,16 @@ def parse():
                          "their line instead of the solve benchmark")
     ap.add_argument("--rollout-cells", type=int, nargs=3, default=(192, 128, 128))
     ap.add_argument("--no-rollout", action="store_true",
-                    help="skip the 20-step sphere-wake channel rollout reported beside the solve benchmark")
+                    help="skip the 200-step sphere-wake channel rollout reported beside the solve benchmark")
     ap.add_argument("--adjoint-n", type=int, default=96)
     ap.add_argument("--adjoint-dirs", type=int, default=200)
     ap.add_argument("--profile", action="store_true",
                     help="profiling driver: raw RHS, two outer iterations of each precision, no other work")
     ap.add_argument("--profile-krylov", action="store_true",
                     help="profiling driver: raw RHS, one mixed FGMRES solve capped at 6 MG applications")
+    ap.add_argument("--profile-fp64", action="store_true",
+                    help="profiling driver: one launch each of the FP64 kernels (face_vel_rhs, correct_vel, "
+                         "rhs_advec_diff, calc_residual, a factored FP64 x sweep) and the DFMA roof on the sphere grid")
     return ap.parse_args()
 
 
@@ -341,6 +344,18 @@ def _reference_replica(job):
                     "end": time.time()})
     o.close()
     return out
+
+
+def profile_fp64_instr():
+    """FP64-pipe thread-instructions per interior cell of the FP64 kernels,
+    from the committed ncu summary (profiles/fp64_kernels_160.md); {} when
+    absent."""
+    import re
+    f = ROOT / "profiles" / "fp64_kernels_160.md"
+    if not f.exists():
+        return {}
+    return {m.group(1): float(m.group(2))
+            for m in re.finditer(r"fp64_instr_per_cell\s+(\w+):\s*([0-9.eE+]+)", f.read_text())}
 
 
 def run_reference(args, rank, world):
@@ -767,6 +782,29 @@ def main():
         print(json.dumps(channel_rollout(args.rollout, args.rollout_cells, args.krylov)))
         return
 
+    if args.profile_fp64:
+        from flow_structure_interaction_fem_ibm_gb300 import problem as P
+        pr = P.sphere(args.n, seed=args.seed, stretch=1.5)
+        s = PoissonSolver(pr.params, pr.x, pr.y, pr.z).set_boundary(pr.geom)   # plain FP64 handle
+        sh = pr.shape[::-1]
+        g = torch.Generator(device="cuda").manual_seed(1)
+        rnd = lambda: torch.randn(sh, dtype=torch.float64, device="cuda", generator=g)
+        u, v, w, pp = rnd(), rnd(), rnd(), rnd()
+        faces = [torch.zeros(sh, dtype=torch.float64, device="cuda") for _ in range(3)]
+        nlu0 = torch.zeros(sh, dtype=torch.float64, device="cuda")
+        fp = [t.data_ptr() for t in faces]
+        s.face_vel_rhs(1e-3, u.data_ptr(), v.data_ptr(), w.data_ptr(), *fp, nlu0.data_ptr())
+        s.correct_vel(1e-3, pp.data_ptr(), u.data_ptr(), v.data_ptr(), w.data_ptr(), *fp)
+        visc = torch.full(sh, 1e-3, dtype=torch.float64, device="cuda")
+        nl = [torch.zeros(sh, dtype=torch.float64, device="cuda") for _ in range(3)]
+        s.rhs_advec_diff(1e-3, [u.data_ptr(), v.data_ptr(), w.data_ptr()], fp, visc.data_ptr(),
+                         [t.data_ptr() for t in nl], advec_scheme=2)
+        out = {k: s.time_kernel(w_, 0, 1) for k, w_ in (("calc_residual", 5), ("line_x_fp64", 0), ("dfma", 10))}
+        torch.cuda.synchronize()
+        print(json.dumps({"profile": "fp64", "grid": args.n, "ms_and_bytes": out}))
+        s.close()
+        return
+
     if args.steps_only:
         from flow_structure_interaction_fem_ibm_gb300 import problem as P
         pr = P.sphere(args.n, seed=args.seed, stretch=1.5)
@@ -949,6 +987,30 @@ def main():
         steps_ops = projection_steps(s_mixed, pr, peak)
         steps_ops["device_step"] = device_time_step(args.n, args.seed, args.tol, args.krylov)
 
+    # FP64 kernels against both roofs: HBM (measured copy bandwidth) and the FP64 pipe
+    # (measured DFMA rate; FP64 thread-instructions per cell from the committed ncu summary)
+    fp64_roofline = None
+    if steps_ops is not None:
+        roof = steps_ops["fp64_roof"]["tflops"] * 1e12 / 2.0   # FP64-pipe thread-instructions per second
+        ipc = profile_fp64_instr()
+        cells = float(args.n) ** 3
+        k = {"face_vel_rhs": steps_ops["no_van_kan"]["face_vel_rhs"],
+             "correct_vel": steps_ops["no_van_kan"]["correct_vel"],
+             "rhs_advec_diff": steps_ops["rhs_advec_diff_cn"]}
+        ms_r, nb_r = s_fp64.time_kernel(5, 0, 20)
+        k["calc_residual"] = {"device_us": 1e3 * ms_r, "alg_bytes": nb_r}
+        ms_l, nb_l = s_fp64.time_kernel(0, 0, 20)
+        k["line_fp64_x"] = {"device_us": 1e3 * ms_l, "alg_bytes": nb_l}
+        fp64_roofline = {"fp64_roof_tflops": steps_ops["fp64_roof"]["tflops"], "hbm_peak_gbs": peak,
+                         "instr_source": "profiles/fp64_kernels_160.md (ncu sm__inst_executed_pipe_fp64, not this run)",
+                         "kernels": {}}
+        for name, rec in k.items():
+            t = rec["device_us"] * 1e-6
+            ent = {"device_us": rec["device_us"], "hbm_frac": rec["alg_bytes"] / t / 1e9 / peak}
+            if name in ipc:
+                ent["fp64_pipe_frac"] = ipc[name] * cells / t / roof
+            fp64_roofline["kernels"][name] = ent
+
     adjoint = None
     if rank == 0 and not args.no_adjoint:
         s_mixed.close()
@@ -958,7 +1020,7 @@ def main():
 
     rollout = None
     if rank == 0 and not args.no_rollout:
-        rollout = channel_rollout(20, krylov=args.krylov)
+        rollout = channel_rollout(200, krylov=args.krylov)   # config 5: 200 steps
 
     # roofline of the dominant kernel: level-1 FP32 line relaxation (k_line_wp<float,dir,8>),
     # durations from CUDA events around each launch inside the timed solves
@@ -1041,6 +1103,7 @@ def main():
         "wall_ms_per_step": 1e3 * mixed_wall / args.steps,
         "gpu_launches": int(mixed_launch), "clocks": clocks, "e2e": e2e, "roofline": roofline,
         "cpu_baseline": cpu, "config2": config2, "reference_model_256": model256, "tol_1e10": tol10,
+        "fp64_roofline": fp64_roofline,
         "adjoint": adjoint, "projection_steps": steps_ops, "channel_rollout": rollout,
         "setup_s": setup_s,
     }

@@ -193,9 +193,9 @@ cudaError_t init_ad_line_kernels();
 // one colour of the line sweep of itsolv_ad along axis dir on var with right-hand side r
 void launch_ad_line(int dir, int colour, const AdCoefArgs &c, double *var, const double *r, double *gam,
                     cudaStream_t s);
-// max |calc_residual_ad| of var into *maxbits (as the bits of a non-negative double, atomicMax)
-void launch_ad_residual(const AdCoefArgs &c, const double *var, const double *r, unsigned long long *maxbits,
-                        cudaStream_t s);
+// max |calc_residual_ad| over ncomp (2 or 3) components in one pass into *maxbits
+void launch_ad_residual_all(const AdCoefArgs &c, double *const var[3], const double *const r[3], int ncomp,
+                            unsigned long long *maxbits, cudaStream_t s);
 
 // ghost-cell velocities u, v, w (GCM_vel_set_bc_internal); coeffD 8 per ghost, bi the
 // body-intercept velocities (3 x n: u, v, w; null = zero), scratch 6 x n doubles

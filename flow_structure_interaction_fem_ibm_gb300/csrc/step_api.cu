@@ -320,8 +320,8 @@ int fsi_mg_solve_ad(void *handle, int advec_scheme, double dt, const fsi_mg_rhs_
     const int ncomp = three_d ? 3 : 2;
     auto residual = [&](double &mr) -> int {
         CK(cudaMemsetAsync(c.d_maxd, 0, sizeof(unsigned long long), c.s));
-        for (int q = 0; q < ncomp; ++q) launch_ad_residual(a, vel[q], rr[q], c.d_maxd, c.s);
-        c.launches += ncomp;
+        launch_ad_residual_all(a, vel, rr, ncomp, c.d_maxd, c.s);
+        c.launches++;
         unsigned long long bits = 0;
         CK(cudaMemcpyAsync(&bits, c.d_maxd, sizeof(bits), cudaMemcpyDeviceToHost, c.s));
         CK(cudaStreamSynchronize(c.s));

@@ -794,8 +794,13 @@ cudaError_t ad_wp_attr_dir()
     return ad_wp_attr<DIR, 8>();
 }
 
-__global__ void __launch_bounds__(TPB) k_ad_residual(AdCoefArgs A, const double *var, const double *r,
-                                                     unsigned long long *maxbits)
+// calc_residual_ad of up to three components in one pass: the seven row
+// coefficients of a cell are read once and applied to u, v and w (each
+// component by the rows of calc_residual_ad, IBM/CORE_SOLVE_AD.F90), max |res| over all.
+template <int NC>
+__global__ void __launch_bounds__(TPB) k_ad_residual_n(AdCoefArgs A, const double *v0, const double *v1,
+                                                       const double *v2, const double *r0, const double *r1,
+                                                       const double *r2, unsigned long long *maxbits)
 {
     const Dims &d = A.d;
     const int n0 = d.m[0] - 1, n1 = d.m[1] - 1, n2 = d.m[2] - 1;
@@ -806,13 +811,21 @@ __global__ void __launch_bounds__(TPB) k_ad_residual(AdCoefArgs A, const double 
         cell_of((unsigned)t, (unsigned)n0, (unsigned)n1, idx[0], idx[1], idx[2]);
         const long long o = d.idx(idx[0], idx[1], idx[2]);
         if (!(A.fl[o] & FB_IB)) {
-            double v = r[o] - var[o] * (1.0 + A.co[6][o]);
-            for (int a = 0; a < 3; ++a) {
-                const long long s = stride_of(d, a);
-                v = v - var[o - s] * A.co[2 * a][o];
-                v = v - var[o + s] * A.co[2 * a + 1][o];
+            double cm[3], cp[3];
+            for (int a = 0; a < 3; ++a) { cm[a] = A.co[2 * a][o]; cp[a] = A.co[2 * a + 1][o]; }
+            const double diag = 1.0 + A.co[6][o];
+            const double *vv[3] = {v0, v1, v2}, *rr[3] = {r0, r1, r2};
+#pragma unroll
+            for (int q = 0; q < NC; ++q) {
+                const double *var = vv[q];
+                double v = rr[q][o] - var[o] * diag;
+                for (int a = 0; a < 3; ++a) {
+                    const long long s = stride_of(d, a);
+                    v = v - var[o - s] * cm[a];
+                    v = v - var[o + s] * cp[a];
+                }
+                res = fmax(res, fabs(v));
             }
-            res = fabs(v);
         }
     }
     for (int off = 16; off > 0; off >>= 1) res = fmax(res, __shfl_xor_sync(0xffffffffu, res, off));
@@ -911,11 +924,14 @@ void launch_ad_line(int dir, int colour, const AdCoefArgs &c, double *var, const
     else k_ad_line<2><<<nblk(lines), TPB, 0, s>>>(c, var, r, gam, colour);
 }
 
-void launch_ad_residual(const AdCoefArgs &c, const double *var, const double *r, unsigned long long *maxbits,
-                        cudaStream_t s)
+void launch_ad_residual_all(const AdCoefArgs &c, double *const var[3], const double *const r[3], int ncomp,
+                            unsigned long long *maxbits, cudaStream_t s)
 {
     const long long n = (long long)(c.d.m[0] - 1) * (c.d.m[1] - 1) * (c.d.m[2] - 1);
-    k_ad_residual<<<nblk(n), TPB, 0, s>>>(c, var, r, maxbits);
+    if (ncomp == 3)
+        k_ad_residual_n<3><<<nblk(n), TPB, 0, s>>>(c, var[0], var[1], var[2], r[0], r[1], r[2], maxbits);
+    else
+        k_ad_residual_n<2><<<nblk(n), TPB, 0, s>>>(c, var[0], var[1], nullptr, r[0], r[1], nullptr, maxbits);
 }
 
 void launch_correct_vel(const StepArgs &a, cudaStream_t s)
