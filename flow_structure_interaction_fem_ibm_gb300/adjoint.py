@@ -30,8 +30,8 @@ the forward multigrid (MG_Solver): a multigrid solve on the transposed
 ghost-cell operator.  The left null vector w comes from the same solver:
 w = V 1 + d with A_eff^T d = -A_eff^T V 1.
 
-Everything here is FP64 torch on the solver's device; the ghost-row parts
-(nGhost values) are small sparse solves on the host.
+Everything here is FP64 torch on the solver's device, the ghost-row
+elimination included (fixed-point sweeps over the ghost-ghost couplings).
 """
 from __future__ import annotations
 
@@ -42,7 +42,6 @@ from typing import Optional
 
 import numpy as np
 import scipy.sparse as sp
-import scipy.sparse.linalg as spla
 import torch
 
 from .grid import Metrics
@@ -129,35 +128,51 @@ class ProjectionOperators:
         ntot = int(np.prod(self.shape))
         self.C_GF = sp.csr_matrix((vals_f, (rows_f, cols_f)), shape=(nG, ntot))
         self.C_GG = sp.csr_matrix((vals_g, (rows_g, cols_g)), shape=(nG, nG))
-        IG = sp.identity(nG, format="csc")
         self.gidx_np = gi
         self.gidx = torch.as_tensor(gi, device=self.dev)
         # ghost elimination p_G = (I - C_GG)^-1 C_GF p (extend) and its transpose
-        # (extend_T): C_GF and C_GF^T as padded-row gathers on the device and
-        # (I - C_GG)^-1 as a dense matrix there (host sparse LU above DENSE_GHOSTS)
+        # (extend_T): C_GF, C_GF^T, C_GG and C_GG^T as padded-row gathers on the
+        # device; (I - C_GG)^-1 by the fixed-point sweeps x <- r + C_GG x that the
+        # forward ghost rows use (the ghost-ghost couplings contract), with a
+        # sweep count fixed once here so that no call synchronises
         self._gCGF = self._padded(self.C_GF)
         CT = self.C_GF.T.tocsr()
         rows = np.nonzero(np.diff(CT.indptr))[0]            # stencil cells that receive cotangents
         self._ct_rows = torch.as_tensor(rows, device=self.dev)
         self._gCGFT = self._padded(CT[rows])
-        if nG <= self.DENSE_GHOSTS:
-            M = torch.eye(nG, dtype=torch.float64, device=self.dev) - torch.as_tensor(
-                self.C_GG.toarray(), device=self.dev)
-            self._Minv = torch.linalg.inv(M)
-            self._lu = self._luT = None
-        else:
-            self._Minv = None
-            self._lu = spla.splu((IG - self.C_GG).tocsc())
-            self._luT = spla.splu((IG - self.C_GG).T.tocsc())
+        self._gCGG = self._padded(self.C_GG)
+        self._gCGGT = self._padded(self.C_GG.T.tocsr())
+        self._ghost_sweeps = max(self._sweeps_to_converge(False), self._sweeps_to_converge(True))
 
-    DENSE_GHOSTS = 30000
+    GHOST_RTOL = 1e-16    # relative change at which the calibration sweeps stop
+    GHOST_MAX = 5000      # calibration cap; not converging by then is an error
+
+    def _sweeps_to_converge(self, transpose):
+        """Twice the sweeps a random right-hand side needs until the largest
+        change is below GHOST_RTOL of the largest value."""
+        if self.C_GG.nnz == 0:
+            return 1
+        pad = self._gCGGT if transpose else self._gCGG
+        g = torch.Generator(device="cpu").manual_seed(7)
+        r = torch.randn(self.nG, dtype=torch.float64, generator=g).to(self.dev)
+        x = r.clone()
+        for k in range(1, self.GHOST_MAX + 1):
+            xn = r + self._gather_mv(pad, x)
+            d = float((xn - x).abs().max())
+            x = xn
+            if d <= self.GHOST_RTOL * float(x.abs().max()):
+                return 2 * k
+        raise RuntimeError("ghost-row couplings do not contract: (I - C_GG) sweeps did not converge")
 
     def _ghost_solve(self, r, transpose):
         """(I - C_GG)^-1 r, or its transpose."""
-        if self._Minv is not None:
-            return (self._Minv.T if transpose else self._Minv) @ r
-        lu = self._luT if transpose else self._lu
-        return torch.as_tensor(lu.solve(r.cpu().numpy()), device=self.dev)
+        if self.C_GG.nnz == 0:
+            return r
+        pad = self._gCGGT if transpose else self._gCGG
+        x = r
+        for _ in range(self._ghost_sweeps):
+            x = r + self._gather_mv(pad, x)
+        return x
 
     def _padded(self, S):
         """Sparse rows as (cols, vals) padded to the longest row, for a
