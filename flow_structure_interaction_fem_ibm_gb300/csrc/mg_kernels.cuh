@@ -166,7 +166,8 @@ struct RhsAdArgs {
     const double *cm[3], *cp[3], *cb[3];   // dcinv(i) dinv(i), dcinv(i+1) dinv(i), (2 dinv(i)) dinv(i)
     Dims d;
     double dt;
-    int ab2, vankan, three_d;
+    double alfa;                // hybrid advection weight (used when hybrid is set)
+    int ab2, vankan, three_d, hybrid;
 };
 void launch_rhs_advec_diff(const RhsAdArgs &a, cudaStream_t s);
 

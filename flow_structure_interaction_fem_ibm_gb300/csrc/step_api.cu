@@ -216,6 +216,8 @@ int fsi_mg_rhs_advec_diff(void *handle, int advec_scheme, int frac_step_type, do
     a.dt = dt;
     a.ab2 = (advec_scheme == 1) ? 1 : 0;
     a.vankan = (frac_step_type == 1) ? 1 : 0;
+    a.alfa = c.p.alfa;
+    a.hybrid = (std::fabs(c.p.alfa) > 1.0e-3) ? 1 : 0;   // Hybrid (IBM/MAIN.F90:649-652)
     a.three_d = three_d ? 1 : 0;
     launch_rhs_advec_diff(a, c.s);
     c.last_ad = a; c.have_ad = true;

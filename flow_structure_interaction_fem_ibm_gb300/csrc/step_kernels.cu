@@ -480,7 +480,39 @@ __global__ void __launch_bounds__(TPB) k_rhs_advec_diff(RhsAdArgs A)
             const double *bc = A.bc[3 * q + a];
             const double ve = pp ? bc_at(bc, o) : fma(A.fx[a][i + 1], U[o + s], A.gx[a][i + 1] * uc);
             const double vw = mm ? bc_at(bc, o) : fma(A.fx[a][i], uc, A.gx[a][i] * U[o - s]);
-            const double term = (ve * A.face[a][o + s] - vw * A.face[a][o]) * A.dxinv[a][i];
+            const double F0 = A.face[a][o], F1 = A.face[a][o + s];
+            double term;
+            if (A.hybrid) {
+                // second-order upwind face values blended by alfa (IBM/CORE_RHS_AD.F90:150-382); the
+                // reference's 0/1 mask products are selects here.  iumm / iupp mark the first and
+                // last two cells of the axis (IBM/BOUNDARY_SET.F90:90-127), where the upwind value
+                // falls back to the central one.
+                const double *di = A.dxinv[a];
+                const int nn = d.m[a], nc = nn - 1;
+                const int imm = i - 2 > 0 ? i - 2 : 0, ipp = i + 2 < nn ? i + 2 : nn;
+                const double em1 = (di[i - 1] + 2.0 * di[i]) / (di[i - 1] + di[i]);
+                const double em2 = di[i] / (di[i - 1] + di[i]);
+                const double ep1 = (di[ipp] + 2.0 * di[i + 1]) / (di[ipp] + di[i + 1]);
+                // the x direction weights vel(ipp) with edxWeightp1, as the reference writes it
+                const double ep2 = (a == 0) ? ep1 : di[i + 1] / (di[ipp] + di[i + 1]);
+                const double wm1 = (di[imm] + 2.0 * di[i - 1]) / (di[imm] + di[i - 1]);
+                const double wm2 = di[i - 1] / (di[imm] + di[i - 1]);
+                const double wp1 = (di[i + 1] + 2.0 * di[i]) / (di[i + 1] + di[i]);
+                const double wp2 = di[i] / (di[i + 1] + di[i]);
+                const bool edge_m = (i <= 2), edge_p = (i >= nc - 1);
+                const double Um = U[o - s], Up = U[o + s];
+                const double e_from_m = edge_m ? ve : em1 * uc - em2 * Um;
+                const double e_from_p = edge_p ? ve : ep1 * Up - ep2 * U[o + (long long)(ipp - i) * s];
+                const double w_from_m = edge_m ? vw : wm1 * Um - wm2 * U[o - (long long)(i - imm) * s];
+                const double w_from_p = edge_p ? vw : wp1 * uc - wp2 * Up;
+                const double ve_up = pp ? bc_at(bc, o) : (signbit(F1) ? e_from_p : e_from_m);
+                const double vw_up = mm ? bc_at(bc, o) : (signbit(F0) ? w_from_p : w_from_m);
+                const double veh = (1.0 - A.alfa) * ve + A.alfa * ve_up;
+                const double vwh = (1.0 - A.alfa) * vw + A.alfa * vw_up;
+                term = (veh * F1 - vwh * F0) * A.dxinv[a][i];
+            } else {
+                term = (ve * F1 - vw * F0) * A.dxinv[a][i];
+            }
             adv = (a == 0) ? term : adv + term;
         }
         // rhs_loadAB

@@ -27,7 +27,7 @@ MODULE fsi_mg_gpu
     INTEGER(C_INT) :: iterMax_Poisson, iterMax_ad, bc(6), pbc(6)
     INTEGER(C_INT) :: internal_boundary_present, boundary_formulation
     INTEGER(C_INT) :: coarse_flag_mode, precision_mode, outer_krylov
-    REAL(C_DOUBLE) :: omega, restol_Poisson, restol_ad, ppp(6), outflow_area
+    REAL(C_DOUBLE) :: omega, restol_Poisson, restol_ad, ppp(6), outflow_area, alfa
   END TYPE fsi_mg_params
 
   ! device pointers of the momentum right-hand side (fsi_mg_rhs_ad_fields)
@@ -208,6 +208,7 @@ SUBROUTINE MG_initial()
   p%omega = omega; p%restol_Poisson = restol_Poisson; p%restol_ad = restol_ad
   p%ppp = [pppx1, pppx2, pppy1, pppy2, pppz1, pppz2]
   p%outflow_area = outflow_area
+  p%alfa = alfa                              ! hybrid advection weight (flow_parameters)
   rc = fsi_mg_create(p, x, y, z, fsi_mg_handle)
   IF (rc /= 0) CALL fsi_mg_abort('MG_initial', rc)
 END SUBROUTINE MG_initial

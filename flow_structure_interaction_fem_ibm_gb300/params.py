@@ -51,6 +51,7 @@ class FsiMgParams(ctypes.Structure):
         ("restol_ad", ctypes.c_double),
         ("ppp", ctypes.c_double * 6),
         ("outflow_area", ctypes.c_double),
+        ("alfa", ctypes.c_double),
     ]
 
 
@@ -85,6 +86,7 @@ class SolverParams:
     restol_ad: float = 1e-13
     ppp: tuple = (0.0,) * 6
     outflow_area: float = 1.0
+    alfa: float = 0.0
     extra: dict = field(default_factory=dict)
 
     def to_c(self) -> FsiMgParams:

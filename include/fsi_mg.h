@@ -55,6 +55,8 @@ typedef struct {
     double restol_ad;         /* ghost-row fixed-point tolerance */
     double ppp[6];            /* Dirichlet pressure values pppx1..pppz2 */
     double outflow_area;      /* from set_outflow_area (IBM/BOUNDARY_SET.F90:134-221) */
+    double alfa;              /* hybrid advection weight (IBM/MAIN.F90:461,649-652): |alfa| > 1e-3 blends
+                                 second-order upwind faces into rhs_advec (IBM/CORE_RHS_AD.F90:150-382) */
 } fsi_mg_params;
 
 /* MG_initial (IBM/CORE_MG.F90:31): level counts and sizes, coarse metrics,
@@ -218,8 +220,9 @@ typedef struct {
 int fsi_mg_set_bc(void *handle, const fsi_mg_bc_values *values, double *d_u, double *d_v, double *d_w,
                   double *const d_bc[9], double *correction_vel);
 
-/* rhs_advec_diff (IBM/CORE_RHS_AD.F90:13-75): central advection with the face
- * velocities (rhs_advec without the hybrid upwinding, :80-382), the
+/* rhs_advec_diff (IBM/CORE_RHS_AD.F90:13-75): advection with the face
+ * velocities (rhs_advec, :80-382: central, blended with second-order upwind
+ * faces by fsi_mg_params.alfa when |alfa| > 1e-3), the
  * Adams-Bashforth or Crank-Nicolson loading of the advection term
  * (rhs_loadAB, :385-430; advec_scheme 1 ADAMS_BASHFORTH2, 2 CRANK_NICOLSON1,
  * 3 CRANK_NICOLSON2), the explicit half of the diffusion with the total

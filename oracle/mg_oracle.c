@@ -1627,17 +1627,54 @@ int or_set_bc(or_ctx *c, const double *val, const double *freq, double time, dou
  * exp_weight NULL: 1.5 (no fresh cells). */
 static double arr_at(const double *a, size_t f) { return a ? a[f] : 0.0; }
 
+/* Second-neighbour flags of the hybrid scheme (IBM/BOUNDARY_SET.F90:90-127,
+ * set_outer_iup): iumm is 1 in the first two cells of an axis, iupp in the
+ * last two; the internal-boundary settings of SSM are not used under GCM. */
+static int hyb_mm(int i) { return (i == 1 || i == 2) ? 1 : 0; }
+static int hyb_pp(int i, int ncell) { return (i == ncell || i == ncell - 1) ? 1 : 0; }
+
+/* rhs_advec (IBM/CORE_RHS_AD.F90:80-382): central advection, blended with
+ * second-order upwind face values by alfa when Hybrid (|alfa| > 1e-3,
+ * IBM/MAIN.F90:649-652).  The x-direction upwind face value from the plus
+ * side weights vel(ipp) with edxWeightp1, as the reference writes it
+ * (:203-205); y and z use their p2 weights. */
 static void rhs_advec_one(or_ctx *c, const double *vel, double *nlvel, const double *bcx, const double *bcy,
                           const double *bcz, const double *face_u, const double *face_v, const double *face_w)
 {
     const int8_t *ium = c->fl[0], *iup = c->fl[1], *jum = c->fl[2], *jup = c->fl[3], *kum = c->fl[4], *kup = c->fl[5];
+    const double alfa = c->p.alfa;
+    const int hybrid = fabs(alfa) > 1.0e-3;
+    const int three_d = (c->p.ndim == DIM_3D);
+    const double *dxinv = c->dxinv[0], *dyinv = c->dxinv[1], *dzinv = c->dxinv[2];
+    const int nx = c->nx, ny = c->ny, nz = c->nz;
     for (int k = 1; k <= c->nzc; ++k)
         for (int j = 1; j <= c->nyc; ++j)
             for (int i = 1; i <= c->nxc; ++i) {
                 const size_t f = FI(c, i, j, k);
                 const double vele = (fxw(c, 0, i + 1) * vel[FI(c, i + 1, j, k)] + (1.0 - fxw(c, 0, i + 1)) * vel[f]) * (1 - iup[f]) + arr_at(bcx, f) * iup[f];
                 const double velw = (fxw(c, 0, i) * vel[f] + (1.0 - fxw(c, 0, i)) * vel[FI(c, i - 1, j, k)]) * (1 - ium[f]) + arr_at(bcx, f) * ium[f];
-                nlvel[f] = (vele * face_u[FI(c, i + 1, j, k)] - velw * face_u[f]) * c->dxinv[0][i];
+                if (hybrid) {
+                    const int imm = (i - 2 > 0) ? i - 2 : 0, ipp = (i + 2 < nx) ? i + 2 : nx;
+                    const double USign = copysign(1.0, face_u[f]), USignP = copysign(1.0, face_u[FI(c, i + 1, j, k)]);
+                    const double em1 = (dxinv[i - 1] + 2.0 * dxinv[i]) / (dxinv[i - 1] + dxinv[i]);
+                    const double em2 = dxinv[i] / (dxinv[i - 1] + dxinv[i]);
+                    const double ep1 = (dxinv[ipp] + 2.0 * dxinv[i + 1]) / (dxinv[ipp] + dxinv[i + 1]);
+                    const double wm1 = (dxinv[imm] + 2.0 * dxinv[i - 1]) / (dxinv[imm] + dxinv[i - 1]);
+                    const double wm2 = dxinv[i - 1] / (dxinv[imm] + dxinv[i - 1]);
+                    const double wp1 = (dxinv[i + 1] + 2.0 * dxinv[i]) / (dxinv[i + 1] + dxinv[i]);
+                    const double wp2 = dxinv[i] / (dxinv[i + 1] + dxinv[i]);
+                    const double mm = hyb_mm(i), pp = hyb_pp(i, c->nxc);
+                    const double vele_up = ((1.0 + USignP) * (mm * vele + (1 - mm) * (em1 * vel[f] - em2 * vel[FI(c, i - 1, j, k)]))
+                                            + (1.0 - USignP) * (pp * vele + (1 - pp) * (ep1 * vel[FI(c, i + 1, j, k)] - ep1 * vel[FI(c, ipp, j, k)])))
+                                           * 0.5 * (1 - iup[f]) + arr_at(bcx, f) * iup[f];
+                    const double velw_up = ((1.0 + USign) * (mm * velw + (1 - mm) * (wm1 * vel[FI(c, i - 1, j, k)] - wm2 * vel[FI(c, imm, j, k)]))
+                                            + (1.0 - USign) * (pp * velw + (1 - pp) * (wp1 * vel[f] - wp2 * vel[FI(c, i + 1, j, k)])))
+                                           * 0.5 * (1 - ium[f]) + arr_at(bcx, f) * ium[f];
+                    nlvel[f] = (((1.0 - alfa) * vele + alfa * vele_up) * face_u[FI(c, i + 1, j, k)]
+                                - ((1.0 - alfa) * velw + alfa * velw_up) * face_u[f]) * dxinv[i];
+                } else {
+                    nlvel[f] = (vele * face_u[FI(c, i + 1, j, k)] - velw * face_u[f]) * dxinv[i];
+                }
             }
     for (int k = 1; k <= c->nzc; ++k)
         for (int j = 1; j <= c->nyc; ++j)
@@ -1645,16 +1682,60 @@ static void rhs_advec_one(or_ctx *c, const double *vel, double *nlvel, const dou
                 const size_t f = FI(c, i, j, k);
                 const double veln = (fxw(c, 1, j + 1) * vel[FI(c, i, j + 1, k)] + (1.0 - fxw(c, 1, j + 1)) * vel[f]) * (1 - jup[f]) + arr_at(bcy, f) * jup[f];
                 const double vels = (fxw(c, 1, j) * vel[f] + (1.0 - fxw(c, 1, j)) * vel[FI(c, i, j - 1, k)]) * (1 - jum[f]) + arr_at(bcy, f) * jum[f];
-                nlvel[f] = nlvel[f] + (veln * face_v[FI(c, i, j + 1, k)] - vels * face_v[f]) * c->dxinv[1][j];
+                if (hybrid) {
+                    const int jmm = (j - 2 > 0) ? j - 2 : 0, jpp = (j + 2 < ny) ? j + 2 : ny;
+                    const double VSign = copysign(1.0, face_v[f]), VSignP = copysign(1.0, face_v[FI(c, i, j + 1, k)]);
+                    const double nm1 = (dyinv[j - 1] + 2.0 * dyinv[j]) / (dyinv[j - 1] + dyinv[j]);
+                    const double nm2 = dyinv[j] / (dyinv[j - 1] + dyinv[j]);
+                    const double np1 = (dyinv[jpp] + 2.0 * dyinv[j + 1]) / (dyinv[jpp] + dyinv[j + 1]);
+                    const double np2 = dyinv[j + 1] / (dyinv[jpp] + dyinv[j + 1]);
+                    const double sm1 = (dyinv[jmm] + 2.0 * dyinv[j - 1]) / (dyinv[jmm] + dyinv[j - 1]);
+                    const double sm2 = dyinv[j - 1] / (dyinv[jmm] + dyinv[j - 1]);
+                    const double sp1 = (dyinv[j + 1] + 2.0 * dyinv[j]) / (dyinv[j + 1] + dyinv[j]);
+                    const double sp2 = dyinv[j] / (dyinv[j + 1] + dyinv[j]);
+                    const double mm = hyb_mm(j), pp = hyb_pp(j, c->nyc);
+                    const double veln_up = ((1.0 + VSignP) * (mm * veln + (1 - mm) * (nm1 * vel[f] - nm2 * vel[FI(c, i, j - 1, k)]))
+                                            + (1.0 - VSignP) * (pp * veln + (1 - pp) * (np1 * vel[FI(c, i, j + 1, k)] - np2 * vel[FI(c, i, jpp, k)])))
+                                           * 0.5 * (1 - jup[f]) + arr_at(bcy, f) * jup[f];
+                    const double vels_up = ((1.0 + VSign) * (mm * vels + (1 - mm) * (sm1 * vel[FI(c, i, j - 1, k)] - sm2 * vel[FI(c, i, jmm, k)]))
+                                            + (1.0 - VSign) * (pp * vels + (1 - pp) * (sp1 * vel[f] - sp2 * vel[FI(c, i, j + 1, k)])))
+                                           * 0.5 * (1 - jum[f]) + arr_at(bcy, f) * jum[f];
+                    nlvel[f] = nlvel[f] + (((1.0 - alfa) * veln + alfa * veln_up) * face_v[FI(c, i, j + 1, k)]
+                                           - ((1.0 - alfa) * vels + alfa * vels_up) * face_v[f]) * dyinv[j];
+                } else {
+                    nlvel[f] = nlvel[f] + (veln * face_v[FI(c, i, j + 1, k)] - vels * face_v[f]) * dyinv[j];
+                }
             }
-    if (c->p.ndim == DIM_3D)
+    if (three_d)
         for (int k = 1; k <= c->nzc; ++k)
             for (int j = 1; j <= c->nyc; ++j)
                 for (int i = 1; i <= c->nxc; ++i) {
                     const size_t f = FI(c, i, j, k);
                     const double velf = (fxw(c, 2, k + 1) * vel[FI(c, i, j, k + 1)] + (1.0 - fxw(c, 2, k + 1)) * vel[f]) * (1 - kup[f]) + arr_at(bcz, f) * kup[f];
                     const double velb = (fxw(c, 2, k) * vel[f] + (1.0 - fxw(c, 2, k)) * vel[FI(c, i, j, k - 1)]) * (1 - kum[f]) + arr_at(bcz, f) * kum[f];
-                    nlvel[f] = nlvel[f] + (velf * face_w[FI(c, i, j, k + 1)] - velb * face_w[f]) * c->dxinv[2][k];
+                    if (hybrid) {
+                        const int kmm = (k - 2 > 0) ? k - 2 : 0, kpp = (k + 2 < nz) ? k + 2 : nz;
+                        const double WSign = copysign(1.0, face_w[f]), WSignP = copysign(1.0, face_w[FI(c, i, j, k + 1)]);
+                        const double fm1 = (dzinv[k - 1] + 2.0 * dzinv[k]) / (dzinv[k - 1] + dzinv[k]);
+                        const double fm2 = dzinv[k] / (dzinv[k - 1] + dzinv[k]);
+                        const double fp1 = (dzinv[kpp] + 2.0 * dzinv[k + 1]) / (dzinv[kpp] + dzinv[k + 1]);
+                        const double fp2 = dzinv[k + 1] / (dzinv[kpp] + dzinv[k + 1]);
+                        const double bm1 = (dzinv[kmm] + 2.0 * dzinv[k - 1]) / (dzinv[kmm] + dzinv[k - 1]);
+                        const double bm2 = dzinv[k - 1] / (dzinv[kmm] + dzinv[k - 1]);
+                        const double bp1 = (dzinv[k + 1] + 2.0 * dzinv[k]) / (dzinv[k + 1] + dzinv[k]);
+                        const double bp2 = dzinv[k] / (dzinv[k + 1] + dzinv[k]);
+                        const double mm = hyb_mm(k), pp = hyb_pp(k, c->nzc);
+                        const double velf_up = ((1.0 + WSignP) * (mm * velf + (1 - mm) * (fm1 * vel[f] - fm2 * vel[FI(c, i, j, k - 1)]))
+                                                + (1.0 - WSignP) * (pp * velf + (1 - pp) * (fp1 * vel[FI(c, i, j, k + 1)] - fp2 * vel[FI(c, i, j, kpp)])))
+                                               * 0.5 * (1 - kup[f]) + arr_at(bcz, f) * kup[f];
+                        const double velb_up = ((1.0 + WSign) * (mm * velb + (1 - mm) * (bm1 * vel[FI(c, i, j, k - 1)] - bm2 * vel[FI(c, i, j, kmm)]))
+                                                + (1.0 - WSign) * (pp * velb + (1 - pp) * (bp1 * vel[f] - bp2 * vel[FI(c, i, j, k + 1)])))
+                                               * 0.5 * (1 - kum[f]) + arr_at(bcz, f) * kum[f];
+                        nlvel[f] = nlvel[f] + (((1.0 - alfa) * velf + alfa * velf_up) * face_w[FI(c, i, j, k + 1)]
+                                               - ((1.0 - alfa) * velb + alfa * velb_up) * face_w[f]) * dzinv[k];
+                    } else {
+                        nlvel[f] = nlvel[f] + (velf * face_w[FI(c, i, j, k + 1)] - velb * face_w[f]) * dzinv[k];
+                    }
                 }
 }
 

@@ -46,6 +46,7 @@ typedef struct {
     double omega, restol_Poisson, restol_ad;
     double ppp[6];            /* Dirichlet pressure values x1,x2,y1,y2,z1,z2 */
     double outflow_area;
+    double alfa;              /* hybrid advection weight; |alfa| > 1e-3 switches the hybrid scheme on */
 } fsi_mg_params;
 
 typedef struct or_ctx or_ctx;
