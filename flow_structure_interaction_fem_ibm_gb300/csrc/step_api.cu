@@ -228,9 +228,8 @@ int fsi_mg_rhs_advec_diff(void *handle, int advec_scheme, int frac_step_type, do
 
 static int ad_coef_args(Ctx &c, int advec_scheme, double dt, const fsi_mg_rhs_ad_fields *fl, AdCoefArgs &a)
 {
-    if (advec_scheme < 1 || advec_scheme > 2)
-        return fail(-1, "advec_scheme must be 1 (AB2) or 2 (CRANK_NICOLSON1); CRANK_NICOLSON2 re-evaluates "
-                        "face_vel inside the iteration and is not supported");
+    if (advec_scheme < 1 || advec_scheme > 3)
+        return fail(-1, "advec_scheme must be 1 (AB2), 2 (CRANK_NICOLSON1) or 3 (CRANK_NICOLSON2)");
     if (!(dt > 0.0)) return fail(-1, "dt must be positive");
     TRY(step_ready(c));
     const bool three_d = (c.p.ndim == 3);
@@ -284,25 +283,32 @@ int fsi_mg_solve_ad(void *handle, int advec_scheme, double dt, const fsi_mg_rhs_
     bool zero_gradient = false;
     for (int q = 0; q < 6; ++q) zero_gradient |= (c.p.bc[q] == BC_ZERO_GRADIENT);
     const bool mass_consv = zero_gradient && c.p.boundary_formulation == GCM_METHOD;
+    // CRANK_NICOLSON2 re-evaluates face_vel of the current velocities after each set of
+    // sweeps (IBM/CORE_SOLVE_AD.F90:155-157 and :236)
+    const bool cn2 = (advec_scheme == 3);
     const long long n = c.L1.d.sxy * (c.nz + 2);
     StepArgs fv{};
     ZgArgs zg{};
-    if (mass_consv) {
+    if (mass_consv)
         for (int q = 0; q < 9; ++q)
             if (!fl->bc[q]) return fail(-1, "solve_ad with zero-gradient sides and a GCM body needs all nine bc arrays");
-        if (fl->p) return fail(-1, "solve_ad with zero-gradient sides and a GCM body re-evaluates face_vel, "
-                                   "which is restated for NO_VAN_KAN only (fields.p must be NULL)");
+    if (cn2 || mass_consv) {
+        if (fl->p) return fail(-1, "solve_ad re-evaluates face_vel (CRANK_NICOLSON2, or zero-gradient sides with a "
+                                   "GCM body), which is restated for NO_VAN_KAN only (fields.p must be NULL)");
         if (!d_w) return fail(-1, "null w");
-        if (!(c.p.outflow_area > 0.0)) return fail(-1, "outflow_area must be > 0 with zero-gradient BCs");
         if (!c.zg_div) TRY(c.alloc(&c.zg_div, (size_t)n));
         TRY(ensure_step_partials(c));
-        // face_vel into the step's faces; with dt = 1 the divergence sum is the net face flux
+        // face_vel into the step's faces (a missing bc array reads as 0); the divergence goes to
+        // scratch, and with dt = 1 its sum is the net face flux of the outflow balance
         fv = step_args(c, 1.0);
         const double *vl[3] = {d_u, d_v, d_w};
         double *fc[3] = {const_cast<double *>(fl->face_u), const_cast<double *>(fl->face_v),
                          const_cast<double *>(fl->face_w)};
         for (int d = 0; d < 3; ++d) { fv.vel[d] = vl[d]; fv.bc[d] = fl->bc[4 * d]; fv.face[d] = fc[d]; }
         fv.nlu0 = c.zg_div;
+    }
+    if (mass_consv) {
+        if (!(c.p.outflow_area > 0.0)) return fail(-1, "outflow_area must be > 0 with zero-gradient BCs");
         zg.nl[0] = fl->nlu; zg.nl[1] = fl->nlv; zg.nl[2] = fl->nlw;   // nlw may be NULL in 2D
         for (int q = 0; q < 9; ++q) zg.bc[q] = const_cast<double *>(fl->bc[q]);
         zg.fl = c.L1.fl;
@@ -359,6 +365,11 @@ int fsi_mg_solve_ad(void *handle, int advec_scheme, double dt, const fsi_mg_rhs_
                 launch_ad_coef(a, c.s);
                 c.launches++;
             }
+        }
+        if (cn2) {   // face_vel of the current velocities; the rows' convective terms follow it
+            launch_face_vel_rhs(fv, false, c.step_partials, c.step_cap, (double *)c.result, c.s);
+            launch_ad_coef(a, c.s);
+            c.launches += 3;
         }
         TRY(residual(mr));
         ++it;

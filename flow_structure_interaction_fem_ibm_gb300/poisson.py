@@ -202,7 +202,9 @@ class PoissonSolver:
         """solve_ad (IBM/CORE_SOLVE_AD.F90:12-267) on device pointers: vel =
         (u, v, w) INOUT, nl the right-hand sides.  With zero-gradient sides and
         a GCM body the faces, the zero-gradient planes of bc (all nine arrays)
-        and nl are INOUT too (GCM_enforce_global_mass_consv with 1/Re = reinv).
+        and nl are INOUT too (GCM_enforce_global_mass_consv with 1/Re = reinv);
+        advec_scheme 3 (CRANK_NICOLSON2) rewrites the faces every iteration with
+        face_vel of the current velocities (bc's normal components, 0 where NULL).
         Returns (status, iterations, maxres)."""
         f = self._ad_fields(faces, visc, nl, bc=bc, bcvisc=bcvisc, reinv=reinv)
         it, mr = ctypes.c_int(), ctypes.c_double()

@@ -28,7 +28,8 @@ class FractionalStep:
 
     ``bc_values`` are the 6 x 3 outer boundary values of set_bc (side x1..z2,
     component u, v, w); ``reinv`` is 1/Re (viscTot = reinv everywhere, a
-    laminar run); ``advec_scheme`` 1 ADAMS_BASHFORTH2 or 2 CRANK_NICOLSON1.
+    laminar run); ``advec_scheme`` 1 ADAMS_BASHFORTH2, 2 CRANK_NICOLSON1 or
+    3 CRANK_NICOLSON2 (face_vel re-evaluated inside the momentum iteration).
     The pressure solve uses the problem's solver parameters."""
 
     def __init__(self, problem, dt: float, reinv: float, bc_values, advec_scheme: int = 2,

@@ -237,8 +237,8 @@ int fsi_mg_rhs_advec_diff(void *handle, int advec_scheme, int frac_step_type, do
  * the boundary values bc of flagged faces, times the implicit coefficients
  * (diffusion with viscTot / bcvisc, Crank-Nicolson convection with the
  * faces), move from the operator to nlu, nlv, nlw (INOUT).  Uses face_*,
- * bc, viscTot, bcvisc and nl* of the fields; advec_scheme 1 (AB2) or 2
- * (CRANK_NICOLSON1). */
+ * bc, viscTot, bcvisc and nl* of the fields; advec_scheme 1 (AB2), or 2 / 3
+ * (CRANK_NICOLSON1 / 2, the same terms). */
 int fsi_mg_rhs_adjust_bc(void *handle, int advec_scheme, double dt, const fsi_mg_rhs_ad_fields *fields);
 
 /* solve_ad (IBM/CORE_SOLVE_AD.F90:12-267), line-SOR branch, stationary
@@ -250,7 +250,11 @@ int fsi_mg_rhs_adjust_bc(void *handle, int advec_scheme, double dt, const fsi_mg
  * solution), then under GCM the ghost-cell velocities of
  * fsi_mg_set_velocity_ghosts, until max |calc_residual_ad| <= restol_ad or
  * iterMax_ad iterations (status 1, the reference prints and continues).
- * advec_scheme 1 (AB2) or 2 (CRANK_NICOLSON1).  With zero-gradient sides and
+ * advec_scheme 1 (AB2), 2 (CRANK_NICOLSON1) or 3 (CRANK_NICOLSON2: after the
+ * sweeps, the ghost velocities and the mass balance, every iteration evaluates
+ * face_vel of the current velocities into fields.face_u..face_w (NO_VAN_KAN,
+ * fields.p NULL; a NULL bc array reads as 0) and the rows and the residual
+ * use the new faces, :155-157 and :236).  With zero-gradient sides and
  * a GCM body every iteration ends with GCM_enforce_global_mass_consv
  * (IBM/GCM_GLOBAL_MASS_CONSERVE.F90:6-252): face_vel of the current velocities
  * (NO_VAN_KAN; fields.p must be NULL) into fields.face_u..face_w, the net face

@@ -2116,6 +2116,12 @@ int or_solve_ad(or_ctx *c, int advec_scheme, double dt, double *const *faces_w, 
         }
         if (gcm && c->vg_on) gcm_vel_set_bc_internal(c, u, v, w);
         if (mass_consv) gcm_enforce_global_mass_consv(c, dt, reinv, u, v, w, faces_w, bc9, nlr);
+        /* CRANK_NICOLSON2: face_vel of the current velocities after the sweeps (and the
+         * ghost-cell velocities under GCM), IBM/CORE_SOLVE_AD.F90:155,236; the rows' convective
+         * terms and the residual then use the new faces */
+        if (advec_scheme == 3)
+            or_face_vel(c, 0, dt, u, v, w, NULL, bc9 ? bc9[0] : NULL, bc9 ? bc9[4] : NULL, bc9 ? bc9[8] : NULL,
+                        faces_w[0], faces_w[1], faces_w[2]);
         mr = 0.0;
         for (int q = 0; q < ncomp; ++q) {
             const double rq = calc_residual_ad(c, half_dt, faces, vel[q], rr[q]);

@@ -251,7 +251,9 @@ class Oracle:
         """solve_ad on vel = (u, v, w) in place; returns (iterations, maxres).
         With zero-gradient sides and a GCM body each iteration also rewrites
         faces, the zero-gradient planes of bc9 and nl (GCM_enforce_global_mass_consv
-        with 1/Re = reinv)."""
+        with 1/Re = reinv); with advec_scheme 3 (CRANK_NICOLSON2) each iteration
+        rewrites faces with face_vel of the current velocities (bc9's normal
+        components, or 0 without bc9)."""
         mr = ctypes.c_double()
         b9 = None if bc9 is None else (_dp * 9)(*[_p(a) for a in bc9])
         it = lib().or_solve_ad(self.h, advec_scheme, dt, (_dp * 3)(*[_p(a) for a in faces]), *(_p(a) for a in vel),

@@ -91,7 +91,7 @@ def oracle_rollout(pr, u0, v0, w0, steps, scheme):
 @pytest.mark.gpu
 @pytest.mark.parametrize("solver", [(1, 0), (1, 30), (0, 30)], ids=["mixed_stationary", "mixed_fgmres30",
                                                                     "fp64_fgmres30"])
-@pytest.mark.parametrize("scheme", [1, 2], ids=["ab2", "cn"])
+@pytest.mark.parametrize("scheme", [1, 2, 3], ids=["ab2", "cn", "cn2"])
 def test_gpu_channel_rollout_matches_oracle(gpu_built, scheme, solver):
     from flow_structure_interaction_fem_ibm_gb300.time_step import FractionalStep
     pr = small_channel()

@@ -74,7 +74,7 @@ def test_whole_time_step_matches_oracle(gpu_built, scheme):
         s.rhs_advec_diff(dt, vp, fp, dvisc.data_ptr(), nlp, nl_old=[t.data_ptr() for t in dold], bcvisc=bv,
                          advec_scheme=scheme)
         s.rhs_adjust_bc(dt, fp, dvisc.data_ptr(), nlp, bcvisc=bv, advec_scheme=scheme)
-        st_ad, _, mr_g = s.solve_ad(dt, fp, dvisc.data_ptr(), vp, nlp, bcvisc=bv, advec_scheme=scheme)
+        st_ad, _, mr_g = s.solve_ad(dt, fp, dvisc.data_ptr(), vp, nlp, bcvisc=bv, advec_scheme=scheme, bc=bp)
         assert st_ad == 0 and mr_g <= 1e-12
         dnlu0, dpp, dp = (dev(np.zeros(pr.shape, order="F")) for _ in range(3))
         s.face_vel_rhs(dt, *vp, *fp, dnlu0.data_ptr())
@@ -129,7 +129,7 @@ def oracle_channel_step(pr, f, dt, visc, scheme):
         corr = o.set_bc([u, v, w], bc9, CHANNEL_VALUES, time=dt)
         o.set_solve_ad(dt, visc, (visc,) * 3)
         o.rhs_adjust_bc(dt, faces, nl, bc9=bc9, advec_scheme=scheme)
-        it_ad, mr_ad = o.solve_ad(dt, faces, [u, v, w], nl, advec_scheme=scheme)
+        it_ad, mr_ad = o.solve_ad(dt, faces, [u, v, w], nl, advec_scheme=scheme, bc9=bc9)
         bcn = (bc9[0], bc9[4], bc9[8])
         faces = list(o.face_vel(dt, u, v, w, bc=bcn))
         nlu0, _ = o.rhs_poisson(dt, *faces)
@@ -148,7 +148,7 @@ def oracle_channel_step(pr, f, dt, visc, scheme):
         o.close()
 
 
-@pytest.mark.parametrize("scheme", [1, 2], ids=["ab2", "cn"])
+@pytest.mark.parametrize("scheme", [1, 2, 3], ids=["ab2", "cn", "cn2"])
 def test_channel_time_step_with_set_bc_matches_oracle(gpu_built, scheme):
     import torch
     from flow_structure_interaction_fem_ibm_gb300.poisson import PoissonSolver
@@ -186,7 +186,7 @@ def test_channel_time_step_with_set_bc_matches_oracle(gpu_built, scheme):
         corr = s.set_bc(vp, bp, CHANNEL_VALUES, time=dt)
         assert abs(corr - ref["corr"]) <= 1e-12 * abs(ref["corr"])
         s.rhs_adjust_bc(dt, fp, dvisc.data_ptr(), nlp, bc=bp, bcvisc=bv, advec_scheme=scheme)
-        st_ad, _, mr_g = s.solve_ad(dt, fp, dvisc.data_ptr(), vp, nlp, bcvisc=bv, advec_scheme=scheme)
+        st_ad, _, mr_g = s.solve_ad(dt, fp, dvisc.data_ptr(), vp, nlp, bcvisc=bv, advec_scheme=scheme, bc=bp)
         assert st_ad == 0 and mr_g <= 1e-12
         dnlu0, dpp, dp = (dev(np.zeros(pr.shape, order="F")) for _ in range(3))
         s.face_vel_rhs(dt, *vp, *fp, dnlu0.data_ptr(), d_bc=bn)

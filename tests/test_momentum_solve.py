@@ -91,6 +91,43 @@ def test_solve_ad_converges_to_the_discrete_operator(scheme):
         o.close()
 
 
+def test_crank_nicolson2_converges_with_the_faces_of_its_velocities():
+    """CRANK_NICOLSON2 (IBM/CORE_SOLVE_AD.F90:155-157) re-evaluates face_vel of
+    the current velocities after every set of sweeps: at convergence the faces
+    are face_vel of the returned velocities and those velocities satisfy the
+    momentum rows formed with them."""
+    pr = _box()
+    f = step_fields(pr, 5)
+    dt, nu = 0.05, 0.02
+    visc = np.full(pr.shape, nu, order="F")
+    faces = [0.5 * a for a in f["faces"]]
+    o = Oracle(pr)
+    try:
+        o.set_solve_ad(dt, visc, bcvisc=(visc, visc, visc))
+        vel = [a.copy(order="F") for a in (f["u"], f["v"], f["w"])]
+        rhs = [f["pPrime"], f["p"], f["u"]]
+        start = [a.copy(order="F") for a in faces]
+        it, mr = o.solve_ad(dt, faces, vel, rhs, advec_scheme=3)
+        assert 1 < it < 500 and mr <= 1e-12
+        assert max(np.abs(a - b).max() for a, b in zip(faces, start)) > 1e-3   # the faces moved
+        again = o.face_vel(dt, *vel, faces=[a.copy(order="F") for a in faces])
+        for a, b in zip(faces, again):
+            assert np.array_equal(a, b)
+        n = pr.params
+        I = (slice(1, n.nx), slice(1, n.ny), slice(1, n.nz))
+        for q in range(3):
+            res = rhs[q][I] - _operator(pr, dt, nu, faces, vel[q], 0.5 * dt)
+            assert np.abs(res).max() <= 1e-11
+        # the red-black line order reaches the same fixed point
+        vel2 = [a.copy(order="F") for a in (f["u"], f["v"], f["w"])]
+        faces2 = [0.5 * a for a in f["faces"]]
+        o.solve_ad(dt, faces2, vel2, rhs, advec_scheme=3, order=1)
+        for a, b in zip(vel, vel2):
+            assert np.abs(a - b).max() <= 1e-10 * max(1.0, np.abs(a).max())
+    finally:
+        o.close()
+
+
 def test_solve_ad_identity_without_viscosity_or_convection():
     pr = _box()
     f = step_fields(pr, 6)
@@ -130,7 +167,7 @@ def _setup(pr, seed):
 
 @pytest.mark.gpu
 @pytest.mark.parametrize("case", _gpu_cases(), ids=lambda c: c[0])
-@pytest.mark.parametrize("scheme", [1, 2], ids=["ab2", "cn"])
+@pytest.mark.parametrize("scheme", [1, 2, 3], ids=["ab2", "cn", "cn2"])
 @pytest.mark.parametrize("mode", ["one_iteration", "converged"])
 def test_gpu_solve_ad_matches_oracle(gpu_built, case, scheme, mode):
     import torch
@@ -152,8 +189,9 @@ def test_gpu_solve_ad_matches_oracle(gpu_built, case, scheme, mode):
             s.set_velocity_ghosts(g.coeffD, bi)
         o.set_solve_ad(dt, f["visc"], f["bcvisc"])
         vel = [f[k].copy(order="F") for k in "uvw"]
+        faces = [a.copy(order="F") for a in f["faces"]]   # CRANK_NICOLSON2 rewrites them
         order = 1 if mode == "one_iteration" else 0
-        it_ref, mr_ref = o.solve_ad(dt, f["faces"], vel, f["rhs"], advec_scheme=scheme, order=order)
+        it_ref, mr_ref = o.solve_ad(dt, faces, vel, f["rhs"], advec_scheme=scheme, order=order)
         dvel = [dev(f[k]) for k in "uvw"]
         dfaces = [dev(a) for a in f["faces"]]
         drhs = [dev(a) for a in f["rhs"]]
@@ -177,6 +215,10 @@ def test_gpu_solve_ad_matches_oracle(gpu_built, case, scheme, mode):
             got = host(dvel[q])
             err = np.abs(got - vel[q])[keep].max()
             assert err <= tol * max(1.0, np.abs(vel[q]).max()), (q, err)
+        if scheme == 3 and mode == "converged":   # the faces of the converged velocities
+            for q in range(3):
+                err = np.abs(host(dfaces[q]) - faces[q]).max()
+                assert err <= tol * max(1.0, np.abs(faces[q]).max()), ("face", q, err)
     finally:
         s.close()
         o.close()

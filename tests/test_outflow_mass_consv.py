@@ -84,7 +84,7 @@ def oracle_solve_ad(pr, inp, scheme):
     return dict(vel=vel, faces=faces, bc9=bc9, nl=nl, it=it, mr=mr, final_faces=final)
 
 
-@pytest.mark.parametrize("scheme", [1, 2], ids=["ab2", "cn"])
+@pytest.mark.parametrize("scheme", [1, 2, 3], ids=["ab2", "cn", "cn2"])
 def test_oracle_outflow_balance_in_solve_ad(scheme):
     pr = _channel_sphere()
     inp = oracle_inputs(pr, scheme)
@@ -112,7 +112,7 @@ def test_oracle_solve_ad_refuses_outflow_balance_without_bc():
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("scheme", [1, 2], ids=["ab2", "cn"])
+@pytest.mark.parametrize("scheme", [1, 2, 3], ids=["ab2", "cn", "cn2"])
 def test_gpu_outflow_balance_in_solve_ad_matches_oracle(gpu_built, scheme):
     import torch
     from flow_structure_interaction_fem_ibm_gb300.poisson import PoissonSolver
