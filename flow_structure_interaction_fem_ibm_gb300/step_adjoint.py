@@ -1,0 +1,975 @@
+"""Adjoint of the whole fractional time step (torch harness around the GPU
+step), for rollouts such as the sphere-wake channel.
+
+One step of ``time_step.FractionalStep`` (IBM/CORE_TIME_STEP.F90:201-267,
+NO_VAN_KAN, Crank-Nicolson, stationary body, laminar viscosity 1/Re) maps
+the state S = (u, v, w, face_u, face_v, face_w, bc9) to the next one:
+
+    nl   = rhs_advec_diff(vel, faces, bc9)          IBM/CORE_RHS_AD.F90:13-585
+    vel1, bc1 = set_bc(vel, t + dt)                 IBM/CORE_SET_BC.F90:22-377,
+                                                    IBM/CORE_SET_OUTER_GHOST.F90:1-63
+    nl1  = rhs_adjust_bc(faces, bc1, nl)            IBM/CORE_RHS_AD.F90:588-780
+    vel2, bc2 = solve_ad(vel1, nl1, bc1, faces)     IBM/CORE_SOLVE_AD.F90:12-267 (implicit)
+    faces3 = face_vel(vel2, bc2); f = rhs_poisson   IBM/CORE_FRAC_STEP_ROUTINES.F90:6-240,
+                                                    IBM/CORE_POISSON.F90:123-163
+    p    = solve_poisson(f)                         the GPU multigrid (implicit)
+    vel3, faces4 = correct_vel(p, vel2, faces3)     IBM/CORE_FRAC_STEP_ROUTINES.F90:244-448
+
+Every explicit routine is restated here as differentiable FP64 torch
+(``StepOperators``, checked against the oracle's literal loops), so torch
+autograd supplies their transposes.  The two implicit solves are
+``torch.autograd.Function``s: their forward runs the product (the C-ABI
+solve_ad and pressure solve on device arrays) and their backward solves the
+transposed linearised system:
+
+* solve_ad with zero-gradient outflow and a GCM body ends every iteration
+  with GCM_enforce_global_mass_consv (IBM/GCM_GLOBAL_MASS_CONSERVE.F90:6-252),
+  so its converged state X = (u, v, w, s) -- s the accumulated shift of the
+  zero-gradient planes -- solves F(X, theta) = 0: the momentum rows formed
+  with the faces face_vel(u, bc + s e) and the right-hand sides
+  nl + T(bc) - T(bc + s e), the ghost-cell velocity rows
+  (IBM/GCM_GHOSTCELL_VEL_UPDATE_UNSTRUC.F90:126-247), u = 0 in dead cells and
+  zero net face flux.  Backward: GMRES on J^T lambda = Xbar with J^T v a
+  vector-Jacobian product of F, then thetabar = -(dF/dtheta)^T lambda.
+* The pressure solve with zero-gradient outflow solves
+  B p = A_eff p + n1 (phi . p) / outflow_area = f, phi = A_eff^T vol (the
+  compatibility fixed point of GCM_enforce_p_compatibility,
+  IBM/GCM_GLOBAL_MASS_CONSERVE.F90:260-394); backward: B^T z = E^T pbar by
+  FGMRES preconditioned with one forward multigrid application, and
+  fbar = z - w_B (1 . z) / (1 . w_B), w_B the left null vector of B.
+
+``RolloutAdjoint`` runs the forward rollout on the product, keeps the state
+every ``checkpoint_every`` steps, and in the backward pass recomputes each
+segment's states and pulls the cotangent back step by step.
+"""
+from __future__ import annotations
+
+import copy
+import math
+from typing import Optional
+
+import numpy as np
+import torch
+
+from .adjoint import ProjectionOperators, _DeviceMG, fgmres, fortran_zeros, as_fortran
+from .grid import Metrics
+from .params import DIM_3D, GCM_METHOD
+
+_INC = ((0, 0, 0), (0, 1, 0), (1, 1, 0), (1, 0, 0), (0, 0, 1), (0, 1, 1), (1, 1, 1), (1, 0, 1))  # incI/J/K
+BC_DIRICHLET, BC_ZERO_GRADIENT, BC_SYMMETRY = 1, 2, 4
+
+
+class StepOperators:
+    """Differentiable FP64 restatement of the explicit routines of one
+    fractional step on one geometry (arrays indexed [i, j, k] over the full
+    (0:nx+1, 0:ny+1, 0:nz+1) layout), plus the residuals of the two implicit
+    solves.  Constant viscosity ``reinv`` (viscTot = bcvisc = 1/Re)."""
+
+    def __init__(self, problem, dt: float, reinv: float, bc_values, device="cpu", advec_scheme: int = 2):
+        p = problem.params
+        if advec_scheme not in (2, 3):
+            raise ValueError("the step adjoint restates the Crank-Nicolson schemes (advec_scheme 2 or 3)")
+        if abs(p.alfa) > 1e-3:
+            raise ValueError("the step adjoint restates central advection (alfa = 0)")
+        if p.ndim != DIM_3D:
+            raise ValueError("the step adjoint is 3D")
+        for s, t in enumerate(p.bc):
+            if t not in (BC_DIRICHLET, BC_ZERO_GRADIENT, BC_SYMMETRY):
+                raise ValueError(f"velocity side {s}: type {t} is not restated (Dirichlet, zero gradient, symmetry)")
+        self.pr = problem
+        self.dev = torch.device(device)
+        self.dt, self.reinv = float(dt), float(reinv)
+        self.values = np.asarray(bc_values, dtype=np.float64).reshape(6, 3)
+        self.n = (p.nx - 1, p.ny - 1, p.nz - 1)
+        self.shape = problem.shape
+        self.bctype = tuple(int(t) for t in p.bc)
+        self.zg = any(t == BC_ZERO_GRADIENT for t in self.bctype)
+        self.gcm = p.boundary_formulation == GCM_METHOD
+        self.mass_consv = self.zg and self.gcm
+        self.area = float(p.outflow_area)
+        T = lambda a: torch.as_tensor(np.ascontiguousarray(a, dtype=np.float64), device=self.dev)
+        ms = [Metrics(problem.x), Metrics(problem.y), Metrics(problem.z)]
+        self.fx = [T(m.fx) for m in ms]
+        self.dxinv = [T(m.dxinv) for m in ms]
+        self.dxcinv = [T(m.dxcinv) for m in ms]
+        self.dx = [T(m.dx) for m in ms]
+        g = problem.geom
+        self.fl = [T(f) for f in g.flags]
+        I = self.I = tuple(slice(1, m + 1) for m in self.n)
+        ib = T(g.iblank)[I]
+        gh = T(g.ghost)[I]
+        self.fluid = 1.0 - ib                     # interior cells, [i, j, k] over 1..n
+        self.ghostm = ib * gh
+        self.dead = ib * (1.0 - gh)
+        n0, n1, n2 = self.n
+        self.vol = self.dx[0][1:n0 + 1][:, None, None] * self.dx[1][1:n1 + 1][None, :, None] \
+            * self.dx[2][1:n2 + 1][None, None, :]
+        self.face_area = [self.vol * self.col(self.dxinv[a], a) for a in range(3)]
+        # set_solve_ad's implicit diffusion coefficients (IBM/CORE_SET_SOLVERS.F90:20-95)
+        visc = torch.full(self.shape, self.reinv, dtype=torch.float64, device=self.dev)
+        self.adm, self.adp, self.amd, self.apd, self.nuM, self.nuP = [], [], [], [], [], []
+        for a in range(3):
+            m, pp = self.cells(self.fl[2 * a], a), self.cells(self.fl[2 * a + 1], a)
+            fxm, fxp = self.col(self.fx[a], a), self.col(self.fx[a], a, 1)
+            nuP = (fxp * self.cells(visc, a, 1) + (1.0 - fxp) * self.cells(visc, a)) * (1 - pp) + self.reinv * pp
+            nuM = (fxm * self.cells(visc, a) + (1.0 - fxm) * self.cells(visc, a, -1)) * (1 - m) + self.reinv * m
+            self.nuM.append(nuM)
+            self.nuP.append(nuP)
+            tm = (self.col(self.dxcinv[a], a) * (1 - m) + self.col(self.dxinv[a], a) * m * 2.0) * self.col(self.dxinv[a], a)
+            tp = (self.col(self.dxcinv[a], a, 1) * (1 - pp) + self.col(self.dxinv[a], a) * pp * 2.0) \
+                * self.col(self.dxinv[a], a)
+            self.adm.append(-(0.5 * self.dt * nuM) * tm)
+            self.adp.append(-(0.5 * self.dt * nuP) * tp)
+            # rhs_bc_terms of the outflow balance: constant reinv (IBM/GCM_GLOBAL_MASS_CONSERVE.F90:90-252)
+            self.amd.append(-(0.50 * self.dt * self.reinv) * tm)
+            self.apd.append(-(0.50 * self.dt * self.reinv) * tp)
+        self._ghost_setup()
+
+    # --------------------------------------------------------- indexing --
+    def cells(self, X, a: int, off: int = 0):
+        """Interior cells of X shifted by `off` along axis a ([i, j, k] order)."""
+        sl = list(self.I)
+        sl[a] = slice(1 + off, self.n[a] + 1 + off)
+        return X[tuple(sl)]
+
+    def col(self, v, a: int, off: int = 0):
+        """1-D metric v at t + off along axis a, shaped to broadcast over the interior."""
+        shp = [1, 1, 1]
+        shp[a] = -1
+        return v[1 + off:self.n[a] + 1 + off].reshape(shp)
+
+    def plane(self, X, a: int, i: int):
+        """Plane i of axis a over the transverse range 0..n+1 that set_bc and
+        zg_correct_planes loop over (the arrays carry one more layer)."""
+        sl = [slice(0, m + 2) for m in self.n]
+        sl[a] = i
+        return X[tuple(sl)]
+
+    def zeros(self):
+        return torch.zeros(self.shape, dtype=torch.float64, device=self.dev)
+
+    def put_interior(self, base, val):
+        out = self.zeros() if base is None else base.clone()
+        out[self.I] = val
+        return out
+
+    def _faces_along(self, a, F1n, Flast, base):
+        """Full face array of axis a from faces 1..n (F1n) and face n+1 (Flast),
+        other entries from base; dead-cell faces zeroed under GCM
+        (GCM_set_face_vel_body, IBM/GCM_GHOSTCELL_VEL_UPDATE_UNSTRUC.F90:387-423)."""
+        F = torch.cat([F1n, Flast], dim=a)
+        if self.gcm:
+            dc = self.dead
+            z1 = torch.zeros_like(dc.narrow(a, 0, 1))
+            dm = torch.clamp(torch.cat([dc, z1], dim=a) + torch.cat([z1, dc], dim=a), max=1.0)
+            F = F * (1.0 - dm)
+        out = self.zeros() if base is None else base.clone()
+        sl = list(self.I)
+        sl[a] = slice(1, self.n[a] + 2)
+        out[tuple(sl)] = F
+        return out
+
+    def _mask_faces(self, a, Fm, Flast, b):
+        """The two mask loops of face_vel / correct_vel (IBM/CORE_FRAC_STEP_ROUTINES.F90:
+        178-195, :425-441): face t takes bc(t) if ium(t), else bc(t-1) if
+        iup(t-1), else its value; face n+1 bc(n) if iup(n)."""
+        n = self.n[a]
+        m, pp = self.cells(self.fl[2 * a], a), self.cells(self.fl[2 * a + 1], a)
+        first = Fm.narrow(a, 0, 1) * (1 - m.narrow(a, 0, 1)) + b.narrow(a, 0, 1) * m.narrow(a, 0, 1)
+        pprev, bprev = pp.narrow(a, 0, n - 1), b.narrow(a, 0, n - 1)
+        mt, bt = m.narrow(a, 1, n - 1), b.narrow(a, 1, n - 1)
+        mid = (Fm.narrow(a, 1, n - 1) * (1 - pprev) + bprev * pprev) * (1 - mt) + bt * mt
+        pl, bl = pp.narrow(a, n - 1, 1), b.narrow(a, n - 1, 1)
+        last = Flast * (1 - pl) + bl * pl
+        return torch.cat([first, mid], dim=a), last
+
+    # --------------------------------------------------------- face_vel --
+    def face_vel(self, vel, bcn, base=None):
+        """face_vel, NO_VAN_KAN (IBM/CORE_FRAC_STEP_ROUTINES.F90:6-240): faces of
+        the interior transverse range; bcn = (bcxu, bcyv, bczw)."""
+        out = []
+        for a in range(3):
+            U = vel[a]
+            b = self.cells(bcn[a], a) if bcn[a] is not None else torch.zeros_like(self.fluid)
+            m, pp = self.cells(self.fl[2 * a], a), self.cells(self.fl[2 * a + 1], a)
+            fxm, fxp = self.col(self.fx[a], a), self.col(self.fx[a], a, 1)
+            Uc, Um, Up = self.cells(U, a), self.cells(U, a, -1), self.cells(U, a, 1)
+            vm = (fxm * Uc + (1.0 - fxm) * Um) * (1 - m) + b * m
+            n = self.n[a]
+            vp_last = ((fxp * Up + (1.0 - fxp) * Uc) * (1 - pp) + b * pp).narrow(a, n - 1, 1)
+            F1n, Flast = self._mask_faces(a, vm, vp_last, b)
+            out.append(self._faces_along(a, F1n, Flast, None if base is None else base[a]))
+        return out
+
+    def rhs_poisson(self, faces):
+        """nlu0 = dtinv div(face) (1 - iblank) on the interior (IBM/CORE_POISSON.F90:273-285)."""
+        d = 0.0
+        for a in range(3):
+            d = d + (self.cells(faces[a], a, 1) - self.cells(faces[a], a)) * self.col(self.dxinv[a], a)
+        return self.put_interior(None, (1.0 / self.dt) * d * self.fluid)
+
+    def massflux(self, faces):
+        """Net face flux out of the fluid cells (IBM/GCM_GLOBAL_MASS_CONSERVE.F90:30-48)."""
+        t = 0.0
+        for a in range(3):
+            t = t + (self.cells(faces[a], a, 1) - self.cells(faces[a], a)) * self.face_area[a]
+        return (t * self.fluid).sum()
+
+    # --------------------------------------------------- rhs_advec_diff --
+    def rhs_advec_diff(self, vel, faces, bc9):
+        """Crank-Nicolson right-hand sides nl = vel - dt/2 N(vel) + dt/2 D(vel)
+        on the interior (rhs_advec central branch, rhs_loadAB, rhs_diff)."""
+        out = []
+        for q in range(3):
+            U = vel[q]
+            conv, diff = 0.0, 0.0
+            for a in range(3):
+                b = self.cells(bc9[3 * q + a], a)
+                m, pp = self.cells(self.fl[2 * a], a), self.cells(self.fl[2 * a + 1], a)
+                fxm, fxp = self.col(self.fx[a], a), self.col(self.fx[a], a, 1)
+                Uc, Um, Up = self.cells(U, a), self.cells(U, a, -1), self.cells(U, a, 1)
+                velp = (fxp * Up + (1.0 - fxp) * Uc) * (1 - pp) + b * pp
+                velm = (fxm * Uc + (1.0 - fxm) * Um) * (1 - m) + b * m
+                conv = conv + (velp * self.cells(faces[a], a, 1) - velm * self.cells(faces[a], a)) \
+                    * self.col(self.dxinv[a], a)
+                dinv = self.col(self.dxinv[a], a)
+                am = (self.col(self.dxcinv[a], a) * (1 - m) + dinv * m * 2.0) * dinv * self.nuM[a]
+                ap = (self.col(self.dxcinv[a], a, 1) * (1 - pp) + dinv * pp * 2.0) * dinv * self.nuP[a]
+                diff = diff + am * (Um * (1 - m) + b * m) - (am + ap) * Uc + ap * (Up * (1 - pp) + b * pp)
+            nl = self.cells(U, 0) - self.dt * (conv * 0.5) + 0.5 * self.dt * diff
+            out.append(self.put_interior(None, nl))
+        return out
+
+    def rhs_adjust_bc(self, faces, bc9, nl):
+        """Boundary values of flagged faces times the implicit coefficients move
+        to the right-hand sides (IBM/CORE_RHS_AD.F90:588-780)."""
+        h = 0.5 * self.dt
+        md, pd = [], []
+        for a in range(3):
+            m, pp = self.cells(self.fl[2 * a], a), self.cells(self.fl[2 * a + 1], a)
+            fxm, fxp = self.col(self.fx[a], a), self.col(self.fx[a], a, 1)
+            dinv = self.col(self.dxinv[a], a)
+            md.append(self.adm[a] - h * self.cells(faces[a], a) * ((1.0 - fxm) * (1 - m) + m) * dinv)
+            pd.append(self.adp[a] + h * self.cells(faces[a], a, 1) * (fxp * (1 - pp) + pp) * dinv)
+        out = []
+        for q in range(3):
+            r = self.cells(nl[q], 0)
+            for a in range(3):
+                b = self.cells(bc9[3 * q + a], a)
+                m, pp = self.cells(self.fl[2 * a], a), self.cells(self.fl[2 * a + 1], a)
+                r = r - md[a] * b * m - pd[a] * b * pp
+            out.append(self.put_interior(nl[q], r))
+        return out
+
+    def bc_terms(self, bc9):
+        """sum_a amd bc m + apd bc p per component (rhs_bc_terms with reinv)."""
+        out = []
+        for q in range(3):
+            t = 0.0
+            for a in range(3):
+                b = self.cells(bc9[3 * q + a], a)
+                m, pp = self.cells(self.fl[2 * a], a), self.cells(self.fl[2 * a + 1], a)
+                t = t + self.amd[a] * b * m + self.apd[a] * b * pp
+            out.append(t)
+        return out
+
+    # ------------------------------------------------------------ solve_ad --
+    def ad_rows(self, faces):
+        """Row coefficients (am, ap per axis, sum of ac) of itsolv_ad / calc_residual_ad
+        with the Crank-Nicolson convective terms (IBM/CORE_SOLVE_AD.F90:343-390)."""
+        h = 0.5 * self.dt
+        am, ap, acs = [], [], 0.0
+        for a in range(3):
+            m, pp = self.cells(self.fl[2 * a], a), self.cells(self.fl[2 * a + 1], a)
+            fxm, fxp = self.col(self.fx[a], a), self.col(self.fx[a], a, 1)
+            dinv = self.col(self.dxinv[a], a)
+            Fm, Fp = self.cells(faces[a], a), self.cells(faces[a], a, 1)
+            am.append(self.adm[a] - h * Fm * (1.0 - fxm) * dinv)
+            ap.append(self.adp[a] + h * Fp * fxp * dinv)
+            acs = acs + (-(self.adm[a] + self.adp[a]) + h * (Fp * (1.0 - fxp) * (1 - pp) - Fm * fxm * (1 - m)) * dinv)
+        return am, ap, acs
+
+    def row_op(self, U, rows):
+        am, ap, acs = rows
+        r = self.cells(U, 0) * (1.0 + acs)
+        for a in range(3):
+            m, pp = self.cells(self.fl[2 * a], a), self.cells(self.fl[2 * a + 1], a)
+            r = r + self.cells(U, a, -1) * am[a] * (1 - m) + self.cells(U, a, 1) * ap[a] * (1 - pp)
+        return r
+
+    def shift_zg(self, bc9, s):
+        """bc9 with the normal component of every zero-gradient plane shifted by
+        -s (minus sides) / +s (plus sides) (zg_correct_planes)."""
+        out = list(bc9)
+        for a in range(3):
+            for side in (0, 1):
+                if self.bctype[2 * a + side] != BC_ZERO_GRADIENT:
+                    continue
+                q = 4 * a
+                b = out[q].clone()
+                i = 1 if side == 0 else self.n[a]
+                self.plane(b, a, i).add_(-s if side == 0 else s)
+                out[q] = b
+        return out
+
+    def ad_system(self, U3, s, nl, bc9, faces_in):
+        """F(X, theta) of the converged solve_ad: momentum rows of fluid cells,
+        ghost-velocity rows, u = 0 in dead cells (interior arrays), and with the
+        outflow balance the net face flux / outflow_area."""
+        vel = [self.put_interior(None, U) for U in U3]
+        if self.mass_consv:
+            bcs = self.shift_zg(bc9, s)
+            faces = self.face_vel(vel, (bcs[0], bcs[4], bcs[8]))
+            t0, t1 = self.bc_terms(bc9), self.bc_terms(bcs)
+            rhs = [self.cells(nl[q], 0) + t0[q] - t1[q] for q in range(3)]
+            rs = self.massflux(faces) / self.area
+        else:
+            faces = faces_in
+            rhs = [self.cells(nl[q], 0) for q in range(3)]
+            rs = None
+        rows = self.ad_rows(faces)
+        out = []
+        for q in range(3):
+            r = self.fluid * (rhs[q] - self.row_op(vel[q], rows)) + self.dead * U3[q]
+            if self.nG:
+                r = r + self.ghost_residual(vel[q])
+            out.append(r)
+        return out, rs
+
+    # --------------------------------------------------- ghost velocities --
+    def _ghost_setup(self):
+        """Ghost-cell velocity rows u_g = -iw sum_r coeffGCMD(r, g) u(stencil r) (body
+        at rest, probeLengthNormalized 2: bw = 2, iw = 1) as flat gathers over the
+        [i, j, k] C-order flattening of the full array."""
+        g = self.pr.geom
+        self.nG = int(g.nGhost) if self.gcm else 0
+        if not self.nG:
+            return
+        sx, sy, sz = self.shape
+        lin = lambda i, j, k: (i * sy + j) * sz + k
+        self.iw = 1.0
+        gflat = np.array([lin(g.iG[n], g.jG[n], g.kG[n]) for n in range(self.nG)], dtype=np.int64)
+        rows, cols, vals = [], [], []
+        for n in range(self.nG):
+            for r, (a, b, c) in enumerate(_INC):
+                ii, jj, kk = g.iCI[n] + a, g.jCI[n] + b, g.kCI[n] + c
+                if (ii, jj, kk) == (g.iG[n], g.jG[n], g.kG[n]):
+                    continue   # the intercept value (zero for a body at rest)
+                rows.append(n); cols.append(lin(ii, jj, kk)); vals.append(float(g.coeffD[r, n]))
+        L = lambda a: torch.as_tensor(np.asarray(a, dtype=np.int64), device=self.dev)
+        self.g_flat = L(gflat)
+        self.g_rows, self.g_cols = L(rows), L(cols)
+        self.g_vals = torch.as_tensor(np.asarray(vals), device=self.dev)
+        # interior positions of the ghosts
+        self.g_int = L([((g.iG[n] - 1) * self.n[1] + (g.jG[n] - 1)) * self.n[2] + (g.kG[n] - 1)
+                        for n in range(self.nG)])
+        # ghost-ghost couplings for the fixed-point sweeps
+        pos = {int(v): n for n, v in enumerate(gflat)}
+        gg = [(r_, pos[int(c)], v) for r_, c, v in zip(rows, cols, vals) if int(c) in pos]
+        self.gg_rows = L([t[0] for t in gg]); self.gg_cols = L([t[1] for t in gg])
+        self.gg_vals = torch.as_tensor(np.asarray([t[2] for t in gg], dtype=np.float64), device=self.dev)
+
+    def ghost_gather(self, U):
+        """sum_r coeffGCMD(r, g) U(stencil r) for every ghost g (U a full array)."""
+        Uf = U.reshape(-1)
+        return torch.zeros(self.nG, dtype=U.dtype, device=self.dev).index_add(0, self.g_rows,
+                                                                              self.g_vals * Uf[self.g_cols])
+
+    def ghost_residual(self, U):
+        """u_g + iw sum_r coeffGCMD u(stencil r) at the ghosts, as an interior array."""
+        rg = U.reshape(-1)[self.g_flat] + self.iw * self.ghost_gather(U)
+        return torch.zeros(self.fluid.numel(), dtype=U.dtype, device=self.dev).index_add(
+            0, self.g_int, rg).reshape(self.fluid.shape)
+
+    def vel_ghosts(self, vel):
+        """Ghost-cell velocities of the corrected velocities (VelGhosts)."""
+        if not self.nG:
+            return list(vel)
+        return list(VelGhosts.apply(self, *vel))
+
+    # --------------------------------------------------------- correct_vel --
+    def correct_vel(self, p, vel, faces, bcn):
+        """correct_vel (IBM/CORE_FRAC_STEP_ROUTINES.F90:244-448): cell update of the
+        fluid cells, ghost-cell velocities, face pressure correction and masks."""
+        new = []
+        for a in range(3):
+            m, pp = self.cells(self.fl[2 * a], a), self.cells(self.fl[2 * a + 1], a)
+            fxm, fxp = self.col(self.fx[a], a), self.col(self.fx[a], a, 1)
+            Pc, Pm, Pp = self.cells(p, a), self.cells(p, a, -1), self.cells(p, a, 1)
+            pe = (fxp * Pp + (1.0 - fxp) * Pc) * (1 - pp) + Pc * pp
+            pw = (fxm * Pc + (1.0 - fxm) * Pm) * (1 - m) + Pc * m
+            g = (pe - pw) * self.col(self.dxinv[a], a)
+            new.append(self.put_interior(vel[a], self.cells(vel[a], 0) - self.dt * g * self.fluid))
+        if self.gcm:
+            new = self.vel_ghosts(new)
+        fout = []
+        for a in range(3):
+            n = self.n[a]
+            m, pp = self.cells(self.fl[2 * a], a), self.cells(self.fl[2 * a + 1], a)
+            b = self.cells(bcn[a], a) if bcn[a] is not None else torch.zeros_like(self.fluid)
+            Pc, Pm = self.cells(p, a), self.cells(p, a, -1)
+            pgm = (Pc - Pm) * self.col(self.dxcinv[a], a)
+            Fc = self.cells(faces[a], a) - self.dt * pgm * (1 - m)
+            pgp_last = ((self.cells(p, a, 1) - Pc) * self.col(self.dxcinv[a], a, 1)).narrow(a, n - 1, 1)
+            Flast = self.cells(faces[a], a, 1).narrow(a, n - 1, 1) - self.dt * pgp_last * (1 - pp.narrow(a, n - 1, 1))
+            F1n, FL = self._mask_faces(a, Fc, Flast, b)
+            fout.append(self._faces_along(a, F1n, FL, faces[a]))
+        return new, fout
+
+    # ----------------------------------------------------------- set_bc --
+    def set_bc(self, vel, bc9, time: float):
+        """set_bc's outer sides (Dirichlet, zero gradient, symmetry;
+        IBM/CORE_SET_BC.F90:22-298), enforce_global_mass_consv (:304-377) and
+        set_outer_ghost_vel (IBM/CORE_SET_OUTER_GHOST.F90:1-63).  Returns (vel, bc9)."""
+        del time   # the restated side types do not depend on time
+        bc = [b.clone() for b in bc9]
+        for a in range(3):
+            for side in (0, 1):
+                s = 2 * a + side
+                i = 1 if side == 0 else self.n[a]
+                for q in range(3):
+                    dst = self.plane(bc[3 * q + a], a, i)
+                    t = self.bctype[s]
+                    if t == BC_DIRICHLET:
+                        dst.fill_(float(self.values[s, q]))
+                    elif t == BC_ZERO_GRADIENT or (t == BC_SYMMETRY and q != a):
+                        dst.copy_(self.plane(vel[q], a, i))
+                    else:
+                        dst.fill_(0.0)
+        if self.zg:
+            t = 0.0
+            for a in range(3):
+                b = self.cells(bc[4 * a], a)
+                m, pp = self.cells(self.fl[2 * a], a), self.cells(self.fl[2 * a + 1], a)
+                t = t + (b * pp - b * m) * self.face_area[a]
+            massflux = (t * self.fluid).sum()
+            bc = self.shift_zg(bc, -massflux / self.area)   # correction_vel
+        out = [v.clone() for v in vel]
+        for a in range(3):
+            na = self.n[a]
+            for q in range(3):
+                va = out[q]
+                ba = bc[3 * q + a]
+                lo = 2.0 * self.plane(ba, a, 1) - self.plane(va, a, 1)
+                hi = 2.0 * self.plane(ba, a, na) - self.plane(va, a, na)
+                self.plane(va, a, 0).copy_(lo)
+                self.plane(va, a, na + 1).copy_(hi)
+        return out, bc
+
+
+class VelGhosts(torch.autograd.Function):
+    """Ghost-cell velocities u_g = -iw sum_r coeffGCMD u(stencil r) for u, v, w
+    (GCM_vel_set_bc_internal at rest): the fixed point of the ghost rows,
+    independent of the incoming ghost values; backward by the transposed
+    fixed point."""
+
+    SWEEPS_MAX = 5000
+
+    @staticmethod
+    def _fixed_point(ops, rhs, rows, cols, vals):
+        x = rhs
+        for _ in range(VelGhosts.SWEEPS_MAX):
+            xn = rhs - ops.iw * torch.zeros_like(rhs).index_add(0, rows, vals * x[cols])
+            d = float((xn - x).abs().max())
+            x = xn
+            if d <= 1e-16 * max(1.0, float(x.abs().max())):
+                return x
+        raise RuntimeError("ghost-cell velocity rows did not converge")
+
+    @staticmethod
+    def forward(ctx, ops, u, v, w):
+        ctx.ops = ops
+        outs = []
+        for U in (u, v, w):
+            Uc = U.detach().clone(memory_format=torch.contiguous_format)
+            flat = Uc.reshape(-1)
+            flat[ops.g_flat] = 0.0
+            rhs = -ops.iw * ops.ghost_gather(Uc)   # contributions of the non-ghost stencil cells
+            x = VelGhosts._fixed_point(ops, rhs, ops.gg_rows, ops.gg_cols, ops.gg_vals)
+            flat[ops.g_flat] = x
+            outs.append(Uc)
+        return tuple(outs)
+
+    @staticmethod
+    def backward(ctx, gu, gv, gw):
+        ops = ctx.ops
+        res = []
+        for G in (gu, gv, gw):
+            if G is None:
+                res.append(None)
+                continue
+            Gf = G.reshape(-1).clone()
+            gG = Gf[ops.g_flat].clone()
+            # (I + iw C_GG)^T y = gG
+            y = VelGhosts._fixed_point(ops, gG, ops.gg_cols, ops.gg_rows, ops.gg_vals)
+            Gf[ops.g_flat] = 0.0
+            # u_G = -iw (C_GF u + C_GG u_G): cotangent -iw C_GF^T y on the non-ghost stencil cells
+            contrib = torch.zeros_like(Gf).index_add(0, ops.g_cols, -ops.iw * ops.g_vals * y[ops.g_rows])
+            contrib[ops.g_flat] = 0.0
+            res.append((Gf + contrib).reshape(G.shape))
+        return (None, *res)
+
+
+# ------------------------------------------------------------------ GMRES --
+def gmres_flat(matvec, b, rtol=1e-12, m=40, max_apps=2000):
+    """Restarted GMRES(m) on 1-D vectors (classical Gram-Schmidt twice).
+    Returns (x, applications, relative residual)."""
+    beta0 = float(torch.linalg.vector_norm(b))
+    x = torch.zeros_like(b)
+    if beta0 == 0.0:
+        return x, 0, 0.0
+    N = b.numel()
+    V = torch.empty((m + 1, N), dtype=b.dtype, device=b.device)
+    apps, r, rel = 0, b.clone(), 1.0
+    while apps < max_apps:
+        beta = float(torch.linalg.vector_norm(r))
+        rel = beta / beta0
+        if rel <= rtol:
+            break
+        V[0] = r / beta
+        H = np.zeros((m + 1, m))
+        g = np.zeros(m + 1)
+        g[0] = beta
+        cs, sn = np.zeros(m), np.zeros(m)
+        k = 0
+        for j in range(m):
+            wv = matvec(V[j]).clone()
+            apps += 1
+            Vj = V[:j + 1]
+            h1 = Vj @ wv
+            wv -= Vj.T @ h1
+            h2 = Vj @ wv
+            wv -= Vj.T @ h2
+            hn_d = torch.linalg.vector_norm(wv)
+            hv = torch.cat([h1 + h2, hn_d.reshape(1)]).cpu().numpy()
+            H[:j + 1, j] = hv[:j + 1]
+            hn = float(hv[j + 1])
+            H[j + 1, j] = hn
+            for i in range(j):
+                a_, b_ = H[i, j], H[i + 1, j]
+                H[i, j], H[i + 1, j] = cs[i] * a_ + sn[i] * b_, -sn[i] * a_ + cs[i] * b_
+            rr = math.hypot(H[j, j], H[j + 1, j])
+            cs[j], sn[j] = (H[j, j] / rr, H[j + 1, j] / rr) if rr > 0 else (1.0, 0.0)
+            H[j, j], H[j + 1, j] = rr, 0.0
+            g[j + 1], g[j] = -sn[j] * g[j], cs[j] * g[j]
+            k = j + 1
+            if abs(g[j + 1]) <= 0.5 * rtol * beta0 or hn == 0.0 or apps >= max_apps:
+                break
+            V[j + 1] = wv / hn
+        y = np.linalg.solve(np.triu(H[:k, :k]), g[:k])
+        x += torch.as_tensor(y, dtype=b.dtype, device=b.device) @ V[:k]
+        r = b - matvec(x)
+        apps += 1
+    return x, apps, rel
+
+
+# --------------------------------------------------------------- backends --
+class OracleBackend:
+    """The implicit solves on the oracle (CPU; test infrastructure): solve_ad
+    with the outflow balance, and the pressure through the LSOR branch of
+    solve_poisson, whose smoother adds the outflow term nlw0."""
+
+    device = torch.device("cpu")
+
+    def __init__(self, problem, dt, reinv, advec_scheme=2):
+        from oracle.oracle import Oracle
+        pr = copy.deepcopy(problem)
+        pr.params.pp_solver_type = 1
+        self.pr = pr
+        self.o = Oracle(pr)
+        if pr.geom.nGhost:
+            self.o.set_vel_ghosts(pr.geom.coeffD, None)
+        sh = pr.shape
+        self.visc = np.full(sh, reinv, order="F")
+        self.o.set_solve_ad(dt, self.visc, (self.visc,) * 3)
+        self.dt, self.reinv, self.scheme = dt, reinv, advec_scheme
+        self.pPrime = np.zeros(sh, order="F")
+
+    @staticmethod
+    def _np(t):
+        return np.asfortranarray(t.detach().cpu().numpy())
+
+    def solve_ad(self, vel, nl, bc, faces):
+        v = [self._np(t) for t in vel]
+        n = [self._np(t) for t in nl]
+        b = [self._np(t) for t in bc]
+        f = [self._np(t) for t in faces]
+        it, mr = self.o.solve_ad(self.dt, f, v, n, advec_scheme=self.scheme, bc9=b, reinv=self.reinv)
+        T = lambda a: torch.as_tensor(np.ascontiguousarray(a))
+        return [T(a) for a in v], [T(a) for a in b], (it, mr)
+
+    def pressure(self, nlu0):
+        self.pr.nlu0 = self._np(nlu0)
+        sol = self.o.solve(self.pPrime)
+        if sol["status"] not in (0,):
+            raise RuntimeError(f"oracle pressure solve status {sol['status']}")
+        self.pPrime = sol["p"]
+        return torch.as_tensor(np.ascontiguousarray(sol["p"]))
+
+    def mg_apply(self, r):
+        var = np.zeros(self.pr.shape, order="F")
+        self.o.mg_solver(var, self._np(r))
+        return torch.as_tensor(np.ascontiguousarray(var))
+
+    def close(self):
+        self.o.close()
+
+
+class DeviceBackend:
+    """The implicit solves on the product (C ABI on device arrays): solve_ad and
+    the pressure solve with the problem's solver parameters, and one FP64
+    MG_Solver application for the transposed pressure solve."""
+
+    device = torch.device("cuda")
+
+    def __init__(self, problem, dt, reinv, advec_scheme=2):
+        from .poisson import PoissonSolver
+        self.pr = problem
+        p = problem.params
+        self.s = PoissonSolver(p, problem.x, problem.y, problem.z).set_boundary(problem.geom)
+        if problem.geom.nGhost:
+            self.s.set_velocity_ghosts(problem.geom.coeffD, None)
+        self.mg = _DeviceMG(problem, self.device)
+        shape = tuple(reversed(problem.shape))
+        z = lambda: torch.zeros(shape, dtype=torch.float64, device=self.device)
+        self.vel = [z() for _ in range(3)]
+        self.nl = [z() for _ in range(3)]
+        self.bc = [z() for _ in range(9)]
+        self.faces = [z() for _ in range(3)]
+        self.visc = torch.full(shape, float(reinv), dtype=torch.float64, device=self.device)
+        self.pPrime, self.nlu0, self.nlw0 = z(), z(), z()
+        self.dt, self.reinv, self.scheme = float(dt), float(reinv), int(advec_scheme)
+
+    @staticmethod
+    def _load(bufs, ts):
+        for b, t in zip(bufs, ts):
+            b.permute(2, 1, 0).copy_(t.detach())
+
+    @staticmethod
+    def _view(bufs):
+        return [b.permute(2, 1, 0).clone() for b in bufs]
+
+    def solve_ad(self, vel, nl, bc, faces):
+        self._load(self.vel, vel); self._load(self.nl, nl); self._load(self.bc, bc); self._load(self.faces, faces)
+        P = lambda ts: [t.data_ptr() for t in ts]
+        vis = self.visc.data_ptr()
+        st, it, mr = self.s.solve_ad(self.dt, P(self.faces), vis, P(self.vel), P(self.nl), bcvisc=[vis] * 3,
+                                     advec_scheme=self.scheme, bc=P(self.bc), reinv=self.reinv)
+        if st != 0:
+            raise RuntimeError(f"solve_ad status {st} (maxres {mr})")
+        return self._view(self.vel), self._view(self.bc), (it, mr)
+
+    def pressure(self, nlu0):
+        self.nlu0.permute(2, 1, 0).copy_(nlu0.detach())
+        st, it, mr, _, _ = self.s.solve_poisson_device(self.pPrime.data_ptr(), self.nlu0.data_ptr(),
+                                                        self.nlw0.data_ptr())
+        if st not in (0,):
+            raise RuntimeError(f"pressure solve status {st} (maxres {mr})")
+        return self.pPrime.permute(2, 1, 0).clone()
+
+    def mg_apply(self, r):
+        return self.mg.precondition(as_fortran(r))
+
+    def close(self):
+        self.s.close()
+        self.mg.close()
+
+
+# -------------------------------------------------------- implicit solves --
+class _SolveAD(torch.autograd.Function):
+    """solve_ad as a function of (vel, nl, bc, faces): forward by the backend,
+    backward by the implicit-function theorem on StepOperators.ad_system."""
+
+    @staticmethod
+    def forward(ctx, sa, *args):
+        vel, nl, bc, faces = args[0:3], args[3:6], args[6:15], args[15:18]
+        v2, b2, info = sa.backend.solve_ad(vel, nl, bc, faces)
+        sa.last_ad = info
+        ops = sa.ops
+        s = 0.0
+        if ops.mass_consv:
+            a, side = sa.zg_side
+            i = 1 if side == 0 else ops.n[a]
+            d = (ops.plane(b2[4 * a], a, i) - ops.plane(bc[4 * a].detach(), a, i))[1:-1, 1:-1]
+            s = float(d.mean()) * (-1.0 if side == 0 else 1.0)
+        ctx.sa, ctx.s = sa, s
+        ctx.save_for_backward(*v2, *[t.detach() for t in args[3:18]])
+        return (*v2, *b2)
+
+    @staticmethod
+    def backward(ctx, *g):
+        sa, ops = ctx.sa, ctx.sa.ops
+        saved = ctx.saved_tensors
+        v2, nl, bc, faces = saved[0:3], saved[3:6], saved[6:15], saved[15:18]
+        zero = lambda: torch.zeros(ops.shape, dtype=torch.float64, device=ops.dev)
+        gv = [zero() if t is None else t for t in g[0:3]]
+        gb = [zero() if t is None else t for t in g[3:12]]
+        # interior cotangents of the solution; the outer layers pass through from vel
+        Xbar = [ops.cells(t, 0) for t in gv]
+        gvel_in = [t.clone() for t in gv]
+        for t in gvel_in:
+            t[ops.I] = 0.0
+        sbar = torch.zeros((), dtype=torch.float64, device=ops.dev)
+        if ops.mass_consv:
+            for a in range(3):
+                for side in (0, 1):
+                    if ops.bctype[2 * a + side] == BC_ZERO_GRADIENT:
+                        i = 1 if side == 0 else ops.n[a]
+                        sbar = sbar + ops.plane(gb[4 * a], a, i).sum() * (-1.0 if side == 0 else 1.0)
+        with torch.enable_grad():
+            X = [ops.cells(t, 0).detach().clone().requires_grad_(True) for t in v2]
+            s = torch.tensor(ctx.s, dtype=torch.float64, device=ops.dev, requires_grad=True)
+            th = [t.detach().clone().requires_grad_(True) for t in (*nl, *bc, *faces)]
+            r, rs = ops.ad_system(X, s, th[0:3], th[3:12], th[12:15])
+            outs = list(r) + ([rs] if rs is not None else [])
+            xs = X + ([s] if rs is not None else [])
+            sizes = [t.numel() for t in outs]
+
+            def split(v):
+                parts, o = [], 0
+                for t, sz in zip(outs, sizes):
+                    parts.append(v[o:o + sz].reshape(t.shape))
+                    o += sz
+                return parts
+
+            def JT(v):
+                gr = torch.autograd.grad(outs, xs, grad_outputs=split(v), retain_graph=True)
+                return torch.cat([t.reshape(-1) for t in gr])
+
+            rhs = torch.cat([t.reshape(-1) for t in Xbar] + ([sbar.reshape(1)] if rs is not None else []))
+            lam, apps, rel = gmres_flat(JT, rhs, rtol=sa.rtol_ad)
+            sa.stats["ad_transposed_applications"] = sa.stats.get("ad_transposed_applications", 0) + apps
+            sa.stats["ad_transposed_rel_residual"] = max(sa.stats.get("ad_transposed_rel_residual", 0.0), rel)
+            gth = torch.autograd.grad(outs, th, grad_outputs=split(lam), allow_unused=True)
+        gth = [zero() if t is None else -t for t in gth]
+        gnl, gbc, gfaces = gth[0:3], gth[3:12], gth[12:15]
+        gbc = [a + b for a, b in zip(gb, gbc)]
+        return (None, *gvel_in, *gnl, *gbc, *gfaces)
+
+
+class _Pressure(torch.autograd.Function):
+    """The pressure solve B p = f (p with ghost and outer values): forward by
+    the backend, backward B^T z = E^T pbar and fbar = P_B^T z."""
+
+    @staticmethod
+    def forward(ctx, sa, nlu0):
+        ctx.sa = sa
+        return sa.backend.pressure(nlu0)
+
+    @staticmethod
+    def backward(ctx, gp):
+        sa = ctx.sa
+        s = sa.pops.extend_T(as_fortran(gp))
+        z = sa.solve_BT(s)
+        one = sa.pops.fluid
+        w = sa.left_null()
+        zhat = (z - w * (float((one * z).sum()) / float((one * w).sum()))) * one
+        return None, zhat.contiguous()
+
+
+class StepAdjoint:
+    """One fractional step as a torch graph (explicit routines restated,
+    implicit solves by the backend) and the transposed pressure operator."""
+
+    def __init__(self, problem, dt, reinv, bc_values, backend, advec_scheme=2):
+        self.pr = problem
+        self.backend = backend
+        dev = backend.device
+        self.ops = StepOperators(problem, dt, reinv, bc_values, device=dev, advec_scheme=advec_scheme)
+        self.pops = ProjectionOperators(problem, dev)
+        self.dt = float(dt)
+        self.rtol_ad, self.rtol_p = 1e-12, 1e-11
+        self.stats = {}
+        self.last_ad = None
+        ops = self.ops
+        self.zg_side = None
+        for s, t in enumerate(ops.bctype):
+            if t == BC_ZERO_GRADIENT:
+                self.zg_side = (s // 2, s % 2)
+                break
+        # n1: the outflow term of a unit shift of the zero-gradient planes (-1 minus, +1 plus)
+        n1 = ops.zeros()
+        acc = 0.0
+        for a in range(3):
+            for side in (0, 1):
+                if ops.bctype[2 * a + side] == BC_ZERO_GRADIENT:
+                    acc = acc - ops.col(ops.dxinv[a], a) * ops.cells(ops.fl[2 * a + side], a)
+        if ops.zg:
+            n1[ops.I] = acc * ops.fluid
+        self.n1 = as_fortran(n1)
+        self.area = ops.area
+        self._w = None
+
+    # pressure operator B = A_eff + n1 (vol^T A_eff) / area and its transpose
+    def apply_B(self, pf):
+        Ap = self.pops.apply_eff(pf)
+        if not self.ops.zg:
+            return Ap
+        return Ap + self.n1 * (float((self.pops.vol * Ap).sum()) / self.area)
+
+    def apply_BT(self, z):
+        if not self.ops.zg:
+            return self.pops.apply_eff_T(z)
+        return self.pops.apply_eff_T(z + self.pops.vol * (float((self.n1 * z).sum()) / self.area))
+
+    def _precond(self, v):
+        vol = self.pops.vol
+        vinv = torch.where(vol > 0, 1.0 / torch.where(vol > 0, vol, torch.ones_like(vol)), torch.zeros_like(vol))
+        return vol * (as_fortran(self.backend.mg_apply(as_fortran(vinv * v))) * self.pops.fluid)
+
+    def solve_BT(self, s, rtol=None):
+        z, apps, rel = fgmres(self.apply_BT, self._precond, s * self.pops.fluid, None,
+                              rtol=self.rtol_p if rtol is None else rtol, m=60)
+        self.stats["p_transposed_applications"] = self.stats.get("p_transposed_applications", 0) + apps
+        self.stats["p_transposed_rel_residual"] = max(self.stats.get("p_transposed_rel_residual", 0.0), rel)
+        return z
+
+    def left_null(self):
+        """w_B with w_B^T B = 0, w_B . 1_F = fluid volume."""
+        if self._w is None:
+            v1 = self.pops.vol.clone()
+            d = self.solve_BT(-self.apply_BT(v1), rtol=1e-13)
+            w = (v1 + d) * self.pops.fluid
+            self._w = w * (float(self.pops.vol.sum()) / float(w.sum()))
+        return self._w
+
+    # ---------------------------------------------------------------- step --
+    def step(self, vel, faces, bc, time=0.0):
+        """One step as a torch graph: returns (vel, faces, bc) after the step."""
+        ops = self.ops
+        nl = ops.rhs_advec_diff(vel, faces, bc)
+        vel1, bc1 = ops.set_bc(vel, bc, time + self.dt)
+        nl1 = ops.rhs_adjust_bc(faces, bc1, nl)
+        out = _SolveAD.apply(self, *vel1, *nl1, *bc1, *faces)
+        vel2, bc2 = list(out[0:3]), list(out[3:12])
+        bn = (bc2[0], bc2[4], bc2[8])
+        faces3 = ops.face_vel(vel2, bn, base=faces)
+        nlu0 = ops.rhs_poisson(faces3)
+        p = _Pressure.apply(self, nlu0)
+        vel3, faces4 = ops.correct_vel(p, vel2, faces3, bn)
+        return vel3, faces4, bc2
+
+    def step_vjp(self, state, cot, time=0.0):
+        """(state cotangent before the step) for the cotangent `cot` of the
+        state after it; state = (vel3, faces3, bc9) lists."""
+        vel, faces, bc = [[t.detach().clone().requires_grad_(True) for t in grp] for grp in state]
+        with torch.enable_grad():
+            out = self.step(vel, faces, bc, time)
+            flat_out = [*out[0], *out[1], *out[2]]
+            flat_cot = [*cot[0], *cot[1], *cot[2]]
+            keep = [(o, c) for o, c in zip(flat_out, flat_cot) if c is not None]
+            gr = torch.autograd.grad([o for o, _ in keep], [*vel, *faces, *bc], grad_outputs=[c for _, c in keep],
+                                     allow_unused=True)
+        z = lambda t: torch.zeros(self.ops.shape, dtype=torch.float64, device=self.ops.dev) if t is None else t
+        gr = [z(t) for t in gr]
+        return gr[0:3], gr[3:6], gr[6:15]
+
+
+def wake_plane_loss(problem, u, x_plane: float, device=None):
+    """Mean streamwise velocity over the fluid cells of the cell plane whose
+    centres lie nearest x = x_plane; returns (loss, plane index)."""
+    m = Metrics(problem.x)
+    n0 = problem.params.nx - 1
+    i = int(np.argmin(np.abs(m.xc[1:n0 + 1] - x_plane))) + 1
+    p = problem.params
+    fl = torch.as_tensor(np.ascontiguousarray(1.0 - problem.geom.iblank[i, 1:p.ny, 1:p.nz], dtype=np.float64),
+                         device=u.device if device is None else device)
+    return (u[i, 1:p.ny, 1:p.nz] * fl).sum() / fl.sum(), i
+
+
+# ---------------------------------------------------------------- rollout --
+class RolloutAdjoint:
+    """Forward rollout on the product (``time_step.FractionalStep``) with the
+    state (u, v, w, faces, bc9, pPrime) kept every ``checkpoint_every`` steps
+    over the last ``adjoint_steps`` steps; ``gradient`` recomputes each
+    segment's states from its checkpoint on the product and pulls the
+    cotangent of the final state back one step at a time through
+    ``StepAdjoint.step_vjp``.  The result is dL/d(state) at step
+    ``steps - adjoint_steps``."""
+
+    def __init__(self, problem, dt, reinv, bc_values, advec_scheme=2):
+        from .time_step import FractionalStep
+        self.pr, self.dt, self.reinv, self.scheme = problem, float(dt), float(reinv), int(advec_scheme)
+        self.values = np.asarray(bc_values, dtype=np.float64).reshape(6, 3)
+        self.fs = FractionalStep(problem, dt, reinv, self.values, advec_scheme=advec_scheme)
+        self.backend = DeviceBackend(problem, dt, reinv, advec_scheme)
+        self.sa = StepAdjoint(problem, dt, reinv, self.values, self.backend, advec_scheme)
+        self.checkpoints = {}
+        self.times = {}
+
+    def _save(self):
+        fs = self.fs
+        cl = lambda ts: [t.permute(2, 1, 0).clone() for t in ts]
+        return dict(vel=cl(fs.vel), faces=cl(fs.faces), bc=cl(fs.bc), pPrime=fs.pPrime.clone(), time=fs.time,
+                    ntime=fs.ntime)
+
+    def _load(self, st):
+        fs = self.fs
+        for dst, grp in ((fs.vel, st["vel"]), (fs.faces, st["faces"]), (fs.bc, st["bc"])):
+            for b, t in zip(dst, grp):
+                b.permute(2, 1, 0).copy_(t)
+        fs.pPrime.copy_(st["pPrime"])
+        fs.time, fs.ntime = st["time"], st["ntime"]
+
+    def forward(self, u0, v0, w0, steps: int, adjoint_steps: int, checkpoint_every: int):
+        """Runs `steps` product steps from (u0, v0, w0); returns the final state."""
+        if not 0 < adjoint_steps <= steps:
+            raise ValueError("0 < adjoint_steps <= steps")
+        self.steps, self.adj, self.every = steps, adjoint_steps, max(1, int(checkpoint_every))
+        self.first = steps - adjoint_steps
+        self.checkpoints.clear()
+        self.fs.start(u0, v0, w0)
+        torch.cuda.synchronize()
+        t0 = time_now()
+        for n in range(steps):
+            if n >= self.first and (n - self.first) % self.every == 0:
+                self.checkpoints[n] = self._save()
+            rec = self.fs.step()
+            if rec["ad_status"] != 0 or rec["poisson_status"] != 0 or rec["ghost_status"] != 0:
+                raise RuntimeError(f"forward step {n}: {rec}")
+        torch.cuda.synchronize()
+        self.times["forward_s"] = time_now() - t0
+        self.final = self._save()
+        return self.final
+
+    def gradient(self, loss_fn):
+        """dL/d(state at step steps - adjoint_steps) for L = loss_fn(vel) of the
+        final velocities ([i, j, k] tensors); returns (L, cotangent state)."""
+        torch.cuda.synchronize()
+        t0 = time_now()
+        vel = [t.detach().clone().requires_grad_(True) for t in self.final["vel"]]
+        with torch.enable_grad():
+            L = loss_fn(vel)
+            gv = torch.autograd.grad(L, vel, allow_unused=True)
+        sh = self.sa.ops.shape
+        z = lambda: torch.zeros(sh, dtype=torch.float64, device=self.sa.ops.dev)
+        cot = ([z() if g is None else g for g in gv], [z(), z(), z()], [z() for _ in range(9)])
+        starts = sorted(self.checkpoints)
+        recompute = 0.0
+        for c in reversed(starts):
+            end = min(c + self.every, self.steps)
+            # recompute the segment's states on the product
+            tr = time_now()
+            self._load(self.checkpoints[c])
+            states = [(self.checkpoints[c], c)]
+            for n in range(c, end - 1):
+                self.fs.step()
+                states.append((self._save(), n + 1))
+            torch.cuda.synchronize()
+            recompute += time_now() - tr
+            for st, n in reversed(states):
+                self.backend.pPrime.copy_(st["pPrime"])
+                cot = self.sa.step_vjp((st["vel"], st["faces"], st["bc"]), cot, time=st["time"])
+        torch.cuda.synchronize()
+        self.times["adjoint_s"] = time_now() - t0
+        self.times["recompute_s"] = recompute
+        return float(L), cot
+
+    def close(self):
+        self.fs.close()
+        self.backend.close()
+
+
+def time_now():
+    import time
+    return time.perf_counter()

@@ -74,7 +74,7 @@ def test_whole_time_step_matches_oracle(gpu_built, scheme):
         s.rhs_advec_diff(dt, vp, fp, dvisc.data_ptr(), nlp, nl_old=[t.data_ptr() for t in dold], bcvisc=bv,
                          advec_scheme=scheme)
         s.rhs_adjust_bc(dt, fp, dvisc.data_ptr(), nlp, bcvisc=bv, advec_scheme=scheme)
-        st_ad, _, mr_g = s.solve_ad(dt, fp, dvisc.data_ptr(), vp, nlp, bcvisc=bv, advec_scheme=scheme, bc=bp)
+        st_ad, _, mr_g = s.solve_ad(dt, fp, dvisc.data_ptr(), vp, nlp, bcvisc=bv, advec_scheme=scheme)
         assert st_ad == 0 and mr_g <= 1e-12
         dnlu0, dpp, dp = (dev(np.zeros(pr.shape, order="F")) for _ in range(3))
         s.face_vel_rhs(dt, *vp, *fp, dnlu0.data_ptr())
