@@ -67,6 +67,8 @@ def parse():
                     help="run N fractional steps of the 192x128x128 sphere channel (Re 300, dt 0.005) and print "
                          "their line instead of the solve benchmark")
     ap.add_argument("--rollout-cells", type=int, nargs=3, default=(192, 128, 128))
+    ap.add_argument("--rollout-adjoint", type=int, default=0,
+                    help="with --rollout: the adjoint over the last N steps (checkpoints every 10)")
     ap.add_argument("--no-rollout", action="store_true",
                     help="skip the 200-step sphere-wake channel rollout reported beside the solve benchmark")
     ap.add_argument("--adjoint-n", type=int, default=96)
@@ -609,7 +611,8 @@ def device_time_step(n, seed, tol, krylov, steps=3, reinv=1e-3, dt=1e-3):
             "host_copies_per_step": 0}
 
 
-def channel_rollout(steps, cells=(192, 128, 128), krylov=30, warmup=2, restol=1e-6, dt=0.005, re=300.0):
+def channel_rollout(steps, cells=(192, 128, 128), krylov=30, warmup=2, restol=1e-6, dt=0.005, re=300.0,
+                    adjoint_steps=50, checkpoint_every=10, x_plane=3.0):
     """The sphere-wake rollout: a 192 x 128 x 128 uniform channel on [0,6] x
     [0,4]^2, sphere of diameter 1 at (1.5, 2, 2) (GCM ghost cells), uniform
     inflow U = 1, zero-gradient outflow with the outflow mass balance,
@@ -621,7 +624,13 @@ def channel_rollout(steps, cells=(192, 128, 128), krylov=30, warmup=2, restol=1e
     FractionalStep keeps every field in HBM; a step is one call per routine.
     Reports steps/s over the untimed steps after `warmup`, the per-stage wall
     time of one extra instrumented step, the solvers' iteration counts, the
-    divergence of the corrected faces and the peak device memory."""
+    divergence of the corrected faces and the peak device memory.
+    With adjoint_steps > 0 the rollout runs through step_adjoint.RolloutAdjoint
+    (the same product step, with the state kept every checkpoint_every steps
+    over the last adjoint_steps), then the adjoint of the loss "mean
+    streamwise velocity in the cell plane nearest x = x_plane" back over those
+    steps, its cost against the forward cost of the same steps, and one
+    central-difference check of it on the product rollout."""
     import torch
     from flow_structure_interaction_fem_ibm_gb300 import problem as P
     from flow_structure_interaction_fem_ibm_gb300.grid import Metrics
@@ -638,17 +647,27 @@ def channel_rollout(steps, cells=(192, 128, 128), krylov=30, warmup=2, restol=1e
     zero = np.zeros(pr.shape, order="F")
     torch.cuda.reset_peak_memory_stats()
     free0, total = torch.cuda.mem_get_info()
-    fs = FractionalStep(pr, dt, 1.0 / re, inflow, advec_scheme=2).start(u0, zero, zero)
-    setup_s = time.perf_counter() - t0
-    for _ in range(warmup):
-        fs.step()
-    torch.cuda.synchronize()
-    t1 = time.perf_counter()
-    recs = [fs.step() for _ in range(steps)]
-    torch.cuda.synchronize()
-    wall = time.perf_counter() - t1
-    stage = fs.step(timed=True)
-    free1, _ = torch.cuda.mem_get_info()
+    ra = None
+    if adjoint_steps > 0:
+        from flow_structure_interaction_fem_ibm_gb300.step_adjoint import RolloutAdjoint
+        ra = RolloutAdjoint(pr, dt, 1.0 / re, inflow, advec_scheme=2)
+        fs = ra.fs
+        setup_s = time.perf_counter() - t0
+        ra.forward(u0, zero, zero, steps=warmup + steps, adjoint_steps=min(adjoint_steps, steps),
+                   checkpoint_every=checkpoint_every, warmup=warmup)
+        wall = ra.times["forward_s"]
+        recs = ra.records[warmup:]
+    else:
+        fs = FractionalStep(pr, dt, 1.0 / re, inflow, advec_scheme=2).start(u0, zero, zero)
+        setup_s = time.perf_counter() - t0
+        for _ in range(warmup):
+            fs.step()
+        torch.cuda.synchronize()
+        t1 = time.perf_counter()
+        recs = [fs.step() for _ in range(steps)]
+        torch.cuda.synchronize()
+        wall = time.perf_counter() - t1
+    free_fwd, _ = torch.cuda.mem_get_info()
     lib_bytes = int(fs.s.stats()["device_bytes"])
     n = [c for c in cells]
     fu, fv, fw = fs.faces
@@ -666,6 +685,12 @@ def channel_rollout(steps, cells=(192, 128, 128), krylov=30, warmup=2, restol=1e
     jj, ii = divmod(rem, n[0])
     closure = (div + dt * fs.nlw0[K, J, I] * fl).abs()
     u = fs.vel[0]
+    umax = float(u.abs().max())
+    adjoint = None
+    if ra is not None:
+        adjoint = rollout_adjoint_report(pr, ra, x_plane)
+    stage = fs.step(timed=True)
+    free1, _ = torch.cuda.mem_get_info()
     out = {"profile": "channel_rollout",
            "workload": f"channel_{n[0]}x{n[1]}x{n[2]}_[0,6]x[0,4]^2_sphere_d1_at_(1.5,2,2)_Re{re:g}_dt{dt:g}_CN_"
                        f"mixed_{'fgmres' + str(krylov) if krylov else 'stationary'}",
@@ -681,11 +706,58 @@ def channel_rollout(steps, cells=(192, 128, 128), krylov=30, warmup=2, restol=1e
                               "reference's own chain gives the same, to 1e-12); div + dt nlw0 is the projection's "
                               "residual everywhere",
            "restol_Poisson": restol,
-           "u_max": float(u.abs().max()), "time": fs.time, "ghost_cells": int(pr.geom.nGhost),
-           "device_bytes_in_use": int(free0 - free1), "torch_peak_bytes": int(torch.cuda.max_memory_allocated()),
-           "library_bytes": lib_bytes, "setup_s": setup_s}
-    fs.close()
+           "u_max": umax, "time": fs.time, "ghost_cells": int(pr.geom.nGhost),
+           "device_bytes_in_use_forward": int(free0 - free_fwd), "device_bytes_in_use": int(free0 - free1),
+           "torch_peak_bytes": int(torch.cuda.max_memory_allocated()),
+           "library_bytes": lib_bytes, "setup_s": setup_s, "adjoint": adjoint}
+    if ra is not None:
+        ra.close()
+    else:
+        fs.close()
     return out
+
+
+def rollout_adjoint_report(pr, ra, x_plane):
+    """The adjoint of the last ra.adj steps of a finished RolloutAdjoint
+    forward for L = mean streamwise velocity in the plane nearest x_plane,
+    timed against the forward cost of the same steps, and one central
+    difference of L on the product rollout in a random direction of the
+    velocities at the first adjoint step."""
+    import torch
+    from flow_structure_interaction_fem_ibm_gb300.step_adjoint import wake_plane_loss
+    loss_fn = lambda vel: wake_plane_loss(pr, vel[0], x_plane)[0]
+    torch.cuda.reset_peak_memory_stats()
+    L, cot = ra.gradient(loss_fn)
+    adj_peak = int(torch.cuda.max_memory_allocated())
+    fwd_per_step = ra.times["forward_s"] / max(1, ra.times["forward_steps"])
+    fwd_same = fwd_per_step * ra.adj
+    g = torch.Generator(device="cpu").manual_seed(12)
+    fl = torch.as_tensor(np.ascontiguousarray(1.0 - pr.geom.iblank), device="cuda")
+    inner = torch.zeros(pr.shape, dtype=torch.float64, device="cuda")
+    inner[ra.sa.ops.I] = 1.0
+    d = [torch.randn(pr.shape, dtype=torch.float64, generator=g).cuda() * fl * inner for _ in range(3)]
+    adj_dot = sum(float((a * b).sum()) for a, b in zip(cot[0], d))
+    h = 1e-3
+    base = ra.checkpoints[ra.first]
+    vals = []
+    for sgn in (1.0, -1.0):
+        st = dict(base)
+        st["vel"] = [a + sgn * h * b for a, b in zip(base["vel"], d)]
+        vals.append(float(loss_fn(ra.rerun(st, ra.adj))))
+    fd = (vals[0] - vals[1]) / (2 * h)
+    st = ra.sa.stats
+    return {"loss": "mean u over the fluid cells of the cell plane nearest x = %g" % x_plane, "L": L,
+            "adjoint_steps": ra.adj, "checkpoint_every": ra.every, "checkpoints": len(ra.checkpoints),
+            "adjoint_s": ra.times["adjoint_s"], "recompute_s": ra.times["recompute_s"],
+            "forward_s_same_steps": fwd_same, "adjoint_over_forward": ra.times["adjoint_s"] / fwd_same,
+            "adjoint_peak_torch_bytes": adj_peak,
+            "fd_check": {"h": h, "direction": "seeded N(0,1) on u, v, w of the fluid interior cells at the first "
+                                             "adjoint step", "fd": fd, "adjoint": adj_dot,
+                         "rel_diff": abs(fd - adj_dot) / max(abs(fd), 1e-300)},
+            "transposed_solves": {"momentum_gmres_applications": st.get("ad_transposed_applications", 0),
+                                  "momentum_max_rel_residual": st.get("ad_transposed_rel_residual", 0.0),
+                                  "pressure_fgmres_applications": st.get("p_transposed_applications", 0),
+                                  "pressure_max_rel_residual": st.get("p_transposed_rel_residual", 0.0)}}
 
 
 def rel_l2_mean_free(pr, a, b):
@@ -779,7 +851,8 @@ def main():
         return
 
     if args.rollout > 0:
-        print(json.dumps(channel_rollout(args.rollout, args.rollout_cells, args.krylov)))
+        print(json.dumps(channel_rollout(args.rollout, args.rollout_cells, args.krylov,
+                                         adjoint_steps=args.rollout_adjoint)))
         return
 
     if args.profile_fp64:

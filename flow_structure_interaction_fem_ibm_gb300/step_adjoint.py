@@ -911,26 +911,44 @@ class RolloutAdjoint:
         fs.pPrime.copy_(st["pPrime"])
         fs.time, fs.ntime = st["time"], st["ntime"]
 
-    def forward(self, u0, v0, w0, steps: int, adjoint_steps: int, checkpoint_every: int):
-        """Runs `steps` product steps from (u0, v0, w0); returns the final state."""
+    def forward(self, u0, v0, w0, steps: int, adjoint_steps: int, checkpoint_every: int, warmup: int = 0):
+        """Runs `steps` product steps from (u0, v0, w0); returns the final state.
+        times["forward_s"] covers the steps after the first `warmup`;
+        records holds the solvers' record of every step."""
         if not 0 < adjoint_steps <= steps:
             raise ValueError("0 < adjoint_steps <= steps")
         self.steps, self.adj, self.every = steps, adjoint_steps, max(1, int(checkpoint_every))
         self.first = steps - adjoint_steps
         self.checkpoints.clear()
+        self.records = []
         self.fs.start(u0, v0, w0)
         torch.cuda.synchronize()
         t0 = time_now()
         for n in range(steps):
+            if n == warmup:
+                torch.cuda.synchronize()
+                t0 = time_now()
             if n >= self.first and (n - self.first) % self.every == 0:
                 self.checkpoints[n] = self._save()
             rec = self.fs.step()
+            self.records.append(rec)
             if rec["ad_status"] != 0 or rec["poisson_status"] != 0 or rec["ghost_status"] != 0:
                 raise RuntimeError(f"forward step {n}: {rec}")
         torch.cuda.synchronize()
         self.times["forward_s"] = time_now() - t0
+        self.times["forward_steps"] = steps - min(warmup, steps)
         self.final = self._save()
         return self.final
+
+    def rerun(self, state, steps: int):
+        """The product's rollout of `steps` steps from a state (a checkpoint
+        dict, possibly perturbed); returns the final velocities ([i, j, k])."""
+        self._load(state)
+        for _ in range(steps):
+            rec = self.fs.step()
+            if rec["ad_status"] != 0 or rec["poisson_status"] != 0:
+                raise RuntimeError(f"rerun step: {rec}")
+        return [t.permute(2, 1, 0) for t in self.fs.vel]
 
     def gradient(self, loss_fn):
         """dL/d(state at step steps - adjoint_steps) for L = loss_fn(vel) of the
@@ -963,7 +981,7 @@ class RolloutAdjoint:
         torch.cuda.synchronize()
         self.times["adjoint_s"] = time_now() - t0
         self.times["recompute_s"] = recompute
-        return float(L), cot
+        return float(L.detach()), cot
 
     def close(self):
         self.fs.close()
