@@ -361,7 +361,7 @@ class _DeviceMG:
     (FGMRES(m) around MG_Solver, FP64) and single MG_Solver applications (the
     preconditioner of the transposed solve)."""
 
-    def __init__(self, problem, device):
+    def __init__(self, problem, device, mixed_precondition: bool = False):
         from .poisson import PoissonSolver
         self.ops_shape = problem.shape
         self.dev = device
@@ -369,6 +369,8 @@ class _DeviceMG:
         base.precision_mode = PRECISION_FP64
         one = copy.deepcopy(base)
         one.outer_krylov, one.iterMax_Poisson, one.restol_Poisson = 0, 1, 0.0
+        if mixed_precondition:   # one FP32 MG_Solver application inside the FP64 residual
+            one.precision_mode = 1
         self.s_one = PoissonSolver(one, problem.x, problem.y, problem.z).set_boundary(problem.geom)
         self.base = base
         self.problem = problem

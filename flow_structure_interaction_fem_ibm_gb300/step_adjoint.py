@@ -622,14 +622,14 @@ class DeviceBackend:
 
     device = torch.device("cuda")
 
-    def __init__(self, problem, dt, reinv, advec_scheme=2):
+    def __init__(self, problem, dt, reinv, advec_scheme=2, mixed_precondition=False):
         from .poisson import PoissonSolver
         self.pr = problem
         p = problem.params
         self.s = PoissonSolver(p, problem.x, problem.y, problem.z).set_boundary(problem.geom)
         if problem.geom.nGhost:
             self.s.set_velocity_ghosts(problem.geom.coeffD, None)
-        self.mg = _DeviceMG(problem, self.device)
+        self.mg = _DeviceMG(problem, self.device, mixed_precondition=mixed_precondition)
         shape = tuple(reversed(problem.shape))
         z = lambda: torch.zeros(shape, dtype=torch.float64, device=self.device)
         self.vel = [z() for _ in range(3)]
@@ -683,7 +683,12 @@ class _SolveAD(torch.autograd.Function):
     @staticmethod
     def forward(ctx, sa, *args):
         vel, nl, bc, faces = args[0:3], args[3:6], args[6:15], args[15:18]
-        v2, b2, info = sa.backend.solve_ad(vel, nl, bc, faces)
+        if sa.replay:
+            v2, b2, info = sa.replay.pop(0)
+        else:
+            v2, b2, info = sa.backend.solve_ad(vel, nl, bc, faces)
+            if sa.record is not None:
+                sa.record.append((v2, b2, info))
         sa.last_ad = info
         ops = sa.ops
         s = 0.0
@@ -716,6 +721,7 @@ class _SolveAD(torch.autograd.Function):
                     if ops.bctype[2 * a + side] == BC_ZERO_GRADIENT:
                         i = 1 if side == 0 else ops.n[a]
                         sbar = sbar + ops.plane(gb[4 * a], a, i).sum() * (-1.0 if side == 0 else 1.0)
+        t0 = _sync_time(ops.dev)
         with torch.enable_grad():
             X = [ops.cells(t, 0).detach().clone().requires_grad_(True) for t in v2]
             s = torch.tensor(ctx.s, dtype=torch.float64, device=ops.dev, requires_grad=True)
@@ -742,6 +748,7 @@ class _SolveAD(torch.autograd.Function):
             sa.stats["ad_transposed_rel_residual"] = max(sa.stats.get("ad_transposed_rel_residual", 0.0), rel)
             gth = torch.autograd.grad(outs, th, grad_outputs=split(lam), allow_unused=True)
         gth = [zero() if t is None else -t for t in gth]
+        sa.stats["ad_transposed_s"] = sa.stats.get("ad_transposed_s", 0.0) + _sync_time(ops.dev) - t0
         gnl, gbc, gfaces = gth[0:3], gth[3:12], gth[12:15]
         gbc = [a + b for a, b in zip(gb, gbc)]
         return (None, *gvel_in, *gnl, *gbc, *gfaces)
@@ -754,16 +761,23 @@ class _Pressure(torch.autograd.Function):
     @staticmethod
     def forward(ctx, sa, nlu0):
         ctx.sa = sa
-        return sa.backend.pressure(nlu0)
+        if sa.replay:
+            return sa.replay.pop(0)
+        p = sa.backend.pressure(nlu0)
+        if sa.record is not None:
+            sa.record.append(p)
+        return p
 
     @staticmethod
     def backward(ctx, gp):
         sa = ctx.sa
+        t0 = _sync_time(sa.ops.dev)
         s = sa.pops.extend_T(as_fortran(gp))
         z = sa.solve_BT(s)
         one = sa.pops.fluid
         w = sa.left_null()
         zhat = (z - w * (float((one * z).sum()) / float((one * w).sum()))) * one
+        sa.stats["p_transposed_s"] = sa.stats.get("p_transposed_s", 0.0) + _sync_time(sa.ops.dev) - t0
         return None, zhat.contiguous()
 
 
@@ -781,6 +795,9 @@ class StepAdjoint:
         self.rtol_ad, self.rtol_p = 1e-12, 1e-11
         self.stats = {}
         self.last_ad = None
+        # record: the implicit solves' outputs of a step are appended here;
+        # replay: a recorded list is consumed instead of solving again
+        self.record, self.replay = None, None
         ops = self.ops
         self.zg_side = None
         for s, t in enumerate(ops.bctype):
@@ -849,9 +866,29 @@ class StepAdjoint:
         vel3, faces4 = ops.correct_vel(p, vel2, faces3, bn)
         return vel3, faces4, bc2
 
-    def step_vjp(self, state, cot, time=0.0):
+    def step_recorded(self, state, time=0.0):
+        """One step without a graph; returns (next state, the recorded
+        outputs of its implicit solves) for step_vjp's replay."""
+        self.record, self.replay = [], None
+        try:
+            with torch.no_grad():
+                out = self.step(*state, time=time)
+            return out, self.record
+        finally:
+            self.record = None
+
+    def step_vjp(self, state, cot, time=0.0, replay=None):
         """(state cotangent before the step) for the cotangent `cot` of the
-        state after it; state = (vel3, faces3, bc9) lists."""
+        state after it; state = (vel3, faces3, bc9) lists.  With `replay`
+        (from step_recorded on the same state) the implicit solves are not
+        run again."""
+        self.replay = list(replay) if replay else None
+        try:
+            return self._step_vjp(state, cot, time)
+        finally:
+            self.replay = None
+
+    def _step_vjp(self, state, cot, time=0.0):
         vel, faces, bc = [[t.detach().clone().requires_grad_(True) for t in grp] for grp in state]
         with torch.enable_grad():
             out = self.step(vel, faces, bc, time)
@@ -882,18 +919,21 @@ class RolloutAdjoint:
     """Forward rollout on the product (``time_step.FractionalStep``) with the
     state (u, v, w, faces, bc9, pPrime) kept every ``checkpoint_every`` steps
     over the last ``adjoint_steps`` steps; ``gradient`` recomputes each
-    segment's states from its checkpoint on the product and pulls the
+    segment's states from its checkpoint (the step graph without gradients,
+    implicit solves on the product, their outputs kept) and pulls the
     cotangent of the final state back one step at a time through
-    ``StepAdjoint.step_vjp``.  The result is dL/d(state) at step
-    ``steps - adjoint_steps``."""
+    ``StepAdjoint.step_vjp`` with those solves replayed.  The result is
+    dL/d(state) at step ``steps - adjoint_steps``."""
 
-    def __init__(self, problem, dt, reinv, bc_values, advec_scheme=2):
+    def __init__(self, problem, dt, reinv, bc_values, advec_scheme=2, rtol_ad=1e-12, rtol_p=1e-11,
+                 mixed_precondition=False):
         from .time_step import FractionalStep
         self.pr, self.dt, self.reinv, self.scheme = problem, float(dt), float(reinv), int(advec_scheme)
         self.values = np.asarray(bc_values, dtype=np.float64).reshape(6, 3)
         self.fs = FractionalStep(problem, dt, reinv, self.values, advec_scheme=advec_scheme)
-        self.backend = DeviceBackend(problem, dt, reinv, advec_scheme)
+        self.backend = DeviceBackend(problem, dt, reinv, advec_scheme, mixed_precondition=mixed_precondition)
         self.sa = StepAdjoint(problem, dt, reinv, self.values, self.backend, advec_scheme)
+        self.sa.rtol_ad, self.sa.rtol_p = float(rtol_ad), float(rtol_p)
         self.checkpoints = {}
         self.times = {}
 
@@ -955,6 +995,9 @@ class RolloutAdjoint:
         final velocities ([i, j, k] tensors); returns (L, cotangent state)."""
         torch.cuda.synchronize()
         t0 = time_now()
+        self.sa.left_null()   # once per geometry (the first call solves for it)
+        torch.cuda.synchronize()
+        self.times["left_null_s"] = time_now() - t0
         vel = [t.detach().clone().requires_grad_(True) for t in self.final["vel"]]
         with torch.enable_grad():
             L = loss_fn(vel)
@@ -966,18 +1009,21 @@ class RolloutAdjoint:
         recompute = 0.0
         for c in reversed(starts):
             end = min(c + self.every, self.steps)
-            # recompute the segment's states on the product
+            # recompute the segment's states from its checkpoint (the step graph without
+            # gradients, implicit solves on the product), keeping each step's solves
             tr = time_now()
-            self._load(self.checkpoints[c])
-            states = [(self.checkpoints[c], c)]
-            for n in range(c, end - 1):
-                self.fs.step()
-                states.append((self._save(), n + 1))
+            ck = self.checkpoints[c]
+            self.backend.pPrime.copy_(ck["pPrime"])
+            S, t = (ck["vel"], ck["faces"], ck["bc"]), ck["time"]
+            seg = []
+            for n in range(c, end):
+                S1, rec = self.sa.step_recorded(S, time=t)
+                seg.append((S, rec, t))
+                S, t = S1, t + self.dt
             torch.cuda.synchronize()
             recompute += time_now() - tr
-            for st, n in reversed(states):
-                self.backend.pPrime.copy_(st["pPrime"])
-                cot = self.sa.step_vjp((st["vel"], st["faces"], st["bc"]), cot, time=st["time"])
+            for S, rec, t in reversed(seg):
+                cot = self.sa.step_vjp(S, cot, time=t, replay=rec)
         torch.cuda.synchronize()
         self.times["adjoint_s"] = time_now() - t0
         self.times["recompute_s"] = recompute
@@ -991,3 +1037,9 @@ class RolloutAdjoint:
 def time_now():
     import time
     return time.perf_counter()
+
+
+def _sync_time(dev):
+    if dev.type == "cuda":
+        torch.cuda.synchronize()
+    return time_now()

@@ -255,3 +255,29 @@ def test_two_step_adjoint_matches_central_differences(part):
         assert sa.stats["ad_transposed_rel_residual"] <= 1e-12
     finally:
         be.close()
+
+
+def test_replayed_solves_give_the_same_cotangent():
+    """step_vjp with the implicit solves recorded by step_recorded (the
+    rollout's recompute pass) equals step_vjp solving them again."""
+    pr = _channel()
+    be = OracleBackend(pr, DT, NU)
+    sa = StepAdjoint(pr, DT, NU, INFLOW, be)
+    sh = pr.shape
+    try:
+        u, v, w = _velocity(pr)
+        vel, bc = sa.ops.set_bc([T(u), T(v), T(w)], [torch.zeros(sh, dtype=torch.float64) for _ in range(9)], 0.0)
+        S0 = (vel, sa.ops.face_vel(vel, (bc[0], bc[4], bc[8])), bc)
+        be.pPrime[...] = 0.0
+        S1, rec = sa.step_recorded(S0)
+        assert len(rec) == 2
+        g = torch.Generator().manual_seed(2)
+        cot = tuple([torch.randn(sh, dtype=torch.float64, generator=g) for _ in grp] for grp in S1)
+        a = sa.step_vjp(S0, cot, replay=rec)
+        be.pPrime[...] = 0.0
+        b = sa.step_vjp(S0, cot)
+        for ga, gb in zip(a, b):
+            for x, y in zip(ga, gb):
+                assert float((x - y).abs().max()) <= 1e-12 * max(1.0, float(y.abs().max()))
+    finally:
+        be.close()
