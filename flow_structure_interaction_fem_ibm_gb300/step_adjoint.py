@@ -511,16 +511,19 @@ class VelGhosts(torch.autograd.Function):
 
 
 # ------------------------------------------------------------------ GMRES --
-def gmres_flat(matvec, b, rtol=1e-12, m=40, max_apps=2000):
-    """Restarted GMRES(m) on 1-D vectors (classical Gram-Schmidt twice).
-    Returns (x, applications, relative residual)."""
+def gmres_flat(matvec, b, rtol=1e-12, m=40, max_apps=2000, x0=None):
+    """Restarted GMRES(m) on 1-D vectors (classical Gram-Schmidt twice), from
+    x0 (or zero); the tolerance is relative to |b|.  Returns (x, applications,
+    relative residual)."""
     beta0 = float(torch.linalg.vector_norm(b))
-    x = torch.zeros_like(b)
+    x = torch.zeros_like(b) if x0 is None else x0.clone()
     if beta0 == 0.0:
-        return x, 0, 0.0
+        return torch.zeros_like(b), 0, 0.0
     N = b.numel()
     V = torch.empty((m + 1, N), dtype=b.dtype, device=b.device)
-    apps, r, rel = 0, b.clone(), 1.0
+    apps, rel = 0, 1.0
+    r = b.clone() if x0 is None else b - matvec(x)
+    apps += 0 if x0 is None else 1
     while apps < max_apps:
         beta = float(torch.linalg.vector_norm(r))
         rel = beta / beta0
@@ -743,7 +746,10 @@ class _SolveAD(torch.autograd.Function):
                 return torch.cat([t.reshape(-1) for t in gr])
 
             rhs = torch.cat([t.reshape(-1) for t in Xbar] + ([sbar.reshape(1)] if rs is not None else []))
-            lam, apps, rel = gmres_flat(JT, rhs, rtol=sa.rtol_ad)
+            x0 = sa._lam_prev if (sa.warm_start and sa._lam_prev is not None
+                                  and sa._lam_prev.shape == rhs.shape) else None
+            lam, apps, rel = gmres_flat(JT, rhs, rtol=sa.rtol_ad, x0=x0)
+            sa._lam_prev = lam
             sa.stats["ad_transposed_applications"] = sa.stats.get("ad_transposed_applications", 0) + apps
             sa.stats["ad_transposed_rel_residual"] = max(sa.stats.get("ad_transposed_rel_residual", 0.0), rel)
             gth = torch.autograd.grad(outs, th, grad_outputs=split(lam), allow_unused=True)
@@ -773,7 +779,8 @@ class _Pressure(torch.autograd.Function):
         sa = ctx.sa
         t0 = _sync_time(sa.ops.dev)
         s = sa.pops.extend_T(as_fortran(gp))
-        z = sa.solve_BT(s)
+        z = sa.solve_BT(s, z0=sa._z_prev if sa.warm_start else None)
+        sa._z_prev = z
         one = sa.pops.fluid
         w = sa.left_null()
         zhat = (z - w * (float((one * z).sum()) / float((one * w).sum()))) * one
@@ -798,6 +805,9 @@ class StepAdjoint:
         # record: the implicit solves' outputs of a step are appended here;
         # replay: a recorded list is consumed instead of solving again
         self.record, self.replay = None, None
+        # warm starts of the transposed solves from the previous step's solutions
+        self.warm_start = False
+        self._lam_prev, self._z_prev = None, None
         ops = self.ops
         self.zg_side = None
         for s, t in enumerate(ops.bctype):
@@ -834,9 +844,20 @@ class StepAdjoint:
         vinv = torch.where(vol > 0, 1.0 / torch.where(vol > 0, vol, torch.ones_like(vol)), torch.zeros_like(vol))
         return vol * (as_fortran(self.backend.mg_apply(as_fortran(vinv * v))) * self.pops.fluid)
 
-    def solve_BT(self, s, rtol=None):
-        z, apps, rel = fgmres(self.apply_BT, self._precond, s * self.pops.fluid, None,
-                              rtol=self.rtol_p if rtol is None else rtol, m=60)
+    def solve_BT(self, s, rtol=None, z0=None):
+        """B^T z = s by FGMRES(60), from z0 (or zero); rtol relative to |s|."""
+        rtol = self.rtol_p if rtol is None else rtol
+        s = s * self.pops.fluid
+        if z0 is None:
+            z, apps, rel = fgmres(self.apply_BT, self._precond, s, None, rtol=rtol, m=60)
+        else:
+            r0 = s - self.apply_BT(z0)
+            ns, nr = float(torch.linalg.vector_norm(s)), float(torch.linalg.vector_norm(r0))
+            if nr <= rtol * ns:
+                z, apps, rel = z0, 1, nr / max(ns, 1e-300)
+            else:
+                dz, apps, rel = fgmres(self.apply_BT, self._precond, r0, None, rtol=rtol * ns / nr, m=60)
+                z, apps, rel = z0 + dz, apps + 1, rel * nr / max(ns, 1e-300)
         self.stats["p_transposed_applications"] = self.stats.get("p_transposed_applications", 0) + apps
         self.stats["p_transposed_rel_residual"] = max(self.stats.get("p_transposed_rel_residual", 0.0), rel)
         return z
@@ -926,7 +947,7 @@ class RolloutAdjoint:
     dL/d(state) at step ``steps - adjoint_steps``."""
 
     def __init__(self, problem, dt, reinv, bc_values, advec_scheme=2, rtol_ad=1e-12, rtol_p=1e-11,
-                 mixed_precondition=False):
+                 mixed_precondition=False, warm_start=True):
         from .time_step import FractionalStep
         self.pr, self.dt, self.reinv, self.scheme = problem, float(dt), float(reinv), int(advec_scheme)
         self.values = np.asarray(bc_values, dtype=np.float64).reshape(6, 3)
@@ -934,6 +955,7 @@ class RolloutAdjoint:
         self.backend = DeviceBackend(problem, dt, reinv, advec_scheme, mixed_precondition=mixed_precondition)
         self.sa = StepAdjoint(problem, dt, reinv, self.values, self.backend, advec_scheme)
         self.sa.rtol_ad, self.sa.rtol_p = float(rtol_ad), float(rtol_p)
+        self.sa.warm_start = bool(warm_start)
         self.checkpoints = {}
         self.times = {}
 

@@ -196,11 +196,13 @@ def test_ghost_velocity_map_transpose():
         assert float(ops.ghost_residual(t.detach()).abs().max()) <= 1e-14
 
 
-@pytest.mark.parametrize("part", ["velocity", "faces", "bc"])
+@pytest.mark.parametrize("part", ["velocity", "faces", "bc", "velocity_warm_start"])
 def test_two_step_adjoint_matches_central_differences(part):
     pr = _channel()
     be = OracleBackend(pr, DT, NU)
     sa = StepAdjoint(pr, DT, NU, INFLOW, be)
+    if part == "velocity_warm_start":   # transposed solves started from the later step's solutions
+        sa.warm_start, part = True, "velocity"
     ops = sa.ops
     sh = pr.shape
     try:
