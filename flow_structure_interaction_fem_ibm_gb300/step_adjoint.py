@@ -368,6 +368,8 @@ class StepOperators:
         gg = [(r_, pos[int(c)], v) for r_, c, v in zip(rows, cols, vals) if int(c) in pos]
         self.gg_rows = L([t[0] for t in gg]); self.gg_cols = L([t[1] for t in gg])
         self.gg_vals = torch.as_tensor(np.asarray([t[2] for t in gg], dtype=np.float64), device=self.dev)
+        self.g_sweeps = VelGhosts.calibrate(self, self.gg_rows, self.gg_cols, self.gg_vals)
+        self.g_sweeps_T = VelGhosts.calibrate(self, self.gg_cols, self.gg_rows, self.gg_vals)
 
     def ghost_gather(self, U):
         """sum_r coeffGCMD(r, g) U(stencil r) for every ghost g (U a full array)."""
@@ -461,20 +463,37 @@ class VelGhosts(torch.autograd.Function):
     """Ghost-cell velocities u_g = -iw sum_r coeffGCMD u(stencil r) for u, v, w
     (GCM_vel_set_bc_internal at rest): the fixed point of the ghost rows,
     independent of the incoming ghost values; backward by the transposed
-    fixed point."""
+    fixed point.  Both run a sweep count fixed once per geometry (twice what
+    a random right-hand side needs to change by less than 1e-16), so no
+    sweep synchronises with the host."""
 
     SWEEPS_MAX = 5000
 
     @staticmethod
-    def _fixed_point(ops, rhs, rows, cols, vals):
+    def _sweep(ops, rhs, x, rows, cols, vals):
+        return rhs - ops.iw * torch.zeros_like(rhs).index_add(0, rows, vals * x[cols])
+
+    @staticmethod
+    def calibrate(ops, rows, cols, vals):
+        if rows.numel() == 0:
+            return 1
+        g = torch.Generator(device="cpu").manual_seed(7)
+        rhs = torch.randn(ops.nG, dtype=torch.float64, generator=g).to(ops.dev)
         x = rhs
-        for _ in range(VelGhosts.SWEEPS_MAX):
-            xn = rhs - ops.iw * torch.zeros_like(rhs).index_add(0, rows, vals * x[cols])
+        for k in range(1, VelGhosts.SWEEPS_MAX + 1):
+            xn = VelGhosts._sweep(ops, rhs, x, rows, cols, vals)
             d = float((xn - x).abs().max())
             x = xn
-            if d <= 1e-16 * max(1.0, float(x.abs().max())):
-                return x
-        raise RuntimeError("ghost-cell velocity rows did not converge")
+            if d <= 1e-16 * float(x.abs().max()):
+                return 2 * k
+        raise RuntimeError("ghost-cell velocity rows do not contract")
+
+    @staticmethod
+    def _fixed_point(ops, rhs, rows, cols, vals, sweeps):
+        x = rhs
+        for _ in range(sweeps):
+            x = VelGhosts._sweep(ops, rhs, x, rows, cols, vals)
+        return x
 
     @staticmethod
     def forward(ctx, ops, u, v, w):
@@ -485,7 +504,7 @@ class VelGhosts(torch.autograd.Function):
             flat = Uc.reshape(-1)
             flat[ops.g_flat] = 0.0
             rhs = -ops.iw * ops.ghost_gather(Uc)   # contributions of the non-ghost stencil cells
-            x = VelGhosts._fixed_point(ops, rhs, ops.gg_rows, ops.gg_cols, ops.gg_vals)
+            x = VelGhosts._fixed_point(ops, rhs, ops.gg_rows, ops.gg_cols, ops.gg_vals, ops.g_sweeps)
             flat[ops.g_flat] = x
             outs.append(Uc)
         return tuple(outs)
@@ -501,7 +520,7 @@ class VelGhosts(torch.autograd.Function):
             Gf = G.reshape(-1).clone()
             gG = Gf[ops.g_flat].clone()
             # (I + iw C_GG)^T y = gG
-            y = VelGhosts._fixed_point(ops, gG, ops.gg_cols, ops.gg_rows, ops.gg_vals)
+            y = VelGhosts._fixed_point(ops, gG, ops.gg_cols, ops.gg_rows, ops.gg_vals, ops.g_sweeps_T)
             Gf[ops.g_flat] = 0.0
             # u_G = -iw (C_GF u + C_GG u_G): cotangent -iw C_GF^T y on the non-ghost stencil cells
             contrib = torch.zeros_like(Gf).index_add(0, ops.g_cols, -ops.iw * ops.g_vals * y[ops.g_rows])
@@ -729,21 +748,8 @@ class _SolveAD(torch.autograd.Function):
             X = [ops.cells(t, 0).detach().clone().requires_grad_(True) for t in v2]
             s = torch.tensor(ctx.s, dtype=torch.float64, device=ops.dev, requires_grad=True)
             th = [t.detach().clone().requires_grad_(True) for t in (*nl, *bc, *faces)]
-            r, rs = ops.ad_system(X, s, th[0:3], th[3:12], th[12:15])
-            outs = list(r) + ([rs] if rs is not None else [])
-            xs = X + ([s] if rs is not None else [])
-            sizes = [t.numel() for t in outs]
-
-            def split(v):
-                parts, o = [], 0
-                for t, sz in zip(outs, sizes):
-                    parts.append(v[o:o + sz].reshape(t.shape))
-                    o += sz
-                return parts
-
-            def JT(v):
-                gr = torch.autograd.grad(outs, xs, grad_outputs=split(v), retain_graph=True)
-                return torch.cat([t.reshape(-1) for t in gr])
+            JT, outs, split = _ad_vjp(sa, ops, X, s, th)
+            rs = outs[3] if len(outs) > 3 else None
 
             rhs = torch.cat([t.reshape(-1) for t in Xbar] + ([sbar.reshape(1)] if rs is not None else []))
             x0 = sa._lam_prev if (sa.warm_start and sa._lam_prev is not None
@@ -758,6 +764,71 @@ class _SolveAD(torch.autograd.Function):
         gnl, gbc, gfaces = gth[0:3], gth[3:12], gth[12:15]
         gbc = [a + b for a, b in zip(gb, gbc)]
         return (None, *gvel_in, *gnl, *gbc, *gfaces)
+
+
+def _ad_vjp(sa, ops, X, s, th):
+    """F of solve_ad at (X, s, theta) and its vector-Jacobian product in X.
+    On the GPU the product is one CUDA graph (the forward and the warm-up run
+    on a side stream, so that autograd issues the backward kernels there, and
+    the capture records them): a GMRES iteration then costs one replay instead
+    of launching the backward pass's kernels one by one from Python.  Returns
+    (JT, outs, split)."""
+    side = None
+    if ops.dev.type == "cuda" and sa.graph_vjp:
+        side = torch.cuda.Stream()
+        side.wait_stream(torch.cuda.current_stream())
+    ctxm = torch.cuda.stream(side) if side is not None else _nullcontext()
+    with ctxm:
+        r, rs = ops.ad_system(X, s, th[0:3], th[3:12], th[12:15])
+        outs = list(r) + ([rs] if rs is not None else [])
+    xs = X + ([s] if rs is not None else [])
+    sizes = [t.numel() for t in outs]
+
+    def split(v):
+        parts, o = [], 0
+        for t, sz in zip(outs, sizes):
+            parts.append(v[o:o + sz].reshape(t.shape))
+            o += sz
+        return parts
+
+    def eager(v):
+        gr = torch.autograd.grad(outs, xs, grad_outputs=split(v), retain_graph=True)
+        return torch.cat([t.reshape(-1) for t in gr])
+
+    if side is None:
+        return eager, outs, split
+    try:
+        with torch.cuda.stream(side):
+            static_v = [torch.zeros_like(t) for t in outs]
+            for _ in range(2):
+                torch.autograd.grad(outs, xs, grad_outputs=static_v, retain_graph=True)
+            graph = torch.cuda.CUDAGraph()
+            with torch.cuda.graph(graph, stream=side):
+                static_g = torch.autograd.grad(outs, xs, grad_outputs=static_v, retain_graph=True)
+                static_out = torch.cat([t.reshape(-1) for t in static_g])
+        torch.cuda.current_stream().wait_stream(side)
+    except RuntimeError as e:   # capture refused: the eager product
+        torch.cuda.current_stream().wait_stream(side)
+        sa.stats["vjp_graph_error"] = str(e)[:200]
+        return eager, outs, split
+    sa.stats["vjp_graph"] = True
+
+    def graphed(v):
+        for dst, src in zip(static_v, split(v)):
+            dst.copy_(src)
+        graph.replay()
+        return static_out.clone()
+
+    graphed.graph = graph
+    return graphed, outs, split
+
+
+class _nullcontext:
+    def __enter__(self):
+        return None
+
+    def __exit__(self, *a):
+        return False
 
 
 class _Pressure(torch.autograd.Function):
@@ -808,6 +879,8 @@ class StepAdjoint:
         # warm starts of the transposed solves from the previous step's solutions
         self.warm_start = False
         self._lam_prev, self._z_prev = None, None
+        # the GMRES matrix-vector product of the transposed solve_ad system as one CUDA graph
+        self.graph_vjp = True
         ops = self.ops
         self.zg_side = None
         for s, t in enumerate(ops.bctype):
