@@ -586,57 +586,9 @@ def gmres_flat(matvec, b, rtol=1e-12, m=40, max_apps=2000, x0=None):
 
 
 # --------------------------------------------------------------- backends --
-class OracleBackend:
-    """The implicit solves on the oracle (CPU; test infrastructure): solve_ad
-    with the outflow balance, and the pressure through the LSOR branch of
-    solve_poisson, whose smoother adds the outflow term nlw0."""
-
-    device = torch.device("cpu")
-
-    def __init__(self, problem, dt, reinv, advec_scheme=2):
-        from oracle.oracle import Oracle
-        pr = copy.deepcopy(problem)
-        pr.params.pp_solver_type = 1
-        self.pr = pr
-        self.o = Oracle(pr)
-        if pr.geom.nGhost:
-            self.o.set_vel_ghosts(pr.geom.coeffD, None)
-        sh = pr.shape
-        self.visc = np.full(sh, reinv, order="F")
-        self.o.set_solve_ad(dt, self.visc, (self.visc,) * 3)
-        self.dt, self.reinv, self.scheme = dt, reinv, advec_scheme
-        self.pPrime = np.zeros(sh, order="F")
-
-    @staticmethod
-    def _np(t):
-        return np.asfortranarray(t.detach().cpu().numpy())
-
-    def solve_ad(self, vel, nl, bc, faces):
-        v = [self._np(t) for t in vel]
-        n = [self._np(t) for t in nl]
-        b = [self._np(t) for t in bc]
-        f = [self._np(t) for t in faces]
-        it, mr = self.o.solve_ad(self.dt, f, v, n, advec_scheme=self.scheme, bc9=b, reinv=self.reinv)
-        T = lambda a: torch.as_tensor(np.ascontiguousarray(a))
-        return [T(a) for a in v], [T(a) for a in b], (it, mr)
-
-    def pressure(self, nlu0):
-        self.pr.nlu0 = self._np(nlu0)
-        sol = self.o.solve(self.pPrime)
-        if sol["status"] not in (0,):
-            raise RuntimeError(f"oracle pressure solve status {sol['status']}")
-        self.pPrime = sol["p"]
-        return torch.as_tensor(np.ascontiguousarray(sol["p"]))
-
-    def mg_apply(self, r):
-        var = np.zeros(self.pr.shape, order="F")
-        self.o.mg_solver(var, self._np(r))
-        return torch.as_tensor(np.ascontiguousarray(var))
-
-    def close(self):
-        self.o.close()
-
-
+# A backend runs the two implicit solves of a step: solve_ad(vel, nl, bc, faces)
+# -> (vel, bc, info), pressure(nlu0) -> p (full array after correct_pressure) and
+# mg_apply(r) -> one forward MG_Solver application; it has .device and .pPrime.
 class DeviceBackend:
     """The implicit solves on the product (C ABI on device arrays): solve_ad and
     the pressure solve with the problem's solver parameters, and one FP64

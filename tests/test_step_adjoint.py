@@ -16,9 +16,9 @@ import pytest
 import torch
 
 from flow_structure_interaction_fem_ibm_gb300 import problem as P
-from flow_structure_interaction_fem_ibm_gb300.step_adjoint import (OracleBackend, StepAdjoint, StepOperators,
-                                                                   VelGhosts, wake_plane_loss)
+from flow_structure_interaction_fem_ibm_gb300.step_adjoint import StepAdjoint, StepOperators, VelGhosts, wake_plane_loss
 from oracle.oracle import Oracle
+from tests.step_adjoint_oracle import OracleBackend
 
 DT, NU = 0.005, 1.0 / 300.0
 INFLOW = np.array([[1.0, 0.0, 0.0]] + [[0.0, 0.0, 0.0]] * 5)
