@@ -625,18 +625,23 @@ class DeviceBackend:
 
     def solve_ad(self, vel, nl, bc, faces):
         self._load(self.vel, vel); self._load(self.nl, nl); self._load(self.bc, bc); self._load(self.faces, faces)
+        # the library's stream does not wait for torch's: the inputs must be complete
+        torch.cuda.synchronize()
         P = lambda ts: [t.data_ptr() for t in ts]
         vis = self.visc.data_ptr()
         st, it, mr = self.s.solve_ad(self.dt, P(self.faces), vis, P(self.vel), P(self.nl), bcvisc=[vis] * 3,
                                      advec_scheme=self.scheme, bc=P(self.bc), reinv=self.reinv)
+        torch.cuda.synchronize()
         if st != 0:
             raise RuntimeError(f"solve_ad status {st} (maxres {mr})")
         return self._view(self.vel), self._view(self.bc), (it, mr)
 
     def pressure(self, nlu0):
         self.nlu0.permute(2, 1, 0).copy_(nlu0.detach())
+        torch.cuda.synchronize()
         st, it, mr, _, _ = self.s.solve_poisson_device(self.pPrime.data_ptr(), self.nlu0.data_ptr(),
                                                         self.nlw0.data_ptr())
+        torch.cuda.synchronize()
         if st not in (0,):
             raise RuntimeError(f"pressure solve status {st} (maxres {mr})")
         return self.pPrime.permute(2, 1, 0).clone()
@@ -986,6 +991,7 @@ class RolloutAdjoint:
 
     def _save(self):
         fs = self.fs
+        torch.cuda.synchronize()   # the product's stream has finished the step
         cl = lambda ts: [t.permute(2, 1, 0).clone() for t in ts]
         return dict(vel=cl(fs.vel), faces=cl(fs.faces), bc=cl(fs.bc), pPrime=fs.pPrime.clone(), time=fs.time,
                     ntime=fs.ntime)
@@ -997,6 +1003,7 @@ class RolloutAdjoint:
                 b.permute(2, 1, 0).copy_(t)
         fs.pPrime.copy_(st["pPrime"])
         fs.time, fs.ntime = st["time"], st["ntime"]
+        torch.cuda.synchronize()   # before the product's stream reads them
 
     def forward(self, u0, v0, w0, steps: int, adjoint_steps: int, checkpoint_every: int, warmup: int = 0):
         """Runs `steps` product steps from (u0, v0, w0); returns the final state.
@@ -1035,6 +1042,7 @@ class RolloutAdjoint:
             rec = self.fs.step()
             if rec["ad_status"] != 0 or rec["poisson_status"] != 0:
                 raise RuntimeError(f"rerun step: {rec}")
+        torch.cuda.synchronize()
         return [t.permute(2, 1, 0) for t in self.fs.vel]
 
     def gradient(self, loss_fn):
@@ -1061,6 +1069,7 @@ class RolloutAdjoint:
             tr = time_now()
             ck = self.checkpoints[c]
             self.backend.pPrime.copy_(ck["pPrime"])
+            torch.cuda.synchronize()
             S, t = (ck["vel"], ck["faces"], ck["bc"]), ck["time"]
             seg = []
             for n in range(c, end):

@@ -87,6 +87,8 @@ class FractionalStep:
         face velocities the first step's advection uses."""
         for t, a in zip(self.vel, (u, v, w)):
             t.copy_(self._dev(a))
+        # the library queues its work on its own stream, which does not wait for torch's
+        torch.cuda.synchronize()
         vp = self._ptrs(self.vel)
         self.s.set_bc(vp, self._ptrs(self.bc), self.values, self.freq, self.time, self.tstart_gust, self.xout,
                       self.yout)
@@ -144,6 +146,7 @@ class FractionalStep:
         return rec
 
     def fields(self) -> dict:
+        self.torch.cuda.synchronize()   # the library's stream has finished
         return dict(u=self.host(self.vel[0]), v=self.host(self.vel[1]), w=self.host(self.vel[2]),
                     faces=[self.host(t) for t in self.faces], p=self.host(self.p),
                     pPrime=self.host(self.pPrime), bc=[self.host(t) for t in self.bc])

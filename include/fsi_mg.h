@@ -10,7 +10,12 @@
  * A full field is REAL(8) (0:nx+1,0:ny+1,0:nz+1); flags are INTEGER(1) over
  * the same range; node arrays are (0:n+1).  Pointers are host pointers unless
  * the entry point says otherwise.  One host thread per handle; a handle owns
- * one CUDA stream and all device memory of its hierarchy.
+ * one CUDA stream and all device memory of its hierarchy.  That stream is
+ * non-blocking: it does not wait for work on other streams, so device inputs
+ * written on another stream (a torch tensor copy, for one) must be complete
+ * before the call (cudaDeviceSynchronize or an event), and a device output
+ * read on another stream needs the same unless the entry point returned a
+ * value it had to read back (statuses, iteration counts, sums).
  *
  * Status codes (all entry points):
  *    0  success / converged
