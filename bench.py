@@ -481,6 +481,7 @@ def projection_steps(solver, pr, peak, reps=20):
     faces = [torch.zeros(sh, dtype=torch.float64, device="cuda") for _ in range(3)]
     nlu0 = torch.zeros(sh, dtype=torch.float64, device="cuda")
     fp = [t.data_ptr() for t in faces]
+    torch.cuda.synchronize()   # the library's stream does not wait for torch's
     out = {}
     for frac, tag in ((0, "no_van_kan"), (1, "van_kan")):
         calls = {
@@ -507,6 +508,7 @@ def projection_steps(solver, pr, peak, reps=20):
     # momentum right-hand side (rhs_advec_diff, Crank-Nicolson, constant viscosity array, no bc arrays)
     visc = torch.full(sh, 1e-3, dtype=torch.float64, device="cuda")
     nl = [torch.zeros(sh, dtype=torch.float64, device="cuda") for _ in range(3)]
+    torch.cuda.synchronize()
     solver.rhs_advec_diff(1e-3, [u.data_ptr(), v.data_ptr(), w.data_ptr()], fp, visc.data_ptr(),
                           [t.data_ptr() for t in nl], advec_scheme=2)
     ms, nb = solver.time_kernel(9, 0, reps)
@@ -559,7 +561,8 @@ def device_time_step(n, seed, tol, krylov, steps=3, reinv=1e-3, dt=1e-3):
     vp = [u.data_ptr(), v.data_ptr(), w.data_ptr()]
     nlp = [t.data_ptr() for t in nl]
     vis = [visc.data_ptr()] * 3
-    # the previous step's face velocities
+    # the previous step's face velocities (the library's stream does not wait for torch's)
+    torch.cuda.synchronize()
     s.face_vel_rhs(dt, u0.data_ptr(), v0.data_ptr(), w0.data_ptr(), *[t.data_ptr() for t in faces0], nlu0.data_ptr())
     dinv = [torch.from_numpy(Metrics(c).dxinv).cuda() for c in (pr.x, pr.y, pr.z)]
     names = ["rhs_advec_diff", "rhs_adjust_bc", "solve_ad", "face_vel_rhs", "solve", "correct_vel",
@@ -880,10 +883,11 @@ def main():
         faces = [torch.zeros(sh, dtype=torch.float64, device="cuda") for _ in range(3)]
         nlu0 = torch.zeros(sh, dtype=torch.float64, device="cuda")
         fp = [t.data_ptr() for t in faces]
-        s.face_vel_rhs(1e-3, u.data_ptr(), v.data_ptr(), w.data_ptr(), *fp, nlu0.data_ptr())
-        s.correct_vel(1e-3, pp.data_ptr(), u.data_ptr(), v.data_ptr(), w.data_ptr(), *fp)
         visc = torch.full(sh, 1e-3, dtype=torch.float64, device="cuda")
         nl = [torch.zeros(sh, dtype=torch.float64, device="cuda") for _ in range(3)]
+        torch.cuda.synchronize()   # the library's stream does not wait for torch's
+        s.face_vel_rhs(1e-3, u.data_ptr(), v.data_ptr(), w.data_ptr(), *fp, nlu0.data_ptr())
+        s.correct_vel(1e-3, pp.data_ptr(), u.data_ptr(), v.data_ptr(), w.data_ptr(), *fp)
         s.rhs_advec_diff(1e-3, [u.data_ptr(), v.data_ptr(), w.data_ptr()], fp, visc.data_ptr(),
                          [t.data_ptr() for t in nl], advec_scheme=2)
         out = {k: s.time_kernel(w_, 0, 1) for k, w_ in (("calc_residual", 5), ("line_x_fp64", 0), ("dfma", 10))}
