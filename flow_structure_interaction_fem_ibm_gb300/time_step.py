@@ -88,7 +88,7 @@ class FractionalStep:
         for t, a in zip(self.vel, (u, v, w)):
             t.copy_(self._dev(a))
         # the library queues its work on its own stream, which does not wait for torch's
-        torch.cuda.synchronize()
+        self.torch.cuda.synchronize()
         vp = self._ptrs(self.vel)
         self.s.set_bc(vp, self._ptrs(self.bc), self.values, self.freq, self.time, self.tstart_gust, self.xout,
                       self.yout)
