@@ -59,6 +59,8 @@ def parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--krylov", type=int, default=30, help="FGMRES restart length around MG_Solver (0: stationary)")
+    ap.add_argument("--mgcycle", choices=("V", "W", "F"), default="F",
+                    help="multigrid cycle of the headline forms (mgCycleX/Y/Z; the stationary forms keep V)")
     ap.add_argument("--no-adjoint", action="store_true")
     ap.add_argument("--no-steps", action="store_true", help="skip the face_vel/correct_vel/update_pressure timing")
     ap.add_argument("--steps-only", action="store_true",
@@ -860,6 +862,8 @@ def main():
         pr = P.sphere(args.n, seed=args.seed, stretch=1.5)
         pp = copy.deepcopy(pr.params)
         pp.precision_mode, pp.outer_krylov, pp.iterMax_Poisson, pp.restol_Poisson = 1, args.krylov, 6, 0.0
+        c = {"V": 1, "W": 2, "F": 3}[args.mgcycle]
+        pp.mgcycle = (c, c, c)
         s = PoissonSolver(pp, pr.x, pr.y, pr.z).set_boundary(pr.geom)
         p = np.zeros(pr.shape, order="F")
         s.solve_poisson(p, pr.nlu0)
@@ -929,9 +933,12 @@ def main():
     pr, shift = build_problem(args.n, args.seed, args.tol, PoissonSolver)
     restol = pr.params.restol_Poisson
 
+    cyc = {"V": 1, "W": 2, "F": 3}[args.mgcycle]
+
     def make(mode, krylov, **kw):
         q = copy.deepcopy(pr.params)
         q.precision_mode, q.outer_krylov = mode, krylov
+        q.mgcycle = (cyc, cyc, cyc)
         for k, v in kw.items():
             setattr(q, k, v)
         return PoissonSolver(q, pr.x, pr.y, pr.z).set_boundary(pr.geom)
@@ -988,15 +995,29 @@ def main():
     fp64_value = replica_throughput(world, k64, fp64_s)
 
     # the reference's own stationary outer iteration (outer_krylov = 0), mixed: one full solve
-    s_stat = make(1, 0, iterMax_Poisson=4000)
+    s_stat = make(1, 0, iterMax_Poisson=4000, mgcycle=(1, 1, 1))
     st_stat, it_stat, dev_stat = step(s_stat, must_converge=False)
     s_stat.close()
     # FP64 stationary: time per outer iteration (the solve needs the same iteration count)
-    s_stat64 = make(0, 0, iterMax_Poisson=12, restol_Poisson=0.0)
+    s_stat64 = make(0, 0, iterMax_Poisson=12, restol_Poisson=0.0, mgcycle=(1, 1, 1))
     step(s_stat64, must_converge=False)
     _, it64, dev64 = step(s_stat64, must_converge=False)
     s_stat64.close()
+    # the headline forms with the other cycles (V is the reference's default)
+    cycles = {}
+    for cname, c in (("V", 1), ("W", 2), ("F", 3)):
+        if c == cyc:
+            continue
+        for fname, mode in (("mixed", 1), ("fp64", 0)):
+            if cname == "W" and fname == "fp64":
+                continue
+            sv = make(mode, args.krylov, mgcycle=(c, c, c))
+            tc, _, itc, _ = timed(sv, 2, 1)
+            cycles[f"{cname}_{fname}"] = {"ms_per_solve": 1e3 * tc / 2, "iters": itc[0],
+                                           "solves_per_s": replica_throughput(world, 2, tc)}
+            sv.close()
     stationary = {
+        "cycle": "V (the reference's default mgCycle)",
         "mixed": {"status": st_stat, "iters": it_stat, "seconds": dev_stat,
                   "solves_per_s": (1.0 / dev_stat) if st_stat == 0 else None},
         "fp64": {"ms_per_iteration": 1e3 * dev64 / it64,
@@ -1181,6 +1202,7 @@ def main():
         "scaling": "weak", "vs_baseline": None, "dtype": "f32 cycle + f64 refinement", "data": "synthetic",
         "config": {"workload": f"sphere_{args.n}^3_tanh1.5_r0.15_tol{args.tol:g}_mixed_fgmres{args.krylov}",
                    "grid": args.n, "tol": args.tol, "restol": restol, "stretch": 1.5, "radius": 0.15,
+                   "mg_cycle": args.mgcycle,
                    "triangles": 5120, "nGhost": int(pr.geom.nGhost), "compat_shift": shift,
                    "outer": f"FGMRES({args.krylov}) preconditioned by MG_Solver" if args.krylov else "stationary",
                    "l2": "inputs larger than L2 (two 139 MB FP64 fields + hierarchy)",
@@ -1190,7 +1212,7 @@ def main():
         "error": {"mixed_vs_fp64_rel_l2": err, "mixed_vs_fp64_tight_rel_l2": err_tight,
                   "fp64_vs_fp64_tight_rel_l2": err64_tight, "tight_restol": restol * 1e-2,
                   "tight_status": st_t, "tight_iters": it_t},
-        "iters_mixed": mixed_iters[0], "iters_fp64": fp64_iters[0], "stationary": stationary,
+        "iters_mixed": mixed_iters[0], "iters_fp64": fp64_iters[0], "stationary": stationary, "cycles": cycles,
         "wall_ms_per_step": 1e3 * mixed_wall / args.steps,
         "gpu_launches": int(mixed_launch), "clocks": clocks, "e2e": e2e, "roofline": roofline,
         "cpu_baseline": cpu, "config2": config2, "reference_model_256": model256, "tol_1e10": tol10,
