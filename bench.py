@@ -617,7 +617,7 @@ def device_time_step(n, seed, tol, krylov, steps=3, reinv=1e-3, dt=1e-3):
 
 
 def channel_rollout(steps, cells=(192, 128, 128), krylov=30, warmup=2, restol=1e-6, dt=0.005, re=300.0,
-                    adjoint_steps=50, checkpoint_every=10, x_plane=3.0):
+                    adjoint_steps=50, checkpoint_every=10, x_plane=3.0, mgcycle=3):
     """The sphere-wake rollout: a 192 x 128 x 128 uniform channel on [0,6] x
     [0,4]^2, sphere of diameter 1 at (1.5, 2, 2) (GCM ghost cells), uniform
     inflow U = 1, zero-gradient outflow with the outflow mass balance,
@@ -646,6 +646,7 @@ def channel_rollout(steps, cells=(192, 128, 128), krylov=30, warmup=2, restol=1e
     q.precision_mode, q.outer_krylov = 1, krylov
     q.restol_Poisson, q.iterMax_Poisson = restol, 2000
     q.restol_ad, q.iterMax_ad = 1e-10, 200
+    q.mgcycle = (mgcycle,) * 3
     inflow = np.array([[1.0, 0.0, 0.0]] + [[0.0, 0.0, 0.0]] * 5)
     fluid = 1.0 - pr.geom.iblank
     u0 = np.asfortranarray(fluid.astype(np.float64))
@@ -702,7 +703,7 @@ def channel_rollout(steps, cells=(192, 128, 128), krylov=30, warmup=2, restol=1e
     free1, _ = torch.cuda.mem_get_info()
     out = {"profile": "channel_rollout",
            "workload": f"channel_{n[0]}x{n[1]}x{n[2]}_[0,6]x[0,4]^2_sphere_d1_at_(1.5,2,2)_Re{re:g}_dt{dt:g}_CN_"
-                       f"mixed_{'fgmres' + str(krylov) if krylov else 'stationary'}",
+                       f"mixed_{'fgmres' + str(krylov) if krylov else 'stationary'}_{'VWF'[mgcycle - 1]}cycle",
            "steps": steps, "warmup": warmup, "ms_per_step": 1e3 * wall / steps, "steps_per_s": steps / wall,
            "stage_ms": stage["ms"], "poisson_iters": [r["poisson_iters"] for r in recs],
            "ad_iters": [r["ad_iters"] for r in recs],
@@ -873,7 +874,8 @@ def main():
 
     if args.rollout > 0:
         print(json.dumps(channel_rollout(args.rollout, args.rollout_cells, args.krylov,
-                                         adjoint_steps=args.rollout_adjoint)))
+                                         adjoint_steps=args.rollout_adjoint,
+                                         mgcycle={"V": 1, "W": 2, "F": 3}[args.mgcycle])))
         return
 
     if args.profile_fp64:
@@ -1132,7 +1134,8 @@ def main():
 
     rollout = None
     if rank == 0 and not args.no_rollout:
-        rollout = channel_rollout(200, krylov=args.krylov)   # config 5: 200 steps
+        rollout = channel_rollout(200, krylov=args.krylov,   # config 5: 200 steps
+                                  mgcycle={"V": 1, "W": 2, "F": 3}[args.mgcycle])
 
     # roofline of the dominant kernel: level-1 FP32 line relaxation (k_line_wp<float,dir,8>),
     # durations from CUDA events around each launch inside the timed solves
