@@ -78,6 +78,7 @@ class StepOperators:
                 raise ValueError(f"velocity side {s}: type {t} is not restated (Dirichlet, zero gradient, symmetry)")
         self.pr = problem
         self.dev = torch.device(device)
+        self.scheme = int(advec_scheme)
         self.dt, self.reinv = float(dt), float(reinv)
         self.values = np.asarray(bc_values, dtype=np.float64).reshape(6, 3)
         self.n = (p.nx - 1, p.ny - 1, p.nz - 1)
@@ -324,7 +325,9 @@ class StepOperators:
             rhs = [self.cells(nl[q], 0) + t0[q] - t1[q] for q in range(3)]
             rs = self.massflux(faces) / self.area
         else:
-            faces = faces_in
+            # CRANK_NICOLSON2 re-evaluates face_vel of the current velocities every iteration
+            # (IBM/CORE_SOLVE_AD.F90:155-157); CRANK_NICOLSON1 keeps the step's faces
+            faces = self.face_vel(vel, (bc9[0], bc9[4], bc9[8])) if self.scheme == 3 else faces_in
             rhs = [self.cells(nl[q], 0) for q in range(3)]
             rs = None
         rows = self.ad_rows(faces)
@@ -851,7 +854,9 @@ class StepAdjoint:
             for side in (0, 1):
                 if ops.bctype[2 * a + side] == BC_ZERO_GRADIENT:
                     acc = acc - ops.col(ops.dxinv[a], a) * ops.cells(ops.fl[2 * a + side], a)
-        if ops.zg:
+        # the compatibility fixed point of GCM_correct_pressure (zero-gradient sides with GCM)
+        self.rank1 = ops.zg and ops.gcm
+        if self.rank1:
             n1[ops.I] = acc * ops.fluid
         self.n1 = as_fortran(n1)
         self.area = ops.area
@@ -860,12 +865,12 @@ class StepAdjoint:
     # pressure operator B = A_eff + n1 (vol^T A_eff) / area and its transpose
     def apply_B(self, pf):
         Ap = self.pops.apply_eff(pf)
-        if not self.ops.zg:
+        if not self.rank1:
             return Ap
         return Ap + self.n1 * (float((self.pops.vol * Ap).sum()) / self.area)
 
     def apply_BT(self, z):
-        if not self.ops.zg:
+        if not self.rank1:
             return self.pops.apply_eff_T(z)
         return self.pops.apply_eff_T(z + self.pops.vol * (float((self.n1 * z).sum()) / self.area))
 

@@ -283,3 +283,63 @@ def test_replayed_solves_give_the_same_cotangent():
                 assert float((x - y).abs().max()) <= 1e-12 * max(1.0, float(y.abs().max()))
     finally:
         be.close()
+
+
+def _box_channel():
+    """Channel box without a body (Dirichlet inflow, zero-gradient outflow,
+    symmetry sides): solve_ad has no outflow balance, and CRANK_NICOLSON2
+    re-evaluates the faces inside its iteration."""
+    p = P.default_params(3, 12, 8, 8, body=False)
+    p.bc = (1, 2, 4, 4, 4, 4)
+    p.restol_ad, p.iterMax_ad = 1e-14, 1000
+    p.restol_Poisson, p.iterMax_Poisson = 1e-12, 20000
+    x, y, z = P.make_grid(p.nx, p.ny, p.nz, "tanh", beta=1.5)
+    geom = P.empty_geometry(p)
+    p.outflow_area = P.outflow_area(p, x, y, z, geom.iblank)
+    return P.Problem(p, x, y, z, geom, np.zeros(P.full_shape(p), order="F"), name="box_channel")
+
+
+@pytest.mark.parametrize("scheme", [2, 3], ids=["cn", "cn2"])
+def test_two_step_adjoint_without_a_body(scheme):
+    pr = _box_channel()
+    be = OracleBackend(pr, DT, NU, advec_scheme=scheme)
+    sa = StepAdjoint(pr, DT, NU, INFLOW, be, advec_scheme=scheme)
+    assert not sa.ops.mass_consv and not sa.rank1
+    sh = pr.shape
+    try:
+        u, v, w = _velocity(pr)
+        vel, bc = sa.ops.set_bc([T(u), T(v), T(w)], [torch.zeros(sh, dtype=torch.float64) for _ in range(9)], 0.0)
+        S0 = (vel, sa.ops.face_vel(vel, (bc[0], bc[4], bc[8])), bc)
+
+        def run(S):
+            be.pPrime[...] = 0.0
+            with torch.no_grad():
+                for n in range(2):
+                    S = sa.step(*S, time=n * DT)
+            return S
+
+        be.pPrime[...] = 0.0
+        with torch.no_grad():
+            S1 = sa.step(*S0)
+            S2 = sa.step(*S1, time=DT)
+        uf = S2[0][0].clone().requires_grad_(True)
+        with torch.enable_grad():
+            gu = torch.autograd.grad(wake_plane_loss(pr, uf, 0.6)[0], uf)[0]
+        z = lambda: torch.zeros(sh, dtype=torch.float64)
+        cot = ([gu, z(), z()], [z(), z(), z()], [z() for _ in range(9)])
+        for S, t in ((S1, DT), (S0, 0.0)):
+            be.pPrime[...] = 0.0
+            cot = sa.step_vjp(S, cot, time=t)
+        rng = np.random.default_rng(13)
+        inner = torch.zeros(sh, dtype=torch.float64)
+        inner[sa.ops.I] = 1.0
+        d = [T(rng.standard_normal(sh)) * inner for _ in range(3)]
+        adj = sum(float((a * b).sum()) for a, b in zip(cot[0], d))
+        h = 1e-5
+        Lp = float(wake_plane_loss(pr, run(([a + h * b for a, b in zip(S0[0], d)], S0[1], S0[2]))[0][0], 0.6)[0])
+        Lm = float(wake_plane_loss(pr, run(([a - h * b for a, b in zip(S0[0], d)], S0[1], S0[2]))[0][0], 0.6)[0])
+        fd = (Lp - Lm) / (2 * h)
+        assert abs(fd) > 1e-6
+        assert abs(fd - adj) <= 1e-7 * abs(fd) + 1e-11, (fd, adj)
+    finally:
+        be.close()
