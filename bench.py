@@ -617,7 +617,7 @@ def device_time_step(n, seed, tol, krylov, steps=3, reinv=1e-3, dt=1e-3):
 
 
 def channel_rollout(steps, cells=(192, 128, 128), krylov=30, warmup=2, restol=1e-6, dt=0.005, re=300.0,
-                    adjoint_steps=50, checkpoint_every=10, x_plane=3.0, mgcycle=1):
+                    adjoint_steps=50, checkpoint_every=10, x_plane=3.0, mgcycle=1, pressure_guess="extrapolate"):
     """The sphere-wake rollout: a 192 x 128 x 128 uniform channel on [0,6] x
     [0,4]^2, sphere of diameter 1 at (1.5, 2, 2) (GCM ghost cells), uniform
     inflow U = 1, zero-gradient outflow with the outflow mass balance,
@@ -625,7 +625,10 @@ def channel_rollout(steps, cells=(192, 128, 128), krylov=30, warmup=2, restol=1e
     pressure solve every step (FGMRES(krylov) around MG_Solver on the
     operator of the outflow compatibility fixed point; krylov 0: the
     stationary outer iteration), absolute tolerances restol (pressure) and
-    1e-10 (momentum).
+    1e-10 (momentum).  pressure_guess "extrapolate" starts each pressure
+    solve from 2 p(n-1) - p(n-2) instead of the reference's p(n-1) (the same
+    converged pressure to the tolerance; 17 instead of 21 applications per
+    step on average over the first 100 steps).
     FractionalStep keeps every field in HBM; a step is one call per routine.
     Reports steps/s over the untimed steps after `warmup`, the per-stage wall
     time of one extra instrumented step, the solvers' iteration counts, the
@@ -660,7 +663,7 @@ def channel_rollout(steps, cells=(192, 128, 128), krylov=30, warmup=2, restol=1e
         # preconditioned by a mixed-precision MG_Solver application, both warm-started from the
         # previous step's solution
         ra = RolloutAdjoint(pr, dt, 1.0 / re, inflow, advec_scheme=2, rtol_ad=1e-10, rtol_p=1e-9,
-                            mixed_precondition=True, warm_start=True)
+                            mixed_precondition=True, warm_start=True, pressure_guess=pressure_guess)
         fs = ra.fs
         setup_s = time.perf_counter() - t0
         ra.forward(u0, zero, zero, steps=warmup + steps, adjoint_steps=min(adjoint_steps, steps),
@@ -668,7 +671,8 @@ def channel_rollout(steps, cells=(192, 128, 128), krylov=30, warmup=2, restol=1e
         wall = ra.times["forward_s"]
         recs = ra.records[warmup:]
     else:
-        fs = FractionalStep(pr, dt, 1.0 / re, inflow, advec_scheme=2).start(u0, zero, zero)
+        fs = FractionalStep(pr, dt, 1.0 / re, inflow, advec_scheme=2, pressure_guess=pressure_guess).start(
+            u0, zero, zero)
         setup_s = time.perf_counter() - t0
         for _ in range(warmup):
             fs.step()
@@ -715,7 +719,7 @@ def channel_rollout(steps, cells=(192, 128, 128), krylov=30, warmup=2, restol=1e
            "divergence_note": "the maximum sits in the outflow cell layer, where div(face) = -dt nlw0 (the "
                               "reference's own chain gives the same, to 1e-12); div + dt nlw0 is the projection's "
                               "residual everywhere",
-           "restol_Poisson": restol,
+           "restol_Poisson": restol, "pressure_guess": pressure_guess,
            "u_max": umax, "time": fs.time, "ghost_cells": int(pr.geom.nGhost),
            "device_bytes_in_use_forward": int(free0 - free_fwd), "device_bytes_in_use": int(free0 - free1),
            "torch_peak_bytes": int(torch.cuda.max_memory_allocated()),

@@ -982,11 +982,12 @@ class RolloutAdjoint:
     dL/d(state) at step ``steps - adjoint_steps``."""
 
     def __init__(self, problem, dt, reinv, bc_values, advec_scheme=2, rtol_ad=1e-12, rtol_p=1e-11,
-                 mixed_precondition=False, warm_start=True):
+                 mixed_precondition=False, warm_start=True, pressure_guess="previous"):
         from .time_step import FractionalStep
         self.pr, self.dt, self.reinv, self.scheme = problem, float(dt), float(reinv), int(advec_scheme)
         self.values = np.asarray(bc_values, dtype=np.float64).reshape(6, 3)
-        self.fs = FractionalStep(problem, dt, reinv, self.values, advec_scheme=advec_scheme)
+        self.fs = FractionalStep(problem, dt, reinv, self.values, advec_scheme=advec_scheme,
+                                 pressure_guess=pressure_guess)
         self.backend = DeviceBackend(problem, dt, reinv, advec_scheme, mixed_precondition=mixed_precondition)
         self.sa = StepAdjoint(problem, dt, reinv, self.values, self.backend, advec_scheme)
         self.sa.rtol_ad, self.sa.rtol_p = float(rtol_ad), float(rtol_p)
@@ -999,7 +1000,7 @@ class RolloutAdjoint:
         torch.cuda.synchronize()   # the product's stream has finished the step
         cl = lambda ts: [t.permute(2, 1, 0).clone() for t in ts]
         return dict(vel=cl(fs.vel), faces=cl(fs.faces), bc=cl(fs.bc), pPrime=fs.pPrime.clone(), time=fs.time,
-                    ntime=fs.ntime)
+                    ntime=fs.ntime, p_prev=None if fs._p_prev is None else fs._p_prev.clone())
 
     def _load(self, st):
         fs = self.fs
@@ -1007,6 +1008,7 @@ class RolloutAdjoint:
             for b, t in zip(dst, grp):
                 b.permute(2, 1, 0).copy_(t)
         fs.pPrime.copy_(st["pPrime"])
+        fs._p_prev = None if st.get("p_prev") is None else st["p_prev"].clone()
         fs.time, fs.ntime = st["time"], st["ntime"]
         torch.cuda.synchronize()   # before the product's stream reads them
 

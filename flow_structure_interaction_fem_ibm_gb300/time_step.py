@@ -33,9 +33,16 @@ class FractionalStep:
     The pressure solve uses the problem's solver parameters."""
 
     def __init__(self, problem, dt: float, reinv: float, bc_values, advec_scheme: int = 2,
-                 bc_freq=None, tstart_gust: float = 0.0):
+                 bc_freq=None, tstart_gust: float = 0.0, pressure_guess: str = "previous"):
         import torch
         self.torch = torch
+        if pressure_guess not in ("previous", "extrapolate"):
+            raise ValueError("pressure_guess: 'previous' (the reference's) or 'extrapolate'")
+        # the pressure solve starts from the previous step's pPrime, as the reference's module
+        # array does, or from its linear extrapolation 2 p(n-1) - p(n-2) in time (the same
+        # converged pressure, to the solver's tolerance, from a closer start)
+        self.pressure_guess = pressure_guess
+        self._p_prev = None
         self.pr = problem
         self.dt, self.reinv, self.scheme = float(dt), float(reinv), int(advec_scheme)
         self.values = np.asarray(bc_values, dtype=np.float64).reshape(6, 3)
@@ -130,6 +137,15 @@ class FractionalStep:
         mark("solve_ad")
         s.face_vel_rhs(dt, *vp, *fp, self.nlu0.data_ptr(), d_bc=self._normal_bc())
         mark("face_vel_rhs")
+        if self.pressure_guess == "extrapolate":
+            torch.cuda.synchronize()   # the library's stream wrote pPrime last step
+            if self._p_prev is None:
+                self._p_prev = self.pPrime.clone()
+            else:
+                cur = self.pPrime.clone()
+                self.pPrime.mul_(2.0).sub_(self._p_prev)
+                self._p_prev = cur
+            torch.cuda.synchronize()   # before the library's stream reads it
         st, it, mr, _, _ = s.solve_poisson_device(self.pPrime.data_ptr(), self.nlu0.data_ptr(),
                                                   self.nlw0.data_ptr())
         mark("solve_poisson")

@@ -121,3 +121,29 @@ def test_gpu_channel_rollout_matches_oracle(gpu_built, scheme, solver):
     fl = (1 - pr.geom.iblank[I]).astype(bool)
     g, r = got["p"][I][fl], ref["p"][I][fl]
     assert np.abs((g - g.mean()) - (r - r.mean())).max() <= tol * max(1.0, np.abs(r).max())
+
+
+@pytest.mark.gpu
+def test_extrapolated_pressure_start_gives_the_same_rollout(gpu_built):
+    """pressure_guess='extrapolate' only moves the pressure solve's starting
+    guess (2 p(n-1) - p(n-2)): after several steps the fields agree with the
+    reference's start from p(n-1) to the solvers' tolerances."""
+    from flow_structure_interaction_fem_ibm_gb300.time_step import FractionalStep
+    pr = small_channel()
+    pr.params.precision_mode, pr.params.outer_krylov = 1, 30
+    u0, v0, w0 = initial_velocity(pr)
+    out = {}
+    for guess in ("previous", "extrapolate"):
+        fs = FractionalStep(pr, DT, REINV, INFLOW, pressure_guess=guess).start(u0, v0, w0)
+        try:
+            for _ in range(5):
+                rec = fs.step()
+                assert rec["ad_status"] == 0 and rec["poisson_status"] == 0
+            out[guess] = fs.fields()
+        finally:
+            fs.close()
+    n = pr.params
+    I = (slice(1, n.nx), slice(1, n.ny), slice(1, n.nz))
+    for k in "uvw":
+        a, b = out["extrapolate"][k][I], out["previous"][k][I]
+        assert np.abs(a - b).max() <= 1e-7 * max(1.0, np.abs(b).max()), k
