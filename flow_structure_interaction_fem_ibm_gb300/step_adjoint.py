@@ -599,9 +599,11 @@ class DeviceBackend:
 
     device = torch.device("cuda")
 
-    def __init__(self, problem, dt, reinv, advec_scheme=2, mixed_precondition=False):
+    def __init__(self, problem, dt, reinv, advec_scheme=2, mixed_precondition=False, pressure_guess="previous"):
         from .poisson import PoissonSolver
         self.pr = problem
+        self.pressure_guess = pressure_guess   # as FractionalStep: 'previous' or 'extrapolate'
+        self.p_prev = None
         p = problem.params
         self.s = PoissonSolver(p, problem.x, problem.y, problem.z).set_boundary(problem.geom)
         if problem.geom.nGhost:
@@ -641,6 +643,13 @@ class DeviceBackend:
 
     def pressure(self, nlu0):
         self.nlu0.permute(2, 1, 0).copy_(nlu0.detach())
+        if self.pressure_guess == "extrapolate":
+            if self.p_prev is None:
+                self.p_prev = self.pPrime.clone()
+            else:
+                cur = self.pPrime.clone()
+                self.pPrime.mul_(2.0).sub_(self.p_prev)
+                self.p_prev = cur
         torch.cuda.synchronize()
         st, it, mr, _, _ = self.s.solve_poisson_device(self.pPrime.data_ptr(), self.nlu0.data_ptr(),
                                                         self.nlw0.data_ptr())
@@ -988,7 +997,8 @@ class RolloutAdjoint:
         self.values = np.asarray(bc_values, dtype=np.float64).reshape(6, 3)
         self.fs = FractionalStep(problem, dt, reinv, self.values, advec_scheme=advec_scheme,
                                  pressure_guess=pressure_guess)
-        self.backend = DeviceBackend(problem, dt, reinv, advec_scheme, mixed_precondition=mixed_precondition)
+        self.backend = DeviceBackend(problem, dt, reinv, advec_scheme, mixed_precondition=mixed_precondition,
+                                     pressure_guess=pressure_guess)
         self.sa = StepAdjoint(problem, dt, reinv, self.values, self.backend, advec_scheme)
         self.sa.rtol_ad, self.sa.rtol_p = float(rtol_ad), float(rtol_p)
         self.sa.warm_start = bool(warm_start)
@@ -1076,6 +1086,7 @@ class RolloutAdjoint:
             tr = time_now()
             ck = self.checkpoints[c]
             self.backend.pPrime.copy_(ck["pPrime"])
+            self.backend.p_prev = None if ck.get("p_prev") is None else ck["p_prev"].clone()
             torch.cuda.synchronize()
             S, t = (ck["vel"], ck["faces"], ck["bc"]), ck["time"]
             seg = []
