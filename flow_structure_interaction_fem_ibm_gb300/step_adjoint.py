@@ -721,10 +721,9 @@ class _SolveAD(torch.autograd.Function):
             rs = outs[3] if len(outs) > 3 else None
 
             rhs = torch.cat([t.reshape(-1) for t in Xbar] + ([sbar.reshape(1)] if rs is not None else []))
-            x0 = sa._lam_prev if (sa.warm_start and sa._lam_prev is not None
-                                  and sa._lam_prev.shape == rhs.shape) else None
+            x0 = sa._guess(sa._lam_hist, rhs.shape) if sa.warm_start else None
             lam, apps, rel = gmres_flat(JT, rhs, rtol=sa.rtol_ad, x0=x0)
-            sa._lam_prev = lam
+            sa._lam_hist = [lam] + sa._lam_hist[:1]
             sa.stats["ad_transposed_applications"] = sa.stats.get("ad_transposed_applications", 0) + apps
             sa.stats["ad_transposed_rel_residual"] = max(sa.stats.get("ad_transposed_rel_residual", 0.0), rel)
             gth = torch.autograd.grad(outs, th, grad_outputs=split(lam), allow_unused=True)
@@ -819,8 +818,8 @@ class _Pressure(torch.autograd.Function):
         sa = ctx.sa
         t0 = _sync_time(sa.ops.dev)
         s = sa.pops.extend_T(as_fortran(gp))
-        z = sa.solve_BT(s, z0=sa._z_prev if sa.warm_start else None)
-        sa._z_prev = z
+        z = sa.solve_BT(s, z0=sa._guess(sa._z_hist, s.shape) if sa.warm_start else None)
+        sa._z_hist = [z] + sa._z_hist[:1]
         one = sa.pops.fluid
         w = sa.left_null()
         zhat = (z - w * (float((one * z).sum()) / float((one * w).sum()))) * one
@@ -847,7 +846,7 @@ class StepAdjoint:
         self.record, self.replay = None, None
         # warm starts of the transposed solves from the previous step's solutions
         self.warm_start = False
-        self._lam_prev, self._z_prev = None, None
+        self._lam_hist, self._z_hist = [], []   # the last two solutions, latest first
         # the GMRES matrix-vector product of the transposed solve_ad system as one CUDA graph
         self.graph_vjp = True
         ops = self.ops
@@ -870,6 +869,15 @@ class StepAdjoint:
         self.n1 = as_fortran(n1)
         self.area = ops.area
         self._w = None
+
+    @staticmethod
+    def _guess(hist, shape):
+        """Start of a transposed solve: the linear extrapolation of the two
+        previous steps' solutions (the previous one alone after one step)."""
+        h = [t for t in hist if t.shape == shape]
+        if not h:
+            return None
+        return 2.0 * h[0] - h[1] if len(h) > 1 else h[0]
 
     # pressure operator B = A_eff + n1 (vol^T A_eff) / area and its transpose
     def apply_B(self, pf):
