@@ -847,6 +847,7 @@ class StepAdjoint:
         # warm starts of the transposed solves from the previous step's solutions
         self.warm_start = False
         self._lam_hist, self._z_hist = [], []   # the last two solutions, latest first
+        self._bt = None
         # the GMRES matrix-vector product of the transposed solve_ad system as one CUDA graph
         self.graph_vjp = True
         ops = self.ops
@@ -886,10 +887,40 @@ class StepAdjoint:
             return Ap
         return Ap + self.n1 * (float((self.pops.vol * Ap).sum()) / self.area)
 
-    def apply_BT(self, z):
+    def _apply_BT_eager(self, z):
         if not self.rank1:
             return self.pops.apply_eff_T(z)
-        return self.pops.apply_eff_T(z + self.pops.vol * (float((self.n1 * z).sum()) / self.area))
+        return self.pops.apply_eff_T(z + self.pops.vol * ((self.n1 * z).sum() / self.area))
+
+    def apply_BT(self, z):
+        """B^T z.  On the GPU one CUDA graph replay: the ghost-row sweeps of the
+        extension's transpose alone are a few hundred small kernels, which
+        launched one by one from Python would bound the transposed solve."""
+        if self.ops.dev.type != "cuda" or not self.graph_vjp:
+            return self._apply_BT_eager(z)
+        if self._bt is None:
+            zin = fortran_zeros(self.ops.shape, self.ops.dev)
+            side = torch.cuda.Stream()
+            side.wait_stream(torch.cuda.current_stream())
+            try:
+                with torch.cuda.stream(side):
+                    for _ in range(2):
+                        self._apply_BT_eager(zin)
+                    g = torch.cuda.CUDAGraph()
+                    with torch.cuda.graph(g, stream=side):
+                        zout = self._apply_BT_eager(zin)
+                torch.cuda.current_stream().wait_stream(side)
+                self._bt = (g, zin, zout)
+            except RuntimeError as e:   # capture refused: eager from now on
+                torch.cuda.current_stream().wait_stream(side)
+                self.stats["apply_BT_graph_error"] = str(e)[:200]
+                self._bt = False
+        if self._bt is False:
+            return self._apply_BT_eager(z)
+        g, zin, zout = self._bt
+        zin.copy_(z)
+        g.replay()
+        return zout.clone()
 
     def _precond(self, v):
         vol = self.pops.vol
