@@ -59,8 +59,11 @@ def parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--krylov", type=int, default=30, help="FGMRES restart length around MG_Solver (0: stationary)")
-    ap.add_argument("--mgcycle", choices=("V", "W", "F"), default="F",
-                    help="multigrid cycle of the headline forms (mgCycleX/Y/Z; the stationary forms keep V)")
+    ap.add_argument("--mgcycle", choices=("V", "W", "F"), default="V",
+                    help="multigrid cycle of the headline forms (mgCycleX/Y/Z)")
+    ap.add_argument("--iter-finest", type=int, default=1,
+                    help="line sweeps per colour and direction on the finest levels of the headline forms "
+                         "(iterFinest; the reference's input uses 2, the stationary forms keep it)")
     ap.add_argument("--no-adjoint", action="store_true")
     ap.add_argument("--no-steps", action="store_true", help="skip the face_vel/correct_vel/update_pressure timing")
     ap.add_argument("--steps-only", action="store_true",
@@ -617,7 +620,8 @@ def device_time_step(n, seed, tol, krylov, steps=3, reinv=1e-3, dt=1e-3):
 
 
 def channel_rollout(steps, cells=(192, 128, 128), krylov=30, warmup=2, restol=1e-6, dt=0.005, re=300.0,
-                    adjoint_steps=50, checkpoint_every=10, x_plane=3.0, mgcycle=1, pressure_guess="extrapolate"):
+                    adjoint_steps=50, checkpoint_every=10, x_plane=3.0, mgcycle=1, pressure_guess="extrapolate",
+                    iter_finest=1):
     """The sphere-wake rollout: a 192 x 128 x 128 uniform channel on [0,6] x
     [0,4]^2, sphere of diameter 1 at (1.5, 2, 2) (GCM ghost cells), uniform
     inflow U = 1, zero-gradient outflow with the outflow mass balance,
@@ -650,6 +654,7 @@ def channel_rollout(steps, cells=(192, 128, 128), krylov=30, warmup=2, restol=1e
     q.restol_Poisson, q.iterMax_Poisson = restol, 2000
     q.restol_ad, q.iterMax_ad = 1e-10, 200
     q.mgcycle = (mgcycle,) * 3
+    q.iterFinest = iter_finest
     inflow = np.array([[1.0, 0.0, 0.0]] + [[0.0, 0.0, 0.0]] * 5)
     fluid = 1.0 - pr.geom.iblank
     u0 = np.asfortranarray(fluid.astype(np.float64))
@@ -719,7 +724,8 @@ def channel_rollout(steps, cells=(192, 128, 128), krylov=30, warmup=2, restol=1e
            "divergence_note": "the maximum sits in the outflow cell layer, where div(face) = -dt nlw0 (the "
                               "reference's own chain gives the same, to 1e-12); div + dt nlw0 is the projection's "
                               "residual everywhere",
-           "restol_Poisson": restol, "pressure_guess": pressure_guess,
+           "restol_Poisson": restol, "pressure_guess": pressure_guess, "iterFinest": iter_finest,
+           "mg_cycle": "VWF"[mgcycle - 1],
            "u_max": umax, "time": fs.time, "ghost_cells": int(pr.geom.nGhost),
            "device_bytes_in_use_forward": int(free0 - free_fwd), "device_bytes_in_use": int(free0 - free1),
            "torch_peak_bytes": int(torch.cuda.max_memory_allocated()),
@@ -869,6 +875,7 @@ def main():
         pp.precision_mode, pp.outer_krylov, pp.iterMax_Poisson, pp.restol_Poisson = 1, args.krylov, 6, 0.0
         c = {"V": 1, "W": 2, "F": 3}[args.mgcycle]
         pp.mgcycle = (c, c, c)
+        pp.iterFinest = args.iter_finest
         s = PoissonSolver(pp, pr.x, pr.y, pr.z).set_boundary(pr.geom)
         p = np.zeros(pr.shape, order="F")
         s.solve_poisson(p, pr.nlu0)
@@ -878,7 +885,7 @@ def main():
 
     if args.rollout > 0:
         print(json.dumps(channel_rollout(args.rollout, args.rollout_cells, args.krylov,
-                                         adjoint_steps=args.rollout_adjoint)))
+                                         adjoint_steps=args.rollout_adjoint, iter_finest=args.iter_finest)))
         return
 
     if args.profile_fp64:
@@ -944,6 +951,7 @@ def main():
         q = copy.deepcopy(pr.params)
         q.precision_mode, q.outer_krylov = mode, krylov
         q.mgcycle = (cyc, cyc, cyc)
+        q.iterFinest = args.iter_finest
         for k, v in kw.items():
             setattr(q, k, v)
         return PoissonSolver(q, pr.x, pr.y, pr.z).set_boundary(pr.geom)
@@ -1000,29 +1008,30 @@ def main():
     fp64_value = replica_throughput(world, k64, fp64_s)
 
     # the reference's own stationary outer iteration (outer_krylov = 0), mixed: one full solve
-    s_stat = make(1, 0, iterMax_Poisson=4000, mgcycle=(1, 1, 1))
+    s_stat = make(1, 0, iterMax_Poisson=4000, mgcycle=(1, 1, 1), iterFinest=pr.params.iterFinest)
     st_stat, it_stat, dev_stat = step(s_stat, must_converge=False)
     s_stat.close()
     # FP64 stationary: time per outer iteration (the solve needs the same iteration count)
-    s_stat64 = make(0, 0, iterMax_Poisson=12, restol_Poisson=0.0, mgcycle=(1, 1, 1))
+    s_stat64 = make(0, 0, iterMax_Poisson=12, restol_Poisson=0.0, mgcycle=(1, 1, 1),
+                    iterFinest=pr.params.iterFinest)
     step(s_stat64, must_converge=False)
     _, it64, dev64 = step(s_stat64, must_converge=False)
     s_stat64.close()
-    # the headline forms with the other cycles (V is the reference's default)
-    cycles = {}
-    for cname, c in (("V", 1), ("W", 2), ("F", 3)):
-        if c == cyc:
+    # the headline forms with other cycles and smoothing counts (V-cycles with iterFinest 2
+    # are the reference input's settings)
+    cycles = {"headline": {"cycle": args.mgcycle, "iterFinest": args.iter_finest}}
+    for cname, fin, fname, mode in (("V", 2, "mixed", 1), ("F", 2, "mixed", 1), ("F", 1, "mixed", 1),
+                                    ("W", 2, "mixed", 1), ("V", 2, "fp64", 0), ("F", 2, "fp64", 0)):
+        c = {"V": 1, "W": 2, "F": 3}[cname]
+        if c == cyc and fin == args.iter_finest:
             continue
-        for fname, mode in (("mixed", 1), ("fp64", 0)):
-            if cname == "W" and fname == "fp64":
-                continue
-            sv = make(mode, args.krylov, mgcycle=(c, c, c))
-            tc, _, itc, _ = timed(sv, 2, 1)
-            cycles[f"{cname}_{fname}"] = {"ms_per_solve": 1e3 * tc / 2, "iters": itc[0],
-                                           "solves_per_s": replica_throughput(world, 2, tc)}
-            sv.close()
+        sv = make(mode, args.krylov, mgcycle=(c, c, c), iterFinest=fin)
+        tc, _, itc, _ = timed(sv, 2, 1)
+        cycles[f"{cname}_finest{fin}_{fname}"] = {"ms_per_solve": 1e3 * tc / 2, "iters": itc[0],
+                                                  "solves_per_s": replica_throughput(world, 2, tc)}
+        sv.close()
     stationary = {
-        "cycle": "V (the reference's default mgCycle)",
+        "cycle": "V, iterFinest as the reference input (the reference's own iteration)",
         "mixed": {"status": st_stat, "iters": it_stat, "seconds": dev_stat,
                   "solves_per_s": (1.0 / dev_stat) if st_stat == 0 else None},
         "fp64": {"ms_per_iteration": 1e3 * dev64 / it64,
@@ -1140,7 +1149,7 @@ def main():
         # config 5: 200 steps; V-cycles: from the previous step's pressure a V-cycle FGMRES
         # reaches the tolerance in fewer, cheaper applications (111 ms per step against
         # 142 ms on F-cycles)
-        rollout = channel_rollout(200, krylov=args.krylov, mgcycle=1)
+        rollout = channel_rollout(200, krylov=args.krylov, mgcycle=1, iter_finest=args.iter_finest)
 
     # roofline of the dominant kernel: level-1 FP32 line relaxation (k_line_wp<float,dir,8>),
     # durations from CUDA events around each launch inside the timed solves
@@ -1210,7 +1219,7 @@ def main():
         "scaling": "weak", "vs_baseline": None, "dtype": "f32 cycle + f64 refinement", "data": "synthetic",
         "config": {"workload": f"sphere_{args.n}^3_tanh1.5_r0.15_tol{args.tol:g}_mixed_fgmres{args.krylov}",
                    "grid": args.n, "tol": args.tol, "restol": restol, "stretch": 1.5, "radius": 0.15,
-                   "mg_cycle": args.mgcycle,
+                   "mg_cycle": args.mgcycle, "iterFinest": args.iter_finest,
                    "triangles": 5120, "nGhost": int(pr.geom.nGhost), "compat_shift": shift,
                    "outer": f"FGMRES({args.krylov}) preconditioned by MG_Solver" if args.krylov else "stationary",
                    "l2": "inputs larger than L2 (two 139 MB FP64 fields + hierarchy)",

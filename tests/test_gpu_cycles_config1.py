@@ -131,3 +131,27 @@ def test_config1_mixed_precision_error(gpu_built):
         got = solve(_config1(restol_Poisson=1e-10 * abs(pr.nlu0).max(), precision_mode=1, **kw))
         assert got["status"] == 0
         assert rel_l2_mean_free(got["p"][I], ref["p"][I], m, v) <= 1e-8
+
+
+@pytest.mark.parametrize("cyc", [(1, 1, 1), (3, 3, 3)], ids=["V", "F"])
+@pytest.mark.parametrize("counts", [(1, 10), (1, 4), (3, 2)], ids=lambda c: "finest%d_coarsest%d" % c)
+def test_mg_solver_one_call_smoothing_counts(counts, cyc, gpu_built):
+    """iterFinest / iterCoarsest (IBM/CORE_MG.F90:1148-1153, read at IBM/MAIN.F90:485):
+    one MG_Solver call equals the oracle's with the same counts."""
+    fin, coa = counts
+    pr = sphere_problem(16, stretch=1.5, mgcycle=cyc, iRedBlack=3, coarse_flag_mode=1, iterFinest=fin,
+                        iterCoarsest=coa)
+    o = Oracle(pr)
+    g = PoissonSolver(pr.params, pr.x, pr.y, pr.z).set_boundary(pr.geom)
+    try:
+        rng = np.random.default_rng(8)
+        p = np.asfortranarray(rng.standard_normal(pr.shape))
+        o.subtract_average(p)
+        ref = o.mg_solver(p.copy(order="F"), pr.nlu0)
+        got = p.copy(order="F")
+        g.MG_Solver(got, pr.nlu0)
+        I = tuple(slice(0, m) for m in (pr.params.nx + 1, pr.params.ny + 1, pr.params.nz + 1))
+        assert _rel(got[I], ref[I]) < 1e-10
+    finally:
+        g.close()
+        o.close()
