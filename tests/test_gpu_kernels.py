@@ -31,6 +31,9 @@ def cases():
         ("sphere48_tanh", lambda: P.sphere(48, seed=6, stretch=1.5)),
         # 256-cell x- and z-lines: the pipelined FP32 sweep in those directions
         ("sphere_256x20x256", lambda: P.sphere((256, 20, 256), seed=7, stretch=1.5)),
+        # full 64-cell y-lines and 32-cell z-lines over 64 x-cells (lines of exactly 32 S cells in
+        # every direction of a 3D grid)
+        ("sphere_64x64x32", lambda: P.sphere((64, 64, 32), seed=8, stretch=1.5)),
     ]
 
 
