@@ -44,9 +44,7 @@ segment's states and pulls the cotangent back step by step.
 """
 from __future__ import annotations
 
-import copy
 import math
-from typing import Optional
 
 import numpy as np
 import torch
