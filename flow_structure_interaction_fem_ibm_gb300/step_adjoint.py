@@ -65,8 +65,8 @@ class StepOperators:
 
     def __init__(self, problem, dt: float, reinv: float, bc_values, device="cpu", advec_scheme: int = 2):
         p = problem.params
-        if advec_scheme not in (2, 3):
-            raise ValueError("the step adjoint restates the Crank-Nicolson schemes (advec_scheme 2 or 3)")
+        if advec_scheme not in (1, 2, 3):
+            raise ValueError("advec_scheme 1 (ADAMS_BASHFORTH2), 2 or 3 (CRANK_NICOLSON1 / 2)")
         if abs(p.alfa) > 1e-3:
             raise ValueError("the step adjoint restates central advection (alfa = 0)")
         if p.ndim != DIM_3D:
@@ -78,6 +78,8 @@ class StepOperators:
         self.dev = torch.device(device)
         self.scheme = int(advec_scheme)
         self.dt, self.reinv = float(dt), float(reinv)
+        # the implicit convective terms: Crank-Nicolson halves, Adams-Bashforth none
+        self.half = 0.0 if self.scheme == 1 else 0.5 * self.dt
         self.values = np.asarray(bc_values, dtype=np.float64).reshape(6, 3)
         self.n = (p.nx - 1, p.ny - 1, p.nz - 1)
         self.shape = problem.shape
@@ -215,10 +217,12 @@ class StepOperators:
         return (t * self.fluid).sum()
 
     # --------------------------------------------------- rhs_advec_diff --
-    def rhs_advec_diff(self, vel, faces, bc9):
-        """Crank-Nicolson right-hand sides nl = vel - dt/2 N(vel) + dt/2 D(vel)
-        on the interior (rhs_advec central branch, rhs_loadAB, rhs_diff)."""
-        out = []
+    def rhs_advec_diff(self, vel, faces, bc9, nl_old=None):
+        """Right-hand sides on the interior (rhs_advec central branch,
+        rhs_loadAB, rhs_diff): Crank-Nicolson nl = vel - dt/2 N(vel) +
+        dt/2 D(vel); Adams-Bashforth nl = vel - dt (1.5 N(vel) - 0.5 N_old) +
+        dt/2 D(vel), which also returns the new N_old = N(vel)."""
+        out, new_old = [], []
         for q in range(3):
             U = vel[q]
             conv, diff = 0.0, 0.0
@@ -235,14 +239,19 @@ class StepOperators:
                 am = (self.col(self.dxcinv[a], a) * (1 - m) + dinv * m * 2.0) * dinv * self.nuM[a]
                 ap = (self.col(self.dxcinv[a], a, 1) * (1 - pp) + dinv * pp * 2.0) * dinv * self.nuP[a]
                 diff = diff + am * (Um * (1 - m) + b * m) - (am + ap) * Uc + ap * (Up * (1 - pp) + b * pp)
-            nl = self.cells(U, 0) - self.dt * (conv * 0.5) + 0.5 * self.dt * diff
+            if self.scheme == 1:
+                load = 1.5 * conv - (1.5 - 1.0) * self.cells(nl_old[q], 0)
+                new_old.append(self.put_interior(nl_old[q], conv))
+            else:
+                load = conv * 0.5
+            nl = self.cells(U, 0) - self.dt * load + 0.5 * self.dt * diff
             out.append(self.put_interior(None, nl))
-        return out
+        return (out, new_old) if self.scheme == 1 else out
 
     def rhs_adjust_bc(self, faces, bc9, nl):
         """Boundary values of flagged faces times the implicit coefficients move
         to the right-hand sides (IBM/CORE_RHS_AD.F90:588-780)."""
-        h = 0.5 * self.dt
+        h = self.half
         md, pd = [], []
         for a in range(3):
             m, pp = self.cells(self.fl[2 * a], a), self.cells(self.fl[2 * a + 1], a)
@@ -276,7 +285,7 @@ class StepOperators:
     def ad_rows(self, faces):
         """Row coefficients (am, ap per axis, sum of ac) of itsolv_ad / calc_residual_ad
         with the Crank-Nicolson convective terms (IBM/CORE_SOLVE_AD.F90:343-390)."""
-        h = 0.5 * self.dt
+        h = self.half
         am, ap, acs = [], [], 0.0
         for a in range(3):
             m, pp = self.cells(self.fl[2 * a], a), self.cells(self.fl[2 * a + 1], a)
@@ -953,10 +962,15 @@ class StepAdjoint:
         return self._w
 
     # ---------------------------------------------------------------- step --
-    def step(self, vel, faces, bc, time=0.0):
-        """One step as a torch graph: returns (vel, faces, bc) after the step."""
+    def step(self, vel, faces, bc, *rest, time=0.0):
+        """One step as a torch graph: returns the state after the step, (vel,
+        faces, bc), with Adams-Bashforth (vel, faces, bc, nl_old) (rest =
+        (nl_old,): the previous step's convective terms)."""
         ops = self.ops
-        nl = ops.rhs_advec_diff(vel, faces, bc)
+        if ops.scheme == 1:
+            nl, nl_old = ops.rhs_advec_diff(vel, faces, bc, rest[0])
+        else:
+            nl = ops.rhs_advec_diff(vel, faces, bc)
         vel1, bc1 = ops.set_bc(vel, bc, time + self.dt)
         nl1 = ops.rhs_adjust_bc(faces, bc1, nl)
         out = _SolveAD.apply(self, *vel1, *nl1, *bc1, *faces)
@@ -966,7 +980,7 @@ class StepAdjoint:
         nlu0 = ops.rhs_poisson(faces3)
         p = _Pressure.apply(self, nlu0)
         vel3, faces4 = ops.correct_vel(p, vel2, faces3, bn)
-        return vel3, faces4, bc2
+        return (vel3, faces4, bc2, nl_old) if ops.scheme == 1 else (vel3, faces4, bc2)
 
     def step_recorded(self, state, time=0.0):
         """One step without a graph; returns (next state, the recorded
@@ -991,17 +1005,22 @@ class StepAdjoint:
             self.replay = None
 
     def _step_vjp(self, state, cot, time=0.0):
-        vel, faces, bc = [[t.detach().clone().requires_grad_(True) for t in grp] for grp in state]
+        groups = [[t.detach().clone().requires_grad_(True) for t in grp] for grp in state]
         with torch.enable_grad():
-            out = self.step(vel, faces, bc, time)
-            flat_out = [*out[0], *out[1], *out[2]]
-            flat_cot = [*cot[0], *cot[1], *cot[2]]
+            out = self.step(*groups, time=time)
+            flat_out = [t for grp in out for t in grp]
+            flat_cot = [t for grp in cot for t in grp]
             keep = [(o, c) for o, c in zip(flat_out, flat_cot) if c is not None]
-            gr = torch.autograd.grad([o for o, _ in keep], [*vel, *faces, *bc], grad_outputs=[c for _, c in keep],
+            inputs = [t for grp in groups for t in grp]
+            gr = torch.autograd.grad([o for o, _ in keep], inputs, grad_outputs=[c for _, c in keep],
                                      allow_unused=True)
         z = lambda t: torch.zeros(self.ops.shape, dtype=torch.float64, device=self.ops.dev) if t is None else t
         gr = [z(t) for t in gr]
-        return gr[0:3], gr[3:6], gr[6:15]
+        res, o = [], 0
+        for grp in groups:
+            res.append(gr[o:o + len(grp)])
+            o += len(grp)
+        return tuple(res)
 
 
 def wake_plane_loss(problem, u, x_plane: float, device=None):
@@ -1046,18 +1065,23 @@ class RolloutAdjoint:
         fs = self.fs
         torch.cuda.synchronize()   # the product's stream has finished the step
         cl = lambda ts: [t.permute(2, 1, 0).clone() for t in ts]
-        return dict(vel=cl(fs.vel), faces=cl(fs.faces), bc=cl(fs.bc), pPrime=fs.pPrime.clone(), time=fs.time,
-                    ntime=fs.ntime, p_prev=None if fs._p_prev is None else fs._p_prev.clone())
+        return dict(vel=cl(fs.vel), faces=cl(fs.faces), bc=cl(fs.bc), nl_old=cl(fs.nl_old), pPrime=fs.pPrime.clone(),
+                    time=fs.time, ntime=fs.ntime, p_prev=None if fs._p_prev is None else fs._p_prev.clone())
 
     def _load(self, st):
         fs = self.fs
-        for dst, grp in ((fs.vel, st["vel"]), (fs.faces, st["faces"]), (fs.bc, st["bc"])):
+        for dst, grp in ((fs.vel, st["vel"]), (fs.faces, st["faces"]), (fs.bc, st["bc"]), (fs.nl_old, st["nl_old"])):
             for b, t in zip(dst, grp):
                 b.permute(2, 1, 0).copy_(t)
         fs.pPrime.copy_(st["pPrime"])
         fs._p_prev = None if st.get("p_prev") is None else st["p_prev"].clone()
         fs.time, fs.ntime = st["time"], st["ntime"]
         torch.cuda.synchronize()   # before the product's stream reads them
+
+    def _state(self, st):
+        """The step graph's state from a saved state."""
+        S = (st["vel"], st["faces"], st["bc"])
+        return S + (st["nl_old"],) if self.scheme == 1 else S
 
     def forward(self, u0, v0, w0, steps: int, adjoint_steps: int, checkpoint_every: int, warmup: int = 0):
         """Runs `steps` product steps from (u0, v0, w0); returns the final state.
@@ -1114,6 +1138,8 @@ class RolloutAdjoint:
         sh = self.sa.ops.shape
         z = lambda: torch.zeros(sh, dtype=torch.float64, device=self.sa.ops.dev)
         cot = ([z() if g is None else g for g in gv], [z(), z(), z()], [z() for _ in range(9)])
+        if self.scheme == 1:   # Adams-Bashforth carries the convective terms of the last step
+            cot = cot + ([z(), z(), z()],)
         starts = sorted(self.checkpoints)
         recompute = 0.0
         for c in reversed(starts):
@@ -1125,7 +1151,7 @@ class RolloutAdjoint:
             self.backend.pPrime.copy_(ck["pPrime"])
             self.backend.p_prev = None if ck.get("p_prev") is None else ck["p_prev"].clone()
             torch.cuda.synchronize()
-            S, t = (ck["vel"], ck["faces"], ck["bc"]), ck["time"]
+            S, t = self._state(ck), ck["time"]
             seg = []
             for n in range(c, end):
                 S1, rec = self.sa.step_recorded(S, time=t)

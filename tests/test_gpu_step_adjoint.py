@@ -69,11 +69,12 @@ def test_torch_step_matches_the_product_step(gpu_built):
 
 
 @pytest.mark.gpu
-def test_rollout_adjoint_matches_central_differences(gpu_built):
+@pytest.mark.parametrize("scheme", [2, 1], ids=["cn", "ab2"])
+def test_rollout_adjoint_matches_central_differences(gpu_built, scheme):
     import torch
     from flow_structure_interaction_fem_ibm_gb300.step_adjoint import RolloutAdjoint, wake_plane_loss
     pr = _channel()
-    ra = RolloutAdjoint(pr, DT, REINV, INFLOW)
+    ra = RolloutAdjoint(pr, DT, REINV, INFLOW, advec_scheme=scheme)
     steps, adj, every = 6, 4, 2
     try:
         ra.forward(*_velocity(pr), steps=steps, adjoint_steps=adj, checkpoint_every=every)

@@ -343,3 +343,83 @@ def test_two_step_adjoint_without_a_body(scheme):
         assert abs(fd - adj) <= 1e-7 * abs(fd) + 1e-11, (fd, adj)
     finally:
         be.close()
+
+
+def test_adams_bashforth_right_hand_side_matches_the_oracle():
+    """rhs_advec_diff with ADAMS_BASHFORTH2 (rhs_loadAB, IBM/CORE_RHS_AD.F90:385-430):
+    nl and the updated history nl_old against the oracle's loops."""
+    pr = _channel()
+    ops = StepOperators(pr, DT, NU, INFLOW, advec_scheme=1)
+    rng = np.random.default_rng(21)
+    sh = pr.shape
+    r = lambda: np.asfortranarray(rng.standard_normal(sh))
+    o = Oracle(pr)
+    try:
+        u, v, w = r(), r(), r()
+        faces = [r(), r(), r()]
+        bc9 = [r() for _ in range(9)]
+        old = [r(), r(), r()]
+        visc = np.full(sh, NU, order="F")
+        nl = [np.zeros(sh, order="F") for _ in range(3)]
+        old_o = [a.copy(order="F") for a in old]
+        o.rhs_advec_diff(DT, u, v, w, faces, visc, old_o, nl, bc9=bc9, bcvisc=(visc,) * 3, advec_scheme=1)
+        nlt, oldt = ops.rhs_advec_diff([T(u), T(v), T(w)], [T(a) for a in faces], [T(b) for b in bc9],
+                                       [T(a) for a in old])
+        for a, b in zip(nlt, nl):
+            assert _close(N(a)[ops.I], b[ops.I], 1e-14)
+        for a, b in zip(oldt, old_o):
+            assert _close(N(a), b, 1e-14)
+    finally:
+        o.close()
+
+
+def test_two_step_adjoint_adams_bashforth():
+    """ADAMS_BASHFORTH2 carries the convective terms of the last step: the
+    state gains nl_old, and the adjoint of two steps matches central
+    differences in the velocity and in that history."""
+    pr = _channel()
+    be = OracleBackend(pr, DT, NU, advec_scheme=1)
+    sa = StepAdjoint(pr, DT, NU, INFLOW, be, advec_scheme=1)
+    sh = pr.shape
+    try:
+        u, v, w = _velocity(pr)
+        vel, bc = sa.ops.set_bc([T(u), T(v), T(w)], [torch.zeros(sh, dtype=torch.float64) for _ in range(9)], 0.0)
+        rng = np.random.default_rng(4)
+        old = [T(0.1 * rng.standard_normal(sh)) for _ in range(3)]
+        S0 = (vel, sa.ops.face_vel(vel, (bc[0], bc[4], bc[8])), bc, old)
+
+        def run(S):
+            be.pPrime[...] = 0.0
+            with torch.no_grad():
+                for n in range(2):
+                    S = sa.step(*S, time=n * DT)
+            return S
+
+        be.pPrime[...] = 0.0
+        with torch.no_grad():
+            S1 = sa.step(*S0)
+            S2 = sa.step(*S1, time=DT)
+        uf = S2[0][0].clone().requires_grad_(True)
+        with torch.enable_grad():
+            gu = torch.autograd.grad(wake_plane_loss(pr, uf, 3.0)[0], uf)[0]
+        z = lambda: torch.zeros(sh, dtype=torch.float64)
+        cot = ([gu, z(), z()], [z(), z(), z()], [z() for _ in range(9)], [z(), z(), z()])
+        for S, t in ((S1, DT), (S0, 0.0)):
+            be.pPrime[...] = 0.0
+            cot = sa.step_vjp(S, cot, time=t)
+        inner = torch.zeros(sh, dtype=torch.float64)
+        inner[sa.ops.I] = 1.0
+        for k in (0, 3):
+            d = [T(rng.standard_normal(sh)) * inner for _ in range(3)]
+            adj = sum(float((a * b).sum()) for a, b in zip(cot[k], d))
+            h = 1e-5
+
+            def moved(sgn):
+                return tuple([a + sgn * h * b for a, b in zip(S0[k], d)] if i == k else S0[i] for i in range(4))
+
+            fd = (float(wake_plane_loss(pr, run(moved(1.0))[0][0], 3.0)[0])
+                  - float(wake_plane_loss(pr, run(moved(-1.0))[0][0], 3.0)[0])) / (2 * h)
+            assert abs(fd) > 1e-7
+            assert abs(fd - adj) <= 1e-7 * abs(fd) + 1e-11, (k, fd, adj)
+    finally:
+        be.close()
