@@ -94,11 +94,7 @@ def test_rollout_adjoint_matches_central_differences(gpu_built, scheme):
             def run(sgn):
                 st = dict(base)
                 st["vel"] = [a + sgn * h * b for a, b in zip(base["vel"], d)]
-                ra._load(st)
-                for _ in range(adj):
-                    rec = ra.fs.step()
-                    assert rec["ad_status"] == 0 and rec["poisson_status"] == 0
-                return float(loss_fn([t.permute(2, 1, 0) for t in ra.fs.vel]))
+                return float(loss_fn(ra.rerun(st, adj)))   # the product's rollout from the moved state
 
             fd = (run(1.0) - run(-1.0)) / (2 * h)
             assert abs(fd) > 1e-5
