@@ -13,9 +13,10 @@
  * one CUDA stream and all device memory of its hierarchy.  That stream is
  * non-blocking: it does not wait for work on other streams, so device inputs
  * written on another stream (a torch tensor copy, for one) must be complete
- * before the call (cudaDeviceSynchronize or an event), and a device output
- * read on another stream needs the same unless the entry point returned a
- * value it had to read back (statuses, iteration counts, sums).
+ * before the call (cudaDeviceSynchronize or an event).  Every handle entry
+ * point waits for its own work before it returns, so its outputs can be read
+ * on any stream afterwards; fsi_mg_subtract_average_noalloc only queues its
+ * work on the stream it is given.
  *
  * Status codes (all entry points):
  *    0  success / converged
