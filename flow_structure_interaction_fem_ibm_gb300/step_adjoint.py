@@ -67,8 +67,6 @@ class StepOperators:
         p = problem.params
         if advec_scheme not in (1, 2, 3):
             raise ValueError("advec_scheme 1 (ADAMS_BASHFORTH2), 2 or 3 (CRANK_NICOLSON1 / 2)")
-        if abs(p.alfa) > 1e-3:
-            raise ValueError("the step adjoint restates central advection (alfa = 0)")
         if p.ndim != DIM_3D:
             raise ValueError("the step adjoint is 3D")
         for s, t in enumerate(p.bc):
@@ -80,6 +78,9 @@ class StepOperators:
         self.dt, self.reinv = float(dt), float(reinv)
         # the implicit convective terms: Crank-Nicolson halves, Adams-Bashforth none
         self.half = 0.0 if self.scheme == 1 else 0.5 * self.dt
+        # hybrid advection: second-order upwind faces blended in by alfa (IBM/MAIN.F90:649-652)
+        self.alfa = float(p.alfa)
+        self.hybrid = abs(self.alfa) > 1.0e-3
         self.values = np.asarray(bc_values, dtype=np.float64).reshape(6, 3)
         self.n = (p.nx - 1, p.ny - 1, p.nz - 1)
         self.shape = problem.shape
@@ -233,6 +234,8 @@ class StepOperators:
                 Uc, Um, Up = self.cells(U, a), self.cells(U, a, -1), self.cells(U, a, 1)
                 velp = (fxp * Up + (1.0 - fxp) * Uc) * (1 - pp) + b * pp
                 velm = (fxm * Uc + (1.0 - fxm) * Um) * (1 - m) + b * m
+                if self.hybrid:
+                    velp, velm = self._hybrid_faces(U, a, velp, velm, b, m, pp, faces[a])
                 conv = conv + (velp * self.cells(faces[a], a, 1) - velm * self.cells(faces[a], a)) \
                     * self.col(self.dxinv[a], a)
                 dinv = self.col(self.dxinv[a], a)
@@ -247,6 +250,50 @@ class StepOperators:
             nl = self.cells(U, 0) - self.dt * load + 0.5 * self.dt * diff
             out.append(self.put_interior(None, nl))
         return (out, new_old) if self.scheme == 1 else out
+
+    def _hybrid_faces(self, U, a, vele, velw, b, m, pp, F):
+        """The face values of rhs_advec's hybrid branch (IBM/CORE_RHS_AD.F90:150-382):
+        (1 - alfa) central + alfa second-order upwind, the upwind side chosen by
+        the sign of the face velocity, the first and last two cells of the axis
+        (iumm / iupp) falling back to the central value; along x the plus-side
+        value weights U(ipp) with edxWeightp1, as the reference writes it."""
+        n = self.n[a]
+        t = torch.arange(1, n + 1, device=self.dev)
+        shp = [1, 1, 1]
+        shp[a] = -1
+        dinv = self.dxinv[a]
+        d = lambda idx: dinv[idx].reshape(shp)
+        imm = torch.clamp(t - 2, min=0)                 # i-2, or 0
+        ipp = torch.clamp(t + 2, max=n + 1)             # i+2, or the node count
+        tm, tp = t - 1, t + 1
+        em1 = (d(tm) + 2.0 * d(t)) / (d(tm) + d(t))
+        em2 = d(t) / (d(tm) + d(t))
+        ep1 = (d(ipp) + 2.0 * d(tp)) / (d(ipp) + d(tp))
+        ep2 = ep1 if a == 0 else d(tp) / (d(ipp) + d(tp))
+        wm1 = (d(imm) + 2.0 * d(tm)) / (d(imm) + d(tm))
+        wm2 = d(tm) / (d(imm) + d(tm))
+        wp1 = (d(tp) + 2.0 * d(t)) / (d(tp) + d(t))
+        wp2 = d(t) / (d(tp) + d(t))
+        mm = ((t == 1) | (t == 2)).to(torch.float64).reshape(shp)
+        pq = ((t == n) | (t == n - 1)).to(torch.float64).reshape(shp)
+        sl = list(self.I)
+
+        def along(idx):   # U at the cells idx along a, interior elsewhere
+            sl2 = list(sl)
+            sl2[a] = slice(None)
+            return U[tuple(sl2)].index_select(a, idx)
+
+        Uc, Um, Up = self.cells(U, a), self.cells(U, a, -1), self.cells(U, a, 1)
+        Umm, Upp = along(imm), along(ipp)
+        one = torch.ones_like(Uc)
+        sp = torch.copysign(one, self.cells(F, a, 1))
+        sm = torch.copysign(one, self.cells(F, a))
+        vele_up = ((1.0 + sp) * (mm * vele + (1 - mm) * (em1 * Uc - em2 * Um))
+                   + (1.0 - sp) * (pq * vele + (1 - pq) * (ep1 * Up - ep2 * Upp))) * 0.5 * (1 - pp) + b * pp
+        velw_up = ((1.0 + sm) * (mm * velw + (1 - mm) * (wm1 * Um - wm2 * Umm))
+                   + (1.0 - sm) * (pq * velw + (1 - pq) * (wp1 * Uc - wp2 * Up))) * 0.5 * (1 - m) + b * m
+        al = self.alfa
+        return (1.0 - al) * vele + al * vele_up, (1.0 - al) * velw + al * velw_up
 
     def rhs_adjust_bc(self, faces, bc9, nl):
         """Boundary values of flagged faces times the implicit coefficients move
