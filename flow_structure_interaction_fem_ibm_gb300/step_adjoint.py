@@ -2,8 +2,10 @@
 step), for rollouts such as the sphere-wake channel.
 
 One step of ``time_step.FractionalStep`` (IBM/CORE_TIME_STEP.F90:201-267,
-NO_VAN_KAN, Crank-Nicolson, stationary body, laminar viscosity 1/Re) maps
-the state S = (u, v, w, face_u, face_v, face_w, bc9) to the next one:
+NO_VAN_KAN, Crank-Nicolson 1 / 2 or Adams-Bashforth, central or hybrid
+advection, stationary body, laminar viscosity 1/Re) maps the state
+S = (u, v, w, face_u, face_v, face_w, bc9[, nl_old with Adams-Bashforth]) to
+the next one:
 
     nl   = rhs_advec_diff(vel, faces, bc9)          IBM/CORE_RHS_AD.F90:13-585
     vel1, bc1 = set_bc(vel, t + dt)                 IBM/CORE_SET_BC.F90:22-377,
