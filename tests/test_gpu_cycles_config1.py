@@ -155,3 +155,24 @@ def test_mg_solver_one_call_smoothing_counts(counts, cyc, gpu_built):
     finally:
         g.close()
         o.close()
+
+
+@pytest.mark.parametrize("omega", [0.8, 1.3])
+def test_mg_solver_one_call_relaxation(omega, gpu_built):
+    """The line-SOR relaxation var (1 - omega) + omega sol (IBM/CORE_MG.F90:2008,
+    read at IBM/MAIN.F90:478): one MG_Solver call against the oracle's."""
+    pr = sphere_problem(16, stretch=1.5, iRedBlack=3, coarse_flag_mode=1, omega=omega)
+    o = Oracle(pr)
+    g = PoissonSolver(pr.params, pr.x, pr.y, pr.z).set_boundary(pr.geom)
+    try:
+        rng = np.random.default_rng(8)
+        p = np.asfortranarray(rng.standard_normal(pr.shape))
+        o.subtract_average(p)
+        ref = o.mg_solver(p.copy(order="F"), pr.nlu0)
+        got = p.copy(order="F")
+        g.MG_Solver(got, pr.nlu0)
+        I = tuple(slice(0, m) for m in (pr.params.nx + 1, pr.params.ny + 1, pr.params.nz + 1))
+        assert _rel(got[I], ref[I]) < 1e-10
+    finally:
+        g.close()
+        o.close()

@@ -261,3 +261,28 @@ def test_subtract_average_fresh_cells(pair):
     finally:
         o.set_fresh(None)
         g.set_fresh_cells(None)
+
+
+@pytest.mark.parametrize("omega", [0.8, 1.3])
+def test_line_smoother_sweeps_with_relaxation(omega, gpu_built):
+    """One MG_itsolv at every level with omega != 1 (the relaxed store
+    var (1 - omega) + omega sol of the line kernels): FP64 within 1e-12 and the
+    FP32 smoother within its rounding of the FP64 oracle."""
+    pr = P.sphere((64, 64, 32), seed=8, stretch=1.5)
+    pr.params.iRedBlack, pr.params.coarse_flag_mode, pr.params.omega = 3, 1, omega
+    o = Oracle(pr)
+    g = PoissonSolver(pr.params, pr.x, pr.y, pr.z).set_boundary(pr.geom)
+    try:
+        rng = np.random.default_rng(14)
+        for d, n in levels(o, pr.params.ndim):
+            sh = o.level_shape(d, n)
+            v0 = np.asfortranarray(rng.standard_normal(sh).astype(np.float32).astype(np.float64))
+            r = np.asfortranarray(rng.standard_normal(sh).astype(np.float32).astype(np.float64))
+            ref = o.itsolv(d, n, v0.copy(order="F"), r)
+            for op, tol in ((0, RTOL), (7, 2e-5)):
+                got = v0.copy(order="F")
+                g.debug_op(op, d, n, got, r)
+                assert rel(got, ref) < tol, (op, d, n, rel(got, ref))
+    finally:
+        g.close()
+        o.close()
