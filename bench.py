@@ -64,6 +64,9 @@ def parse():
     ap.add_argument("--iter-finest", type=int, default=1,
                     help="line sweeps per colour and direction on the finest levels of the headline forms "
                          "(iterFinest; the reference's input uses 2, the stationary forms keep it)")
+    ap.add_argument("--omega", type=float, default=1.5,
+                    help="line-SOR relaxation of the headline forms (omega; the reference's input uses 1, the "
+                         "stationary forms keep it)")
     ap.add_argument("--no-adjoint", action="store_true")
     ap.add_argument("--no-steps", action="store_true", help="skip the face_vel/correct_vel/update_pressure timing")
     ap.add_argument("--steps-only", action="store_true",
@@ -876,6 +879,7 @@ def main():
         c = {"V": 1, "W": 2, "F": 3}[args.mgcycle]
         pp.mgcycle = (c, c, c)
         pp.iterFinest = args.iter_finest
+        pp.omega = args.omega
         s = PoissonSolver(pp, pr.x, pr.y, pr.z).set_boundary(pr.geom)
         p = np.zeros(pr.shape, order="F")
         s.solve_poisson(p, pr.nlu0)
@@ -952,6 +956,7 @@ def main():
         q.precision_mode, q.outer_krylov = mode, krylov
         q.mgcycle = (cyc, cyc, cyc)
         q.iterFinest = args.iter_finest
+        q.omega = args.omega
         for k, v in kw.items():
             setattr(q, k, v)
         return PoissonSolver(q, pr.x, pr.y, pr.z).set_boundary(pr.geom)
@@ -1008,27 +1013,30 @@ def main():
     fp64_value = replica_throughput(world, k64, fp64_s)
 
     # the reference's own stationary outer iteration (outer_krylov = 0), mixed: one full solve
-    s_stat = make(1, 0, iterMax_Poisson=4000, mgcycle=(1, 1, 1), iterFinest=pr.params.iterFinest)
+    s_stat = make(1, 0, iterMax_Poisson=4000, mgcycle=(1, 1, 1), iterFinest=pr.params.iterFinest,
+                  omega=pr.params.omega)
     st_stat, it_stat, dev_stat = step(s_stat, must_converge=False)
     s_stat.close()
     # FP64 stationary: time per outer iteration (the solve needs the same iteration count)
     s_stat64 = make(0, 0, iterMax_Poisson=12, restol_Poisson=0.0, mgcycle=(1, 1, 1),
-                    iterFinest=pr.params.iterFinest)
+                    iterFinest=pr.params.iterFinest, omega=pr.params.omega)
     step(s_stat64, must_converge=False)
     _, it64, dev64 = step(s_stat64, must_converge=False)
     s_stat64.close()
     # the headline forms with other cycles and smoothing counts (V-cycles with iterFinest 2
     # are the reference input's settings)
-    cycles = {"headline": {"cycle": args.mgcycle, "iterFinest": args.iter_finest}}
-    for cname, fin, fname, mode in (("V", 2, "mixed", 1), ("F", 2, "mixed", 1), ("F", 1, "mixed", 1),
-                                    ("W", 2, "mixed", 1), ("V", 2, "fp64", 0), ("F", 2, "fp64", 0)):
+    cycles = {"headline": {"cycle": args.mgcycle, "iterFinest": args.iter_finest, "omega": args.omega}}
+    for cname, fin, om, fname, mode in (("V", 2, 1.0, "mixed", 1), ("V", 1, 1.0, "mixed", 1),
+                                        ("F", 2, 1.0, "mixed", 1), ("F", 1, 1.0, "mixed", 1),
+                                        ("W", 2, 1.0, "mixed", 1), ("V", 2, 1.0, "fp64", 0),
+                                        ("V", 1, 1.0, "fp64", 0)):
         c = {"V": 1, "W": 2, "F": 3}[cname]
-        if c == cyc and fin == args.iter_finest:
+        if c == cyc and fin == args.iter_finest and om == args.omega:
             continue
-        sv = make(mode, args.krylov, mgcycle=(c, c, c), iterFinest=fin)
+        sv = make(mode, args.krylov, mgcycle=(c, c, c), iterFinest=fin, omega=om)
         tc, _, itc, _ = timed(sv, 2, 1)
-        cycles[f"{cname}_finest{fin}_{fname}"] = {"ms_per_solve": 1e3 * tc / 2, "iters": itc[0],
-                                                  "solves_per_s": replica_throughput(world, 2, tc)}
+        cycles[f"{cname}_finest{fin}_omega{om:g}_{fname}"] = {"ms_per_solve": 1e3 * tc / 2, "iters": itc[0],
+                                                              "solves_per_s": replica_throughput(world, 2, tc)}
         sv.close()
     stationary = {
         "cycle": "V, iterFinest as the reference input (the reference's own iteration)",
@@ -1219,7 +1227,7 @@ def main():
         "scaling": "weak", "vs_baseline": None, "dtype": "f32 cycle + f64 refinement", "data": "synthetic",
         "config": {"workload": f"sphere_{args.n}^3_tanh1.5_r0.15_tol{args.tol:g}_mixed_fgmres{args.krylov}",
                    "grid": args.n, "tol": args.tol, "restol": restol, "stretch": 1.5, "radius": 0.15,
-                   "mg_cycle": args.mgcycle, "iterFinest": args.iter_finest,
+                   "mg_cycle": args.mgcycle, "iterFinest": args.iter_finest, "omega": args.omega,
                    "triangles": 5120, "nGhost": int(pr.geom.nGhost), "compat_shift": shift,
                    "outer": f"FGMRES({args.krylov}) preconditioned by MG_Solver" if args.krylov else "stationary",
                    "l2": "inputs larger than L2 (two 139 MB FP64 fields + hierarchy)",

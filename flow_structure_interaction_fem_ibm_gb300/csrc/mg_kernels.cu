@@ -299,7 +299,7 @@ __device__ __forceinline__ void stage_line_rows(const LineArgs<T> &A, int L, int
                 if (A.dir_hi) dd = dd - A.ppp_hi * cc;
                 cc = T(0);
             }
-            put(r, aa, bb, cc, dd);
+            put(r, aa, bb, cc, dd, in[u].vo);
         }
     }
 }
@@ -320,6 +320,10 @@ __global__ void __launch_bounds__(256) k_line_wp(LineArgs<T> A)
     T *sm = reinterpret_cast<T *>(smem_raw);
     constexpr int RP = wp_pitch<S>();
     T *sa = sm, *sb = sm + WP_LINES * RP, *sc = sm + 2 * WP_LINES * RP, *sd = sm + 3 * WP_LINES * RP;
+    // relaxed y/z sweeps (!OMEGA1): the rows' old values as staged, for the store; x-lines
+    // reload them with a coalesced load instead (their store phase is cheaper that way)
+    constexpr bool KEEP_OLD = !OMEGA1 && DIR != 0;
+    T *sv = sm + 4 * WP_LINES * RP;
     const Dims &d = A.d;
     const int nb = d.m[X::b] - 1, nc = d.m[X::c] - 1;
     const int L = FULL ? 32 * S : d.m[X::a] - 1;   // FULL: every row of every lane is a line row
@@ -349,9 +353,11 @@ __global__ void __launch_bounds__(256) k_line_wp(LineArgs<T> A)
 
     // ---- 1. staging: loads for up to 4 rows are issued before any use ----
     if (oks)
-        stage_line_rows<T, DIR, S, FULL>(A, L, base, ps, qs, rr, sa_, sb_, sc_, [&](int r, T aa, T bb, T cc, T dd) {
+        stage_line_rows<T, DIR, S, FULL>(A, L, base, ps, qs, rr, sa_, sb_, sc_,
+                                         [&](int r, T aa, T bb, T cc, T dd, T vo) {
             const int si = sidx(gs, r);
             sa[si] = aa; sb[si] = bb; sc[si] = cc; sd[si] = dd;
+            if (KEEP_OLD) sv[si] = vo;
         });
     __syncthreads();
 
@@ -432,7 +438,9 @@ __global__ void __launch_bounds__(256) k_line_wp(LineArgs<T> A)
             const int i = r + 1;
             const int o = base + i * sa_;
             const T x = sd[sidx(gs, r)];
-            A.v[o] = OMEGA1 ? x : A.v[o] * (T(1) - A.omega) + A.omega * x;
+            // the old value as staged (no other thread writes the cell in between)
+            const T old = OMEGA1 ? T(0) : (KEEP_OLD ? sv[sidx(gs, r)] : A.v[o]);
+            A.v[o] = OMEGA1 ? x : old * (T(1) - A.omega) + A.omega * x;
         }
         if (rr == 0 && A.dir_lo) A.v[base] = A.ppp_lo;
         if (rr == (L - 1) % 32 && A.dir_hi) A.v[base + (L + 1) * sa_] = A.ppp_hi;
@@ -1675,7 +1683,7 @@ __global__ void __launch_bounds__(TPB) k_avg_partial_rows(const double *p, const
 
 // ------------------------------------------------------------- launchers --
 template <typename T, int DIR, int S, bool O1>
-size_t wp_smem() { return 4 * (size_t)WP_LINES * wp_pitch<S>() * sizeof(T); }
+size_t wp_smem() { return (O1 || DIR == 0 ? 4 : 5) * (size_t)WP_LINES * wp_pitch<S>() * sizeof(T); }
 
 template <typename T, int DIR, int S, bool O1>
 void launch_wp_one(const LineArgs<T> &a, long long nlines, cudaStream_t s)
@@ -1691,15 +1699,16 @@ void launch_wp_one(const LineArgs<T> &a, long long nlines, cudaStream_t s)
 template <typename T, int DIR, int S>
 cudaError_t wp_attr()
 {
-    const int b = (int)wp_smem<T, DIR, S, true>();
+    const int b = (int)wp_smem<T, DIR, S, true>(), b0 = (int)wp_smem<T, DIR, S, false>();
     cudaError_t e;
     if ((e = cudaFuncSetAttribute(k_line_wp<T, DIR, S, true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, b)))
         return e;
     if ((e = cudaFuncSetAttribute(k_line_wp<T, DIR, S, true, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, b)))
         return e;
-    if ((e = cudaFuncSetAttribute(k_line_wp<T, DIR, S, false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, b)))
+    if ((e = cudaFuncSetAttribute(k_line_wp<T, DIR, S, false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                  b0)))
         return e;
-    return cudaFuncSetAttribute(k_line_wp<T, DIR, S, false, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, b);
+    return cudaFuncSetAttribute(k_line_wp<T, DIR, S, false, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, b0);
 }
 
 template <typename T, int DIR>
