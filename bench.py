@@ -933,6 +933,7 @@ def main():
         for mode in (1, 0):
             pp = copy.deepcopy(pr.params)
             pp.precision_mode, pp.iterMax_Poisson, pp.restol_Poisson = mode, 2, 0.0
+            pp.omega = args.omega   # the headline's relaxation (the sweep kernels' relaxed store)
             s = PoissonSolver(pp, pr.x, pr.y, pr.z).set_boundary(pr.geom)
             p = np.zeros(pr.shape, order="F")
             s.solve_poisson(p, pr.nlu0)

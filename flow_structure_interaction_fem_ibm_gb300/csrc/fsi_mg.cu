@@ -1695,14 +1695,16 @@ int fsi_mg_line_timing(void *handle, int enable, double *out)
     }
     if (out) {
         // algorithmic bytes of one colour of a level-1 line sweep: the colour's
-        // rhs, flags and new values plus the other colour's values (omega = 1)
+        // rhs, flags and new values plus the other colour's values, and with a
+        // relaxation omega != 1 the colour's old values (var (1 - omega) + omega sol)
         const double cells = (double)(c.nx - 1) * (c.ny - 1) * (c.p.ndim == 3 ? c.nz - 1 : 1);
+        const double relaxed = (c.p.omega != 1.0) ? 1.0 : 0.0;
         out[0] = (double)c.lt_n[1];
         out[1] = c.lt_ms[1];
-        out[2] = 0.5 * (4.0 + 1.0 + 4.0 + 4.0) * cells;
+        out[2] = 0.5 * (4.0 + 1.0 + 4.0 + 4.0 + 4.0 * relaxed) * cells;
         out[3] = (double)c.lt_n[0];
         out[4] = c.lt_ms[0];
-        out[5] = 0.5 * (8.0 + 1.0 + 8.0 + 8.0) * cells;
+        out[5] = 0.5 * (8.0 + 1.0 + 8.0 + 8.0 + 8.0 * relaxed) * cells;
     }
     return 0;
 }
