@@ -624,7 +624,7 @@ def device_time_step(n, seed, tol, krylov, steps=3, reinv=1e-3, dt=1e-3):
 
 def channel_rollout(steps, cells=(192, 128, 128), krylov=30, warmup=2, restol=1e-6, dt=0.005, re=300.0,
                     adjoint_steps=50, checkpoint_every=10, x_plane=3.0, mgcycle=1, pressure_guess="extrapolate",
-                    iter_finest=1):
+                    iter_finest=1, omega=1.0):
     """The sphere-wake rollout: a 192 x 128 x 128 uniform channel on [0,6] x
     [0,4]^2, sphere of diameter 1 at (1.5, 2, 2) (GCM ghost cells), uniform
     inflow U = 1, zero-gradient outflow with the outflow mass balance,
@@ -658,6 +658,7 @@ def channel_rollout(steps, cells=(192, 128, 128), krylov=30, warmup=2, restol=1e
     q.restol_ad, q.iterMax_ad = 1e-10, 200
     q.mgcycle = (mgcycle,) * 3
     q.iterFinest = iter_finest
+    q.omega = omega
     inflow = np.array([[1.0, 0.0, 0.0]] + [[0.0, 0.0, 0.0]] * 5)
     fluid = 1.0 - pr.geom.iblank
     u0 = np.asfortranarray(fluid.astype(np.float64))
@@ -727,7 +728,7 @@ def channel_rollout(steps, cells=(192, 128, 128), krylov=30, warmup=2, restol=1e
            "divergence_note": "the maximum sits in the outflow cell layer, where div(face) = -dt nlw0 (the "
                               "reference's own chain gives the same, to 1e-12); div + dt nlw0 is the projection's "
                               "residual everywhere",
-           "restol_Poisson": restol, "pressure_guess": pressure_guess, "iterFinest": iter_finest,
+           "restol_Poisson": restol, "pressure_guess": pressure_guess, "iterFinest": iter_finest, "omega": omega,
            "mg_cycle": "VWF"[mgcycle - 1],
            "u_max": umax, "time": fs.time, "ghost_cells": int(pr.geom.nGhost),
            "device_bytes_in_use_forward": int(free0 - free_fwd), "device_bytes_in_use": int(free0 - free1),
@@ -889,7 +890,8 @@ def main():
 
     if args.rollout > 0:
         print(json.dumps(channel_rollout(args.rollout, args.rollout_cells, args.krylov,
-                                         adjoint_steps=args.rollout_adjoint, iter_finest=args.iter_finest)))
+                                         adjoint_steps=args.rollout_adjoint, iter_finest=args.iter_finest,
+                                         omega=args.omega)))
         return
 
     if args.profile_fp64:
