@@ -8,8 +8,11 @@
 //   - iblank by directional (scan-line) fill of cell centres enclosed by the
 //     surface (the fill step of IBM/BOUNDARY_IBLANK_FAST.F90:2-501),
 //   - ghost marks and the ordered ghost list (IBM/GCM_SET_BOUNDARY.F90:49-118),
-//   - body intercept = closest surface point among the elements that share the
-//     three closest markers (IBM/GCM_INTERCEPT_KERNELS_UNSTRUC.F90:26-398),
+//   - body intercept by the reference's selection rules (the first element
+//     whose normal projection passes the area test, else an edge foot from the
+//     closest marker, over the three closest markers;
+//     IBM/GCM_INTERCEPT_KERNELS_UNSTRUC.F90:26-398), with the reference's
+//     inward element normals (IBM/BOUNDARY_SET_ARCLENGTH_NORM.F90:69-165,200-320),
 //   - image point, stencil cell search and the Neumann Vandermonde inverse
 //     (IBM/GCM_SET_BOUNDARY.F90:124-494, LU with partial pivoting in place of
 //     DGETRF/DGETRI from IBM/Lapack_VICAR.F90).
@@ -36,30 +39,155 @@ inline size_t fidx(int nx, int ny, int i, int j, int k)
     return (size_t)i + (size_t)(nx + 2) * ((size_t)j + (size_t)(ny + 2) * (size_t)k);
 }
 
-// Closest point on triangle abc to p (Ericson, Real-Time Collision Detection, 5.1.5).
-V3 closest_on_tri(V3 p, V3 a, V3 b, V3 c)
+// The reference's surface conventions (IBM/BOUNDARY_SET_ARCLENGTH_NORM.F90:
+// 69-165, 200-320): element normals point INTO the body, n = (p2 - p1) x
+// (p3 - p2) / |.| over the nodes in inward order, centroid (p1 + p2 + p3) / 3.
+// A closed surface given outward (positive signed volume, as fsi_geom_icosphere
+// writes it) is read with nodes 2 and 3 swapped, as determine_norm_dir_unstruc
+// reorders it.
+struct Surface {
+    int nv = 0, nt = 0;
+    const double *verts = nullptr;
+    std::vector<int> nodes;               // (3, nt), inward order
+    std::vector<V3> nrm;                  // inward unit normals
+    std::vector<std::vector<int>> vtri;   // marker -> its elements, ascending
+    V3 p(int m) const { return V3{verts[3 * m], verts[3 * m + 1], verts[3 * m + 2]}; }
+    int node(int e, int q) const { return nodes[3 * (size_t)e + q]; }
+};
+
+Surface make_surface(int nv, const double *verts, int nt, const int32_t *tris)
 {
-    V3 ab = b - a, ac = c - a, ap = p - a;
-    double d1 = dot(ab, ap), d2 = dot(ac, ap);
-    if (d1 <= 0 && d2 <= 0) return a;
-    V3 bp = p - b;
-    double d3 = dot(ab, bp), d4 = dot(ac, bp);
-    if (d3 >= 0 && d4 <= d3) return b;
-    double vc = d1 * d4 - d3 * d2;
-    if (vc <= 0 && d1 >= 0 && d3 <= 0) { double v = d1 / (d1 - d3); return a + v * ab; }
-    V3 cp = p - c;
-    double d5 = dot(ab, cp), d6 = dot(ac, cp);
-    if (d6 >= 0 && d5 <= d6) return c;
-    double vb = d5 * d2 - d1 * d6;
-    if (vb <= 0 && d2 >= 0 && d6 <= 0) { double w = d2 / (d2 - d6); return a + w * ac; }
-    double va = d3 * d6 - d5 * d4;
-    if (va <= 0 && (d4 - d3) >= 0 && (d5 - d6) >= 0) {
-        double w = (d4 - d3) / ((d4 - d3) + (d5 - d6));
-        return b + w * (c - b);
+    Surface s;
+    s.nv = nv; s.nt = nt; s.verts = verts;
+    double vol6 = 0.0;
+    for (int t = 0; t < nt; ++t) {
+        V3 a = s.p(tris[3 * t]), b = s.p(tris[3 * t + 1]), c = s.p(tris[3 * t + 2]);
+        vol6 += dot(a, cross(b, c));
     }
-    double denom = 1.0 / (va + vb + vc);
-    double v = vb * denom, w = vc * denom;
-    return a + v * ab + w * ac;
+    const bool outward = vol6 > 0.0;
+    s.nodes.resize(3 * (size_t)nt);
+    for (int t = 0; t < nt; ++t) {
+        s.nodes[3 * (size_t)t] = tris[3 * t];
+        s.nodes[3 * (size_t)t + 1] = outward ? tris[3 * t + 2] : tris[3 * t + 1];
+        s.nodes[3 * (size_t)t + 2] = outward ? tris[3 * t + 1] : tris[3 * t + 2];
+    }
+    s.nrm.resize(nt);
+    s.vtri.assign(nv, {});
+    for (int t = 0; t < nt; ++t) {
+        V3 p1 = s.p(s.node(t, 0)), p2 = s.p(s.node(t, 1)), p3 = s.p(s.node(t, 2));
+        V3 a = p2 - p1, b = p3 - p2;
+        V3 n{a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x};
+        double mag = std::sqrt(n.x * n.x + n.y * n.y + n.z * n.z);
+        s.nrm[t] = V3{n.x / mag, n.y / mag, n.z / mag};
+        for (int q = 0; q < 3; ++q) s.vtri[s.node(t, q)].push_back(t);
+    }
+    return s;
+}
+
+// The angle between a and b as the reference's vector_angle takes it
+// (IBM/AMODULES.F90:968-988): acos of the cosine, 0 or pi outside (-1, 1).
+double vec_angle(V3 a, V3 b)
+{
+    auto len = [](V3 v) { double s = 0.0; s = s + v.x * v.x; s = s + v.y * v.y; s = s + v.z * v.z; return std::sqrt(s); };
+    double c = dot(a, b) / (len(a) * len(b));
+    if (c < 1.0 && c > -1.0) return std::acos(c);
+    return c > 0.0 ? 0.0 : 4.0 * std::atan(1.0);
+}
+
+// Normal projection of p onto element e's plane and the Heron-area test of
+// check_BIInsideTriangle (IBM/BOUNDARY_IBLANK_FAST.F90:1028-1159): inside when
+// |area(124) + area(234) + area(314) - area(123)| < 1e-4 area(123).
+bool project_inside(const Surface &s, int e, V3 p, V3 &bi)
+{
+    const V3 n = s.nrm[e];
+    const V3 p1 = s.p(s.node(e, 0)), p2 = s.p(s.node(e, 1)), p3 = s.p(s.node(e, 2));
+    double plane = -n.x * p1.x - n.y * p1.y - n.z * p1.z;
+    double d = -(n.x * p.x + n.y * p.y + n.z * p.z + plane);
+    bi = V3{p.x + n.x * d, p.y + n.y * d, p.z + n.z * d};
+    auto side = [](V3 a, V3 b) {
+        return std::sqrt((a.x - b.x) * (a.x - b.x) + (a.y - b.y) * (a.y - b.y) + (a.z - b.z) * (a.z - b.z));
+    };
+    double s12 = side(p2, p1), s23 = side(p3, p2), s31 = side(p1, p3);
+    double s14 = side(bi, p1), s24 = side(bi, p2), s34 = side(bi, p3);
+    auto heron = [](double a, double b, double c) {
+        double h = 0.5 * (a + b + c);
+        return std::sqrt(h * (h - a) * (h - b) * (h - c));
+    };
+    double a123 = heron(s12, s23, s31);
+    double diff = heron(s12, s24, s14) + heron(s23, s24, s34) + heron(s31, s34, s14) - a123;
+    return std::fabs(diff) < 1.0e-4 * a123;
+}
+
+// Body intercept of the point p (GCM_calc_bodyIntercept_Unstruc,
+// IBM/GCM_INTERCEPT_KERNELS_UNSTRUC.F90:26-398).  For each of the three
+// closest markers: the first of its elements (ascending) whose normal
+// projection passes the inside test gives the intercept; failing that, the
+// element whose outward normal makes the smallest angle with (p - marker)
+// (last of equals) is taken and the intercept is the nearer foot on its two
+// edges that leave the marker, clamped to the marker.  Of the three
+// candidates the nearest (first of equals) wins.
+void body_intercept(const Surface &s, V3 p, V3 &bi, int &elem)
+{
+    int best[3] = {-1, -1, -1};
+    double bd[3] = {1e300, 1e300, 1e300};
+    for (int m = 0; m < s.nv; ++m) {
+        V3 q = s.p(m);
+        double dx = q.x - p.x, dy = q.y - p.y, dz = q.z - p.z;
+        double d = dx * dx + dy * dy + dz * dz;
+        for (int r = 0; r < 3; ++r)
+            if (d < bd[r]) {
+                for (int u = 2; u > r; --u) { bd[u] = bd[u - 1]; best[u] = best[u - 1]; }
+                bd[r] = d; best[r] = m;
+                break;
+            }
+    }
+    V3 cand[3];
+    int cel[3];
+    for (int c = 0; c < 3; ++c) {
+        const int mk = best[c];
+        const V3 cv = s.p(mk);
+        int ce = -1;
+        bool found = false;
+        double angMin = 1.0e16;
+        V3 b{0, 0, 0};
+        for (int e : s.vtri[mk]) {
+            V3 t;
+            if (project_inside(s, e, p, t)) { b = t; ce = e; found = true; break; }
+            double ang = vec_angle(p - cv, -1.0 * s.nrm[e]);
+            if (ang <= angMin) { angMin = ang; ce = e; b = t; }
+        }
+        if (!found) {
+            int a = s.node(ce, 0), bb = s.node(ce, 1), cc = s.node(ce, 2), na, nb;
+            if (a == mk) { na = bb; nb = cc; }
+            else if (bb == mk) { na = cc; nb = a; }
+            else { na = a; nb = bb; }
+            const V3 v01 = p - cv;
+            double dmin = 1.0e16;
+            V3 ei = cv;
+            for (int edge = 0; edge < 2; ++edge) {
+                V3 v12 = s.p(edge == 0 ? na : nb) - cv;
+                double mag = std::sqrt(v12.x * v12.x + v12.y * v12.y + v12.z * v12.z);
+                double inv = 1.0 / mag;
+                v12 = V3{v12.x * inv, v12.y * inv, v12.z * inv};
+                double pl = v01.x * v12.x + v01.y * v12.y + v01.z * v12.z;
+                V3 t = (pl < 0.0 || pl > mag) ? cv : V3{cv.x + pl * v12.x, cv.y + pl * v12.y, cv.z + pl * v12.z};
+                double d = (t.x - p.x) * (t.x - p.x) + (t.y - p.y) * (t.y - p.y) + (t.z - p.z) * (t.z - p.z);
+                if (d < dmin) { dmin = d; ei = t; }
+            }
+            b = ei;
+        }
+        cand[c] = b;
+        cel[c] = ce;
+    }
+    int w = 0;
+    double dw = 0.0;
+    for (int c = 0; c < 3; ++c) {
+        V3 r = cand[c] - p;
+        double d = r.x * r.x + r.y * r.y + r.z * r.z;
+        if (c == 0 || d < dw) { dw = d; w = c; }
+    }
+    bi = cand[w];
+    elem = cel[w];
 }
 
 // In-place inverse of an 8x8 column-major matrix by LU with partial pivoting.
@@ -279,47 +407,15 @@ int fsi_geom_gcm_coeffs(int nx, int ny, int nz, const double *x, const double *y
     for (int j = 0; j <= ny; ++j) { yc[j] = 0.5 * (y[j] + y[j + 1]); dyv[j] = y[j + 1] - y[j]; }
     for (int k = 0; k <= nz; ++k) { zc[k] = 0.5 * (z[k] + z[k + 1]); dzv[k] = z[k + 1] - z[k]; }
     xc[nx + 1] = x[nx + 1]; yc[ny + 1] = y[ny + 1]; zc[nz + 1] = z[nz + 1];
-    // vertex -> elements adjacency and element normals
-    std::vector<std::vector<int>> vtri(nv);
-    std::vector<V3> nrm(nt);
-    for (int t = 0; t < nt; ++t) {
-        for (int q = 0; q < 3; ++q) vtri[tris[3 * t + q]].push_back(t);
-        const double *a = verts + 3 * tris[3 * t], *b = verts + 3 * tris[3 * t + 1], *c = verts + 3 * tris[3 * t + 2];
-        V3 n = cross(V3{b[0] - a[0], b[1] - a[1], b[2] - a[2]}, V3{c[0] - a[0], c[1] - a[1], c[2] - a[2]});
-        double s = 1.0 / std::sqrt(dot(n, n));
-        nrm[t] = s * n;
-    }
+    const Surface surf = make_surface(nv, verts, nt, tris);
     for (int n = 0; n < nGhost; ++n) {
         int g_i = iG[n], g_j = jG[n], g_k = kG[n];
         V3 gc{xc[g_i], yc[g_j], zc[g_k]};
-        // three closest markers
-        int best[3] = {-1, -1, -1};
-        double bd[3] = {1e300, 1e300, 1e300};
-        for (int m = 0; m < nv; ++m) {
-            V3 pm{verts[3 * m], verts[3 * m + 1], verts[3 * m + 2]};
-            double d = dot(pm - gc, pm - gc);
-            for (int q = 0; q < 3; ++q)
-                if (d < bd[q]) {
-                    for (int r = 2; r > q; --r) { bd[r] = bd[r - 1]; best[r] = best[r - 1]; }
-                    bd[q] = d; best[q] = m;
-                    break;
-                }
-        }
-        double dmin = 1e300;
-        int celem = -1;
-        V3 bip{0, 0, 0};
-        for (int q = 0; q < 3; ++q) {
-            if (best[q] < 0) continue;
-            for (int t : vtri[best[q]]) {
-                const double *a = verts + 3 * tris[3 * t], *b = verts + 3 * tris[3 * t + 1],
-                             *c = verts + 3 * tris[3 * t + 2];
-                V3 cp = closest_on_tri(gc, V3{a[0], a[1], a[2]}, V3{b[0], b[1], b[2]}, V3{c[0], c[1], c[2]});
-                double d = dot(cp - gc, cp - gc);
-                if (d < dmin) { dmin = d; celem = t; bip = cp; }
-            }
-        }
+        V3 bip;
+        int celem;
+        body_intercept(surf, gc, bip, celem);
         double ds = std::sqrt(dot(bip - gc, bip - gc));
-        V3 slope = (1.0 / ds) * (bip - gc);
+        V3 slope{(bip.x - gc.x) / ds, (bip.y - gc.y) / ds, (bip.z - gc.z) / ds};
         double pl = ds * probeLengthNormalized;
         V3 ipt = gc + pl * slope;
         probeLength[n] = pl;
@@ -336,7 +432,7 @@ int fsi_geom_gcm_coeffs(int nx, int ny, int nz, const double *x, const double *y
             if (zc[k] <= ipt.z && zc[k + 1] > ipt.z) ck = k;
         if (ci < 0 || cj < 0 || ck < 0) return -(n + 1);
         iCI[n] = ci; jCI[n] = cj; kCI[n] = ck;
-        V3 bn = nrm[celem];
+        V3 bn = surf.nrm[celem];   // inward, as the reference's (the sign only scales the Neumann row)
         // The reference builds the Vandermonde matrix in absolute coordinates
         // (IBM/GCM_SET_BOUNDARY.F90:392-440), which loses about log10(1/h^3)
         // digits on fine cells, so the weights of a constant no longer sum to 1
