@@ -6,7 +6,8 @@
 //   - icosphere surface generation (stands in for unstruc_surface_in.dat,
 //     IBM/BOUNDARY_MARKER_INIT.F90:209-247),
 //   - iblank by directional (scan-line) fill of cell centres enclosed by the
-//     surface (the fill step of IBM/BOUNDARY_IBLANK_FAST.F90:2-501),
+//     surface (the fill step of IBM/BOUNDARY_IBLANK_FAST.F90:2-501), then the
+//     reference's clean-up passes for a solid body (IBM/BOUNDARY_SET.F90:267-410),
 //   - ghost marks and the ordered ghost list (IBM/GCM_SET_BOUNDARY.F90:49-118),
 //   - body intercept by the reference's selection rules (the first element
 //     whose normal projection passes the area test, else an edge foot from the
@@ -349,9 +350,43 @@ long fsi_geom_iblank(int nx, int ny, int nz, const double *x, const double *y, c
             std::sort(hits.begin(), hits.end());
             for (int i = 1; i <= nx - 1; ++i) {
                 int left = (int)(std::lower_bound(hits.begin(), hits.end(), xc[i]) - hits.begin());
-                if (left & 1) { iblank[fidx(nx, ny, i, j, k)] = 1; ++nsolid; }
+                if (left & 1) iblank[fidx(nx, ny, i, j, k)] = 1;
             }
         }
+    // The clean-up passes set_internal_boundary runs on a solid body
+    // (IBM/BOUNDARY_SET.F90:267-410), in its order.  find_isolatedIblank (:440-499):
+    // a solid cell with no other solid cell in its 3x3x3 block (clipped to the
+    // interior) turns fluid.  find_iblankHoles (:502-602) acts under SSM only.
+    const int nxc = nx - 1, nyc = ny - 1, nzc = nz - 1;
+    for (int k = 1; k <= nzc; ++k)
+        for (int j = 1; j <= nyc; ++j)
+            for (int i = 1; i <= nxc; ++i) {
+                if (iblank[fidx(nx, ny, i, j, k)] != 1) continue;
+                int solid = 0;
+                for (int c = std::max(k - 1, 1); c <= std::min(k + 1, nzc); ++c)
+                    for (int b = std::max(j - 1, 1); b <= std::min(j + 1, nyc); ++b)
+                        for (int a = std::max(i - 1, 1); a <= std::min(i + 1, nxc); ++a)
+                            solid += iblank[fidx(nx, ny, a, b, c)];
+                if (solid <= 1) iblank[fidx(nx, ny, i, j, k)] = 0;
+            }
+    // fill_cell (IBM/SSM_SET_BC.F90:1425-1511): a fluid cell whose solid
+    // neighbour faces it across a flagged face closes.  Under GCM the level-1
+    // flags are set_outer_iup's (IBM/BOUNDARY_SET.F90:54-130): the low face of
+    // the first cell and the high face of the last cell of every line.  One
+    // pass per direction, x then y then z, updating in place.
+    const int dims[3] = {nxc, nyc, nzc};
+    for (int axis = 0; axis < 3; ++axis)
+        for (int k = 1; k <= nzc; ++k)
+            for (int j = 1; j <= nyc; ++j)
+                for (int i = 1; i <= nxc; ++i) {
+                    int8_t &cell = iblank[fidx(nx, ny, i, j, k)];
+                    if (cell != 0) continue;
+                    const int pos = axis == 0 ? i : axis == 1 ? j : k;
+                    const int8_t lo = iblank[fidx(nx, ny, i - (axis == 0), j - (axis == 1), k - (axis == 2))];
+                    const int8_t hi = iblank[fidx(nx, ny, i + (axis == 0), j + (axis == 1), k + (axis == 2))];
+                    if ((lo == 1 && pos == dims[axis]) || (hi == 1 && pos == 1)) cell = 1;
+                }
+    for (size_t o = 0; o < nf; ++o) nsolid += iblank[o];
     return nsolid;
 }
 

@@ -13,7 +13,9 @@
  *                      around every element's bounding box is classified by
  *                      search_vertex_dotNorm (:504-1024), the other cells are
  *                      filled along i, then j, then k from the first decided
- *                      cell of each line.
+ *                      cell of each line; then the clean-up passes of
+ *                      set_internal_boundary for a solid body
+ *                      (IBM/BOUNDARY_SET.F90:267-410).
  *   og_ghost_list      GCM_set_internal_boundary (IBM/GCM_SET_BOUNDARY.F90:
  *                      22-118): ghost marks and their (k, j, i) order.
  *   og_gcm             the rest of GCM_set_internal_boundary (:119-304):
@@ -452,15 +454,46 @@ long og_iblank(int nx, int ny, int nz, const double *x, const double *y, const d
                 if (und[fi(nx, ny, i, j, k)] == 1) tmp[fi(nx, ny, i, j, k)] = tmp[fi(nx, ny, i, j, k - 1)];
     memset(iblank, 0, nf);
     if (band) memset(band, 0, nf);
-    result = 0;
     for (int k = 1; k <= nzc; ++k)
         for (int j = 1; j <= nyc; ++j)
             for (int i = 1; i <= nxc; ++i) {
                 size_t o = fi(nx, ny, i, j, k);
                 iblank[o] = tmp[o];
-                result += tmp[o];
                 if (band && und[o] == -1) band[o] = 1;
             }
+    /* set_internal_boundary (IBM/BOUNDARY_SET.F90:267-410) then runs, for
+     * solid bodies, find_isolatedIblank(1) (:440-499), find_iblankHoles(1)
+     * (:502-602, which acts under SSM only) and fill_cell
+     * (IBM/SSM_SET_BC.F90:1425-1511) */
+    for (int k = 1; k <= nzc; ++k)
+        for (int j = 1; j <= nyc; ++j)
+            for (int i = 1; i <= nxc; ++i) {
+                if (iblank[fi(nx, ny, i, j, k)] != 1) continue;
+                int sum = 0;
+                for (int kk = (k - 1 > 1 ? k - 1 : 1); kk <= (k + 1 < nzc ? k + 1 : nzc); ++kk)
+                    for (int jj = (j - 1 > 1 ? j - 1 : 1); jj <= (j + 1 < nyc ? j + 1 : nyc); ++jj)
+                        for (int ii = (i - 1 > 1 ? i - 1 : 1); ii <= (i + 1 < nxc ? i + 1 : nxc); ++ii)
+                            sum += iblank[fi(nx, ny, ii, jj, kk)];
+                if (sum <= 1) iblank[fi(nx, ny, i, j, k)] = 0;
+            }
+    /* fill_cell: a fluid cell between a solid neighbour and a flagged face
+     * turns solid; under GCM the level-1 face flags are those of
+     * set_outer_iup (IBM/BOUNDARY_SET.F90:54-130), set on the first and last
+     * cell of every line */
+    for (int pass = 0; pass < 3; ++pass)
+        for (int k = 1; k <= nzc; ++k)
+            for (int j = 1; j <= nyc; ++j)
+                for (int i = 1; i <= nxc; ++i) {
+                    size_t o = fi(nx, ny, i, j, k);
+                    if (iblank[o] != 0) continue;
+                    int c = pass == 0 ? i : pass == 1 ? j : k, last = pass == 0 ? nxc : pass == 1 ? nyc : nzc;
+                    size_t om = pass == 0 ? fi(nx, ny, i - 1, j, k) : pass == 1 ? fi(nx, ny, i, j - 1, k) : fi(nx, ny, i, j, k - 1);
+                    size_t op = pass == 0 ? fi(nx, ny, i + 1, j, k) : pass == 1 ? fi(nx, ny, i, j + 1, k) : fi(nx, ny, i, j, k + 1);
+                    int up = c == last, um = c == 1;
+                    if ((iblank[om] == 1 && up) || (iblank[op] == 1 && um)) iblank[o] = 1;
+                }
+    result = 0;
+    for (size_t o = 0; o < nf; ++o) result += iblank[o];
     surf_close(&s);
 done:
     free(xc); free(dxv); free(yc); free(dyv); free(zc); free(dzv);

@@ -128,3 +128,36 @@ def test_oracle_orientation_step():
     assert L.og_orient_inward(v.size // 3, v.ctypes.data_as(dp), t1.size // 3, t1.ctypes.data_as(ip), 2.0, 2.0, 2.0) == 1
     assert np.array_equal(t1.reshape(-1, 3), t.reshape(-1, 3)[:, [0, 2, 1]])
     assert L.og_orient_inward(v.size // 3, v.ctypes.data_as(dp), t1.size // 3, t1.ctypes.data_as(ip), 2.0, 2.0, 2.0) == 0
+
+
+def _custom(n, centre, radius):
+    p = P.default_params(3, n, n, n, body=True)
+    x, y, z = make_grid(p.nx, p.ny, p.nz, "uniform")
+    v, t = P.icosphere(3, radius, centre)
+    g = P.body_geometry(p, x, y, z, v, t)
+    r = reference_geometry(p.nx, p.ny, p.nz, x, y, z, v, t, (3.0, 3.0, 3.0))
+    return p, g, r
+
+
+def test_isolated_solid_cell_is_removed():
+    """find_isolatedIblank (IBM/BOUNDARY_SET.F90:440-499): a body that
+    encloses a single cell centre leaves no solid cell."""
+    h = 1.0 / 16
+    p, g, r = _custom(16, (7.5 * h, 7.5 * h, 7.5 * h), 0.3 * h)
+    assert int(r.band.sum()) > 0
+    assert int(g.iblank.sum()) == 0 and int(r.iblank.sum()) == 0
+    assert g.nGhost == 0
+
+
+def test_one_cell_gap_at_the_outer_wall_is_closed():
+    """fill_cell (IBM/SSM_SET_BC.F90:1425-1511): a fluid cell between the body
+    and the flagged outer face turns solid, in the product as in the oracle."""
+    h = 1.0 / 16
+    p, g, r = _custom(16, (12.0 * h, 8.0 * h, 8.0 * h), 2.75 * h)
+    I = (slice(1, p.nx), slice(1, p.ny), slice(1, p.nz))
+    assert np.array_equal(g.iblank[I], r.iblank[I])
+    nxc = p.nx - 1
+    closed = (g.iblank[nxc] == 1) & (g.iblank[nxc - 1] == 1)
+    assert closed.any()                          # the gap cells on the axis lines closed
+    assert (g.iblank[nxc][g.iblank[nxc - 1] == 0] == 0).all()
+    assert g.nGhost == r.nGhost and np.array_equal(g.xBI, r.xBI)
