@@ -55,7 +55,7 @@ def build_geometry(force: bool = False) -> Path:
     lib = OUT / "libfsi_geom.so"
     if force or _stale(lib, [src]):
         tmp = lib.with_suffix(f".so.tmp{os.getpid()}")
-        _run(["g++", "-O2", "-std=c++17", "-fPIC", "-shared", "-ffp-contract=off",
+        _run(["g++", "-O2", "-std=c++17", "-fPIC", "-shared", "-ffp-contract=off", "-pthread",
               "-o", str(tmp), str(src)])
         os.replace(tmp, lib)
     return lib

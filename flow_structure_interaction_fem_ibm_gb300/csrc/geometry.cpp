@@ -5,9 +5,10 @@
 // closed triangulated surfaces (UNSTRUCTURED_SURFACE bodies):
 //   - icosphere surface generation (stands in for unstruc_surface_in.dat,
 //     IBM/BOUNDARY_MARKER_INIT.F90:209-247),
-//   - iblank by directional (scan-line) fill of cell centres enclosed by the
-//     surface (the fill step of IBM/BOUNDARY_IBLANK_FAST.F90:2-501), then the
-//     reference's clean-up passes for a solid body (IBM/BOUNDARY_SET.F90:267-410),
+//   - iblank by the reference's band and dot-normal classification and fill
+//     (IBM/BOUNDARY_IBLANK_FAST.F90:2-1024; the band cells spread over the host
+//     threads), then its clean-up passes for a solid body
+//     (IBM/BOUNDARY_SET.F90:267-410),
 //   - ghost marks and the ordered ghost list (IBM/GCM_SET_BOUNDARY.F90:49-118),
 //   - body intercept by the reference's selection rules (the first element
 //     whose normal projection passes the area test, else an edge foot from the
@@ -19,10 +20,12 @@
 //     DGETRF/DGETRI from IBM/Lapack_VICAR.F90).
 // Arrays are Fortran column-major with lower bound 0, as in the reference.
 #include <algorithm>
+#include <atomic>
 #include <cmath>
 #include <cstdint>
 #include <cstring>
 #include <map>
+#include <thread>
 #include <utility>
 #include <vector>
 
@@ -51,6 +54,7 @@ struct Surface {
     const double *verts = nullptr;
     std::vector<int> nodes;               // (3, nt), inward order
     std::vector<V3> nrm;                  // inward unit normals
+    std::vector<V3> cen;                  // centroids
     std::vector<std::vector<int>> vtri;   // marker -> its elements, ascending
     V3 p(int m) const { return V3{verts[3 * m], verts[3 * m + 1], verts[3 * m + 2]}; }
     int node(int e, int q) const { return nodes[3 * (size_t)e + q]; }
@@ -73,6 +77,7 @@ Surface make_surface(int nv, const double *verts, int nt, const int32_t *tris)
         s.nodes[3 * (size_t)t + 2] = outward ? tris[3 * t + 1] : tris[3 * t + 2];
     }
     s.nrm.resize(nt);
+    s.cen.resize(nt);
     s.vtri.assign(nv, {});
     for (int t = 0; t < nt; ++t) {
         V3 p1 = s.p(s.node(t, 0)), p2 = s.p(s.node(t, 1)), p3 = s.p(s.node(t, 2));
@@ -80,6 +85,7 @@ Surface make_surface(int nv, const double *verts, int nt, const int32_t *tris)
         V3 n{a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x};
         double mag = std::sqrt(n.x * n.x + n.y * n.y + n.z * n.z);
         s.nrm[t] = V3{n.x / mag, n.y / mag, n.z / mag};
+        s.cen[t] = V3{(p1.x + p2.x + p3.x) / 3.0, (p1.y + p2.y + p3.y) / 3.0, (p1.z + p2.z + p3.z) / 3.0};
         for (int q = 0; q < 3; ++q) s.vtri[s.node(t, q)].push_back(t);
     }
     return s;
@@ -117,6 +123,128 @@ bool project_inside(const Surface &s, int e, V3 p, V3 &bi)
     double a123 = heron(s12, s23, s31);
     double diff = heron(s12, s24, s14) + heron(s23, s24, s34) + heron(s31, s34, s14) - a123;
     return std::fabs(diff) < 1.0e-4 * a123;
+}
+
+// The k markers nearest p in (squared distance, index) order: the order of
+// repeated MINLOC with each found marker set aside.
+void nearest_markers(const Surface &s, V3 p, int k, int *out)
+{
+    double bd[8];
+    for (int r = 0; r < k; ++r) { bd[r] = 1e300; out[r] = -1; }
+    for (int m = 0; m < s.nv; ++m) {
+        V3 q = s.p(m);
+        double dx = q.x - p.x, dy = q.y - p.y, dz = q.z - p.z;
+        double d = dx * dx + dy * dy + dz * dz;
+        for (int r = 0; r < k; ++r)
+            if (d < bd[r]) {
+                for (int u = k - 1; u > r; --u) { bd[u] = bd[u - 1]; out[u] = out[u - 1]; }
+                bd[r] = d; out[r] = m;
+                break;
+            }
+    }
+}
+
+// Signed distance of p from the plane (n, ref) as get_distance_face takes it
+// (IBM/BOUNDARY_IBLANK_FAST.F90:3535-3555): |p - ref| cos(angle(n, p - ref)).
+double plane_distance(V3 n, V3 ref, V3 p)
+{
+    if (p.x == ref.x && p.y == ref.y && p.z == ref.z) return 0.0;
+    V3 v = p - ref;
+    double len = 0.0;
+    len = len + v.x * v.x; len = len + v.y * v.y; len = len + v.z * v.z;
+    return std::sqrt(len) * std::cos(vec_angle(n, v));
+}
+
+// Whether the segment from p1 to p2 passes through element e: the segment's
+// crossing of the element's plane (get_inter, :3513-3533, an end within 1e-10
+// of the plane taken as is) lies inside the triangle by pointInTriangle's
+// test (:3862-3910): the three (edge x (point - vertex)) vectors, each scaled
+// by the first one's length, agree in direction within pi/10.
+bool segment_crosses(const Surface &s, int e, V3 p1, V3 p2)
+{
+    const V3 n = s.nrm[e], ref = s.cen[e];
+    double l1 = n.x * (p1.x - ref.x) + n.y * (p1.y - ref.y) + n.z * (p1.z - ref.z);
+    double l2 = n.x * (p2.x - ref.x) + n.y * (p2.y - ref.y) + n.z * (p2.z - ref.z);
+    V3 q;
+    if (std::fabs(l1) < 1e-10) q = p1;
+    else if (std::fabs(l2) < 1e-10) q = p2;
+    else {
+        double t = l1 / (l1 - l2);
+        q = V3{p1.x + t * (p2.x - p1.x), p1.y + t * (p2.y - p1.y), p1.z + t * (p2.z - p1.z)};
+    }
+    const V3 a = s.p(s.node(e, 0)), b = s.p(s.node(e, 1)), c = s.p(s.node(e, 2));
+    V3 c1 = cross(b - a, q - a), c2 = cross(c - b, q - b), c3 = cross(a - c, q - c);
+    auto len = [](V3 v) { double t = 0.0; t = t + v.x * v.x; t = t + v.y * v.y; t = t + v.z * v.z; return std::sqrt(t); };
+    double m1 = len(c1), m2 = len(c2), m3 = len(c3);
+    if (m1 < 1e-20 || m2 < 1e-20 || m3 < 1e-20) return false;
+    c1 = V3{c1.x / m1, c1.y / m1, c1.z / m1};
+    c2 = V3{c2.x / m1, c2.y / m1, c2.z / m1};
+    c3 = V3{c3.x / m1, c3.y / m1, c3.z / m1};
+    const double lim = 4.0 * std::atan(1.0) / 10.0;
+    return vec_angle(c1, c2) < lim && vec_angle(c2, c3) < lim;
+}
+
+// search_vertex_dotNorm (IBM/BOUNDARY_IBLANK_FAST.F90:504-1024) for the cell
+// centre p: true when p is solid (dot product >= 0 with the inward normal of
+// the chosen element).  The reference marker is the first of the seven
+// nearest markers whose segment to p crosses none of the elements around the
+// seven that do not contain it; a marker whose elements' normals are at least
+// pi/2 apart (check_if_edge_marker, :3580-3703) makes p fluid; otherwise the
+// element is, among the marker's elements, the nearest plane whose normal
+// projection passes the area test, or before the first such element the
+// smallest angle between (p - marker) and the outward normal (last of equals).
+// Returns -1 when no reference marker exists (the reference stops there).
+int dot_normal_solid(const Surface &s, V3 p, std::vector<int> &around)
+{
+    int near[7];
+    nearest_markers(s, p, 7, near);
+    around.clear();
+    for (int q = 0; q < 7; ++q)
+        if (near[q] >= 0) around.insert(around.end(), s.vtri[near[q]].begin(), s.vtri[near[q]].end());
+    std::sort(around.begin(), around.end());
+    around.erase(std::unique(around.begin(), around.end()), around.end());
+    int ref = -1;
+    for (int q = 0; q < 7 && ref < 0; ++q) {
+        if (near[q] < 0) break;
+        const int mk = near[q];
+        const V3 pm = s.p(mk);
+        bool blocked = false;
+        for (int e : around) {
+            if (s.node(e, 0) == mk || s.node(e, 1) == mk || s.node(e, 2) == mk) continue;
+            double dc = plane_distance(s.nrm[e], s.cen[e], p), dm = plane_distance(s.nrm[e], s.cen[e], pm);
+            if (dc * dm > 0.0) continue;
+            if (segment_crosses(s, e, p, pm)) { blocked = true; break; }
+        }
+        if (!blocked) ref = mk;
+    }
+    if (ref < 0) return -1;
+    const std::vector<int> &own = s.vtri[ref];
+    if (own.size() < 2) return -1;
+    const double half_pi = 4.0 * std::atan(1.0) / 2.0;
+    for (size_t a = 0; a + 1 < own.size(); ++a)
+        for (size_t b = a + 1; b < own.size(); ++b)
+            if (vec_angle(-1.0 * s.nrm[own[a]], -1.0 * s.nrm[own[b]]) >= half_pi) return 0;
+    double distIn = 1.0e16, angMin = 1.0e16;
+    bool inside = false;
+    int ce = -1;
+    for (int e : own) {
+        V3 bi;
+        const V3 n = s.nrm[e];
+        if (project_inside(s, e, p, bi)) {
+            inside = true;
+            const V3 p1 = s.p(s.node(e, 0));
+            double plane = -n.x * p1.x - n.y * p1.y - n.z * p1.z;
+            double d = std::fabs(-(n.x * p.x + n.y * p.y + n.z * p.z + plane));
+            if (d <= distIn) { distIn = d; ce = e; }
+        } else if (!inside) {
+            double ang = vec_angle(p - s.p(ref), -1.0 * n);
+            if (ang <= angMin) { angMin = ang; ce = e; }
+        }
+    }
+    if (ce < 0) return -1;
+    const V3 c = s.cen[ce], n = s.nrm[ce];
+    double dn = (p.x - c.x) * n.x + (p.y - c.y) * n.y + (p.z - c.z) * n.z;
+    return dn >= 0.0 ? 1 : 0;
 }
 
 // Body intercept of the point p (GCM_calc_bodyIntercept_Unstruc,
@@ -300,59 +428,91 @@ int fsi_geom_icosphere(int nsub, double radius, double cx, double cy, double cz,
     return 0;
 }
 
-// iblank(i,j,k) = 1 for cell centres enclosed by the closed surface, i,j,k in
-// 1..n?-1; ghost layers stay 0.  Scan lines along x: a centre is inside when an
-// odd number of surface crossings lie to its left.  Crossings are found with a
-// half-open rule on the (y,z) projection so that a line through a shared edge
-// or vertex is counted once.  Returns the number of solid cells.
+// iblank(i,j,k) = 1 for solid cells, i,j,k in 1..n?-1 (ghost layers stay 0), by
+// the reference's set_iblank_canonical_body_fast (IBM/BOUNDARY_IBLANK_FAST.F90:
+// 2-501): the cells whose centres bracket an element's bounding box form a band
+// classified one by one by the dot-normal test; every other cell takes the value
+// of the nearest band cell before it along k (or the first one after it when
+// none precedes; a line without band cells is fluid) -- the reference's i and j
+// fills are overwritten by its k fill.  Returns the number of solid cells, or -1
+// when the dot-normal test finds no reference marker for a band cell.
 long fsi_geom_iblank(int nx, int ny, int nz, const double *x, const double *y, const double *z,
                      int nv, const double *verts, int nt, const int32_t *tris, int8_t *iblank)
 {
-    (void)nv;
-    std::vector<double> xc(nx + 1), yc(ny + 1), zc(nz + 1);
+    std::vector<double> xc(nx + 2), yc(ny + 2), zc(nz + 2);
     for (int i = 0; i <= nx; ++i) xc[i] = 0.5 * (x[i] + x[i + 1]);
     for (int j = 0; j <= ny; ++j) yc[j] = 0.5 * (y[j] + y[j + 1]);
     for (int k = 0; k <= nz; ++k) zc[k] = 0.5 * (z[k] + z[k + 1]);
-    size_t nf = (size_t)(nx + 2) * (size_t)(ny + 2) * (size_t)(nz + 2);
+    const size_t nf = (size_t)(nx + 2) * (size_t)(ny + 2) * (size_t)(nz + 2);
     std::memset(iblank, 0, nf);
-    long nsolid = 0;
-    std::vector<double> hits;
-    for (int k = 1; k <= nz - 1; ++k)
-        for (int j = 1; j <= ny - 1; ++j) {
-            const double py = yc[j], pz = zc[k];
-            hits.clear();
-            for (int t = 0; t < nt; ++t) {
-                const double *a = verts + 3 * tris[3 * t], *b = verts + 3 * tris[3 * t + 1],
-                             *c = verts + 3 * tris[3 * t + 2];
-                double ymin = std::min({a[1], b[1], c[1]}), ymax = std::max({a[1], b[1], c[1]});
-                double zmin = std::min({a[2], b[2], c[2]}), zmax = std::max({a[2], b[2], c[2]});
-                if (py < ymin || py > ymax || pz < zmin || pz > zmax) continue;
-                // barycentric test in the (y,z) plane with a half-open edge rule
-                auto edge = [&](const double *p, const double *q) {
-                    return (q[1] - p[1]) * (pz - p[2]) - (q[2] - p[2]) * (py - p[1]);
-                };
-                double e0 = edge(a, b), e1 = edge(b, c), e2 = edge(c, a);
-                auto owns = [](double e, const double *p, const double *q) {
-                    if (e != 0.0) return e > 0.0;
-                    // tie-break: edges whose direction points to +y, or to +z when flat in y
-                    double dy = q[1] - p[1], dz = q[2] - p[2];
-                    return dy > 0.0 || (dy == 0.0 && dz < 0.0);
-                };
-                bool pos = owns(e0, a, b) && owns(e1, b, c) && owns(e2, c, a);
-                bool neg = owns(-e0, b, a) && owns(-e1, c, b) && owns(-e2, a, c);
-                if (!pos && !neg) continue;
-                double area = e0 + e1 + e2;
-                if (area == 0.0) continue;
-                double xh = (e1 * a[0] + e2 * b[0] + e0 * c[0]) / area;
-                hits.push_back(xh);
+    std::vector<int8_t> band(nf, 0);
+    const Surface surf = make_surface(nv, verts, nt, tris);
+    const int n_[3] = {nx, ny, nz};
+    const double *lo_node[3] = {x, y, z};
+    const std::vector<double> *cc[3] = {&xc, &yc, &zc};
+    for (int t = 0; t < nt; ++t) {
+        const V3 v[3] = {surf.p(surf.node(t, 0)), surf.p(surf.node(t, 1)), surf.p(surf.node(t, 2))};
+        auto comp = [](V3 a, int d) { return d == 0 ? a.x : d == 1 ? a.y : a.z; };
+        bool outside = false;
+        int lo[3], hi[3];
+        for (int d = 0; d < 3 && !outside; ++d) {
+            const double a = comp(v[0], d), b = comp(v[1], d), c = comp(v[2], d);
+            const double first = lo_node[d][1], last = lo_node[d][n_[d]];
+            if ((a <= first && b <= first && c <= first) || (a >= last && b >= last && c >= last)) outside = true;
+            const double bmin = std::min({a, b, c}), bmax = std::max({a, b, c});
+            int cmin = 0, cmax = 0;
+            const std::vector<double> &w = *cc[d];
+            for (int i = 0; i < n_[d]; ++i) {
+                if ((w[i] - bmin) * (w[i + 1] - bmin) <= 0.0) cmin = i;
+                if ((w[i] - bmax) * (w[i + 1] - bmax) <= 0.0) cmax = i + 1;
             }
-            if (hits.empty()) continue;
-            std::sort(hits.begin(), hits.end());
-            for (int i = 1; i <= nx - 1; ++i) {
-                int left = (int)(std::lower_bound(hits.begin(), hits.end(), xc[i]) - hits.begin());
-                if (left & 1) iblank[fidx(nx, ny, i, j, k)] = 1;
+            lo[d] = cmin == 0 ? 1 : cmin;
+            hi[d] = (cmax == 0 || cmax == n_[d]) ? n_[d] - 1 : cmax;
+        }
+        if (outside) continue;
+        for (int k = lo[2]; k <= hi[2]; ++k)
+            for (int j = lo[1]; j <= hi[1]; ++j)
+                for (int i = lo[0]; i <= hi[0]; ++i) band[fidx(nx, ny, i, j, k)] = 1;
+    }
+    // the band cells are independent: split them over the host threads
+    std::vector<size_t> cells;
+    for (int k = 1; k <= nz - 1; ++k)
+        for (int j = 1; j <= ny - 1; ++j)
+            for (int i = 1; i <= nx - 1; ++i)
+                if (band[fidx(nx, ny, i, j, k)]) cells.push_back(fidx(nx, ny, i, j, k));
+    const unsigned hw = std::max(1u, std::thread::hardware_concurrency());
+    const size_t nthreads = std::min<size_t>(std::min(hw, 64u), std::max<size_t>(1, cells.size() / 2048));
+    std::atomic<bool> failed(false);
+    auto work = [&](size_t t0) {
+        std::vector<int> around;
+        around.reserve(64);
+        for (size_t q = t0; q < cells.size() && !failed.load(std::memory_order_relaxed); q += nthreads) {
+            const size_t o = cells[q];
+            const int i = (int)(o % (size_t)(nx + 2)), j = (int)((o / (size_t)(nx + 2)) % (size_t)(ny + 2));
+            const int k = (int)(o / ((size_t)(nx + 2) * (size_t)(ny + 2)));
+            int solid = dot_normal_solid(surf, V3{xc[i], yc[j], zc[k]}, around);
+            if (solid < 0) failed = true;
+            else iblank[o] = (int8_t)solid;
+        }
+    };
+    std::vector<std::thread> pool;
+    for (size_t t = 1; t < nthreads; ++t) pool.emplace_back(work, t);
+    work(0);
+    for (auto &th : pool) th.join();
+    if (failed) return -1;
+    // the k fill: seed from the first band cell of the line, carry upward
+    for (int j = 1; j <= ny - 1; ++j)
+        for (int i = 1; i <= nx - 1; ++i) {
+            int8_t carry = 0;
+            for (int k = 1; k <= nz; ++k)
+                if (band[fidx(nx, ny, i, j, k)]) { carry = iblank[fidx(nx, ny, i, j, k)]; break; }
+            for (int k = 1; k <= nz - 1; ++k) {
+                const size_t o = fidx(nx, ny, i, j, k);
+                if (band[o]) carry = iblank[o];
+                else iblank[o] = carry;
             }
         }
+    long nsolid = 0;
     // The clean-up passes set_internal_boundary runs on a solid body
     // (IBM/BOUNDARY_SET.F90:267-410), in its order.  find_isolatedIblank (:440-499):
     // a solid cell with no other solid cell in its 3x3x3 block (clipped to the
