@@ -254,8 +254,9 @@ int dot_normal_solid(const Surface &s, V3 p, std::vector<int> &around)
 // element whose outward normal makes the smallest angle with (p - marker)
 // (last of equals) is taken and the intercept is the nearer foot on its two
 // edges that leave the marker, clamped to the marker.  Of the three
-// candidates the nearest (first of equals) wins.
-void body_intercept(const Surface &s, V3 p, V3 &bi, int &elem)
+// candidates the nearest (first of equals) wins.  False when the surface has
+// fewer than three markers or one of the three belongs to no element.
+bool body_intercept(const Surface &s, V3 p, V3 &bi, int &elem)
 {
     int best[3] = {-1, -1, -1};
     double bd[3] = {1e300, 1e300, 1e300};
@@ -274,6 +275,7 @@ void body_intercept(const Surface &s, V3 p, V3 &bi, int &elem)
     int cel[3];
     for (int c = 0; c < 3; ++c) {
         const int mk = best[c];
+        if (mk < 0) return false;   // fewer than three markers
         const V3 cv = s.p(mk);
         int ce = -1;
         bool found = false;
@@ -285,6 +287,7 @@ void body_intercept(const Surface &s, V3 p, V3 &bi, int &elem)
             double ang = vec_angle(p - cv, -1.0 * s.nrm[e]);
             if (ang <= angMin) { angMin = ang; ce = e; b = t; }
         }
+        if (ce < 0) return false;
         if (!found) {
             int a = s.node(ce, 0), bb = s.node(ce, 1), cc = s.node(ce, 2), na, nb;
             if (a == mk) { na = bb; nb = cc; }
@@ -317,6 +320,7 @@ void body_intercept(const Surface &s, V3 p, V3 &bi, int &elem)
     }
     bi = cand[w];
     elem = cel[w];
+    return true;
 }
 
 // In-place inverse of an 8x8 column-major matrix by LU with partial pivoting.
@@ -375,9 +379,9 @@ extern "C" {
 // Icosahedron subdivided nsub times and projected onto a sphere; outward-oriented
 // triangles.  nsub = 4 gives 2562 vertices and 5120 triangles.  Returns 0, or -1
 // if the capacities are too small (the required counts are still written).
-int fsi_geom_icosphere(int nsub, double radius, double cx, double cy, double cz,
-                       double *verts, int cap_verts, int32_t *tris, int cap_tris,
-                       int *nv_out, int *nt_out)
+static int icosphere_impl(int nsub, double radius, double cx, double cy, double cz,
+                          double *verts, int cap_verts, int32_t *tris, int cap_tris,
+                          int *nv_out, int *nt_out)
 {
     const double t = (1.0 + std::sqrt(5.0)) / 2.0;
     std::vector<V3> v = {{-1, t, 0}, {1, t, 0}, {-1, -t, 0}, {1, -t, 0}, {0, -1, t}, {0, 1, t},
@@ -436,8 +440,8 @@ int fsi_geom_icosphere(int nsub, double radius, double cx, double cy, double cz,
 // none precedes; a line without band cells is fluid) -- the reference's i and j
 // fills are overwritten by its k fill.  Returns the number of solid cells, or -1
 // when the dot-normal test finds no reference marker for a band cell.
-long fsi_geom_iblank(int nx, int ny, int nz, const double *x, const double *y, const double *z,
-                     int nv, const double *verts, int nt, const int32_t *tris, int8_t *iblank)
+static long iblank_impl(int nx, int ny, int nz, const double *x, const double *y, const double *z,
+                        int nv, const double *verts, int nt, const int32_t *tris, int8_t *iblank)
 {
     std::vector<double> xc(nx + 2), yc(ny + 2), zc(nz + 2);
     for (int i = 0; i <= nx; ++i) xc[i] = 0.5 * (x[i] + x[i + 1]);
@@ -482,22 +486,27 @@ long fsi_geom_iblank(int nx, int ny, int nz, const double *x, const double *y, c
                 if (band[fidx(nx, ny, i, j, k)]) cells.push_back(fidx(nx, ny, i, j, k));
     const unsigned hw = std::max(1u, std::thread::hardware_concurrency());
     const size_t nthreads = std::min<size_t>(std::min(hw, 64u), std::max<size_t>(1, cells.size() / 2048));
+    const size_t chunk = 256;
+    std::atomic<size_t> next(0);
     std::atomic<bool> failed(false);
-    auto work = [&](size_t t0) {
+    auto work = [&]() {   // chunks taken from a shared counter: any number of workers covers every cell
         std::vector<int> around;
         around.reserve(64);
-        for (size_t q = t0; q < cells.size() && !failed.load(std::memory_order_relaxed); q += nthreads) {
-            const size_t o = cells[q];
-            const int i = (int)(o % (size_t)(nx + 2)), j = (int)((o / (size_t)(nx + 2)) % (size_t)(ny + 2));
-            const int k = (int)(o / ((size_t)(nx + 2) * (size_t)(ny + 2)));
-            int solid = dot_normal_solid(surf, V3{xc[i], yc[j], zc[k]}, around);
-            if (solid < 0) failed = true;
-            else iblank[o] = (int8_t)solid;
-        }
+        for (size_t q0 = next.fetch_add(chunk); q0 < cells.size() && !failed.load(); q0 = next.fetch_add(chunk))
+            for (size_t q = q0; q < std::min(q0 + chunk, cells.size()); ++q) {
+                const size_t o = cells[q];
+                const int i = (int)(o % (size_t)(nx + 2)), j = (int)((o / (size_t)(nx + 2)) % (size_t)(ny + 2));
+                const int k = (int)(o / ((size_t)(nx + 2) * (size_t)(ny + 2)));
+                int solid = dot_normal_solid(surf, V3{xc[i], yc[j], zc[k]}, around);
+                if (solid < 0) failed = true;
+                else iblank[o] = (int8_t)solid;
+            }
     };
     std::vector<std::thread> pool;
-    for (size_t t = 1; t < nthreads; ++t) pool.emplace_back(work, t);
-    work(0);
+    for (size_t t = 1; t < nthreads; ++t) {
+        try { pool.emplace_back(work); } catch (...) { break; }   // fewer workers if a thread cannot start
+    }
+    work();
     for (auto &th : pool) th.join();
     if (failed) return -1;
     // the k fill: seed from the first band cell of the line, carry upward
@@ -587,12 +596,12 @@ int fsi_geom_ghost_list(int nx, int ny, int nz, const int8_t *iblank, int8_t *gh
 // ghost (IBM/GCM_SET_BOUNDARY.F90:124-304, :307-494).  coeff is (8, nGhost)
 // column-major like coeffGCMN; bi (3, nGhost) and ip (3, nGhost) are optional.
 // Returns 0, or -(n+1) for the first ghost whose stencil search failed.
-int fsi_geom_gcm_coeffs(int nx, int ny, int nz, const double *x, const double *y, const double *z,
-                        int nv, const double *verts, int nt, const int32_t *tris,
-                        double probeLengthNormalized, int nGhost,
-                        const int32_t *iG, const int32_t *jG, const int32_t *kG,
-                        int32_t *iCI, int32_t *jCI, int32_t *kCI, double *coeff,
-                        double *probeLength, double *bi, double *ip, double *coeffD)
+static int gcm_coeffs_impl(int nx, int ny, int nz, const double *x, const double *y, const double *z,
+                           int nv, const double *verts, int nt, const int32_t *tris,
+                           double probeLengthNormalized, int nGhost,
+                           const int32_t *iG, const int32_t *jG, const int32_t *kG,
+                           int32_t *iCI, int32_t *jCI, int32_t *kCI, double *coeff,
+                           double *probeLength, double *bi, double *ip, double *coeffD)
 {
     static const int incI[8] = {0, 0, 1, 1, 0, 0, 1, 1};
     static const int incJ[8] = {0, 1, 1, 0, 0, 1, 1, 0};
@@ -608,7 +617,7 @@ int fsi_geom_gcm_coeffs(int nx, int ny, int nz, const double *x, const double *y
         V3 gc{xc[g_i], yc[g_j], zc[g_k]};
         V3 bip;
         int celem;
-        body_intercept(surf, gc, bip, celem);
+        if (!body_intercept(surf, gc, bip, celem)) return -(n + 1);
         double ds = std::sqrt(dot(bip - gc, bip - gc));
         V3 slope{(bip.x - gc.x) / ds, (bip.y - gc.y) / ds, (bip.z - gc.z) / ds};
         double pl = ds * probeLengthNormalized;
@@ -697,6 +706,37 @@ int fsi_geom_gcm_coeffs(int nx, int ny, int nz, const double *x, const double *y
         }
     }
     return 0;
+}
+
+// The exported entry points: no C++ exception crosses the C boundary (an
+// allocation failure returns -2; the first two keep their documented codes
+// otherwise).
+int fsi_geom_icosphere(int nsub, double radius, double cx, double cy, double cz,
+                       double *verts, int cap_verts, int32_t *tris, int cap_tris,
+                       int *nv_out, int *nt_out)
+{
+    try { return icosphere_impl(nsub, radius, cx, cy, cz, verts, cap_verts, tris, cap_tris, nv_out, nt_out); }
+    catch (...) { return -2; }
+}
+
+long fsi_geom_iblank(int nx, int ny, int nz, const double *x, const double *y, const double *z,
+                     int nv, const double *verts, int nt, const int32_t *tris, int8_t *iblank)
+{
+    try { return iblank_impl(nx, ny, nz, x, y, z, nv, verts, nt, tris, iblank); }
+    catch (...) { return -2; }
+}
+
+int fsi_geom_gcm_coeffs(int nx, int ny, int nz, const double *x, const double *y, const double *z,
+                        int nv, const double *verts, int nt, const int32_t *tris,
+                        double probeLengthNormalized, int nGhost,
+                        const int32_t *iG, const int32_t *jG, const int32_t *kG,
+                        int32_t *iCI, int32_t *jCI, int32_t *kCI, double *coeff,
+                        double *probeLength, double *bi, double *ip, double *coeffD)
+{
+    try {
+        return gcm_coeffs_impl(nx, ny, nz, x, y, z, nv, verts, nt, tris, probeLengthNormalized, nGhost, iG, jG, kG,
+                               iCI, jCI, kCI, coeff, probeLength, bi, ip, coeffD);
+    } catch (...) { return -(nGhost + 2); }
 }
 
 } // extern "C"

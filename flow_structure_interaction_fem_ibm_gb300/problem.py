@@ -105,7 +105,7 @@ def icosphere(nsub: int = 4, radius: float = 0.15, centre=(0.5, 0.5, 0.5)):
                               _native.ptr(verts, ctypes.c_double), nv_cap,
                               _native.ptr(tris, ctypes.c_int32), nt_cap, ctypes.byref(nv), ctypes.byref(nt))
     if rc != 0:
-        raise RuntimeError("icosphere capacity")
+        raise RuntimeError("icosphere capacity" if rc == -1 else "icosphere: out of host memory")
     return verts[: 3 * nv.value].copy(), tris[: 3 * nt.value].copy()
 
 
@@ -116,9 +116,12 @@ def body_geometry(p: SolverParams, x, y, z, verts, tris, probe_length_normalized
     sh = full_shape(p)
     nv, nt = verts.size // 3, tris.size // 3
     iblank = np.zeros(sh, np.int8, order="F")
-    g.fsi_geom_iblank(p.nx, p.ny, p.nz, _native.ptr(x, ctypes.c_double), _native.ptr(y, ctypes.c_double),
-                      _native.ptr(z, ctypes.c_double), nv, _native.ptr(verts, ctypes.c_double), nt,
-                      _native.ptr(tris, ctypes.c_int32), iblank.ctypes.data_as(_native.c_i8_p))
+    ns = g.fsi_geom_iblank(p.nx, p.ny, p.nz, _native.ptr(x, ctypes.c_double), _native.ptr(y, ctypes.c_double),
+                           _native.ptr(z, ctypes.c_double), nv, _native.ptr(verts, ctypes.c_double), nt,
+                           _native.ptr(tris, ctypes.c_int32), iblank.ctypes.data_as(_native.c_i8_p))
+    if ns < 0:
+        raise RuntimeError("iblank: no reference marker for a band cell (the reference stops there)"
+                           if ns == -1 else "iblank: out of host memory")
     ghost = np.zeros(sh, np.int8, order="F")
     cap = int(iblank.sum()) + 1
     iG = np.zeros(cap, np.int32); jG = np.zeros(cap, np.int32); kG = np.zeros(cap, np.int32)
@@ -144,6 +147,8 @@ def body_geometry(p: SolverParams, x, y, z, verts, tris, probe_length_normalized
                                coeff.ctypes.data_as(_native.c_double_p), _native.ptr(probe, ctypes.c_double),
                                xBI.ctypes.data_as(_native.c_double_p), xIP.ctypes.data_as(_native.c_double_p),
                                coeffD.ctypes.data_as(_native.c_double_p))
+    if rc == -(n + 2):
+        raise RuntimeError("image-point coefficients: out of host memory")
     if rc != 0:
         raise RuntimeError(f"image-point stencil search failed for ghost {-rc - 1}")
     return Geometry(iblank=iblank, ghost=ghost, flags=outer_flags(p), nGhost=n, iG=iG, jG=jG, kG=kG,
