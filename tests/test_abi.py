@@ -136,3 +136,37 @@ def test_c_driver_solves_like_the_python_binding(gpu_built, tmp_path, case):
     fl = 1.0 - pr.geom.iblank[I]
     vol = cell_volumes(pr) * fl
     assert abs(mean - float((ref["p"][I] * vol).sum() / vol.sum())) <= 1e-12 * max(1.0, np.abs(ref["p"]).max())
+
+
+# ------------------------------------------------- parameter validation --
+import pytest
+
+from flow_structure_interaction_fem_ibm_gb300.grid import make_grid
+from flow_structure_interaction_fem_ibm_gb300.params import SolverParams
+from flow_structure_interaction_fem_ibm_gb300.poisson import FsiMgError, PoissonSolver
+
+BAD_PARAMS = [
+    ("periodic", dict(bc=(5, 5, 1, 1, 1, 1)), "periodic"),
+    ("pbc", dict(pbc=(2, 2, 2, 2, 2, 3)), "pbc"),
+    ("omega_high", dict(omega=2.0), "omega"),
+    ("omega_zero", dict(omega=0.0), "omega"),
+    ("krylov", dict(outer_krylov=61), "outer_krylov"),
+    ("lsor", dict(pp_solver_type=1), "pp_solver_type"),
+    ("cycle", dict(mgcycle=(1, 4, 1)), "mgcycle"),
+    ("precision", dict(precision_mode=2), "precision_mode"),
+    ("ndim", dict(ndim=4), "ndim"),
+    ("2d_nz", dict(ndim=2, nz=3), "nz = 2"),
+    ("tiny", dict(nx=2), "too small"),
+]
+
+
+@pytest.mark.parametrize("change,match", [(c, m) for _, c, m in BAD_PARAMS], ids=[b[0] for b in BAD_PARAMS])
+def test_create_rejects_bad_parameters_before_any_device_call(change, match):
+    """fsi_mg_create validates every parameter on the host and returns -1
+    with the reason before it looks for a device (no GPU needed)."""
+    p = SolverParams(ndim=3, nx=9, ny=9, nz=9)
+    for k, v in change.items():
+        setattr(p, k, v)
+    x, y, z = make_grid(max(p.nx, 3), max(p.ny, 3), max(p.nz, 2))
+    with pytest.raises(FsiMgError, match=match):
+        PoissonSolver(p, x, y, z)
