@@ -846,6 +846,19 @@ def config2_gpu(pr, solver_cls, krylov, reps=3):
     return out, fields
 
 
+def _section(fn, *a, **kw):
+    """One auxiliary section of the benchmark line (projection steps, adjoint
+    check, rollout): a failure is reported in the line as {"error": ...},
+    with its traceback on stderr, instead of losing the measurements taken
+    before it."""
+    try:
+        return fn(*a, **kw)
+    except Exception as e:
+        import traceback
+        traceback.print_exc(file=sys.stderr)
+        return {"error": f"{type(e).__name__}: {e}"}
+
+
 def main():
     args = parse()
     rank, world, local = dist_env()
@@ -1121,13 +1134,14 @@ def main():
     peak = peaks.get("hbm_gbs", 6800.0)
     steps_ops = None
     if not args.no_steps:
-        steps_ops = projection_steps(s_mixed, pr, peak)
-        steps_ops["device_step"] = device_time_step(args.n, args.seed, args.tol, args.krylov)
+        steps_ops = _section(projection_steps, s_mixed, pr, peak)
+        if "error" not in steps_ops:
+            steps_ops["device_step"] = _section(device_time_step, args.n, args.seed, args.tol, args.krylov)
 
     # FP64 kernels against both roofs: HBM (measured copy bandwidth) and the FP64 pipe
     # (measured DFMA rate; FP64 thread-instructions per cell from the committed ncu summary)
     fp64_roofline = None
-    if steps_ops is not None:
+    if steps_ops is not None and "error" not in steps_ops:
         roof = steps_ops["fp64_roof"]["tflops"] * 1e12 / 2.0   # FP64-pipe thread-instructions per second
         ipc = profile_fp64_instr()
         cells = float(args.n) ** 3
@@ -1153,7 +1167,7 @@ def main():
         s_mixed.close()
         s_fp64.close()
         s_mixed = s_fp64 = None
-        adjoint = adjoint_check(args.adjoint_n, args.adjoint_dirs)
+        adjoint = _section(adjoint_check, args.adjoint_n, args.adjoint_dirs)
 
     rollout = None
     if rank == 0 and not args.no_rollout:
@@ -1161,8 +1175,8 @@ def main():
         # reaches the tolerance in fewer, cheaper applications (111 ms per step against
         # 142 ms on F-cycles); the headline's relaxation: over 40 steps 17.1 instead of 20.2
         # applications per step and 97.8 instead of 108.8 ms per step at omega 1.5 vs 1
-        rollout = channel_rollout(200, krylov=args.krylov, mgcycle=1, iter_finest=args.iter_finest,
-                                  omega=args.omega)
+        rollout = _section(channel_rollout, 200, krylov=args.krylov, mgcycle=1, iter_finest=args.iter_finest,
+                           omega=args.omega)
 
     # roofline of the dominant kernel: level-1 FP32 line relaxation (k_line_wp<float,dir,8>),
     # durations from CUDA events around each launch inside the timed solves
