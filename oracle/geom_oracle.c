@@ -294,7 +294,10 @@ static int search_vertex_dotnorm(const surf_t *s, const double *p, double *scrat
     if (em == 1) { *dotNorm = -1.0; *elemOut = -1; return 0; }
     nn = 0;
     for (int m = 0; m < s->nt; ++m)
-        if (node(s, m, 0) == ref || node(s, m, 1) == ref || node(s, m, 2) == ref) nbr[nn++] = m;
+        if (node(s, m, 0) == ref || node(s, m, 1) == ref || node(s, m, 2) == ref) {
+            if (nn >= OG_NSIZE) return -1;
+            nbr[nn++] = m;
+        }
     /* the element: among those whose normal projection falls inside, the
      * nearest plane (last of equals); before the first such element, the
      * smallest outside angle (last of equals) */
