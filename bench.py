@@ -310,11 +310,15 @@ def profile_traffic(n):
 
 
 # Discrete compatibility shifts of the config-2 workload (128^3 stretched
-# sphere, seed 2), as this benchmark's GPU plateau solves compute them (the
-# value its own line prints as config2.compat_shift).  The reference arm runs
-# no GPU code, so it takes the shift from here; the shift is a property of the
-# discrete operator and the right-hand side, not of the solver.
-CONFIG2_SHIFT = {1e-8: -0.00035806123334163623}
+# sphere, seed 2), from two FP64 plateau solves of the oracle on the current
+# geometry (problem.compatibility_shift, plateau to 1e-10 relative; the value
+# the GPU arm computes for itself and prints as config2.compat_shift agrees to
+# its mixed-precision plateau).  The reference arm runs no GPU code, so it
+# takes the shift from here; the shift is a property of the discrete operator
+# and the right-hand side, not of the solver.  It must follow the geometry:
+# an error dc leaves a residual floor of about 51 dc in max-norm, against a
+# tolerance of 1.9e-6.
+CONFIG2_SHIFT = {1e-8: -0.0003587849847243156}
 
 
 def config2_problem(tol, shift=None, solver_cls=None):
