@@ -521,7 +521,6 @@ static long iblank_impl(int nx, int ny, int nz, const double *x, const double *y
                 else iblank[o] = carry;
             }
         }
-    long nsolid = 0;
     // The clean-up passes set_internal_boundary runs on a solid body
     // (IBM/BOUNDARY_SET.F90:267-410), in its order.  find_isolatedIblank (:440-499):
     // a solid cell with no other solid cell in its 3x3x3 block (clipped to the
@@ -555,6 +554,7 @@ static long iblank_impl(int nx, int ny, int nz, const double *x, const double *y
                     const int8_t hi = iblank[fidx(nx, ny, i + (axis == 0), j + (axis == 1), k + (axis == 2))];
                     if ((lo == 1 && pos == dims[axis]) || (hi == 1 && pos == 1)) cell = 1;
                 }
+    long nsolid = 0;
     for (size_t o = 0; o < nf; ++o) nsolid += iblank[o];
     return nsolid;
 }
