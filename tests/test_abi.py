@@ -170,3 +170,74 @@ def test_create_rejects_bad_parameters_before_any_device_call(change, match):
     x, y, z = make_grid(max(p.nx, 3), max(p.ny, 3), max(p.nz, 2))
     with pytest.raises(FsiMgError, match=match):
         PoissonSolver(p, x, y, z)
+
+
+# ------------------------------------------- Fortran shim vs the header --
+SHIM = Path(__file__).resolve().parents[1] / "flow_structure_interaction_fem_ibm_gb300" / "fortran" / "fsi_mg_shim.F90"
+
+
+def _c_struct(name):
+    """(field name, kind, element count) in memory order of a struct of the header."""
+    text = re.sub(r"/\*.*?\*/", "", HEADER.read_text(), flags=re.S)
+    end = re.search(r"\}\s*" + name + r"\s*;", text).start()
+    body = text[text.rindex("typedef struct {", 0, end) + len("typedef struct {"):end]
+    out = []
+    for decl in filter(None, (d.strip() for d in body.split(";"))):
+        base = "double" if "double" in decl.split()[0:2] or decl.startswith("const double") else "int"
+        names = re.sub(r"^(const\s+)?(double|int)\s+", "", decl)
+        for item in (n.strip() for n in names.split(",")):
+            kind = "ptr" if item.startswith("*") else base
+            dims = [int(v) for v in re.findall(r"\[(\d+)\]", item)]
+            count = 1
+            for v in dims:
+                count *= v
+            out.append((re.sub(r"[\*\s]|\[.*", "", item).lower(), kind, count))
+    return out
+
+
+def _f_type(name):
+    text = "\n".join(l.split("!")[0] for l in SHIM.read_text().splitlines())
+    body = re.search(r"TYPE, BIND\(C\) :: " + name + r"\n(.*?)END TYPE " + name, text, flags=re.S).group(1)
+    kinds = {"INTEGER(C_INT)": "int", "REAL(C_DOUBLE)": "double", "TYPE(C_PTR)": "ptr"}
+    out = []
+    for line in filter(None, (l.strip() for l in body.splitlines())):
+        decl, names = line.split("::")
+        kind = kinds[decl.strip()]
+        for item in re.findall(r"\w+(?:\([\d,\s]+\))?", names):
+            dims = [int(v) for v in re.findall(r"\d+", item[item.index("("):])] if "(" in item else []
+            count = 1
+            for v in dims:
+                count *= v
+            out.append((item.split("(")[0].lower(), kind, count))
+    return out
+
+
+@pytest.mark.parametrize("name", ["fsi_mg_params", "fsi_mg_rhs_ad_fields", "fsi_mg_bc_values"])
+def test_fortran_shim_types_match_the_header(name):
+    """The shim's BIND(C) types have the C structs' fields, in order, with
+    the same kinds and element counts (no Fortran compiler here or on the GPU
+    host, so this textual check is what keeps the two layouts together)."""
+    assert _f_type(name) == _c_struct(name)
+
+
+def _c_prototypes():
+    text = re.sub(r"/\*.*?\*/", "", HEADER.read_text(), flags=re.S)
+    protos = {}
+    for m in re.finditer(r"\b(fsi_mg_\w+)\s*\(([^)]*)\)\s*;", text):
+        args = m.group(2).strip()
+        protos[m.group(1)] = 0 if args in ("", "void") else len(args.split(","))
+    return protos
+
+
+def test_fortran_shim_interfaces_match_the_header():
+    """Every BIND(C) interface of the shim binds a declared entry point with
+    the same number of arguments."""
+    text = re.sub(r"&\s*\n\s*", "", SHIM.read_text())
+    found = re.findall(r"FUNCTION\s+\w+\s*\(([^)]*)\)\s*BIND\(C,\s*NAME='(fsi_mg_\w+)'\)", text)
+    found += [(a, n) for a, n in re.findall(r"SUBROUTINE\s+\w+\s*\(([^)]*)\)\s*BIND\(C,\s*NAME='(fsi_mg_\w+)'\)", text)]
+    protos = _c_prototypes()
+    assert len(found) >= 10
+    for args, cname in found:
+        assert cname in protos, cname
+        nargs = 0 if not args.strip() else len(args.split(","))
+        assert nargs == protos[cname], (cname, nargs, protos[cname])
