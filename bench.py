@@ -319,6 +319,26 @@ def profile_traffic(n):
 # an error dc leaves a residual floor of about 51 dc in max-norm, against a
 # tolerance of 1.9e-6.
 CONFIG2_SHIFT = {1e-8: -0.0003587849847243156}
+# Digest of the config-2 inputs that shift belongs to (config2_digest); a CPU
+# test compares it with the current geometry so that a geometry change cannot
+# leave a stale shift behind.
+CONFIG2_DIGEST = "de9188c1e263b9d8"
+
+
+def config2_digest():
+    """Digest of the config-2 workload's inputs: iblank, ghost list, stencil
+    cells, image-point weights (to 1e-10) and the mean-free right-hand side
+    (to 1e-8 of its scale)."""
+    import hashlib
+    from flow_structure_interaction_fem_ibm_gb300 import problem as P
+    pr = P.sphere(128, seed=2, stretch=1.5)
+    g = pr.geom
+    scale = float(np.abs(pr.nlu0).max())
+    h = hashlib.sha256()
+    for a in (g.iblank, g.iG, g.jG, g.kG, g.iCI, g.jCI, g.kCI, np.round(g.coeff, 10),
+              np.round(pr.nlu0 / scale, 8)):
+        h.update(np.ascontiguousarray(a).tobytes())
+    return h.hexdigest()[:16]
 
 
 def config2_problem(tol, shift=None, solver_cls=None):
